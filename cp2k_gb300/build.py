@@ -70,6 +70,7 @@ def build_grid(force: bool = False, verbose_ptxas: bool = False) -> str:
     os.makedirs(objdir, exist_ok=True)
     nvcc = _nvcc()
     flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                    "-Xcompiler", "-ffp-contract=off",
                     "-Xcompiler", "-fvisibility=hidden", "-I", INCLUDE, "-I", CSRC,
                     "--expt-relaxed-constexpr"]
     if verbose_ptxas:

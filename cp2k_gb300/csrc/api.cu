@@ -1,0 +1,1189 @@
+// Host side of the GB300 grid backend: the C ABI of include/grid_gb300.h.
+//
+// Task-list creation does, once per geometry and in FP64 on the host, what
+// CP2K's reference computes per task inside its loops (the Gaussian product
+// centre and prefactor, the cube centre, the discretised radius and its
+// sphere bounds, the general-path index box: src/grid/ref/grid_ref_collint.h:
+// 207-245, 583-640, 917-947), sorts the tasks into per-subblock runs and into
+// cost-ordered work queues, and uploads everything into device-resident
+// arrays.  Collocate / integrate calls then only move pab/hab/grids and
+// launch kernels.  Host code is compiled with -ffp-contract=off so the
+// discrete decisions (floor/ceil of FP64 expressions) match the reference's
+// ISO-C build bit for bit on x86-64 and aarch64.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "gb300_internal.h"
+#include "grid_gb300.h"
+
+#define GB300_API extern "C" __attribute__((visibility("default")))
+
+namespace gb300 {
+
+static std::atomic<long long> g_launches{0};
+void count_launch(int n) { g_launches += n; }
+
+static std::mutex g_err_mu;
+static char g_last_error[512] = "";
+
+[[noreturn]] static void fail(const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    snprintf(g_last_error, sizeof(g_last_error), "%s", buf);
+  }
+  fprintf(stderr, "grid_gb300 error: %s\n", buf);
+  abort();
+}
+
+#define CK(x)                                                                  \
+  do {                                                                         \
+    cudaError_t e_ = (x);                                                      \
+    if (e_ != cudaSuccess)                                                     \
+      fail("%s failed: %s (%s:%d)", #x, cudaGetErrorString(e_), __FILE__,     \
+           __LINE__);                                                          \
+  } while (0)
+
+int persistent_blocks(const void *kernel, int threads, size_t smem) {
+  static std::mutex mu;
+  static std::map<std::pair<const void *, size_t>, int> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  auto key = std::make_pair(kernel, smem);
+  auto it = cache.find(key);
+  if (it != cache.end())
+    return it->second;
+  int dev = 0, nsm = 0, per_sm = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
+  if (per_sm < 1)
+    fail("kernel does not fit on an SM (%zu B shared memory)", smem);
+  const int nb = nsm * per_sm;
+  cache[key] = nb;
+  return nb;
+}
+
+} // namespace gb300
+
+using namespace gb300;
+
+// ===========================================================================
+// offload buffers (src/offload/offload_buffer.c)
+// ===========================================================================
+GB300_API void offload_create_buffer(const int length, offload_buffer **buffer) {
+  const size_t bytes = (size_t)(length > 0 ? length : 1) * sizeof(double);
+  offload_buffer *b = *buffer;
+  if (b != nullptr) {
+    if (b->size >= (size_t)length * sizeof(double)) {
+      b->size = (size_t)length * sizeof(double);
+      return; // reuse, as the reference does
+    }
+    offload_free_buffer(b);
+  }
+  b = (offload_buffer *)malloc(sizeof(offload_buffer));
+  if (!b)
+    fail("out of host memory");
+  b->size = (size_t)length * sizeof(double);
+  CK(cudaMallocHost((void **)&b->host_buffer, bytes));
+  CK(cudaMalloc((void **)&b->device_buffer, bytes));
+  *buffer = b;
+}
+
+GB300_API void offload_free_buffer(offload_buffer *buffer) {
+  if (!buffer)
+    return;
+  CK(cudaFreeHost(buffer->host_buffer));
+  CK(cudaFree(buffer->device_buffer));
+  free(buffer);
+}
+
+GB300_API double *offload_get_buffer_host_pointer(offload_buffer *buffer) {
+  return buffer ? buffer->host_buffer : nullptr;
+}
+
+// ===========================================================================
+// basis sets (src/grid/common/grid_basis_set.c:19-86)
+// ===========================================================================
+GB300_API void grid_create_basis_set(const int nset, const int nsgf, const int maxco,
+                                     const int maxpgf, const int *lmin, const int *lmax,
+                                     const int *npgf, const int *nsgf_set,
+                                     const int *first_sgf, const double *sphi,
+                                     const double *zet, grid_basis_set **basis_set) {
+  grid_basis_set *b = (grid_basis_set *)malloc(sizeof(grid_basis_set));
+  if (!b)
+    fail("out of host memory");
+  b->nset = nset;
+  b->nsgf = nsgf;
+  b->maxco = maxco;
+  b->maxpgf = maxpgf;
+  auto dup_i = [&](const int *src) {
+    int *p = (int *)malloc(sizeof(int) * (nset > 0 ? nset : 1));
+    if (nset > 0)
+      memcpy(p, src, sizeof(int) * nset);
+    return p;
+  };
+  b->lmin = dup_i(lmin);
+  b->lmax = dup_i(lmax);
+  b->npgf = dup_i(npgf);
+  b->nsgf_set = dup_i(nsgf_set);
+  b->first_sgf = dup_i(first_sgf);
+  const size_t ns = (size_t)nsgf * maxco, nz = (size_t)nset * maxpgf;
+  b->sphi = (double *)malloc(sizeof(double) * (ns ? ns : 1));
+  b->zet = (double *)malloc(sizeof(double) * (nz ? nz : 1));
+  if (ns)
+    memcpy(b->sphi, sphi, sizeof(double) * ns);
+  if (nz)
+    memcpy(b->zet, zet, sizeof(double) * nz);
+  for (int i = 0; i < nset; i++)
+    if (b->lmax[i] > GB300_LMAX || b->lmin[i] < 0 || b->lmin[i] > b->lmax[i])
+      fail("basis set: unsupported angular momentum range [%d, %d]", b->lmin[i], b->lmax[i]);
+  *basis_set = b;
+}
+
+GB300_API void grid_free_basis_set(grid_basis_set *b) {
+  if (!b)
+    return;
+  free(b->lmin);
+  free(b->lmax);
+  free(b->npgf);
+  free(b->nsgf_set);
+  free(b->first_sgf);
+  free(b->sphi);
+  free(b->zet);
+  free(b);
+}
+
+// ===========================================================================
+// library config (src/grid/common/grid_library.c)
+// ===========================================================================
+static grid_library_config g_config = {GRID_BACKEND_AUTO, false, false};
+static long long g_counters[2][4][GB300_LP_MAX + 1];
+static bool g_initialized = false;
+
+GB300_API void grid_library_init(void) {
+  if (g_initialized)
+    return;
+  memset(g_counters, 0, sizeof(g_counters));
+  g_initialized = true;
+}
+
+GB300_API void grid_library_finalize(void) { g_initialized = false; }
+
+GB300_API void grid_library_set_config(const enum grid_backend backend, const bool validate,
+                                       const bool apply_cutoff) {
+  g_config.backend = backend;
+  g_config.validate = validate;
+  g_config.apply_cutoff = apply_cutoff;
+}
+
+GB300_API grid_library_config grid_library_get_config(void) { return g_config; }
+
+GB300_API void grid_library_counter_add(const int lp, const enum grid_backend backend,
+                                        const enum grid_library_kernel kernel,
+                                        const int increment) {
+  (void)backend;
+  if (lp < 0 || lp > GB300_LP_MAX || kernel < 0 || kernel > 3)
+    return;
+  __atomic_fetch_add(&g_counters[0][kernel][lp], (long long)increment, __ATOMIC_RELAXED);
+}
+
+GB300_API void grid_library_print_stats(const int fortran_comm,
+                                        void (*print_func)(const char *, int, int),
+                                        const int output_unit) {
+  (void)fortran_comm;
+  static const char *names[4] = {"collocate ortho", "integrate ortho", "collocate general",
+                                 "integrate general"};
+  char line[160];
+  snprintf(line, sizeof(line), "\n %-26s %6s %16s\n", "GB300 GRID KERNEL", "LP", "COUNT");
+  print_func(line, (int)strlen(line), output_unit);
+  for (int k = 0; k < 4; k++)
+    for (int lp = 0; lp <= GB300_LP_MAX; lp++)
+      if (g_counters[0][k][lp]) {
+        snprintf(line, sizeof(line), " %-26s %6d %16lld\n", names[k], lp, g_counters[0][k][lp]);
+        print_func(line, (int)strlen(line), output_unit);
+      }
+}
+
+GB300_API long long grid_gb300_kernel_launches(void) { return g_launches.load(); }
+
+GB300_API const char *grid_gb300_last_error(void) { return g_last_error; }
+
+// ===========================================================================
+// task lists
+// ===========================================================================
+namespace gb300 {
+
+struct Queue {
+  int *d_idx = nullptr;
+  int n = 0;
+  int extent = 0; // ortho: max cube width; general: max j-range
+};
+
+struct Mode { // everything that depends on the l shifts of a call
+  LDiffs d;
+  std::vector<int> coef_off; // per task (block order)
+  int *d_coef_off = nullptr;
+  size_t coef_total = 0;
+  Queue q[2][kNumBuckets]; // [general][bucket]
+  int coef_words = 0;      // per-warp shared memory words of coefficient/post
+  int sched_version = -1;
+};
+
+struct TaskList {
+  bool empty = false;
+  bool ortho = true;
+  int ntasks = 0, nlevels = 0, natoms = 0, nkinds = 0, nblocks = 0;
+  long long buffer_len = 0;
+  int precision = GRID_GB300_FP64;
+  int schedule = GRID_GB300_SCHEDULE_SIZE;
+  int sched_version = 0;
+  LevelSet levels{};
+  std::vector<TaskDesc> tasks; // block order
+  std::vector<SubblockDesc> subs;
+  std::vector<SphereHdr> sph;
+  std::vector<int16_t> sph_tab;
+  std::vector<long long> points; // per task (block order)
+  std::vector<float> model_cost; // per task, empty unless a model was applied
+  std::vector<int> npts_local;   // [nlevels][3]
+  size_t cart_total = 0;
+  int contract_words = 1;
+  // device
+  TaskDesc *d_tasks = nullptr;
+  SubblockDesc *d_subs = nullptr;
+  SphereHdr *d_sph = nullptr;
+  int16_t *d_sph_tab = nullptr;
+  double *d_atom_pos = nullptr;
+  double *d_sphi = nullptr;
+  LevelSet *d_levels = nullptr;
+  double *d_pab_cart = nullptr, *d_hab_cart = nullptr;
+  void *d_coef = nullptr; // collocate coefficients
+  size_t coef_cap = 0;
+  double *d_coef_int = nullptr; // integrated coefficients
+  size_t coef_int_cap = 0;
+  float *d_grid32[GB300_MAX_LEVELS] = {};
+  double *d_forces = nullptr, *d_virial = nullptr;
+  int *d_counters = nullptr; // one per queue launch
+  int *d_error = nullptr;
+  long long *d_cycles = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[5] = {};
+  double timings[4] = {0, 0, 0, 0};
+  std::map<int, Mode> modes;
+};
+
+static int mode_key(const LDiffs &d) {
+  return ((d.la_max + 4) << 12) | ((d.la_min + 4) << 8) | ((d.lb_max + 4) << 4) | (d.lb_min + 4);
+}
+
+// grid_prepare_pab.h:447-517
+static LDiffs func_ldiffs(int f) {
+  LDiffs d{0, 0, 0, 0};
+  if (f == GRID_FUNC_AB)
+    return d;
+  if (f >= 411 && f <= 433 && f % 10 >= 1 && f % 10 <= 3)
+    return LDiffs{1, -1, 2, -1};
+  if ((f >= 701 && f <= 703) || (f >= 801 && f <= 803))
+    return LDiffs{2, -2, 2, -2};
+  if (f == 200 || (f >= 301 && f <= 303) || (f >= 501 && f <= 503) || (f >= 601 && f <= 603) ||
+      (f >= 901 && f <= 906) || (f >= 1001 && f <= 1003))
+    return LDiffs{1, -1, 1, -1};
+  fail("unknown grid_func %d", f);
+}
+
+// grid_process_vab.h:222-251
+static LDiffs integrate_ldiffs(bool forces, bool virial, bool tau) {
+  LDiffs d{0, 0, 0, 0};
+  if (forces || virial) {
+    d.la_max += 1;
+    d.la_min -= 1;
+    d.lb_min -= 1;
+  }
+  if (virial) {
+    d.la_max += 1;
+    d.lb_max += 1;
+  }
+  if (tau) {
+    d.la_max += 1;
+    d.lb_max += 1;
+    d.la_min -= 1;
+    d.lb_min -= 1;
+  }
+  return d;
+}
+
+// Sphere bounds of one (level, discretised radius), with the reference's
+// expressions (grid_ref_collint.h:237-245, 139-151, 44-52).
+static void build_sphere(const LevelDesc &L, double disr, SphereHdr &h,
+                         std::vector<int16_t> &tab, long long &npoints) {
+  for (int i = 0; i < 3; i++)
+    h.lb[i] = (int)ceil(-1e-8 - disr * L.dh_inv[i * 4]);
+  h.cmax = std::max(std::max(1 - h.lb[0], 1 - h.lb[1]), 1 - h.lb[2]);
+  h.off = (int)tab.size();
+  const int K = 1 - h.lb[2];
+  std::vector<int> js(K), rows;
+  std::vector<int16_t> is;
+  npoints = 0;
+  for (int kk = 0; kk < K; kk++) {
+    const int k1 = -kk;
+    const int kd = (2 * k1 - 1) / 2;
+    const double kr = kd * L.dh[8];
+    const double kremain = disr * disr - kr * kr;
+    const int jstart = (int)ceil(-1e-8 - sqrt(fmax(0.0, kremain)) * L.dh_inv[4]);
+    js[kk] = jstart;
+    rows.push_back((int)is.size());
+    for (int jj = 0; jj <= -jstart; jj++) {
+      const int j1 = -jj;
+      const int jd = (2 * j1 - 1) / 2;
+      const double jr = jd * L.dh[4];
+      const double jremain = kremain - jr * jr;
+      const int istart = (int)ceil(-1e-8 - sqrt(fmax(0.0, jremain)) * L.dh_inv[0]);
+      is.push_back((int16_t)istart);
+      npoints += 4LL * (2 - 2 * istart); // rows j1, j2 of planes k1, k2
+    }
+  }
+  for (int kk = 0; kk < K; kk++)
+    tab.push_back((int16_t)js[kk]);
+  for (int kk = 0; kk < K; kk++)
+    tab.push_back((int16_t)rows[kk]);
+  if (is.size() > 32767)
+    fail("sphere table row offsets exceed int16");
+  tab.insert(tab.end(), is.begin(), is.end());
+}
+
+template <typename T> static T *dalloc_copy(const std::vector<T> &v) {
+  T *p = nullptr;
+  const size_t n = v.empty() ? 1 : v.size();
+  CK(cudaMalloc((void **)&p, sizeof(T) * n));
+  if (!v.empty())
+    CK(cudaMemcpy(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  return p;
+}
+
+static void free_device(TaskList *t) {
+  void *ptrs[] = {t->d_tasks, t->d_subs, t->d_sph, t->d_sph_tab, t->d_atom_pos, t->d_sphi,
+                  t->d_levels, t->d_pab_cart, t->d_hab_cart, t->d_coef, t->d_coef_int,
+                  t->d_forces, t->d_virial, t->d_counters, t->d_error, t->d_cycles};
+  for (void *p : ptrs)
+    if (p)
+      cudaFree(p);
+  for (int l = 0; l < GB300_MAX_LEVELS; l++)
+    if (t->d_grid32[l])
+      cudaFree(t->d_grid32[l]);
+  for (auto &kv : t->modes) {
+    if (kv.second.d_coef_off)
+      cudaFree(kv.second.d_coef_off);
+    for (auto &qq : kv.second.q)
+      for (auto &q : qq)
+        if (q.d_idx)
+          cudaFree(q.d_idx);
+  }
+  for (auto &e : t->ev)
+    if (e)
+      cudaEventDestroy(e);
+  if (t->stream)
+    cudaStreamDestroy(t->stream);
+}
+
+static bool sphi_is_identity(const grid_basis_set *b, int iset) {
+  const int nco = b->npgf[iset] * ncoset(b->lmax[iset]);
+  if (b->nsgf_set[iset] != nco)
+    return false;
+  const int s0 = b->first_sgf[iset] - 1;
+  for (int r = 0; r < nco; r++)
+    for (int c = 0; c < nco; c++)
+      if (b->sphi[(size_t)(s0 + r) * b->maxco + c] != (r == c ? 1.0 : 0.0))
+        return false;
+  return true;
+}
+
+static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nkinds,
+                        int nblocks, const int *block_offsets, const double *atom_positions,
+                        const int *atom_kinds, const grid_basis_set **basis_sets,
+                        const int *level_list, const int *iatom_list, const int *jatom_list,
+                        const int *iset_list, const int *jset_list, const int *ipgf_list,
+                        const int *jpgf_list, const int *border_mask_list,
+                        const int *block_num_list, const double *radius_list,
+                        const double *rab_list, const int *npts_global, const int *npts_local,
+                        const int *shift_local, const int *border_width, const double *dh,
+                        const double *dh_inv) {
+  TaskList *t = new TaskList();
+  t->ortho = ortho;
+  t->ntasks = ntasks;
+  t->nlevels = nlevels;
+  t->natoms = natoms;
+  t->nkinds = nkinds;
+  t->nblocks = nblocks;
+  if (nlevels > GB300_MAX_LEVELS)
+    fail("at most %d grid levels are supported (got %d)", GB300_MAX_LEVELS, nlevels);
+  t->npts_local.assign(npts_local, npts_local + 3 * std::max(nlevels, 0));
+  if (ntasks == 0 || nblocks == 0 || nlevels == 0) {
+    t->empty = true;
+    return t;
+  }
+  // ---- levels
+  t->levels.nlevels = nlevels;
+  for (int l = 0; l < nlevels; l++) {
+    LevelDesc &L = t->levels.lv[l];
+    for (int i = 0; i < 3; i++) {
+      L.npts_global[i] = npts_global[3 * l + i];
+      L.npts_local[i] = npts_local[3 * l + i];
+      L.shift[i] = shift_local[3 * l + i];
+      L.border_width[i] = border_width[3 * l + i];
+      if (L.npts_global[i] < 1 || L.npts_local[i] < 1)
+        fail("level %d: empty grid", l);
+    }
+    L.dh_max = 0.0;
+    for (int i = 0; i < 9; i++) {
+      L.dh[i] = dh[9 * l + i];
+      L.dh_inv[i] = dh_inv[9 * l + i];
+      L.dh_max = fmax(L.dh_max, fabs(L.dh[i]));
+    }
+  }
+  // ---- basis data on device: concatenated sphi per kind
+  std::vector<long long> sphi_off(nkinds);
+  std::vector<double> sphi_all;
+  for (int k = 0; k < nkinds; k++) {
+    const grid_basis_set *b = basis_sets[k];
+    sphi_off[k] = (long long)sphi_all.size();
+    sphi_all.insert(sphi_all.end(), b->sphi, b->sphi + (size_t)b->nsgf * b->maxco);
+  }
+  // ---- block order
+  std::vector<int> order(ntasks);
+  std::iota(order.begin(), order.end(), 0);
+  for (int i = 0; i < ntasks; i++) {
+    const int lev = level_list[i], ia = iatom_list[i], ja = jatom_list[i], bn = block_num_list[i];
+    if (lev < 1 || lev > nlevels || ia < 1 || ia > natoms || ja < 1 || ja > natoms || bn < 1 ||
+        bn > nblocks)
+      fail("task %d: index out of range (level %d, atoms %d/%d, block %d)", i, lev, ia, ja, bn);
+    const grid_basis_set *bi = basis_sets[atom_kinds[ia - 1] - 1];
+    const grid_basis_set *bj = basis_sets[atom_kinds[ja - 1] - 1];
+    if (iset_list[i] < 1 || iset_list[i] > bi->nset || jset_list[i] < 1 || jset_list[i] > bj->nset ||
+        ipgf_list[i] < 1 || ipgf_list[i] > bi->npgf[iset_list[i] - 1] || jpgf_list[i] < 1 ||
+        jpgf_list[i] > bj->npgf[jset_list[i] - 1])
+      fail("task %d: set/pgf index out of range", i);
+    if (!(radius_list[i] >= 0.0) || !std::isfinite(radius_list[i]))
+      fail("task %d: invalid radius %g", i, radius_list[i]);
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    if (block_num_list[a] != block_num_list[b])
+      return block_num_list[a] < block_num_list[b];
+    if (iset_list[a] != iset_list[b])
+      return iset_list[a] < iset_list[b];
+    if (jset_list[a] != jset_list[b])
+      return jset_list[a] < jset_list[b];
+    return level_list[a] < level_list[b];
+  });
+  // ---- tasks, subblocks, sphere tables
+  t->tasks.resize(ntasks);
+  t->points.assign(ntasks, 0);
+  std::map<std::pair<int, long long>, int> sphere_of;
+  std::vector<long long> sphere_points;
+  long long maxbuf = 0;
+  for (int s = 0; s < ntasks; s++) {
+    const int i = order[s];
+    TaskDesc &d = t->tasks[s];
+    memset(&d, 0, sizeof(d));
+    const int lev = level_list[i] - 1, ia = iatom_list[i] - 1, ja = jatom_list[i] - 1;
+    const int iset = iset_list[i] - 1, jset = jset_list[i] - 1;
+    const grid_basis_set *bi = basis_sets[atom_kinds[ia] - 1];
+    const grid_basis_set *bj = basis_sets[atom_kinds[ja] - 1];
+    const LevelDesc &L = t->levels.lv[lev];
+    d.level = lev;
+    d.iatom = ia;
+    d.jatom = ja;
+    d.orig = i;
+    d.la_max = (int8_t)bi->lmax[iset];
+    d.la_min = (int8_t)bi->lmin[iset];
+    d.lb_max = (int8_t)bj->lmax[jset];
+    d.lb_min = (int8_t)bj->lmin[jset];
+    d.o1 = (int16_t)((ipgf_list[i] - 1) * ncoset(bi->lmax[iset]));
+    d.o2 = (int16_t)((jpgf_list[i] - 1) * ncoset(bj->lmax[jset]));
+    d.border_mask = (uint8_t)border_mask_list[i];
+    d.radius = radius_list[i];
+    const double zeta = bi->zet[iset * bi->maxpgf + ipgf_list[i] - 1];
+    const double zetb = bj->zet[jset * bj->maxpgf + jpgf_list[i] - 1];
+    d.zeta = zeta;
+    d.zetb = zetb;
+    // cab_to_grid (grid_ref_collint.h:917-947)
+    const double zetp = zeta + zetb, f = zetb / zetp;
+    const double *rab = &rab_list[3 * i], *ra = &atom_positions[3 * ia];
+    const double rab2 = rab[0] * rab[0] + rab[1] * rab[1] + rab[2] * rab[2];
+    d.zetp = zetp;
+    d.prefexp = exp(-zeta * f * rab2);
+    for (int k = 0; k < 3; k++) {
+      d.rab[k] = rab[k];
+      d.rp[k] = ra[k] + f * rab[k];
+    }
+    if (2.0 * d.radius < L.dh_max) {
+      d.flags |= TF_SKIP;
+    } else if (ortho && d.border_mask == 0) {
+      // ortho_cxyz_to_grid (grid_ref_collint.h:207-245)
+      for (int k = 0; k < 3; k++) {
+        double s_ = 0.0;
+        for (int j = 0; j < 3; j++)
+          s_ += L.dh_inv[j * 3 + k] * d.rp[j];
+        d.center[k] = (int)floor(s_);
+        d.roff[k] = d.rp[k] - ((double)d.center[k]) * L.dh[k * 4];
+      }
+      const double drmin = fmin(L.dh[0], fmin(L.dh[4], L.dh[8]));
+      const double nrad = fmax(1.0, ceil(d.radius / drmin));
+      const auto key = std::make_pair(lev, (long long)nrad);
+      auto it = sphere_of.find(key);
+      if (it == sphere_of.end()) {
+        SphereHdr h;
+        long long np = 0;
+        build_sphere(L, drmin * nrad, h, t->sph_tab, np);
+        t->sph.push_back(h);
+        sphere_points.push_back(np);
+        it = sphere_of.emplace(key, (int)t->sph.size() - 1).first;
+      }
+      d.sphere = it->second;
+      const SphereHdr &h = t->sph[d.sphere];
+      for (int k = 0; k < 3; k++)
+        if (L.npts_global[k] != L.npts_local[k]) { // grid_ref_collint.h:247-255
+          const int off = imod(d.center[k] + h.lb[k] - L.shift[k], L.npts_global[k]) - h.lb[k];
+          if (!(off + 1 - h.lb[k] < L.npts_local[k] && off + h.lb[k] >= 0))
+            fail("task %d: cube does not fit into the local grid of level %d", i, lev);
+        }
+      t->points[s] = sphere_points[d.sphere];
+    } else {
+      // general_cijk_to_grid (grid_ref_collint.h:609-640)
+      d.flags |= TF_GENERAL;
+      for (int k = 0; k < 3; k++) {
+        double g = 0.0;
+        for (int j = 0; j < 3; j++)
+          g += L.dh_inv[j * 3 + k] * d.rp[j];
+        d.roff[k] = g;
+        d.center[k] = INT32_MAX;
+        d.imax[k] = INT32_MIN;
+      }
+      for (int a = -1; a <= 1; a++)
+        for (int b = -1; b <= 1; b++)
+          for (int c = -1; c <= 1; c++) {
+            const double x = d.rp[0] + a * d.radius, y = d.rp[1] + b * d.radius,
+                         z = d.rp[2] + c * d.radius;
+            for (int k = 0; k < 3; k++) {
+              const double r = L.dh_inv[0 * 3 + k] * x + L.dh_inv[1 * 3 + k] * y +
+                               L.dh_inv[2 * 3 + k] * z;
+              d.center[k] = std::min(d.center[k], (int)floor(r));
+              d.imax[k] = std::max(d.imax[k], (int)ceil(r));
+            }
+          }
+      // points: rows of the box (host count, same expressions as the kernel)
+      long long np = 0;
+      const int w = d.imax[0] - d.center[0] + 1;
+      (void)w;
+      for (int k = d.center[2]; k <= d.imax[2]; k++)
+        for (int j = d.center[1]; j <= d.imax[1]; j++) {
+          double qa = 0, qb = 0, qc = 0;
+          for (int c = 0; c < 3; c++) {
+            const double v = (0 - d.roff[0]) * L.dh[c] + (j - d.roff[1]) * L.dh[3 + c] +
+                             (k - d.roff[2]) * L.dh[6 + c];
+            qa += L.dh[c] * L.dh[c];
+            qb += 2.0 * v * L.dh[c];
+            qc += v * v;
+          }
+          const double disc = qb * qb - 4.0 * qa * (qc - d.radius * d.radius);
+          if (0.0 < disc) {
+            const double sq = sqrt(disc), inv2a = 1.0 / (2.0 * qa);
+            const int lo = (int)ceil((-qb - sq) * inv2a), hi = (int)floor((-qb + sq) * inv2a);
+            if (hi >= lo)
+              np += hi - lo + 1;
+          }
+        }
+      t->points[s] = np;
+    }
+    // subblock bookkeeping
+    const int bn = block_num_list[i] - 1;
+    const bool new_sub = s == 0 || block_num_list[order[s - 1]] != block_num_list[i] ||
+                         iset_list[order[s - 1]] != iset_list[i] ||
+                         jset_list[order[s - 1]] != jset_list[i];
+    if (new_sub) {
+      SubblockDesc sb;
+      memset(&sb, 0, sizeof(sb));
+      sb.block_offset = block_offsets[bn];
+      sb.ncoa = bi->npgf[iset] * ncoset(bi->lmax[iset]);
+      sb.ncob = bj->npgf[jset] * ncoset(bj->lmax[jset]);
+      sb.nsgf_seta = bi->nsgf_set[iset];
+      sb.nsgf_setb = bj->nsgf_set[jset];
+      sb.sgfa = bi->first_sgf[iset] - 1;
+      sb.sgfb = bj->first_sgf[jset] - 1;
+      sb.nsgfa = bi->nsgf;
+      sb.nsgfb = bj->nsgf;
+      sb.maxcoa = bi->maxco;
+      sb.maxcob = bj->maxco;
+      sb.sphia = (int)(sphi_off[atom_kinds[ia] - 1] + (long long)sb.sgfa * bi->maxco);
+      sb.sphib = (int)(sphi_off[atom_kinds[ja] - 1] + (long long)sb.sgfb * bj->maxco);
+      sb.transpose = ia <= ja;
+      sb.identity = sphi_is_identity(bi, iset) && sphi_is_identity(bj, jset);
+      sb.iatom = ia;
+      sb.jatom = ja;
+      sb.first_task = s;
+      sb.cart_offset = (int)t->cart_total;
+      t->cart_total += (size_t)sb.ncoa * sb.ncob;
+      if (t->cart_total > (size_t)INT32_MAX)
+        fail("Cartesian scratch exceeds int offsets");
+      t->contract_words = std::max(t->contract_words, sb.nsgf_setb * sb.ncoa);
+      t->subs.push_back(sb);
+      maxbuf = std::max(maxbuf, (long long)block_offsets[bn] + (long long)bi->nsgf * bj->nsgf);
+    }
+    t->subs.back().ntasks++;
+    d.subblock = (int)t->subs.size() - 1;
+  }
+  t->buffer_len = maxbuf;
+  // ---- upload
+  CK(cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking));
+  for (auto &e : t->ev)
+    CK(cudaEventCreate(&e));
+  t->d_tasks = dalloc_copy(t->tasks);
+  t->d_subs = dalloc_copy(t->subs);
+  t->d_sph = dalloc_copy(t->sph);
+  t->d_sph_tab = dalloc_copy(t->sph_tab);
+  t->d_atom_pos = dalloc_copy(std::vector<double>(atom_positions, atom_positions + 3 * natoms));
+  t->d_sphi = dalloc_copy(sphi_all);
+  CK(cudaMalloc((void **)&t->d_levels, sizeof(LevelSet)));
+  CK(cudaMemcpy(t->d_levels, &t->levels, sizeof(LevelSet), cudaMemcpyHostToDevice));
+  CK(cudaMalloc((void **)&t->d_pab_cart, sizeof(double) * std::max<size_t>(t->cart_total, 1)));
+  CK(cudaMalloc((void **)&t->d_hab_cart, sizeof(double) * std::max<size_t>(t->cart_total, 1)));
+  CK(cudaMalloc((void **)&t->d_forces, sizeof(double) * 3 * std::max(natoms, 1)));
+  CK(cudaMalloc((void **)&t->d_virial, sizeof(double) * 9));
+  CK(cudaMalloc((void **)&t->d_counters, sizeof(int) * 64));
+  CK(cudaMalloc((void **)&t->d_error, sizeof(int)));
+  CK(cudaMemset(t->d_error, 0, sizeof(int)));
+  return t;
+}
+
+} // namespace gb300
+
+namespace gb300 {
+
+static Mode &get_mode(TaskList *t, const LDiffs &d) {
+  const int key = mode_key(d);
+  auto it = t->modes.find(key);
+  if (it != t->modes.end() && it->second.sched_version == t->sched_version)
+    return it->second;
+  Mode &m = t->modes[key];
+  m.d = d;
+  if (m.d_coef_off == nullptr) {
+    m.coef_off.resize(t->ntasks);
+    size_t off = 0;
+    int words = 4;
+    for (int s = 0; s < t->ntasks; s++) {
+      const TaskDesc &k = t->tasks[s];
+      const int la = k.la_max + d.la_max, lb = k.lb_max + d.lb_max;
+      m.coef_off[s] = (int)off;
+      if (!(k.flags & TF_SKIP)) {
+        off += ncoset(la + lb);
+        words = std::max(words, (int)coef_words(la, lb));
+      }
+      if (off > (size_t)INT32_MAX)
+        fail("coefficient buffer exceeds int offsets");
+    }
+    m.coef_total = off;
+    m.coef_words = words;
+    m.d_coef_off = dalloc_copy(m.coef_off);
+  }
+  // work queues, descending cost
+  std::vector<std::pair<double, int>> items[2][kNumBuckets];
+  for (int s = 0; s < t->ntasks; s++) {
+    const TaskDesc &k = t->tasks[s];
+    if (k.flags & TF_SKIP)
+      continue;
+    const int lp = k.la_max + d.la_max + k.lb_max + d.lb_max;
+    const int b = bucket_of(lp);
+    if (b < 0)
+      fail("contraction order lp=%d exceeds %d", lp, GB300_LP_MAX);
+    const int g = (k.flags & TF_GENERAL) ? 1 : 0;
+    double cost;
+    if (t->schedule == GRID_GB300_SCHEDULE_INPUT)
+      cost = -(double)k.orig;
+    else if (t->schedule == GRID_GB300_SCHEDULE_MODEL && !t->model_cost.empty())
+      cost = t->model_cost[s];
+    else
+      cost = (double)t->points[s] * (lp + 1) + 64.0 * (lp + 1) * (lp + 2);
+    items[g][b].push_back({cost, s});
+  }
+  for (int g = 0; g < 2; g++)
+    for (int b = 0; b < kNumBuckets; b++) {
+      Queue &q = m.q[g][b];
+      if (q.d_idx)
+        cudaFree(q.d_idx);
+      q.d_idx = nullptr;
+      auto &v = items[g][b];
+      std::stable_sort(v.begin(), v.end(), [](const std::pair<double, int> &x,
+                                              const std::pair<double, int> &y) {
+        return x.first > y.first;
+      });
+      std::vector<int> idx(v.size());
+      int ext = 1;
+      for (size_t i = 0; i < v.size(); i++) {
+        idx[i] = v[i].second;
+        const TaskDesc &k = t->tasks[idx[i]];
+        if (g == 0)
+          ext = std::max(ext, 2 * t->sph[k.sphere].cmax + 2);
+        else
+          ext = std::max(ext, k.imax[1] - k.center[1] + 1);
+      }
+      q.n = (int)idx.size();
+      q.extent = ext;
+      if (q.n)
+        q.d_idx = dalloc_copy(idx);
+    }
+  m.sched_version = t->sched_version;
+  return m;
+}
+
+static void ensure(void **p, size_t *cap, size_t bytes) {
+  if (*cap >= bytes && *p)
+    return;
+  if (*p)
+    CK(cudaFree(*p));
+  CK(cudaMalloc(p, std::max<size_t>(bytes, 16)));
+  *cap = bytes;
+}
+
+static void check_device_error(TaskList *t) {
+  int err = 0;
+  CK(cudaMemcpy(&err, t->d_error, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err)
+    fail("grid kernel reported error code %d (work item exceeded its shared-memory sizing)", err);
+}
+
+static double ev_ms(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+static void read_timings(TaskList *t) {
+  CK(cudaEventSynchronize(t->ev[3]));
+  t->timings[0] = ev_ms(t->ev[0], t->ev[1]);
+  t->timings[1] = ev_ms(t->ev[1], t->ev[2]);
+  t->timings[2] = ev_ms(t->ev[2], t->ev[3]);
+  t->timings[3] = ev_ms(t->ev[0], t->ev[3]);
+}
+
+static void run_collocate(TaskList *t, int func, const double *pab, double *const *grids,
+                          cudaStream_t s) {
+  const LDiffs d = func_ldiffs(func);
+  Mode &m = get_mode(t, d);
+  const bool fp32 = t->precision == GRID_GB300_MIXED;
+  ensure(&t->d_coef, &t->coef_cap, m.coef_total * (fp32 ? 4 : 8));
+  CK(cudaEventRecord(t->ev[0], s));
+  ContractArgs ca{t->d_subs, (int)t->subs.size(), t->d_sphi, pab, nullptr, t->d_pab_cart,
+                  t->contract_words};
+  launch_decontract(ca, s);
+  CoefArgs co{t->d_tasks, t->d_subs, m.d_coef_off, t->d_atom_pos, t->d_pab_cart, t->d_coef,
+              t->ntasks, func, d, t->d_levels};
+  launch_coefficients(co, fp32, m.coef_words, s);
+  CK(cudaEventRecord(t->ev[1], s));
+  for (int l = 0; l < t->nlevels; l++) {
+    const int *n = &t->npts_local[3 * l];
+    CK(cudaMemsetAsync(grids[l], 0, sizeof(double) * (size_t)n[0] * n[1] * n[2], s));
+  }
+  CK(cudaMemsetAsync(t->d_counters, 0, sizeof(int) * 64, s));
+  GridArgs ga{};
+  ga.tasks = t->d_tasks;
+  ga.coef_off = m.d_coef_off;
+  ga.coef = t->d_coef;
+  ga.sph = t->d_sph;
+  ga.sph_tab = t->d_sph_tab;
+  for (int l = 0; l < t->nlevels; l++)
+    ga.grids[l] = grids[l];
+  ga.levels = t->levels;
+  ga.d = d;
+  ga.task_cycles = t->d_cycles;
+  ga.error = t->d_error;
+  int qi = 0;
+  for (int g = 0; g < 2; g++)
+    for (int b = 0; b < kNumBuckets; b++) {
+      const Queue &q = m.q[g][b];
+      if (!q.n)
+        continue;
+      ga.queue = q.d_idx;
+      ga.nqueue = q.n;
+      ga.counter = t->d_counters + qi++;
+      launch_collocate(ga, fp32, g == 1, b, q.extent, 0, s);
+      grid_library_counter_add(kBucketLp[b], GRID_BACKEND_GB300,
+                               g ? GRID_COLLOCATE_GENERAL : GRID_COLLOCATE_ORTHO, q.n);
+    }
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(t->ev[2], s));
+  CK(cudaEventRecord(t->ev[3], s));
+}
+
+static void run_integrate(TaskList *t, bool tau, const double *pab, const double *const *grids,
+                          double *hab, double *forces, double *virial, cudaStream_t s) {
+  const LDiffs d = integrate_ldiffs(forces != nullptr, virial != nullptr, tau);
+  Mode &m = get_mode(t, d);
+  const bool fp32 = t->precision == GRID_GB300_MIXED;
+  const bool need_pab = forces != nullptr || virial != nullptr;
+  ensure((void **)&t->d_coef_int, &t->coef_int_cap, m.coef_total * 8);
+  CK(cudaEventRecord(t->ev[0], s));
+  if (fp32)
+    for (int l = 0; l < t->nlevels; l++) {
+      const int *n = &t->npts_local[3 * l];
+      const size_t np = (size_t)n[0] * n[1] * n[2];
+      if (!t->d_grid32[l])
+        CK(cudaMalloc((void **)&t->d_grid32[l], sizeof(float) * np));
+      launch_grid_to_fp32(grids[l], t->d_grid32[l], np, s);
+    }
+  if (need_pab) {
+    ContractArgs ca{t->d_subs, (int)t->subs.size(), t->d_sphi, pab, nullptr, t->d_pab_cart,
+                    t->contract_words};
+    launch_decontract(ca, s);
+  }
+  CK(cudaMemsetAsync(t->d_counters, 0, sizeof(int) * 64, s));
+  CK(cudaEventRecord(t->ev[1], s));
+  GridArgs ga{};
+  ga.tasks = t->d_tasks;
+  ga.coef_off = m.d_coef_off;
+  ga.coef_out = t->d_coef_int;
+  ga.sph = t->d_sph;
+  ga.sph_tab = t->d_sph_tab;
+  for (int l = 0; l < t->nlevels; l++)
+    ga.grids_in[l] = fp32 ? (const void *)t->d_grid32[l] : (const void *)grids[l];
+  ga.levels = t->levels;
+  ga.d = d;
+  ga.task_cycles = t->d_cycles;
+  ga.error = t->d_error;
+  int qi = 0;
+  for (int g = 0; g < 2; g++)
+    for (int b = 0; b < kNumBuckets; b++) {
+      const Queue &q = m.q[g][b];
+      if (!q.n)
+        continue;
+      ga.queue = q.d_idx;
+      ga.nqueue = q.n;
+      ga.counter = t->d_counters + qi++;
+      launch_integrate(ga, fp32, g == 1, b, q.extent, 0, s);
+      grid_library_counter_add(kBucketLp[b], GRID_BACKEND_GB300,
+                               g ? GRID_INTEGRATE_GENERAL : GRID_INTEGRATE_ORTHO, q.n);
+    }
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(t->ev[2], s));
+  CK(cudaMemsetAsync(t->d_hab_cart, 0, sizeof(double) * std::max<size_t>(t->cart_total, 1), s));
+  if (forces)
+    CK(cudaMemsetAsync(forces, 0, sizeof(double) * 3 * t->natoms, s));
+  if (virial)
+    CK(cudaMemsetAsync(virial, 0, sizeof(double) * 9, s));
+  PostArgs pa{t->d_tasks, t->d_subs, m.d_coef_off, t->d_coef_int,
+              need_pab ? t->d_pab_cart : nullptr, t->d_hab_cart, t->d_atom_pos, forces, virial,
+              t->ntasks, tau ? 1 : 0, d, t->d_levels};
+  launch_post(pa, fp32, m.coef_words, s);
+  CK(cudaMemsetAsync(hab, 0, sizeof(double) * (size_t)t->buffer_len, s));
+  ContractArgs cb{t->d_subs, (int)t->subs.size(), t->d_sphi, nullptr, hab, t->d_hab_cart,
+                  t->contract_words};
+  launch_contract_hab(cb, s);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(t->ev[3], s));
+}
+
+static TaskList *TL(const void *p) {
+  if (!p)
+    fail("null task list");
+  return (TaskList *)p;
+}
+
+} // namespace gb300
+
+// ===========================================================================
+// backend-level entry points
+// ===========================================================================
+GB300_API void grid_gb300_create_task_list(
+    const bool orthorhombic, const int ntasks, const int nlevels, const int natoms,
+    const int nkinds, const int nblocks, const int *block_offsets, const double *atom_positions,
+    const int *atom_kinds, const grid_basis_set **basis_sets, const int *level_list,
+    const int *iatom_list, const int *jatom_list, const int *iset_list, const int *jset_list,
+    const int *ipgf_list, const int *jpgf_list, const int *border_mask_list,
+    const int *block_num_list, const double *radius_list, const double *rab_list,
+    const int *npts_global, const int *npts_local, const int *shift_local,
+    const int *border_width, const double *dh, const double *dh_inv,
+    grid_gb300_task_list **task_list) {
+  int prec = GRID_GB300_FP64, sched = GRID_GB300_SCHEDULE_SIZE;
+  if (*task_list) { // re-creation keeps the caller's settings
+    prec = TL(*task_list)->precision;
+    sched = TL(*task_list)->schedule;
+    grid_gb300_free_task_list(*task_list);
+  }
+  TaskList *t = create(orthorhombic, ntasks, nlevels, natoms, nkinds, nblocks, block_offsets,
+                       atom_positions, atom_kinds, basis_sets, level_list, iatom_list,
+                       jatom_list, iset_list, jset_list, ipgf_list, jpgf_list,
+                       border_mask_list, block_num_list, radius_list, rab_list, npts_global,
+                       npts_local, shift_local, border_width, dh, dh_inv);
+  t->precision = prec;
+  t->schedule = sched;
+  *task_list = t;
+}
+
+GB300_API void grid_gb300_free_task_list(grid_gb300_task_list *task_list) {
+  if (!task_list)
+    return;
+  TaskList *t = TL(task_list);
+  free_device(t);
+  delete t;
+}
+
+GB300_API void grid_gb300_collocate_device_async(const grid_gb300_task_list *task_list, int func,
+                                                 const double *pab_blocks, double *const *grids,
+                                                 void *stream) {
+  TaskList *t = TL(task_list);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (t->empty) {
+    for (int l = 0; l < t->nlevels; l++) {
+      const int *n = &t->npts_local[3 * l];
+      CK(cudaMemsetAsync(grids[l], 0, sizeof(double) * (size_t)n[0] * n[1] * n[2], s));
+    }
+    return;
+  }
+  run_collocate(t, func, pab_blocks, grids, s);
+}
+
+GB300_API void grid_gb300_integrate_device_async(const grid_gb300_task_list *task_list,
+                                                 bool compute_tau, const double *pab_blocks,
+                                                 const double *const *grids, double *hab_blocks,
+                                                 double *forces, double *virial, void *stream) {
+  TaskList *t = TL(task_list);
+  cudaStream_t s = (cudaStream_t)stream;
+  if ((forces || virial) && !pab_blocks)
+    fail("forces and virial require pab_blocks");
+  if (t->empty) {
+    if (t->buffer_len)
+      CK(cudaMemsetAsync(hab_blocks, 0, sizeof(double) * t->buffer_len, s));
+    if (forces)
+      CK(cudaMemsetAsync(forces, 0, sizeof(double) * 3 * t->natoms, s));
+    if (virial)
+      CK(cudaMemsetAsync(virial, 0, sizeof(double) * 9, s));
+    return;
+  }
+  run_integrate(t, compute_tau, pab_blocks, grids, hab_blocks, forces, virial, s);
+}
+
+GB300_API void grid_gb300_collocate_task_list(const grid_gb300_task_list *task_list,
+                                              const enum grid_func func, const int nlevels,
+                                              const offload_buffer *pab_blocks,
+                                              offload_buffer **grids) {
+  TaskList *t = TL(task_list);
+  if (nlevels != t->nlevels)
+    fail("collocate: nlevels %d does not match the task list (%d)", nlevels, t->nlevels);
+  if (t->empty) {
+    for (int l = 0; l < nlevels; l++)
+      memset(grids[l]->host_buffer, 0, grids[l]->size);
+    return;
+  }
+  cudaStream_t s = t->stream;
+  CK(cudaMemcpyAsync(pab_blocks->device_buffer, pab_blocks->host_buffer, pab_blocks->size,
+                     cudaMemcpyHostToDevice, s));
+  double *g[GB300_MAX_LEVELS];
+  for (int l = 0; l < nlevels; l++)
+    g[l] = grids[l]->device_buffer;
+  run_collocate(t, func, pab_blocks->device_buffer, g, s);
+  for (int l = 0; l < nlevels; l++)
+    CK(cudaMemcpyAsync(grids[l]->host_buffer, grids[l]->device_buffer, grids[l]->size,
+                       cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  read_timings(t);
+  check_device_error(t);
+}
+
+GB300_API void grid_gb300_integrate_task_list(const grid_gb300_task_list *task_list,
+                                              const bool compute_tau, const int nlevels,
+                                              const offload_buffer *pab_blocks,
+                                              const offload_buffer **grids,
+                                              offload_buffer *hab_blocks, double *forces,
+                                              double *virial) {
+  TaskList *t = TL(task_list);
+  if (nlevels != t->nlevels)
+    fail("integrate: nlevels %d does not match the task list (%d)", nlevels, t->nlevels);
+  if ((forces || virial) && !pab_blocks)
+    fail("forces and virial require pab_blocks");
+  if (t->empty) {
+    memset(hab_blocks->host_buffer, 0, hab_blocks->size);
+    if (forces)
+      memset(forces, 0, sizeof(double) * 3 * t->natoms);
+    if (virial)
+      memset(virial, 0, sizeof(double) * 9);
+    return;
+  }
+  if ((long long)(hab_blocks->size / sizeof(double)) < t->buffer_len)
+    fail("integrate: hab buffer holds %zu doubles, the task list needs %lld",
+         hab_blocks->size / sizeof(double), t->buffer_len);
+  cudaStream_t s = t->stream;
+  const double *g[GB300_MAX_LEVELS];
+  for (int l = 0; l < nlevels; l++) {
+    CK(cudaMemcpyAsync(grids[l]->device_buffer, grids[l]->host_buffer, grids[l]->size,
+                       cudaMemcpyHostToDevice, s));
+    g[l] = grids[l]->device_buffer;
+  }
+  if (pab_blocks && (forces || virial))
+    CK(cudaMemcpyAsync(pab_blocks->device_buffer, pab_blocks->host_buffer, pab_blocks->size,
+                       cudaMemcpyHostToDevice, s));
+  run_integrate(t, compute_tau, pab_blocks ? pab_blocks->device_buffer : nullptr, g,
+                hab_blocks->device_buffer, forces ? t->d_forces : nullptr,
+                virial ? t->d_virial : nullptr, s);
+  CK(cudaMemcpyAsync(hab_blocks->host_buffer, hab_blocks->device_buffer, hab_blocks->size,
+                     cudaMemcpyDeviceToHost, s));
+  if (forces)
+    CK(cudaMemcpyAsync(forces, t->d_forces, sizeof(double) * 3 * t->natoms,
+                       cudaMemcpyDeviceToHost, s));
+  if (virial)
+    CK(cudaMemcpyAsync(virial, t->d_virial, sizeof(double) * 9, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  read_timings(t);
+  check_device_error(t);
+}
+
+// ===========================================================================
+// CP2K task-list surface (src/grid/grid_task_list.c)
+// ===========================================================================
+struct TopList {
+  int nlevels = 0;
+  int natoms = 0;
+  std::vector<int> npts_local;
+  grid_gb300_task_list *impl = nullptr;
+};
+
+GB300_API void grid_create_task_list(
+    const bool orthorhombic, const int ntasks, const int nlevels, const int natoms,
+    const int nkinds, const int nblocks, const int *block_offsets, const double *atom_positions,
+    const int *atom_kinds, const grid_basis_set **basis_sets, const int *level_list,
+    const int *iatom_list, const int *jatom_list, const int *iset_list, const int *jset_list,
+    const int *ipgf_list, const int *jpgf_list, const int *border_mask_list,
+    const int *block_num_list, const double *radius_list, const double *rab_list,
+    const int *npts_global, const int *npts_local, const int *shift_local,
+    const int *border_width, const double *dh, const double *dh_inv,
+    grid_task_list **task_list) {
+  const int be = g_config.backend;
+  if (be != GRID_BACKEND_AUTO && be != GRID_BACKEND_GPU && be != GRID_BACKEND_GB300)
+    fail("grid backend %d is provided by CP2K's own grid library, not by this one", be);
+  TopList *tl = (TopList *)*task_list;
+  if (!tl)
+    tl = new TopList();
+  tl->nlevels = nlevels;
+  tl->natoms = natoms;
+  tl->npts_local.assign(npts_local, npts_local + 3 * std::max(nlevels, 0));
+  grid_gb300_create_task_list(orthorhombic, ntasks, nlevels, natoms, nkinds, nblocks,
+                              block_offsets, atom_positions, atom_kinds, basis_sets, level_list,
+                              iatom_list, jatom_list, iset_list, jset_list, ipgf_list,
+                              jpgf_list, border_mask_list, block_num_list, radius_list,
+                              rab_list, npts_global, npts_local, shift_local, border_width, dh,
+                              dh_inv, &tl->impl);
+  *task_list = tl;
+}
+
+GB300_API grid_gb300_task_list *grid_gb300_backend_handle(const grid_task_list *task_list) {
+  return task_list ? ((const TopList *)task_list)->impl : nullptr;
+}
+
+GB300_API void grid_free_task_list(grid_task_list *task_list) {
+  if (!task_list)
+    return;
+  TopList *tl = (TopList *)task_list;
+  grid_gb300_free_task_list(tl->impl);
+  delete tl;
+}
+
+static void check_npts(const TopList *tl, int nlevels, const int *npts_local) {
+  if (nlevels != tl->nlevels)
+    fail("nlevels %d does not match the task list (%d)", nlevels, tl->nlevels);
+  for (int i = 0; i < 3 * nlevels; i++)
+    if (npts_local[i] != tl->npts_local[i])
+      fail("npts_local of level %d does not match the task list", i / 3);
+}
+
+GB300_API void grid_collocate_task_list(const grid_task_list *task_list,
+                                        const enum grid_func func, const int nlevels,
+                                        const int *npts_local, const offload_buffer *pab_blocks,
+                                        offload_buffer **grids) {
+  const TopList *tl = (const TopList *)task_list;
+  if (!tl)
+    return;
+  check_npts(tl, nlevels, npts_local);
+  grid_gb300_collocate_task_list(tl->impl, func, nlevels, pab_blocks, grids);
+}
+
+GB300_API void grid_integrate_task_list(const grid_task_list *task_list, const bool compute_tau,
+                                        const int natoms, const int nlevels,
+                                        const int *npts_local, const offload_buffer *pab_blocks,
+                                        const offload_buffer **grids, offload_buffer *hab_blocks,
+                                        double *forces, double *virial) {
+  const TopList *tl = (const TopList *)task_list;
+  if (!tl)
+    return;
+  check_npts(tl, nlevels, npts_local);
+  if (natoms != tl->natoms)
+    fail("natoms %d does not match the task list (%d)", natoms, tl->natoms);
+  grid_gb300_integrate_task_list(tl->impl, compute_tau, nlevels, pab_blocks, grids, hab_blocks,
+                                 forces, virial);
+}
+
+// ===========================================================================
+// extensions
+// ===========================================================================
+GB300_API void grid_gb300_set_precision(const grid_gb300_task_list *task_list, int precision) {
+  if (precision != GRID_GB300_FP64 && precision != GRID_GB300_MIXED)
+    fail("unknown precision mode %d", precision);
+  TL(task_list)->precision = precision;
+}
+
+GB300_API int grid_gb300_get_precision(const grid_gb300_task_list *task_list) {
+  return TL(task_list)->precision;
+}
+
+GB300_API void grid_gb300_set_schedule(const grid_gb300_task_list *task_list, int schedule) {
+  if (schedule < GRID_GB300_SCHEDULE_SIZE || schedule > GRID_GB300_SCHEDULE_INPUT)
+    fail("unknown schedule %d", schedule);
+  TaskList *t = TL(task_list);
+  if (t->schedule != schedule) {
+    t->schedule = schedule;
+    t->sched_version++;
+  }
+}
+
+GB300_API void grid_gb300_task_list_info(const grid_gb300_task_list *task_list, int *ntasks,
+                                         int *nlevels, int *natoms, long long *buffer_len) {
+  const TaskList *t = TL(task_list);
+  if (ntasks)
+    *ntasks = t->ntasks;
+  if (nlevels)
+    *nlevels = t->nlevels;
+  if (natoms)
+    *natoms = t->natoms;
+  if (buffer_len)
+    *buffer_len = t->buffer_len;
+}
+
+GB300_API void grid_gb300_task_sizes(const grid_gb300_task_list *task_list, long long *points,
+                                     int *lp) {
+  const TaskList *t = TL(task_list);
+  for (int s = 0; s < (int)t->tasks.size(); s++) {
+    const TaskDesc &k = t->tasks[s];
+    if (points)
+      points[k.orig] = (k.flags & TF_SKIP) ? 0 : t->points[s];
+    if (lp)
+      lp[k.orig] = k.la_max + k.lb_max;
+  }
+}
+
+GB300_API void grid_gb300_last_timings(const grid_gb300_task_list *task_list,
+                                       double timings_ms[4]) {
+  const TaskList *t = TL(task_list);
+  for (int i = 0; i < 4; i++)
+    timings_ms[i] = t->timings[i];
+}

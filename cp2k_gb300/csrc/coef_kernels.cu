@@ -1,0 +1,677 @@
+// Per-task and per-subblock small dense transforms of the GB300 backend.
+//
+//  decontract   spherical P sub-block -> Cartesian pab           (per subblock)
+//               (src/grid/ref/grid_ref_task_list.c:237-271, load_pab)
+//  coefficients pab -> C_ab (grid_func) -> C_xyz about rp (-> C_ijk for the
+//               general path)                                     (per task)
+//               (common/grid_prepare_pab.h, ref/grid_ref_collint.h:698-911)
+//  post         integrated C_xyz (C_ijk) -> C_ab -> hab, forces, virial
+//               (ref/grid_ref_integrate.c:44-152, common/grid_process_vab.h)
+//  contract_hab Cartesian hab -> spherical block, accumulated     (per subblock)
+//               (src/grid/ref/grid_ref_task_list.c:462-499, store_hab)
+//
+// One warp per task / subblock, operands staged in shared memory.  The
+// per-task work is templated on the arithmetic type: FP64 for the plain path,
+// FP32 for the mixed path (accumulation into hab / forces / virial stays FP64
+// atomics in both).
+#include <cuda_runtime.h>
+
+#include <cstdio>
+
+#include "gb300_internal.h"
+
+namespace gb300 {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+struct Orb {
+  int l[3];
+};
+__device__ __forceinline__ Orb up(int d, Orb a) {
+  a.l[d] += 1;
+  return a;
+}
+__device__ __forceinline__ Orb dn(int d, Orb a) {
+  a.l[d] = a.l[d] > 0 ? a.l[d] - 1 : 0;
+  return a;
+}
+__device__ __forceinline__ int oidx(Orb a) { return coset(a.l[0], a.l[1], a.l[2]); }
+
+// orbital of Cartesian index i within shell l (inverse of coset)
+__device__ __forceinline__ Orb orb_of(int l, int i) {
+  // coset ordering inside a shell: lx descending, then lz ascending
+  int lx = l;
+  int base = 0;
+  while (i >= base + (l - lx + 1)) {
+    base += l - lx + 1;
+    lx--;
+  }
+  const int lz = i - base;
+  Orb o;
+  o.l[0] = lx;
+  o.l[2] = lz;
+  o.l[1] = l - lx - lz;
+  return o;
+}
+
+// ------------------------------------------------------------------------
+// grid_func: P_ab -> C_ab  (grid_prepare_pab.h:26-430)
+// ------------------------------------------------------------------------
+template <typename T> struct CabW {
+  T *c;
+  int n1;
+  __device__ __forceinline__ void add(Orb a, Orb b, T v) const {
+    if (v != T(0))
+      atomicAdd(&c[oidx(b) * n1 + oidx(a)], v);
+  }
+};
+
+template <typename T>
+__device__ void term_dij_b(int pair, T fa, Orb a, Orb b, T zb, const CabW<T> &w) {
+  const int i1 = pair, i2 = (pair + 1) % 3;
+  w.add(a, dn(i1, dn(i2, b)), T(b.l[i1] * b.l[i2]) * fa);
+  w.add(a, up(i1, dn(i2, b)), T(-2) * zb * T(b.l[i2]) * fa);
+  w.add(a, dn(i1, up(i2, b)), T(-2) * zb * T(b.l[i1]) * fa);
+  w.add(a, up(i1, up(i2, b)), T(4) * zb * zb * fa);
+}
+
+template <typename T>
+__device__ void term_dii_b(int d, T fa, Orb a, Orb b, T zb, const CabW<T> &w) {
+  w.add(a, dn(d, dn(d, b)), T(b.l[d] * (b.l[d] - 1)) * fa);
+  w.add(a, b, T(-2) * zb * T(2 * b.l[d] + 1) * fa);
+  w.add(a, up(d, up(d, b)), T(4) * zb * zb * fa);
+}
+
+template <typename T>
+__device__ void prep_one(int f, Orb a, Orb b, T za, T zb, T p, const CabW<T> &w) {
+  if (f == 100) {
+    w.add(a, b, p);
+  } else if (f == 200) {
+    for (int i = 0; i < 3; i++) {
+      w.add(dn(i, a), dn(i, b), T(0.5) * T(a.l[i] * b.l[i]) * p);
+      w.add(dn(i, a), up(i, b), -T(a.l[i]) * zb * p);
+      w.add(up(i, a), dn(i, b), -za * T(b.l[i]) * p);
+      w.add(up(i, a), up(i, b), T(2) * za * zb * p);
+    }
+  } else if (f >= 301 && f <= 303) {
+    const int d = f - 301;
+    w.add(a, dn(d, b), T(b.l[d]) * p);
+    w.add(a, up(d, b), T(-2) * zb * p);
+    w.add(dn(d, a), b, -T(a.l[d]) * p);
+    w.add(up(d, a), b, T(2) * za * p);
+  } else if (f >= 411 && f <= 433) {
+    const int d = f / 10 - 41, r = f % 10 - 1;
+    const Orb br = up(r, b);
+    w.add(a, dn(d, br), T(b.l[d]) * p);
+    w.add(a, up(d, br), T(-2) * zb * p);
+    w.add(dn(d, a), br, -T(a.l[d]) * p);
+    w.add(up(d, a), br, T(2) * za * p);
+  } else if (f >= 501 && f <= 503) {
+    const int d = f - 501;
+    w.add(a, dn(d, b), T(b.l[d]) * p);
+    w.add(a, up(d, b), T(-2) * zb * p);
+    w.add(dn(d, a), b, T(a.l[d]) * p);
+    w.add(up(d, a), b, T(-2) * za * p);
+  } else if (f >= 901 && f <= 903) {
+    const int d = f - 901;
+    w.add(dn(d, a), b, -T(a.l[d]) * p);
+    w.add(up(d, a), b, T(2) * za * p);
+  } else if (f >= 904 && f <= 906) {
+    const int d = f - 904;
+    w.add(a, dn(d, b), -T(b.l[d]) * p);
+    w.add(a, up(d, b), T(2) * zb * p);
+  } else if (f >= 1001 && f <= 1003) {
+    const int d = f - 1001;
+    w.add(up(d, a), b, T(2) * za * p);
+  } else if (f >= 601 && f <= 603) {
+    const int d = f - 601;
+    w.add(dn(d, a), dn(d, b), T(a.l[d] * b.l[d]) * p);
+    w.add(dn(d, a), up(d, b), T(-2) * T(a.l[d]) * zb * p);
+    w.add(up(d, a), dn(d, b), T(-2) * za * T(b.l[d]) * p);
+    w.add(up(d, a), up(d, b), T(4) * za * zb * p);
+  } else if (f >= 701 && f <= 703) {
+    const int pair = f - 701, d1 = pair, d2 = (pair + 1) % 3;
+    term_dij_b<T>(pair, T(a.l[d1] * a.l[d2]) * p, dn(d1, dn(d2, a)), b, zb, w);
+    term_dij_b<T>(pair, T(-2) * za * T(a.l[d2]) * p, up(d1, dn(d2, a)), b, zb, w);
+    term_dij_b<T>(pair, T(-2) * za * T(a.l[d1]) * p, dn(d1, up(d2, a)), b, zb, w);
+    term_dij_b<T>(pair, T(4) * za * za * p, up(d1, up(d2, a)), b, zb, w);
+  } else if (f >= 801 && f <= 803) {
+    const int d = f - 801;
+    term_dii_b<T>(d, T(a.l[d] * (a.l[d] - 1)) * p, dn(d, dn(d, a)), b, zb, w);
+    term_dii_b<T>(d, T(-2) * za * T(2 * a.l[d] + 1) * p, a, b, zb, w);
+    term_dii_b<T>(d, T(4) * za * za * p, up(d, up(d, a)), b, zb, w);
+  }
+}
+
+// ------------------------------------------------------------------------
+// Binomial expansion tables alpha[dir][lxb][lxa][l]: coefficient of (x-p)^l
+// in (x-a)^lxa (x-b)^lxb  (grid_ref_collint.h:838-861)
+// ------------------------------------------------------------------------
+template <typename T>
+__device__ void fill_alpha(T *alpha, int la, int lb, int lp, const double ra[3],
+                           const double rb[3], const double rp[3], int lane) {
+  const int na = la + 1, nb = lb + 1, P = lp + 1;
+  for (int e = lane; e < 3 * na * nb * P; e += 32)
+    alpha[e] = T(0);
+  __syncwarp();
+  for (int e = lane; e < 3 * na * nb; e += 32) {
+    const int d = e / (na * nb), r = e % (na * nb), xb = r / na, xa = r % na;
+    const double pa = rp[d] - ra[d], pb = rp[d] - rb[d];
+    T *al = alpha + ((size_t)(d * nb + xb) * na + xa) * P;
+    double ca = 1.0, powa = 1.0;
+    for (int k = 0; k <= xa; k++) {
+      double cb = 1.0, powb = 1.0;
+      for (int m = 0; m <= xb; m++) {
+        al[xa - k + xb - m] += (T)(ca * cb * powa * powb);
+        cb = cb * (double)(xb - m) / (double)(m + 1);
+        powb *= pb;
+      }
+      ca = ca * (double)(xa - k) / (double)(k + 1);
+      powa *= pa;
+    }
+  }
+  __syncwarp();
+}
+
+// sum over C_ab entries of one C_xyz monomial (or the adjoint), gathering
+// only pairs whose alpha products are structurally non-zero.
+template <typename T>
+__device__ T cab_cxyz_term(const T *cab, int n1, const T *alpha, int la, int lb,
+                           int lp, int px, int py, int pz) {
+  const int na = la + 1, nb = lb + 1, P = lp + 1;
+  auto A = [&](int d, int xb, int xa, int l) {
+    return alpha[((size_t)(d * nb + xb) * na + xa) * P + l];
+  };
+  T s = T(0);
+  for (int az = 0; az <= la; az++)
+    for (int bz = 0; bz <= lb; bz++) {
+      if (az + bz < pz)
+        continue;
+      const T wz = A(2, bz, az, pz);
+      for (int ay = 0; ay <= la - az; ay++)
+        for (int by = 0; by <= lb - bz; by++) {
+          if (ay + by < py)
+            continue;
+          const T wyz = wz * A(1, by, ay, py);
+          for (int ax = 0; ax <= la - az - ay; ax++)
+            for (int bx = 0; bx <= lb - bz - by; bx++) {
+              if (ax + bx < px)
+                continue;
+              s += wyz * A(0, bx, ax, px) * cab[coset(bx, by, bz) * n1 + coset(ax, ay, az)];
+            }
+        }
+    }
+  return s;
+}
+
+// C_ab entry (a, b) from C_xyz (integrate adjoint of the above)
+template <typename T>
+__device__ T cxyz_cab_term(const T *cxyz, const T *alpha, int la, int lb, int lp, Orb a,
+                           Orb b) {
+  const int na = la + 1, nb = lb + 1, P = lp + 1;
+  auto A = [&](int d, int xb, int xa, int l) {
+    return alpha[((size_t)(d * nb + xb) * na + xa) * P + l];
+  };
+  T s = T(0);
+  for (int pz = 0; pz <= a.l[2] + b.l[2]; pz++) {
+    const T wz = A(2, b.l[2], a.l[2], pz);
+    for (int py = 0; py <= a.l[1] + b.l[1]; py++) {
+      const T wyz = wz * A(1, b.l[1], a.l[1], py);
+      for (int px = 0; px <= a.l[0] + b.l[0]; px++)
+        s += wyz * A(0, b.l[0], a.l[0], px) * cxyz[cidx(pz, py, px, lp)];
+    }
+  }
+  return s;
+}
+
+// multinomial weight of lattice split for the general path
+__device__ __forceinline__ double fact(int n) {
+  double f = 1.0;
+  for (int i = 2; i <= n; i++)
+    f *= i;
+  return f;
+}
+__device__ __forceinline__ double ipow(double x, int n) {
+  double r = 1.0;
+  for (int i = 0; i < n; i++)
+    r *= x;
+  return r;
+}
+
+// C_xyz term (lx, ly, lz) <-> C_ijk through x_c = sum_d u_d dh[d][c]
+// (grid_ref_collint.h:698-762).  forward: scatter cxyz[e] into cijk (smem
+// atomics); adjoint: gather cijk into the returned value.
+template <typename T>
+__device__ T cxyz_cijk_term(bool forward, const double *h, int lp, int lx, int ly, int lz,
+                            T cval, T *cijk_scatter, const T *cijk_gather) {
+  const double fl = fact(lx) * fact(ly) * fact(lz);
+  double acc = 0.0;
+  for (int ix = 0; ix <= lx; ix++)
+    for (int jx = 0; jx <= lx - ix; jx++) {
+      const int kx = lx - ix - jx;
+      const double wx = ipow(h[0], ix) * ipow(h[3], jx) * ipow(h[6], kx) /
+                        (fact(ix) * fact(jx) * fact(kx));
+      for (int iy = 0; iy <= ly; iy++)
+        for (int jy = 0; jy <= ly - iy; jy++) {
+          const int ky = ly - iy - jy;
+          const double wy = ipow(h[1], iy) * ipow(h[4], jy) * ipow(h[7], ky) /
+                            (fact(iy) * fact(jy) * fact(ky));
+          for (int iz = 0; iz <= lz; iz++)
+            for (int jz = 0; jz <= lz - iz; jz++) {
+              const int kz = lz - iz - jz;
+              const double wz = ipow(h[2], iz) * ipow(h[5], jz) * ipow(h[8], kz) /
+                                (fact(iz) * fact(jz) * fact(kz));
+              const int e = cidx(kx + ky + kz, jx + jy + jz, ix + iy + iz, lp);
+              const double wgt = wx * wy * wz * fl;
+              if (forward)
+                atomicAdd(&cijk_scatter[e], (T)(wgt * (double)cval));
+              else
+                acc += wgt * (double)cijk_gather[e];
+            }
+        }
+    }
+  return (T)acc;
+}
+
+template <typename T> struct CoefSmem {
+  // cab [n2][n1], alpha, cxyz, cijk
+  static __host__ __device__ size_t words(int n1, int n2, int la, int lb, int lp) {
+    return (size_t)n1 * n2 + 3 * (size_t)(la + 1) * (lb + 1) * (lp + 1) + 2 * (size_t)ncoset(lp) + 4;
+  }
+};
+
+// ------------------------------------------------------------------------
+// coefficients: one warp per task
+// ------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(128) coefficients_kernel(CoefArgs a, int words_per_warp) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  T *ws = (T *)smem + (size_t)(threadIdx.x >> 5) * words_per_warp;
+  T *out = (T *)a.coef;
+  for (int t = gw; t < a.ntasks; t += nwarps) {
+    const TaskDesc d = a.tasks[t];
+    if (d.flags & TF_SKIP)
+      continue;
+    const SubblockDesc sb = a.subs[d.subblock];
+    const int la_max = d.la_max + a.d.la_max, lb_max = d.lb_max + a.d.lb_max;
+    const int lp = la_max + lb_max;
+    const int n1 = ncoset(la_max), n2 = ncoset(lb_max);
+    T *cab = ws;
+    T *alpha = cab + (size_t)n1 * n2;
+    T *cxyz = alpha + 3 * (size_t)(la_max + 1) * (lb_max + 1) * (lp + 1);
+    T *cijk = cxyz + ncoset(lp);
+    for (int e = lane; e < n1 * n2; e += 32)
+      cab[e] = T(0);
+    __syncwarp();
+    // P_ab -> C_ab
+    const CabW<T> w{cab, n1};
+    const double *pab = a.pab_cart + sb.cart_offset;
+    const int na = ncoset(d.la_max) - ncoset(d.la_min - 1);
+    const int nb = ncoset(d.lb_max) - ncoset(d.lb_min - 1);
+    for (int e = lane; e < na * nb; e += 32) {
+      const int ia = ncoset(d.la_min - 1) + e % na, ib = ncoset(d.lb_min - 1) + e / na;
+      // orbital of Cartesian index ia
+      int l = 0;
+      while (ncoset(l) <= ia)
+        l++;
+      const Orb oa = orb_of(l, ia - ncoset(l - 1));
+      int m = 0;
+      while (ncoset(m) <= ib)
+        m++;
+      const Orb ob = orb_of(m, ib - ncoset(m - 1));
+      const T p = (T)pab[(size_t)(d.o2 + ib) * sb.ncoa + d.o1 + ia];
+      prep_one<T>(a.func, oa, ob, (T)d.zeta, (T)d.zetb, p, w);
+    }
+    __syncwarp();
+    const double *ra = a.atom_pos + 3 * d.iatom;
+    double rb[3];
+    for (int i = 0; i < 3; i++)
+      rb[i] = ra[i] + d.rab[i];
+    fill_alpha<T>(alpha, la_max, lb_max, lp, ra, rb, d.rp, lane);
+    const double pref = d.prefexp * ((d.iatom == d.jatom) ? 1.0 : 2.0);
+    const int nco = ncoset(lp);
+    const bool general = d.flags & TF_GENERAL;
+    for (int e = lane; e < nco; e += 32) {
+      int pz, py, px;
+      decode_cidx(e, lp, pz, py, px);
+      const T v = cab_cxyz_term<T>(cab, n1, alpha, la_max, lb_max, lp, px, py, pz) * (T)pref;
+      if (general) {
+        cxyz[e] = v;
+        cijk[e] = T(0);
+      } else {
+        out[a.coef_off[t] + e] = v;
+      }
+    }
+    if (general) {
+      __syncwarp();
+      const double *h = a.levels->lv[d.level].dh;
+      for (int e = lane; e < nco; e += 32) {
+        int lz, ly, lx;
+        decode_cidx(e, lp, lz, ly, lx);
+        cxyz_cijk_term<T>(true, h, lp, lx, ly, lz, cxyz[e], cijk, nullptr);
+      }
+      __syncwarp();
+      for (int e = lane; e < nco; e += 32)
+        out[a.coef_off[t] + e] = cijk[e];
+    }
+    __syncwarp();
+  }
+}
+
+// ------------------------------------------------------------------------
+// post: integrated C_xyz -> C_ab -> hab / forces / virial (one warp per task)
+// ------------------------------------------------------------------------
+template <typename T> struct VabCtx {
+  const T *c;
+  int m1;
+  T za, zb;
+  T rab[3];
+  __device__ __forceinline__ T g(Orb a, Orb b) const { return c[oidx(b) * m1 + oidx(a)]; }
+};
+
+enum { V_HAB, V_FA, V_FB, V_VA, V_VB };
+
+template <typename T>
+__device__ T vab_plain(const VabCtx<T> &x, int kind, int i, int j, Orb a, Orb b) {
+  switch (kind) {
+  case V_HAB:
+    return x.g(a, b);
+  case V_FA:
+    return T(2) * x.za * x.g(up(i, a), b) - T(a.l[i]) * x.g(dn(i, a), b);
+  case V_FB:
+    return T(2) * x.zb * (x.g(up(i, a), b) - x.rab[i] * x.g(a, b)) - T(b.l[i]) * x.g(a, dn(i, b));
+  case V_VA:
+    return T(2) * x.za * x.g(up(i, up(j, a)), b) - T(a.l[j]) * x.g(up(i, dn(j, a)), b);
+  default:
+    return T(2) * x.zb *
+               (x.g(up(i, up(j, a)), b) - x.g(up(i, a), b) * x.rab[j] -
+                x.g(up(j, a), b) * x.rab[i] + x.g(a, b) * x.rab[j] * x.rab[i]) -
+           T(b.l[j]) * x.g(a, up(i, dn(j, b)));
+  }
+}
+
+template <typename T>
+__device__ T vab(const VabCtx<T> &x, bool tau, int kind, int i, int j, Orb a, Orb b) {
+  if (!tau)
+    return vab_plain(x, kind, i, j, a, b);
+  T s = T(0);
+  for (int k = 0; k < 3; k++) {
+    s += T(0.5) * T(a.l[k] * b.l[k]) * vab_plain(x, kind, i, j, dn(k, a), dn(k, b));
+    s -= x.za * T(b.l[k]) * vab_plain(x, kind, i, j, up(k, a), dn(k, b));
+    s -= T(a.l[k]) * x.zb * vab_plain(x, kind, i, j, dn(k, a), up(k, b));
+    s += T(2) * x.za * x.zb * vab_plain(x, kind, i, j, up(k, a), up(k, b));
+  }
+  return s;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) post_kernel(PostArgs a, int words_per_warp) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ double vir_cta[9];
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  T *ws = (T *)smem + (size_t)(threadIdx.x >> 5) * words_per_warp;
+  if (threadIdx.x < 9)
+    vir_cta[threadIdx.x] = 0.0;
+  __syncthreads();
+  for (int t = gw; t < a.ntasks; t += nwarps) {
+    const TaskDesc d = a.tasks[t];
+    if (d.flags & TF_SKIP)
+      continue;
+    const SubblockDesc sb = a.subs[d.subblock];
+    const int la_max = d.la_max + a.d.la_max, lb_max = d.lb_max + a.d.lb_max;
+    const int lp = la_max + lb_max;
+    const int m1 = ncoset(la_max), m2 = ncoset(lb_max);
+    T *cab = ws;
+    T *alpha = cab + (size_t)m1 * m2;
+    T *cxyz = alpha + 3 * (size_t)(la_max + 1) * (lb_max + 1) * (lp + 1);
+    T *cijk = cxyz + ncoset(lp);
+    const int nco = ncoset(lp);
+    const double *src = a.coef + a.coef_off[t];
+    const bool general = d.flags & TF_GENERAL;
+    for (int e = lane; e < nco; e += 32) {
+      if (general)
+        cijk[e] = (T)src[e];
+      else
+        cxyz[e] = (T)src[e];
+    }
+    __syncwarp();
+    if (general) {
+      const double *h = a.levels->lv[d.level].dh;
+      for (int e = lane; e < nco; e += 32) {
+        int lz, ly, lx;
+        decode_cidx(e, lp, lz, ly, lx);
+        cxyz[e] = cxyz_cijk_term<T>(false, h, lp, lx, ly, lz, T(0), nullptr, cijk);
+      }
+      __syncwarp();
+    }
+    const double *ra = a.atom_pos + 3 * d.iatom;
+    double rb[3];
+    for (int i = 0; i < 3; i++)
+      rb[i] = ra[i] + d.rab[i];
+    fill_alpha<T>(alpha, la_max, lb_max, lp, ra, rb, d.rp, lane);
+    const T pref = (T)d.prefexp;
+    for (int e = lane; e < m1 * m2; e += 32) {
+      const int ia = e % m1, ib = e / m1;
+      int l = 0;
+      while (ncoset(l) <= ia)
+        l++;
+      int m = 0;
+      while (ncoset(m) <= ib)
+        m++;
+      const Orb oa = orb_of(l, ia - ncoset(l - 1)), ob = orb_of(m, ib - ncoset(m - 1));
+      cab[e] = cxyz_cab_term<T>(cxyz, alpha, la_max, lb_max, lp, oa, ob) * pref;
+    }
+    __syncwarp();
+    VabCtx<T> x{cab, m1, (T)d.zeta, (T)d.zetb, {(T)d.rab[0], (T)d.rab[1], (T)d.rab[2]}};
+    const bool tau = a.compute_tau;
+    const int na = ncoset(d.la_max) - ncoset(d.la_min - 1);
+    const int nb = ncoset(d.lb_max) - ncoset(d.lb_min - 1);
+    double f[6] = {0, 0, 0, 0, 0, 0}, v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const double *pab = a.pab_cart ? a.pab_cart + sb.cart_offset : nullptr;
+    double *hab = a.hab_cart + sb.cart_offset;
+    for (int e = lane; e < na * nb; e += 32) {
+      const int ia = ncoset(d.la_min - 1) + e % na, ib = ncoset(d.lb_min - 1) + e / na;
+      int l = 0;
+      while (ncoset(l) <= ia)
+        l++;
+      int m = 0;
+      while (ncoset(m) <= ib)
+        m++;
+      const Orb oa = orb_of(l, ia - ncoset(l - 1)), ob = orb_of(m, ib - ncoset(m - 1));
+      const size_t el = (size_t)(d.o2 + ib) * sb.ncoa + d.o1 + ia;
+      atomicAdd(&hab[el], (double)vab<T>(x, tau, V_HAB, 0, 0, oa, ob));
+      if (a.forces || a.virial) {
+        const double p = pab[el];
+        if (a.forces)
+          for (int i = 0; i < 3; i++) {
+            f[i] += p * (double)vab<T>(x, tau, V_FA, i, 0, oa, ob);
+            f[3 + i] += p * (double)vab<T>(x, tau, V_FB, i, 0, oa, ob);
+          }
+        if (a.virial)
+          for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++)
+              v[i * 3 + j] += p * ((double)vab<T>(x, tau, V_VA, i, j, oa, ob) +
+                                   (double)vab<T>(x, tau, V_VB, i, j, oa, ob));
+      }
+    }
+    const double scale = (d.iatom == d.jatom) ? 1.0 : 2.0;
+    if (a.forces) {
+      for (int i = 0; i < 6; i++) {
+        double s = f[i];
+        for (int o = 16; o > 0; o >>= 1)
+          s += __shfl_xor_sync(FULL, s, o);
+        f[i] = s;
+      }
+      if (lane == 0)
+        for (int i = 0; i < 3; i++) {
+          atomicAdd(&a.forces[3 * d.iatom + i], scale * f[i]);
+          atomicAdd(&a.forces[3 * d.jatom + i], scale * f[3 + i]);
+        }
+    }
+    if (a.virial) {
+      for (int i = 0; i < 9; i++) {
+        double s = v[i];
+        for (int o = 16; o > 0; o >>= 1)
+          s += __shfl_xor_sync(FULL, s, o);
+        v[i] = s;
+      }
+      if (lane == 0)
+        for (int i = 0; i < 9; i++)
+          atomicAdd(&vir_cta[i], scale * v[i]);
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  if (a.virial && threadIdx.x < 9)
+    atomicAdd(&a.virial[threadIdx.x], vir_cta[threadIdx.x]);
+}
+
+// ------------------------------------------------------------------------
+// decontract / contract: one warp per subblock, FP64
+// ------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) decontract_kernel(ContractArgs a, int words_per_warp) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  double *work = (double *)smem + (size_t)(threadIdx.x >> 5) * words_per_warp;
+  for (int s = gw; s < a.nsubs; s += nwarps) {
+    const SubblockDesc sb = a.subs[s];
+    const double *blk = a.blocks + sb.block_offset;
+    double *out = a.cart + sb.cart_offset;
+    auto P = [&](int sbi, int sai) {
+      return sb.transpose ? blk[(size_t)(sb.sgfb + sbi) * sb.nsgfa + sb.sgfa + sai]
+                          : blk[(size_t)(sb.sgfa + sai) * sb.nsgfb + sb.sgfb + sbi];
+    };
+    if (sb.identity) {
+      for (int e = lane; e < sb.ncoa * sb.ncob; e += 32)
+        out[e] = P(e / sb.ncoa, e % sb.ncoa);
+    } else {
+      // work[sb][ca] = sum_sa P[sb][sa] sphi_a[sa][ca]
+      for (int e = lane; e < sb.nsgf_setb * sb.ncoa; e += 32) {
+        const int r = e / sb.ncoa, ca = e % sb.ncoa;
+        double acc = 0.0;
+        for (int sa = 0; sa < sb.nsgf_seta; sa++)
+          acc += P(r, sa) * a.sphi[sb.sphia + (size_t)sa * sb.maxcoa + ca];
+        work[e] = acc;
+      }
+      __syncwarp();
+      for (int e = lane; e < sb.ncob * sb.ncoa; e += 32) {
+        const int cb = e / sb.ncoa, ca = e % sb.ncoa;
+        double acc = 0.0;
+        for (int r = 0; r < sb.nsgf_setb; r++)
+          acc += a.sphi[sb.sphib + (size_t)r * sb.maxcob + cb] * work[r * sb.ncoa + ca];
+        out[e] = acc;
+      }
+      __syncwarp();
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128) contract_hab_kernel(ContractArgs a, int words_per_warp) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  double *work = (double *)smem + (size_t)(threadIdx.x >> 5) * words_per_warp;
+  for (int s = gw; s < a.nsubs; s += nwarps) {
+    const SubblockDesc sb = a.subs[s];
+    double *blk = a.blocks_out + sb.block_offset;
+    const double *hab = a.cart + sb.cart_offset;
+    auto H = [&](int sbi, int sai) -> double & {
+      return sb.transpose ? blk[(size_t)(sb.sgfb + sbi) * sb.nsgfa + sb.sgfa + sai]
+                          : blk[(size_t)(sb.sgfa + sai) * sb.nsgfb + sb.sgfb + sbi];
+    };
+    if (sb.identity) {
+      for (int e = lane; e < sb.ncoa * sb.ncob; e += 32)
+        H(e / sb.ncoa, e % sb.ncoa) += hab[e];
+    } else {
+      // work[sb][ca] = sum_cb sphi_b[sb][cb] hab[cb][ca]
+      for (int e = lane; e < sb.nsgf_setb * sb.ncoa; e += 32) {
+        const int r = e / sb.ncoa, ca = e % sb.ncoa;
+        double acc = 0.0;
+        for (int cb = 0; cb < sb.ncob; cb++)
+          acc += a.sphi[sb.sphib + (size_t)r * sb.maxcob + cb] * hab[(size_t)cb * sb.ncoa + ca];
+        work[e] = acc;
+      }
+      __syncwarp();
+      for (int e = lane; e < sb.nsgf_setb * sb.nsgf_seta; e += 32) {
+        const int r = e / sb.nsgf_seta, sa = e % sb.nsgf_seta;
+        double acc = 0.0;
+        for (int ca = 0; ca < sb.ncoa; ca++)
+          acc += work[r * sb.ncoa + ca] * a.sphi[sb.sphia + (size_t)sa * sb.maxcoa + ca];
+        H(r, sa) += acc;
+      }
+      __syncwarp();
+    }
+  }
+}
+
+int grid_size_for(int nwarps_needed) {
+  int nb = (nwarps_needed + 3) / 4;
+  if (nb > 152 * 32)
+    nb = 152 * 32;
+  return nb < 1 ? 1 : nb;
+}
+
+} // namespace
+
+void launch_decontract(const ContractArgs &a, cudaStream_t s) {
+  if (a.nsubs == 0)
+    return;
+  const size_t smem = 4 * sizeof(double) * (size_t)a.words;
+  cudaFuncSetAttribute(decontract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  decontract_kernel<<<grid_size_for(a.nsubs), 128, smem, s>>>(a, a.words);
+  count_launch();
+}
+
+void launch_contract_hab(const ContractArgs &a, cudaStream_t s) {
+  if (a.nsubs == 0)
+    return;
+  const size_t smem = 4 * sizeof(double) * (size_t)a.words;
+  cudaFuncSetAttribute(contract_hab_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  contract_hab_kernel<<<grid_size_for(a.nsubs), 128, smem, s>>>(a, a.words);
+  count_launch();
+}
+
+void launch_coefficients(const CoefArgs &a, bool fp32, int words_per_warp, cudaStream_t s) {
+  if (a.ntasks == 0)
+    return;
+  const size_t smem = 4 * (size_t)words_per_warp * (fp32 ? 4 : 8);
+  if (fp32) {
+    cudaFuncSetAttribute(coefficients_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    coefficients_kernel<float><<<grid_size_for(a.ntasks), 128, smem, s>>>(a, words_per_warp);
+  } else {
+    cudaFuncSetAttribute(coefficients_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    coefficients_kernel<double><<<grid_size_for(a.ntasks), 128, smem, s>>>(a, words_per_warp);
+  }
+  count_launch();
+}
+
+void launch_post(const PostArgs &a, bool fp32, int words_per_warp, cudaStream_t s) {
+  if (a.ntasks == 0)
+    return;
+  const size_t smem = 4 * (size_t)words_per_warp * (fp32 ? 4 : 8);
+  if (fp32) {
+    cudaFuncSetAttribute(post_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    post_kernel<float><<<grid_size_for(a.ntasks), 128, smem, s>>>(a, words_per_warp);
+  } else {
+    cudaFuncSetAttribute(post_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    post_kernel<double><<<grid_size_for(a.ntasks), 128, smem, s>>>(a, words_per_warp);
+  }
+  count_launch();
+}
+
+size_t coef_words(int la, int lb) {
+  const int lp = la + lb;
+  return CoefSmem<double>::words(ncoset(la), ncoset(lb), la, lb, lp);
+}
+
+} // namespace gb300

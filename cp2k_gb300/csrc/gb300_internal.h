@@ -1,0 +1,232 @@
+// Internal definitions shared by the GB300 grid backend's translation units.
+//
+// Data layout in HBM (one task list):
+//   TaskDesc[ntasks]      geometry + indices of every task, sorted by
+//                         (block, iset, jset, level) so the per-subblock
+//                         kernels walk contiguous runs; 176 B per task.
+//   SubblockDesc[nsub]    one per (block, iset, jset): offsets into the
+//                         spherical pab/hab buffer and the Cartesian scratch.
+//   sphere tables         int16 row bounds per (level, discretised radius),
+//                         built on the host with the reference's FP64
+//                         expressions (src/grid/ref/grid_ref_collint.h:
+//                         139-151, 44-52, 237-245).
+//   queues                per (path, lp bucket) the task order taken by the
+//                         persistent grid kernels.
+//   coefficients          per task the C_xyz (ortho) or C_ijk (general)
+//                         polynomial, compact: lz outer, ly, lx inner.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#define GB300_MAX_LEVELS 8
+#define GB300_LMAX 8    // largest l of a set this backend accepts
+#define GB300_LP_MAX 16 // la + lb after every angular-momentum shift
+
+namespace gb300 {
+
+enum TaskFlags : uint8_t {
+  TF_SKIP = 1,    // 2*radius < dh_max: maps onto no grid point
+  TF_GENERAL = 2, // non-orthorhombic cell or border_mask != 0
+};
+
+struct __align__(16) TaskDesc {
+  double rp[3];       // Gaussian product centre
+  double zetp;        // zeta + zetb
+  double zeta, zetb;  //
+  double prefexp;     // exp(-zeta*zetb/zetp*|rab|^2)  (rscale applied later)
+  double radius;      //
+  double roff[3];     // ortho: rp - centre*dh ; general: gp = dh_inv^T rp
+  double rab[3];      //
+  int center[3];      // ortho: cube centre ; general: index_min
+  int imax[3];        // general: index_max
+  int level;          // 0-based
+  int sphere;         // ortho: sphere-table index
+  int subblock;       // SubblockDesc index
+  int iatom, jatom;   // 0-based
+  int orig;           // position in the caller's list
+  int16_t o1, o2;     // first Cartesian index of ipgf / jpgf in the subblock
+  int8_t la_max, la_min, lb_max, lb_min;
+  uint8_t flags;
+  uint8_t border_mask;
+  uint8_t pad_[6];
+};
+static_assert(sizeof(TaskDesc) == 176, "TaskDesc layout");
+
+struct SubblockDesc {
+  int block_offset;  // spherical block in pab/hab buffers
+  int cart_offset;   // Cartesian pab/hab scratch
+  int ncoa, ncob;    // Cartesian sizes (npgf * ncoset(lmax))
+  int nsgf_seta, nsgf_setb;
+  int sgfa, sgfb;    // first spherical function of the set (0-based)
+  int nsgfa, nsgfb;  // spherical size of the whole atom basis
+  int maxcoa, maxcob;
+  int sphia, sphib;  // offsets of sphi rows sgfa / sgfb in the device sphi
+  int transpose;     // iatom <= jatom: block stored [sgfb][sgfa]
+  int identity;      // both contractions are identities (copy instead of gemm)
+  int iatom, jatom;
+  int first_task, ntasks;
+};
+
+struct SphereHdr {
+  int lb[3];
+  int cmax;
+  int off; // into the int16 table: [K] jstart, [K] row offsets, istart rows
+};
+
+struct LevelDesc {
+  int npts_global[3];
+  int npts_local[3];
+  int shift[3];
+  int border_width[3];
+  double dh[9];
+  double dh_inv[9];
+  double dh_max;
+};
+
+struct LevelSet {
+  int nlevels;
+  LevelDesc lv[GB300_MAX_LEVELS];
+};
+
+// l-range changes of the collocated / integrated C_ab relative to the basis
+struct LDiffs {
+  int la_max, la_min, lb_max, lb_min;
+};
+
+__host__ __device__ inline int ncoset(int l) {
+  return l < 0 ? 0 : (l + 1) * (l + 2) * (l + 3) / 6;
+}
+__host__ __device__ inline int coset(int lx, int ly, int lz) {
+  const int l = lx + ly + lz;
+  return l == 0 ? 0 : ncoset(l - 1) + ((l - lx) * (l - lx + 1)) / 2 + lz;
+}
+// number of (a, b) with a + b <= m
+__host__ __device__ inline int ntri(int m) { return m < 0 ? 0 : (m + 1) * (m + 2) / 2; }
+// compact index of x^lx y^ly z^lz in a polynomial of degree <= lp
+__host__ __device__ inline int cidx(int lz, int ly, int lx, int lp) {
+  const int m = lp - lz;
+  return ncoset(lp) - ncoset(m) + ly * (m + 1) - (ly * (ly - 1)) / 2 + lx;
+}
+__host__ __device__ inline int imod(int a, int m) { return ((a % m) + m) % m; }
+// inverse of cidx
+__host__ __device__ inline void decode_cidx(int e, int lp, int &lz, int &ly, int &lx) {
+  lz = 0;
+  int rem = e;
+  while (rem >= ntri(lp - lz)) {
+    rem -= ntri(lp - lz);
+    lz++;
+  }
+  const int m = lp - lz;
+  ly = 0;
+  while (rem > m - ly) {
+    rem -= m - ly + 1;
+    ly++;
+  }
+  lx = rem;
+}
+
+// -------------------------------------------------------------------------
+// kernel entry points (launch wrappers), implemented in the .cu files
+// -------------------------------------------------------------------------
+struct CoefArgs {
+  const TaskDesc *tasks;
+  const SubblockDesc *subs;
+  const int *coef_off;  // per task offset into the coefficient buffer
+  const double *atom_pos;
+  const double *pab_cart; // Cartesian pab scratch (FP64)
+  void *coef;             // T*
+  int ntasks;
+  int func;
+  LDiffs d;
+  const LevelSet *levels; // device copy
+};
+
+struct GridArgs {
+  const TaskDesc *tasks;
+  const int *queue;
+  int nqueue;
+  int *counter;           // work counter, zeroed before launch
+  const int *coef_off;
+  const void *coef;       // T* (collocate) ; double* out (integrate)
+  void *coef_out;
+  const SphereHdr *sph;
+  const int16_t *sph_tab;
+  double *grids[GB300_MAX_LEVELS];         // collocate targets
+  const void *grids_in[GB300_MAX_LEVELS];  // integrate sources (T*)
+  LevelSet levels;
+  LDiffs d;
+  int nwarps_total;
+  long long *task_cycles; // optional per-task timings (clock64)
+  int *error;             // device error word
+};
+
+struct PostArgs {
+  const TaskDesc *tasks;
+  const SubblockDesc *subs;
+  const int *coef_off;
+  const double *coef;     // integrated C_xyz / C_ijk (FP64)
+  const double *pab_cart; // for forces / virial
+  double *hab_cart;       // accumulated Cartesian hab scratch
+  const double *atom_pos;
+  double *forces;         // [natoms][3] or null
+  double *virial;         // [9] or null
+  int ntasks;
+  int compute_tau;
+  LDiffs d;
+  const LevelSet *levels;
+};
+
+struct ContractArgs {
+  const SubblockDesc *subs;
+  int nsubs;
+  const double *sphi;
+  const double *blocks; // spherical pab (decontract) ; hab out (contract)
+  double *blocks_out;
+  double *cart;         // Cartesian scratch
+  int words;            // per-warp shared-memory doubles (largest work array)
+};
+size_t coef_words(int la, int lb);
+
+void launch_decontract(const ContractArgs &a, cudaStream_t s);
+void launch_contract_hab(const ContractArgs &a, cudaStream_t s);
+void launch_coefficients(const CoefArgs &a, bool fp32, int max_smem_words,
+                         cudaStream_t s);
+// `extent` is the largest cube width (2*cmax+2) of the queue for the
+// orthorhombic kernels and the largest j-range of the box for the general ones;
+// it sizes the per-warp shared memory (4 warps per CTA).
+void launch_collocate(const GridArgs &a, bool fp32, bool general, int bucket,
+                      int extent, int nblocks, cudaStream_t s);
+void launch_integrate(const GridArgs &a, bool fp32, bool general, int bucket,
+                      int extent, int nblocks, cudaStream_t s);
+void launch_collocate_general_impl(const GridArgs &a, bool fp32, int lpb,
+                                   int njmax, int nblocks, cudaStream_t s);
+void launch_integrate_general_impl(const GridArgs &a, bool fp32, int lpb,
+                                   int njmax, int nblocks, cudaStream_t s);
+size_t ortho_smem_per_warp(bool fp32, int bucket, int wmax);
+size_t general_smem_per_warp(bool fp32, int bucket, int njmax);
+constexpr int kWarpsPerCta = 4;
+void launch_post(const PostArgs &a, bool fp32, int max_smem_words,
+                 cudaStream_t s);
+void launch_grid_to_fp32(const double *src, float *dst, size_t n,
+                         cudaStream_t s);
+
+// lp bucket limits of the templated grid kernels
+constexpr int kNumBuckets = 4;
+constexpr int kBucketLp[kNumBuckets] = {4, 6, 9, 16};
+inline int bucket_of(int lp) {
+  for (int b = 0; b < kNumBuckets; b++)
+    if (lp <= kBucketLp[b])
+      return b;
+  return -1;
+}
+
+// counts launches for grid_gb300_kernel_launches()
+void count_launch(int n = 1);
+
+// persistent grid size: CTAs that fit on all SMs at once for this kernel
+int persistent_blocks(const void *kernel, int threads, size_t smem);
+
+} // namespace gb300

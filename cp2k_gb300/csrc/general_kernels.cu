@@ -1,0 +1,513 @@
+// Collocate / integrate kernels for non-orthorhombic cells and border-masked
+// tasks (CP2K's "general" path, src/grid/ref/grid_ref_collint.h:333-794).
+//
+// The polynomial lives in lattice-index coordinates (C_ijk, produced by the
+// coefficient kernel from C_xyz), the point set is the index box around the
+// sphere with per-row bounds from a quadratic in i (grid_ref_collint.h:
+// 424-463).  Those bounds are computed in FP64 with explicitly rounded
+// operations (no FMA contraction) so the visited points are exactly the
+// reference's.  Mapping onto the warp as in the orthorhombic kernels: lane <->
+// i, planes k and rows j sequential, per-point lp+1 FMAs.
+//
+// Gaussian: FP64 path uses the reference's three pair factors (Mathieu's
+// split, grid_ref_collint.h:358-367): e_ki per lane and plane, e_jk per row
+// (precomputed per plane in shared memory), e_ij by a multiplicative
+// recurrence along j.  FP32 path evaluates exp(-zetp r^2) per point from
+// cube-local Cartesian offsets.
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cmath>
+
+#include "gb300_internal.h"
+
+namespace gb300 {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+template <typename T> __device__ __forceinline__ T wsum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    v += __shfl_xor_sync(FULL, v, o);
+  return v;
+}
+
+template <typename T, int LPB> struct GenSmem {
+  static constexpr int P = LPB + 1;
+  static __host__ __device__ constexpr int red_stride() {
+    return ((P * (P + 1)) / 2 + P) | 1;
+  }
+  static __host__ __device__ size_t bytes(int nj) {
+    size_t b = sizeof(double) * ncoset(LPB) + sizeof(double) * (size_t)nj; // acc, ejk
+    b += sizeof(T) * (ncoset(LPB) + ntri(LPB));                            // coef, cij
+    b += sizeof(T) * 32 * (size_t)red_stride();                            // fold
+    b += sizeof(int2) * (size_t)nj;                                         // row bounds
+    return (b + 15) & ~size_t(15);
+  }
+};
+
+struct GenTask {
+  double gp[3];
+  int imin[3], imax[3];
+  int bnd[3][2];
+  double h[9];  // dh
+  double hh[3]; // |h0|^2, |h1|^2, |h2|^2
+  double h01, h12, h20;
+};
+
+__device__ __forceinline__ void gen_setup(const TaskDesc &d, const LevelDesc &L, GenTask &g) {
+  for (int i = 0; i < 3; i++) {
+    g.gp[i] = d.roff[i];
+    g.imin[i] = d.center[i];
+    g.imax[i] = d.imax[i];
+    g.bnd[i][0] = 0;
+    g.bnd[i][1] = L.npts_local[i] - 1;
+    if (d.border_mask & (1 << (2 * i)))
+      g.bnd[i][0] += L.border_width[i];
+    if (d.border_mask & (1 << (2 * i + 1)))
+      g.bnd[i][1] -= L.border_width[i];
+  }
+  for (int i = 0; i < 9; i++)
+    g.h[i] = L.dh[i];
+  for (int a = 0; a < 3; a++)
+    g.hh[a] = g.h[a * 3] * g.h[a * 3] + g.h[a * 3 + 1] * g.h[a * 3 + 1] +
+              g.h[a * 3 + 2] * g.h[a * 3 + 2];
+  auto dot = [&](int a, int b) {
+    return g.h[a * 3] * g.h[b * 3] + g.h[a * 3 + 1] * g.h[b * 3 + 1] + g.h[a * 3 + 2] * g.h[b * 3 + 2];
+  };
+  g.h01 = dot(0, 1);
+  g.h12 = dot(1, 2);
+  g.h20 = dot(2, 0);
+}
+
+// grid index along dir for lattice index c, or -1 when outside the bounds
+__device__ __forceinline__ int gmap(int c, int dir, const GenTask &g, const LevelDesc &L) {
+  const int v = imod(c - L.shift[dir], L.npts_global[dir]);
+  return (g.bnd[dir][0] <= v && v <= g.bnd[dir][1]) ? v : -1;
+}
+
+// Row bounds of (j, k) exactly as grid_ref_collint.h:431-463 evaluates them.
+__device__ __forceinline__ int2 row_bounds(int j, int k, const GenTask &g, double radius) {
+  double a = 0.0, b = 0.0, c = 0.0;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const double t0 = __dmul_rn(-g.gp[0], g.h[0 * 3 + i]);
+    const double t1 = __dmul_rn(__dsub_rn((double)j, g.gp[1]), g.h[1 * 3 + i]);
+    const double t2 = __dmul_rn(__dsub_rn((double)k, g.gp[2]), g.h[2 * 3 + i]);
+    const double v = __dadd_rn(__dadd_rn(t0, t1), t2);
+    a = __dadd_rn(a, __dmul_rn(g.h[i], g.h[i]));
+    b = __dadd_rn(b, __dmul_rn(__dmul_rn(2.0, v), g.h[i]));
+    c = __dadd_rn(c, __dmul_rn(v, v));
+  }
+  const double disc = __dsub_rn(__dmul_rn(b, b),
+                                __dmul_rn(__dmul_rn(4.0, a), __dsub_rn(c, __dmul_rn(radius, radius))));
+  if (!(0.0 < disc))
+    return make_int2(1, 0);
+  const double sq = __dsqrt_rn(disc);
+  const double inv2a = __ddiv_rn(1.0, __dmul_rn(2.0, a));
+  return make_int2((int)ceil(__dmul_rn(__dsub_rn(-b, sq), inv2a)),
+                   (int)floor(__dmul_rn(__dadd_rn(-b, sq), inv2a)));
+}
+
+// Per-plane preparation shared by collocate and integrate: row bounds (and
+// for FP64 the e_jk factors) for every j of the box.
+template <typename T>
+__device__ __forceinline__ void plane_rows(int k, const GenTask &g, const LevelDesc &L,
+                                           double radius, double zetp, int2 *rows,
+                                           double *ejk, int lane) {
+  const int nj = g.imax[1] - g.imin[1] + 1;
+  const double dk = (double)k - g.gp[2];
+  for (int r = lane; r < nj; r += 32) {
+    const int j = g.imin[1] + r;
+    int2 rb = make_int2(1, 0);
+    if (gmap(j, 1, g, L) >= 0)
+      rb = row_bounds(j, k, g, radius);
+    rows[r] = rb;
+    if (sizeof(T) == 8) {
+      const double dj = (double)j - g.gp[1];
+      ejk[r] = exp(-zetp * (dj * dj * g.hh[1] + 2.0 * dj * dk * g.h12));
+    }
+  }
+}
+
+template <typename T, int LPB>
+__global__ void __launch_bounds__(128) collocate_general(GridArgs a, int njmax) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int P = LPB + 1;
+  const int lane = threadIdx.x & 31;
+  unsigned char *ws = smem + (threadIdx.x >> 5) * GenSmem<T, LPB>::bytes(njmax);
+  double *ejk = (double *)ws + ncoset(LPB);
+  T *coef = (T *)(ejk + njmax);
+  T *cij = coef + ncoset(LPB);
+  T *red = cij + ntri(LPB);
+  int2 *rows = (int2 *)(((uintptr_t)(red + 32 * GenSmem<T, LPB>::red_stride()) + 7) & ~uintptr_t(7));
+  const T *coefs = (const T *)a.coef;
+
+  for (;;) {
+    int qi = 0;
+    if (lane == 0)
+      qi = atomicAdd(a.counter, 1);
+    qi = __shfl_sync(FULL, qi, 0);
+    if (qi >= a.nqueue)
+      break;
+    const int t = a.queue[qi];
+    const long long t0 = clock64();
+    const TaskDesc d = a.tasks[t];
+    const LevelDesc &L = a.levels.lv[d.level];
+    GenTask g;
+    gen_setup(d, L, g);
+    const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
+    const int nj = g.imax[1] - g.imin[1] + 1;
+    if (nj > njmax || lp > LPB) {
+      if (lane == 0)
+        atomicOr(a.error, 1);
+      continue;
+    }
+    const int nco = ncoset(lp), ntr = ntri(lp);
+    const T *csrc = coefs + a.coef_off[t];
+    for (int e = lane; e < nco; e += 32)
+      coef[e] = csrc[e];
+    double *grid = a.grids[d.level];
+    const size_t nx = L.npts_local[0], nxy = nx * L.npts_local[1];
+    const int width = g.imax[0] - g.imin[0] + 1;
+    const int SW = width <= 8 ? 8 : (width <= 16 ? 16 : 32);
+    const int G = 32 / SW, sub = lane % SW, grp = lane / SW;
+    const double zetp = d.zetp;
+    const float fj0 = (float)((double)g.imin[1] - g.gp[1]);
+
+    for (int xc = g.imin[0]; xc <= g.imax[0]; xc += SW) {
+      const int i = xc + sub;
+      const bool xin = i <= g.imax[0];
+      const int ig = xin ? gmap(i, 0, g, L) : -1;
+      const double di = (double)i - g.gp[0];
+      T px[P];
+      {
+        T p = T(1);
+#pragma unroll
+        for (int l = 0; l < P; l++) {
+          px[l] = p;
+          p *= (T)di;
+        }
+      }
+      // FP64: e_ij(i, j) = exp(-zetp (di^2 |h0|^2 + 2 di dj h0.h1)) along j
+      const double dj_first = (double)(g.imin[1] + grp) - g.gp[1];
+      const double eij0 = (sizeof(T) == 8)
+                              ? exp(-zetp * (di * di * g.hh[0] + 2.0 * di * dj_first * g.h01))
+                              : 0.0;
+      const double eij_step = (sizeof(T) == 8) ? exp(-zetp * 2.0 * di * g.h01 * G) : 0.0;
+      // FP32: cube-local Cartesian offset of the lane's i
+      float rx[3];
+#pragma unroll
+      for (int c = 0; c < 3; c++)
+        rx[c] = (float)(di * g.h[c]);
+
+      for (int k = g.imin[2]; k <= g.imax[2]; k++) {
+        const int kg = gmap(k, 2, g, L);
+        if (kg < 0)
+          continue;
+        const double dk = (double)k - g.gp[2];
+        plane_rows<T>(k, g, L, d.radius, zetp, rows, ejk, lane);
+        // C_ij = sum_kl C_ijk dk^kl
+        for (int e = lane; e < ntr; e += 32) {
+          int jl = 0, rem = e;
+          while (rem > lp - jl) {
+            rem -= lp - jl + 1;
+            jl++;
+          }
+          const int il = rem;
+          T s = 0, pk = T(1);
+          for (int kl = 0; kl <= lp - jl - il; kl++) {
+            s += coef[cidx(kl, jl, il, lp)] * pk;
+            pk *= (T)dk;
+          }
+          cij[e] = s;
+        }
+        __syncwarp();
+        T q[P];
+#pragma unroll
+        for (int jl = 0; jl < P; jl++) {
+          T s = 0;
+          if (jl <= lp) {
+            const T *row = cij + jl * (lp + 1) - (jl * (jl - 1)) / 2;
+#pragma unroll
+            for (int il = 0; il < P; il++)
+              if (il <= lp - jl)
+                s += row[il] * px[il];
+          }
+          q[jl] = s;
+        }
+        const double eki = (sizeof(T) == 8)
+                               ? exp(-zetp * (dk * dk * g.hh[2] + 2.0 * dk * di * g.h20))
+                               : 0.0;
+        float rk[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+          rk[c] = rx[c] + (float)(dk * g.h[6 + c]);
+        double eij = eij0;
+        double *gplane = grid + (size_t)kg * nxy;
+        for (int j0 = g.imin[1]; j0 <= g.imax[1]; j0 += G, eij *= eij_step) {
+          const int j = j0 + grp;
+          if (j > g.imax[1] || ig < 0)
+            continue;
+          const int2 rb = rows[j - g.imin[1]];
+          if (i < rb.x || i > rb.y)
+            continue;
+          const int jg = gmap(j, 1, g, L); // >= 0 since rb non-empty
+          const float djf = (float)(j - g.imin[1]) + fj0;
+          T gauss;
+          if (sizeof(T) == 8) {
+            gauss = (T)(eij * ejk[j - g.imin[1]] * eki);
+          } else {
+            float r2 = 0.f;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+              const float rc = fmaf(djf, (float)g.h[3 + c], rk[c]);
+              r2 = fmaf(rc, rc, r2);
+            }
+            gauss = (T)expf(-(float)zetp * r2);
+          }
+          T v = 0, pj = T(1);
+          const T djt = (sizeof(T) == 8) ? (T)((double)j - g.gp[1]) : (T)djf;
+#pragma unroll
+          for (int jl = 0; jl < P; jl++) {
+            if (jl <= lp)
+              v += q[jl] * pj;
+            pj *= djt;
+          }
+          atomicAdd(gplane + (size_t)jg * nx + ig, (double)(v * gauss));
+        }
+        __syncwarp();
+      }
+    }
+    if (a.task_cycles && lane == 0)
+      a.task_cycles[t] = clock64() - t0;
+    __syncwarp();
+  }
+}
+
+template <typename T, int LPB>
+__global__ void __launch_bounds__(128) integrate_general(GridArgs a, int njmax) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int P = LPB + 1;
+  constexpr int NKJ = (LPB + 1) * (LPB + 2) / 2;
+  const int lane = threadIdx.x & 31;
+  unsigned char *ws = smem + (threadIdx.x >> 5) * GenSmem<T, LPB>::bytes(njmax);
+  double *acc = (double *)ws;
+  double *ejk = acc + ncoset(LPB);
+  T *coef = (T *)(ejk + njmax);
+  T *cij = coef + ncoset(LPB);
+  T *red = cij + ntri(LPB);
+  int2 *rows = (int2 *)(((uintptr_t)(red + 32 * GenSmem<T, LPB>::red_stride()) + 7) & ~uintptr_t(7));
+  double *out = (double *)a.coef_out;
+
+  for (;;) {
+    int qi = 0;
+    if (lane == 0)
+      qi = atomicAdd(a.counter, 1);
+    qi = __shfl_sync(FULL, qi, 0);
+    if (qi >= a.nqueue)
+      break;
+    const int t = a.queue[qi];
+    const long long t0 = clock64();
+    const TaskDesc d = a.tasks[t];
+    const LevelDesc &L = a.levels.lv[d.level];
+    GenTask g;
+    gen_setup(d, L, g);
+    const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
+    const int nj = g.imax[1] - g.imin[1] + 1;
+    if (nj > njmax || lp > LPB) {
+      if (lane == 0)
+        atomicOr(a.error, 1);
+      continue;
+    }
+    const int nco = ncoset(lp);
+    for (int e = lane; e < nco; e += 32)
+      acc[e] = 0.0;
+    __syncwarp();
+    const T *grid = (const T *)a.grids_in[d.level];
+    const size_t nx = L.npts_local[0], nxy = nx * L.npts_local[1];
+    const int width = g.imax[0] - g.imin[0] + 1;
+    const int SW = width <= 8 ? 8 : (width <= 16 ? 16 : 32);
+    const int G = 32 / SW, sub = lane % SW, grp = lane / SW;
+    const double zetp = d.zetp;
+    const float fj0 = (float)((double)g.imin[1] - g.gp[1]);
+
+    for (int xc = g.imin[0]; xc <= g.imax[0]; xc += SW) {
+      const int i = xc + sub;
+      const bool xin = i <= g.imax[0];
+      const int ig = xin ? gmap(i, 0, g, L) : -1;
+      const double di = (double)i - g.gp[0];
+      const double dj_first = (double)(g.imin[1] + grp) - g.gp[1];
+      const double eij0 = (sizeof(T) == 8)
+                              ? exp(-zetp * (di * di * g.hh[0] + 2.0 * di * dj_first * g.h01))
+                              : 0.0;
+      const double eij_step = (sizeof(T) == 8) ? exp(-zetp * 2.0 * di * g.h01 * G) : 0.0;
+      float rx[3];
+#pragma unroll
+      for (int c = 0; c < 3; c++)
+        rx[c] = (float)(di * g.h[c]);
+      T akj[NKJ];
+#pragma unroll
+      for (int e = 0; e < NKJ; e++)
+        akj[e] = T(0);
+
+      for (int k = g.imin[2]; k <= g.imax[2]; k++) {
+        const int kg = gmap(k, 2, g, L);
+        if (kg < 0)
+          continue;
+        const double dk = (double)k - g.gp[2];
+        plane_rows<T>(k, g, L, d.radius, zetp, rows, ejk, lane);
+        __syncwarp();
+        const double eki = (sizeof(T) == 8)
+                               ? exp(-zetp * (dk * dk * g.hh[2] + 2.0 * dk * di * g.h20))
+                               : 0.0;
+        float rk[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+          rk[c] = rx[c] + (float)(dk * g.h[6 + c]);
+        T wj[P];
+#pragma unroll
+        for (int l = 0; l < P; l++)
+          wj[l] = T(0);
+        double eij = eij0;
+        const T *gplane = grid + (size_t)kg * nxy;
+        for (int j0 = g.imin[1]; j0 <= g.imax[1]; j0 += G, eij *= eij_step) {
+          const int j = j0 + grp;
+          if (j > g.imax[1] || ig < 0)
+            continue;
+          const int2 rb = rows[j - g.imin[1]];
+          if (i < rb.x || i > rb.y)
+            continue;
+          const int jg = gmap(j, 1, g, L);
+          const float djf = (float)(j - g.imin[1]) + fj0;
+          T gauss;
+          if (sizeof(T) == 8) {
+            gauss = (T)(eij * ejk[j - g.imin[1]] * eki);
+          } else {
+            float r2 = 0.f;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+              const float rc = fmaf(djf, (float)g.h[3 + c], rk[c]);
+              r2 = fmaf(rc, rc, r2);
+            }
+            gauss = (T)expf(-(float)zetp * r2);
+          }
+          const T vg = __ldg(gplane + (size_t)jg * nx + ig) * gauss;
+          const T djt = (sizeof(T) == 8) ? (T)((double)j - g.gp[1]) : (T)djf;
+          T pj = T(1);
+#pragma unroll
+          for (int jl = 0; jl < P; jl++) {
+            if (jl <= lp)
+              wj[jl] += vg * pj;
+            pj *= djt;
+          }
+        }
+        __syncwarp();
+        T pk = T(1);
+#pragma unroll
+        for (int kl = 0; kl < P; kl++) {
+          if (kl > lp)
+            break;
+#pragma unroll
+          for (int jl = 0; jl < P; jl++)
+            if (jl <= lp - kl)
+              akj[kl * P - (kl * (kl - 1)) / 2 + jl] += wj[jl] * pk;
+          pk *= (T)dk;
+        }
+      }
+      // fold i and reduce over the warp through shared memory
+      {
+        constexpr int RS = GenSmem<T, LPB>::red_stride();
+        T *rl = red + lane * RS;
+#pragma unroll
+        for (int e = 0; e < NKJ; e++)
+          rl[e] = akj[e];
+        T pi = xin ? T(1) : T(0);
+#pragma unroll
+        for (int l = 0; l < P; l++) {
+          rl[NKJ + l] = pi;
+          pi *= (T)di;
+        }
+        __syncwarp();
+        for (int e = lane; e < nco; e += 32) {
+          int kl, jl, il;
+          decode_cidx(e, lp, kl, jl, il);
+          const int kj = kl * P - (kl * (kl - 1)) / 2 + jl;
+          T s = T(0);
+#pragma unroll 8
+          for (int r = 0; r < 32; r++)
+            s += red[r * RS + kj] * red[r * RS + NKJ + il];
+          acc[e] += (double)s;
+        }
+        __syncwarp();
+      }
+    }
+    __syncwarp();
+    double *dst = out + a.coef_off[t];
+    for (int e = lane; e < nco; e += 32)
+      dst[e] = acc[e];
+    if (a.task_cycles && lane == 0)
+      a.task_cycles[t] = clock64() - t0;
+    __syncwarp();
+  }
+}
+
+template <typename T, int LPB>
+void launch_gen(const GridArgs &a, bool collocate, int njmax, int nblocks, cudaStream_t s) {
+  const size_t smem = kWarpsPerCta * GenSmem<T, LPB>::bytes(njmax);
+  if (collocate) {
+    auto k = collocate_general<T, LPB>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (nblocks <= 0)
+      nblocks = persistent_blocks((const void *)k, 32 * kWarpsPerCta, smem);
+    k<<<nblocks, 32 * kWarpsPerCta, smem, s>>>(a, njmax);
+  } else {
+    auto k = integrate_general<T, LPB>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (nblocks <= 0)
+      nblocks = persistent_blocks((const void *)k, 32 * kWarpsPerCta, smem);
+    k<<<nblocks, 32 * kWarpsPerCta, smem, s>>>(a, njmax);
+  }
+  count_launch();
+}
+
+void launch_gen_any(const GridArgs &a, bool collocate, bool fp32, int lpb, int njmax,
+                    int nblocks, cudaStream_t s) {
+  switch (lpb) {
+#define GB_CASE(LP)                                                            \
+  case LP:                                                                     \
+    if (fp32)                                                                  \
+      launch_gen<float, LP>(a, collocate, njmax, nblocks, s);                  \
+    else                                                                       \
+      launch_gen<double, LP>(a, collocate, njmax, nblocks, s);                 \
+    break;
+    GB_CASE(4) GB_CASE(6) GB_CASE(9) GB_CASE(16)
+#undef GB_CASE
+  }
+}
+
+} // namespace
+
+size_t general_smem_per_warp(bool fp32, int bucket, int njmax) {
+  const int lpb = kBucketLp[bucket];
+#define GB_CASE(LP)                                                            \
+  if (lpb == LP)                                                               \
+    return fp32 ? GenSmem<float, LP>::bytes(njmax) : GenSmem<double, LP>::bytes(njmax);
+  GB_CASE(4) GB_CASE(6) GB_CASE(9) GB_CASE(16)
+#undef GB_CASE
+  return 0;
+}
+
+void launch_collocate_general_impl(const GridArgs &a, bool fp32, int lpb, int njmax,
+                                   int nblocks, cudaStream_t s) {
+  launch_gen_any(a, true, fp32, lpb, njmax, nblocks, s);
+}
+
+void launch_integrate_general_impl(const GridArgs &a, bool fp32, int lpb, int njmax,
+                                   int nblocks, cudaStream_t s) {
+  launch_gen_any(a, false, fp32, lpb, njmax, nblocks, s);
+}
+
+} // namespace gb300

@@ -1,0 +1,306 @@
+"""Python mirror of CP2K's grid API (src/grid/grid_api.F) over the C ABI of
+libgb300grid.so (include/grid_gb300.h).
+
+The classes follow the Fortran wrappers' argument meaning:
+  * ``BasisSet``      -> grid_create_basis_set / grid_free_basis_set
+  * ``GridTaskList``  -> grid_create_task_list / grid_collocate_task_list /
+                         grid_integrate_task_list / grid_free_task_list
+with host buffers passed as CP2K's offload buffers (pinned host + device
+copies).  Device-resident variants take torch CUDA tensors and call the
+``grid_gb300_*_device_async`` entry points.  There is no CPU path: loading
+fails loudly when the CUDA library is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build
+from .tasklist import TaskListInputs
+
+GRID_FUNC_AB = 100
+GRID_FUNC_DADB = 200
+GRID_BACKEND_AUTO, GRID_BACKEND_REF, GRID_BACKEND_CPU = 10, 11, 12
+GRID_BACKEND_DGEMM, GRID_BACKEND_GPU, GRID_BACKEND_GB300 = 13, 14, 15
+FP64, MIXED = 0, 1
+SCHEDULE_SIZE, SCHEDULE_MODEL, SCHEDULE_INPUT = 0, 1, 2
+
+# every grid_func value (src/grid/common/grid_constants.h:10-46)
+GRID_FUNCS = [100, 200, 301, 302, 303, 411, 412, 413, 421, 422, 423, 431, 432, 433,
+              501, 502, 503, 601, 602, 603, 701, 702, 703, 801, 802, 803,
+              901, 902, 903, 904, 905, 906, 1001, 1002, 1003]
+
+
+class OffloadBuffer(C.Structure):
+    _fields_ = [("size", C.c_size_t), ("host_buffer", C.POINTER(C.c_double)),
+                ("device_buffer", C.POINTER(C.c_double))]
+
+
+_LIB = None
+vp = C.c_void_p
+
+
+def lib_path() -> str:
+    return build.GRID_LIB
+
+
+def lib():
+    """Load libgb300grid.so.  Raises if it has not been built."""
+    global _LIB
+    if _LIB is None:
+        path = lib_path()
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing: run cp2k_gb300.build.build_all() first")
+        L = C.CDLL(path)
+        L.offload_create_buffer.argtypes = [C.c_int, C.POINTER(C.POINTER(OffloadBuffer))]
+        L.offload_free_buffer.argtypes = [C.POINTER(OffloadBuffer)]
+        L.offload_get_buffer_host_pointer.argtypes = [C.POINTER(OffloadBuffer)]
+        L.offload_get_buffer_host_pointer.restype = C.POINTER(C.c_double)
+        L.grid_create_basis_set.argtypes = [C.c_int] * 4 + [vp] * 7 + [C.POINTER(vp)]
+        L.grid_free_basis_set.argtypes = [vp]
+        L.grid_library_init.argtypes = []
+        L.grid_library_finalize.argtypes = []
+        L.grid_library_set_config.argtypes = [C.c_int, C.c_bool, C.c_bool]
+        create_args = [C.c_bool] + [C.c_int] * 5 + [vp] * 21 + [C.POINTER(vp)]
+        L.grid_create_task_list.argtypes = create_args
+        L.grid_gb300_create_task_list.argtypes = create_args
+        L.grid_free_task_list.argtypes = [vp]
+        L.grid_gb300_free_task_list.argtypes = [vp]
+        L.grid_collocate_task_list.argtypes = [vp, C.c_int, C.c_int, vp, C.POINTER(OffloadBuffer),
+                                               C.POINTER(C.POINTER(OffloadBuffer))]
+        L.grid_integrate_task_list.argtypes = [vp, C.c_bool, C.c_int, C.c_int, vp,
+                                               C.POINTER(OffloadBuffer),
+                                               C.POINTER(C.POINTER(OffloadBuffer)),
+                                               C.POINTER(OffloadBuffer), vp, vp]
+        L.grid_gb300_collocate_task_list.argtypes = [vp, C.c_int, C.c_int, C.POINTER(OffloadBuffer),
+                                                     C.POINTER(C.POINTER(OffloadBuffer))]
+        L.grid_gb300_integrate_task_list.argtypes = [vp, C.c_bool, C.c_int, C.POINTER(OffloadBuffer),
+                                                     C.POINTER(C.POINTER(OffloadBuffer)),
+                                                     C.POINTER(OffloadBuffer), vp, vp]
+        L.grid_gb300_collocate_device_async.argtypes = [vp, C.c_int, vp, vp, vp]
+        L.grid_gb300_integrate_device_async.argtypes = [vp, C.c_bool, vp, vp, vp, vp, vp, vp]
+        L.grid_gb300_set_precision.argtypes = [vp, C.c_int]
+        L.grid_gb300_get_precision.argtypes = [vp]
+        L.grid_gb300_set_schedule.argtypes = [vp, C.c_int]
+        L.grid_gb300_task_list_info.argtypes = [vp, vp, vp, vp, vp]
+        L.grid_gb300_task_sizes.argtypes = [vp, vp, vp]
+        L.grid_gb300_last_timings.argtypes = [vp, vp]
+        L.grid_gb300_backend_handle.argtypes = [vp]
+        L.grid_gb300_backend_handle.restype = vp
+        L.grid_gb300_kernel_launches.restype = C.c_longlong
+        L.grid_gb300_last_error.restype = C.c_char_p
+        L.grid_library_init()
+        _LIB = L
+    return _LIB
+
+
+def kernel_launches() -> int:
+    return int(lib().grid_gb300_kernel_launches())
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Buffer:
+    """CP2K offload buffer: pinned host memory + device memory of n doubles."""
+
+    def __init__(self, n: int):
+        self.n = int(n)
+        self.ptr = C.POINTER(OffloadBuffer)()
+        lib().offload_create_buffer(max(self.n, 0), C.byref(self.ptr))
+
+    @property
+    def host(self) -> np.ndarray:
+        if self.n == 0:
+            return np.zeros(0)
+        return np.ctypeslib.as_array(self.ptr.contents.host_buffer, shape=(self.n,))
+
+    @property
+    def device_ptr(self) -> int:
+        return C.cast(self.ptr.contents.device_buffer, C.c_void_p).value
+
+    def free(self):
+        if self.ptr:
+            lib().offload_free_buffer(self.ptr)
+            self.ptr = C.POINTER(OffloadBuffer)()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class BasisSet:
+    def __init__(self, b):
+        self._arrays = [np.ascontiguousarray(x, np.int32) for x in
+                        (b.lmin, b.lmax, b.npgf, b.nsgf_set, b.first_sgf)]
+        self._arrays += [np.ascontiguousarray(b.sphi, np.float64),
+                         np.ascontiguousarray(b.zet, np.float64)]
+        self.h = C.c_void_p()
+        lib().grid_create_basis_set(b.nset, b.nsgf, b.maxco, b.maxpgf,
+                                    *[_p(a) for a in self._arrays], C.byref(self.h))
+
+    def free(self):
+        if self.h:
+            lib().grid_free_basis_set(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class GridTaskList:
+    """A GB300 task list for ``TaskListInputs`` (see cp2k_gb300.tasklist).
+
+    ``api="cp2k"`` goes through grid_create_task_list & co. (the CP2K surface),
+    ``api="backend"`` through grid_gb300_* (what CP2K's dispatcher binds)."""
+
+    def __init__(self, inp: TaskListInputs, precision: int = FP64,
+                 schedule: int = SCHEDULE_SIZE, api: str = "backend"):
+        L = lib()
+        self.inp = inp
+        self.api = api
+        self.basis = [BasisSet(b) for b in inp.basis_sets]
+        self._bs = (C.c_void_p * max(1, len(self.basis)))(*[b.h.value for b in self.basis])
+        i32 = lambda a: np.ascontiguousarray(a, np.int32)
+        f64 = lambda a: np.ascontiguousarray(a, np.float64)
+        self._arrays = [i32(inp.block_offsets), f64(inp.atom_positions), i32(inp.atom_kinds)]
+        lists = [i32(inp.level_list), i32(inp.iatom_list), i32(inp.jatom_list),
+                 i32(inp.iset_list), i32(inp.jset_list), i32(inp.ipgf_list), i32(inp.jpgf_list),
+                 i32(inp.border_mask_list), i32(inp.block_num_list), f64(inp.radius_list),
+                 f64(inp.rab_list)]
+        levels = [i32(inp.npts_global), i32(inp.npts_local), i32(inp.shift_local),
+                  i32(inp.border_width), f64(inp.dh), f64(inp.dh_inv)]
+        self._arrays += lists + levels
+        self.npts_local = levels[1]
+        self.h = C.c_void_p()
+        fn = L.grid_create_task_list if api == "cp2k" else L.grid_gb300_create_task_list
+        fn(bool(inp.orthorhombic), inp.ntasks, inp.nlevels, inp.natoms, inp.nkinds,
+           inp.nblocks, _p(self._arrays[0]), _p(self._arrays[1]), _p(self._arrays[2]),
+           C.cast(self._bs, C.c_void_p), *[_p(a) for a in lists], *[_p(a) for a in levels],
+           C.byref(self.h))
+        self.impl = self._impl_handle()
+        self.set_precision(precision)
+        self.set_schedule(schedule)
+        self._pab = None
+        self._hab = None
+        self._grids = None
+
+    def _impl_handle(self):
+        if self.api == "cp2k":
+            return C.c_void_p(lib().grid_gb300_backend_handle(self.h))
+        return self.h
+
+    # ------------------------------------------------------------ settings
+    def set_precision(self, precision: int):
+        lib().grid_gb300_set_precision(self.impl, int(precision))
+
+    def set_schedule(self, schedule: int):
+        lib().grid_gb300_set_schedule(self.impl, int(schedule))
+
+    def sizes(self):
+        """(grid points visited, lp) per task in input order."""
+        n = self.inp.ntasks
+        pts = np.zeros(n, np.int64)
+        lp = np.zeros(n, np.int32)
+        lib().grid_gb300_task_sizes(self.impl, _p(pts), _p(lp))
+        return pts, lp
+
+    def timings(self):
+        t = np.zeros(4)
+        lib().grid_gb300_last_timings(self.impl, _p(t))
+        return {"coef_ms": t[0], "grid_ms": t[1], "post_ms": t[2], "total_ms": t[3]}
+
+    # ------------------------------------------------------ host buffers
+    def _buffers(self):
+        if self._grids is None:
+            self._pab = Buffer(self.inp.buffer_size)
+            self._hab = Buffer(self.inp.buffer_size)
+            self._grids = [Buffer(n) for n in self.inp.grid_sizes()]
+        return self._pab, self._hab, self._grids
+
+    def collocate(self, func: int, pab_blocks: np.ndarray) -> list:
+        """grid_collocate_task_list with host buffers; returns copies of the grids."""
+        L = lib()
+        pab, _, grids = self._buffers()
+        pab.host[:] = pab_blocks
+        arr = (C.POINTER(OffloadBuffer) * len(grids))(*[g.ptr for g in grids])
+        if self.api == "cp2k":
+            L.grid_collocate_task_list(self.h, int(func), self.inp.nlevels, _p(self.npts_local),
+                                       pab.ptr, arr)
+        else:
+            L.grid_gb300_collocate_task_list(self.impl, int(func), self.inp.nlevels, pab.ptr, arr)
+        return [g.host.copy() for g in grids]
+
+    def integrate(self, grids, pab_blocks=None, compute_tau=False, forces=False, virial=False):
+        """grid_integrate_task_list with host buffers; returns (hab, forces, virial)."""
+        L = lib()
+        pab, hab, gb = self._buffers()
+        for b, g in zip(gb, grids):
+            b.host[:] = g
+        if pab_blocks is not None:
+            pab.host[:] = pab_blocks
+        arr = (C.POINTER(OffloadBuffer) * len(gb))(*[b.ptr for b in gb])
+        f = np.zeros((self.inp.natoms, 3)) if forces else None
+        v = np.zeros((3, 3)) if virial else None
+        fp = _p(f) if f is not None else None
+        vp_ = _p(v) if v is not None else None
+        pp = pab.ptr if pab_blocks is not None else None
+        if self.api == "cp2k":
+            L.grid_integrate_task_list(self.h, bool(compute_tau), self.inp.natoms,
+                                       self.inp.nlevels, _p(self.npts_local), pp, arr, hab.ptr,
+                                       fp, vp_)
+        else:
+            L.grid_gb300_integrate_task_list(self.impl, bool(compute_tau), self.inp.nlevels, pp,
+                                             arr, hab.ptr, fp, vp_)
+        return hab.host.copy(), f, v
+
+    # ---------------------------------------------------- device buffers
+    def collocate_device(self, func: int, pab_dev, grids_dev, stream=None):
+        """Enqueue collocation on device tensors (torch, float64, contiguous)."""
+        ptrs = (C.c_void_p * len(grids_dev))(*[g.data_ptr() for g in grids_dev])
+        lib().grid_gb300_collocate_device_async(self.impl, int(func), C.c_void_p(pab_dev.data_ptr()),
+                                                C.cast(ptrs, C.c_void_p), _stream(stream))
+
+    def integrate_device(self, grids_dev, hab_dev, pab_dev=None, forces_dev=None,
+                         virial_dev=None, compute_tau=False, stream=None):
+        ptrs = (C.c_void_p * len(grids_dev))(*[g.data_ptr() for g in grids_dev])
+        dp = lambda x: C.c_void_p(x.data_ptr()) if x is not None else None
+        lib().grid_gb300_integrate_device_async(
+            self.impl, bool(compute_tau), dp(pab_dev), C.cast(ptrs, C.c_void_p), dp(hab_dev),
+            dp(forces_dev), dp(virial_dev), _stream(stream))
+
+    def close(self):
+        if self.h:
+            fn = lib().grid_free_task_list if self.api == "cp2k" else lib().grid_gb300_free_task_list
+            fn(self.h)
+            self.h = C.c_void_p()
+        for b in (self._pab, self._hab):
+            if b is not None:
+                b.free()
+        for g in self._grids or []:
+            g.free()
+        self._grids = None
+        for b in self.basis:
+            b.free()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    if hasattr(stream, "cuda_stream"):
+        return C.c_void_p(stream.cuda_stream)
+    return C.c_void_p(int(stream))

@@ -1,0 +1,303 @@
+/*
+ * C ABI of the GB300 grid backend (libgb300grid.so).
+ *
+ * Two layers, both plain C (no CUDA or torch types in any signature):
+ *
+ *  1. The CP2K grid library surface, symbol for symbol, so that Quickstep's
+ *     Fortran binding (src/grid/grid_api.F) can call this library unchanged:
+ *     offload buffers, basis sets, task lists, library config.  AUTO, GPU and
+ *     the new GB300 backend value all run on this backend; REF/CPU/DGEMM are
+ *     served by CP2K's own library and are rejected here with an error.
+ *
+ *  2. The backend-level entry points grid_gb300_* with the signatures of
+ *     CP2K's per-backend functions (src/grid/gpu/grid_gpu_task_list.h:25-54),
+ *     which CP2K's dispatcher (src/grid/grid_task_list.c:93-134, 199-223,
+ *     324-350) binds from a new `case GRID_BACKEND_GB300:`.  Extensions for
+ *     device-resident buffers, precision and schedule follow them.
+ *
+ * Errors: the CP2K surface has no status codes (it aborts, see
+ * src/grid/grid_task_list.c:131-133); this library does the same on misuse
+ * after printing a message, and additionally records the message for
+ * grid_gb300_last_error().  Calls are synchronous unless named *_async.
+ */
+#ifndef GRID_GB300_H
+#define GRID_GB300_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- src/offload/offload_buffer.h:16-20 -------------------------------- */
+typedef struct {
+  size_t size;          /* bytes */
+  double *host_buffer;  /* pinned host memory */
+  double *device_buffer;
+} offload_buffer;
+
+/* Replaces offload_create_buffer (src/offload/offload_buffer.h:26). */
+void offload_create_buffer(const int length, offload_buffer **buffer);
+/* Replaces offload_free_buffer (src/offload/offload_buffer.h:32). */
+void offload_free_buffer(offload_buffer *buffer);
+/* Replaces offload_get_buffer_host_pointer (src/offload/offload_buffer.h:38). */
+double *offload_get_buffer_host_pointer(offload_buffer *buffer);
+
+/* ---- src/grid/common/grid_constants.h:10-54 ---------------------------- */
+enum grid_func {
+  GRID_FUNC_AB = 100,
+  GRID_FUNC_DADB = 200,
+  GRID_FUNC_ADBmDAB_X = 301,
+  GRID_FUNC_ADBmDAB_Y = 302,
+  GRID_FUNC_ADBmDAB_Z = 303,
+  GRID_FUNC_ARDBmDARB_XX = 411,
+  GRID_FUNC_ARDBmDARB_XY = 412,
+  GRID_FUNC_ARDBmDARB_XZ = 413,
+  GRID_FUNC_ARDBmDARB_YX = 421,
+  GRID_FUNC_ARDBmDARB_YY = 422,
+  GRID_FUNC_ARDBmDARB_YZ = 423,
+  GRID_FUNC_ARDBmDARB_ZX = 431,
+  GRID_FUNC_ARDBmDARB_ZY = 432,
+  GRID_FUNC_ARDBmDARB_ZZ = 433,
+  GRID_FUNC_DABpADB_X = 501,
+  GRID_FUNC_DABpADB_Y = 502,
+  GRID_FUNC_DABpADB_Z = 503,
+  GRID_FUNC_DX = 601,
+  GRID_FUNC_DY = 602,
+  GRID_FUNC_DZ = 603,
+  GRID_FUNC_DXDY = 701,
+  GRID_FUNC_DYDZ = 702,
+  GRID_FUNC_DZDX = 703,
+  GRID_FUNC_DXDX = 801,
+  GRID_FUNC_DYDY = 802,
+  GRID_FUNC_DZDZ = 803,
+  GRID_FUNC_DAB_X = 901,
+  GRID_FUNC_DAB_Y = 902,
+  GRID_FUNC_DAB_Z = 903,
+  GRID_FUNC_ADB_X = 904,
+  GRID_FUNC_ADB_Y = 905,
+  GRID_FUNC_ADB_Z = 906,
+  GRID_FUNC_CORE_X = 1001,
+  GRID_FUNC_CORE_Y = 1002,
+  GRID_FUNC_CORE_Z = 1003,
+};
+
+enum grid_backend {
+  GRID_BACKEND_AUTO = 10,
+  GRID_BACKEND_REF = 11,
+  GRID_BACKEND_CPU = 12,
+  GRID_BACKEND_DGEMM = 13,
+  GRID_BACKEND_GPU = 14,
+  GRID_BACKEND_GB300 = 15, /* new: this library */
+};
+
+/* ---- src/grid/common/grid_basis_set.h:14-64 ---------------------------- */
+typedef struct {
+  int nset;
+  int nsgf;
+  int maxco;
+  int maxpgf;
+  int *lmin;
+  int *lmax;
+  int *npgf;
+  int *nsgf_set;
+  int *first_sgf;
+  double *sphi; /* [nsgf][maxco] */
+  double *zet;  /* [nset][maxpgf] */
+} grid_basis_set;
+
+/* Replaces grid_create_basis_set (src/grid/common/grid_basis_set.h:52). */
+void grid_create_basis_set(const int nset, const int nsgf, const int maxco,
+                           const int maxpgf, const int *lmin, const int *lmax,
+                           const int *npgf, const int *nsgf_set,
+                           const int *first_sgf, const double *sphi,
+                           const double *zet, grid_basis_set **basis_set);
+/* Replaces grid_free_basis_set (src/grid/common/grid_basis_set.h:64). */
+void grid_free_basis_set(grid_basis_set *basis_set);
+
+/* ---- src/grid/common/grid_library.h:22-85 ------------------------------ */
+typedef struct {
+  enum grid_backend backend;
+  bool validate;
+  bool apply_cutoff;
+} grid_library_config;
+
+enum grid_library_kernel {
+  GRID_COLLOCATE_ORTHO = 0,
+  GRID_INTEGRATE_ORTHO = 1,
+  GRID_COLLOCATE_GENERAL = 2,
+  GRID_INTEGRATE_GENERAL = 3,
+};
+
+/* Replaces grid_library_init (src/grid/common/grid_library.h:25). */
+void grid_library_init(void);
+/* Replaces grid_library_finalize (src/grid/common/grid_library.h:31). */
+void grid_library_finalize(void);
+/* Replaces grid_library_set_config (src/grid/common/grid_library.h:47).
+ * validate=true is accepted and recorded; the shadow REF run it asks for is
+ * not linked into this library (no CPU path here) -- parity against REF is
+ * checked by the test-suite instead. */
+void grid_library_set_config(const enum grid_backend backend,
+                             const bool validate, const bool apply_cutoff);
+/* Replaces grid_library_get_config (src/grid/common/grid_library.h:53). */
+grid_library_config grid_library_get_config(void);
+/* Replaces grid_library_print_stats (src/grid/common/grid_library.h:59). */
+void grid_library_print_stats(const int fortran_comm,
+                              void (*print_func)(const char *, int, int),
+                              const int output_unit);
+/* Replaces grid_library_counter_add (src/grid/common/grid_library.h:81). */
+void grid_library_counter_add(const int lp, const enum grid_backend backend,
+                              const enum grid_library_kernel kernel,
+                              const int increment);
+
+/* ---- src/grid/grid_task_list.h:16-126 ---------------------------------- */
+typedef void grid_task_list;
+
+/* Replaces grid_create_task_list (src/grid/grid_task_list.h:59-72).
+ * Arrays are C row-major: atom_positions[natoms][3], rab_list[ntasks][3],
+ * npts_*[nlevels][3], dh/dh_inv[nlevels][3][3].  Task lists are 1-based. */
+void grid_create_task_list(
+    const bool orthorhombic, const int ntasks, const int nlevels,
+    const int natoms, const int nkinds, const int nblocks,
+    const int *block_offsets, const double *atom_positions,
+    const int *atom_kinds, const grid_basis_set **basis_sets,
+    const int *level_list, const int *iatom_list, const int *jatom_list,
+    const int *iset_list, const int *jset_list, const int *ipgf_list,
+    const int *jpgf_list, const int *border_mask_list,
+    const int *block_num_list, const double *radius_list,
+    const double *rab_list, const int *npts_global, const int *npts_local,
+    const int *shift_local, const int *border_width, const double *dh,
+    const double *dh_inv, grid_task_list **task_list);
+
+/* Replaces grid_free_task_list (src/grid/grid_task_list.h:78). */
+void grid_free_task_list(grid_task_list *task_list);
+
+/* Replaces grid_collocate_task_list (src/grid/grid_task_list.h:95-99).
+ * Grids are overwritten (host_buffer of each grid on return). */
+void grid_collocate_task_list(const grid_task_list *task_list,
+                              const enum grid_func func, const int nlevels,
+                              const int *npts_local,
+                              const offload_buffer *pab_blocks,
+                              offload_buffer **grids);
+
+/* Replaces grid_integrate_task_list (src/grid/grid_task_list.h:122-126).
+ * hab, forces[natoms][3] and virial[3][3] are overwritten; forces and virial
+ * may be NULL and require pab_blocks when given. */
+void grid_integrate_task_list(const grid_task_list *task_list,
+                              const bool compute_tau, const int natoms,
+                              const int nlevels, const int *npts_local,
+                              const offload_buffer *pab_blocks,
+                              const offload_buffer **grids,
+                              offload_buffer *hab_blocks, double *forces,
+                              double *virial);
+
+/* ---- backend level (src/grid/gpu/grid_gpu_task_list.h:25-54) ----------- */
+typedef void grid_gb300_task_list;
+
+/* Replaces grid_gpu_create_task_list (src/grid/gpu/grid_gpu_task_list.h:25). */
+void grid_gb300_create_task_list(
+    const bool orthorhombic, const int ntasks, const int nlevels,
+    const int natoms, const int nkinds, const int nblocks,
+    const int *block_offsets, const double *atom_positions,
+    const int *atom_kinds, const grid_basis_set **basis_sets,
+    const int *level_list, const int *iatom_list, const int *jatom_list,
+    const int *iset_list, const int *jset_list, const int *ipgf_list,
+    const int *jpgf_list, const int *border_mask_list,
+    const int *block_num_list, const double *radius_list,
+    const double *rab_list, const int *npts_global, const int *npts_local,
+    const int *shift_local, const int *border_width, const double *dh,
+    const double *dh_inv, grid_gb300_task_list **task_list);
+
+/* Replaces grid_gpu_free_task_list (src/grid/gpu/grid_gpu_task_list.h:40). */
+void grid_gb300_free_task_list(grid_gb300_task_list *task_list);
+
+/* Replaces grid_gpu_collocate_task_list (grid_gpu_task_list.h:46-49). */
+void grid_gb300_collocate_task_list(const grid_gb300_task_list *task_list,
+                                    const enum grid_func func,
+                                    const int nlevels,
+                                    const offload_buffer *pab_blocks,
+                                    offload_buffer **grids);
+
+/* Replaces grid_gpu_integrate_task_list (grid_gpu_task_list.h:50-54).
+ * forces is [natoms][3], virial [3][3]; either may be NULL. */
+void grid_gb300_integrate_task_list(const grid_gb300_task_list *task_list,
+                                    const bool compute_tau, const int nlevels,
+                                    const offload_buffer *pab_blocks,
+                                    const offload_buffer **grids,
+                                    offload_buffer *hab_blocks, double *forces,
+                                    double *virial);
+
+/* ---- extensions (no counterpart in CP2K) ------------------------------ */
+
+/* Arithmetic of the grid kernels:
+ *  GRID_GB300_FP64  -- everything in FP64 (parity 1e-12 with REF);
+ *  GRID_GB300_MIXED -- FP32 per-point polynomial x Gaussian and the C_ab <->
+ *                      C_xyz transforms; FP64 prefactors/geometry, FP64
+ *                      accumulation into the grid and into hab/forces/virial. */
+enum grid_gb300_precision { GRID_GB300_FP64 = 0, GRID_GB300_MIXED = 1 };
+
+/* Order in which the persistent kernels take tasks:
+ *  GRID_GB300_SCHEDULE_SIZE  -- descending analytic size (points x (lp+1));
+ *  GRID_GB300_SCHEDULE_MODEL -- descending cost predicted by the loaded MLP
+ *                               cost model (falls back to SIZE without one);
+ *  GRID_GB300_SCHEDULE_INPUT -- list order as given (no reordering). */
+enum grid_gb300_schedule {
+  GRID_GB300_SCHEDULE_SIZE = 0,
+  GRID_GB300_SCHEDULE_MODEL = 1,
+  GRID_GB300_SCHEDULE_INPUT = 2,
+};
+
+void grid_gb300_set_precision(const grid_gb300_task_list *task_list,
+                              int precision);
+int grid_gb300_get_precision(const grid_gb300_task_list *task_list);
+void grid_gb300_set_schedule(const grid_gb300_task_list *task_list,
+                             int schedule);
+
+/* Device-resident variants: pab/hab/grid pointers are device addresses
+ * (FP64), grids[level] laid out x-fastest as npts_local.  The work is
+ * enqueued on `stream` (a cudaStream_t passed as void*, NULL = the legacy
+ * default stream); *_async return without synchronising. */
+void grid_gb300_collocate_device_async(const grid_gb300_task_list *task_list,
+                                       int func, const double *pab_blocks,
+                                       double *const *grids, void *stream);
+void grid_gb300_integrate_device_async(const grid_gb300_task_list *task_list,
+                                       bool compute_tau,
+                                       const double *pab_blocks,
+                                       const double *const *grids,
+                                       double *hab_blocks, double *forces,
+                                       double *virial, void *stream);
+
+/* The backend-level handle behind a task list made by grid_create_task_list,
+ * for calling the grid_gb300_* extensions on it. */
+grid_gb300_task_list *grid_gb300_backend_handle(const grid_task_list *task_list);
+
+/* Number of tasks, levels, atoms and the pab/hab buffer length (doubles)
+ * recorded at creation; any pointer may be NULL. */
+void grid_gb300_task_list_info(const grid_gb300_task_list *task_list,
+                               int *ntasks, int *nlevels, int *natoms,
+                               long long *buffer_len);
+
+/* Per-task analytic sizes in the caller's task order: grid points visited
+ * and contraction order lp for collocation with func GRID_FUNC_AB. */
+void grid_gb300_task_sizes(const grid_gb300_task_list *task_list,
+                           long long *points, int *lp);
+
+/* Kernel timing of the last call on this task list (milliseconds, CUDA
+ * events on the launching stream): [0] coefficient kernels, [1] grid kernel,
+ * [2] post-processing, [3] total device time. */
+void grid_gb300_last_timings(const grid_gb300_task_list *task_list,
+                             double timings_ms[4]);
+
+/* Number of kernels this library launched on the device since load. */
+long long grid_gb300_kernel_launches(void);
+
+/* Last error message recorded by the library ("" if none). */
+const char *grid_gb300_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GRID_GB300_H */
