@@ -34,6 +34,8 @@ namespace gb300 {
 
 static std::atomic<long long> g_launches{0};
 void count_launch(int n) { g_launches += n; }
+static std::atomic<const char *> g_launch_error{nullptr};
+void launch_error(const char *msg) { g_launch_error = msg; }
 
 static std::mutex g_err_mu;
 static char g_last_error[512] = "";
@@ -759,6 +761,8 @@ static void ensure(void **p, size_t *cap, size_t bytes) {
 }
 
 static void check_device_error(TaskList *t) {
+  if (const char *m = g_launch_error.exchange(nullptr))
+    fail("%s", m);
   int err = 0;
   CK(cudaMemcpy(&err, t->d_error, sizeof(int), cudaMemcpyDeviceToHost));
   if (err)

@@ -276,9 +276,9 @@ __device__ T cxyz_cijk_term(bool forward, const double *h, int lp, int lx, int l
 }
 
 template <typename T> struct CoefSmem {
-  // cab [n2][n1], alpha, cxyz, cijk
+  // cab [n2][n1], alpha, cxyz, cijk (+ slack)
   static __host__ __device__ size_t words(int n1, int n2, int la, int lb, int lp) {
-    return (size_t)n1 * n2 + 3 * (size_t)(la + 1) * (lb + 1) * (lp + 1) + 2 * (size_t)ncoset(lp) + 4;
+    return (size_t)n1 * n2 + 3 * (size_t)(la + 1) * (lb + 1) * (lp + 1) + 2 * (size_t)ncoset(lp) + 8;
   }
 };
 
@@ -614,8 +614,8 @@ __global__ void __launch_bounds__(128) contract_hab_kernel(ContractArgs a, int w
   }
 }
 
-int grid_size_for(int nwarps_needed) {
-  int nb = (nwarps_needed + 3) / 4;
+int grid_size_for(int nwarps_needed, int warps_per_cta = 4) {
+  int nb = (nwarps_needed + warps_per_cta - 1) / warps_per_cta;
   if (nb > 152 * 32)
     nb = 152 * 32;
   return nb < 1 ? 1 : nb;
@@ -626,31 +626,43 @@ int grid_size_for(int nwarps_needed) {
 void launch_decontract(const ContractArgs &a, cudaStream_t s) {
   if (a.nsubs == 0)
     return;
-  const size_t smem = 4 * sizeof(double) * (size_t)a.words;
+  const size_t per_warp = sizeof(double) * (size_t)a.words;
+  const int nw = warps_for(per_warp);
+  if (nw < 1)
+    return launch_error("decontraction: sub-block too large for shared memory");
+  const size_t smem = nw * per_warp;
   cudaFuncSetAttribute(decontract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  decontract_kernel<<<grid_size_for(a.nsubs), 128, smem, s>>>(a, a.words);
+  decontract_kernel<<<grid_size_for(a.nsubs, nw), 32 * nw, smem, s>>>(a, a.words);
   count_launch();
 }
 
 void launch_contract_hab(const ContractArgs &a, cudaStream_t s) {
   if (a.nsubs == 0)
     return;
-  const size_t smem = 4 * sizeof(double) * (size_t)a.words;
+  const size_t per_warp = sizeof(double) * (size_t)a.words;
+  const int nw = warps_for(per_warp);
+  if (nw < 1)
+    return launch_error("contraction: sub-block too large for shared memory");
+  const size_t smem = nw * per_warp;
   cudaFuncSetAttribute(contract_hab_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  contract_hab_kernel<<<grid_size_for(a.nsubs), 128, smem, s>>>(a, a.words);
+  contract_hab_kernel<<<grid_size_for(a.nsubs, nw), 32 * nw, smem, s>>>(a, a.words);
   count_launch();
 }
 
 void launch_coefficients(const CoefArgs &a, bool fp32, int words_per_warp, cudaStream_t s) {
   if (a.ntasks == 0)
     return;
-  const size_t smem = 4 * (size_t)words_per_warp * (fp32 ? 4 : 8);
+  const size_t per_warp = (size_t)words_per_warp * (fp32 ? 4 : 8);
+  const int nw = warps_for(per_warp);
+  if (nw < 1)
+    return launch_error("coefficients: angular momenta too large for shared memory");
+  const size_t smem = nw * per_warp;
   if (fp32) {
     cudaFuncSetAttribute(coefficients_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    coefficients_kernel<float><<<grid_size_for(a.ntasks), 128, smem, s>>>(a, words_per_warp);
+    coefficients_kernel<float><<<grid_size_for(a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_warp);
   } else {
     cudaFuncSetAttribute(coefficients_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    coefficients_kernel<double><<<grid_size_for(a.ntasks), 128, smem, s>>>(a, words_per_warp);
+    coefficients_kernel<double><<<grid_size_for(a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_warp);
   }
   count_launch();
 }
@@ -658,13 +670,17 @@ void launch_coefficients(const CoefArgs &a, bool fp32, int words_per_warp, cudaS
 void launch_post(const PostArgs &a, bool fp32, int words_per_warp, cudaStream_t s) {
   if (a.ntasks == 0)
     return;
-  const size_t smem = 4 * (size_t)words_per_warp * (fp32 ? 4 : 8);
+  const size_t per_warp = (size_t)words_per_warp * (fp32 ? 4 : 8);
+  const int nw = warps_for(per_warp);
+  if (nw < 1)
+    return launch_error("coefficients: angular momenta too large for shared memory");
+  const size_t smem = nw * per_warp;
   if (fp32) {
     cudaFuncSetAttribute(post_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    post_kernel<float><<<grid_size_for(a.ntasks), 128, smem, s>>>(a, words_per_warp);
+    post_kernel<float><<<grid_size_for(a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_warp);
   } else {
     cudaFuncSetAttribute(post_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    post_kernel<double><<<grid_size_for(a.ntasks), 128, smem, s>>>(a, words_per_warp);
+    post_kernel<double><<<grid_size_for(a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_warp);
   }
   count_launch();
 }

@@ -208,6 +208,12 @@ void launch_integrate_general_impl(const GridArgs &a, bool fp32, int lpb,
 size_t ortho_smem_per_warp(bool fp32, int bucket, int wmax);
 size_t general_smem_per_warp(bool fp32, int bucket, int njmax);
 constexpr int kWarpsPerCta = 4;
+constexpr size_t kSmemBudget = 200 * 1024; // dynamic shared memory per CTA
+// warps per CTA so that per-warp regions fit the budget (0: does not fit)
+inline int warps_for(size_t per_warp) {
+  int w = (int)(kSmemBudget / (per_warp ? per_warp : 1));
+  return w > kWarpsPerCta ? kWarpsPerCta : w;
+}
 void launch_post(const PostArgs &a, bool fp32, int max_smem_words,
                  cudaStream_t s);
 void launch_grid_to_fp32(const double *src, float *dst, size_t n,
@@ -225,6 +231,9 @@ inline int bucket_of(int lp) {
 
 // counts launches for grid_gb300_kernel_launches()
 void count_launch(int n = 1);
+// records a launch-configuration error; the host call fails after the launch
+// sequence (reported like a device error)
+void launch_error(const char *msg);
 
 // persistent grid size: CTAs that fit on all SMs at once for this kernel
 int persistent_blocks(const void *kernel, int threads, size_t smem);

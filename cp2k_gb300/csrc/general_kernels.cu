@@ -44,6 +44,7 @@ template <typename T, int LPB> struct GenSmem {
     b += sizeof(T) * (ncoset(LPB) + ntri(LPB));                            // coef, cij
     b += sizeof(T) * 32 * (size_t)red_stride();                            // fold
     b += sizeof(int2) * (size_t)nj;                                         // row bounds
+    b += 32;                                                                // alignment slack
     return (b + 15) & ~size_t(15);
   }
 };
@@ -456,19 +457,23 @@ __global__ void __launch_bounds__(128) integrate_general(GridArgs a, int njmax) 
 
 template <typename T, int LPB>
 void launch_gen(const GridArgs &a, bool collocate, int njmax, int nblocks, cudaStream_t s) {
-  const size_t smem = kWarpsPerCta * GenSmem<T, LPB>::bytes(njmax);
+  const size_t per_warp = GenSmem<T, LPB>::bytes(njmax);
+  const int nw = warps_for(per_warp);
+  const size_t smem = nw * per_warp;
+  if (nw < 1)
+    return launch_error("general path: box too large for shared memory");
   if (collocate) {
     auto k = collocate_general<T, LPB>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (nblocks <= 0)
-      nblocks = persistent_blocks((const void *)k, 32 * kWarpsPerCta, smem);
-    k<<<nblocks, 32 * kWarpsPerCta, smem, s>>>(a, njmax);
+      nblocks = persistent_blocks((const void *)k, 32 * nw, smem);
+    k<<<nblocks, 32 * nw, smem, s>>>(a, njmax);
   } else {
     auto k = integrate_general<T, LPB>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (nblocks <= 0)
-      nblocks = persistent_blocks((const void *)k, 32 * kWarpsPerCta, smem);
-    k<<<nblocks, 32 * kWarpsPerCta, smem, s>>>(a, njmax);
+      nblocks = persistent_blocks((const void *)k, 32 * nw, smem);
+    k<<<nblocks, 32 * nw, smem, s>>>(a, njmax);
   }
   count_launch();
 }

@@ -59,6 +59,7 @@ template <typename T, int LPB> struct OrthoSmem {
     b += sizeof(int) * 3 * (size_t)wmax;
     b += sizeof(double) * ncoset(LPB); // integrate accumulator
     b += sizeof(T) * 32 * (size_t)red_stride(); // integrate x-fold transpose
+    b += 32;                                     // alignment slack
     return (b + 15) & ~size_t(15);
   }
 };
@@ -356,32 +357,40 @@ __global__ void __launch_bounds__(128)
 template <typename T, int LPB>
 static void launch_coll_t(const GridArgs &a, bool general, int wmax, int nblocks,
                           cudaStream_t s) {
-  const size_t smem = kWarpsPerCta * OrthoSmem<T, LPB>::bytes(wmax);
+  const size_t per_warp = OrthoSmem<T, LPB>::bytes(wmax);
+  const int nw = warps_for(per_warp);
+  const size_t smem = nw * per_warp;
   if (general) {
     launch_collocate_general_impl(a, sizeof(T) == 4, LPB, wmax, nblocks, s);
     return;
   }
+  if (nw < 1)
+    return launch_error("collocate: cube too large for shared memory");
   auto k = collocate_ortho<T, LPB>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (nblocks <= 0)
-    nblocks = persistent_blocks((const void *)k, 32 * kWarpsPerCta, smem);
-  k<<<nblocks, 32 * kWarpsPerCta, smem, s>>>(a, wmax);
+    nblocks = persistent_blocks((const void *)k, 32 * nw, smem);
+  k<<<nblocks, 32 * nw, smem, s>>>(a, wmax);
   count_launch();
 }
 
 template <typename T, int LPB>
 static void launch_int_t(const GridArgs &a, bool general, int wmax, int nblocks,
                          cudaStream_t s) {
-  const size_t smem = kWarpsPerCta * OrthoSmem<T, LPB>::bytes(wmax);
+  const size_t per_warp = OrthoSmem<T, LPB>::bytes(wmax);
+  const int nw = warps_for(per_warp);
+  const size_t smem = nw * per_warp;
   if (general) {
     launch_integrate_general_impl(a, sizeof(T) == 4, LPB, wmax, nblocks, s);
     return;
   }
+  if (nw < 1)
+    return launch_error("integrate: cube too large for shared memory");
   auto k = integrate_ortho<T, LPB>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (nblocks <= 0)
-    nblocks = persistent_blocks((const void *)k, 32 * kWarpsPerCta, smem);
-  k<<<nblocks, 32 * kWarpsPerCta, smem, s>>>(a, wmax);
+    nblocks = persistent_blocks((const void *)k, 32 * nw, smem);
+  k<<<nblocks, 32 * nw, smem, s>>>(a, wmax);
   count_launch();
 }
 
