@@ -1,0 +1,418 @@
+"""Benchmark: collocate + integrate per SCF step on one GB300, mixed vs FP64.
+
+Workload: the 512-atom water-like box (24.8 A cubic, O:H 1:2, O 3 sets up to
+l=2 and H 2 sets up to l=1, two primitives per set, exponents log-uniform in
+[0.04, 40] bohr^-2, 5 grid levels 216^3 .. 54^3, ~3.8e5 tasks), seeded
+synthetic data.  One step = grid_collocate_task_list(GRID_FUNC_AB) +
+grid_integrate_task_list (hab only), as one SCF iteration does.
+
+  value      mixed-precision ms per step, device-resident buffers, CUDA events
+             on the launching stream, L2 flushed between steps;
+  e2e        the same step through the CP2K C ABI with host offload buffers
+             (H2D pab + V grids, D2H rho grids + hab inside the timed region);
+  fp64_*     the plain FP64 path timed the same way;
+  errors     mixed vs the FP64 path on the same inputs (the FP64 path is
+             pinned to the oracle at 1e-12 by the test-suite);
+  roofline   dominant kernel (integrate) against measured peaks;
+  cpu_baseline  the oracle (FP64 C restatement of CP2K's REF backend) on the
+             host cores, on a bounded random sample of the tasks, scaled to a
+             full step by grid points.
+
+--impl reference times the reference's CPU implementation of the path (the
+oracle port, all host threads) on the same workload and prints the same
+metric.  Under torchrun every rank runs an independent replica (the path has
+no data exchange on one GPU); rank 0 prints the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "collocate+integrate ms per SCF step, mixed vs FP64, 1 GB300, stated error"
+WORKLOAD = "c2_512atoms"
+CONFIG = {
+    "workload": "512-atom water-like box, 24.8 A cubic, 5 levels 216^3..54^3, "
+                "O 3 sets l<=2 / H 2 sets l<=1, 2 primitives per set, zeta in [0.04, 40]",
+    "step": "collocate(GRID_FUNC_AB) + integrate(hab)",
+    "seed": 1,
+    "l2": "flushed (256 MiB write) between timed steps; pab buffer 468 MB > L2",
+}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        try:
+            import torch
+            if not torch.cuda.is_available():
+                backend = "gloo"
+        except Exception:
+            backend = "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if torch.cuda.is_available() and dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# --------------------------------------------------------------------------
+# CPU baseline: the oracle on a bounded sample
+# --------------------------------------------------------------------------
+def cpu_sample_time(inp, pab, V, target_s: float = 3.0, seed: int = 0):
+    """Times the oracle's collocate + integrate on a random subset of tasks and
+    scales to the whole task list by grid points visited."""
+    from cp2k_gb300.tasklist import TaskListInputs
+    from oracle import oracle as O
+
+    full = O.OracleTaskList(inp)
+    pts, _ = full.count_points(100)
+    full.close()
+    total = float(pts.sum())
+    rng = np.random.default_rng(seed)
+    keys = ("level_list", "iatom_list", "jatom_list", "iset_list", "jset_list", "ipgf_list",
+            "jpgf_list", "border_mask_list", "block_num_list", "radius_list", "rab_list")
+
+    def timed(frac):
+        sel = np.sort(rng.choice(inp.ntasks, size=max(1, int(frac * inp.ntasks)), replace=False))
+        sub = TaskListInputs(**{**inp.__dict__, **{k: getattr(inp, k)[sel] for k in keys}})
+        tl = O.OracleTaskList(sub)
+        t0 = time.perf_counter()
+        tl.collocate(100, pab)
+        tl.integrate(V)
+        dt = time.perf_counter() - t0
+        tl.close()
+        return sel, dt
+
+    # two independent samples, the second twice the size of the first, fit
+    # t = t_fixed + t_per_point * points so that per-call costs (thread-local
+    # grid reduction) are not scaled up with the points
+    frac = 0.002
+    sel, dt = timed(frac)
+    frac = min(0.5, frac * target_s / max(dt, 1e-3))
+    sel1, dt1 = timed(frac)
+    sel2, dt2 = timed(min(1.0, 2 * frac))
+    p1, p2 = float(pts[sel1].sum()), float(pts[sel2].sum())
+    per_pt = max((dt2 - dt1) / max(p2 - p1, 1.0), dt2 / max(p2, 1.0) * 0.5)
+    fixed = max(0.0, dt1 - per_pt * p1)
+    ms = (fixed + per_pt * total) * 1e3
+    sel, dt, sample_pts = sel2, dt2, p2
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return ms, threads, (f"{len(sel)} of {inp.ntasks} tasks ({sample_pts / total * 100:.2f}% of "
+                         f"grid points) in {dt:.2f} s and a half-size sample; fixed + per-point cost "
+                         f"fitted and scaled to all grid points")
+
+
+def reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    from cp2k_gb300 import build
+    from cp2k_gb300 import workload as W
+
+    build.build_workload()
+    inp = W.config(WORKLOAD)
+    pab = W.density_blocks(inp)
+    V = W.potential_grids(inp)
+    vals = []
+    for _ in range(max(1, args.warmup)):
+        cpu_sample_time(inp, pab, V)
+    for k in range(args.steps):
+        ms, threads, sample = cpu_sample_time(inp, pab, V, seed=k)
+        vals.append(ms)
+    v = float(np.mean(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "ms",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": v, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": CONFIG,
+        "cpu_baseline": {"value": v, "unit": "ms", "cores": threads, "kind": "port",
+                         "sample": sample + "; oracle = C restatement of CP2K's REF backend "
+                                            "(CP2K's own library cannot be built on this host)"},
+        "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------
+# GPU arm
+# --------------------------------------------------------------------------
+def measure_fp32_peak(torch):
+    """CUDA-core FP32 FMA peak as cuBLAS SGEMM reaches it (TF32 disabled)."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192
+    a = torch.randn(n, n, device="cuda")
+    b = torch.randn(n, n, device="cuda")
+    for _ in range(2):
+        torch.mm(a, b)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 0.0
+    for _ in range(5):
+        e0.record()
+        torch.mm(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    del a, b
+    return best
+
+
+def gpu_arm(args, world, rank, local):
+    import torch
+
+    from cp2k_gb300 import grid as G
+    from cp2k_gb300 import workload as W
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    inp = W.config(WORKLOAD)
+    pab_h = W.density_blocks(inp)
+    V_h = W.potential_grids(inp)
+    pab = torch.tensor(pab_h, device=dev)
+    V = [torch.tensor(v, device=dev) for v in V_h]
+    grids = [torch.empty(n, dtype=torch.float64, device=dev) for n in inp.grid_sizes()]
+    hab = torch.empty(inp.buffer_size, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    tl = G.GridTaskList(inp, api="cp2k")
+    stream = torch.cuda.Stream(device=dev)
+
+    def run_steps(prec, nsteps, timed):
+        tl.set_precision(prec)
+        times, kt = [], []
+        for _ in range(nsteps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            with torch.cuda.stream(stream):
+                e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+                e[0].record(stream)
+                tl.collocate_device(100, pab, grids, stream=stream)
+                tl.integrate_device(V, hab, stream=stream)
+                e[1].record(stream)
+            torch.cuda.synchronize()
+            times.append(e[0].elapsed_time(e[1]))
+            kt.append(tl.timings())
+        return times, kt
+
+    # warm-up both paths, then the timed regions
+    run_steps(G.MIXED, args.warmup, False)
+    run_steps(G.FP64, max(1, min(args.warmup, 2)), False)
+    launches0 = G.kernel_launches()
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_mixed, kt_mixed = run_steps(G.MIXED, args.steps, True)
+    launches = G.kernel_launches() - launches0
+    torch.cuda.synchronize()
+    barrier(world)
+    rho_mixed = [g.clone() for g in grids]
+    hab_mixed = hab.clone()
+    t_fp64, _ = run_steps(G.FP64, max(1, min(args.steps, 3)), True)
+    rho64 = [g.clone() for g in grids]
+    hab64 = hab.clone()
+
+    ms_mixed = max_over_ranks(float(np.mean(t_mixed)), world)
+    ms_fp64 = max_over_ranks(float(np.mean(t_fp64)), world)
+
+    # dominant kernel: integrate grid kernel of the mixed path, timed alone
+    tl.set_precision(G.MIXED)
+    with torch.cuda.stream(stream):
+        tl.collocate_device(100, pab, grids, stream=stream)
+    torch.cuda.synchronize()
+    kern = []
+    for _ in range(3):
+        flush.zero_()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            tl.integrate_device(V, hab, stream=stream)
+        torch.cuda.synchronize()
+        kern.append(tl.timings()["grid_ms"])
+    t_int_ms = float(np.median(kern))
+    with torch.cuda.stream(stream):
+        tl.collocate_device(100, pab, grids, stream=stream)
+    torch.cuda.synchronize()
+    t_coll_ms = tl.timings()["grid_ms"]
+
+    # errors of the mixed path against the FP64 path
+    dvol = [abs(float(np.linalg.det(d))) for d in inp.dh]
+    err_rel = max(float(((a - b).abs() / b.abs().clamp(min=1.0)).max()) for a, b in zip(rho_mixed, rho64))
+    err_max = max(float((a - b).abs().max()) for a, b in zip(rho_mixed, rho64)) / \
+        max(float(b.abs().max()) for b in rho64)
+    e64 = sum(float((g * v).sum()) * dv for g, v, dv in zip(rho64, V, dvol))
+    e32 = sum(float((g * v).sum()) * dv for g, v, dv in zip(rho_mixed, V, dvol))
+    err_hab = float((hab_mixed - hab64).abs().max()) / max(1.0, float(hab64.abs().max()))
+    err_e_per_atom = abs(e32 - e64) / inp.natoms
+
+    # algorithmic work of the dominant kernel
+    pts, lp = tl.sizes()
+    flops = float((2.0 * (lp + 1) * pts).sum())
+    grid_pts = float(sum(inp.grid_sizes()))
+    bytes_int = 4.0 * grid_pts + 8.0 * 0  # FP32 copy of V read once
+    peaks, peak_kind = _peaks()
+    fp32_peak = measure_fp32_peak(torch)
+    achieved_gbs = bytes_int / (t_int_ms * 1e-3) / 1e9
+    achieved_tf = flops / (t_int_ms * 1e-3) / 1e12
+
+    # e2e through the CP2K C ABI with host offload buffers
+    tl.set_precision(G.MIXED)
+    tl.collocate(100, pab_h)
+    tl.integrate(V_h)
+    torch.cuda.synchronize()
+    e2e = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        tl.collocate(100, pab_h)
+        tl.integrate(V_h)
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms = max_over_ranks(float(np.mean(e2e)), world)
+    h2d = 8 * inp.buffer_size + 8 * int(grid_pts)
+    d2h = 8 * int(grid_pts) + 8 * inp.buffer_size
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        ms, threads, sample = cpu_sample_time(inp, pab_h, V_h)
+        cpu = {"value": ms, "unit": "ms", "cores": threads, "kind": "port", "sample": sample}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": ms_mixed, "unit": "ms", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mixed,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 bulk / f64 accumulate", "data": "synthetic",
+            "config": {**CONFIG, "ntasks": inp.ntasks, "parallelism": f"replicas x{world}"},
+            "fp64_ms_per_step": ms_fp64, "speedup_vs_fp64": ms_fp64 / ms_mixed,
+            "errors_mixed_vs_fp64": {
+                "rho_max_rel_ref_measure": err_rel, "rho_max_abs_over_max_rho": err_max,
+                "energy_ha_per_atom": err_e_per_atom, "hab_max_rel": err_hab},
+            "kernel_ms": {"collocate_grid_mixed": t_coll_ms, "integrate_grid_mixed": t_int_ms},
+            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks.get("hbm_gbs"),
+                         "unit": "GB/s", "frac": achieved_gbs / peaks.get("hbm_gbs", 1.0),
+                         "traffic": None, "kernel": "integrate_ortho<float,4> (mixed)",
+                         "peak_kind": peak_kind},
+            "roofline_fp32": {"bound": "fp32_fma", "achieved": achieved_tf, "peak": fp32_peak,
+                              "unit": "TFLOP/s", "frac": achieved_tf / fp32_peak,
+                              "peak_kind": "measured cuBLAS SGEMM (TF32 off) on this GPU",
+                              "flops_per_launch": flops},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    tl.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        reference_arm(args, world, rank)
+    else:
+        gpu_arm(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1187,7 +1187,9 @@ GB300_API void grid_gb300_task_sizes(const grid_gb300_task_list *task_list, long
 
 GB300_API void grid_gb300_last_timings(const grid_gb300_task_list *task_list,
                                        double timings_ms[4]) {
-  const TaskList *t = TL(task_list);
+  TaskList *t = TL(task_list);
+  if (!t->empty)
+    read_timings(t);
   for (int i = 0; i < 4; i++)
     timings_ms[i] = t->timings[i];
 }

@@ -285,8 +285,9 @@ void grid_gb300_task_sizes(const grid_gb300_task_list *task_list,
                            long long *points, int *lp);
 
 /* Kernel timing of the last call on this task list (milliseconds, CUDA
- * events on the launching stream): [0] coefficient kernels, [1] grid kernel,
- * [2] post-processing, [3] total device time. */
+ * events on the launching stream; waits for that call to finish):
+ * [0] coefficient kernels, [1] grid kernels, [2] post-processing,
+ * [3] total device time. */
 void grid_gb300_last_timings(const grid_gb300_task_list *task_list,
                              double timings_ms[4]);
 
