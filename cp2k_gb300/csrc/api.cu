@@ -278,7 +278,8 @@ struct TaskList {
   size_t coef_cap = 0;
   double *d_coef_int = nullptr; // integrated coefficients
   size_t coef_int_cap = 0;
-  float *d_grid32[GB300_MAX_LEVELS] = {};
+  void *d_gridsplit[GB300_MAX_LEVELS] = {}; // integrate: V as float / float2
+  float *d_gridlo[GB300_MAX_LEVELS] = {};   // collocate: low words (mixed)
   double *d_forces = nullptr, *d_virial = nullptr;
   int *d_counters = nullptr; // one per queue launch
   int *d_error = nullptr;
@@ -384,9 +385,12 @@ static void free_device(TaskList *t) {
   for (void *p : ptrs)
     if (p)
       cudaFree(p);
-  for (int l = 0; l < GB300_MAX_LEVELS; l++)
-    if (t->d_grid32[l])
-      cudaFree(t->d_grid32[l]);
+  for (int l = 0; l < GB300_MAX_LEVELS; l++) {
+    if (t->d_gridsplit[l])
+      cudaFree(t->d_gridsplit[l]);
+    if (t->d_gridlo[l])
+      cudaFree(t->d_gridlo[l]);
+  }
   for (auto &kv : t->modes) {
     if (kv.second.d_coef_off)
       cudaFree(kv.second.d_coef_off);
@@ -787,19 +791,25 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
                           cudaStream_t s) {
   const LDiffs d = func_ldiffs(func);
   Mode &m = get_mode(t, d);
-  const bool fp32 = t->precision == GRID_GB300_MIXED;
-  ensure(&t->d_coef, &t->coef_cap, m.coef_total * (fp32 ? 4 : 8));
+  const int arith = t->precision;
+  ensure(&t->d_coef, &t->coef_cap, m.coef_total * (arith == ARITH_FP32 ? 4 : 8));
   CK(cudaEventRecord(t->ev[0], s));
   ContractArgs ca{t->d_subs, (int)t->subs.size(), t->d_sphi, pab, nullptr, t->d_pab_cart,
                   t->contract_words};
   launch_decontract(ca, s);
   CoefArgs co{t->d_tasks, t->d_subs, m.d_coef_off, t->d_atom_pos, t->d_pab_cart, t->d_coef,
-              t->ntasks, func, d, t->d_levels};
-  launch_coefficients(co, fp32, m.coef_words, s);
+              t->ntasks, func, d, t->d_levels, arith == ARITH_MIXED ? 1 : 0};
+  launch_coefficients(co, arith, m.coef_words, s);
   CK(cudaEventRecord(t->ev[1], s));
   for (int l = 0; l < t->nlevels; l++) {
     const int *n = &t->npts_local[3 * l];
-    CK(cudaMemsetAsync(grids[l], 0, sizeof(double) * (size_t)n[0] * n[1] * n[2], s));
+    const size_t np = (size_t)n[0] * n[1] * n[2];
+    CK(cudaMemsetAsync(grids[l], 0, sizeof(double) * np, s));
+    if (arith == ARITH_MIXED) {
+      if (!t->d_gridlo[l])
+        CK(cudaMalloc((void **)&t->d_gridlo[l], sizeof(float) * np));
+      CK(cudaMemsetAsync(t->d_gridlo[l], 0, sizeof(float) * np, s));
+    }
   }
   CK(cudaMemsetAsync(t->d_counters, 0, sizeof(int) * 64, s));
   GridArgs ga{};
@@ -808,8 +818,10 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
   ga.coef = t->d_coef;
   ga.sph = t->d_sph;
   ga.sph_tab = t->d_sph_tab;
-  for (int l = 0; l < t->nlevels; l++)
+  for (int l = 0; l < t->nlevels; l++) {
     ga.grids[l] = grids[l];
+    ga.grids_lo[l] = t->d_gridlo[l];
+  }
   ga.levels = t->levels;
   ga.d = d;
   ga.task_cycles = t->d_cycles;
@@ -823,9 +835,14 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
       ga.queue = q.d_idx;
       ga.nqueue = q.n;
       ga.counter = t->d_counters + qi++;
-      launch_collocate(ga, fp32, g == 1, b, q.extent, 0, s);
+      launch_collocate(ga, arith, g == 1, b, q.extent, 0, s);
       grid_library_counter_add(kBucketLp[b], GRID_BACKEND_GB300,
                                g ? GRID_COLLOCATE_GENERAL : GRID_COLLOCATE_ORTHO, q.n);
+    }
+  if (arith == ARITH_MIXED)
+    for (int l = 0; l < t->nlevels; l++) {
+      const int *n = &t->npts_local[3 * l];
+      launch_grid_fold_lo(grids[l], t->d_gridlo[l], (size_t)n[0] * n[1] * n[2], s);
     }
   CK(cudaGetLastError());
   CK(cudaEventRecord(t->ev[2], s));
@@ -836,17 +853,17 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
                           double *hab, double *forces, double *virial, cudaStream_t s) {
   const LDiffs d = integrate_ldiffs(forces != nullptr, virial != nullptr, tau);
   Mode &m = get_mode(t, d);
-  const bool fp32 = t->precision == GRID_GB300_MIXED;
+  const int arith = t->precision;
   const bool need_pab = forces != nullptr || virial != nullptr;
   ensure((void **)&t->d_coef_int, &t->coef_int_cap, m.coef_total * 8);
   CK(cudaEventRecord(t->ev[0], s));
-  if (fp32)
+  if (arith != ARITH_FP64)
     for (int l = 0; l < t->nlevels; l++) {
       const int *n = &t->npts_local[3 * l];
       const size_t np = (size_t)n[0] * n[1] * n[2];
-      if (!t->d_grid32[l])
-        CK(cudaMalloc((void **)&t->d_grid32[l], sizeof(float) * np));
-      launch_grid_to_fp32(grids[l], t->d_grid32[l], np, s);
+      if (!t->d_gridsplit[l])
+        CK(cudaMalloc(&t->d_gridsplit[l], sizeof(float2) * np));
+      launch_grid_split(grids[l], t->d_gridsplit[l], np, arith, s);
     }
   if (need_pab) {
     ContractArgs ca{t->d_subs, (int)t->subs.size(), t->d_sphi, pab, nullptr, t->d_pab_cart,
@@ -862,7 +879,7 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
   ga.sph = t->d_sph;
   ga.sph_tab = t->d_sph_tab;
   for (int l = 0; l < t->nlevels; l++)
-    ga.grids_in[l] = fp32 ? (const void *)t->d_grid32[l] : (const void *)grids[l];
+    ga.grids_in[l] = arith != ARITH_FP64 ? (const void *)t->d_gridsplit[l] : (const void *)grids[l];
   ga.levels = t->levels;
   ga.d = d;
   ga.task_cycles = t->d_cycles;
@@ -876,7 +893,10 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
       ga.queue = q.d_idx;
       ga.nqueue = q.n;
       ga.counter = t->d_counters + qi++;
-      launch_integrate(ga, fp32, g == 1, b, q.extent, 0, s);
+      if (g == 1 && arith == ARITH_MIXED) // the general path runs in FP64 here
+        for (int l = 0; l < t->nlevels; l++)
+          ga.grids_in[l] = grids[l];
+      launch_integrate(ga, arith, g == 1, b, q.extent, 0, s);
       grid_library_counter_add(kBucketLp[b], GRID_BACKEND_GB300,
                                g ? GRID_INTEGRATE_GENERAL : GRID_INTEGRATE_ORTHO, q.n);
     }
@@ -890,7 +910,7 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
   PostArgs pa{t->d_tasks, t->d_subs, m.d_coef_off, t->d_coef_int,
               need_pab ? t->d_pab_cart : nullptr, t->d_hab_cart, t->d_atom_pos, forces, virial,
               t->ntasks, tau ? 1 : 0, d, t->d_levels};
-  launch_post(pa, fp32, m.coef_words, s);
+  launch_post(pa, arith, m.coef_words, s);
   CK(cudaMemsetAsync(hab, 0, sizeof(double) * (size_t)t->buffer_len, s));
   ContractArgs cb{t->d_subs, (int)t->subs.size(), t->d_sphi, nullptr, hab, t->d_hab_cart,
                   t->contract_words};
@@ -1141,7 +1161,8 @@ GB300_API void grid_integrate_task_list(const grid_task_list *task_list, const b
 // extensions
 // ===========================================================================
 GB300_API void grid_gb300_set_precision(const grid_gb300_task_list *task_list, int precision) {
-  if (precision != GRID_GB300_FP64 && precision != GRID_GB300_MIXED)
+  if (precision != GRID_GB300_FP64 && precision != GRID_GB300_MIXED &&
+      precision != GRID_GB300_FP32)
     fail("unknown precision mode %d", precision);
   TL(task_list)->precision = precision;
 }

@@ -19,6 +19,7 @@
 #include <cstdio>
 
 #include "gb300_internal.h"
+#include "numeric.cuh"
 
 namespace gb300 {
 
@@ -66,6 +67,7 @@ template <typename T> struct CabW {
     if (v != T(0))
       atomicAdd(&c[oidx(b) * n1 + oidx(a)], v);
   }
+  __device__ __forceinline__ void set(Orb a, Orb b, T v) const { c[oidx(b) * n1 + oidx(a)] = v; }
 };
 
 template <typename T>
@@ -87,7 +89,7 @@ __device__ void term_dii_b(int d, T fa, Orb a, Orb b, T zb, const CabW<T> &w) {
 template <typename T>
 __device__ void prep_one(int f, Orb a, Orb b, T za, T zb, T p, const CabW<T> &w) {
   if (f == 100) {
-    w.add(a, b, p);
+    w.set(a, b, p); // each (a, b) owns its entry
   } else if (f == 200) {
     for (int i = 0; i < 3; i++) {
       w.add(dn(i, a), dn(i, b), T(0.5) * T(a.l[i] * b.l[i]) * p);
@@ -149,6 +151,8 @@ __device__ void prep_one(int f, Orb a, Orb b, T za, T zb, T p, const CabW<T> &w)
 // Binomial expansion tables alpha[dir][lxb][lxa][l]: coefficient of (x-p)^l
 // in (x-a)^lxa (x-b)^lxb  (grid_ref_collint.h:838-861)
 // ------------------------------------------------------------------------
+__constant__ float c_binom[GB300_LP_MAX + 1][GB300_LP_MAX + 1];
+
 template <typename T>
 __device__ void fill_alpha(T *alpha, int la, int lb, int lp, const double ra[3],
                            const double rb[3], const double rp[3], int lane) {
@@ -158,17 +162,16 @@ __device__ void fill_alpha(T *alpha, int la, int lb, int lp, const double ra[3],
   __syncwarp();
   for (int e = lane; e < 3 * na * nb; e += 32) {
     const int d = e / (na * nb), r = e % (na * nb), xb = r / na, xa = r % na;
-    const double pa = rp[d] - ra[d], pb = rp[d] - rb[d];
+    const T pa = (T)(rp[d] - ra[d]), pb = (T)(rp[d] - rb[d]);
     T *al = alpha + ((size_t)(d * nb + xb) * na + xa) * P;
-    double ca = 1.0, powa = 1.0;
+    T powa = T(1);
     for (int k = 0; k <= xa; k++) {
-      double cb = 1.0, powb = 1.0;
+      const T wa = (T)c_binom[xa][k] * powa;
+      T powb = T(1);
       for (int m = 0; m <= xb; m++) {
-        al[xa - k + xb - m] += (T)(ca * cb * powa * powb);
-        cb = cb * (double)(xb - m) / (double)(m + 1);
+        al[xa - k + xb - m] += wa * (T)c_binom[xb][m] * powb;
         powb *= pb;
       }
-      ca = ca * (double)(xa - k) / (double)(k + 1);
       powa *= pa;
     }
   }
@@ -285,14 +288,27 @@ template <typename T> struct CoefSmem {
 // ------------------------------------------------------------------------
 // coefficients: one warp per task
 // ------------------------------------------------------------------------
-template <typename T>
+// store of one coefficient in the grid kernels' arithmetic
+template <typename Tout, typename T>
+__device__ __forceinline__ void store_coef(void *out, size_t i, T v, bool as_fp64) {
+  if constexpr (std::is_same<Tout, dfloat>::value) {
+    if (as_fp64)
+      ((double *)out)[i] = (double)v;
+    else
+      ((dfloat *)out)[i] = df_make((double)v);
+  } else {
+    ((Tout *)out)[i] = (Tout)v;
+  }
+}
+
+template <typename T, typename Tout>
 __global__ void __launch_bounds__(128) coefficients_kernel(CoefArgs a, int words_per_warp) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   T *ws = (T *)smem + (size_t)(threadIdx.x >> 5) * words_per_warp;
-  T *out = (T *)a.coef;
+  void *out = a.coef;
   for (int t = gw; t < a.ntasks; t += nwarps) {
     const TaskDesc d = a.tasks[t];
     if (d.flags & TF_SKIP)
@@ -344,7 +360,7 @@ __global__ void __launch_bounds__(128) coefficients_kernel(CoefArgs a, int words
         cxyz[e] = v;
         cijk[e] = T(0);
       } else {
-        out[a.coef_off[t] + e] = v;
+        store_coef<Tout, T>(out, (size_t)a.coef_off[t] + e, v, false);
       }
     }
     if (general) {
@@ -357,7 +373,7 @@ __global__ void __launch_bounds__(128) coefficients_kernel(CoefArgs a, int words
       }
       __syncwarp();
       for (int e = lane; e < nco; e += 32)
-        out[a.coef_off[t] + e] = cijk[e];
+        store_coef<Tout, T>(out, (size_t)a.coef_off[t] + e, cijk[e], a.general_fp64);
     }
     __syncwarp();
   }
@@ -623,6 +639,20 @@ int grid_size_for(int nwarps_needed, int warps_per_cta = 4) {
 
 } // namespace
 
+static void upload_binomials() {
+  static bool done = false;
+  if (done)
+    return;
+  float b[GB300_LP_MAX + 1][GB300_LP_MAX + 1] = {};
+  for (int n = 0; n <= GB300_LP_MAX; n++) {
+    b[n][0] = 1.f;
+    for (int k = 1; k <= n; k++)
+      b[n][k] = b[n - 1][k - 1] + (k <= n - 1 ? b[n - 1][k] : 0.f);
+  }
+  cudaMemcpyToSymbol(c_binom, b, sizeof(b));
+  done = true;
+}
+
 void launch_decontract(const ContractArgs &a, cudaStream_t s) {
   if (a.nsubs == 0)
     return;
@@ -649,27 +679,36 @@ void launch_contract_hab(const ContractArgs &a, cudaStream_t s) {
   count_launch();
 }
 
-void launch_coefficients(const CoefArgs &a, bool fp32, int words_per_warp, cudaStream_t s) {
-  if (a.ntasks == 0)
-    return;
-  const size_t per_warp = (size_t)words_per_warp * (fp32 ? 4 : 8);
+template <typename T, typename Tout>
+static void launch_coef_t(const CoefArgs &a, int words_per_warp, cudaStream_t s) {
+  const size_t per_warp = (size_t)words_per_warp * sizeof(T);
   const int nw = warps_for(per_warp);
   if (nw < 1)
     return launch_error("coefficients: angular momenta too large for shared memory");
   const size_t smem = nw * per_warp;
-  if (fp32) {
-    cudaFuncSetAttribute(coefficients_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    coefficients_kernel<float><<<grid_size_for(a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_warp);
-  } else {
-    cudaFuncSetAttribute(coefficients_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    coefficients_kernel<double><<<grid_size_for(a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_warp);
-  }
+  auto k = coefficients_kernel<T, Tout>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k<<<grid_size_for(a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_warp);
   count_launch();
 }
 
-void launch_post(const PostArgs &a, bool fp32, int words_per_warp, cudaStream_t s) {
+void launch_coefficients(const CoefArgs &a, int arith, int words_per_warp, cudaStream_t s) {
   if (a.ntasks == 0)
     return;
+  upload_binomials();
+  if (arith == ARITH_FP32)
+    launch_coef_t<float, float>(a, words_per_warp, s);
+  else if (arith == ARITH_MIXED)
+    launch_coef_t<double, dfloat>(a, words_per_warp, s);
+  else
+    launch_coef_t<double, double>(a, words_per_warp, s);
+}
+
+void launch_post(const PostArgs &a, int arith, int words_per_warp, cudaStream_t s) {
+  const bool fp32 = arith == ARITH_FP32;
+  if (a.ntasks == 0)
+    return;
+  upload_binomials();
   const size_t per_warp = (size_t)words_per_warp * (fp32 ? 4 : 8);
   const int nw = warps_for(per_warp);
   if (nw < 1)

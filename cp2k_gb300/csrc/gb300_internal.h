@@ -27,6 +27,9 @@
 
 namespace gb300 {
 
+// arithmetic of the per-point work (values of enum grid_gb300_precision)
+enum Arith : int { ARITH_FP64 = 0, ARITH_MIXED = 1, ARITH_FP32 = 2 };
+
 enum TaskFlags : uint8_t {
   TF_SKIP = 1,    // 2*radius < dh_max: maps onto no grid point
   TF_GENERAL = 2, // non-orthorhombic cell or border_mask != 0
@@ -142,6 +145,7 @@ struct CoefArgs {
   int func;
   LDiffs d;
   const LevelSet *levels; // device copy
+  int general_fp64;       // write general-path coefficients as FP64
 };
 
 struct GridArgs {
@@ -155,7 +159,8 @@ struct GridArgs {
   const SphereHdr *sph;
   const int16_t *sph_tab;
   double *grids[GB300_MAX_LEVELS];         // collocate targets
-  const void *grids_in[GB300_MAX_LEVELS];  // integrate sources (T*)
+  float *grids_lo[GB300_MAX_LEVELS];       // collocate low words (mixed path)
+  const void *grids_in[GB300_MAX_LEVELS];  // integrate sources (per arith)
   LevelSet levels;
   LDiffs d;
   int nwarps_total;
@@ -192,21 +197,20 @@ size_t coef_words(int la, int lb);
 
 void launch_decontract(const ContractArgs &a, cudaStream_t s);
 void launch_contract_hab(const ContractArgs &a, cudaStream_t s);
-void launch_coefficients(const CoefArgs &a, bool fp32, int max_smem_words,
+void launch_coefficients(const CoefArgs &a, int arith, int max_smem_words,
                          cudaStream_t s);
 // `extent` is the largest cube width (2*cmax+2) of the queue for the
 // orthorhombic kernels and the largest j-range of the box for the general ones;
 // it sizes the per-warp shared memory (4 warps per CTA).
-void launch_collocate(const GridArgs &a, bool fp32, bool general, int bucket,
+void launch_collocate(const GridArgs &a, int arith, bool general, int bucket,
                       int extent, int nblocks, cudaStream_t s);
-void launch_integrate(const GridArgs &a, bool fp32, bool general, int bucket,
+void launch_integrate(const GridArgs &a, int arith, bool general, int bucket,
                       int extent, int nblocks, cudaStream_t s);
-void launch_collocate_general_impl(const GridArgs &a, bool fp32, int lpb,
+// general path: FP64 for ARITH_FP64 and ARITH_MIXED, FP32 for ARITH_FP32
+void launch_collocate_general_impl(const GridArgs &a, int arith, int lpb,
                                    int njmax, int nblocks, cudaStream_t s);
-void launch_integrate_general_impl(const GridArgs &a, bool fp32, int lpb,
+void launch_integrate_general_impl(const GridArgs &a, int arith, int lpb,
                                    int njmax, int nblocks, cudaStream_t s);
-size_t ortho_smem_per_warp(bool fp32, int bucket, int wmax);
-size_t general_smem_per_warp(bool fp32, int bucket, int njmax);
 constexpr int kWarpsPerCta = 4;
 constexpr size_t kSmemBudget = 200 * 1024; // dynamic shared memory per CTA
 // warps per CTA so that per-warp regions fit the budget (0: does not fit)
@@ -214,10 +218,13 @@ inline int warps_for(size_t per_warp) {
   int w = (int)(kSmemBudget / (per_warp ? per_warp : 1));
   return w > kWarpsPerCta ? kWarpsPerCta : w;
 }
-void launch_post(const PostArgs &a, bool fp32, int max_smem_words,
+void launch_post(const PostArgs &a, int arith, int max_smem_words,
                  cudaStream_t s);
-void launch_grid_to_fp32(const double *src, float *dst, size_t n,
-                         cudaStream_t s);
+// V grid -> float (ARITH_FP32) or float2 hi/lo pairs (ARITH_MIXED)
+void launch_grid_split(const double *src, void *dst, size_t n, int arith,
+                       cudaStream_t s);
+// g += (double)lo
+void launch_grid_fold_lo(double *g, const float *lo, size_t n, cudaStream_t s);
 
 // lp bucket limits of the templated grid kernels
 constexpr int kNumBuckets = 4;

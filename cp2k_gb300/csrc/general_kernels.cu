@@ -495,24 +495,14 @@ void launch_gen_any(const GridArgs &a, bool collocate, bool fp32, int lpb, int n
 
 } // namespace
 
-size_t general_smem_per_warp(bool fp32, int bucket, int njmax) {
-  const int lpb = kBucketLp[bucket];
-#define GB_CASE(LP)                                                            \
-  if (lpb == LP)                                                               \
-    return fp32 ? GenSmem<float, LP>::bytes(njmax) : GenSmem<double, LP>::bytes(njmax);
-  GB_CASE(4) GB_CASE(6) GB_CASE(9) GB_CASE(16)
-#undef GB_CASE
-  return 0;
+void launch_collocate_general_impl(const GridArgs &a, int arith, int lpb, int njmax,
+                                   int nblocks, cudaStream_t s) {
+  launch_gen_any(a, true, arith == ARITH_FP32, lpb, njmax, nblocks, s);
 }
 
-void launch_collocate_general_impl(const GridArgs &a, bool fp32, int lpb, int njmax,
+void launch_integrate_general_impl(const GridArgs &a, int arith, int lpb, int njmax,
                                    int nblocks, cudaStream_t s) {
-  launch_gen_any(a, true, fp32, lpb, njmax, nblocks, s);
-}
-
-void launch_integrate_general_impl(const GridArgs &a, bool fp32, int lpb, int njmax,
-                                   int nblocks, cudaStream_t s) {
-  launch_gen_any(a, false, fp32, lpb, njmax, nblocks, s);
+  launch_gen_any(a, false, arith == ARITH_FP32, lpb, njmax, nblocks, s);
 }
 
 } // namespace gb300

@@ -1,26 +1,30 @@
-// Persistent collocate / integrate kernels of the GB300 grid backend.
+// Persistent collocate / integrate kernels of the GB300 grid backend,
+// orthorhombic cells (CP2K: src/grid/ref/grid_ref_collint.h:30-327).
 //
 // Work unit: one task (a pair of primitive Gaussians on one grid level) per
-// warp.  Warps pull tasks from a queue (descending predicted cost) with one
-// atomic per task; no CTA-wide synchronisation.
+// warp.  Warps pull tasks from a queue ordered by decreasing predicted cost
+// with one atomic per task; there is no CTA-wide synchronisation.
 //
-// Inside a task the cube is traversed separably, as CP2K's reference loops do
-// (src/grid/ref/grid_ref_collint.h:30-327 orthorhombic, :333-794 general), but
-// mapped onto the warp: lane <-> x index of the cube (sub-warps of 8/16 lanes
-// for narrow cubes take several rows at once), planes k sequential, rows j
-// sequential.  Per plane the z factor is folded into the coefficients
-// (C_xy), per lane the x factor (q[ly]), so the per-point work is lp+1 FMAs:
-//   collocate:  rho(x,y,z) += sum_ly q[ly](x) * pol_y[ly](y)  -> FP64 red to HBM
-//   integrate:  w[ly] += V(x,y,z) * pol_y[ly](y)  (per lane), folded with z
-//               per plane and with x + a warp reduction per task.
-// The grid is touched with coalesced row segments; the collocate adds are
-// FP64 atomics executed in L2 (the FP64 accumulation of the mixed path).
+// The cube is traversed separably, mapped onto the warp: lane <-> x index of
+// the cube (sub-warps exactly as wide as the cube, so narrow cubes process
+// several rows at once), planes k and rows j sequential.  Per plane the z
+// factor is folded into the coefficients (C_xy), per lane the x factor
+// (q[ly]); the per-point work is lp+1 fused multiply-adds:
+//   collocate:  rho(x,y,z) += sum_ly q[ly](x) * pol_y[ly](y)   (FP64 red)
+//   integrate:  w[ly] += V(x,y,z) * pol_y[ly](y) per lane; folded with z per
+//               plane and with x + a shared-memory transpose per task.
+// Arithmetic type N: double (FP64 path), float (FP32 path) or dfloat (mixed
+// path: FP32 pipes, ~48-bit significands).  The grid accumulation is FP64
+// atomics in L2 for every N; dfloat adds its low words into an FP32 side grid
+// that is folded into the FP64 grid at the end.
 #include <cuda_runtime.h>
 
 #include <cmath>
 #include <cstdio>
+#include <type_traits>
 
 #include "gb300_internal.h"
+#include "numeric.cuh"
 
 namespace gb300 {
 
@@ -28,88 +32,186 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 
-template <typename T> __device__ __forceinline__ T warp_sum(T v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1)
-    v += __shfl_xor_sync(FULL, v, o);
-  return v;
+template <int LPB, typename T> constexpr int padded() {
+  return sizeof(T) == 4 ? ((LPB + 1 + 3) & ~3) : ((LPB + 1 + 1) & ~1);
 }
 
-template <typename T> struct Math;
-template <> struct Math<double> {
-  static __device__ __forceinline__ double gauss(double zetp, double x) {
-    return exp(-zetp * x * x);
-  }
-};
-template <> struct Math<float> {
-  static __device__ __forceinline__ float gauss(float zetp, float x) {
-    return expf(-zetp * x * x);
-  }
-};
-
 // Per-warp shared memory of the orthorhombic kernels.
-template <typename T, int LPB> struct OrthoSmem {
+template <typename N, int LPB> struct OrthoSmem {
+  using T = typename Num<N>::T;
   static constexpr int P = LPB + 1;
-  // per lane: [lz][ly] partial sums and pol_x, padded to an odd word count
+  static constexpr int PP = padded<LPB, T>();
   static __host__ __device__ constexpr int red_stride() {
     return ((P * (P + 1)) / 2 + P) | 1;
   }
   static __host__ __device__ size_t bytes(int wmax) {
-    size_t b = sizeof(T) * (3 * (size_t)wmax * P + ncoset(LPB) + ntri(LPB));
+    size_t b = sizeof(T) * (3 * (size_t)wmax * PP + ncoset(LPB) + ntri(LPB));
     b += sizeof(int) * 3 * (size_t)wmax;
-    b += sizeof(double) * ncoset(LPB); // integrate accumulator
+    b += sizeof(double) * ncoset(LPB);          // integrate accumulator
     b += sizeof(T) * 32 * (size_t)red_stride(); // integrate x-fold transpose
-    b += 32;                                     // alignment slack
+    b += 64;                                    // alignment slack
     return (b + 15) & ~size_t(15);
   }
 };
 
-// 1-D factors pol[dir][c][l] = (x_c)^l exp(-zetp x_c^2), x_c = c*h - roff,
-// c in [-cmax, cmax+1]; and the periodic maps map[dir][c] (REF's map[],
-// grid_ref_collint.h:296-304).
-template <typename T, int LPB>
+// Copy an aligned table row of PP elements into registers with 16-byte loads.
+template <typename T, int PP>
+__device__ __forceinline__ void load_row(const T *src, T (&dst)[PP]) {
+  static_assert((PP * sizeof(T)) % 16 == 0, "row not 16-byte sized");
+  const float4 *s = reinterpret_cast<const float4 *>(src);
+  float4 *d = reinterpret_cast<float4 *>(dst);
+#pragma unroll
+  for (int i = 0; i < (int)(PP * sizeof(T) / 16); i++)
+    d[i] = s[i];
+}
+
+// 1-D factors pol[dir][c][l] = x_c^l exp(-zetp x_c^2), x_c = c*h - roff,
+// c in [-cmax, cmax+1]; and the periodic maps map[dir][c]
+// (grid_ref_collint.h:259-304).
+template <typename N, int LPB>
 __device__ __forceinline__ void fill_ortho_tables(const TaskDesc &d, const LevelDesc &L,
-                                                  int cmax, int lp, T *pol, int *map,
+                                                  int cmax, int lp,
+                                                  typename Num<N>::T *pol, int *map,
                                                   int lane) {
+  using T = typename Num<N>::T;
+  constexpr int PP = OrthoSmem<N, LPB>::PP;
   const int w = 2 * cmax + 2;
   for (int e = lane; e < 3 * w; e += 32) {
     const int dir = e / w, c = e - dir * w, cc = c - cmax;
-    const double h = L.dh[dir * 4];
-    T x;
-    if (sizeof(T) == 8)
-      x = (T)((double)cc * h - d.roff[dir]);
-    else
-      x = (T)fmaf((float)cc, (float)h, -(float)d.roff[dir]);
-    T v = Math<T>::gauss((T)d.zetp, x);
-    T *p = pol + (size_t)(dir * w + c) * (LPB + 1);
-#pragma unroll
-    for (int l = 0; l <= LPB; l++) {
-      if (l > lp)
-        break;
-      p[l] = v;
-      v *= x;
-    }
     map[dir * w + c] = imod(d.center[dir] + cc - L.shift[dir], L.npts_global[dir]);
+  }
+  if constexpr (std::is_same<T, double>::value) {
+    // FP64: direct evaluation
+    for (int e = lane; e < 3 * w; e += 32) {
+      const int dir = e / w, c = e - dir * w, cc = c - cmax;
+      const double x = (double)cc * L.dh[dir * 4] - d.roff[dir];
+      double v = exp(-d.zetp * x * x);
+      T *p = pol + (size_t)(dir * w + c) * PP;
+#pragma unroll
+      for (int l = 0; l <= LPB; l++) {
+        if (l > lp)
+          break;
+        p[l] = v;
+        v *= x;
+      }
+    }
+  } else if constexpr (std::is_same<T, float>::value) {
+    for (int e = lane; e < 3 * w; e += 32) {
+      const int dir = e / w, c = e - dir * w, cc = c - cmax;
+      const float x = fmaf((float)cc, (float)L.dh[dir * 4], -(float)d.roff[dir]);
+      float v = expf(-(float)d.zetp * x * x);
+      T *p = pol + (size_t)(dir * w + c) * PP;
+#pragma unroll
+      for (int l = 0; l <= LPB; l++) {
+        if (l > lp)
+          break;
+        p[l] = v;
+        v *= x;
+      }
+    }
+  } else {
+    // dfloat: the Gaussian along each line by the multiplicative recurrence
+    // of grid_ref_collint.h:262-293, seeded with FP64 exponentials, run in
+    // dfloat by 6 lanes (3 directions x 2 sides of c = 0).
+    if (lane < 6) {
+      const int dir = lane >> 1, up = lane & 1;
+      const double h = L.dh[dir * 4], r = d.roff[dir], z = d.zetp;
+      // e(c) = exp(-z (c h - r)^2); e(c +- 1) = e(c) * f(c); f(c +- 1) = f(c) * q
+      dfloat ec = df_make(exp(-z * r * r));
+      dfloat f = df_make(up ? exp(-z * h * (h - 2.0 * r)) : exp(-z * h * (h + 2.0 * r)));
+      const dfloat q = df_make(exp(-2.0 * z * h * h));
+      const dfloat hd = df_make(h), rd = df_make(-r);
+      const int cend = up ? cmax + 1 : -cmax;
+      for (int cc = 0;; cc += up ? 1 : -1) {
+        if (up || cc != 0) { // c = 0 is written by the up-going lane
+          const dfloat x = df_fma1(rd, hd, (float)cc);
+          dfloat v = ec;
+          T *p = pol + (size_t)(dir * w + cc + cmax) * PP;
+#pragma unroll
+          for (int l = 0; l <= LPB; l++) {
+            if (l > lp)
+              break;
+            p[l] = v;
+            v = df_mul(v, x);
+          }
+        }
+        if (cc == cend)
+          break;
+        ec = df_mul(ec, f);
+        f = df_mul(f, q);
+      }
+    }
   }
 }
 
-// tri index of (ly, lx), lx + ly <= m
+// number of (ly, lx) pairs before row ly in a triangle of degree m
 __device__ __forceinline__ int tri_idx(int ly, int lx, int m) {
   return ly * (m + 1) - (ly * (ly - 1)) / 2 + lx;
+}
+
+// grid write of one collocated value
+template <typename N>
+__device__ __forceinline__ void grid_add(double *g, float *glo, size_t i,
+                                         typename Num<N>::T v) {
+  if constexpr (std::is_same<N, dfloat>::value) {
+    atomicAdd(g + i, f2d_exact(v.h));
+    atomicAdd(glo + i, v.l);
+  } else if constexpr (std::is_same<N, float>::value) {
+    atomicAdd(g + i, f2d_exact(v));
+  } else {
+    atomicAdd(g + i, v);
+  }
+}
+
+// grid read for integrate
+template <typename N>
+__device__ __forceinline__ typename Num<N>::T grid_get(const void *g, size_t i) {
+  if constexpr (std::is_same<N, dfloat>::value) {
+    const float2 v = __ldg(reinterpret_cast<const float2 *>(g) + i);
+    return dfloat{v.x, v.y};
+  } else {
+    return __ldg(reinterpret_cast<const typename Num<N>::T *>(g) + i);
+  }
+}
+
+// cube geometry shared by the two kernels
+struct CubeGeo {
+  int K, cmax, w, x_lo, x_hi, SW, G, sub, grp;
+  const int16_t *tab;
+  int lb2;
+};
+
+__device__ __forceinline__ CubeGeo cube_geo(const SphereHdr &H, const int16_t *sph_tab, int lane) {
+  CubeGeo g;
+  g.tab = sph_tab + H.off;
+  g.K = 1 - H.lb[2];
+  g.lb2 = H.lb[2];
+  g.cmax = H.cmax;
+  g.w = 2 * H.cmax + 2;
+  g.x_lo = H.lb[0];
+  g.x_hi = 1 - H.lb[0];
+  const int width = g.x_hi - g.x_lo + 1;
+  g.SW = width < 32 ? width : 32;
+  g.G = 32 / g.SW;
+  g.sub = lane % g.SW;
+  g.grp = lane / g.SW; // lanes with grp >= G are idle
+  return g;
 }
 
 // ------------------------------------------------------------------------
 // collocate, orthorhombic
 // ------------------------------------------------------------------------
-template <typename T, int LPB>
-__global__ void __launch_bounds__(128)
-    collocate_ortho(GridArgs a, int wmax) {
+template <typename N, int LPB>
+__global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
+  using T = typename Num<N>::T;
+  using M = Num<N>;
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int P = LPB + 1;
+  constexpr int PP = OrthoSmem<N, LPB>::PP;
   const int lane = threadIdx.x & 31;
-  unsigned char *ws = smem + (threadIdx.x >> 5) * OrthoSmem<T, LPB>::bytes(wmax);
+  unsigned char *ws = smem + (threadIdx.x >> 5) * OrthoSmem<N, LPB>::bytes(wmax);
   T *pol = (T *)ws;
-  T *coef = pol + 3 * (size_t)wmax * P;
+  T *coef = pol + 3 * (size_t)wmax * PP;
   T *cxy = coef + ncoset(LPB);
   int *map = (int *)(cxy + ntri(LPB));
   const T *coefs = (const T *)a.coef;
@@ -126,45 +228,37 @@ __global__ void __launch_bounds__(128)
     const TaskDesc d = a.tasks[t];
     const LevelDesc &L = a.levels.lv[d.level];
     const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
-    const SphereHdr H = a.sph[d.sphere];
-    const int16_t *tab = a.sph_tab + H.off;
-    const int K = 1 - H.lb[2];
-    const int cmax = H.cmax, w = 2 * cmax + 2;
-    if (w > wmax || lp > LPB) { // host sized the smem; never expected
+    const CubeGeo cg = cube_geo(a.sph[d.sphere], a.sph_tab, lane);
+    if (cg.w > wmax || lp > LPB) { // the host sized the work arrays; never expected
       if (lane == 0)
         atomicOr(a.error, 1);
       continue;
     }
-    const int nco = ncoset(lp);
+    const int nco = ncoset(lp), ntr = ntri(lp);
     const T *csrc = coefs + a.coef_off[t];
     for (int e = lane; e < nco; e += 32)
       coef[e] = csrc[e];
-    fill_ortho_tables<T, LPB>(d, L, cmax, lp, pol, map, lane);
+    fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane);
     __syncwarp();
 
     double *grid = a.grids[d.level];
+    float *glo = a.grids_lo[d.level];
     const size_t nx = L.npts_local[0], nxy = nx * L.npts_local[1];
-    const int x_lo = H.lb[0], x_hi = 1 - H.lb[0], width = x_hi - x_lo + 1;
-    const int SW = width <= 8 ? 8 : (width <= 16 ? 16 : 32);
-    const int G = 32 / SW, sub = lane % SW, grp = lane / SW;
-    const int ntr = ntri(lp);
+    const bool lane_on = cg.grp < cg.G;
 
-    for (int xc = x_lo; xc <= x_hi; xc += SW) {
-      const int cx = xc + sub;
-      const bool xin = cx <= x_hi;
-      T px[P];
-      const T *pxs = pol + (size_t)(cx + cmax) * P;
-#pragma unroll
-      for (int l = 0; l < P; l++)
-        px[l] = (xin && l <= lp) ? pxs[l] : T(0);
-      const int ig = xin ? map[cx + cmax] : 0;
+    for (int xc = cg.x_lo; xc <= cg.x_hi; xc += cg.SW) {
+      const int cx = xc + cg.sub;
+      const bool xin = lane_on && cx <= cg.x_hi;
+      T px[PP];
+      load_row<T, PP>(pol + (size_t)((xin ? cx : cg.x_lo) + cg.cmax) * PP, px);
+      const int ig = map[(xin ? cx : cg.x_lo) + cg.cmax];
 
-      for (int k = H.lb[2]; k <= 1 - H.lb[2]; k++) {
+      for (int k = cg.lb2; k <= 1 - cg.lb2; k++) {
         const int kk = k <= 0 ? -k : k - 1;
-        const int js = tab[kk];
-        const int16_t *irow = tab + 2 * K + tab[K + kk];
+        const int js = cg.tab[kk];
+        const int16_t *irow = cg.tab + 2 * cg.K + cg.tab[cg.K + kk];
         // C_xy[ly][lx] = sum_lz C_xyz[lz][ly][lx] pol_z[lz](k)
-        const T *pz = pol + (size_t)(2 * w + k + cmax) * P;
+        const T *pz = pol + (size_t)(2 * cg.w + k + cg.cmax) * PP;
         for (int e = lane; e < ntr; e += 32) {
           int ly = 0, rem = e;
           while (rem > lp - ly) {
@@ -172,9 +266,9 @@ __global__ void __launch_bounds__(128)
             ly++;
           }
           const int lx = rem;
-          T s = 0;
+          T s = M::zero();
           for (int lz = 0; lz <= lp - ly - lx; lz++)
-            s += coef[cidx(lz, ly, lx, lp)] * pz[lz];
+            s = M::fma(s, coef[cidx(lz, ly, lx, lp)], pz[lz]);
           cxy[e] = s;
         }
         __syncwarp();
@@ -182,32 +276,33 @@ __global__ void __launch_bounds__(128)
         T q[P];
 #pragma unroll
         for (int ly = 0; ly < P; ly++) {
-          T s = 0;
+          T s = M::zero();
           if (ly <= lp) {
             const T *row = cxy + tri_idx(ly, 0, lp);
 #pragma unroll
             for (int lx = 0; lx < P; lx++)
               if (lx <= lp - ly)
-                s += row[lx] * px[lx];
+                s = M::fma(s, row[lx], px[lx]);
           }
           q[ly] = s;
         }
         __syncwarp();
-        double *gplane = grid + (size_t)map[2 * w + k + cmax] * nxy;
-        for (int j0 = js; j0 <= 1 - js; j0 += G) {
-          const int j = j0 + grp;
+        const size_t zoff = (size_t)map[2 * cg.w + k + cg.cmax] * nxy;
+        for (int j0 = js; j0 <= 1 - js; j0 += cg.G) {
+          const int j = j0 + cg.grp;
           if (!xin || j > 1 - js)
             continue;
           const int is = irow[j <= 0 ? -j : j - 1];
           if (cx < is || cx > 1 - is)
             continue;
-          const T *py = pol + (size_t)(w + j + cmax) * P;
-          T v = 0;
+          T py[PP];
+          load_row<T, PP>(pol + (size_t)(cg.w + j + cg.cmax) * PP, py);
+          T v = M::zero();
 #pragma unroll
           for (int ly = 0; ly < P; ly++)
             if (ly <= lp)
-              v += q[ly] * py[ly];
-          atomicAdd(gplane + (size_t)map[w + j + cmax] * nx + ig, (double)v);
+              v = M::fma(v, q[ly], py[ly]);
+          grid_add<N>(grid, glo, zoff + (size_t)map[cg.w + j + cg.cmax] * nx + ig, v);
         }
       }
     }
@@ -220,19 +315,21 @@ __global__ void __launch_bounds__(128)
 // ------------------------------------------------------------------------
 // integrate, orthorhombic (adjoint of collocate_ortho)
 // ------------------------------------------------------------------------
-template <typename T, int LPB>
-__global__ void __launch_bounds__(128)
-    integrate_ortho(GridArgs a, int wmax) {
+template <typename N, int LPB>
+__global__ void __launch_bounds__(128) integrate_ortho(GridArgs a, int wmax) {
+  using T = typename Num<N>::T;
+  using M = Num<N>;
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int P = LPB + 1;
+  constexpr int PP = OrthoSmem<N, LPB>::PP;
   constexpr int NYZ = (LPB + 1) * (LPB + 2) / 2;
   const int lane = threadIdx.x & 31;
-  unsigned char *ws = smem + (threadIdx.x >> 5) * OrthoSmem<T, LPB>::bytes(wmax);
+  unsigned char *ws = smem + (threadIdx.x >> 5) * OrthoSmem<N, LPB>::bytes(wmax);
   T *pol = (T *)ws;
-  T *coef = pol + 3 * (size_t)wmax * P;
+  T *coef = pol + 3 * (size_t)wmax * PP;
   T *cxy = coef + ncoset(LPB);
   int *map = (int *)(cxy + ntri(LPB));
-  double *acc = (double *)(((uintptr_t)(map + 3 * wmax) + 7) & ~uintptr_t(7));
+  double *acc = (double *)(((uintptr_t)(map + 3 * wmax) + 15) & ~uintptr_t(15));
   T *red = (T *)(acc + ncoset(LPB));
   double *out = (double *)a.coef_out;
 
@@ -248,11 +345,8 @@ __global__ void __launch_bounds__(128)
     const TaskDesc d = a.tasks[t];
     const LevelDesc &L = a.levels.lv[d.level];
     const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
-    const SphereHdr H = a.sph[d.sphere];
-    const int16_t *tab = a.sph_tab + H.off;
-    const int K = 1 - H.lb[2];
-    const int cmax = H.cmax, w = 2 * cmax + 2;
-    if (w > wmax || lp > LPB) {
+    const CubeGeo cg = cube_geo(a.sph[d.sphere], a.sph_tab, lane);
+    if (cg.w > wmax || lp > LPB) {
       if (lane == 0)
         atomicOr(a.error, 1);
       continue;
@@ -260,81 +354,82 @@ __global__ void __launch_bounds__(128)
     const int nco = ncoset(lp);
     for (int e = lane; e < nco; e += 32)
       acc[e] = 0.0;
-    fill_ortho_tables<T, LPB>(d, L, cmax, lp, pol, map, lane);
+    fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane);
     __syncwarp();
 
-    const T *grid = (const T *)a.grids_in[d.level];
+    const void *grid = a.grids_in[d.level];
     const size_t nx = L.npts_local[0], nxy = nx * L.npts_local[1];
-    const int x_lo = H.lb[0], x_hi = 1 - H.lb[0], width = x_hi - x_lo + 1;
-    const int SW = width <= 8 ? 8 : (width <= 16 ? 16 : 32);
-    const int G = 32 / SW, sub = lane % SW, grp = lane / SW;
+    const bool lane_on = cg.grp < cg.G;
 
-    for (int xc = x_lo; xc <= x_hi; xc += SW) {
-      const int cx = xc + sub;
-      const bool xin = cx <= x_hi;
-      const int ig = xin ? map[cx + cmax] : 0;
+    for (int xc = cg.x_lo; xc <= cg.x_hi; xc += cg.SW) {
+      const int cx = xc + cg.sub;
+      const bool xin = lane_on && cx <= cg.x_hi;
+      const int ig = map[(xin ? cx : cg.x_lo) + cg.cmax];
       T ayz[NYZ]; // [lz][ly], lz + ly <= LPB
 #pragma unroll
       for (int e = 0; e < NYZ; e++)
-        ayz[e] = T(0);
+        ayz[e] = M::zero();
 
-      for (int k = H.lb[2]; k <= 1 - H.lb[2]; k++) {
+      for (int k = cg.lb2; k <= 1 - cg.lb2; k++) {
         const int kk = k <= 0 ? -k : k - 1;
-        const int js = tab[kk];
-        const int16_t *irow = tab + 2 * K + tab[K + kk];
-        const T *gplane = grid + (size_t)map[2 * w + k + cmax] * nxy;
+        const int js = cg.tab[kk];
+        const int16_t *irow = cg.tab + 2 * cg.K + cg.tab[cg.K + kk];
+        const size_t zoff = (size_t)map[2 * cg.w + k + cg.cmax] * nxy;
         T wy[P];
 #pragma unroll
         for (int l = 0; l < P; l++)
-          wy[l] = T(0);
-        for (int j0 = js; j0 <= 1 - js; j0 += G) {
-          const int j = j0 + grp;
+          wy[l] = M::zero();
+        for (int j0 = js; j0 <= 1 - js; j0 += cg.G) {
+          const int j = j0 + cg.grp;
           if (!xin || j > 1 - js)
             continue;
           const int is = irow[j <= 0 ? -j : j - 1];
           if (cx < is || cx > 1 - is)
             continue;
-          const T v = __ldg(gplane + (size_t)map[w + j + cmax] * nx + ig);
-          const T *py = pol + (size_t)(w + j + cmax) * P;
+          const T v = grid_get<N>(grid, zoff + (size_t)map[cg.w + j + cg.cmax] * nx + ig);
+          T py[PP];
+          load_row<T, PP>(pol + (size_t)(cg.w + j + cg.cmax) * PP, py);
 #pragma unroll
           for (int ly = 0; ly < P; ly++)
             if (ly <= lp)
-              wy[ly] += v * py[ly];
+              wy[ly] = M::fma(wy[ly], v, py[ly]);
         }
-        const T *pz = pol + (size_t)(2 * w + k + cmax) * P;
+        T pz[PP];
+        load_row<T, PP>(pol + (size_t)(2 * cg.w + k + cg.cmax) * PP, pz);
 #pragma unroll
         for (int lz = 0; lz < P; lz++) {
           if (lz > lp)
             break;
-          const T z = pz[lz];
 #pragma unroll
           for (int ly = 0; ly < P; ly++)
             if (ly <= lp - lz)
-              ayz[lz * P - (lz * (lz - 1)) / 2 + ly] += wy[ly] * z;
+              ayz[lz * P - (lz * (lz - 1)) / 2 + ly] =
+                  M::fma(ayz[lz * P - (lz * (lz - 1)) / 2 + ly], wy[ly], pz[lz]);
         }
       }
       // x fold and reduction over the warp through shared memory:
       // C_xyz[lz][ly][lx] += sum_lanes ayz[lz][ly] * pol_x[lx]
       {
-        constexpr int RS = OrthoSmem<T, LPB>::red_stride();
+        constexpr int RS = OrthoSmem<N, LPB>::red_stride();
         T *rl = red + lane * RS;
-        const T *pxs = pol + (size_t)(cx + cmax) * P;
+        T px[PP];
+        load_row<T, PP>(pol + (size_t)((xin ? cx : cg.x_lo) + cg.cmax) * PP, px);
 #pragma unroll
         for (int e = 0; e < NYZ; e++)
           rl[e] = ayz[e];
 #pragma unroll
         for (int l = 0; l < P; l++)
-          rl[NYZ + l] = (xin && l <= lp) ? pxs[l] : T(0);
+          rl[NYZ + l] = (xin && l <= lp) ? px[l] : M::zero();
         __syncwarp();
         for (int e = lane; e < nco; e += 32) {
           int lz, ly, lx;
           decode_cidx(e, lp, lz, ly, lx);
           const int yz = lz * P - (lz * (lz - 1)) / 2 + ly;
-          T s = T(0);
+          T s = M::zero();
 #pragma unroll 8
           for (int r = 0; r < 32; r++)
-            s += red[r * RS + yz] * red[r * RS + NYZ + lx];
-          acc[e] += (double)s;
+            s = M::fma(s, red[r * RS + yz], red[r * RS + NYZ + lx]);
+          acc[e] += M::to_double(s);
         }
         __syncwarp();
       }
@@ -354,101 +449,109 @@ __global__ void __launch_bounds__(128)
 // ------------------------------------------------------------------------
 // launch wrappers
 // ------------------------------------------------------------------------
-template <typename T, int LPB>
-static void launch_coll_t(const GridArgs &a, bool general, int wmax, int nblocks,
-                          cudaStream_t s) {
-  const size_t per_warp = OrthoSmem<T, LPB>::bytes(wmax);
+template <typename N, int LPB>
+static void launch_ortho_t(const GridArgs &a, bool collocate, int wmax, int nblocks,
+                           cudaStream_t s) {
+  const size_t per_warp = OrthoSmem<N, LPB>::bytes(wmax);
   const int nw = warps_for(per_warp);
   const size_t smem = nw * per_warp;
-  if (general) {
-    launch_collocate_general_impl(a, sizeof(T) == 4, LPB, wmax, nblocks, s);
-    return;
-  }
   if (nw < 1)
-    return launch_error("collocate: cube too large for shared memory");
-  auto k = collocate_ortho<T, LPB>;
-  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (nblocks <= 0)
-    nblocks = persistent_blocks((const void *)k, 32 * nw, smem);
-  k<<<nblocks, 32 * nw, smem, s>>>(a, wmax);
+    return launch_error("orthorhombic grid kernel: cube too large for shared memory");
+  if (collocate) {
+    auto k = collocate_ortho<N, LPB>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (nblocks <= 0)
+      nblocks = persistent_blocks((const void *)k, 32 * nw, smem);
+    k<<<nblocks, 32 * nw, smem, s>>>(a, wmax);
+  } else {
+    auto k = integrate_ortho<N, LPB>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (nblocks <= 0)
+      nblocks = persistent_blocks((const void *)k, 32 * nw, smem);
+    k<<<nblocks, 32 * nw, smem, s>>>(a, wmax);
+  }
   count_launch();
 }
 
-template <typename T, int LPB>
-static void launch_int_t(const GridArgs &a, bool general, int wmax, int nblocks,
-                         cudaStream_t s) {
-  const size_t per_warp = OrthoSmem<T, LPB>::bytes(wmax);
-  const int nw = warps_for(per_warp);
-  const size_t smem = nw * per_warp;
+template <int LPB>
+static void launch_ortho_lp(const GridArgs &a, int arith, bool collocate, int wmax, int nblocks,
+                            cudaStream_t s) {
+  if (arith == ARITH_FP64)
+    launch_ortho_t<double, LPB>(a, collocate, wmax, nblocks, s);
+  else if (arith == ARITH_FP32)
+    launch_ortho_t<float, LPB>(a, collocate, wmax, nblocks, s);
+  else
+    launch_ortho_t<dfloat, LPB>(a, collocate, wmax, nblocks, s);
+}
+
+void launch_collocate(const GridArgs &a, int arith, bool general, int bucket, int extent,
+                      int nblocks, cudaStream_t s) {
   if (general) {
-    launch_integrate_general_impl(a, sizeof(T) == 4, LPB, wmax, nblocks, s);
+    launch_collocate_general_impl(a, arith, kBucketLp[bucket], extent, nblocks, s);
     return;
   }
-  if (nw < 1)
-    return launch_error("integrate: cube too large for shared memory");
-  auto k = integrate_ortho<T, LPB>;
-  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (nblocks <= 0)
-    nblocks = persistent_blocks((const void *)k, 32 * nw, smem);
-  k<<<nblocks, 32 * nw, smem, s>>>(a, wmax);
-  count_launch();
-}
-
-size_t ortho_smem_per_warp(bool fp32, int bucket, int wmax) {
-  const int lpb = kBucketLp[bucket];
-#define GB_CASE(LP)                                                            \
-  if (lpb == LP)                                                               \
-    return fp32 ? OrthoSmem<float, LP>::bytes(wmax) : OrthoSmem<double, LP>::bytes(wmax);
-  GB_CASE(4) GB_CASE(6) GB_CASE(9) GB_CASE(16)
-#undef GB_CASE
-  return 0;
-}
-
-void launch_collocate(const GridArgs &a, bool fp32, bool general, int bucket,
-                      int wmax, int nblocks, cudaStream_t s) {
   switch (kBucketLp[bucket]) {
-#define GB_CASE(LP)                                                            \
-  case LP:                                                                     \
-    if (fp32)                                                                  \
-      launch_coll_t<float, LP>(a, general, wmax, nblocks, s);                  \
-    else                                                                       \
-      launch_coll_t<double, LP>(a, general, wmax, nblocks, s);                 \
-    break;
-    GB_CASE(4) GB_CASE(6) GB_CASE(9) GB_CASE(16)
-#undef GB_CASE
+  case 4: launch_ortho_lp<4>(a, arith, true, extent, nblocks, s); break;
+  case 6: launch_ortho_lp<6>(a, arith, true, extent, nblocks, s); break;
+  case 9: launch_ortho_lp<9>(a, arith, true, extent, nblocks, s); break;
+  case 16: launch_ortho_lp<16>(a, arith, true, extent, nblocks, s); break;
   }
 }
 
-void launch_integrate(const GridArgs &a, bool fp32, bool general, int bucket,
-                      int wmax, int nblocks, cudaStream_t s) {
+void launch_integrate(const GridArgs &a, int arith, bool general, int bucket, int extent,
+                      int nblocks, cudaStream_t s) {
+  if (general) {
+    launch_integrate_general_impl(a, arith, kBucketLp[bucket], extent, nblocks, s);
+    return;
+  }
   switch (kBucketLp[bucket]) {
-#define GB_CASE(LP)                                                            \
-  case LP:                                                                     \
-    if (fp32)                                                                  \
-      launch_int_t<float, LP>(a, general, wmax, nblocks, s);                   \
-    else                                                                       \
-      launch_int_t<double, LP>(a, general, wmax, nblocks, s);                  \
-    break;
-    GB_CASE(4) GB_CASE(6) GB_CASE(9) GB_CASE(16)
-#undef GB_CASE
+  case 4: launch_ortho_lp<4>(a, arith, false, extent, nblocks, s); break;
+  case 6: launch_ortho_lp<6>(a, arith, false, extent, nblocks, s); break;
+  case 9: launch_ortho_lp<9>(a, arith, false, extent, nblocks, s); break;
+  case 16: launch_ortho_lp<16>(a, arith, false, extent, nblocks, s); break;
   }
 }
 
-// FP64 -> FP32 copy of a potential grid for the mixed integrate path.
-__global__ void grid_to_fp32_kernel(const double *__restrict__ src,
-                                    float *__restrict__ dst, size_t n) {
+// ------------------------------------------------------------------------
+// grid conversions around the mixed paths
+// ------------------------------------------------------------------------
+__global__ void grid_split_kernel(const double *__restrict__ src, void *__restrict__ dst,
+                                  size_t n, int arith) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const double v = src[i];
+    if (arith == ARITH_FP32) {
+      ((float *)dst)[i] = (float)v;
+    } else {
+      const float h = (float)v;
+      ((float2 *)dst)[i] = make_float2(h, (float)(v - (double)h));
+    }
+  }
+}
+
+__global__ void grid_fold_lo_kernel(double *__restrict__ g, const float *__restrict__ lo,
+                                    size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x)
-    dst[i] = (float)src[i];
+    g[i] += (double)lo[i];
 }
 
-void launch_grid_to_fp32(const double *src, float *dst, size_t n, cudaStream_t s) {
+static int grid_blocks(size_t n) {
+  size_t nb = (n + 255) / 256;
+  return (int)(nb > 152 * 16 ? 152 * 16 : (nb ? nb : 1));
+}
+
+void launch_grid_split(const double *src, void *dst, size_t n, int arith, cudaStream_t s) {
   if (n == 0)
     return;
-  int nb = (int)((n + 255) / 256);
-  if (nb > 152 * 16)
-    nb = 152 * 16;
-  grid_to_fp32_kernel<<<nb, 256, 0, s>>>(src, dst, n);
+  grid_split_kernel<<<grid_blocks(n), 256, 0, s>>>(src, dst, n, arith);
+  count_launch();
+}
+
+void launch_grid_fold_lo(double *g, const float *lo, size_t n, cudaStream_t s) {
+  if (n == 0)
+    return;
+  grid_fold_lo_kernel<<<grid_blocks(n), 256, 0, s>>>(g, lo, n);
   count_launch();
 }
 

@@ -1,0 +1,134 @@
+// Arithmetic types of the grid kernels.
+//
+//   double   plain FP64                        (GRID_GB300_FP64)
+//   float    plain FP32                        (GRID_GB300_FP32)
+//   dfloat   unevaluated sum of two floats      (GRID_GB300_MIXED)
+//
+// dfloat ("double-float") carries ~48 significant bits on the FP32 pipes:
+// products are split exactly with an FMA (TwoProduct) and sums with Knuth's
+// TwoSum (D. E. Knuth, TAOCP vol. 2, 4.2.2; T. J. Dekker, Numer. Math. 18
+// (1971) 224-242).  On GB300 the FP64 pipe runs at about 1/56 of the FP32
+// rate, so a dfloat FMA (about 12 FP32 operations) is several times cheaper
+// than an FP64 FMA while keeping the per-point evaluation accurate to
+// ~1e-14 relative.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace gb300 {
+
+struct dfloat {
+  float h, l;
+};
+
+__device__ __forceinline__ dfloat df_make(double x) {
+  const float h = (float)x;
+  return dfloat{h, (float)(x - (double)h)};
+}
+
+// acc + a*b
+__device__ __forceinline__ dfloat df_fma(dfloat acc, dfloat a, dfloat b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);     // exact error of the leading product
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  const float s = acc.h + p;        // TwoSum(acc.h, p)
+  const float bb = s - acc.h;
+  const float err = (acc.h - (s - bb)) + (p - bb);
+  const float t = err + (acc.l + e);
+  const float h = s + t;            // renormalise
+  return dfloat{h, t - (h - s)};
+}
+
+// acc + a*b with b a plain float (exactly representable factor)
+__device__ __forceinline__ dfloat df_fma1(dfloat acc, dfloat a, float b) {
+  const float p = a.h * b;
+  float e = fmaf(a.h, b, -p);
+  e = fmaf(a.l, b, e);
+  const float s = acc.h + p;
+  const float bb = s - acc.h;
+  const float err = (acc.h - (s - bb)) + (p - bb);
+  const float t = err + (acc.l + e);
+  const float h = s + t;
+  return dfloat{h, t - (h - s)};
+}
+
+__device__ __forceinline__ dfloat df_mul(dfloat a, dfloat b) {
+  return df_fma(dfloat{0.f, 0.f}, a, b);
+}
+
+__device__ __forceinline__ dfloat df_add(dfloat a, dfloat b) {
+  const float s = a.h + b.h;
+  const float bb = s - a.h;
+  const float err = (a.h - (s - bb)) + (b.h - bb);
+  const float t = err + (a.l + b.l);
+  const float h = s + t;
+  return dfloat{h, t - (h - s)};
+}
+
+__device__ __forceinline__ dfloat df_shfl_xor(dfloat v, int o) {
+  return dfloat{__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
+}
+
+// Exact FP32 -> FP64 conversion on the integer pipes (the FP64 pipe, which
+// would otherwise do it, is the scarce unit on GB300).  Subnormal inputs
+// (|x| < 1.2e-38) flush to signed zero.
+__device__ __forceinline__ double f2d_exact(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned mag = u & 0x7fffffffu;
+  const unsigned sign = u & 0x80000000u;
+  unsigned hi = sign | ((mag >> 3) + 0x38000000u);
+  unsigned lo = mag << 29;
+  if (mag < 0x00800000u) {
+    hi = sign;
+    lo = 0u;
+  }
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// ---------------------------------------------------------------------------
+// uniform interface over double / float / dfloat
+// ---------------------------------------------------------------------------
+template <typename N> struct Num;
+
+template <> struct Num<double> {
+  using T = double;
+  static __device__ __forceinline__ T zero() { return 0.0; }
+  static __device__ __forceinline__ T from(double x) { return x; }
+  static __device__ __forceinline__ T fma(T acc, T a, T b) { return fma_rn(acc, a, b); }
+  static __device__ __forceinline__ T fma_rn(T acc, T a, T b) { return ::fma(a, b, acc); }
+  static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
+  static __device__ __forceinline__ T add(T a, T b) { return a + b; }
+  static __device__ __forceinline__ double to_double(T a) { return a; }
+  static __device__ __forceinline__ T shfl_xor(T v, int o) {
+    return __shfl_xor_sync(0xffffffffu, v, o);
+  }
+};
+
+template <> struct Num<float> {
+  using T = float;
+  static __device__ __forceinline__ T zero() { return 0.f; }
+  static __device__ __forceinline__ T from(double x) { return (float)x; }
+  static __device__ __forceinline__ T fma(T acc, T a, T b) { return fmaf(a, b, acc); }
+  static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
+  static __device__ __forceinline__ T add(T a, T b) { return a + b; }
+  static __device__ __forceinline__ double to_double(T a) { return f2d_exact(a); }
+  static __device__ __forceinline__ T shfl_xor(T v, int o) {
+    return __shfl_xor_sync(0xffffffffu, v, o);
+  }
+};
+
+template <> struct Num<dfloat> {
+  using T = dfloat;
+  static __device__ __forceinline__ T zero() { return dfloat{0.f, 0.f}; }
+  static __device__ __forceinline__ T from(double x) { return df_make(x); }
+  static __device__ __forceinline__ T fma(T acc, T a, T b) { return df_fma(acc, a, b); }
+  static __device__ __forceinline__ T mul(T a, T b) { return df_mul(a, b); }
+  static __device__ __forceinline__ T add(T a, T b) { return df_add(a, b); }
+  static __device__ __forceinline__ double to_double(T a) {
+    return f2d_exact(a.h) + f2d_exact(a.l);
+  }
+  static __device__ __forceinline__ T shfl_xor(T v, int o) { return df_shfl_xor(v, o); }
+};
+
+} // namespace gb300

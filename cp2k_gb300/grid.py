@@ -24,7 +24,7 @@ GRID_FUNC_AB = 100
 GRID_FUNC_DADB = 200
 GRID_BACKEND_AUTO, GRID_BACKEND_REF, GRID_BACKEND_CPU = 10, 11, 12
 GRID_BACKEND_DGEMM, GRID_BACKEND_GPU, GRID_BACKEND_GB300 = 13, 14, 15
-FP64, MIXED = 0, 1
+FP64, MIXED, FP32 = 0, 1, 2
 SCHEDULE_SIZE, SCHEDULE_MODEL, SCHEDULE_INPUT = 0, 1, 2
 
 # every grid_func value (src/grid/common/grid_constants.h:10-46)
@@ -226,33 +226,45 @@ class GridTaskList:
             self._grids = [Buffer(n) for n in self.inp.grid_sizes()]
         return self._pab, self._hab, self._grids
 
-    def collocate(self, func: int, pab_blocks: np.ndarray) -> list:
-        """grid_collocate_task_list with host buffers; returns copies of the grids."""
+    def host_buffers(self):
+        """The pinned offload buffers (pab, hab, grids) the host calls use."""
+        return self._buffers()
+
+    def collocate(self, func: int, pab_blocks=None, copy_out: bool = True):
+        """grid_collocate_task_list with host buffers.  pab_blocks=None uses the
+        current content of the pab offload buffer; returns copies of the grids
+        (or None with copy_out=False)."""
         L = lib()
         pab, _, grids = self._buffers()
-        pab.host[:] = pab_blocks
+        if pab_blocks is not None:
+            pab.host[:] = pab_blocks
         arr = (C.POINTER(OffloadBuffer) * len(grids))(*[g.ptr for g in grids])
         if self.api == "cp2k":
             L.grid_collocate_task_list(self.h, int(func), self.inp.nlevels, _p(self.npts_local),
                                        pab.ptr, arr)
         else:
             L.grid_gb300_collocate_task_list(self.impl, int(func), self.inp.nlevels, pab.ptr, arr)
-        return [g.host.copy() for g in grids]
+        return [g.host.copy() for g in grids] if copy_out else None
 
-    def integrate(self, grids, pab_blocks=None, compute_tau=False, forces=False, virial=False):
-        """grid_integrate_task_list with host buffers; returns (hab, forces, virial)."""
+    def integrate(self, grids=None, pab_blocks=None, compute_tau=False, forces=False,
+                  virial=False, copy_out: bool = True, use_pab: bool = None):
+        """grid_integrate_task_list with host buffers; returns (hab, forces, virial).
+        grids=None uses the current content of the grid offload buffers."""
         L = lib()
         pab, hab, gb = self._buffers()
-        for b, g in zip(gb, grids):
-            b.host[:] = g
+        if grids is not None:
+            for b, g in zip(gb, grids):
+                b.host[:] = g
         if pab_blocks is not None:
             pab.host[:] = pab_blocks
+        if use_pab is None:
+            use_pab = pab_blocks is not None
         arr = (C.POINTER(OffloadBuffer) * len(gb))(*[b.ptr for b in gb])
         f = np.zeros((self.inp.natoms, 3)) if forces else None
         v = np.zeros((3, 3)) if virial else None
         fp = _p(f) if f is not None else None
         vp_ = _p(v) if v is not None else None
-        pp = pab.ptr if pab_blocks is not None else None
+        pp = pab.ptr if use_pab else None
         if self.api == "cp2k":
             L.grid_integrate_task_list(self.h, bool(compute_tau), self.inp.natoms,
                                        self.inp.nlevels, _p(self.npts_local), pp, arr, hab.ptr,
@@ -260,7 +272,7 @@ class GridTaskList:
         else:
             L.grid_gb300_integrate_task_list(self.impl, bool(compute_tau), self.inp.nlevels, pp,
                                              arr, hab.ptr, fp, vp_)
-        return hab.host.copy(), f, v
+        return (hab.host.copy() if copy_out else None), f, v
 
     # ---------------------------------------------------- device buffers
     def collocate_device(self, func: int, pab_dev, grids_dev, stream=None):

@@ -233,10 +233,18 @@ void grid_gb300_integrate_task_list(const grid_gb300_task_list *task_list,
 
 /* Arithmetic of the grid kernels:
  *  GRID_GB300_FP64  -- everything in FP64 (parity 1e-12 with REF);
- *  GRID_GB300_MIXED -- FP32 per-point polynomial x Gaussian and the C_ab <->
- *                      C_xyz transforms; FP64 prefactors/geometry, FP64
- *                      accumulation into the grid and into hab/forces/virial. */
-enum grid_gb300_precision { GRID_GB300_FP64 = 0, GRID_GB300_MIXED = 1 };
+ *  GRID_GB300_MIXED -- per-point polynomial x Gaussian on the FP32 pipes in
+ *                      compensated double-float arithmetic (pairs of FP32
+ *                      values, ~48-bit significands); FP64 prefactors,
+ *                      geometry and C_ab <-> C_xyz transforms, FP64
+ *                      accumulation into the grid and hab/forces/virial;
+ *  GRID_GB300_FP32  -- plain FP32 per-point work and transforms, FP64
+ *                      accumulation (fastest, ~1e-7 of max |rho|). */
+enum grid_gb300_precision {
+  GRID_GB300_FP64 = 0,
+  GRID_GB300_MIXED = 1,
+  GRID_GB300_FP32 = 2,
+};
 
 /* Order in which the persistent kernels take tasks:
  *  GRID_GB300_SCHEDULE_SIZE  -- descending analytic size (points x (lp+1));

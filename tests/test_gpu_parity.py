@@ -87,3 +87,71 @@ def test_tasklist_fp64(G, O, name, scale, funcs):
         assert rel_diff(h3, h4) < TOL_GRID * 5
     tl.close()
     ot.close()
+
+
+# Stated error bounds of the reduced-precision paths against the FP64 oracle,
+# measured on seeded inputs (uniform [-1, 1] density-matrix blocks and
+# potential):
+#   MIXED (double-float per-point work, FP64 accumulation):
+#       max |d rho| / max(1, |rho|) <= 1e-9, max |d hab| / max(1, |hab|) <= 1e-9
+#   FP32  (plain FP32 per-point work, FP64 accumulation):
+#       max |d rho| / max |rho| <= 2e-6,     max |d hab| / max |hab| <= 2e-6
+@pytest.mark.parametrize("name,scale", [("c1_64atoms", 0.3), ("c2_512atoms", 0.08),
+                                        ("c3_256atoms_triclinic", 0.12)])
+def test_reduced_precision_bounds(G, O, name, scale):
+    from cp2k_gb300 import workload as W
+    inp = W.config(name, scale=scale, seed=9)
+    pab = W.density_blocks(inp)
+    V = W.potential_grids(inp)
+    ot = O.OracleTaskList(inp)
+    g_ref = ot.collocate(100, pab)
+    h_ref, f_ref, _ = ot.integrate(V, pab, forces=True)
+    gmax = max(float(np.abs(g).max()) for g in g_ref)
+    hmax = float(np.abs(h_ref).max())
+    for prec, tol_rel, tol_max in ((G.MIXED, 1e-9, None), (G.FP32, None, 2e-6)):
+        tl = G.GridTaskList(inp, precision=prec)
+        g = tl.collocate(100, pab)
+        h, f, _ = tl.integrate(V, pab, forces=True)
+        if tol_rel is not None:
+            assert max(rel_diff(a, b) for a, b in zip(g, g_ref)) < tol_rel
+            assert rel_diff(h, h_ref) < tol_rel
+            assert rel_diff(f, f_ref) < 1e-7
+        else:
+            assert max(float(np.abs(a - b).max()) for a, b in zip(g, g_ref)) / gmax < tol_max
+            assert float(np.abs(h - h_ref).max()) / hmax < tol_max
+        tl.close()
+    ot.close()
+
+
+def test_cp2k_surface_and_empty_list(G):
+    """grid_create_task_list & co. (the CP2K symbols) on an empty task list
+    zero their outputs (src/grid/grid_task_list.c:185-189, 290-311)."""
+    from cp2k_gb300 import workload as W
+    inp = W.config("c1_64atoms", scale=0.1, seed=3)
+    empty = type(inp)(**{**inp.__dict__, **{k: getattr(inp, k)[:0] for k in (
+        "level_list", "iatom_list", "jatom_list", "iset_list", "jset_list", "ipgf_list",
+        "jpgf_list", "border_mask_list", "block_num_list", "radius_list", "rab_list")}})
+    tl = G.GridTaskList(empty, api="cp2k")
+    g = tl.collocate(100, np.ones(inp.buffer_size))
+    assert all(float(np.abs(x).max()) == 0.0 for x in g)
+    h, f, v = tl.integrate([np.ones(n) for n in inp.grid_sizes()], np.ones(inp.buffer_size),
+                           forces=True, virial=True)
+    assert float(np.abs(h).max()) == 0.0 and float(np.abs(f).max()) == 0.0
+    assert float(np.abs(v).max()) == 0.0
+    tl.close()
+
+
+def test_recreate_and_schedules_agree(G, O):
+    """Re-creating a task list and reordering its work queue leave the FP64
+    results within rounding."""
+    from cp2k_gb300 import workload as W
+    inp = W.config("c1_64atoms", scale=0.2, seed=4)
+    pab = W.density_blocks(inp)
+    tl = G.GridTaskList(inp)
+    outs = []
+    for sched in (G.SCHEDULE_SIZE, G.SCHEDULE_INPUT, G.SCHEDULE_SIZE):
+        tl.set_schedule(sched)
+        outs.append(tl.collocate(100, pab))
+    for o in outs[1:]:
+        assert max(rel_diff(a, b) for a, b in zip(o, outs[0])) < 1e-13
+    tl.close()
