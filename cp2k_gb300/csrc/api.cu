@@ -338,7 +338,7 @@ static void build_sphere(const LevelDesc &L, double disr, SphereHdr &h,
     h.lb[i] = (int)ceil(-1e-8 - disr * L.dh_inv[i * 4]);
   h.cmax = std::max(std::max(1 - h.lb[0], 1 - h.lb[1]), 1 - h.lb[2]);
   h.off = (int)tab.size();
-  const int K = 1 - h.lb[2];
+  const int K = 1 - h.lb[2], NX = 1 - h.lb[0];
   std::vector<int> js(K), rows;
   std::vector<int16_t> is;
   npoints = 0;
@@ -360,13 +360,27 @@ static void build_sphere(const LevelDesc &L, double disr, SphereHdr &h,
       npoints += 4LL * (2 - 2 * istart); // rows j1, j2 of planes k1, k2
     }
   }
+  // last row index JJ per (plane, x): x with distance index ii lies on rows
+  // j in [-JJ, JJ + 1] (row jj holds x iff istart(kk, jj) <= -ii; istart
+  // grows with jj), -1 if no row of the plane holds x.
+  std::vector<int16_t> jx((size_t)K * NX, -1);
+  for (int kk = 0; kk < K; kk++)
+    for (int ii = 0; ii < NX; ii++) {
+      int last = -1;
+      for (int jj = 0; jj <= -js[kk]; jj++)
+        if (is[rows[kk] + jj] <= -ii)
+          last = jj;
+      jx[(size_t)kk * NX + ii] = (int16_t)last;
+    }
   for (int kk = 0; kk < K; kk++)
     tab.push_back((int16_t)js[kk]);
   for (int kk = 0; kk < K; kk++)
     tab.push_back((int16_t)rows[kk]);
-  if (is.size() > 32767)
-    fail("sphere table row offsets exceed int16");
+  if (is.size() + jx.size() + 2 * (size_t)K > 32767)
+    fail("sphere table exceeds int16 offsets");
   tab.insert(tab.end(), is.begin(), is.end());
+  h.jxo = 2 * K + (int)is.size();
+  tab.insert(tab.end(), jx.begin(), jx.end());
 }
 
 template <typename T> static T *dalloc_copy(const std::vector<T> &v) {

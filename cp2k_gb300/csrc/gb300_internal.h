@@ -77,6 +77,7 @@ struct SphereHdr {
   int lb[3];
   int cmax;
   int off; // into the int16 table: [K] jstart, [K] row offsets, istart rows
+  int jxo; // relative offset of the [K][1-lb[0]] table of last row index per x
 };
 
 struct LevelDesc {

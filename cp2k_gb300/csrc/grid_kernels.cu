@@ -176,14 +176,17 @@ __device__ __forceinline__ typename Num<N>::T grid_get(const void *g, size_t i) 
 
 // cube geometry shared by the two kernels
 struct CubeGeo {
-  int K, cmax, w, x_lo, x_hi, SW, G, sub, grp;
+  int K, cmax, w, x_lo, x_hi, SW, G, sub, grp, NX;
   const int16_t *tab;
+  const int16_t *jx; // [K][NX] last row index per (plane, x)
   int lb2;
 };
 
 __device__ __forceinline__ CubeGeo cube_geo(const SphereHdr &H, const int16_t *sph_tab, int lane) {
   CubeGeo g;
   g.tab = sph_tab + H.off;
+  g.jx = g.tab + H.jxo;
+  g.NX = 1 - H.lb[0];
   g.K = 1 - H.lb[2];
   g.lb2 = H.lb[2];
   g.cmax = H.cmax;
@@ -256,7 +259,6 @@ __global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
       for (int k = cg.lb2; k <= 1 - cg.lb2; k++) {
         const int kk = k <= 0 ? -k : k - 1;
         const int js = cg.tab[kk];
-        const int16_t *irow = cg.tab + 2 * cg.K + cg.tab[cg.K + kk];
         // C_xy[ly][lx] = sum_lz C_xyz[lz][ly][lx] pol_z[lz](k)
         const T *pz = pol + (size_t)(2 * cg.w + k + cg.cmax) * PP;
         for (int e = lane; e < ntr; e += 32) {
@@ -288,21 +290,30 @@ __global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
         }
         __syncwarp();
         const size_t zoff = (size_t)map[2 * cg.w + k + cg.cmax] * nxy;
-        for (int j0 = js; j0 <= 1 - js; j0 += cg.G) {
-          const int j = j0 + cg.grp;
-          if (!xin || j > 1 - js)
+        // rows of this lane's x on the plane: j in [jlo, jhi]
+        const int JJ = xin ? (int)cg.jx[kk * cg.NX + (cx <= 0 ? -cx : cx - 1)] : -1;
+        const int jlo = -JJ, jhi = JJ + 1, jend = 1 - js;
+        for (int j = js + cg.grp; j <= jend; j += 2 * cg.G) {
+          const int j2 = j + cg.G;
+          const bool in1 = j >= jlo && j <= jhi;
+          const bool in2 = j2 >= jlo && j2 <= jhi;
+          if (!(in1 || in2))
             continue;
-          const int is = irow[j <= 0 ? -j : j - 1];
-          if (cx < is || cx > 1 - is)
-            continue;
-          T py[PP];
-          load_row<T, PP>(pol + (size_t)(cg.w + j + cg.cmax) * PP, py);
-          T v = M::zero();
+          const int j2c = j2 <= jend ? j2 : jend;
+          T p1[PP], p2[PP];
+          load_row<T, PP>(pol + (size_t)(cg.w + j + cg.cmax) * PP, p1);
+          load_row<T, PP>(pol + (size_t)(cg.w + j2c + cg.cmax) * PP, p2);
+          T v1 = M::zero(), v2 = M::zero();
 #pragma unroll
           for (int ly = 0; ly < P; ly++)
-            if (ly <= lp)
-              v = M::fma(v, q[ly], py[ly]);
-          grid_add<N>(grid, glo, zoff + (size_t)map[cg.w + j + cg.cmax] * nx + ig, v);
+            if (ly <= lp) {
+              v1 = M::fma(v1, q[ly], p1[ly]);
+              v2 = M::fma(v2, q[ly], p2[ly]);
+            }
+          if (in1)
+            grid_add<N>(grid, glo, zoff + (size_t)map[cg.w + j + cg.cmax] * nx + ig, v1);
+          if (in2)
+            grid_add<N>(grid, glo, zoff + (size_t)map[cg.w + j2c + cg.cmax] * nx + ig, v2);
         }
       }
     }
@@ -373,26 +384,31 @@ __global__ void __launch_bounds__(128) integrate_ortho(GridArgs a, int wmax) {
       for (int k = cg.lb2; k <= 1 - cg.lb2; k++) {
         const int kk = k <= 0 ? -k : k - 1;
         const int js = cg.tab[kk];
-        const int16_t *irow = cg.tab + 2 * cg.K + cg.tab[cg.K + kk];
         const size_t zoff = (size_t)map[2 * cg.w + k + cg.cmax] * nxy;
         T wy[P];
 #pragma unroll
         for (int l = 0; l < P; l++)
           wy[l] = M::zero();
-        for (int j0 = js; j0 <= 1 - js; j0 += cg.G) {
-          const int j = j0 + cg.grp;
-          if (!xin || j > 1 - js)
+        const int JJ = xin ? (int)cg.jx[kk * cg.NX + (cx <= 0 ? -cx : cx - 1)] : -1;
+        const int jlo = -JJ, jhi = JJ + 1, jend = 1 - js;
+        for (int j = js + cg.grp; j <= jend; j += 2 * cg.G) {
+          const int j2 = j + cg.G;
+          const bool in1 = j >= jlo && j <= jhi;
+          const bool in2 = j2 >= jlo && j2 <= jhi;
+          if (!(in1 || in2))
             continue;
-          const int is = irow[j <= 0 ? -j : j - 1];
-          if (cx < is || cx > 1 - is)
-            continue;
-          const T v = grid_get<N>(grid, zoff + (size_t)map[cg.w + j + cg.cmax] * nx + ig);
-          T py[PP];
-          load_row<T, PP>(pol + (size_t)(cg.w + j + cg.cmax) * PP, py);
+          const int j2c = j2 <= jend ? j2 : jend;
+          const T v1 =
+              in1 ? grid_get<N>(grid, zoff + (size_t)map[cg.w + j + cg.cmax] * nx + ig) : M::zero();
+          const T v2 =
+              in2 ? grid_get<N>(grid, zoff + (size_t)map[cg.w + j2c + cg.cmax] * nx + ig) : M::zero();
+          T p1[PP], p2[PP];
+          load_row<T, PP>(pol + (size_t)(cg.w + j + cg.cmax) * PP, p1);
+          load_row<T, PP>(pol + (size_t)(cg.w + j2c + cg.cmax) * PP, p2);
 #pragma unroll
           for (int ly = 0; ly < P; ly++)
             if (ly <= lp)
-              wy[ly] = M::fma(wy[ly], v, py[ly]);
+              wy[ly] = M::fma(M::fma(wy[ly], v1, p1[ly]), v2, p2[ly]);
         }
         T pz[PP];
         load_row<T, PP>(pol + (size_t)(2 * cg.w + k + cg.cmax) * PP, pz);
