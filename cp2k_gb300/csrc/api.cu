@@ -242,7 +242,7 @@ struct Mode { // everything that depends on the l shifts of a call
   std::vector<int> coef_off; // per task (block order)
   int *d_coef_off = nullptr;
   size_t coef_total = 0;
-  Queue q[2][kNumBuckets]; // [general][bucket]
+  Queue q[2][kNumBuckets][2]; // [general][bucket][class: 0 = arith, 1 = FP32]
   int coef_words = 0;      // per-warp shared memory words of coefficient/post
   int sched_version = -1;
 };
@@ -262,6 +262,8 @@ struct TaskList {
   std::vector<int16_t> sph_tab;
   std::vector<long long> points; // per task (block order)
   std::vector<float> model_cost; // per task, empty unless a model was applied
+  std::vector<double> gbound;    // per task bound of |contribution| for |P| <= 1
+  double mixed_threshold = 1e-3; // mixed path: tasks with gbound <= this run FP32
   std::vector<int> npts_local;   // [nlevels][3]
   size_t cart_total = 0;
   int contract_words = 1;
@@ -383,6 +385,39 @@ static void build_sphere(const LevelDesc &L, double disr, SphereHdr &h,
   tab.insert(tab.end(), jx.begin(), jx.end());
 }
 
+// Upper bound of |a Gaussian-product contribution| for |P_ab| <= 1: the
+// prefactor times, per direction, the sum over the binomial expansion
+// coefficients of (x-a)^i (x-b)^j about p of max_x |x^n exp(-zetp x^2)|
+// = (n / (2 e zetp))^(n/2).  Used to pick FP32 or double-float per task.
+static double contribution_bound(const TaskDesc &d, const double *ra) {
+  const int la = d.la_max, lb = d.lb_max;
+  double m[2 * GB300_LMAX + 2];
+  for (int n = 0; n <= la + lb; n++)
+    m[n] = n == 0 ? 1.0 : pow(n / (2.0 * M_E * d.zetp), 0.5 * n);
+  double g = d.prefexp * ((d.iatom == d.jatom) ? 1.0 : 2.0);
+  for (int dir = 0; dir < 3; dir++) {
+    const double pa = d.rp[dir] - ra[dir], pb = d.rp[dir] - (ra[dir] + d.rab[dir]);
+    double s = 0.0;
+    for (int xa = 0; xa <= la; xa++)
+      for (int xb = 0; xb <= lb; xb++) {
+        double al[2 * GB300_LMAX + 2] = {0};
+        double ca = 1.0;
+        for (int k = 0; k <= xa; k++) {
+          double cb = 1.0;
+          for (int q = 0; q <= xb; q++) {
+            al[xa - k + xb - q] += ca * cb * pow(pa, k) * pow(pb, q);
+            cb = cb * (xb - q) / (q + 1);
+          }
+          ca = ca * (xa - k) / (k + 1);
+        }
+        for (int n = 0; n <= xa + xb; n++)
+          s += fabs(al[n]) * m[n];
+      }
+    g *= s;
+  }
+  return g;
+}
+
 template <typename T> static T *dalloc_copy(const std::vector<T> &v) {
   T *p = nullptr;
   const size_t n = v.empty() ? 1 : v.size();
@@ -408,10 +443,11 @@ static void free_device(TaskList *t) {
   for (auto &kv : t->modes) {
     if (kv.second.d_coef_off)
       cudaFree(kv.second.d_coef_off);
-    for (auto &qq : kv.second.q)
-      for (auto &q : qq)
-        if (q.d_idx)
-          cudaFree(q.d_idx);
+    for (auto &qg : kv.second.q)
+      for (auto &qb : qg)
+        for (auto &q : qb)
+          if (q.d_idx)
+            cudaFree(q.d_idx);
   }
   for (auto &e : t->ev)
     if (e)
@@ -512,6 +548,7 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
   // ---- tasks, subblocks, sphere tables
   t->tasks.resize(ntasks);
   t->points.assign(ntasks, 0);
+  t->gbound.assign(ntasks, 0.0);
   std::map<std::pair<int, long long>, int> sphere_of;
   std::vector<long long> sphere_points;
   long long maxbuf = 0;
@@ -629,6 +666,7 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
         }
       t->points[s] = np;
     }
+    t->gbound[s] = contribution_bound(d, atom_positions + 3 * ia);
     // subblock bookkeeping
     const int bn = block_num_list[i] - 1;
     const bool new_sub = s == 0 || block_num_list[order[s - 1]] != block_num_list[i] ||
@@ -720,7 +758,7 @@ static Mode &get_mode(TaskList *t, const LDiffs &d) {
     m.d_coef_off = dalloc_copy(m.coef_off);
   }
   // work queues, descending cost
-  std::vector<std::pair<double, int>> items[2][kNumBuckets];
+  std::vector<std::pair<double, int>> items[2][kNumBuckets][2];
   for (int s = 0; s < t->ntasks; s++) {
     const TaskDesc &k = t->tasks[s];
     if (k.flags & TF_SKIP)
@@ -730,6 +768,8 @@ static Mode &get_mode(TaskList *t, const LDiffs &d) {
     if (b < 0)
       fail("contraction order lp=%d exceeds %d", lp, GB300_LP_MAX);
     const int g = (k.flags & TF_GENERAL) ? 1 : 0;
+    const int cls = (t->precision == GRID_GB300_MIXED && g == 0 &&
+                     t->gbound[s] <= t->mixed_threshold) ? 1 : 0;
     double cost;
     if (t->schedule == GRID_GB300_SCHEDULE_INPUT)
       cost = -(double)k.orig;
@@ -737,15 +777,16 @@ static Mode &get_mode(TaskList *t, const LDiffs &d) {
       cost = t->model_cost[s];
     else
       cost = (double)t->points[s] * (lp + 1) + 64.0 * (lp + 1) * (lp + 2);
-    items[g][b].push_back({cost, s});
+    items[g][b][cls].push_back({cost, s});
   }
   for (int g = 0; g < 2; g++)
-    for (int b = 0; b < kNumBuckets; b++) {
-      Queue &q = m.q[g][b];
+    for (int b = 0; b < kNumBuckets; b++)
+      for (int c = 0; c < 2; c++) {
+      Queue &q = m.q[g][b][c];
       if (q.d_idx)
         cudaFree(q.d_idx);
       q.d_idx = nullptr;
-      auto &v = items[g][b];
+      auto &v = items[g][b][c];
       std::stable_sort(v.begin(), v.end(), [](const std::pair<double, int> &x,
                                               const std::pair<double, int> &y) {
         return x.first > y.first;
@@ -827,6 +868,8 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
   }
   CK(cudaMemsetAsync(t->d_counters, 0, sizeof(int) * 64, s));
   GridArgs ga{};
+  ga.coef_stride = 1;
+  ga.grid_stride = 1;
   ga.tasks = t->d_tasks;
   ga.coef_off = m.d_coef_off;
   ga.coef = t->d_coef;
@@ -842,14 +885,16 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
   ga.error = t->d_error;
   int qi = 0;
   for (int g = 0; g < 2; g++)
-    for (int b = 0; b < kNumBuckets; b++) {
-      const Queue &q = m.q[g][b];
+    for (int b = 0; b < kNumBuckets; b++)
+      for (int c = 0; c < 2; c++) {
+      const Queue &q = m.q[g][b][c];
       if (!q.n)
         continue;
       ga.queue = q.d_idx;
       ga.nqueue = q.n;
       ga.counter = t->d_counters + qi++;
-      launch_collocate(ga, arith, g == 1, b, q.extent, 0, s);
+      ga.coef_stride = (c == 1) ? 2 : 1;
+      launch_collocate(ga, c == 1 ? (int)ARITH_FP32 : arith, g == 1, b, q.extent, 0, s);
       grid_library_counter_add(kBucketLp[b], GRID_BACKEND_GB300,
                                g ? GRID_COLLOCATE_GENERAL : GRID_COLLOCATE_ORTHO, q.n);
     }
@@ -887,6 +932,8 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
   CK(cudaMemsetAsync(t->d_counters, 0, sizeof(int) * 64, s));
   CK(cudaEventRecord(t->ev[1], s));
   GridArgs ga{};
+  ga.coef_stride = 1;
+  ga.grid_stride = 1;
   ga.tasks = t->d_tasks;
   ga.coef_off = m.d_coef_off;
   ga.coef_out = t->d_coef_int;
@@ -900,17 +947,19 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
   ga.error = t->d_error;
   int qi = 0;
   for (int g = 0; g < 2; g++)
-    for (int b = 0; b < kNumBuckets; b++) {
-      const Queue &q = m.q[g][b];
+    for (int b = 0; b < kNumBuckets; b++)
+      for (int c = 0; c < 2; c++) {
+      const Queue &q = m.q[g][b][c];
       if (!q.n)
         continue;
       ga.queue = q.d_idx;
       ga.nqueue = q.n;
       ga.counter = t->d_counters + qi++;
+      ga.grid_stride = (c == 1) ? 2 : 1;
       if (g == 1 && arith == ARITH_MIXED) // the general path runs in FP64 here
         for (int l = 0; l < t->nlevels; l++)
           ga.grids_in[l] = grids[l];
-      launch_integrate(ga, arith, g == 1, b, q.extent, 0, s);
+      launch_integrate(ga, c == 1 ? (int)ARITH_FP32 : arith, g == 1, b, q.extent, 0, s);
       grid_library_counter_add(kBucketLp[b], GRID_BACKEND_GB300,
                                g ? GRID_INTEGRATE_GENERAL : GRID_INTEGRATE_ORTHO, q.n);
     }
@@ -1178,11 +1227,46 @@ GB300_API void grid_gb300_set_precision(const grid_gb300_task_list *task_list, i
   if (precision != GRID_GB300_FP64 && precision != GRID_GB300_MIXED &&
       precision != GRID_GB300_FP32)
     fail("unknown precision mode %d", precision);
-  TL(task_list)->precision = precision;
+  TaskList *t = TL(task_list);
+  if (t->precision != precision) {
+    t->precision = precision;
+    t->sched_version++; // queues depend on the precision split
+  }
 }
 
 GB300_API int grid_gb300_get_precision(const grid_gb300_task_list *task_list) {
   return TL(task_list)->precision;
+}
+
+GB300_API void grid_gb300_set_mixed_threshold(const grid_gb300_task_list *task_list,
+                                              double threshold) {
+  TaskList *t = TL(task_list);
+  if (!(threshold >= 0.0))
+    fail("mixed threshold must be >= 0");
+  if (t->mixed_threshold != threshold) {
+    t->mixed_threshold = threshold;
+    t->sched_version++;
+  }
+}
+
+GB300_API void grid_gb300_mixed_split(const grid_gb300_task_list *task_list, double *frac_tasks,
+                                      double *frac_points) {
+  const TaskList *t = TL(task_list);
+  double nt = 0, nf = 0, pt = 0, pf = 0;
+  for (size_t s = 0; s < t->tasks.size(); s++) {
+    if (t->tasks[s].flags & (TF_SKIP | TF_GENERAL))
+      continue;
+    nt += 1;
+    pt += (double)t->points[s];
+    if (t->gbound[s] <= t->mixed_threshold) {
+      nf += 1;
+      pf += (double)t->points[s];
+    }
+  }
+  if (frac_tasks)
+    *frac_tasks = nt ? nf / nt : 0.0;
+  if (frac_points)
+    *frac_points = pt ? pf / pt : 0.0;
 }
 
 GB300_API void grid_gb300_set_schedule(const grid_gb300_task_list *task_list, int schedule) {

@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <type_traits>
 
 #include "gb300_internal.h"
 #include "numeric.cuh"
@@ -162,14 +163,14 @@ __device__ void fill_alpha(T *alpha, int la, int lb, int lp, const double ra[3],
   __syncwarp();
   for (int e = lane; e < 3 * na * nb; e += 32) {
     const int d = e / (na * nb), r = e % (na * nb), xb = r / na, xa = r % na;
-    const T pa = (T)(rp[d] - ra[d]), pb = (T)(rp[d] - rb[d]);
+    const T pa = T(rp[d] - ra[d]), pb = T(rp[d] - rb[d]);
     T *al = alpha + ((size_t)(d * nb + xb) * na + xa) * P;
     T powa = T(1);
     for (int k = 0; k <= xa; k++) {
-      const T wa = (T)c_binom[xa][k] * powa;
+      const T wa = T(c_binom[xa][k]) * powa;
       T powb = T(1);
       for (int m = 0; m <= xb; m++) {
-        al[xa - k + xb - m] += wa * (T)c_binom[xb][m] * powb;
+        al[xa - k + xb - m] += wa * T(c_binom[xb][m]) * powb;
         powb *= pb;
       }
       powa *= pa;
@@ -269,113 +270,130 @@ __device__ T cxyz_cijk_term(bool forward, const double *h, int lp, int lx, int l
               const int e = cidx(kx + ky + kz, jx + jy + jz, ix + iy + iz, lp);
               const double wgt = wx * wy * wz * fl;
               if (forward)
-                atomicAdd(&cijk_scatter[e], (T)(wgt * (double)cval));
+                atomicAdd(&cijk_scatter[e], T(wgt * to_double(cval)));
               else
-                acc += wgt * (double)cijk_gather[e];
+                acc += wgt * to_double(cijk_gather[e]);
             }
         }
     }
-  return (T)acc;
+  return T(acc);
 }
 
-template <typename T> struct CoefSmem {
-  // cab [n2][n1], alpha, cxyz, cijk (+ slack)
-  static __host__ __device__ size_t words(int n1, int n2, int la, int lb, int lp) {
-    return (size_t)n1 * n2 + 3 * (size_t)(la + 1) * (lb + 1) * (lp + 1) + 2 * (size_t)ncoset(lp) + 8;
-  }
-};
+// Per-warp shared memory of the coefficient / post kernels in 8-byte words:
+// cab (FP64) [n2][n1], cab in the working type, alpha, cxyz, cijk.
+__host__ __device__ inline size_t coef_smem_words(int n1, int n2, int la, int lb, int lp) {
+  return 2 * (size_t)n1 * n2 + 3 * (size_t)(la + 1) * (lb + 1) * (lp + 1) +
+         2 * (size_t)ncoset(lp) + 8;
+}
 
-// ------------------------------------------------------------------------
-// coefficients: one warp per task
-// ------------------------------------------------------------------------
+// Decode the Cartesian index i (0 .. ncoset(lmax)-1) into an orbital.
+__device__ __forceinline__ Orb orb_of_index(int i) {
+  int l = 0;
+  while (ncoset(l) <= i)
+    l++;
+  return orb_of(l, i - ncoset(l - 1));
+}
+
 // store of one coefficient in the grid kernels' arithmetic
-template <typename Tout, typename T>
-__device__ __forceinline__ void store_coef(void *out, size_t i, T v, bool as_fp64) {
-  if constexpr (std::is_same<Tout, dfloat>::value) {
-    if (as_fp64)
-      ((double *)out)[i] = (double)v;
+template <typename Tout, typename U>
+__device__ __forceinline__ void store_coef(void *out, size_t i, U v, bool as_fp64) {
+  if (as_fp64) {
+    ((double *)out)[i] = to_double(v);
+  } else if constexpr (std::is_same<Tout, dfloat>::value) {
+    if constexpr (std::is_same<U, dfloat>::value)
+      ((dfloat *)out)[i] = v;
     else
-      ((dfloat *)out)[i] = df_make((double)v);
+      ((dfloat *)out)[i] = df_make(to_double(v));
+  } else if constexpr (std::is_same<Tout, float>::value && std::is_same<U, float>::value) {
+    ((float *)out)[i] = v;
   } else {
-    ((Tout *)out)[i] = (Tout)v;
+    ((Tout *)out)[i] = (Tout)to_double(v);
   }
 }
 
-template <typename T, typename Tout>
-__global__ void __launch_bounds__(128) coefficients_kernel(CoefArgs a, int words_per_warp) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  T *ws = (T *)smem + (size_t)(threadIdx.x >> 5) * words_per_warp;
-  void *out = a.coef;
-  for (int t = gw; t < a.ntasks; t += nwarps) {
-    const TaskDesc d = a.tasks[t];
-    if (d.flags & TF_SKIP)
-      continue;
-    const SubblockDesc sb = a.subs[d.subblock];
-    const int la_max = d.la_max + a.d.la_max, lb_max = d.lb_max + a.d.lb_max;
-    const int lp = la_max + lb_max;
-    const int n1 = ncoset(la_max), n2 = ncoset(lb_max);
-    T *cab = ws;
-    T *alpha = cab + (size_t)n1 * n2;
-    T *cxyz = alpha + 3 * (size_t)(la_max + 1) * (lb_max + 1) * (lp + 1);
-    T *cijk = cxyz + ncoset(lp);
-    for (int e = lane; e < n1 * n2; e += 32)
-      cab[e] = T(0);
-    __syncwarp();
-    // P_ab -> C_ab
-    const CabW<T> w{cab, n1};
-    const double *pab = a.pab_cart + sb.cart_offset;
-    const int na = ncoset(d.la_max) - ncoset(d.la_min - 1);
-    const int nb = ncoset(d.lb_max) - ncoset(d.lb_min - 1);
-    for (int e = lane; e < na * nb; e += 32) {
-      const int ia = ncoset(d.la_min - 1) + e % na, ib = ncoset(d.lb_min - 1) + e / na;
-      // orbital of Cartesian index ia
-      int l = 0;
-      while (ncoset(l) <= ia)
-        l++;
-      const Orb oa = orb_of(l, ia - ncoset(l - 1));
-      int m = 0;
-      while (ncoset(m) <= ib)
-        m++;
-      const Orb ob = orb_of(m, ib - ncoset(m - 1));
-      const T p = (T)pab[(size_t)(d.o2 + ib) * sb.ncoa + d.o1 + ia];
-      prep_one<T>(a.func, oa, ob, (T)d.zeta, (T)d.zetb, p, w);
+// ------------------------------------------------------------------------
+// coefficients of one task (one warp): P_ab -> C_ab -> C_xyz (-> C_ijk)
+// ------------------------------------------------------------------------
+template <typename U, typename Tout>
+__device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *ws, int lane,
+                          bool as_fp64) {
+  const SubblockDesc sb = a.subs[d.subblock];
+  const int la_max = d.la_max + a.d.la_max, lb_max = d.lb_max + a.d.lb_max;
+  const int lp = la_max + lb_max;
+  const int n1 = ncoset(la_max), n2 = ncoset(lb_max);
+  double *cabd = ws;
+  U *cab = (U *)(cabd + (size_t)n1 * n2);
+  U *alpha = (U *)((double *)cab + (size_t)n1 * n2);
+  U *cxyz = (U *)((double *)alpha + 3 * (size_t)(la_max + 1) * (lb_max + 1) * (lp + 1));
+  U *cijk = (U *)((double *)cxyz + ncoset(lp));
+  for (int e = lane; e < n1 * n2; e += 32)
+    cabd[e] = 0.0;
+  __syncwarp();
+  // P_ab -> C_ab in FP64 (grid_prepare_pab.h; a few operations per element)
+  const CabW<double> w{cabd, n1};
+  const double *pab = a.pab_cart + sb.cart_offset;
+  const int na = ncoset(d.la_max) - ncoset(d.la_min - 1);
+  const int nb = ncoset(d.lb_max) - ncoset(d.lb_min - 1);
+  for (int e = lane; e < na * nb; e += 32) {
+    const int ia = ncoset(d.la_min - 1) + e % na, ib = ncoset(d.lb_min - 1) + e / na;
+    const double p = pab[(size_t)(d.o2 + ib) * sb.ncoa + d.o1 + ia];
+    prep_one<double>(a.func, orb_of_index(ia), orb_of_index(ib), d.zeta, d.zetb, p, w);
+  }
+  __syncwarp();
+  for (int e = lane; e < n1 * n2; e += 32)
+    cab[e] = U(cabd[e]);
+  const double *ra = a.atom_pos + 3 * d.iatom;
+  double rb[3];
+  for (int i = 0; i < 3; i++)
+    rb[i] = ra[i] + d.rab[i];
+  fill_alpha<U>(alpha, la_max, lb_max, lp, ra, rb, d.rp, lane);
+  const U pref = U(d.prefexp * ((d.iatom == d.jatom) ? 1.0 : 2.0));
+  const int nco = ncoset(lp);
+  const bool general = d.flags & TF_GENERAL;
+  for (int e = lane; e < nco; e += 32) {
+    int pz, py, px;
+    decode_cidx(e, lp, pz, py, px);
+    const U v = cab_cxyz_term<U>(cab, n1, alpha, la_max, lb_max, lp, px, py, pz) * pref;
+    if (general) {
+      cxyz[e] = v;
+      cijk[e] = U(0);
+    } else {
+      store_coef<Tout, U>(a.coef, (size_t)a.coef_off[t] + e, v, false);
     }
-    __syncwarp();
-    const double *ra = a.atom_pos + 3 * d.iatom;
-    double rb[3];
-    for (int i = 0; i < 3; i++)
-      rb[i] = ra[i] + d.rab[i];
-    fill_alpha<T>(alpha, la_max, lb_max, lp, ra, rb, d.rp, lane);
-    const double pref = d.prefexp * ((d.iatom == d.jatom) ? 1.0 : 2.0);
-    const int nco = ncoset(lp);
-    const bool general = d.flags & TF_GENERAL;
-    for (int e = lane; e < nco; e += 32) {
-      int pz, py, px;
-      decode_cidx(e, lp, pz, py, px);
-      const T v = cab_cxyz_term<T>(cab, n1, alpha, la_max, lb_max, lp, px, py, pz) * (T)pref;
-      if (general) {
-        cxyz[e] = v;
-        cijk[e] = T(0);
-      } else {
-        store_coef<Tout, T>(out, (size_t)a.coef_off[t] + e, v, false);
-      }
-    }
+  }
+  if constexpr (!std::is_same<U, dfloat>::value) {
     if (general) {
       __syncwarp();
       const double *h = a.levels->lv[d.level].dh;
       for (int e = lane; e < nco; e += 32) {
         int lz, ly, lx;
         decode_cidx(e, lp, lz, ly, lx);
-        cxyz_cijk_term<T>(true, h, lp, lx, ly, lz, cxyz[e], cijk, nullptr);
+        cxyz_cijk_term<U>(true, h, lp, lx, ly, lz, cxyz[e], cijk, nullptr);
       }
       __syncwarp();
       for (int e = lane; e < nco; e += 32)
-        store_coef<Tout, T>(out, (size_t)a.coef_off[t] + e, cijk[e], a.general_fp64);
+        store_coef<Tout, U>(a.coef, (size_t)a.coef_off[t] + e, cijk[e], as_fp64);
     }
-    __syncwarp();
+  }
+  __syncwarp();
+}
+
+// U: working type of ortho tasks; general tasks run in FP64 when U is dfloat
+template <typename U, typename Tout>
+__global__ void __launch_bounds__(128) coefficients_kernel(CoefArgs a, int words_per_warp) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  double *ws = (double *)smem + (size_t)(threadIdx.x >> 5) * words_per_warp;
+  for (int t = gw; t < a.ntasks; t += nwarps) {
+    const TaskDesc d = a.tasks[t];
+    if (d.flags & TF_SKIP)
+      continue;
+    if (std::is_same<U, dfloat>::value && (d.flags & TF_GENERAL))
+      coef_task<double, Tout>(a, t, d, ws, lane, a.general_fp64);
+    else
+      coef_task<U, Tout>(a, t, d, ws, lane, false);
   }
 }
 
@@ -425,14 +443,85 @@ __device__ T vab(const VabCtx<T> &x, bool tau, int kind, int i, int j, Orb a, Or
   return s;
 }
 
-template <typename T>
+template <typename U>
+__device__ void post_task(const PostArgs &a, int t, const TaskDesc &d, double *ws, int lane,
+                          double f[6], double v[9]) {
+  const SubblockDesc sb = a.subs[d.subblock];
+  const int la_max = d.la_max + a.d.la_max, lb_max = d.lb_max + a.d.lb_max;
+  const int lp = la_max + lb_max;
+  const int m1 = ncoset(la_max), m2 = ncoset(lb_max);
+  U *cab = (U *)ws;
+  U *alpha = (U *)(ws + (size_t)m1 * m2);
+  U *cxyz = (U *)((double *)alpha + 3 * (size_t)(la_max + 1) * (lb_max + 1) * (lp + 1));
+  U *cijk = (U *)((double *)cxyz + ncoset(lp));
+  const int nco = ncoset(lp);
+  const double *src = a.coef + a.coef_off[t];
+  const bool general = d.flags & TF_GENERAL;
+  for (int e = lane; e < nco; e += 32) {
+    if (general)
+      cijk[e] = U(src[e]);
+    else
+      cxyz[e] = U(src[e]);
+  }
+  __syncwarp();
+  if constexpr (!std::is_same<U, dfloat>::value) {
+    if (general) {
+      const double *h = a.levels->lv[d.level].dh;
+      for (int e = lane; e < nco; e += 32) {
+        int lz, ly, lx;
+        decode_cidx(e, lp, lz, ly, lx);
+        cxyz[e] = cxyz_cijk_term<U>(false, h, lp, lx, ly, lz, U(0), nullptr, cijk);
+      }
+      __syncwarp();
+    }
+  }
+  const double *ra = a.atom_pos + 3 * d.iatom;
+  double rb[3];
+  for (int i = 0; i < 3; i++)
+    rb[i] = ra[i] + d.rab[i];
+  fill_alpha<U>(alpha, la_max, lb_max, lp, ra, rb, d.rp, lane);
+  const U pref = U(d.prefexp);
+  for (int e = lane; e < m1 * m2; e += 32) {
+    const Orb oa = orb_of_index(e % m1), ob = orb_of_index(e / m1);
+    cab[e] = cxyz_cab_term<U>(cxyz, alpha, la_max, lb_max, lp, oa, ob) * pref;
+  }
+  __syncwarp();
+  VabCtx<U> x{cab, m1, U(d.zeta), U(d.zetb), {U(d.rab[0]), U(d.rab[1]), U(d.rab[2])}};
+  const bool tau = a.compute_tau;
+  const int na = ncoset(d.la_max) - ncoset(d.la_min - 1);
+  const int nb = ncoset(d.lb_max) - ncoset(d.lb_min - 1);
+  const double *pab = a.pab_cart ? a.pab_cart + sb.cart_offset : nullptr;
+  double *hab = a.hab_cart + sb.cart_offset;
+  for (int e = lane; e < na * nb; e += 32) {
+    const int ia = ncoset(d.la_min - 1) + e % na, ib = ncoset(d.lb_min - 1) + e / na;
+    const Orb oa = orb_of_index(ia), ob = orb_of_index(ib);
+    const size_t el = (size_t)(d.o2 + ib) * sb.ncoa + d.o1 + ia;
+    atomicAdd(&hab[el], to_double(vab<U>(x, tau, V_HAB, 0, 0, oa, ob)));
+    if (a.forces || a.virial) {
+      const double p = pab[el];
+      if (a.forces)
+        for (int i = 0; i < 3; i++) {
+          f[i] += p * to_double(vab<U>(x, tau, V_FA, i, 0, oa, ob));
+          f[3 + i] += p * to_double(vab<U>(x, tau, V_FB, i, 0, oa, ob));
+        }
+      if (a.virial)
+        for (int i = 0; i < 3; i++)
+          for (int j = 0; j < 3; j++)
+            v[i * 3 + j] += p * (to_double(vab<U>(x, tau, V_VA, i, j, oa, ob)) +
+                                 to_double(vab<U>(x, tau, V_VB, i, j, oa, ob)));
+    }
+  }
+  __syncwarp();
+}
+
+template <typename U>
 __global__ void __launch_bounds__(128) post_kernel(PostArgs a, int words_per_warp) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ double vir_cta[9];
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  T *ws = (T *)smem + (size_t)(threadIdx.x >> 5) * words_per_warp;
+  double *ws = (double *)smem + (size_t)(threadIdx.x >> 5) * words_per_warp;
   if (threadIdx.x < 9)
     vir_cta[threadIdx.x] = 0.0;
   __syncthreads();
@@ -440,83 +529,11 @@ __global__ void __launch_bounds__(128) post_kernel(PostArgs a, int words_per_war
     const TaskDesc d = a.tasks[t];
     if (d.flags & TF_SKIP)
       continue;
-    const SubblockDesc sb = a.subs[d.subblock];
-    const int la_max = d.la_max + a.d.la_max, lb_max = d.lb_max + a.d.lb_max;
-    const int lp = la_max + lb_max;
-    const int m1 = ncoset(la_max), m2 = ncoset(lb_max);
-    T *cab = ws;
-    T *alpha = cab + (size_t)m1 * m2;
-    T *cxyz = alpha + 3 * (size_t)(la_max + 1) * (lb_max + 1) * (lp + 1);
-    T *cijk = cxyz + ncoset(lp);
-    const int nco = ncoset(lp);
-    const double *src = a.coef + a.coef_off[t];
-    const bool general = d.flags & TF_GENERAL;
-    for (int e = lane; e < nco; e += 32) {
-      if (general)
-        cijk[e] = (T)src[e];
-      else
-        cxyz[e] = (T)src[e];
-    }
-    __syncwarp();
-    if (general) {
-      const double *h = a.levels->lv[d.level].dh;
-      for (int e = lane; e < nco; e += 32) {
-        int lz, ly, lx;
-        decode_cidx(e, lp, lz, ly, lx);
-        cxyz[e] = cxyz_cijk_term<T>(false, h, lp, lx, ly, lz, T(0), nullptr, cijk);
-      }
-      __syncwarp();
-    }
-    const double *ra = a.atom_pos + 3 * d.iatom;
-    double rb[3];
-    for (int i = 0; i < 3; i++)
-      rb[i] = ra[i] + d.rab[i];
-    fill_alpha<T>(alpha, la_max, lb_max, lp, ra, rb, d.rp, lane);
-    const T pref = (T)d.prefexp;
-    for (int e = lane; e < m1 * m2; e += 32) {
-      const int ia = e % m1, ib = e / m1;
-      int l = 0;
-      while (ncoset(l) <= ia)
-        l++;
-      int m = 0;
-      while (ncoset(m) <= ib)
-        m++;
-      const Orb oa = orb_of(l, ia - ncoset(l - 1)), ob = orb_of(m, ib - ncoset(m - 1));
-      cab[e] = cxyz_cab_term<T>(cxyz, alpha, la_max, lb_max, lp, oa, ob) * pref;
-    }
-    __syncwarp();
-    VabCtx<T> x{cab, m1, (T)d.zeta, (T)d.zetb, {(T)d.rab[0], (T)d.rab[1], (T)d.rab[2]}};
-    const bool tau = a.compute_tau;
-    const int na = ncoset(d.la_max) - ncoset(d.la_min - 1);
-    const int nb = ncoset(d.lb_max) - ncoset(d.lb_min - 1);
     double f[6] = {0, 0, 0, 0, 0, 0}, v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    const double *pab = a.pab_cart ? a.pab_cart + sb.cart_offset : nullptr;
-    double *hab = a.hab_cart + sb.cart_offset;
-    for (int e = lane; e < na * nb; e += 32) {
-      const int ia = ncoset(d.la_min - 1) + e % na, ib = ncoset(d.lb_min - 1) + e / na;
-      int l = 0;
-      while (ncoset(l) <= ia)
-        l++;
-      int m = 0;
-      while (ncoset(m) <= ib)
-        m++;
-      const Orb oa = orb_of(l, ia - ncoset(l - 1)), ob = orb_of(m, ib - ncoset(m - 1));
-      const size_t el = (size_t)(d.o2 + ib) * sb.ncoa + d.o1 + ia;
-      atomicAdd(&hab[el], (double)vab<T>(x, tau, V_HAB, 0, 0, oa, ob));
-      if (a.forces || a.virial) {
-        const double p = pab[el];
-        if (a.forces)
-          for (int i = 0; i < 3; i++) {
-            f[i] += p * (double)vab<T>(x, tau, V_FA, i, 0, oa, ob);
-            f[3 + i] += p * (double)vab<T>(x, tau, V_FB, i, 0, oa, ob);
-          }
-        if (a.virial)
-          for (int i = 0; i < 3; i++)
-            for (int j = 0; j < 3; j++)
-              v[i * 3 + j] += p * ((double)vab<T>(x, tau, V_VA, i, j, oa, ob) +
-                                   (double)vab<T>(x, tau, V_VB, i, j, oa, ob));
-      }
-    }
+    if (std::is_same<U, dfloat>::value && (d.flags & TF_GENERAL))
+      post_task<double>(a, t, d, ws, lane, f, v);
+    else
+      post_task<U>(a, t, d, ws, lane, f, v);
     const double scale = (d.iatom == d.jatom) ? 1.0 : 2.0;
     if (a.forces) {
       for (int i = 0; i < 6; i++) {
@@ -542,7 +559,6 @@ __global__ void __launch_bounds__(128) post_kernel(PostArgs a, int words_per_war
         for (int i = 0; i < 9; i++)
           atomicAdd(&vir_cta[i], scale * v[i]);
     }
-    __syncwarp();
   }
   __syncthreads();
   if (a.virial && threadIdx.x < 9)
@@ -679,14 +695,14 @@ void launch_contract_hab(const ContractArgs &a, cudaStream_t s) {
   count_launch();
 }
 
-template <typename T, typename Tout>
+template <typename U, typename Tout>
 static void launch_coef_t(const CoefArgs &a, int words_per_warp, cudaStream_t s) {
-  const size_t per_warp = (size_t)words_per_warp * sizeof(T);
+  const size_t per_warp = (size_t)words_per_warp * 8;
   const int nw = warps_for(per_warp);
   if (nw < 1)
     return launch_error("coefficients: angular momenta too large for shared memory");
   const size_t smem = nw * per_warp;
-  auto k = coefficients_kernel<T, Tout>;
+  auto k = coefficients_kernel<U, Tout>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   k<<<grid_size_for(a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_warp);
   count_launch();
@@ -699,34 +715,38 @@ void launch_coefficients(const CoefArgs &a, int arith, int words_per_warp, cudaS
   if (arith == ARITH_FP32)
     launch_coef_t<float, float>(a, words_per_warp, s);
   else if (arith == ARITH_MIXED)
-    launch_coef_t<double, dfloat>(a, words_per_warp, s);
+    launch_coef_t<dfloat, dfloat>(a, words_per_warp, s);
   else
     launch_coef_t<double, double>(a, words_per_warp, s);
 }
 
-void launch_post(const PostArgs &a, int arith, int words_per_warp, cudaStream_t s) {
-  const bool fp32 = arith == ARITH_FP32;
-  if (a.ntasks == 0)
-    return;
-  upload_binomials();
-  const size_t per_warp = (size_t)words_per_warp * (fp32 ? 4 : 8);
+template <typename U>
+static void launch_post_t(const PostArgs &a, int words_per_warp, cudaStream_t s) {
+  const size_t per_warp = (size_t)words_per_warp * 8;
   const int nw = warps_for(per_warp);
   if (nw < 1)
-    return launch_error("coefficients: angular momenta too large for shared memory");
+    return launch_error("post-processing: angular momenta too large for shared memory");
   const size_t smem = nw * per_warp;
-  if (fp32) {
-    cudaFuncSetAttribute(post_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    post_kernel<float><<<grid_size_for(a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_warp);
-  } else {
-    cudaFuncSetAttribute(post_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    post_kernel<double><<<grid_size_for(a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_warp);
-  }
+  auto k = post_kernel<U>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k<<<grid_size_for(a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_warp);
   count_launch();
 }
 
+void launch_post(const PostArgs &a, int arith, int words_per_warp, cudaStream_t s) {
+  if (a.ntasks == 0)
+    return;
+  upload_binomials();
+  if (arith == ARITH_FP32)
+    launch_post_t<float>(a, words_per_warp, s);
+  else if (arith == ARITH_MIXED)
+    launch_post_t<dfloat>(a, words_per_warp, s);
+  else
+    launch_post_t<double>(a, words_per_warp, s);
+}
+
 size_t coef_words(int la, int lb) {
-  const int lp = la + lb;
-  return CoefSmem<double>::words(ncoset(la), ncoset(lb), la, lb, lp);
+  return coef_smem_words(ncoset(la), ncoset(lb), la, lb, la + lb);
 }
 
 } // namespace gb300

@@ -164,6 +164,8 @@ struct GridArgs {
   const void *grids_in[GB300_MAX_LEVELS];  // integrate sources (per arith)
   LevelSet levels;
   LDiffs d;
+  int coef_stride;   // FP32 kernels: floats per stored coefficient (2: dfloat buffer)
+  int grid_stride;   // FP32 integrate: floats per grid point (2: hi/lo pairs)
   int nwarps_total;
   long long *task_cycles; // optional per-task timings (clock64)
   int *error;             // device error word

@@ -165,10 +165,12 @@ __device__ __forceinline__ void grid_add(double *g, float *glo, size_t i,
 
 // grid read for integrate
 template <typename N>
-__device__ __forceinline__ typename Num<N>::T grid_get(const void *g, size_t i) {
+__device__ __forceinline__ typename Num<N>::T grid_get(const void *g, size_t i, int stride = 1) {
   if constexpr (std::is_same<N, dfloat>::value) {
     const float2 v = __ldg(reinterpret_cast<const float2 *>(g) + i);
     return dfloat{v.x, v.y};
+  } else if constexpr (std::is_same<N, float>::value) {
+    return __ldg(reinterpret_cast<const float *>(g) + i * stride);
   } else {
     return __ldg(reinterpret_cast<const typename Num<N>::T *>(g) + i);
   }
@@ -238,9 +240,15 @@ __global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
       continue;
     }
     const int nco = ncoset(lp), ntr = ntri(lp);
-    const T *csrc = coefs + a.coef_off[t];
-    for (int e = lane; e < nco; e += 32)
-      coef[e] = csrc[e];
+    if constexpr (std::is_same<T, float>::value) {
+      const float *csrc = (const float *)a.coef + (size_t)a.coef_off[t] * a.coef_stride;
+      for (int e = lane; e < nco; e += 32)
+        coef[e] = csrc[(size_t)e * a.coef_stride];
+    } else {
+      const T *csrc = coefs + a.coef_off[t];
+      for (int e = lane; e < nco; e += 32)
+        coef[e] = csrc[e];
+    }
     fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane);
     __syncwarp();
 
@@ -369,6 +377,7 @@ __global__ void __launch_bounds__(128) integrate_ortho(GridArgs a, int wmax) {
     __syncwarp();
 
     const void *grid = a.grids_in[d.level];
+    const int gstride = a.grid_stride;
     const size_t nx = L.npts_local[0], nxy = nx * L.npts_local[1];
     const bool lane_on = cg.grp < cg.G;
 
@@ -399,9 +408,11 @@ __global__ void __launch_bounds__(128) integrate_ortho(GridArgs a, int wmax) {
             continue;
           const int j2c = j2 <= jend ? j2 : jend;
           const T v1 =
-              in1 ? grid_get<N>(grid, zoff + (size_t)map[cg.w + j + cg.cmax] * nx + ig) : M::zero();
+              in1 ? grid_get<N>(grid, zoff + (size_t)map[cg.w + j + cg.cmax] * nx + ig, gstride)
+                  : M::zero();
           const T v2 =
-              in2 ? grid_get<N>(grid, zoff + (size_t)map[cg.w + j2c + cg.cmax] * nx + ig) : M::zero();
+              in2 ? grid_get<N>(grid, zoff + (size_t)map[cg.w + j2c + cg.cmax] * nx + ig, gstride)
+                  : M::zero();
           T p1[PP], p2[PP];
           load_row<T, PP>(pol + (size_t)(cg.w + j + cg.cmax) * PP, p1);
           load_row<T, PP>(pol + (size_t)(cg.w + j2c + cg.cmax) * PP, p2);

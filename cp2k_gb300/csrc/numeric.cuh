@@ -19,12 +19,18 @@ namespace gb300 {
 
 struct dfloat {
   float h, l;
+  dfloat() = default;
+  __host__ __device__ constexpr dfloat(float hi, float lo) : h(hi), l(lo) {}
+  __host__ __device__ constexpr dfloat(float x) : h(x), l(0.f) {}
+  __host__ __device__ constexpr dfloat(int x) : h((float)x), l(0.f) {}
+  __device__ explicit dfloat(double x);
 };
 
 __device__ __forceinline__ dfloat df_make(double x) {
   const float h = (float)x;
   return dfloat{h, (float)(x - (double)h)};
 }
+__device__ __forceinline__ dfloat::dfloat(double x) : h((float)x), l((float)(x - (double)(float)x)) {}
 
 // acc + a*b
 __device__ __forceinline__ dfloat df_fma(dfloat acc, dfloat a, dfloat b) {
@@ -65,6 +71,18 @@ __device__ __forceinline__ dfloat df_add(dfloat a, dfloat b) {
   const float h = s + t;
   return dfloat{h, t - (h - s)};
 }
+
+__device__ __forceinline__ dfloat operator+(dfloat a, dfloat b) { return df_add(a, b); }
+__device__ __forceinline__ dfloat operator-(dfloat a) { return dfloat{-a.h, -a.l}; }
+__device__ __forceinline__ dfloat operator-(dfloat a, dfloat b) { return df_add(a, -b); }
+__device__ __forceinline__ dfloat operator*(dfloat a, dfloat b) { return df_mul(a, b); }
+__device__ __forceinline__ dfloat &operator+=(dfloat &a, dfloat b) { return a = df_add(a, b); }
+__device__ __forceinline__ dfloat &operator-=(dfloat &a, dfloat b) { return a = df_add(a, -b); }
+__device__ __forceinline__ dfloat &operator*=(dfloat &a, dfloat b) { return a = df_mul(a, b); }
+__device__ __forceinline__ bool operator!=(dfloat a, dfloat b) { return a.h != b.h || a.l != b.l; }
+__device__ __forceinline__ double to_double(dfloat a) { return (double)a.h + (double)a.l; }
+__device__ __forceinline__ double to_double(double a) { return a; }
+__device__ __forceinline__ double to_double(float a) { return (double)a; }
 
 __device__ __forceinline__ dfloat df_shfl_xor(dfloat v, int o) {
   return dfloat{__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};

@@ -84,6 +84,8 @@ def lib():
         L.grid_gb300_set_precision.argtypes = [vp, C.c_int]
         L.grid_gb300_get_precision.argtypes = [vp]
         L.grid_gb300_set_schedule.argtypes = [vp, C.c_int]
+        L.grid_gb300_set_mixed_threshold.argtypes = [vp, C.c_double]
+        L.grid_gb300_mixed_split.argtypes = [vp, vp, vp]
         L.grid_gb300_task_list_info.argtypes = [vp, vp, vp, vp, vp]
         L.grid_gb300_task_sizes.argtypes = [vp, vp, vp]
         L.grid_gb300_last_timings.argtypes = [vp, vp]
@@ -204,6 +206,14 @@ class GridTaskList:
 
     def set_schedule(self, schedule: int):
         lib().grid_gb300_set_schedule(self.impl, int(schedule))
+
+    def set_mixed_threshold(self, tau: float):
+        lib().grid_gb300_set_mixed_threshold(self.impl, float(tau))
+
+    def mixed_split(self):
+        ft, fp = C.c_double(), C.c_double()
+        lib().grid_gb300_mixed_split(self.impl, C.byref(ft), C.byref(fp))
+        return ft.value, fp.value
 
     def sizes(self):
         """(grid points visited, lp) per task in input order."""

@@ -263,6 +263,17 @@ int grid_gb300_get_precision(const grid_gb300_task_list *task_list);
 void grid_gb300_set_schedule(const grid_gb300_task_list *task_list,
                              int schedule);
 
+/* Mixed path: tasks whose contribution bound (Gaussian-product prefactor x
+ * polynomial maxima, for density-matrix elements of magnitude <= 1) is at
+ * most `threshold` run in plain FP32, the others in double-float.
+ * 0 runs every orthorhombic task in double-float.  Default 1e-3. */
+void grid_gb300_set_mixed_threshold(const grid_gb300_task_list *task_list,
+                                    double threshold);
+/* Share of orthorhombic tasks (and of their grid points) that the mixed path
+ * currently runs in plain FP32. */
+void grid_gb300_mixed_split(const grid_gb300_task_list *task_list,
+                            double *frac_tasks, double *frac_points);
+
 /* Device-resident variants: pab/hab/grid pointers are device addresses
  * (FP64), grids[level] laid out x-fastest as npts_local.  The work is
  * enqueued on `stream` (a cudaStream_t passed as void*, NULL = the legacy
