@@ -17,7 +17,9 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--config", default="c2_512atoms", choices=sorted(W.CONFIGS))
     ap.add_argument("--scale", type=float, default=1.0)
-    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed", "fp32"])
+    ap.add_argument("--threshold", type=float, default=None,
+                    help="mixed path: contribution bound below which tasks run in FP32")
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--forces", action="store_true")
     args = ap.parse_args()
@@ -27,7 +29,10 @@ def main():
     grids = [torch.empty(n, dtype=torch.float64, device="cuda") for n in inp.grid_sizes()]
     hab = torch.empty(inp.buffer_size, dtype=torch.float64, device="cuda")
     f = torch.empty((inp.natoms, 3), dtype=torch.float64, device="cuda") if args.forces else None
-    tl = G.GridTaskList(inp, precision=G.MIXED if args.precision == "mixed" else G.FP64)
+    tl = G.GridTaskList(inp, precision={"mixed": G.MIXED, "fp64": G.FP64,
+                                        "fp32": G.FP32}[args.precision])
+    if args.threshold is not None:
+        tl.set_mixed_threshold(args.threshold)
     s = torch.cuda.current_stream()
     for step in range(args.steps):
         tl.collocate_device(100, pab, grids, stream=s)
