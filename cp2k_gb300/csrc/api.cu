@@ -235,14 +235,20 @@ struct Queue {
   int *d_idx = nullptr;
   int n = 0;
   int extent = 0; // ortho: max cube width; general: max j-range
+  int general = 0, bucket = 0;
+  int fp32 = 0; // mixed path: this queue runs in plain FP32
 };
+
+// cube widths up to this share one work queue; wider cubes get their own so
+// that the common small cubes run with small per-warp tables (more warps)
+constexpr int kSmallExtent = 34;
 
 struct Mode { // everything that depends on the l shifts of a call
   LDiffs d;
   std::vector<int> coef_off; // per task (block order)
   int *d_coef_off = nullptr;
   size_t coef_total = 0;
-  Queue q[2][kNumBuckets][2]; // [general][bucket][class: 0 = arith, 1 = FP32]
+  std::vector<Queue> queues; // launch order
   int coef_words = 0;      // per-warp shared memory words of coefficient/post
   int sched_version = -1;
 };
@@ -263,6 +269,8 @@ struct TaskList {
   std::vector<long long> points; // per task (block order)
   std::vector<float> model_cost; // per task, empty unless a model was applied
   std::vector<double> gbound;    // per task bound of |contribution| for |P| <= 1
+  std::vector<float2> seeds;     // per task [3][6] dfloat recurrence seeds (ortho)
+  float2 *d_seeds = nullptr;
   double mixed_threshold = 1e-3; // mixed path: tasks with gbound <= this run FP32
   std::vector<int> npts_local;   // [nlevels][3]
   size_t cart_total = 0;
@@ -428,7 +436,7 @@ template <typename T> static T *dalloc_copy(const std::vector<T> &v) {
 }
 
 static void free_device(TaskList *t) {
-  void *ptrs[] = {t->d_tasks, t->d_subs, t->d_sph, t->d_sph_tab, t->d_atom_pos, t->d_sphi,
+  void *ptrs[] = {t->d_seeds, t->d_tasks, t->d_subs, t->d_sph, t->d_sph_tab, t->d_atom_pos, t->d_sphi,
                   t->d_levels, t->d_pab_cart, t->d_hab_cart, t->d_coef, t->d_coef_int,
                   t->d_forces, t->d_virial, t->d_counters, t->d_error, t->d_cycles};
   for (void *p : ptrs)
@@ -443,11 +451,9 @@ static void free_device(TaskList *t) {
   for (auto &kv : t->modes) {
     if (kv.second.d_coef_off)
       cudaFree(kv.second.d_coef_off);
-    for (auto &qg : kv.second.q)
-      for (auto &qb : qg)
-        for (auto &q : qb)
-          if (q.d_idx)
-            cudaFree(q.d_idx);
+    for (auto &q : kv.second.queues)
+      if (q.d_idx)
+        cudaFree(q.d_idx);
   }
   for (auto &e : t->ev)
     if (e)
@@ -549,6 +555,7 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
   t->tasks.resize(ntasks);
   t->points.assign(ntasks, 0);
   t->gbound.assign(ntasks, 0.0);
+  t->seeds.assign((size_t)ntasks * 18, make_float2(0.f, 0.f));
   std::map<std::pair<int, long long>, int> sphere_of;
   std::vector<long long> sphere_points;
   long long maxbuf = 0;
@@ -619,6 +626,16 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
             fail("task %d: cube does not fit into the local grid of level %d", i, lev);
         }
       t->points[s] = sphere_points[d.sphere];
+      // FP64 seeds of the dfloat Gaussian recurrences (grid_kernels.cu)
+      for (int dir = 0; dir < 3; dir++) {
+        const double h = L.dh[dir * 4], r = d.roff[dir], z = d.zetp;
+        const double v[6] = {exp(-z * r * r), exp(-z * h * (h - 2.0 * r)),
+                             exp(-z * h * (h + 2.0 * r)), exp(-2.0 * z * h * h), h, -r};
+        for (int q = 0; q < 6; q++) {
+          const float hi = (float)v[q];
+          t->seeds[(size_t)s * 18 + dir * 6 + q] = make_float2(hi, (float)(v[q] - (double)hi));
+        }
+      }
     } else {
       // general_cijk_to_grid (grid_ref_collint.h:609-640)
       d.flags |= TF_GENERAL;
@@ -710,6 +727,7 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
   for (auto &e : t->ev)
     CK(cudaEventCreate(&e));
   t->d_tasks = dalloc_copy(t->tasks);
+  t->d_seeds = dalloc_copy(t->seeds);
   t->d_subs = dalloc_copy(t->subs);
   t->d_sph = dalloc_copy(t->sph);
   t->d_sph_tab = dalloc_copy(t->sph_tab);
@@ -758,7 +776,8 @@ static Mode &get_mode(TaskList *t, const LDiffs &d) {
     m.d_coef_off = dalloc_copy(m.coef_off);
   }
   // work queues, descending cost
-  std::vector<std::pair<double, int>> items[2][kNumBuckets][2];
+  // work queues: (general, lp bucket, FP32 class, size class), descending cost
+  std::map<int, std::vector<std::pair<double, int>>> items;
   for (int s = 0; s < t->ntasks; s++) {
     const TaskDesc &k = t->tasks[s];
     if (k.flags & TF_SKIP)
@@ -770,6 +789,8 @@ static Mode &get_mode(TaskList *t, const LDiffs &d) {
     const int g = (k.flags & TF_GENERAL) ? 1 : 0;
     const int cls = (t->precision == GRID_GB300_MIXED && g == 0 &&
                      t->gbound[s] <= t->mixed_threshold) ? 1 : 0;
+    const int ext = g == 0 ? 2 * t->sph[k.sphere].cmax + 2 : k.imax[1] - k.center[1] + 1;
+    const int sz = ext <= kSmallExtent ? 0 : 1;
     double cost;
     if (t->schedule == GRID_GB300_SCHEDULE_INPUT)
       cost = -(double)k.orig;
@@ -777,35 +798,49 @@ static Mode &get_mode(TaskList *t, const LDiffs &d) {
       cost = t->model_cost[s];
     else
       cost = (double)t->points[s] * (lp + 1) + 64.0 * (lp + 1) * (lp + 2);
-    items[g][b][cls].push_back({cost, s});
+    items[((g * kNumBuckets + b) * 2 + cls) * 2 + sz].push_back({cost, s});
   }
-  for (int g = 0; g < 2; g++)
-    for (int b = 0; b < kNumBuckets; b++)
-      for (int c = 0; c < 2; c++) {
-      Queue &q = m.q[g][b][c];
-      if (q.d_idx)
-        cudaFree(q.d_idx);
-      q.d_idx = nullptr;
-      auto &v = items[g][b][c];
-      std::stable_sort(v.begin(), v.end(), [](const std::pair<double, int> &x,
-                                              const std::pair<double, int> &y) {
-        return x.first > y.first;
-      });
-      std::vector<int> idx(v.size());
-      int ext = 1;
-      for (size_t i = 0; i < v.size(); i++) {
-        idx[i] = v[i].second;
-        const TaskDesc &k = t->tasks[idx[i]];
-        if (g == 0)
-          ext = std::max(ext, 2 * t->sph[k.sphere].cmax + 2);
-        else
-          ext = std::max(ext, k.imax[1] - k.center[1] + 1);
-      }
-      q.n = (int)idx.size();
-      q.extent = ext;
-      if (q.n)
-        q.d_idx = dalloc_copy(idx);
+  for (auto &q : m.queues)
+    if (q.d_idx)
+      cudaFree(q.d_idx);
+  m.queues.clear();
+  // heavier classes first: large cubes, then the arithmetic of the mode, FP32 last
+  std::vector<int> keys;
+  for (auto &kv : items)
+    keys.push_back(kv.first);
+  std::stable_sort(keys.begin(), keys.end(), [](int x, int y) {
+    const int cx = (x >> 1) & 1, cy = (y >> 1) & 1, sx = x & 1, sy = y & 1;
+    if (cx != cy)
+      return cx < cy;
+    if (sx != sy)
+      return sx > sy;
+    return x < y;
+  });
+  for (int key : keys) {
+    auto &v = items[key];
+    std::stable_sort(v.begin(), v.end(), [](const std::pair<double, int> &x,
+                                            const std::pair<double, int> &y) {
+      return x.first > y.first;
+    });
+    Queue q;
+    q.general = key / (2 * 2 * kNumBuckets);
+    q.bucket = (key / 4) % kNumBuckets;
+    q.fp32 = (key >> 1) & 1;
+    std::vector<int> idx(v.size());
+    int ext = 1;
+    for (size_t i = 0; i < v.size(); i++) {
+      idx[i] = v[i].second;
+      const TaskDesc &k = t->tasks[idx[i]];
+      if (q.general == 0)
+        ext = std::max(ext, 2 * t->sph[k.sphere].cmax + 2);
+      else
+        ext = std::max(ext, k.imax[1] - k.center[1] + 1);
     }
+    q.n = (int)idx.size();
+    q.extent = ext;
+    q.d_idx = dalloc_copy(idx);
+    m.queues.push_back(q);
+  }
   m.sched_version = t->sched_version;
   return m;
 }
@@ -882,22 +917,19 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
   ga.levels = t->levels;
   ga.d = d;
   ga.task_cycles = t->d_cycles;
+  ga.seeds = t->d_seeds;
   ga.error = t->d_error;
   int qi = 0;
-  for (int g = 0; g < 2; g++)
-    for (int b = 0; b < kNumBuckets; b++)
-      for (int c = 0; c < 2; c++) {
-      const Queue &q = m.q[g][b][c];
-      if (!q.n)
-        continue;
-      ga.queue = q.d_idx;
-      ga.nqueue = q.n;
-      ga.counter = t->d_counters + qi++;
-      ga.coef_stride = (c == 1) ? 2 : 1;
-      launch_collocate(ga, c == 1 ? (int)ARITH_FP32 : arith, g == 1, b, q.extent, 0, s);
-      grid_library_counter_add(kBucketLp[b], GRID_BACKEND_GB300,
-                               g ? GRID_COLLOCATE_GENERAL : GRID_COLLOCATE_ORTHO, q.n);
-    }
+  for (const Queue &q : m.queues) {
+    ga.queue = q.d_idx;
+    ga.nqueue = q.n;
+    ga.counter = t->d_counters + qi++;
+    ga.coef_stride = q.fp32 ? 2 : 1;
+    launch_collocate(ga, q.fp32 ? (int)ARITH_FP32 : arith, q.general == 1, q.bucket, q.extent,
+                     0, s);
+    grid_library_counter_add(kBucketLp[q.bucket], GRID_BACKEND_GB300,
+                             q.general ? GRID_COLLOCATE_GENERAL : GRID_COLLOCATE_ORTHO, q.n);
+  }
   if (arith == ARITH_MIXED)
     for (int l = 0; l < t->nlevels; l++) {
       const int *n = &t->npts_local[3 * l];
@@ -944,25 +976,22 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
   ga.levels = t->levels;
   ga.d = d;
   ga.task_cycles = t->d_cycles;
+  ga.seeds = t->d_seeds;
   ga.error = t->d_error;
   int qi = 0;
-  for (int g = 0; g < 2; g++)
-    for (int b = 0; b < kNumBuckets; b++)
-      for (int c = 0; c < 2; c++) {
-      const Queue &q = m.q[g][b][c];
-      if (!q.n)
-        continue;
-      ga.queue = q.d_idx;
-      ga.nqueue = q.n;
-      ga.counter = t->d_counters + qi++;
-      ga.grid_stride = (c == 1) ? 2 : 1;
-      if (g == 1 && arith == ARITH_MIXED) // the general path runs in FP64 here
-        for (int l = 0; l < t->nlevels; l++)
-          ga.grids_in[l] = grids[l];
-      launch_integrate(ga, c == 1 ? (int)ARITH_FP32 : arith, g == 1, b, q.extent, 0, s);
-      grid_library_counter_add(kBucketLp[b], GRID_BACKEND_GB300,
-                               g ? GRID_INTEGRATE_GENERAL : GRID_INTEGRATE_ORTHO, q.n);
-    }
+  for (const Queue &q : m.queues) {
+    ga.queue = q.d_idx;
+    ga.nqueue = q.n;
+    ga.counter = t->d_counters + qi++;
+    ga.grid_stride = q.fp32 ? 2 : 1;
+    for (int l = 0; l < t->nlevels; l++) // the general path runs in FP64 in the mixed mode
+      ga.grids_in[l] = (arith == ARITH_FP64 || (q.general && arith == ARITH_MIXED))
+                           ? (const void *)grids[l] : (const void *)t->d_gridsplit[l];
+    launch_integrate(ga, q.fp32 ? (int)ARITH_FP32 : arith, q.general == 1, q.bucket, q.extent,
+                     0, s);
+    grid_library_counter_add(kBucketLp[q.bucket], GRID_BACKEND_GB300,
+                             q.general ? GRID_INTEGRATE_GENERAL : GRID_INTEGRATE_ORTHO, q.n);
+  }
   CK(cudaGetLastError());
   CK(cudaEventRecord(t->ev[2], s));
   CK(cudaMemsetAsync(t->d_hab_cart, 0, sizeof(double) * std::max<size_t>(t->cart_total, 1), s));

@@ -167,6 +167,7 @@ struct GridArgs {
   int coef_stride;   // FP32 kernels: floats per stored coefficient (2: dfloat buffer)
   int grid_stride;   // FP32 integrate: floats per grid point (2: hi/lo pairs)
   int nwarps_total;
+  const float2 *seeds;    // mixed path: per task [3][6] dfloat recurrence seeds
   long long *task_cycles; // optional per-task timings (clock64)
   int *error;             // device error word
 };

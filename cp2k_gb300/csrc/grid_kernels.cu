@@ -44,12 +44,23 @@ template <typename N, int LPB> struct OrthoSmem {
   static __host__ __device__ constexpr int red_stride() {
     return ((P * (P + 1)) / 2 + P) | 1;
   }
-  static __host__ __device__ size_t bytes(int wmax) {
+  // collocate: tables, coefficients, C_xy, periodic maps
+  static __host__ __device__ size_t bytes_coll(int wmax) {
     size_t b = sizeof(T) * (3 * (size_t)wmax * PP + ncoset(LPB) + ntri(LPB));
     b += sizeof(int) * 3 * (size_t)wmax;
-    b += sizeof(double) * ncoset(LPB);          // integrate accumulator
-    b += sizeof(T) * 32 * (size_t)red_stride(); // integrate x-fold transpose
-    b += 64;                                    // alignment slack
+    b += 64; // alignment slack
+    return (b + 15) & ~size_t(15);
+  }
+  // integrate: tables (reused as the x-fold transpose), maps, accumulator
+  static __host__ __device__ size_t pol_words_int(int wmax) {
+    const size_t a = 3 * (size_t)wmax * PP, r = 32 * (size_t)red_stride();
+    return a > r ? a : r;
+  }
+  static __host__ __device__ size_t bytes_int(int wmax) {
+    size_t b = sizeof(T) * pol_words_int(wmax);
+    b += sizeof(int) * 3 * (size_t)wmax;
+    b += sizeof(double) * ncoset(LPB);
+    b += 64;
     return (b + 15) & ~size_t(15);
   }
 };
@@ -72,7 +83,7 @@ template <typename N, int LPB>
 __device__ __forceinline__ void fill_ortho_tables(const TaskDesc &d, const LevelDesc &L,
                                                   int cmax, int lp,
                                                   typename Num<N>::T *pol, int *map,
-                                                  int lane) {
+                                                  int lane, const float2 *seed) {
   using T = typename Num<N>::T;
   constexpr int PP = OrthoSmem<N, LPB>::PP;
   const int w = 2 * cmax + 2;
@@ -111,16 +122,17 @@ __device__ __forceinline__ void fill_ortho_tables(const TaskDesc &d, const Level
     }
   } else {
     // dfloat: the Gaussian along each line by the multiplicative recurrence
-    // of grid_ref_collint.h:262-293, seeded with FP64 exponentials, run in
-    // dfloat by 6 lanes (3 directions x 2 sides of c = 0).
+    // of grid_ref_collint.h:262-293, run in dfloat by 6 lanes (3 directions
+    // x 2 sides of c = 0) from exponentials the host evaluated in FP64:
+    // seed[dir] = {e(0), f_up(0), f_down(0), q, h, -roff} with
+    // e(c) = exp(-z (c h - r)^2), e(c +- 1) = e(c) f(c), f(c +- 1) = f(c) q.
     if (lane < 6) {
       const int dir = lane >> 1, up = lane & 1;
-      const double h = L.dh[dir * 4], r = d.roff[dir], z = d.zetp;
-      // e(c) = exp(-z (c h - r)^2); e(c +- 1) = e(c) * f(c); f(c +- 1) = f(c) * q
-      dfloat ec = df_make(exp(-z * r * r));
-      dfloat f = df_make(up ? exp(-z * h * (h - 2.0 * r)) : exp(-z * h * (h + 2.0 * r)));
-      const dfloat q = df_make(exp(-2.0 * z * h * h));
-      const dfloat hd = df_make(h), rd = df_make(-r);
+      const float2 *sd = seed + 6 * dir;
+      dfloat ec = dfloat{sd[0].x, sd[0].y};
+      dfloat f = up ? dfloat{sd[1].x, sd[1].y} : dfloat{sd[2].x, sd[2].y};
+      const dfloat q = dfloat{sd[3].x, sd[3].y};
+      const dfloat hd = dfloat{sd[4].x, sd[4].y}, rd = dfloat{sd[5].x, sd[5].y};
       const int cend = up ? cmax + 1 : -cmax;
       for (int cc = 0;; cc += up ? 1 : -1) {
         if (up || cc != 0) { // c = 0 is written by the up-going lane
@@ -214,7 +226,7 @@ __global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
   constexpr int P = LPB + 1;
   constexpr int PP = OrthoSmem<N, LPB>::PP;
   const int lane = threadIdx.x & 31;
-  unsigned char *ws = smem + (threadIdx.x >> 5) * OrthoSmem<N, LPB>::bytes(wmax);
+  unsigned char *ws = smem + (threadIdx.x >> 5) * OrthoSmem<N, LPB>::bytes_coll(wmax);
   T *pol = (T *)ws;
   T *coef = pol + 3 * (size_t)wmax * PP;
   T *cxy = coef + ncoset(LPB);
@@ -249,7 +261,7 @@ __global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
       for (int e = lane; e < nco; e += 32)
         coef[e] = csrc[e];
     }
-    fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane);
+    fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane, a.seeds + (size_t)t * 18);
     __syncwarp();
 
     double *grid = a.grids[d.level];
@@ -343,13 +355,11 @@ __global__ void __launch_bounds__(128) integrate_ortho(GridArgs a, int wmax) {
   constexpr int PP = OrthoSmem<N, LPB>::PP;
   constexpr int NYZ = (LPB + 1) * (LPB + 2) / 2;
   const int lane = threadIdx.x & 31;
-  unsigned char *ws = smem + (threadIdx.x >> 5) * OrthoSmem<N, LPB>::bytes(wmax);
+  unsigned char *ws = smem + (threadIdx.x >> 5) * OrthoSmem<N, LPB>::bytes_int(wmax);
   T *pol = (T *)ws;
-  T *coef = pol + 3 * (size_t)wmax * PP;
-  T *cxy = coef + ncoset(LPB);
-  int *map = (int *)(cxy + ntri(LPB));
+  T *red = pol; // the x fold of the last x-chunk overwrites the tables
+  int *map = (int *)(pol + OrthoSmem<N, LPB>::pol_words_int(wmax));
   double *acc = (double *)(((uintptr_t)(map + 3 * wmax) + 15) & ~uintptr_t(15));
-  T *red = (T *)(acc + ncoset(LPB));
   double *out = (double *)a.coef_out;
 
   for (;;) {
@@ -373,7 +383,7 @@ __global__ void __launch_bounds__(128) integrate_ortho(GridArgs a, int wmax) {
     const int nco = ncoset(lp);
     for (int e = lane; e < nco; e += 32)
       acc[e] = 0.0;
-    fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane);
+    fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane, a.seeds + (size_t)t * 18);
     __syncwarp();
 
     const void *grid = a.grids_in[d.level];
@@ -441,6 +451,7 @@ __global__ void __launch_bounds__(128) integrate_ortho(GridArgs a, int wmax) {
         T *rl = red + lane * RS;
         T px[PP];
         load_row<T, PP>(pol + (size_t)((xin ? cx : cg.x_lo) + cg.cmax) * PP, px);
+        __syncwarp(); // every lane holds its pol_x before the tables are overwritten
 #pragma unroll
         for (int e = 0; e < NYZ; e++)
           rl[e] = ayz[e];
@@ -459,6 +470,10 @@ __global__ void __launch_bounds__(128) integrate_ortho(GridArgs a, int wmax) {
           acc[e] += M::to_double(s);
         }
         __syncwarp();
+        if (xc + cg.SW <= cg.x_hi) { // another x-chunk follows: rebuild the tables
+          fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane, a.seeds + (size_t)t * 18);
+          __syncwarp();
+        }
       }
     }
     __syncwarp();
@@ -479,7 +494,8 @@ __global__ void __launch_bounds__(128) integrate_ortho(GridArgs a, int wmax) {
 template <typename N, int LPB>
 static void launch_ortho_t(const GridArgs &a, bool collocate, int wmax, int nblocks,
                            cudaStream_t s) {
-  const size_t per_warp = OrthoSmem<N, LPB>::bytes(wmax);
+  const size_t per_warp =
+      collocate ? OrthoSmem<N, LPB>::bytes_coll(wmax) : OrthoSmem<N, LPB>::bytes_int(wmax);
   const int nw = warps_for(per_warp);
   const size_t smem = nw * per_warp;
   if (nw < 1)
