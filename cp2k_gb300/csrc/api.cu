@@ -271,7 +271,7 @@ struct TaskList {
   std::vector<double> gbound;    // per task bound of |contribution| for |P| <= 1
   std::vector<float2> seeds;     // per task [3][6] dfloat recurrence seeds (ortho)
   float2 *d_seeds = nullptr;
-  double mixed_threshold = 1e-3; // mixed path: tasks with gbound <= this run FP32
+  double mixed_threshold = 1.0;  // mixed path: tasks with gbound <= this run FP32
   std::vector<int> npts_local;   // [nlevels][3]
   size_t cart_total = 0;
   int contract_words = 1;

@@ -266,7 +266,7 @@ void grid_gb300_set_schedule(const grid_gb300_task_list *task_list,
 /* Mixed path: tasks whose contribution bound (Gaussian-product prefactor x
  * polynomial maxima, for density-matrix elements of magnitude <= 1) is at
  * most `threshold` run in plain FP32, the others in double-float.
- * 0 runs every orthorhombic task in double-float.  Default 1e-3. */
+ * 0 runs every orthorhombic task in double-float.  Default 1. */
 void grid_gb300_set_mixed_threshold(const grid_gb300_task_list *task_list,
                                     double threshold);
 /* Share of orthorhombic tasks (and of their grid points) that the mixed path
