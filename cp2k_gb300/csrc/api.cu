@@ -342,8 +342,8 @@ static LDiffs integrate_ldiffs(bool forces, bool virial, bool tau) {
 
 // Sphere bounds of one (level, discretised radius), with the reference's
 // expressions (grid_ref_collint.h:237-245, 139-151, 44-52).
-static void build_sphere(const LevelDesc &L, double disr, SphereHdr &h,
-                         std::vector<int16_t> &tab, long long &npoints) {
+void build_sphere(const LevelDesc &L, double disr, SphereHdr &h, std::vector<int16_t> &tab,
+                  long long &npoints) {
   for (int i = 0; i < 3; i++)
     h.lb[i] = (int)ceil(-1e-8 - disr * L.dh_inv[i * 4]);
   h.cmax = std::max(std::max(1 - h.lb[0], 1 - h.lb[1]), 1 - h.lb[2]);

@@ -18,6 +18,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -239,6 +240,11 @@ inline int bucket_of(int lp) {
       return b;
   return -1;
 }
+
+// Sphere bounds of one (level, discretised radius) appended to `tab`
+// (api.cu); npoints receives the number of grid points the cube visits.
+void build_sphere(const LevelDesc &L, double disr, SphereHdr &h,
+                  std::vector<int16_t> &tab, long long &npoints);
 
 // counts launches for grid_gb300_kernel_launches()
 void count_launch(int n = 1);

@@ -89,6 +89,12 @@ def lib():
         L.grid_gb300_task_list_info.argtypes = [vp, vp, vp, vp, vp]
         L.grid_gb300_task_sizes.argtypes = [vp, vp, vp]
         L.grid_gb300_last_timings.argtypes = [vp, vp]
+        L.grid_gb300_collocate_pgf_product_static.restype = C.c_int
+        L.grid_gb300_collocate_pgf_product_static.argtypes = (
+            [C.c_bool, C.c_int, C.c_int] + [C.c_int] * 4 + [C.c_double] * 3 + [vp] * 4
+            + [vp] * 4 + [C.c_double] + [C.c_int] * 4 + [vp, vp, vp])
+        L.grid_gb300_static_scratch_bytes.restype = C.c_size_t
+        L.grid_gb300_static_scratch_error.restype = C.c_char_p
         L.grid_gb300_backend_handle.argtypes = [vp]
         L.grid_gb300_backend_handle.restype = vp
         L.grid_gb300_kernel_launches.restype = C.c_longlong
@@ -318,6 +324,21 @@ class GridTaskList:
             self.close()
         except Exception:
             pass
+
+
+def collocate_pgf_product_static(t: dict, pab_dev, grid_dev, stream=None) -> int:
+    """grid_gb300_collocate_pgf_product_static for a task description dict
+    (keys as a CP2K .task file); pab_dev / grid_dev are torch CUDA float64
+    tensors.  Returns the entry point's status (0 = ok)."""
+    f64 = lambda x: np.ascontiguousarray(x, np.float64)
+    i32 = lambda x: np.ascontiguousarray(x, np.int32)
+    arrs = [f64(t["dh"]), f64(t["dh_inv"]), f64(t["ra"]), f64(t["rab"]), i32(t["npts_global"]),
+            i32(t["npts_local"]), i32(t["shift_local"]), i32(t["border_width"])]
+    return int(lib().grid_gb300_collocate_pgf_product_static(
+        bool(t["orthorhombic"]), int(t["border_mask"]), int(t["func"]), t["la_max"], t["la_min"],
+        t["lb_max"], t["lb_min"], t["zeta"], t["zetb"], t["rscale"], *[_p(a) for a in arrs],
+        t["radius"], t["o1"], t["o2"], t["n1"], t["n2"], C.c_void_p(pab_dev.data_ptr()),
+        C.c_void_p(grid_dev.data_ptr()), _stream(stream)))
 
 
 def _stream(stream):

@@ -313,6 +313,34 @@ void grid_gb300_last_timings(const grid_gb300_task_list *task_list,
 /* Number of kernels this library launched on the device since load. */
 long long grid_gb300_kernel_launches(void);
 
+/* Allocation-free collocation of one primitive pair, for callers that
+ * cannot allocate device memory at call time (inside CUDA-graph capture, under
+ * a fixed memory arena, in drivers that forbid cudaMalloc after start-up).
+ * No counterpart in CP2K; the arguments mean what they mean for
+ * grid_cpu_collocate_pgf_product (src/grid/cpu/grid_cpu_collocate.h), with
+ * pab ([n2][n1]) and grid (npts_local, x fastest; collocated values are
+ * added) given as device pointers and the work enqueued on `stream`
+ * (cudaStream_t as void*).  FP64 arithmetic.
+ * All per-call scratch lives in one static __device__ array of
+ * grid_gb300_static_scratch_bytes() bytes held by every GPU that loads the
+ * library; no device memory is allocated.  Calls share that array: calls
+ * whose kernels overlap on the GPU race, calls on one stream are ordered.
+ * The first call on a device looks up the array's address and should come
+ * before any stream capture.  Returns 0, or nonzero with a message in
+ * grid_gb300_static_scratch_error() when the task needs more scratch than
+ * the array holds or an argument is out of range. */
+int grid_gb300_collocate_pgf_product_static(
+    const bool orthorhombic, const int border_mask, const int func,
+    const int la_max, const int la_min, const int lb_max, const int lb_min,
+    const double zeta, const double zetb, const double rscale,
+    const double *dh, const double *dh_inv, const double *ra,
+    const double *rab, const int *npts_global, const int *npts_local,
+    const int *shift_local, const int *border_width, const double radius,
+    const int o1, const int o2, const int n1, const int n2,
+    const double *pab, double *grid, void *stream);
+size_t grid_gb300_static_scratch_bytes(void);
+const char *grid_gb300_static_scratch_error(void);
+
 /* Last error message recorded by the library ("" if none). */
 const char *grid_gb300_last_error(void);
 
