@@ -95,11 +95,11 @@ def test_tasklist_fp64(G, O, name, scale, funcs, tol):
 
 # Stated error bounds of the reduced-precision paths against the FP64 oracle,
 # measured on seeded inputs (uniform [-1, 1] density-matrix blocks and
-# potential):
-#   MIXED (double-float per-point work, FP64 accumulation):
-#       max |d rho| / max(1, |rho|) <= 1e-9, max |d hab| / max(1, |hab|) <= 1e-9
-#   FP32  (plain FP32 per-point work, FP64 accumulation):
-#       max |d rho| / max |rho| <= 2e-6,     max |d hab| / max |hab| <= 2e-6
+# potential), max |d| / max(1, |ref|) unless noted:
+#   MIXED, default split (tasks with contribution bound <= 1 in FP32, the rest
+#       in double-float):                  rho, hab <= 1e-6, forces <= 1e-6
+#   MIXED, threshold 0 (all double-float): rho, hab <= 1e-9, forces <= 1e-7
+#   FP32 (plain FP32 per-point work):      max |d| / max |ref| <= 2e-6
 @pytest.mark.parametrize("name,scale", [("c1_64atoms", 0.3), ("c2_512atoms", 0.08),
                                         ("c3_256atoms_triclinic", 0.12)])
 def test_reduced_precision_bounds(G, O, name, scale):
@@ -112,14 +112,18 @@ def test_reduced_precision_bounds(G, O, name, scale):
     h_ref, f_ref, _ = ot.integrate(V, pab, forces=True)
     gmax = max(float(np.abs(g).max()) for g in g_ref)
     hmax = float(np.abs(h_ref).max())
-    for prec, tol_rel, tol_max in ((G.MIXED, 1e-9, None), (G.FP32, None, 2e-6)):
+    for prec, tau, tol_rel, tol_f, tol_max in ((G.MIXED, None, 1e-6, 1e-6, None),
+                                                (G.MIXED, 0.0, 1e-9, 1e-7, None),
+                                                (G.FP32, None, None, None, 2e-6)):
         tl = G.GridTaskList(inp, precision=prec)
+        if tau is not None:
+            tl.set_mixed_threshold(tau)
         g = tl.collocate(100, pab)
         h, f, _ = tl.integrate(V, pab, forces=True)
         if tol_rel is not None:
             assert max(rel_diff(a, b) for a, b in zip(g, g_ref)) < tol_rel
             assert rel_diff(h, h_ref) < tol_rel
-            assert rel_diff(f, f_ref) < 1e-7
+            assert rel_diff(f, f_ref) < tol_f
         else:
             assert max(float(np.abs(a - b).max()) for a, b in zip(g, g_ref)) / gmax < tol_max
             assert float(np.abs(h - h_ref).max()) / hmax < tol_max
@@ -158,4 +162,24 @@ def test_recreate_and_schedules_agree(G, O):
         outs.append(tl.collocate(100, pab))
     for o in outs[1:]:
         assert max(rel_diff(a, b) for a, b in zip(o, outs[0])) < 1e-13
+    tl.close()
+
+
+@pytest.mark.parametrize("case", ["ortho", "tricl"])
+@pytest.mark.parametrize("api", ["backend", "cp2k"])
+def test_ref_golden_fp64(G, case, api):
+    """Against outputs of CP2K's own REF backend (committed fixtures): both the
+    orthorhombic and the general (triclinic) path, rho and tau densities,
+    hab with and without tau, forces and virial."""
+    import golden_cases
+    inp, pab, V, exp = golden_cases.load(case)
+    tl = G.GridTaskList(inp, precision=G.FP64, api=api)
+    for func in (100, 200):
+        got = tl.collocate(func, pab)
+        assert max(rel_diff(a, b) for a, b in zip(got, exp[f"rho{func}"])) < TOL_GRID
+    for tau in (0, 1):
+        h, f, v = tl.integrate(V, pab, compute_tau=bool(tau), forces=True, virial=True)
+        assert rel_diff(h, exp[f"hab_tau{tau}"]) < TOL_GRID
+        assert rel_diff(f, exp[f"forces_tau{tau}"]) < TOL_DERIV
+        assert rel_diff(v, exp[f"virial_tau{tau}"]) < TOL_DERIV
     tl.close()
