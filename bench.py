@@ -13,7 +13,8 @@ grid_integrate_task_list (hab only), as one SCF iteration does.
   fp64_*     the plain FP64 path timed the same way;
   errors     mixed vs the FP64 path on the same inputs (the FP64 path is
              pinned to the oracle at 1e-12 by the test-suite);
-  roofline   dominant kernel (integrate) against measured peaks;
+  roofline   the dominant grid kernel (largest share of a mixed step, from
+             per-launch CUDA events) against measured peaks;
   cpu_baseline  the oracle (FP64 C restatement of CP2K's REF backend) on the
              host cores, on a bounded random sample of the tasks, scaled to a
              full step by grid points.
@@ -150,7 +151,7 @@ def barrier(world: int):
 # --------------------------------------------------------------------------
 # CPU baseline: the oracle on a bounded sample
 # --------------------------------------------------------------------------
-def cpu_sample_time(inp, pab, V, target_s: float = 3.0, seed: int = 0):
+def cpu_sample_time(inp, pab, V, target_s: float = 1.0, seed: int = 0):
     """Times the oracle's collocate + integrate on a random subset of tasks and
     scales to the whole task list by grid points visited."""
     from cp2k_gb300.tasklist import TaskListInputs
@@ -180,7 +181,9 @@ def cpu_sample_time(inp, pab, V, target_s: float = 3.0, seed: int = 0):
     # grid reduction) are not scaled up with the points
     frac = 0.002
     sel, dt = timed(frac)
-    frac = min(0.5, frac * target_s / max(dt, 1e-3))
+    while dt < 0.5 * target_s and frac < 0.25:
+        frac = min(0.25, frac * min(8.0, target_s / max(dt, 1e-3)))
+        sel, dt = timed(frac)
     sel1, dt1 = timed(frac)
     sel2, dt2 = timed(min(1.0, 2 * frac))
     p1, p2 = float(pts[sel1].sum()), float(pts[sel2].sum())
@@ -218,7 +221,8 @@ def reference_arm(args, world, rank):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": CONFIG,
         "cpu_baseline": {"value": v, "unit": "ms", "cores": threads, "kind": "port",
                          "sample": sample + "; oracle = C restatement of CP2K's REF backend "
-                                            "(CP2K's own library cannot be built on this host)"},
+                                            "(CP2K's sources, needed to build its own CPU "
+                                            "backend, are not present on the GPU host)"},
         "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -250,6 +254,30 @@ def measure_fp32_peak(torch):
     return best
 
 
+# DRAM bytes per launch of the dominant kernels, from the ncu capture named
+# beside each figure (dram__bytes_read.sum + dram__bytes_write.sum); the
+# bench cannot run ncu itself.  Keys: kernel label as in "roofline.kernel".
+NCU_TRAFFIC = {}
+
+
+def _kernel_label(info):
+    prec = {0: "double", 1: "dfloat", 2: "float"}[info["precision"]]
+    kind = "general" if info["general"] else "ortho"
+    phase = "collocate" if info["phase"] == 0 else "integrate"
+    return f"{phase}_{kind}<{prec},{info['lp_bucket']}>"
+
+
+def load_cost_model(torch):
+    """The trained task-cost model shipped with the package (trained on this
+    GPU type by cp2k_gb300.costmodel_eval), or None."""
+    from cp2k_gb300 import costmodel as CM
+    path = os.path.join(ROOT, "cp2k_gb300", "costmodel_gb300.npz")
+    if not os.path.exists(path):
+        return None, None
+    with open(path, "rb") as fh:
+        return CM.CostModel.from_bytes(fh.read()), os.path.relpath(path, ROOT)
+
+
 def gpu_arm(args, world, rank, local):
     import torch
 
@@ -268,10 +296,16 @@ def gpu_arm(args, world, rank, local):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     tl = G.GridTaskList(inp, api="cp2k")
     stream = torch.cuda.Stream(device=dev)
+    model, model_path = load_cost_model(torch)
+    if model is not None:
+        with torch.cuda.stream(stream):
+            model.apply(tl, stream=stream)
+    sched_mixed = G.SCHEDULE_MODEL if model is not None else G.SCHEDULE_SIZE
 
-    def run_steps(prec, nsteps, timed):
+    def run_steps(prec, sched, nsteps):
         tl.set_precision(prec)
-        times, kt = [], []
+        tl.set_schedule(sched)
+        times = []
         for _ in range(nsteps):
             flush.zero_()
             torch.cuda.synchronize()
@@ -283,55 +317,70 @@ def gpu_arm(args, world, rank, local):
                 e[1].record(stream)
             torch.cuda.synchronize()
             times.append(e[0].elapsed_time(e[1]))
-            kt.append(tl.timings())
-        return times, kt
+        return times
 
     # warm-up all paths, then the timed regions
-    run_steps(G.MIXED, args.warmup, False)
-    run_steps(G.FP64, max(1, min(args.warmup, 2)), False)
-    run_steps(G.FP32, max(1, min(args.warmup, 2)), False)
+    run_steps(G.MIXED, sched_mixed, args.warmup)
+    run_steps(G.MIXED, G.SCHEDULE_SIZE, max(1, min(args.warmup, 2)))
+    run_steps(G.FP64, G.SCHEDULE_SIZE, max(1, min(args.warmup, 2)))
+    run_steps(G.FP32, sched_mixed, max(1, min(args.warmup, 2)))
     launches0 = G.kernel_launches()
     barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        t_mixed, kt_mixed = run_steps(G.MIXED, args.steps, True)
+        t_mixed = run_steps(G.MIXED, sched_mixed, args.steps)
     launches = G.kernel_launches() - launches0
     torch.cuda.synchronize()
     barrier(world)
     rho_mixed = [g.clone() for g in grids]
     hab_mixed = hab.clone()
-    t_fp64, _ = run_steps(G.FP64, max(1, min(args.steps, 3)), True)
+    t_size = run_steps(G.MIXED, G.SCHEDULE_SIZE, max(1, min(args.steps, 5)))
+    t_fp64 = run_steps(G.FP64, G.SCHEDULE_SIZE, max(1, min(args.steps, 3)))
     rho64 = [g.clone() for g in grids]
     hab64 = hab.clone()
-    t_fp32, _ = run_steps(G.FP32, max(1, min(args.steps, 5)), True)
+    t_fp32 = run_steps(G.FP32, sched_mixed, max(1, min(args.steps, 5)))
     rho32 = [g.clone() for g in grids]
     hab32 = hab.clone()
 
     ms_mixed = max_over_ranks(float(np.mean(t_mixed)), world)
+    ms_size = max_over_ranks(float(np.mean(t_size)), world)
     ms_fp64 = max_over_ranks(float(np.mean(t_fp64)), world)
     ms_fp32 = max_over_ranks(float(np.mean(t_fp32)), world)
 
-    # dominant kernel: integrate grid kernel of the mixed path, timed alone
+    # per-launch CUDA events of one mixed step (outside the timed region):
+    # the dominant kernel is the one with the largest total time
     tl.set_precision(G.MIXED)
-    with torch.cuda.stream(stream):
-        tl.collocate_device(100, pab, grids, stream=stream)
-    torch.cuda.synchronize()
-    kern = []
+    tl.set_schedule(sched_mixed)
+    tl.set_launch_timing(True)
+    per_kernel = {}
     for _ in range(3):
         flush.zero_()
         torch.cuda.synchronize()
         with torch.cuda.stream(stream):
+            tl.collocate_device(100, pab, grids, stream=stream)
+        infos = tl.launch_timings()
+        with torch.cuda.stream(stream):
             tl.integrate_device(V, hab, stream=stream)
-        torch.cuda.synchronize()
-        kern.append(tl.timings()["grid_ms"])
-    t_int_ms = float(np.median(kern))
-    with torch.cuda.stream(stream):
-        tl.collocate_device(100, pab, grids, stream=stream)
-    torch.cuda.synchronize()
-    t_coll_ms = tl.timings()["grid_ms"]
+        infos = infos + tl.launch_timings()
+        for i in infos:
+            k = per_kernel.setdefault(_kernel_label(i), {"ms": [], "points": 0.0, "flops": 0.0,
+                                                         "launches": 0})
+            k["ms"].append(i["ms"])
+            k["points"] += i["points"]
+            k["flops"] += i["flops"]
+            k["launches"] += 1
+    tl.set_launch_timing(False)
+    dom = max(per_kernel, key=lambda k: sum(per_kernel[k]["ms"]))
+    d = per_kernel[dom]
+    avg_ms = float(np.mean(d["ms"]))
+    bytes_per_point = {"dfloat": 8.0, "double": 8.0, "float": 4.0}[dom.split("<")[1].split(",")[0]]
+    alg_bytes = bytes_per_point * d["points"] / d["launches"]
+    alg_flops = d["flops"] / d["launches"]
+    kernel_share = {k: sum(v["ms"]) / sum(sum(x["ms"]) for x in per_kernel.values())
+                    for k, v in sorted(per_kernel.items(), key=lambda kv: -sum(kv[1]["ms"]))}
 
     # errors of the mixed / FP32 paths against the FP64 path
-    dvol = [abs(float(np.linalg.det(d))) for d in inp.dh]
+    dvol = [abs(float(np.linalg.det(d_))) for d_ in inp.dh]
     e64 = sum(float((g * v).sum()) * dv for g, v, dv in zip(rho64, V, dvol))
 
     def errors(rho, habx):
@@ -348,20 +397,17 @@ def gpu_arm(args, world, rank, local):
     err_mixed = errors(rho_mixed, hab_mixed)
     err_fp32 = errors(rho32, hab32)
 
-    # algorithmic work of the dominant kernel
-    pts, lp = tl.sizes()
-    flops = float((2.0 * (lp + 1) * pts).sum())
-    grid_pts = float(sum(inp.grid_sizes()))
-    bytes_int = 4.0 * grid_pts + 8.0 * 0  # FP32 copy of V read once
     peaks, peak_kind = _peaks()
     fp32_peak = measure_fp32_peak(torch)
-    achieved_gbs = bytes_int / (t_int_ms * 1e-3) / 1e9
-    achieved_tf = flops / (t_int_ms * 1e-3) / 1e12
+    achieved_gbs = alg_bytes / (avg_ms * 1e-3) / 1e9
+    achieved_tf = alg_flops / (avg_ms * 1e-3) / 1e12
+    traffic = NCU_TRAFFIC.get(dom)
 
     # e2e through the CP2K C ABI with host offload buffers: inputs are placed
     # in the pinned host buffers once (as CP2K fills them); each timed step
     # copies pab and V host->device, computes, and copies rho and hab back.
     tl.set_precision(G.MIXED)
+    tl.set_schedule(sched_mixed)
     tl.collocate(100, pab_h, copy_out=False)
     tl.integrate(V_h, copy_out=False)
     torch.cuda.synchronize()
@@ -372,8 +418,9 @@ def gpu_arm(args, world, rank, local):
         tl.integrate(copy_out=False)
         e2e.append((time.perf_counter() - t0) * 1e3)
     e2e_ms = max_over_ranks(float(np.mean(e2e)), world)
+    grid_pts = float(sum(inp.grid_sizes()))
     h2d = 8 * inp.buffer_size + 8 * int(grid_pts)  # pab + V grids
-    d2h = 8 * int(grid_pts) + 8 * inp.buffer_size
+    d2h = 8 * int(grid_pts) + 8 * inp.buffer_size  # rho grids + hab
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -386,21 +433,26 @@ def gpu_arm(args, world, rank, local):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mixed,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 pairs (double-float) bulk / f64 accumulate", "data": "synthetic",
-            "config": {**CONFIG, "ntasks": inp.ntasks, "parallelism": f"replicas x{world}"},
+            "config": {**CONFIG, "ntasks": inp.ntasks, "parallelism": f"replicas x{world}",
+                       "schedule": "learned cost model" if model is not None else "size",
+                       "cost_model": model_path},
             "fp64_ms_per_step": ms_fp64, "speedup_vs_fp64": ms_fp64 / ms_mixed,
+            "mixed_size_schedule_ms_per_step": ms_size,
+            "cost_model_gain": ms_size / ms_mixed - 1.0,
             "fp32_ms_per_step": ms_fp32, "fp32_speedup_vs_fp64": ms_fp64 / ms_fp32,
             "errors_mixed_vs_fp64": err_mixed,
             "errors_fp32_vs_fp64": err_fp32,
             "targets": {"speedup_vs_fp64": 3.0, "rho_max_rel": 1e-6, "energy_ha_per_atom": 1e-8},
-            "kernel_ms": {"collocate_grid_mixed": t_coll_ms, "integrate_grid_mixed": t_int_ms},
+            "kernel_share_mixed": kernel_share,
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks.get("hbm_gbs"),
                          "unit": "GB/s", "frac": achieved_gbs / peaks.get("hbm_gbs", 1.0),
-                         "traffic": None, "kernel": "integrate_ortho<dfloat,4> (mixed)",
+                         "traffic": traffic, "kernel": dom, "launch_ms": avg_ms,
+                         "algorithmic_bytes_per_launch": alg_bytes,
                          "peak_kind": peak_kind},
             "roofline_fp32": {"bound": "fp32_fma", "achieved": achieved_tf, "peak": fp32_peak,
                               "unit": "TFLOP/s", "frac": achieved_tf / fp32_peak,
                               "peak_kind": "measured cuBLAS SGEMM (TF32 off) on this GPU",
-                              "flops_per_launch": flops},
+                              "kernel": dom, "flops_per_launch": alg_flops},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},

@@ -237,6 +237,15 @@ struct Queue {
   int extent = 0; // ortho: max cube width; general: max j-range
   int general = 0, bucket = 0;
   int fp32 = 0; // mixed path: this queue runs in plain FP32
+  int key = 0;          // (general, bucket, FP32 class, size class)
+  long long points = 0; // grid points the queue's tasks visit
+  double flops = 0.0;   // 2 (lp+1) points summed over the tasks
+};
+
+// per-launch CUDA-event timing of the grid kernels (opt-in)
+struct LaunchRecord {
+  grid_gb300_launch_info info;
+  cudaEvent_t a = nullptr, b = nullptr;
 };
 
 // cube widths up to this share one work queue; wider cubes get their own so
@@ -268,6 +277,12 @@ struct TaskList {
   std::vector<int16_t> sph_tab;
   std::vector<long long> points; // per task (block order)
   std::vector<float> model_cost; // per task, empty unless a model was applied
+  std::vector<float> features;   // per task [6]: cost-model inputs (block order)
+  bool task_timing = false;      // record clock64 cycles per task
+  bool launch_timing = false;    // record CUDA events around every grid launch
+  std::vector<LaunchRecord> launches; // of the last call
+  std::vector<cudaEvent_t> event_pool;
+  std::map<std::pair<int, int>, LaunchCfg> tuned; // (phase, queue key) -> launch shape
   std::vector<double> gbound;    // per task bound of |contribution| for |P| <= 1
   std::vector<float2> seeds;     // per task [3][6] dfloat recurrence seeds (ortho)
   float2 *d_seeds = nullptr;
@@ -458,6 +473,8 @@ static void free_device(TaskList *t) {
   for (auto &e : t->ev)
     if (e)
       cudaEventDestroy(e);
+  for (auto &e : t->event_pool)
+    cudaEventDestroy(e);
   if (t->stream)
     cudaStreamDestroy(t->stream);
 }
@@ -556,6 +573,18 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
   t->points.assign(ntasks, 0);
   t->gbound.assign(ntasks, 0.0);
   t->seeds.assign((size_t)ntasks * 18, make_float2(0.f, 0.f));
+  t->features.assign((size_t)ntasks * 6, 0.f);
+  // cell skew of the finest level's cell (0 for orthorhombic cells)
+  double skew = 0.0;
+  {
+    const double *h = dh; // rows: step vectors
+    const double det = h[0] * (h[4] * h[8] - h[5] * h[7]) - h[1] * (h[3] * h[8] - h[5] * h[6]) +
+                       h[2] * (h[3] * h[7] - h[4] * h[6]);
+    double norms = 1.0;
+    for (int r = 0; r < 3; r++)
+      norms *= sqrt(h[3 * r] * h[3 * r] + h[3 * r + 1] * h[3 * r + 1] + h[3 * r + 2] * h[3 * r + 2]);
+    skew = norms > 0.0 ? 1.0 - fabs(det) / norms : 0.0;
+  }
   std::map<std::pair<int, long long>, int> sphere_of;
   std::vector<long long> sphere_points;
   long long maxbuf = 0;
@@ -684,6 +713,21 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
       t->points[s] = np;
     }
     t->gbound[s] = contribution_bound(d, atom_positions + 3 * ia);
+    {
+      float *f = &t->features[(size_t)s * 6];
+      f[0] = (float)d.la_max;
+      f[1] = (float)d.lb_max;
+      f[2] = (float)(zeta + zetb);
+      if (d.flags & TF_SKIP)
+        f[3] = 0.f;
+      else if (d.flags & TF_GENERAL)
+        f[3] = 0.5f * (float)std::max(d.imax[0] - d.center[0],
+                                      std::max(d.imax[1] - d.center[1], d.imax[2] - d.center[2]));
+      else
+        f[3] = (float)t->sph[d.sphere].cmax;
+      f[4] = (float)L.dh_max;
+      f[5] = (float)skew;
+    }
     // subblock bookkeeping
     const int bn = block_num_list[i] - 1;
     const bool new_sub = s == 0 || block_num_list[order[s - 1]] != block_num_list[i] ||
@@ -823,6 +867,7 @@ static Mode &get_mode(TaskList *t, const LDiffs &d) {
       return x.first > y.first;
     });
     Queue q;
+    q.key = key;
     q.general = key / (2 * 2 * kNumBuckets);
     q.bucket = (key / 4) % kNumBuckets;
     q.fp32 = (key >> 1) & 1;
@@ -831,6 +876,9 @@ static Mode &get_mode(TaskList *t, const LDiffs &d) {
     for (size_t i = 0; i < v.size(); i++) {
       idx[i] = v[i].second;
       const TaskDesc &k = t->tasks[idx[i]];
+      const int lpk = k.la_max + d.la_max + k.lb_max + d.lb_max;
+      q.points += t->points[idx[i]];
+      q.flops += 2.0 * (lpk + 1) * (double)t->points[idx[i]];
       if (q.general == 0)
         ext = std::max(ext, 2 * t->sph[k.sphere].cmax + 2);
       else
@@ -877,12 +925,66 @@ static void read_timings(TaskList *t) {
   t->timings[3] = ev_ms(t->ev[0], t->ev[3]);
 }
 
+static cudaEvent_t pool_event(TaskList *t, size_t i) {
+  while (t->event_pool.size() <= i) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    t->event_pool.push_back(e);
+  }
+  return t->event_pool[i];
+}
+
+// one persistent grid-kernel launch of a work queue, with its tuned launch
+// shape and (optionally) CUDA events around it
+static void grid_launch(TaskList *t, const Queue &q, int phase, int arith, const GridArgs &ga,
+                        cudaStream_t s) {
+  LaunchCfg cfg;
+  auto it = t->tuned.find({phase, q.key});
+  if (it != t->tuned.end())
+    cfg = it->second;
+  LaunchRecord rec;
+  if (t->launch_timing) {
+    rec.a = pool_event(t, 2 * t->launches.size());
+    rec.b = pool_event(t, 2 * t->launches.size() + 1);
+    CK(cudaEventRecord(rec.a, s));
+  }
+  if (phase == 0)
+    launch_collocate(ga, arith, q.general == 1, q.bucket, q.extent, cfg, s);
+  else
+    launch_integrate(ga, arith, q.general == 1, q.bucket, q.extent, cfg, s);
+  if (t->launch_timing) {
+    CK(cudaEventRecord(rec.b, s));
+    grid_gb300_launch_info &in = rec.info;
+    in.phase = phase;
+    in.precision = arith;
+    in.general = q.general;
+    in.lp_bucket = kBucketLp[q.bucket];
+    in.ntasks = q.n;
+    in.warps_per_block = cfg.warps;
+    in.blocks = cfg.blocks;
+    in.points = q.points;
+    in.flops = q.flops;
+    in.ms = 0.0;
+    t->launches.push_back(rec);
+  }
+}
+
+static void begin_call(TaskList *t, cudaStream_t s) {
+  t->launches.clear();
+  if (t->task_timing) {
+    if (!t->d_cycles)
+      CK(cudaMalloc((void **)&t->d_cycles, sizeof(long long) * std::max(t->ntasks, 1)));
+    CK(cudaMemsetAsync(t->d_cycles, 0, sizeof(long long) * std::max(t->ntasks, 1), s));
+  }
+}
+
 static void run_collocate(TaskList *t, int func, const double *pab, double *const *grids,
                           cudaStream_t s) {
   const LDiffs d = func_ldiffs(func);
   Mode &m = get_mode(t, d);
   const int arith = t->precision;
   ensure(&t->d_coef, &t->coef_cap, m.coef_total * (arith == ARITH_FP32 ? 4 : 8));
+  begin_call(t, s);
   CK(cudaEventRecord(t->ev[0], s));
   ContractArgs ca{t->d_subs, (int)t->subs.size(), t->d_sphi, pab, nullptr, t->d_pab_cart,
                   t->contract_words};
@@ -916,7 +1018,7 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
   }
   ga.levels = t->levels;
   ga.d = d;
-  ga.task_cycles = t->d_cycles;
+  ga.task_cycles = t->task_timing ? t->d_cycles : nullptr;
   ga.seeds = t->d_seeds;
   ga.error = t->d_error;
   int qi = 0;
@@ -925,8 +1027,7 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
     ga.nqueue = q.n;
     ga.counter = t->d_counters + qi++;
     ga.coef_stride = q.fp32 ? 2 : 1;
-    launch_collocate(ga, q.fp32 ? (int)ARITH_FP32 : arith, q.general == 1, q.bucket, q.extent,
-                     0, s);
+    grid_launch(t, q, 0, q.fp32 ? (int)ARITH_FP32 : arith, ga, s);
     grid_library_counter_add(kBucketLp[q.bucket], GRID_BACKEND_GB300,
                              q.general ? GRID_COLLOCATE_GENERAL : GRID_COLLOCATE_ORTHO, q.n);
   }
@@ -947,6 +1048,7 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
   const int arith = t->precision;
   const bool need_pab = forces != nullptr || virial != nullptr;
   ensure((void **)&t->d_coef_int, &t->coef_int_cap, m.coef_total * 8);
+  begin_call(t, s);
   CK(cudaEventRecord(t->ev[0], s));
   if (arith != ARITH_FP64)
     for (int l = 0; l < t->nlevels; l++) {
@@ -975,7 +1077,7 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
     ga.grids_in[l] = arith != ARITH_FP64 ? (const void *)t->d_gridsplit[l] : (const void *)grids[l];
   ga.levels = t->levels;
   ga.d = d;
-  ga.task_cycles = t->d_cycles;
+  ga.task_cycles = t->task_timing ? t->d_cycles : nullptr;
   ga.seeds = t->d_seeds;
   ga.error = t->d_error;
   int qi = 0;
@@ -987,8 +1089,7 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
     for (int l = 0; l < t->nlevels; l++) // the general path runs in FP64 in the mixed mode
       ga.grids_in[l] = (arith == ARITH_FP64 || (q.general && arith == ARITH_MIXED))
                            ? (const void *)grids[l] : (const void *)t->d_gridsplit[l];
-    launch_integrate(ga, q.fp32 ? (int)ARITH_FP32 : arith, q.general == 1, q.bucket, q.extent,
-                     0, s);
+    grid_launch(t, q, 1, q.fp32 ? (int)ARITH_FP32 : arith, ga, s);
     grid_library_counter_add(kBucketLp[q.bucket], GRID_BACKEND_GB300,
                              q.general ? GRID_INTEGRATE_GENERAL : GRID_INTEGRATE_ORTHO, q.n);
   }
@@ -1331,6 +1432,104 @@ GB300_API void grid_gb300_task_sizes(const grid_gb300_task_list *task_list, long
     if (lp)
       lp[k.orig] = k.la_max + k.lb_max;
   }
+}
+
+GB300_API void grid_gb300_set_launch_timing(const grid_gb300_task_list *task_list, int enable) {
+  TL(task_list)->launch_timing = enable != 0;
+}
+
+GB300_API int grid_gb300_launch_timings(const grid_gb300_task_list *task_list, int max,
+                                        grid_gb300_launch_info *info) {
+  TaskList *t = TL(task_list);
+  const int n = (int)t->launches.size();
+  for (int i = 0; i < n && i < max; i++) {
+    LaunchRecord &r = t->launches[i];
+    CK(cudaEventSynchronize(r.b));
+    r.info.ms = ev_ms(r.a, r.b);
+    info[i] = r.info;
+  }
+  return n;
+}
+
+GB300_API void grid_gb300_set_task_timing(const grid_gb300_task_list *task_list, int enable) {
+  TL(task_list)->task_timing = enable != 0;
+}
+
+GB300_API void grid_gb300_task_cycles(const grid_gb300_task_list *task_list, long long *cycles) {
+  TaskList *t = TL(task_list);
+  if (t->empty)
+    return;
+  if (!t->d_cycles) {
+    memset(cycles, 0, sizeof(long long) * t->ntasks);
+    return;
+  }
+  CK(cudaDeviceSynchronize());
+  std::vector<long long> c(t->ntasks);
+  CK(cudaMemcpy(c.data(), t->d_cycles, sizeof(long long) * t->ntasks, cudaMemcpyDeviceToHost));
+  for (int s = 0; s < t->ntasks; s++)
+    cycles[t->tasks[s].orig] = c[s];
+}
+
+GB300_API void grid_gb300_task_features(const grid_gb300_task_list *task_list, float *features) {
+  TaskList *t = TL(task_list);
+  if (t->empty)
+    return;
+  for (int s = 0; s < t->ntasks; s++)
+    memcpy(features + (size_t)t->tasks[s].orig * 6, &t->features[(size_t)s * 6], 6 * sizeof(float));
+}
+
+GB300_API int grid_gb300_cost_model_nparams(void) { return mlp_nparams(); }
+
+GB300_API size_t grid_gb300_cost_model_work_floats(int n) {
+  return (size_t)mlp_tiles(n) * (mlp_nparams() + 1);
+}
+
+GB300_API void grid_gb300_cost_model_loss_grad(const float *params, const float *x, const float *t_,
+                                               int n, float *loss, float *grad, float *work,
+                                               void *stream) {
+  if (n < 1)
+    fail("cost model: no training samples");
+  launch_mlp_loss_grad(params, x, t_, n, loss, grad, work, (cudaStream_t)stream);
+  CK(cudaGetLastError());
+}
+
+GB300_API void grid_gb300_cost_model_adam(float *params, const float *grad, float *m, float *v,
+                                          int step, float lr, float beta1, float beta2, float eps,
+                                          void *stream) {
+  if (step < 1)
+    fail("cost model: Adam steps count from 1");
+  launch_mlp_adam(params, grad, m, v, step, lr, beta1, beta2, eps, (cudaStream_t)stream);
+  CK(cudaGetLastError());
+}
+
+GB300_API void grid_gb300_cost_model_predict(const float *params, const float *x, int n,
+                                             const float *norm, float *y, void *stream) {
+  launch_mlp_predict(params, x, n, norm, y, (cudaStream_t)stream);
+  CK(cudaGetLastError());
+}
+
+GB300_API void grid_gb300_apply_cost_model(const grid_gb300_task_list *task_list,
+                                           const float *params, const float *norm, void *stream) {
+  TaskList *t = TL(task_list);
+  if (t->empty)
+    return;
+  const cudaStream_t s = (cudaStream_t)stream;
+  float *d_x = nullptr, *d_y = nullptr;
+  CK(cudaMalloc((void **)&d_x, sizeof(float) * t->features.size()));
+  CK(cudaMalloc((void **)&d_y, sizeof(float) * t->ntasks));
+  CK(cudaMemcpyAsync(d_x, t->features.data(), sizeof(float) * t->features.size(),
+                     cudaMemcpyHostToDevice, s));
+  launch_mlp_predict(params, d_x, t->ntasks, norm, d_y, s);
+  t->model_cost.resize(t->ntasks);
+  CK(cudaMemcpyAsync(t->model_cost.data(), d_y, sizeof(float) * t->ntasks,
+                     cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  CK(cudaFree(d_x));
+  CK(cudaFree(d_y));
+  for (float &c : t->model_cost)
+    if (!std::isfinite(c))
+      fail("cost model: non-finite prediction");
+  t->sched_version++;
 }
 
 GB300_API void grid_gb300_last_timings(const grid_gb300_task_list *task_list,

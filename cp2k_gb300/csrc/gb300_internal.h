@@ -207,15 +207,33 @@ void launch_coefficients(const CoefArgs &a, int arith, int max_smem_words,
 // `extent` is the largest cube width (2*cmax+2) of the queue for the
 // orthorhombic kernels and the largest j-range of the box for the general ones;
 // it sizes the per-warp shared memory (4 warps per CTA).
+// Launch shape of a persistent grid kernel: inputs (0 = automatic) and, on
+// return, the shape used.
+struct LaunchCfg {
+  int warps = 0;  // warps per CTA (capped by the shared-memory budget)
+  int blocks = 0; // CTAs (automatic: all that fit on the GPU at once)
+};
 void launch_collocate(const GridArgs &a, int arith, bool general, int bucket,
-                      int extent, int nblocks, cudaStream_t s);
+                      int extent, LaunchCfg &cfg, cudaStream_t s);
 void launch_integrate(const GridArgs &a, int arith, bool general, int bucket,
-                      int extent, int nblocks, cudaStream_t s);
+                      int extent, LaunchCfg &cfg, cudaStream_t s);
+inline void launch_collocate(const GridArgs &a, int arith, bool general, int bucket,
+                             int extent, int nblocks, cudaStream_t s) {
+  LaunchCfg c;
+  c.blocks = nblocks;
+  launch_collocate(a, arith, general, bucket, extent, c, s);
+}
+inline void launch_integrate(const GridArgs &a, int arith, bool general, int bucket,
+                             int extent, int nblocks, cudaStream_t s) {
+  LaunchCfg c;
+  c.blocks = nblocks;
+  launch_integrate(a, arith, general, bucket, extent, c, s);
+}
 // general path: FP64 for ARITH_FP64 and ARITH_MIXED, FP32 for ARITH_FP32
 void launch_collocate_general_impl(const GridArgs &a, int arith, int lpb,
-                                   int njmax, int nblocks, cudaStream_t s);
+                                   int njmax, LaunchCfg &cfg, cudaStream_t s);
 void launch_integrate_general_impl(const GridArgs &a, int arith, int lpb,
-                                   int njmax, int nblocks, cudaStream_t s);
+                                   int njmax, LaunchCfg &cfg, cudaStream_t s);
 constexpr int kWarpsPerCta = 4;
 constexpr size_t kSmemBudget = 200 * 1024; // dynamic shared memory per CTA
 // warps per CTA so that per-warp regions fit the budget (0: does not fit)
@@ -251,6 +269,16 @@ void count_launch(int n = 1);
 // records a launch-configuration error; the host call fails after the launch
 // sequence (reported like a device error)
 void launch_error(const char *msg);
+
+// learned cost model (mlp_kernels.cu)
+int mlp_nparams();
+int mlp_tiles(int n);
+void launch_mlp_loss_grad(const float *P, const float *X, const float *T, int n, float *loss,
+                          float *grad, float *work, cudaStream_t s);
+void launch_mlp_adam(float *P, const float *grad, float *m, float *v, int step, float lr,
+                     float beta1, float beta2, float eps, cudaStream_t s);
+void launch_mlp_predict(const float *P, const float *X, int n, const float *norm, float *Y,
+                        cudaStream_t s);
 
 // persistent grid size: CTAs that fit on all SMs at once for this kernel
 int persistent_blocks(const void *kernel, int threads, size_t smem);

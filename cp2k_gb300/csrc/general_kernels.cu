@@ -456,37 +456,36 @@ __global__ void __launch_bounds__(128) integrate_general(GridArgs a, int njmax) 
 }
 
 template <typename T, int LPB>
-void launch_gen(const GridArgs &a, bool collocate, int njmax, int nblocks, cudaStream_t s) {
+void launch_gen(const GridArgs &a, bool collocate, int njmax, LaunchCfg &cfg, cudaStream_t s) {
   const size_t per_warp = GenSmem<T, LPB>::bytes(njmax);
-  const int nw = warps_for(per_warp);
-  const size_t smem = nw * per_warp;
+  int nw = warps_for(per_warp);
   if (nw < 1)
     return launch_error("general path: box too large for shared memory");
-  if (collocate) {
-    auto k = collocate_general<T, LPB>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (nblocks <= 0)
-      nblocks = persistent_blocks((const void *)k, 32 * nw, smem);
-    k<<<nblocks, 32 * nw, smem, s>>>(a, njmax);
-  } else {
-    auto k = integrate_general<T, LPB>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (nblocks <= 0)
-      nblocks = persistent_blocks((const void *)k, 32 * nw, smem);
-    k<<<nblocks, 32 * nw, smem, s>>>(a, njmax);
-  }
+  if (cfg.warps > 0 && cfg.warps < nw)
+    nw = cfg.warps;
+  const size_t smem = nw * per_warp;
+  const void *k = collocate ? (const void *)collocate_general<T, LPB>
+                            : (const void *)integrate_general<T, LPB>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const int nb = cfg.blocks > 0 ? cfg.blocks : persistent_blocks(k, 32 * nw, smem);
+  cfg.warps = nw;
+  cfg.blocks = nb;
+  if (collocate)
+    collocate_general<T, LPB><<<nb, 32 * nw, smem, s>>>(a, njmax);
+  else
+    integrate_general<T, LPB><<<nb, 32 * nw, smem, s>>>(a, njmax);
   count_launch();
 }
 
 void launch_gen_any(const GridArgs &a, bool collocate, bool fp32, int lpb, int njmax,
-                    int nblocks, cudaStream_t s) {
+                    LaunchCfg &cfg, cudaStream_t s) {
   switch (lpb) {
 #define GB_CASE(LP)                                                            \
   case LP:                                                                     \
     if (fp32)                                                                  \
-      launch_gen<float, LP>(a, collocate, njmax, nblocks, s);                  \
+      launch_gen<float, LP>(a, collocate, njmax, cfg, s);                      \
     else                                                                       \
-      launch_gen<double, LP>(a, collocate, njmax, nblocks, s);                 \
+      launch_gen<double, LP>(a, collocate, njmax, cfg, s);                     \
     break;
     GB_CASE(4) GB_CASE(6) GB_CASE(9) GB_CASE(16)
 #undef GB_CASE
@@ -496,13 +495,13 @@ void launch_gen_any(const GridArgs &a, bool collocate, bool fp32, int lpb, int n
 } // namespace
 
 void launch_collocate_general_impl(const GridArgs &a, int arith, int lpb, int njmax,
-                                   int nblocks, cudaStream_t s) {
-  launch_gen_any(a, true, arith == ARITH_FP32, lpb, njmax, nblocks, s);
+                                   LaunchCfg &cfg, cudaStream_t s) {
+  launch_gen_any(a, true, arith == ARITH_FP32, lpb, njmax, cfg, s);
 }
 
 void launch_integrate_general_impl(const GridArgs &a, int arith, int lpb, int njmax,
-                                   int nblocks, cudaStream_t s) {
-  launch_gen_any(a, false, arith == ARITH_FP32, lpb, njmax, nblocks, s);
+                                   LaunchCfg &cfg, cudaStream_t s) {
+  launch_gen_any(a, false, arith == ARITH_FP32, lpb, njmax, cfg, s);
 }
 
 } // namespace gb300

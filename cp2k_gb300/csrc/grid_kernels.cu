@@ -492,67 +492,65 @@ __global__ void __launch_bounds__(128) integrate_ortho(GridArgs a, int wmax) {
 // launch wrappers
 // ------------------------------------------------------------------------
 template <typename N, int LPB>
-static void launch_ortho_t(const GridArgs &a, bool collocate, int wmax, int nblocks,
+static void launch_ortho_t(const GridArgs &a, bool collocate, int wmax, LaunchCfg &cfg,
                            cudaStream_t s) {
   const size_t per_warp =
       collocate ? OrthoSmem<N, LPB>::bytes_coll(wmax) : OrthoSmem<N, LPB>::bytes_int(wmax);
-  const int nw = warps_for(per_warp);
-  const size_t smem = nw * per_warp;
+  int nw = warps_for(per_warp);
   if (nw < 1)
     return launch_error("orthorhombic grid kernel: cube too large for shared memory");
-  if (collocate) {
-    auto k = collocate_ortho<N, LPB>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (nblocks <= 0)
-      nblocks = persistent_blocks((const void *)k, 32 * nw, smem);
-    k<<<nblocks, 32 * nw, smem, s>>>(a, wmax);
-  } else {
-    auto k = integrate_ortho<N, LPB>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (nblocks <= 0)
-      nblocks = persistent_blocks((const void *)k, 32 * nw, smem);
-    k<<<nblocks, 32 * nw, smem, s>>>(a, wmax);
-  }
+  if (cfg.warps > 0 && cfg.warps < nw)
+    nw = cfg.warps;
+  const size_t smem = nw * per_warp;
+  const void *k = collocate ? (const void *)collocate_ortho<N, LPB>
+                            : (const void *)integrate_ortho<N, LPB>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const int nb = cfg.blocks > 0 ? cfg.blocks : persistent_blocks(k, 32 * nw, smem);
+  cfg.warps = nw;
+  cfg.blocks = nb;
+  if (collocate)
+    collocate_ortho<N, LPB><<<nb, 32 * nw, smem, s>>>(a, wmax);
+  else
+    integrate_ortho<N, LPB><<<nb, 32 * nw, smem, s>>>(a, wmax);
   count_launch();
 }
 
 template <int LPB>
-static void launch_ortho_lp(const GridArgs &a, int arith, bool collocate, int wmax, int nblocks,
-                            cudaStream_t s) {
+static void launch_ortho_lp(const GridArgs &a, int arith, bool collocate, int wmax,
+                            LaunchCfg &cfg, cudaStream_t s) {
   if (arith == ARITH_FP64)
-    launch_ortho_t<double, LPB>(a, collocate, wmax, nblocks, s);
+    launch_ortho_t<double, LPB>(a, collocate, wmax, cfg, s);
   else if (arith == ARITH_FP32)
-    launch_ortho_t<float, LPB>(a, collocate, wmax, nblocks, s);
+    launch_ortho_t<float, LPB>(a, collocate, wmax, cfg, s);
   else
-    launch_ortho_t<dfloat, LPB>(a, collocate, wmax, nblocks, s);
+    launch_ortho_t<dfloat, LPB>(a, collocate, wmax, cfg, s);
+}
+
+static void launch_grid(const GridArgs &a, int arith, bool general, bool collocate, int bucket,
+                        int extent, LaunchCfg &cfg, cudaStream_t s) {
+  if (general) {
+    if (collocate)
+      launch_collocate_general_impl(a, arith, kBucketLp[bucket], extent, cfg, s);
+    else
+      launch_integrate_general_impl(a, arith, kBucketLp[bucket], extent, cfg, s);
+    return;
+  }
+  switch (kBucketLp[bucket]) {
+  case 4: launch_ortho_lp<4>(a, arith, collocate, extent, cfg, s); break;
+  case 6: launch_ortho_lp<6>(a, arith, collocate, extent, cfg, s); break;
+  case 9: launch_ortho_lp<9>(a, arith, collocate, extent, cfg, s); break;
+  case 16: launch_ortho_lp<16>(a, arith, collocate, extent, cfg, s); break;
+  }
 }
 
 void launch_collocate(const GridArgs &a, int arith, bool general, int bucket, int extent,
-                      int nblocks, cudaStream_t s) {
-  if (general) {
-    launch_collocate_general_impl(a, arith, kBucketLp[bucket], extent, nblocks, s);
-    return;
-  }
-  switch (kBucketLp[bucket]) {
-  case 4: launch_ortho_lp<4>(a, arith, true, extent, nblocks, s); break;
-  case 6: launch_ortho_lp<6>(a, arith, true, extent, nblocks, s); break;
-  case 9: launch_ortho_lp<9>(a, arith, true, extent, nblocks, s); break;
-  case 16: launch_ortho_lp<16>(a, arith, true, extent, nblocks, s); break;
-  }
+                      LaunchCfg &cfg, cudaStream_t s) {
+  launch_grid(a, arith, general, true, bucket, extent, cfg, s);
 }
 
 void launch_integrate(const GridArgs &a, int arith, bool general, int bucket, int extent,
-                      int nblocks, cudaStream_t s) {
-  if (general) {
-    launch_integrate_general_impl(a, arith, kBucketLp[bucket], extent, nblocks, s);
-    return;
-  }
-  switch (kBucketLp[bucket]) {
-  case 4: launch_ortho_lp<4>(a, arith, false, extent, nblocks, s); break;
-  case 6: launch_ortho_lp<6>(a, arith, false, extent, nblocks, s); break;
-  case 9: launch_ortho_lp<9>(a, arith, false, extent, nblocks, s); break;
-  case 16: launch_ortho_lp<16>(a, arith, false, extent, nblocks, s); break;
-  }
+                      LaunchCfg &cfg, cudaStream_t s) {
+  launch_grid(a, arith, general, false, bucket, extent, cfg, s);
 }
 
 // ------------------------------------------------------------------------

@@ -98,10 +98,30 @@ def lib():
         L.grid_gb300_backend_handle.argtypes = [vp]
         L.grid_gb300_backend_handle.restype = vp
         L.grid_gb300_kernel_launches.restype = C.c_longlong
+        L.grid_gb300_set_launch_timing.argtypes = [vp, C.c_int]
+        L.grid_gb300_launch_timings.argtypes = [vp, C.c_int, vp]
+        L.grid_gb300_launch_timings.restype = C.c_int
+        L.grid_gb300_set_task_timing.argtypes = [vp, C.c_int]
+        L.grid_gb300_task_cycles.argtypes = [vp, vp]
+        L.grid_gb300_task_features.argtypes = [vp, vp]
+        L.grid_gb300_cost_model_nparams.restype = C.c_int
+        L.grid_gb300_cost_model_work_floats.argtypes = [C.c_int]
+        L.grid_gb300_cost_model_work_floats.restype = C.c_size_t
+        L.grid_gb300_cost_model_loss_grad.argtypes = [vp, vp, vp, C.c_int, vp, vp, vp, vp]
+        L.grid_gb300_cost_model_adam.argtypes = [vp, vp, vp, vp, C.c_int] + [C.c_float] * 4 + [vp]
+        L.grid_gb300_cost_model_predict.argtypes = [vp, vp, C.c_int, vp, vp, vp]
+        L.grid_gb300_apply_cost_model.argtypes = [vp, vp, vp, vp]
         L.grid_gb300_last_error.restype = C.c_char_p
         L.grid_library_init()
         _LIB = L
     return _LIB
+
+
+class LaunchInfo(C.Structure):
+    _fields_ = [("phase", C.c_int), ("precision", C.c_int), ("general", C.c_int),
+                ("lp_bucket", C.c_int), ("ntasks", C.c_int), ("warps_per_block", C.c_int),
+                ("blocks", C.c_int), ("points", C.c_longlong), ("flops", C.c_double),
+                ("ms", C.c_double)]
 
 
 def kernel_launches() -> int:
@@ -228,6 +248,33 @@ class GridTaskList:
         lp = np.zeros(n, np.int32)
         lib().grid_gb300_task_sizes(self.impl, _p(pts), _p(lp))
         return pts, lp
+
+    def set_launch_timing(self, enable: bool = True):
+        lib().grid_gb300_set_launch_timing(self.impl, int(bool(enable)))
+
+    def launch_timings(self):
+        """Per grid-kernel launch of the last call (launch timing enabled):
+        list of dicts with phase, precision, general, lp_bucket, ntasks,
+        warps_per_block, blocks, points, flops, ms."""
+        n = lib().grid_gb300_launch_timings(self.impl, 0, None)
+        arr = (LaunchInfo * max(n, 1))()
+        lib().grid_gb300_launch_timings(self.impl, n, C.cast(arr, C.c_void_p))
+        return [{f: getattr(arr[i], f) for f, _ in LaunchInfo._fields_} for i in range(n)]
+
+    def set_task_timing(self, enable: bool = True):
+        lib().grid_gb300_set_task_timing(self.impl, int(bool(enable)))
+
+    def task_cycles(self) -> np.ndarray:
+        """clock64 cycles per task (input order) of the last call."""
+        c = np.zeros(self.inp.ntasks, np.int64)
+        lib().grid_gb300_task_cycles(self.impl, _p(c))
+        return c
+
+    def task_features(self) -> np.ndarray:
+        """[ntasks][6] cost-model features in input order."""
+        f = np.zeros((self.inp.ntasks, 6), np.float32)
+        lib().grid_gb300_task_features(self.impl, _p(f))
+        return f
 
     def timings(self):
         t = np.zeros(4)

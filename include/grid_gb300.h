@@ -313,6 +313,75 @@ void grid_gb300_last_timings(const grid_gb300_task_list *task_list,
 /* Number of kernels this library launched on the device since load. */
 long long grid_gb300_kernel_launches(void);
 
+/* Per-launch timing of the grid kernels (off by default).  When enabled,
+ * every collocate/integrate call records CUDA events around each grid-kernel
+ * launch; grid_gb300_launch_timings waits for the last call and copies up to
+ * `max` records, returning how many launches that call made. */
+typedef struct {
+  int phase;          /* 0 collocate, 1 integrate */
+  int precision;      /* arithmetic of the launch: GRID_GB300_FP64 / _MIXED
+                         (double-float) / _FP32 */
+  int general;        /* 1: general (non-orthorhombic or border) kernel */
+  int lp_bucket;      /* lp limit of the kernel instance (4, 6, 9, 16) */
+  int ntasks;         /* tasks in the launch */
+  int warps_per_block;
+  int blocks;
+  long long points;   /* grid points the tasks visit */
+  double flops;       /* sum over tasks of 2 (lp+1) points */
+  double ms;          /* CUDA-event duration on the launching stream */
+} grid_gb300_launch_info;
+void grid_gb300_set_launch_timing(const grid_gb300_task_list *task_list,
+                                  int enable);
+int grid_gb300_launch_timings(const grid_gb300_task_list *task_list, int max,
+                              grid_gb300_launch_info *info);
+
+/* ---- learned task-cost model ------------------------------------------
+ * A 6 -> 64 -> 64 -> 1 MLP (SiLU, FP32) predicting log(task time) from the
+ * task features below; its prediction orders the work queues under
+ * GRID_GB300_SCHEDULE_MODEL.  Parameters are one flat FP32 device array of
+ * grid_gb300_cost_model_nparams() words:
+ *   W1[64][6] b1[64] W2[64][64] b2[64] w3[64] b3.
+ * All pointers below are device pointers; work is enqueued on `stream`. */
+int grid_gb300_cost_model_nparams(void);
+
+/* Task features in the caller's task order, [ntasks][6] host floats:
+ * la_max, lb_max, zeta_a + zeta_b, cube radius (grid points), level grid
+ * spacing (bohr), cell skew (1 - |det h| / (|a| |b| |c|)). */
+void grid_gb300_task_features(const grid_gb300_task_list *task_list,
+                              float *features);
+
+/* Per-task timing (off by default): when enabled, the grid kernels record
+ * the clock64() cycles each task took; grid_gb300_task_cycles copies the
+ * cycles of the last call in the caller's task order (0 for tasks that were
+ * skipped). */
+void grid_gb300_set_task_timing(const grid_gb300_task_list *task_list,
+                                int enable);
+void grid_gb300_task_cycles(const grid_gb300_task_list *task_list,
+                            long long *cycles);
+
+/* Training: loss = mean squared error of the prediction for the n samples
+ * x[n][6] (standardised features) against targets t[n]; writes the loss
+ * (one float) and its gradient (nparams floats).  `work` must hold
+ * grid_gb300_cost_model_work_floats(n) floats.  Deterministic. */
+size_t grid_gb300_cost_model_work_floats(int n);
+void grid_gb300_cost_model_loss_grad(const float *params, const float *x,
+                                     const float *t, int n, float *loss,
+                                     float *grad, float *work, void *stream);
+/* One Adam step (step counts from 1). */
+void grid_gb300_cost_model_adam(float *params, const float *grad, float *m,
+                                float *v, int step, float lr, float beta1,
+                                float beta2, float eps, void *stream);
+/* Inference: y[s] for raw features x[n][6] standardised on the fly by
+ * norm = {mean[6], scale[6]} (NULL: none). */
+void grid_gb300_cost_model_predict(const float *params, const float *x, int n,
+                                   const float *norm, float *y, void *stream);
+/* Predicts the cost of every task of the list with the given parameters
+ * and normalisation (device pointers) and uses it for
+ * GRID_GB300_SCHEDULE_MODEL.  Synchronises `stream`. */
+void grid_gb300_apply_cost_model(const grid_gb300_task_list *task_list,
+                                 const float *params, const float *norm,
+                                 void *stream);
+
 /* Allocation-free collocation of one primitive pair, for callers that
  * cannot allocate device memory at call time (inside CUDA-graph capture, under
  * a fixed memory arena, in drivers that forbid cudaMalloc after start-up).
