@@ -257,7 +257,11 @@ def measure_fp32_peak(torch):
 # DRAM bytes per launch of the dominant kernels, from the ncu capture named
 # beside each figure (dram__bytes_read.sum + dram__bytes_write.sum); the
 # bench cannot run ncu itself.  Keys: kernel label as in "roofline.kernel".
-NCU_TRAFFIC = {}
+NCU_TRAFFIC = {
+    # profiles/grid_kernels_c2_512atoms_mixed.md (2 launches each, mean)
+    "collocate_ortho<dfloat,4>": 0.5 * ((57.029 + 32.069) + (407.416 + 1458.588)) * 1e6,
+    "integrate_ortho<dfloat,4>": 0.5 * ((39.392 + 0.917) + (322.533 + 42.050)) * 1e6,
+}
 
 
 def _kernel_label(info):
@@ -301,6 +305,15 @@ def gpu_arm(args, world, rank, local):
         with torch.cuda.stream(stream):
             model.apply(tl, stream=stream)
     sched_mixed = G.SCHEDULE_MODEL if model is not None else G.SCHEDULE_SIZE
+    # autotuned size split and launch shapes, per precision, on this workload
+    tuned = {}
+    for prec, sched in ((G.MIXED, sched_mixed), (G.FP64, G.SCHEDULE_SIZE),
+                        (G.FP32, sched_mixed)):
+        tl.set_precision(prec)
+        tl.set_schedule(sched)
+        with torch.cuda.stream(stream):
+            tuned[prec] = (tl.autotune(100, pab, grids, V, hab, stream=stream), tl.tuned_split())
+        torch.cuda.synchronize()
 
     def run_steps(prec, sched, nsteps):
         tl.set_precision(prec)
@@ -334,6 +347,21 @@ def gpu_arm(args, world, rank, local):
     barrier(world)
     rho_mixed = [g.clone() for g in grids]
     hab_mixed = hab.clone()
+    # the same step replayed as one CUDA graph
+    graph = tl.capture_step(100, pab, grids, V, hab, stream=stream)
+    t_graph = []
+    for _ in range(max(1, min(args.steps, 5))):
+        flush.zero_()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            e[0].record(stream)
+            graph.launch(stream=stream)
+            e[1].record(stream)
+        graph.wait(stream=stream)
+        t_graph.append(e[0].elapsed_time(e[1]))
+    graph_kernels = graph.kernels
+    graph.free()
     t_size = run_steps(G.MIXED, G.SCHEDULE_SIZE, max(1, min(args.steps, 5)))
     t_fp64 = run_steps(G.FP64, G.SCHEDULE_SIZE, max(1, min(args.steps, 3)))
     rho64 = [g.clone() for g in grids]
@@ -373,8 +401,17 @@ def gpu_arm(args, world, rank, local):
     dom = max(per_kernel, key=lambda k: sum(per_kernel[k]["ms"]))
     d = per_kernel[dom]
     avg_ms = float(np.mean(d["ms"]))
-    bytes_per_point = {"dfloat": 8.0, "double": 8.0, "float": 4.0}[dom.split("<")[1].split(",")[0]]
-    alg_bytes = bytes_per_point * d["points"] / d["launches"]
+    # algorithmic HBM bytes of one launch: every grid point written once
+    # (collocate: FP64 grid, 8 B, plus the FP32 low-word grid for double-float,
+    # 4 B) or read once (integrate: float2 / double 8 B, float 4 B); the many
+    # per-task visits of a point are L2 traffic, not HBM traffic
+    arith = dom.split("<")[1].split(",")[0]
+    if dom.startswith("collocate"):
+        bytes_per_point = 12.0 if arith == "dfloat" else 8.0
+    else:
+        bytes_per_point = 4.0 if arith == "float" else 8.0
+    alg_bytes = bytes_per_point * float(sum(inp.grid_sizes()))
+    visit_bytes = bytes_per_point * d["points"] / d["launches"]
     alg_flops = d["flops"] / d["launches"]
     kernel_share = {k: sum(v["ms"]) / sum(sum(x["ms"]) for x in per_kernel.values())
                     for k, v in sorted(per_kernel.items(), key=lambda kv: -sum(kv[1]["ms"]))}
@@ -438,6 +475,10 @@ def gpu_arm(args, world, rank, local):
                        "cost_model": model_path},
             "fp64_ms_per_step": ms_fp64, "speedup_vs_fp64": ms_fp64 / ms_mixed,
             "mixed_size_schedule_ms_per_step": ms_size,
+            "mixed_cuda_graph_ms_per_step": max_over_ranks(float(np.mean(t_graph)), world),
+            "cuda_graph_kernels": int(graph_kernels),
+            "autotune": {{0: "fp64", 1: "mixed", 2: "fp32"}[p]: {"grid_ms": v[0], "size_split": v[1]}
+                         for p, v in tuned.items()},
             "cost_model_gain": ms_size / ms_mixed - 1.0,
             "fp32_ms_per_step": ms_fp32, "fp32_speedup_vs_fp64": ms_fp64 / ms_fp32,
             "errors_mixed_vs_fp64": err_mixed,
@@ -448,6 +489,7 @@ def gpu_arm(args, world, rank, local):
                          "unit": "GB/s", "frac": achieved_gbs / peaks.get("hbm_gbs", 1.0),
                          "traffic": traffic, "kernel": dom, "launch_ms": avg_ms,
                          "algorithmic_bytes_per_launch": alg_bytes,
+                         "grid_visit_bytes_per_launch": visit_bytes,
                          "peak_kind": peak_kind},
             "roofline_fp32": {"bound": "fp32_fma", "achieved": achieved_tf, "peak": fp32_peak,
                               "unit": "TFLOP/s", "frac": achieved_tf / fp32_peak,

@@ -23,6 +23,7 @@
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "gb300_internal.h"
@@ -245,11 +246,13 @@ struct Queue {
 // per-launch CUDA-event timing of the grid kernels (opt-in)
 struct LaunchRecord {
   grid_gb300_launch_info info;
+  int key = 0;
   cudaEvent_t a = nullptr, b = nullptr;
 };
 
 // cube widths up to this share one work queue; wider cubes get their own so
-// that the common small cubes run with small per-warp tables (more warps)
+// that the common small cubes run with small per-warp tables (more warps);
+// the autotuner may move the split per task list
 constexpr int kSmallExtent = 34;
 
 struct Mode { // everything that depends on the l shifts of a call
@@ -275,14 +278,19 @@ struct TaskList {
   std::vector<SubblockDesc> subs;
   std::vector<SphereHdr> sph;
   std::vector<int16_t> sph_tab;
+  std::vector<int> sph_pts, sph_ploff; // point lists of the spheres
   std::vector<long long> points; // per task (block order)
   std::vector<float> model_cost; // per task, empty unless a model was applied
   std::vector<float> features;   // per task [6]: cost-model inputs (block order)
   bool task_timing = false;      // record clock64 cycles per task
   bool launch_timing = false;    // record CUDA events around every grid launch
+  bool capturing = false;        // inside grid_gb300_capture_step: no timing events
+  long long gen = 0;             // bumped whenever a device array the kernels use moves
   std::vector<LaunchRecord> launches; // of the last call
   std::vector<cudaEvent_t> event_pool;
-  std::map<std::pair<int, int>, LaunchCfg> tuned; // (phase, queue key) -> launch shape
+  std::map<std::tuple<int, int, int>, LaunchCfg> tuned; // (precision, phase, queue key) -> shape
+  int small_extent[3] = {kSmallExtent, kSmallExtent, kSmallExtent}; // per precision
+  int coll_variant = 1; // orthorhombic collocate lane mapping: 0 row walk, 1 point list
   std::vector<double> gbound;    // per task bound of |contribution| for |P| <= 1
   std::vector<float2> seeds;     // per task [3][6] dfloat recurrence seeds (ortho)
   float2 *d_seeds = nullptr;
@@ -295,6 +303,7 @@ struct TaskList {
   SubblockDesc *d_subs = nullptr;
   SphereHdr *d_sph = nullptr;
   int16_t *d_sph_tab = nullptr;
+  int *d_sph_pts = nullptr, *d_sph_ploff = nullptr;
   double *d_atom_pos = nullptr;
   double *d_sphi = nullptr;
   LevelSet *d_levels = nullptr;
@@ -359,6 +368,7 @@ static LDiffs integrate_ldiffs(bool forces, bool virial, bool tau) {
 // expressions (grid_ref_collint.h:237-245, 139-151, 44-52).
 void build_sphere(const LevelDesc &L, double disr, SphereHdr &h, std::vector<int16_t> &tab,
                   long long &npoints) {
+  h.plo = -1;
   for (int i = 0; i < 3; i++)
     h.lb[i] = (int)ceil(-1e-8 - disr * L.dh_inv[i * 4]);
   h.cmax = std::max(std::max(1 - h.lb[0], 1 - h.lb[1]), 1 - h.lb[2]);
@@ -408,6 +418,26 @@ void build_sphere(const LevelDesc &L, double disr, SphereHdr &h, std::vector<int
   tab.insert(tab.end(), jx.begin(), jx.end());
 }
 
+void build_sphere_points(SphereHdr &h, const std::vector<int16_t> &tab, std::vector<int> &pts,
+                         std::vector<int> &ploff) {
+  const int K = 1 - h.lb[2];
+  const int16_t *t = tab.data() + h.off;
+  h.plo = (int)ploff.size();
+  for (int kk = 0; kk < K; kk++) {
+    ploff.push_back((int)pts.size());
+    const int js = t[kk], row0 = t[K + kk];
+    for (int j = js; j <= 1 - js; j++) {
+      const int jj = j <= 0 ? -j : j - 1;
+      const int i0 = t[2 * K + row0 + jj];
+      for (int x = i0; x <= 1 - i0; x++)
+        pts.push_back((int)((unsigned)(x & 0xffff) | ((unsigned)j << 16)));
+    }
+  }
+  ploff.push_back((int)pts.size());
+  if (pts.size() > (size_t)INT32_MAX)
+    fail("sphere point lists exceed int offsets");
+}
+
 // Upper bound of |a Gaussian-product contribution| for |P_ab| <= 1: the
 // prefactor times, per direction, the sum over the binomial expansion
 // coefficients of (x-a)^i (x-b)^j about p of max_x |x^n exp(-zetp x^2)|
@@ -451,7 +481,8 @@ template <typename T> static T *dalloc_copy(const std::vector<T> &v) {
 }
 
 static void free_device(TaskList *t) {
-  void *ptrs[] = {t->d_seeds, t->d_tasks, t->d_subs, t->d_sph, t->d_sph_tab, t->d_atom_pos, t->d_sphi,
+  void *ptrs[] = {t->d_seeds, t->d_tasks, t->d_subs, t->d_sph, t->d_sph_tab, t->d_sph_pts,
+                  t->d_sph_ploff, t->d_atom_pos, t->d_sphi,
                   t->d_levels, t->d_pab_cart, t->d_hab_cart, t->d_coef, t->d_coef_int,
                   t->d_forces, t->d_virial, t->d_counters, t->d_error, t->d_cycles};
   for (void *p : ptrs)
@@ -642,6 +673,7 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
         SphereHdr h;
         long long np = 0;
         build_sphere(L, drmin * nrad, h, t->sph_tab, np);
+        build_sphere_points(h, t->sph_tab, t->sph_pts, t->sph_ploff);
         t->sph.push_back(h);
         sphere_points.push_back(np);
         it = sphere_of.emplace(key, (int)t->sph.size() - 1).first;
@@ -775,6 +807,8 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
   t->d_subs = dalloc_copy(t->subs);
   t->d_sph = dalloc_copy(t->sph);
   t->d_sph_tab = dalloc_copy(t->sph_tab);
+  t->d_sph_pts = dalloc_copy(t->sph_pts);
+  t->d_sph_ploff = dalloc_copy(t->sph_ploff);
   t->d_atom_pos = dalloc_copy(std::vector<double>(atom_positions, atom_positions + 3 * natoms));
   t->d_sphi = dalloc_copy(sphi_all);
   CK(cudaMalloc((void **)&t->d_levels, sizeof(LevelSet)));
@@ -834,7 +868,7 @@ static Mode &get_mode(TaskList *t, const LDiffs &d) {
     const int cls = (t->precision == GRID_GB300_MIXED && g == 0 &&
                      t->gbound[s] <= t->mixed_threshold) ? 1 : 0;
     const int ext = g == 0 ? 2 * t->sph[k.sphere].cmax + 2 : k.imax[1] - k.center[1] + 1;
-    const int sz = ext <= kSmallExtent ? 0 : 1;
+    const int sz = ext <= t->small_extent[t->precision] ? 0 : 1;
     double cost;
     if (t->schedule == GRID_GB300_SCHEDULE_INPUT)
       cost = -(double)k.orig;
@@ -890,16 +924,19 @@ static Mode &get_mode(TaskList *t, const LDiffs &d) {
     m.queues.push_back(q);
   }
   m.sched_version = t->sched_version;
+  t->gen++;
   return m;
 }
 
-static void ensure(void **p, size_t *cap, size_t bytes) {
+// returns 1 when the buffer was (re)allocated
+static int ensure(void **p, size_t *cap, size_t bytes) {
   if (*cap >= bytes && *p)
-    return;
+    return 0;
   if (*p)
     CK(cudaFree(*p));
   CK(cudaMalloc(p, std::max<size_t>(bytes, 16)));
   *cap = bytes;
+  return 1;
 }
 
 static void check_device_error(TaskList *t) {
@@ -925,6 +962,11 @@ static void read_timings(TaskList *t) {
   t->timings[3] = ev_ms(t->ev[0], t->ev[3]);
 }
 
+static void record_phase(TaskList *t, int i, cudaStream_t s) {
+  if (!t->capturing)
+    CK(cudaEventRecord(t->ev[i], s));
+}
+
 static cudaEvent_t pool_event(TaskList *t, size_t i) {
   while (t->event_pool.size() <= i) {
     cudaEvent_t e;
@@ -939,11 +981,13 @@ static cudaEvent_t pool_event(TaskList *t, size_t i) {
 static void grid_launch(TaskList *t, const Queue &q, int phase, int arith, const GridArgs &ga,
                         cudaStream_t s) {
   LaunchCfg cfg;
-  auto it = t->tuned.find({phase, q.key});
+  cfg.variant = t->coll_variant;
+  auto it = t->tuned.find(std::make_tuple(t->precision, phase, q.key));
   if (it != t->tuned.end())
     cfg = it->second;
   LaunchRecord rec;
-  if (t->launch_timing) {
+  const bool timed = t->launch_timing && !t->capturing;
+  if (timed) {
     rec.a = pool_event(t, 2 * t->launches.size());
     rec.b = pool_event(t, 2 * t->launches.size() + 1);
     CK(cudaEventRecord(rec.a, s));
@@ -952,7 +996,7 @@ static void grid_launch(TaskList *t, const Queue &q, int phase, int arith, const
     launch_collocate(ga, arith, q.general == 1, q.bucket, q.extent, cfg, s);
   else
     launch_integrate(ga, arith, q.general == 1, q.bucket, q.extent, cfg, s);
-  if (t->launch_timing) {
+  if (timed) {
     CK(cudaEventRecord(rec.b, s));
     grid_gb300_launch_info &in = rec.info;
     in.phase = phase;
@@ -965,15 +1009,19 @@ static void grid_launch(TaskList *t, const Queue &q, int phase, int arith, const
     in.points = q.points;
     in.flops = q.flops;
     in.ms = 0.0;
+    rec.key = q.key;
     t->launches.push_back(rec);
   }
 }
 
 static void begin_call(TaskList *t, cudaStream_t s) {
-  t->launches.clear();
+  if (!t->capturing)
+    t->launches.clear();
   if (t->task_timing) {
-    if (!t->d_cycles)
+    if (!t->d_cycles) {
       CK(cudaMalloc((void **)&t->d_cycles, sizeof(long long) * std::max(t->ntasks, 1)));
+      t->gen++;
+    }
     CK(cudaMemsetAsync(t->d_cycles, 0, sizeof(long long) * std::max(t->ntasks, 1), s));
   }
 }
@@ -983,23 +1031,25 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
   const LDiffs d = func_ldiffs(func);
   Mode &m = get_mode(t, d);
   const int arith = t->precision;
-  ensure(&t->d_coef, &t->coef_cap, m.coef_total * (arith == ARITH_FP32 ? 4 : 8));
+  t->gen += ensure(&t->d_coef, &t->coef_cap, m.coef_total * (arith == ARITH_FP32 ? 4 : 8));
   begin_call(t, s);
-  CK(cudaEventRecord(t->ev[0], s));
+  record_phase(t, 0, s);
   ContractArgs ca{t->d_subs, (int)t->subs.size(), t->d_sphi, pab, nullptr, t->d_pab_cart,
                   t->contract_words};
   launch_decontract(ca, s);
   CoefArgs co{t->d_tasks, t->d_subs, m.d_coef_off, t->d_atom_pos, t->d_pab_cart, t->d_coef,
               t->ntasks, func, d, t->d_levels, arith == ARITH_MIXED ? 1 : 0};
   launch_coefficients(co, arith, m.coef_words, s);
-  CK(cudaEventRecord(t->ev[1], s));
+  record_phase(t, 1, s);
   for (int l = 0; l < t->nlevels; l++) {
     const int *n = &t->npts_local[3 * l];
     const size_t np = (size_t)n[0] * n[1] * n[2];
     CK(cudaMemsetAsync(grids[l], 0, sizeof(double) * np, s));
     if (arith == ARITH_MIXED) {
-      if (!t->d_gridlo[l])
+      if (!t->d_gridlo[l]) {
         CK(cudaMalloc((void **)&t->d_gridlo[l], sizeof(float) * np));
+        t->gen++;
+      }
       CK(cudaMemsetAsync(t->d_gridlo[l], 0, sizeof(float) * np, s));
     }
   }
@@ -1012,6 +1062,8 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
   ga.coef = t->d_coef;
   ga.sph = t->d_sph;
   ga.sph_tab = t->d_sph_tab;
+  ga.sph_pts = t->d_sph_pts;
+  ga.sph_ploff = t->d_sph_ploff;
   for (int l = 0; l < t->nlevels; l++) {
     ga.grids[l] = grids[l];
     ga.grids_lo[l] = t->d_gridlo[l];
@@ -1037,8 +1089,8 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
       launch_grid_fold_lo(grids[l], t->d_gridlo[l], (size_t)n[0] * n[1] * n[2], s);
     }
   CK(cudaGetLastError());
-  CK(cudaEventRecord(t->ev[2], s));
-  CK(cudaEventRecord(t->ev[3], s));
+  record_phase(t, 2, s);
+  record_phase(t, 3, s);
 }
 
 static void run_integrate(TaskList *t, bool tau, const double *pab, const double *const *grids,
@@ -1047,15 +1099,17 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
   Mode &m = get_mode(t, d);
   const int arith = t->precision;
   const bool need_pab = forces != nullptr || virial != nullptr;
-  ensure((void **)&t->d_coef_int, &t->coef_int_cap, m.coef_total * 8);
+  t->gen += ensure((void **)&t->d_coef_int, &t->coef_int_cap, m.coef_total * 8);
   begin_call(t, s);
-  CK(cudaEventRecord(t->ev[0], s));
+  record_phase(t, 0, s);
   if (arith != ARITH_FP64)
     for (int l = 0; l < t->nlevels; l++) {
       const int *n = &t->npts_local[3 * l];
       const size_t np = (size_t)n[0] * n[1] * n[2];
-      if (!t->d_gridsplit[l])
+      if (!t->d_gridsplit[l]) {
         CK(cudaMalloc(&t->d_gridsplit[l], sizeof(float2) * np));
+        t->gen++;
+      }
       launch_grid_split(grids[l], t->d_gridsplit[l], np, arith, s);
     }
   if (need_pab) {
@@ -1064,7 +1118,7 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
     launch_decontract(ca, s);
   }
   CK(cudaMemsetAsync(t->d_counters, 0, sizeof(int) * 64, s));
-  CK(cudaEventRecord(t->ev[1], s));
+  record_phase(t, 1, s);
   GridArgs ga{};
   ga.coef_stride = 1;
   ga.grid_stride = 1;
@@ -1073,6 +1127,8 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
   ga.coef_out = t->d_coef_int;
   ga.sph = t->d_sph;
   ga.sph_tab = t->d_sph_tab;
+  ga.sph_pts = t->d_sph_pts;
+  ga.sph_ploff = t->d_sph_ploff;
   for (int l = 0; l < t->nlevels; l++)
     ga.grids_in[l] = arith != ARITH_FP64 ? (const void *)t->d_gridsplit[l] : (const void *)grids[l];
   ga.levels = t->levels;
@@ -1094,7 +1150,7 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
                              q.general ? GRID_INTEGRATE_GENERAL : GRID_INTEGRATE_ORTHO, q.n);
   }
   CK(cudaGetLastError());
-  CK(cudaEventRecord(t->ev[2], s));
+  record_phase(t, 2, s);
   CK(cudaMemsetAsync(t->d_hab_cart, 0, sizeof(double) * std::max<size_t>(t->cart_total, 1), s));
   if (forces)
     CK(cudaMemsetAsync(forces, 0, sizeof(double) * 3 * t->natoms, s));
@@ -1109,7 +1165,7 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
                   t->contract_words};
   launch_contract_hab(cb, s);
   CK(cudaGetLastError());
-  CK(cudaEventRecord(t->ev[3], s));
+  record_phase(t, 3, s);
 }
 
 static TaskList *TL(const void *p) {
@@ -1432,6 +1488,220 @@ GB300_API void grid_gb300_task_sizes(const grid_gb300_task_list *task_list, long
     if (lp)
       lp[k.orig] = k.la_max + k.lb_max;
   }
+}
+
+// ---------------------------------------------------------------------------
+// CUDA-graph capture of one SCF step
+// ---------------------------------------------------------------------------
+namespace gb300 {
+struct StepGraph {
+  TaskList *t = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  long long kernels = 0;
+  long long gen = 0;
+  int sched_version = 0, precision = 0;
+  bool task_timing = false;
+};
+} // namespace gb300
+
+GB300_API grid_gb300_step_graph *grid_gb300_capture_step(
+    const grid_gb300_task_list *task_list, int func, const double *pab_blocks,
+    double *const *rho_grids, bool compute_tau, const double *const *v_grids, double *hab_blocks,
+    double *forces, double *virial, void *stream) {
+  TaskList *t = TL(task_list);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!s)
+    fail("capture_step: needs a created stream (the legacy default stream cannot be captured)");
+  // one plain run: creates the work queues and the lazily allocated arrays
+  // so that the captured sequence allocates nothing
+  grid_gb300_collocate_device_async(task_list, func, pab_blocks, rho_grids, stream);
+  grid_gb300_integrate_device_async(task_list, compute_tau, pab_blocks, v_grids, hab_blocks,
+                                    forces, virial, stream);
+  CK(cudaStreamSynchronize(s));
+  check_device_error(t);
+  StepGraph *g = new StepGraph;
+  g->t = t;
+  g->gen = t->gen;
+  const long long k0 = grid_gb300_kernel_launches();
+  t->capturing = true;
+  CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  grid_gb300_collocate_device_async(task_list, func, pab_blocks, rho_grids, stream);
+  grid_gb300_integrate_device_async(task_list, compute_tau, pab_blocks, v_grids, hab_blocks,
+                                    forces, virial, stream);
+  const cudaError_t e = cudaStreamEndCapture(s, &g->graph);
+  t->capturing = false;
+  if (e != cudaSuccess)
+    fail("capture_step: stream capture failed: %s", cudaGetErrorString(e));
+  if (t->gen != g->gen)
+    fail("capture_step: device arrays moved during capture");
+  g->kernels = grid_gb300_kernel_launches() - k0;
+  g_launches -= g->kernels; // capturing launches nothing
+  CK(cudaGraphInstantiate(&g->exec, g->graph, 0));
+  g->sched_version = t->sched_version;
+  g->precision = t->precision;
+  g->task_timing = t->task_timing;
+  return (grid_gb300_step_graph *)g;
+}
+
+GB300_API void grid_gb300_step_graph_launch(grid_gb300_step_graph *graph, void *stream) {
+  StepGraph *g = (StepGraph *)graph;
+  if (!g)
+    fail("null step graph");
+  const TaskList *t = g->t;
+  if (t->gen != g->gen || t->sched_version != g->sched_version ||
+      t->precision != g->precision || t->task_timing != g->task_timing)
+    fail("step graph: the task list changed since capture (precision, schedule, timing or "
+         "buffers); capture again");
+  CK(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
+  count_launch((int)g->kernels);
+}
+
+GB300_API void grid_gb300_step_graph_wait(grid_gb300_step_graph *graph, void *stream) {
+  StepGraph *g = (StepGraph *)graph;
+  if (!g)
+    fail("null step graph");
+  CK(cudaStreamSynchronize((cudaStream_t)stream));
+  check_device_error(g->t);
+}
+
+GB300_API long long grid_gb300_step_graph_kernels(const grid_gb300_step_graph *graph) {
+  return graph ? ((const StepGraph *)graph)->kernels : 0;
+}
+
+GB300_API void grid_gb300_step_graph_free(grid_gb300_step_graph *graph) {
+  StepGraph *g = (StepGraph *)graph;
+  if (!g)
+    return;
+  if (g->exec)
+    cudaGraphExecDestroy(g->exec);
+  if (g->graph)
+    cudaGraphDestroy(g->graph);
+  delete g;
+}
+
+// ---------------------------------------------------------------------------
+// autotuner: size-class split and per-queue launch shapes, by measurement
+// ---------------------------------------------------------------------------
+namespace gb300 {
+// one SCF step with per-launch events; returns the summed grid-kernel time
+// and appends (phase, key, ms) of every grid launch
+static double tune_step(TaskList *t, int func, const double *pab, double *const *rho,
+                        const double *const *v, double *hab, cudaStream_t s,
+                        std::vector<std::tuple<int, int, double>> *out) {
+  double total = 0.0;
+  for (int phase = 0; phase < 2; phase++) {
+    if (phase == 0)
+      run_collocate(t, func, pab, rho, s);
+    else
+      run_integrate(t, false, pab, v, hab, nullptr, nullptr, s);
+    CK(cudaStreamSynchronize(s));
+    check_device_error(t);
+    for (LaunchRecord &r : t->launches) {
+      const double ms = ev_ms(r.a, r.b);
+      total += ms;
+      if (out)
+        out->emplace_back(phase, r.key, ms);
+    }
+  }
+  return total;
+}
+} // namespace gb300
+
+GB300_API double grid_gb300_autotune(const grid_gb300_task_list *task_list, int func,
+                                     const double *pab_blocks, double *const *rho_grids,
+                                     const double *const *v_grids, double *hab_blocks,
+                                     void *stream) {
+  TaskList *t = TL(task_list);
+  if (t->empty)
+    return 0.0;
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool lt = t->launch_timing;
+  t->launch_timing = true;
+  const int prec = t->precision;
+  for (auto it = t->tuned.begin(); it != t->tuned.end();)
+    it = std::get<0>(it->first) == prec ? t->tuned.erase(it) : std::next(it);
+  // 1. work split: the cube width that separates the small- and large-cube
+  //    queues (best of two timed steps each, after one warm-up step)
+  const int splits[] = {26, 34, 42, 66};
+  int best_split = t->small_extent[prec];
+  double best = 1e300;
+  for (int e : splits) {
+    t->small_extent[prec] = e;
+    t->sched_version++;
+    tune_step(t, func, pab_blocks, rho_grids, v_grids, hab_blocks, s, nullptr);
+    double ms = 1e300;
+    for (int r = 0; r < 2; r++)
+      ms = std::min(ms, tune_step(t, func, pab_blocks, rho_grids, v_grids, hab_blocks, s, nullptr));
+    if (ms < best) {
+      best = ms;
+      best_split = e;
+    }
+  }
+  t->small_extent[prec] = best_split;
+  t->sched_version++;
+  tune_step(t, func, pab_blocks, rho_grids, v_grids, hab_blocks, s, nullptr);
+  // 2. launch shape of every queue: warps per CTA x share of the resident CTAs
+  struct Cand {
+    int warps, occ, variant;
+  };
+  const Cand cands[] = {{4, 100, 0}, {2, 100, 0}, {1, 100, 0}, {4, 75, 0},
+                        {4, 50, 0},  {4, 100, 1}, {2, 100, 1}, {1, 100, 1}};
+  std::map<std::pair<int, int>, std::pair<double, int>> pick; // (phase,key) -> (ms, cand)
+  for (int c = 0; c < (int)(sizeof(cands) / sizeof(cands[0])); c++) {
+    for (const auto &kv : t->modes)
+      for (const Queue &q : kv.second.queues)
+        for (int phase = 0; phase < 2; phase++) {
+          LaunchCfg cfg;
+          cfg.warps = cands[c].warps;
+          cfg.occupancy = cands[c].occ;
+          cfg.variant = cands[c].variant;
+          t->tuned[std::make_tuple(prec, phase, q.key)] = cfg;
+        }
+    std::map<std::pair<int, int>, double> ms;
+    for (int r = 0; r < 2; r++) {
+      std::vector<std::tuple<int, int, double>> rec;
+      tune_step(t, func, pab_blocks, rho_grids, v_grids, hab_blocks, s, &rec);
+      for (auto &x : rec) {
+        auto key = std::make_pair(std::get<0>(x), std::get<1>(x));
+        auto f = ms.find(key);
+        ms[key] = f == ms.end() ? std::get<2>(x) : std::min(f->second, std::get<2>(x));
+      }
+    }
+    for (auto &kv : ms) {
+      auto f = pick.find(kv.first);
+      if (f == pick.end() || kv.second < f->second.first)
+        pick[kv.first] = {kv.second, c};
+    }
+  }
+  double total = 0.0;
+  for (auto &kv : pick) {
+    LaunchCfg cfg;
+    cfg.warps = cands[kv.second.second].warps;
+    cfg.occupancy = cands[kv.second.second].occ;
+    cfg.variant = cands[kv.second.second].variant;
+    t->tuned[std::make_tuple(prec, kv.first.first, kv.first.second)] = cfg;
+    total += kv.second.first;
+  }
+  t->launch_timing = lt;
+  t->launches.clear();
+  t->gen++;
+  return total;
+}
+
+GB300_API void grid_gb300_set_collocate_variant(const grid_gb300_task_list *task_list,
+                                                int variant) {
+  if (variant < 0 || variant > 1)
+    fail("unknown collocate variant %d", variant);
+  TaskList *t = TL(task_list);
+  t->coll_variant = variant;
+  t->tuned.clear();
+  t->gen++;
+}
+
+GB300_API int grid_gb300_tuned_split(const grid_gb300_task_list *task_list) {
+  const TaskList *t = TL(task_list);
+  return t->small_extent[t->precision];
 }
 
 GB300_API void grid_gb300_set_launch_timing(const grid_gb300_task_list *task_list, int enable) {

@@ -79,6 +79,7 @@ struct SphereHdr {
   int cmax;
   int off; // into the int16 table: [K] jstart, [K] row offsets, istart rows
   int jxo; // relative offset of the [K][1-lb[0]] table of last row index per x
+  int plo; // point lists: index of this sphere's plane offsets in sph_ploff (-1: none)
 };
 
 struct LevelDesc {
@@ -160,6 +161,8 @@ struct GridArgs {
   void *coef_out;
   const SphereHdr *sph;
   const int16_t *sph_tab;
+  const int *sph_pts;   // packed (x, j) of every point of a sphere plane, row-major
+  const int *sph_ploff; // per sphere plane kk: start of its points in sph_pts
   double *grids[GB300_MAX_LEVELS];         // collocate targets
   float *grids_lo[GB300_MAX_LEVELS];       // collocate low words (mixed path)
   const void *grids_in[GB300_MAX_LEVELS];  // integrate sources (per arith)
@@ -212,7 +215,15 @@ void launch_coefficients(const CoefArgs &a, int arith, int max_smem_words,
 struct LaunchCfg {
   int warps = 0;  // warps per CTA (capped by the shared-memory budget)
   int blocks = 0; // CTAs (automatic: all that fit on the GPU at once)
+  int occupancy = 100; // automatic CTA count: this percentage of all that fit
+  int variant = 0;     // collocate, orthorhombic: 0 row walk, 1 point list
 };
+inline int cfg_blocks(const LaunchCfg &c, int persistent) {
+  if (c.blocks > 0)
+    return c.blocks;
+  const int nb = persistent * (c.occupancy > 0 ? c.occupancy : 100) / 100;
+  return nb > 0 ? nb : 1;
+}
 void launch_collocate(const GridArgs &a, int arith, bool general, int bucket,
                       int extent, LaunchCfg &cfg, cudaStream_t s);
 void launch_integrate(const GridArgs &a, int arith, bool general, int bucket,
@@ -263,6 +274,13 @@ inline int bucket_of(int lp) {
 // (api.cu); npoints receives the number of grid points the cube visits.
 void build_sphere(const LevelDesc &L, double disr, SphereHdr &h,
                   std::vector<int16_t> &tab, long long &npoints);
+
+// Point lists of a sphere (for the point-list collocate kernel): the points
+// (x, j) of every plane kk in row-major order (j, then x), packed as
+// (x & 0xffff) | (j << 16), appended to `pts`; the K + 1 plane offsets go to
+// `ploff` and h.plo receives their index.
+void build_sphere_points(SphereHdr &h, const std::vector<int16_t> &tab, std::vector<int> &pts,
+                         std::vector<int> &ploff);
 
 // counts launches for grid_gb300_kernel_launches()
 void count_launch(int n = 1);

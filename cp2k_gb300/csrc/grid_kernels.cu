@@ -51,6 +51,11 @@ template <typename N, int LPB> struct OrthoSmem {
     b += 64; // alignment slack
     return (b + 15) & ~size_t(15);
   }
+  // collocate over point lists: as bytes_coll plus the per-plane x folds
+  // q[x][ly] of every x of the cube
+  static __host__ __device__ size_t bytes_coll_pl(int wmax) {
+    return bytes_coll(wmax) + ((sizeof(T) * (size_t)wmax * PP + 15) & ~size_t(15));
+  }
   // integrate: tables (reused as the x-fold transpose), maps, accumulator
   static __host__ __device__ size_t pol_words_int(int wmax) {
     const size_t a = 3 * (size_t)wmax * PP, r = 32 * (size_t)red_stride();
@@ -290,8 +295,8 @@ __global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
           const int lx = rem;
           T s = M::zero();
           for (int lz = 0; lz <= lp - ly - lx; lz++)
-            s = M::fma(s, coef[cidx(lz, ly, lx, lp)], pz[lz]);
-          cxy[e] = s;
+            s = M::fma_acc(s, coef[cidx(lz, ly, lx, lp)], pz[lz]);
+          cxy[e] = M::norm(s);
         }
         __syncwarp();
         // q[ly] = sum_lx C_xy[ly][lx] pol_x[lx](x_lane)
@@ -304,9 +309,9 @@ __global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
 #pragma unroll
             for (int lx = 0; lx < P; lx++)
               if (lx <= lp - ly)
-                s = M::fma(s, row[lx], px[lx]);
+                s = M::fma_acc(s, row[lx], px[lx]);
           }
-          q[ly] = s;
+          q[ly] = M::norm(s);
         }
         __syncwarp();
         const size_t zoff = (size_t)map[2 * cg.w + k + cg.cmax] * nxy;
@@ -327,8 +332,8 @@ __global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
 #pragma unroll
           for (int ly = 0; ly < P; ly++)
             if (ly <= lp) {
-              v1 = M::fma(v1, q[ly], p1[ly]);
-              v2 = M::fma(v2, q[ly], p2[ly]);
+              v1 = M::fma_acc(v1, q[ly], p1[ly]);
+              v2 = M::fma_acc(v2, q[ly], p2[ly]);
             }
           if (in1)
             grid_add<N>(grid, glo, zoff + (size_t)map[cg.w + j + cg.cmax] * nx + ig, v1);
@@ -336,6 +341,142 @@ __global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
             grid_add<N>(grid, glo, zoff + (size_t)map[cg.w + j2c + cg.cmax] * nx + ig, v2);
         }
       }
+    }
+    if (a.task_cycles && lane == 0)
+      a.task_cycles[t] = clock64() - t0;
+    __syncwarp();
+  }
+}
+
+// ------------------------------------------------------------------------
+// collocate, orthorhombic, over the sphere's point lists
+// ------------------------------------------------------------------------
+// Same arithmetic as collocate_ortho, different lane mapping: per plane the
+// warp first folds x into a table q[x][ly] for every x of the cube, then
+// walks the plane's points in row-major order, 32 consecutive points per
+// warp step (two steps per iteration), so every lane has work whatever the
+// cube width and the shape of the plane's disc.  The points come from a
+// host-built list per sphere (shared by all tasks of that sphere, so it
+// stays in L1/L2); consecutive lanes hit consecutive x of a row, keeping the
+// grid atomics coalesced.
+template <typename N, int LPB>
+__global__ void __launch_bounds__(128) collocate_ortho_pl(GridArgs a, int wmax) {
+  using T = typename Num<N>::T;
+  using M = Num<N>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int P = LPB + 1;
+  constexpr int PP = OrthoSmem<N, LPB>::PP;
+  const int lane = threadIdx.x & 31;
+  unsigned char *ws = smem + (threadIdx.x >> 5) * OrthoSmem<N, LPB>::bytes_coll_pl(wmax);
+  T *pol = (T *)ws;
+  T *qt = pol + 3 * (size_t)wmax * PP;
+  T *coef = qt + (size_t)wmax * PP;
+  T *cxy = coef + ncoset(LPB);
+  int *map = (int *)(cxy + ntri(LPB));
+  const T *coefs = (const T *)a.coef;
+
+  for (;;) {
+    int qi = 0;
+    if (lane == 0)
+      qi = atomicAdd(a.counter, 1);
+    qi = __shfl_sync(FULL, qi, 0);
+    if (qi >= a.nqueue)
+      break;
+    const int t = a.queue[qi];
+    const long long t0 = clock64();
+    const TaskDesc d = a.tasks[t];
+    const LevelDesc &L = a.levels.lv[d.level];
+    const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
+    const SphereHdr &H = a.sph[d.sphere];
+    const CubeGeo cg = cube_geo(H, a.sph_tab, lane);
+    if (cg.w > wmax || lp > LPB || H.plo < 0) { // the host sized the work arrays
+      if (lane == 0)
+        atomicOr(a.error, 1);
+      continue;
+    }
+    const int nco = ncoset(lp), ntr = ntri(lp);
+    if constexpr (std::is_same<T, float>::value) {
+      const float *csrc = (const float *)a.coef + (size_t)a.coef_off[t] * a.coef_stride;
+      for (int e = lane; e < nco; e += 32)
+        coef[e] = csrc[(size_t)e * a.coef_stride];
+    } else {
+      const T *csrc = coefs + a.coef_off[t];
+      for (int e = lane; e < nco; e += 32)
+        coef[e] = csrc[e];
+    }
+    fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane, a.seeds + (size_t)t * 18);
+    __syncwarp();
+
+    double *grid = a.grids[d.level];
+    float *glo = a.grids_lo[d.level];
+    const size_t nx = L.npts_local[0], nxy = nx * L.npts_local[1];
+    const int *ploff = a.sph_ploff + H.plo;
+
+    for (int k = cg.lb2; k <= 1 - cg.lb2; k++) {
+      const int kk = k <= 0 ? -k : k - 1;
+      // C_xy[ly][lx] = sum_lz C_xyz[lz][ly][lx] pol_z[lz](k)
+      const T *pz = pol + (size_t)(2 * cg.w + k + cg.cmax) * PP;
+      for (int e = lane; e < ntr; e += 32) {
+        int ly = 0, rem = e;
+        while (rem > lp - ly) {
+          rem -= lp - ly + 1;
+          ly++;
+        }
+        const int lx = rem;
+        T s = M::zero();
+        for (int lz = 0; lz <= lp - ly - lx; lz++)
+          s = M::fma_acc(s, coef[cidx(lz, ly, lx, lp)], pz[lz]);
+        cxy[e] = M::norm(s);
+      }
+      __syncwarp();
+      // q[c][ly] = sum_lx C_xy[ly][lx] pol_x[lx](c), every x of the cube
+      for (int c = lane; c < cg.w; c += 32) {
+        T px[PP];
+        load_row<T, PP>(pol + (size_t)c * PP, px);
+        T *qr = qt + (size_t)c * PP;
+#pragma unroll
+        for (int ly = 0; ly < P; ly++) {
+          T s = M::zero();
+          if (ly <= lp) {
+            const T *row = cxy + tri_idx(ly, 0, lp);
+#pragma unroll
+            for (int lx = 0; lx < P; lx++)
+              if (lx <= lp - ly)
+                s = M::fma_acc(s, row[lx], px[lx]);
+          }
+          qr[ly] = M::norm(s);
+        }
+      }
+      __syncwarp();
+      const size_t zoff = (size_t)map[2 * cg.w + k + cg.cmax] * nxy;
+      const int *pts = a.sph_pts + ploff[kk];
+      const int n = ploff[kk + 1] - ploff[kk];
+      for (int f = lane; f < n; f += 64) {
+        const int f2 = f + 32;
+        const bool two = f2 < n;
+        const int pk1 = __ldg(pts + f);
+        const int pk2 = two ? __ldg(pts + f2) : pk1;
+        const int x1 = (int)(short)(pk1 & 0xffff), j1 = pk1 >> 16;
+        const int x2 = (int)(short)(pk2 & 0xffff), j2 = pk2 >> 16;
+        T q1[PP], q2[PP], p1[PP], p2[PP];
+        load_row<T, PP>(qt + (size_t)(x1 + cg.cmax) * PP, q1);
+        load_row<T, PP>(pol + (size_t)(cg.w + j1 + cg.cmax) * PP, p1);
+        load_row<T, PP>(qt + (size_t)(x2 + cg.cmax) * PP, q2);
+        load_row<T, PP>(pol + (size_t)(cg.w + j2 + cg.cmax) * PP, p2);
+        T v1 = M::zero(), v2 = M::zero();
+#pragma unroll
+        for (int ly = 0; ly < P; ly++)
+          if (ly <= lp) {
+            v1 = M::fma_acc(v1, q1[ly], p1[ly]);
+            v2 = M::fma_acc(v2, q2[ly], p2[ly]);
+          }
+        grid_add<N>(grid, glo,
+                    zoff + (size_t)map[cg.w + j1 + cg.cmax] * nx + map[x1 + cg.cmax], v1);
+        if (two)
+          grid_add<N>(grid, glo,
+                      zoff + (size_t)map[cg.w + j2 + cg.cmax] * nx + map[x2 + cg.cmax], v2);
+      }
+      __syncwarp();
     }
     if (a.task_cycles && lane == 0)
       a.task_cycles[t] = clock64() - t0;
@@ -429,8 +570,11 @@ __global__ void __launch_bounds__(128) integrate_ortho(GridArgs a, int wmax) {
 #pragma unroll
           for (int ly = 0; ly < P; ly++)
             if (ly <= lp)
-              wy[ly] = M::fma(M::fma(wy[ly], v1, p1[ly]), v2, p2[ly]);
+              wy[ly] = M::fma_acc(M::fma_acc(wy[ly], v1, p1[ly]), v2, p2[ly]);
         }
+#pragma unroll
+        for (int l = 0; l < P; l++)
+          wy[l] = M::norm(wy[l]);
         T pz[PP];
         load_row<T, PP>(pol + (size_t)(2 * cg.w + k + cg.cmax) * PP, pz);
 #pragma unroll
@@ -441,7 +585,7 @@ __global__ void __launch_bounds__(128) integrate_ortho(GridArgs a, int wmax) {
           for (int ly = 0; ly < P; ly++)
             if (ly <= lp - lz)
               ayz[lz * P - (lz * (lz - 1)) / 2 + ly] =
-                  M::fma(ayz[lz * P - (lz * (lz - 1)) / 2 + ly], wy[ly], pz[lz]);
+                  M::fma_acc(ayz[lz * P - (lz * (lz - 1)) / 2 + ly], wy[ly], pz[lz]);
         }
       }
       // x fold and reduction over the warp through shared memory:
@@ -454,7 +598,7 @@ __global__ void __launch_bounds__(128) integrate_ortho(GridArgs a, int wmax) {
         __syncwarp(); // every lane holds its pol_x before the tables are overwritten
 #pragma unroll
         for (int e = 0; e < NYZ; e++)
-          rl[e] = ayz[e];
+          rl[e] = M::norm(ayz[e]);
 #pragma unroll
         for (int l = 0; l < P; l++)
           rl[NYZ + l] = (xin && l <= lp) ? px[l] : M::zero();
@@ -466,7 +610,7 @@ __global__ void __launch_bounds__(128) integrate_ortho(GridArgs a, int wmax) {
           T s = M::zero();
 #pragma unroll 8
           for (int r = 0; r < 32; r++)
-            s = M::fma(s, red[r * RS + yz], red[r * RS + NYZ + lx]);
+            s = M::fma_acc(s, red[r * RS + yz], red[r * RS + NYZ + lx]);
           acc[e] += M::to_double(s);
         }
         __syncwarp();
@@ -494,21 +638,26 @@ __global__ void __launch_bounds__(128) integrate_ortho(GridArgs a, int wmax) {
 template <typename N, int LPB>
 static void launch_ortho_t(const GridArgs &a, bool collocate, int wmax, LaunchCfg &cfg,
                            cudaStream_t s) {
-  const size_t per_warp =
-      collocate ? OrthoSmem<N, LPB>::bytes_coll(wmax) : OrthoSmem<N, LPB>::bytes_int(wmax);
+  const bool pl = collocate && cfg.variant == 1;
+  const size_t per_warp = pl ? OrthoSmem<N, LPB>::bytes_coll_pl(wmax)
+                          : collocate ? OrthoSmem<N, LPB>::bytes_coll(wmax)
+                                      : OrthoSmem<N, LPB>::bytes_int(wmax);
   int nw = warps_for(per_warp);
   if (nw < 1)
     return launch_error("orthorhombic grid kernel: cube too large for shared memory");
   if (cfg.warps > 0 && cfg.warps < nw)
     nw = cfg.warps;
   const size_t smem = nw * per_warp;
-  const void *k = collocate ? (const void *)collocate_ortho<N, LPB>
-                            : (const void *)integrate_ortho<N, LPB>;
+  const void *k = pl          ? (const void *)collocate_ortho_pl<N, LPB>
+                  : collocate ? (const void *)collocate_ortho<N, LPB>
+                              : (const void *)integrate_ortho<N, LPB>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  const int nb = cfg.blocks > 0 ? cfg.blocks : persistent_blocks(k, 32 * nw, smem);
+  const int nb = cfg.blocks > 0 ? cfg.blocks : cfg_blocks(cfg, persistent_blocks(k, 32 * nw, smem));
   cfg.warps = nw;
   cfg.blocks = nb;
-  if (collocate)
+  if (pl)
+    collocate_ortho_pl<N, LPB><<<nb, 32 * nw, smem, s>>>(a, wmax);
+  else if (collocate)
     collocate_ortho<N, LPB><<<nb, 32 * nw, smem, s>>>(a, wmax);
   else
     integrate_ortho<N, LPB><<<nb, 32 * nw, smem, s>>>(a, wmax);

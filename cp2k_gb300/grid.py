@@ -98,6 +98,18 @@ def lib():
         L.grid_gb300_backend_handle.argtypes = [vp]
         L.grid_gb300_backend_handle.restype = vp
         L.grid_gb300_kernel_launches.restype = C.c_longlong
+        L.grid_gb300_capture_step.argtypes = [vp, C.c_int, vp, vp, C.c_bool, vp, vp, vp, vp, vp]
+        L.grid_gb300_capture_step.restype = vp
+        L.grid_gb300_step_graph_launch.argtypes = [vp, vp]
+        L.grid_gb300_step_graph_wait.argtypes = [vp, vp]
+        L.grid_gb300_step_graph_kernels.argtypes = [vp]
+        L.grid_gb300_step_graph_kernels.restype = C.c_longlong
+        L.grid_gb300_step_graph_free.argtypes = [vp]
+        L.grid_gb300_autotune.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp]
+        L.grid_gb300_autotune.restype = C.c_double
+        L.grid_gb300_set_collocate_variant.argtypes = [vp, C.c_int]
+        L.grid_gb300_tuned_split.argtypes = [vp]
+        L.grid_gb300_tuned_split.restype = C.c_int
         L.grid_gb300_set_launch_timing.argtypes = [vp, C.c_int]
         L.grid_gb300_launch_timings.argtypes = [vp, C.c_int, vp]
         L.grid_gb300_launch_timings.restype = C.c_int
@@ -352,6 +364,35 @@ class GridTaskList:
             self.impl, bool(compute_tau), dp(pab_dev), C.cast(ptrs, C.c_void_p), dp(hab_dev),
             dp(forces_dev), dp(virial_dev), _stream(stream))
 
+    def autotune(self, func: int, pab_dev, rho_dev, V_dev, hab_dev, stream=None) -> float:
+        """Measures and keeps the fastest size split and launch shapes for the
+        current precision (grid_gb300_autotune); returns grid-kernel ms."""
+        rp = (C.c_void_p * len(rho_dev))(*[g.data_ptr() for g in rho_dev])
+        vp_ = (C.c_void_p * len(V_dev))(*[g.data_ptr() for g in V_dev])
+        return float(lib().grid_gb300_autotune(self.impl, int(func), C.c_void_p(pab_dev.data_ptr()),
+                                               C.cast(rp, C.c_void_p), C.cast(vp_, C.c_void_p),
+                                               C.c_void_p(hab_dev.data_ptr()), _stream(stream)))
+
+    def set_collocate_variant(self, variant: int):
+        """0: row walk, 1: point list (grid_gb300_set_collocate_variant)."""
+        lib().grid_gb300_set_collocate_variant(self.impl, int(variant))
+
+    def tuned_split(self) -> int:
+        return int(lib().grid_gb300_tuned_split(self.impl))
+
+    def capture_step(self, func: int, pab_dev, rho_dev, V_dev, hab_dev, forces_dev=None,
+                     virial_dev=None, compute_tau=False, stream=None):
+        """CUDA graph of one SCF step (collocate func into rho_dev, integrate
+        V_dev into hab_dev) on device tensors; `stream` must be a created
+        torch.cuda.Stream.  Returns a StepGraph."""
+        rp = (C.c_void_p * len(rho_dev))(*[g.data_ptr() for g in rho_dev])
+        vp_ = (C.c_void_p * len(V_dev))(*[g.data_ptr() for g in V_dev])
+        dp = lambda x: C.c_void_p(x.data_ptr()) if x is not None else None
+        h = lib().grid_gb300_capture_step(self.impl, int(func), dp(pab_dev), C.cast(rp, C.c_void_p),
+                                          bool(compute_tau), C.cast(vp_, C.c_void_p), dp(hab_dev),
+                                          dp(forces_dev), dp(virial_dev), _stream(stream))
+        return StepGraph(h, (rp, vp_, pab_dev, rho_dev, V_dev, hab_dev, forces_dev, virial_dev))
+
     def close(self):
         if self.h:
             fn = lib().grid_free_task_list if self.api == "cp2k" else lib().grid_gb300_free_task_list
@@ -369,6 +410,36 @@ class GridTaskList:
     def __del__(self):
         try:
             self.close()
+        except Exception:
+            pass
+
+
+class StepGraph:
+    """A captured SCF step (grid_gb300_capture_step); keeps the buffers it
+    was captured on alive."""
+
+    def __init__(self, handle, keep):
+        self.h = C.c_void_p(handle)
+        self._keep = keep
+
+    @property
+    def kernels(self) -> int:
+        return int(lib().grid_gb300_step_graph_kernels(self.h))
+
+    def launch(self, stream=None):
+        lib().grid_gb300_step_graph_launch(self.h, _stream(stream))
+
+    def wait(self, stream=None):
+        lib().grid_gb300_step_graph_wait(self.h, _stream(stream))
+
+    def free(self):
+        if self.h:
+            lib().grid_gb300_step_graph_free(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
         except Exception:
             pass
 

@@ -313,6 +313,47 @@ void grid_gb300_last_timings(const grid_gb300_task_list *task_list,
 /* Number of kernels this library launched on the device since load. */
 long long grid_gb300_kernel_launches(void);
 
+/* Autotuner: for the current precision, times SCF steps (collocate(func) +
+ * integrate hab, device buffers, on `stream`) over the cube width that splits
+ * small- from large-cube work queues (26, 34, 42, 66) and then, per work
+ * queue, over launch shapes (warps per CTA 1/2/4, 50-100 % of the resident
+ * CTAs, both collocate lane mappings), and keeps the fastest.  Results of later calls are unchanged up to
+ * the order of floating-point atomic additions.  Returns the summed
+ * grid-kernel time (ms) of the chosen shapes. */
+double grid_gb300_autotune(const grid_gb300_task_list *task_list, int func,
+                           const double *pab_blocks, double *const *rho_grids,
+                           const double *const *v_grids, double *hab_blocks,
+                           void *stream);
+/* Lane mapping of the orthorhombic collocate kernel: 0 walks the rows of
+ * each sphere plane with lanes bound to x; 1 (default) walks the plane's
+ * points in row-major order from a per-sphere point list, so that all lanes
+ * have work.  Same arithmetic; clears autotuned shapes. */
+void grid_gb300_set_collocate_variant(const grid_gb300_task_list *task_list,
+                                      int variant);
+/* Cube width separating the small- and large-cube queues at the current
+ * precision (default 34). */
+int grid_gb300_tuned_split(const grid_gb300_task_list *task_list);
+
+/* CUDA-graph capture of one SCF step on device buffers: collocate(func)
+ * into rho_grids, then integrate v_grids into hab (forces / virial optional,
+ * as for grid_gb300_integrate_device_async).  The capture first runs the step
+ * once on `stream` (a created cudaStream_t as void*; the legacy default
+ * stream cannot be captured) so that every work array exists, then records
+ * the step's kernels and memsets as one graph.  A launch replays the step
+ * with the same pointers; it fails if the task list's precision, schedule,
+ * timing switches or internal arrays changed since capture.  Launches are
+ * asynchronous; grid_gb300_step_graph_wait synchronises the stream and checks
+ * the kernels' error word. */
+typedef void grid_gb300_step_graph;
+grid_gb300_step_graph *grid_gb300_capture_step(
+    const grid_gb300_task_list *task_list, int func, const double *pab_blocks,
+    double *const *rho_grids, bool compute_tau, const double *const *v_grids,
+    double *hab_blocks, double *forces, double *virial, void *stream);
+void grid_gb300_step_graph_launch(grid_gb300_step_graph *graph, void *stream);
+void grid_gb300_step_graph_wait(grid_gb300_step_graph *graph, void *stream);
+long long grid_gb300_step_graph_kernels(const grid_gb300_step_graph *graph);
+void grid_gb300_step_graph_free(grid_gb300_step_graph *graph);
+
 /* Per-launch timing of the grid kernels (off by default).  When enabled,
  * every collocate/integrate call records CUDA events around each grid-kernel
  * launch; grid_gb300_launch_timings waits for the last call and copies up to

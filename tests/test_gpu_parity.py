@@ -183,3 +183,26 @@ def test_ref_golden_fp64(G, case, api):
         assert rel_diff(f, exp[f"forces_tau{tau}"]) < TOL_DERIV
         assert rel_diff(v, exp[f"virial_tau{tau}"]) < TOL_DERIV
     tl.close()
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2])
+def test_collocate_variants_agree(G, O, prec):
+    """Row-walk and point-list collocate kernels give the same grids (the same
+    per-point arithmetic; only the order of the FP64 atomic additions
+    differs), and both match the oracle in FP64."""
+    from cp2k_gb300 import workload as W
+    inp = W.config("c2_512atoms", scale=0.1, seed=31)
+    pab = W.density_blocks(inp)
+    tl = G.GridTaskList(inp, precision=prec)
+    out = []
+    for v in (0, 1):
+        tl.set_collocate_variant(v)
+        out.append(tl.collocate(100, pab))
+    for a, b in zip(*out):
+        assert rel_diff(a, b) < 1e-13
+    if prec == G.FP64:
+        ot = O.OracleTaskList(inp)
+        ref = ot.collocate(100, pab)
+        assert max(rel_diff(a, b) for a, b in zip(out[1], ref)) < TOL_GRID
+        ot.close()
+    tl.close()
