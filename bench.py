@@ -341,7 +341,9 @@ def gpu_arm(args, world, rank, local):
     barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
+        torch.cuda.nvtx.range_push("timed_mixed")  # lets a profiler select this region
         t_mixed = run_steps(G.MIXED, sched_mixed, args.steps)
+        torch.cuda.nvtx.range_pop()
     launches = G.kernel_launches() - launches0
     torch.cuda.synchronize()
     barrier(world)

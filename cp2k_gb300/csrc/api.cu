@@ -290,7 +290,7 @@ struct TaskList {
   std::vector<cudaEvent_t> event_pool;
   std::map<std::tuple<int, int, int>, LaunchCfg> tuned; // (precision, phase, queue key) -> shape
   int small_extent[3] = {kSmallExtent, kSmallExtent, kSmallExtent}; // per precision
-  int coll_variant = 1; // orthorhombic collocate lane mapping: 0 row walk, 1 point list
+  int coll_variant = -1; // orthorhombic collocate lanes: 0 row walk, 1 point list, -1 by arith
   std::vector<double> gbound;    // per task bound of |contribution| for |P| <= 1
   std::vector<float2> seeds;     // per task [3][6] dfloat recurrence seeds (ortho)
   float2 *d_seeds = nullptr;
@@ -865,8 +865,8 @@ static Mode &get_mode(TaskList *t, const LDiffs &d) {
     if (b < 0)
       fail("contraction order lp=%d exceeds %d", lp, GB300_LP_MAX);
     const int g = (k.flags & TF_GENERAL) ? 1 : 0;
-    const int cls = (t->precision == GRID_GB300_MIXED && g == 0 &&
-                     t->gbound[s] <= t->mixed_threshold) ? 1 : 0;
+    const int cls = (t->precision == GRID_GB300_MIXED && t->gbound[s] <= t->mixed_threshold)
+                        ? 1 : 0;
     const int ext = g == 0 ? 2 * t->sph[k.sphere].cmax + 2 : k.imax[1] - k.center[1] + 1;
     const int sz = ext <= t->small_extent[t->precision] ? 0 : 1;
     double cost;
@@ -981,7 +981,9 @@ static cudaEvent_t pool_event(TaskList *t, size_t i) {
 static void grid_launch(TaskList *t, const Queue &q, int phase, int arith, const GridArgs &ga,
                         cudaStream_t s) {
   LaunchCfg cfg;
-  cfg.variant = t->coll_variant;
+  // automatic: the point-list kernel pays off where the per-point arithmetic
+  // is expensive (FP64, double-float), the row walk for plain FP32
+  cfg.variant = t->coll_variant >= 0 ? t->coll_variant : (arith == ARITH_FP32 ? 0 : 1);
   auto it = t->tuned.find(std::make_tuple(t->precision, phase, q.key));
   if (it != t->tuned.end())
     cfg = it->second;
@@ -1142,8 +1144,9 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
     ga.nqueue = q.n;
     ga.counter = t->d_counters + qi++;
     ga.grid_stride = q.fp32 ? 2 : 1;
-    for (int l = 0; l < t->nlevels; l++) // the general path runs in FP64 in the mixed mode
-      ga.grids_in[l] = (arith == ARITH_FP64 || (q.general && arith == ARITH_MIXED))
+    // the general path's double-float class runs in FP64 in the mixed mode
+    for (int l = 0; l < t->nlevels; l++)
+      ga.grids_in[l] = (arith == ARITH_FP64 || (q.general && arith == ARITH_MIXED && !q.fp32))
                            ? (const void *)grids[l] : (const void *)t->d_gridsplit[l];
     grid_launch(t, q, 1, q.fp32 ? (int)ARITH_FP32 : arith, ga, s);
     grid_library_counter_add(kBucketLp[q.bucket], GRID_BACKEND_GB300,
@@ -1346,6 +1349,7 @@ GB300_API void grid_create_task_list(
   if (be != GRID_BACKEND_AUTO && be != GRID_BACKEND_GPU && be != GRID_BACKEND_GB300)
     fail("grid backend %d is provided by CP2K's own grid library, not by this one", be);
   TopList *tl = (TopList *)*task_list;
+  const bool fresh = !tl;
   if (!tl)
     tl = new TopList();
   tl->nlevels = nlevels;
@@ -1357,6 +1361,27 @@ GB300_API void grid_create_task_list(
                               jpgf_list, border_mask_list, block_num_list, radius_list,
                               rab_list, npts_global, npts_local, shift_local, border_width, dh,
                               dh_inv, &tl->impl);
+  if (fresh) {
+    // CP2K passes no precision: a new list takes it from the environment
+    if (const char *e = getenv("GRID_GB300_PRECISION")) {
+      const std::string v(e);
+      if (v == "fp64" || v == "FP64")
+        grid_gb300_set_precision(tl->impl, GRID_GB300_FP64);
+      else if (v == "mixed" || v == "MIXED")
+        grid_gb300_set_precision(tl->impl, GRID_GB300_MIXED);
+      else if (v == "fp32" || v == "FP32")
+        grid_gb300_set_precision(tl->impl, GRID_GB300_FP32);
+      else
+        fail("GRID_GB300_PRECISION=%s: expected fp64, mixed or fp32", e);
+    }
+    if (const char *e = getenv("GRID_GB300_MIXED_THRESHOLD")) {
+      char *end = nullptr;
+      const double v = strtod(e, &end);
+      if (end == e || *end != '\0' || !(v >= 0.0))
+        fail("GRID_GB300_MIXED_THRESHOLD=%s: expected a number >= 0", e);
+      grid_gb300_set_mixed_threshold(tl->impl, v);
+    }
+  }
   *task_list = tl;
 }
 
@@ -1440,7 +1465,7 @@ GB300_API void grid_gb300_mixed_split(const grid_gb300_task_list *task_list, dou
   const TaskList *t = TL(task_list);
   double nt = 0, nf = 0, pt = 0, pf = 0;
   for (size_t s = 0; s < t->tasks.size(); s++) {
-    if (t->tasks[s].flags & (TF_SKIP | TF_GENERAL))
+    if (t->tasks[s].flags & TF_SKIP)
       continue;
     nt += 1;
     pt += (double)t->points[s];
@@ -1691,7 +1716,7 @@ GB300_API double grid_gb300_autotune(const grid_gb300_task_list *task_list, int 
 
 GB300_API void grid_gb300_set_collocate_variant(const grid_gb300_task_list *task_list,
                                                 int variant) {
-  if (variant < 0 || variant > 1)
+  if (variant < -1 || variant > 1)
     fail("unknown collocate variant %d", variant);
   TaskList *t = TL(task_list);
   t->coll_variant = variant;

@@ -167,9 +167,16 @@ __global__ void __launch_bounds__(128) collocate_general(GridArgs a, int njmax) 
       continue;
     }
     const int nco = ncoset(lp), ntr = ntri(lp);
-    const T *csrc = coefs + a.coef_off[t];
-    for (int e = lane; e < nco; e += 32)
-      coef[e] = csrc[e];
+    if (sizeof(T) == 4 && a.coef_stride == 2) {
+      // FP32 task of the mixed mode: general-path coefficients are stored in FP64
+      const double *csrc = (const double *)a.coef + a.coef_off[t];
+      for (int e = lane; e < nco; e += 32)
+        coef[e] = (T)csrc[e];
+    } else {
+      const T *csrc = coefs + a.coef_off[t];
+      for (int e = lane; e < nco; e += 32)
+        coef[e] = csrc[e];
+    }
     double *grid = a.grids[d.level];
     const size_t nx = L.npts_local[0], nxy = nx * L.npts_local[1];
     const int width = g.imax[0] - g.imin[0] + 1;
@@ -328,6 +335,7 @@ __global__ void __launch_bounds__(128) integrate_general(GridArgs a, int njmax) 
       acc[e] = 0.0;
     __syncwarp();
     const T *grid = (const T *)a.grids_in[d.level];
+    const int gs = sizeof(T) == 4 ? a.grid_stride : 1;
     const size_t nx = L.npts_local[0], nxy = nx * L.npts_local[1];
     const int width = g.imax[0] - g.imin[0] + 1;
     const int SW = width <= 8 ? 8 : (width <= 16 ? 16 : 32);
@@ -373,7 +381,8 @@ __global__ void __launch_bounds__(128) integrate_general(GridArgs a, int njmax) 
         for (int l = 0; l < P; l++)
           wj[l] = T(0);
         double eij = eij0;
-        const T *gplane = grid + (size_t)kg * nxy;
+        // FP32 tasks of the mixed mode read the high words of the (hi, lo) grid
+        const T *gplane = grid + (size_t)kg * nxy * gs;
         for (int j0 = g.imin[1]; j0 <= g.imax[1]; j0 += G, eij *= eij_step) {
           const int j = j0 + grp;
           if (j > g.imax[1] || ig < 0)
@@ -395,7 +404,7 @@ __global__ void __launch_bounds__(128) integrate_general(GridArgs a, int njmax) 
             }
             gauss = (T)expf(-(float)zetp * r2);
           }
-          const T vg = __ldg(gplane + (size_t)jg * nx + ig) * gauss;
+          const T vg = __ldg(gplane + ((size_t)jg * nx + ig) * gs) * gauss;
           const T djt = (sizeof(T) == 8) ? (T)((double)j - g.gp[1]) : (T)djf;
           T pj = T(1);
 #pragma unroll

@@ -374,7 +374,8 @@ class GridTaskList:
                                                C.c_void_p(hab_dev.data_ptr()), _stream(stream)))
 
     def set_collocate_variant(self, variant: int):
-        """0: row walk, 1: point list (grid_gb300_set_collocate_variant)."""
+        """0: row walk, 1: point list, -1: by arithmetic
+        (grid_gb300_set_collocate_variant)."""
         lib().grid_gb300_set_collocate_variant(self.impl, int(variant))
 
     def tuned_split(self) -> int:

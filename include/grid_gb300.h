@@ -157,7 +157,10 @@ typedef void grid_task_list;
 
 /* Replaces grid_create_task_list (src/grid/grid_task_list.h:59-72).
  * Arrays are C row-major: atom_positions[natoms][3], rab_list[ntasks][3],
- * npts_*[nlevels][3], dh/dh_inv[nlevels][3][3].  Task lists are 1-based. */
+ * npts_*[nlevels][3], dh/dh_inv[nlevels][3][3].  Task lists are 1-based.
+ * A new list computes in FP64 unless the environment sets
+ * GRID_GB300_PRECISION=fp64|mixed|fp32 (and GRID_GB300_MIXED_THRESHOLD, see
+ * grid_gb300_set_mixed_threshold); re-creation keeps the list's settings. */
 void grid_create_task_list(
     const bool orthorhombic, const int ntasks, const int nlevels,
     const int natoms, const int nkinds, const int nblocks,
@@ -265,11 +268,12 @@ void grid_gb300_set_schedule(const grid_gb300_task_list *task_list,
 
 /* Mixed path: tasks whose contribution bound (Gaussian-product prefactor x
  * polynomial maxima, for density-matrix elements of magnitude <= 1) is at
- * most `threshold` run in plain FP32, the others in double-float.
- * 0 runs every orthorhombic task in double-float.  Default 1. */
+ * most `threshold` run in plain FP32, the others in double-float
+ * (orthorhombic kernels) or FP64 (general kernels).  0 runs no task in plain
+ * FP32.  Default 1. */
 void grid_gb300_set_mixed_threshold(const grid_gb300_task_list *task_list,
                                     double threshold);
-/* Share of orthorhombic tasks (and of their grid points) that the mixed path
+/* Share of the tasks (and of their grid points) that the mixed path
  * currently runs in plain FP32. */
 void grid_gb300_mixed_split(const grid_gb300_task_list *task_list,
                             double *frac_tasks, double *frac_points);
@@ -325,9 +329,10 @@ double grid_gb300_autotune(const grid_gb300_task_list *task_list, int func,
                            const double *const *v_grids, double *hab_blocks,
                            void *stream);
 /* Lane mapping of the orthorhombic collocate kernel: 0 walks the rows of
- * each sphere plane with lanes bound to x; 1 (default) walks the plane's
- * points in row-major order from a per-sphere point list, so that all lanes
- * have work.  Same arithmetic; clears autotuned shapes. */
+ * each sphere plane with lanes bound to x; 1 walks the plane's points in
+ * row-major order from a per-sphere point list, so that all lanes have work;
+ * -1 (default) uses 1 for FP64 and double-float launches and 0 for plain
+ * FP32 ones.  Same arithmetic; clears autotuned shapes. */
 void grid_gb300_set_collocate_variant(const grid_gb300_task_list *task_list,
                                       int variant);
 /* Cube width separating the small- and large-cube queues at the current

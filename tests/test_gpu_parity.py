@@ -187,9 +187,9 @@ def test_ref_golden_fp64(G, case, api):
 
 @pytest.mark.parametrize("prec", [0, 1, 2])
 def test_collocate_variants_agree(G, O, prec):
-    """Row-walk and point-list collocate kernels give the same grids (the same
-    per-point arithmetic; only the order of the FP64 atomic additions
-    differs), and both match the oracle in FP64."""
+    """Row-walk and point-list collocate kernels give the same grids up to the
+    order of the FP64 atomic additions (the same per-point arithmetic), and
+    the point-list kernel matches the oracle in FP64."""
     from cp2k_gb300 import workload as W
     inp = W.config("c2_512atoms", scale=0.1, seed=31)
     pab = W.density_blocks(inp)
@@ -198,8 +198,11 @@ def test_collocate_variants_agree(G, O, prec):
     for v in (0, 1):
         tl.set_collocate_variant(v)
         out.append(tl.collocate(100, pab))
+    # FP64: atomic order only; mixed / FP32: also the order of the FP32 adds
+    # into the low-word grid and of the FP32 row sums
+    tol = TOL_GRID if prec == G.FP64 else 1e-10
     for a, b in zip(*out):
-        assert rel_diff(a, b) < 1e-13
+        assert rel_diff(a, b) < tol
     if prec == G.FP64:
         ot = O.OracleTaskList(inp)
         ref = ot.collocate(100, pab)
