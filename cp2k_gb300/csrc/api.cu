@@ -63,6 +63,19 @@ static char g_last_error[512] = "";
            __LINE__);                                                          \
   } while (0)
 
+void set_smem(const void *kernel, size_t smem) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, size_t> done;
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  size_t &cur = done[std::make_pair(dev, kernel)];
+  if (smem > cur) { // the attribute call is slow; make it once per size increase
+    CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    cur = smem;
+  }
+}
+
 int persistent_blocks(const void *kernel, int threads, size_t smem) {
   static std::mutex mu;
   static std::map<std::pair<const void *, size_t>, int> cache;
@@ -304,6 +317,7 @@ struct TaskList {
   SphereHdr *d_sph = nullptr;
   int16_t *d_sph_tab = nullptr;
   int *d_sph_pts = nullptr, *d_sph_ploff = nullptr;
+  double *d_dhtab = nullptr;
   double *d_atom_pos = nullptr;
   double *d_sphi = nullptr;
   LevelSet *d_levels = nullptr;
@@ -418,6 +432,25 @@ void build_sphere(const LevelDesc &L, double disr, SphereHdr &h, std::vector<int
   tab.insert(tab.end(), jx.begin(), jx.end());
 }
 
+void build_dh_table(const LevelSet &ls, std::vector<double> &tab) {
+  tab.assign(dh_table_size(ls.nlevels), 0.0);
+  double f = 1.0;
+  for (int n = 0; n < kPowN; n++) {
+    if (n > 1)
+      f *= n;
+    tab[n] = f;
+    tab[kPowN + n] = 1.0 / f;
+  }
+  for (int l = 0; l < ls.nlevels; l++)
+    for (int c = 0; c < 9; c++) {
+      double p = 1.0;
+      for (int n = 0; n < kPowN; n++) {
+        tab[2 * kPowN + ((size_t)l * 9 + c) * kPowN + n] = p;
+        p *= ls.lv[l].dh[c];
+      }
+    }
+}
+
 void build_sphere_points(SphereHdr &h, const std::vector<int16_t> &tab, std::vector<int> &pts,
                          std::vector<int> &ploff) {
   const int K = 1 - h.lb[2];
@@ -482,7 +515,7 @@ template <typename T> static T *dalloc_copy(const std::vector<T> &v) {
 
 static void free_device(TaskList *t) {
   void *ptrs[] = {t->d_seeds, t->d_tasks, t->d_subs, t->d_sph, t->d_sph_tab, t->d_sph_pts,
-                  t->d_sph_ploff, t->d_atom_pos, t->d_sphi,
+                  t->d_sph_ploff, t->d_dhtab, t->d_atom_pos, t->d_sphi,
                   t->d_levels, t->d_pab_cart, t->d_hab_cart, t->d_coef, t->d_coef_int,
                   t->d_forces, t->d_virial, t->d_counters, t->d_error, t->d_cycles};
   for (void *p : ptrs)
@@ -808,6 +841,11 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
   t->d_sph = dalloc_copy(t->sph);
   t->d_sph_tab = dalloc_copy(t->sph_tab);
   t->d_sph_pts = dalloc_copy(t->sph_pts);
+  {
+    std::vector<double> dt;
+    build_dh_table(t->levels, dt);
+    t->d_dhtab = dalloc_copy(dt);
+  }
   t->d_sph_ploff = dalloc_copy(t->sph_ploff);
   t->d_atom_pos = dalloc_copy(std::vector<double>(atom_positions, atom_positions + 3 * natoms));
   t->d_sphi = dalloc_copy(sphi_all);
@@ -1040,7 +1078,7 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
                   t->contract_words};
   launch_decontract(ca, s);
   CoefArgs co{t->d_tasks, t->d_subs, m.d_coef_off, t->d_atom_pos, t->d_pab_cart, t->d_coef,
-              t->ntasks, func, d, t->d_levels, arith == ARITH_MIXED ? 1 : 0};
+              t->ntasks, func, d, t->d_levels, arith == ARITH_MIXED ? 1 : 0, t->d_dhtab};
   launch_coefficients(co, arith, m.coef_words, s);
   record_phase(t, 1, s);
   for (int l = 0; l < t->nlevels; l++) {
@@ -1161,7 +1199,7 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
     CK(cudaMemsetAsync(virial, 0, sizeof(double) * 9, s));
   PostArgs pa{t->d_tasks, t->d_subs, m.d_coef_off, t->d_coef_int,
               need_pab ? t->d_pab_cart : nullptr, t->d_hab_cart, t->d_atom_pos, forces, virial,
-              t->ntasks, tau ? 1 : 0, d, t->d_levels};
+              t->ntasks, tau ? 1 : 0, d, t->d_levels, t->d_dhtab};
   launch_post(pa, arith, m.coef_words, s);
   CK(cudaMemsetAsync(hab, 0, sizeof(double) * (size_t)t->buffer_len, s));
   ContractArgs cb{t->d_subs, (int)t->subs.size(), t->d_sphi, nullptr, hab, t->d_hab_cart,

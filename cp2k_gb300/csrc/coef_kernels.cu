@@ -230,47 +230,39 @@ __device__ T cxyz_cab_term(const T *cxyz, const T *alpha, int la, int lb, int lp
   return s;
 }
 
-// multinomial weight of lattice split for the general path
-__device__ __forceinline__ double fact(int n) {
-  double f = 1.0;
-  for (int i = 2; i <= n; i++)
-    f *= i;
-  return f;
-}
-__device__ __forceinline__ double ipow(double x, int n) {
-  double r = 1.0;
-  for (int i = 0; i < n; i++)
-    r *= x;
-  return r;
-}
-
 // C_xyz term (lx, ly, lz) <-> C_ijk through x_c = sum_d u_d dh[d][c]
-// (grid_ref_collint.h:698-762).  forward: scatter cxyz[e] into cijk (smem
+// (grid_ref_collint.h:698-762): the multinomial expansion of
+// x^lx y^ly z^lz in the lattice coordinates, with the powers of the step
+// vectors and the (inverse) factorials taken from a table (`tab`: n!, 1/n!,
+// then this level's dh[c]^n) so that the innermost loop has no division and
+// no power or factorial loop.  forward: scatter cxyz[e] into cijk (smem
 // atomics); adjoint: gather cijk into the returned value.
 template <typename T>
-__device__ T cxyz_cijk_term(bool forward, const double *h, int lp, int lx, int ly, int lz,
-                            T cval, T *cijk_scatter, const T *cijk_gather) {
-  const double fl = fact(lx) * fact(ly) * fact(lz);
+__device__ T cxyz_cijk_term(bool forward, const double *tab, int level, int lp, int lx, int ly,
+                            int lz, T cval, T *cijk_scatter, const T *cijk_gather) {
+  const double *F = tab, *IF = tab + kPowN;
+  const double *pw = tab + 2 * kPowN + (size_t)level * 9 * kPowN;
+  const double fl = F[lx] * F[ly] * F[lz];
+  const double cv = forward ? to_double(cval) * fl : fl;
   double acc = 0.0;
   for (int ix = 0; ix <= lx; ix++)
     for (int jx = 0; jx <= lx - ix; jx++) {
       const int kx = lx - ix - jx;
-      const double wx = ipow(h[0], ix) * ipow(h[3], jx) * ipow(h[6], kx) /
-                        (fact(ix) * fact(jx) * fact(kx));
+      const double wx = pw[0 * kPowN + ix] * pw[3 * kPowN + jx] * pw[6 * kPowN + kx] *
+                        (IF[ix] * IF[jx] * IF[kx]) * cv;
       for (int iy = 0; iy <= ly; iy++)
         for (int jy = 0; jy <= ly - iy; jy++) {
           const int ky = ly - iy - jy;
-          const double wy = ipow(h[1], iy) * ipow(h[4], jy) * ipow(h[7], ky) /
-                            (fact(iy) * fact(jy) * fact(ky));
+          const double wxy = wx * pw[1 * kPowN + iy] * pw[4 * kPowN + jy] * pw[7 * kPowN + ky] *
+                             (IF[iy] * IF[jy] * IF[ky]);
           for (int iz = 0; iz <= lz; iz++)
             for (int jz = 0; jz <= lz - iz; jz++) {
               const int kz = lz - iz - jz;
-              const double wz = ipow(h[2], iz) * ipow(h[5], jz) * ipow(h[8], kz) /
-                                (fact(iz) * fact(jz) * fact(kz));
               const int e = cidx(kx + ky + kz, jx + jy + jz, ix + iy + iz, lp);
-              const double wgt = wx * wy * wz * fl;
+              const double wgt = wxy * pw[2 * kPowN + iz] * pw[5 * kPowN + jz] *
+                                 pw[8 * kPowN + kz] * (IF[iz] * IF[jz] * IF[kz]);
               if (forward)
-                atomicAdd(&cijk_scatter[e], T(wgt * to_double(cval)));
+                atomicAdd(&cijk_scatter[e], T(wgt));
               else
                 acc += wgt * to_double(cijk_gather[e]);
             }
@@ -364,11 +356,10 @@ __device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *w
   if constexpr (!std::is_same<U, dfloat>::value) {
     if (general) {
       __syncwarp();
-      const double *h = a.levels->lv[d.level].dh;
       for (int e = lane; e < nco; e += 32) {
         int lz, ly, lx;
         decode_cidx(e, lp, lz, ly, lx);
-        cxyz_cijk_term<U>(true, h, lp, lx, ly, lz, cxyz[e], cijk, nullptr);
+        cxyz_cijk_term<U>(true, a.dhtab, d.level, lp, lx, ly, lz, cxyz[e], cijk, nullptr);
       }
       __syncwarp();
       for (int e = lane; e < nco; e += 32)
@@ -466,11 +457,10 @@ __device__ void post_task(const PostArgs &a, int t, const TaskDesc &d, double *w
   __syncwarp();
   if constexpr (!std::is_same<U, dfloat>::value) {
     if (general) {
-      const double *h = a.levels->lv[d.level].dh;
       for (int e = lane; e < nco; e += 32) {
         int lz, ly, lx;
         decode_cidx(e, lp, lz, ly, lx);
-        cxyz[e] = cxyz_cijk_term<U>(false, h, lp, lx, ly, lz, U(0), nullptr, cijk);
+        cxyz[e] = cxyz_cijk_term<U>(false, a.dhtab, d.level, lp, lx, ly, lz, U(0), nullptr, cijk);
       }
       __syncwarp();
     }
@@ -677,7 +667,7 @@ void launch_decontract(const ContractArgs &a, cudaStream_t s) {
   if (nw < 1)
     return launch_error("decontraction: sub-block too large for shared memory");
   const size_t smem = nw * per_warp;
-  cudaFuncSetAttribute(decontract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  set_smem((const void *)decontract_kernel, smem);
   decontract_kernel<<<grid_size_for(a.nsubs, nw), 32 * nw, smem, s>>>(a, a.words);
   count_launch();
 }
@@ -690,7 +680,7 @@ void launch_contract_hab(const ContractArgs &a, cudaStream_t s) {
   if (nw < 1)
     return launch_error("contraction: sub-block too large for shared memory");
   const size_t smem = nw * per_warp;
-  cudaFuncSetAttribute(contract_hab_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  set_smem((const void *)contract_hab_kernel, smem);
   contract_hab_kernel<<<grid_size_for(a.nsubs, nw), 32 * nw, smem, s>>>(a, a.words);
   count_launch();
 }
@@ -703,7 +693,7 @@ static void launch_coef_t(const CoefArgs &a, int words_per_warp, cudaStream_t s)
     return launch_error("coefficients: angular momenta too large for shared memory");
   const size_t smem = nw * per_warp;
   auto k = coefficients_kernel<U, Tout>;
-  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  set_smem((const void *)k, smem);
   k<<<grid_size_for(a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_warp);
   count_launch();
 }
@@ -728,7 +718,7 @@ static void launch_post_t(const PostArgs &a, int words_per_warp, cudaStream_t s)
     return launch_error("post-processing: angular momenta too large for shared memory");
   const size_t smem = nw * per_warp;
   auto k = post_kernel<U>;
-  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  set_smem((const void *)k, smem);
   k<<<grid_size_for(a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_warp);
   count_launch();
 }

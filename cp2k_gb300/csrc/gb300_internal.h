@@ -149,6 +149,7 @@ struct CoefArgs {
   LDiffs d;
   const LevelSet *levels; // device copy
   int general_fp64;       // write general-path coefficients as FP64
+  const double *dhtab;    // factorials and step-vector powers (build_dh_table)
 };
 
 struct GridArgs {
@@ -190,6 +191,7 @@ struct PostArgs {
   int compute_tau;
   LDiffs d;
   const LevelSet *levels;
+  const double *dhtab; // factorials and step-vector powers (build_dh_table)
 };
 
 struct ContractArgs {
@@ -282,6 +284,12 @@ void build_sphere(const LevelDesc &L, double disr, SphereHdr &h,
 void build_sphere_points(SphereHdr &h, const std::vector<int16_t> &tab, std::vector<int> &pts,
                          std::vector<int> &ploff);
 
+// Table for the general path's C_xyz <-> C_ijk transform: n! and 1/n! for
+// n < kPowN, then per level the powers dh[c]^n (c = 0..8 row-major, n < kPowN)
+constexpr int kPowN = GB300_LP_MAX + 1;
+inline size_t dh_table_size(int nlevels) { return 2 * kPowN + (size_t)nlevels * 9 * kPowN; }
+void build_dh_table(const LevelSet &ls, std::vector<double> &tab);
+
 // counts launches for grid_gb300_kernel_launches()
 void count_launch(int n = 1);
 // records a launch-configuration error; the host call fails after the launch
@@ -297,6 +305,9 @@ void launch_mlp_adam(float *P, const float *grad, float *m, float *v, int step, 
                      float beta1, float beta2, float eps, cudaStream_t s);
 void launch_mlp_predict(const float *P, const float *X, int n, const float *norm, float *Y,
                         cudaStream_t s);
+
+// raises a kernel's dynamic shared-memory limit to at least smem (cached)
+void set_smem(const void *kernel, size_t smem);
 
 // persistent grid size: CTAs that fit on all SMs at once for this kernel
 int persistent_blocks(const void *kernel, int threads, size_t smem);

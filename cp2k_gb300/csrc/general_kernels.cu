@@ -475,7 +475,7 @@ void launch_gen(const GridArgs &a, bool collocate, int njmax, LaunchCfg &cfg, cu
   const size_t smem = nw * per_warp;
   const void *k = collocate ? (const void *)collocate_general<T, LPB>
                             : (const void *)integrate_general<T, LPB>;
-  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  set_smem((const void *)k, smem);
   const int nb = cfg.blocks > 0 ? cfg.blocks : cfg_blocks(cfg, persistent_blocks(k, 32 * nw, smem));
   cfg.warps = nw;
   cfg.blocks = nb;

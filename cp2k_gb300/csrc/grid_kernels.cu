@@ -549,28 +549,37 @@ __global__ void __launch_bounds__(128, LPB <= 4 ? 5 : 1) integrate_ortho(GridArg
 #pragma unroll
         for (int l = 0; l < P; l++)
           wy[l] = M::zero();
+        // this lane's rows of the plane: j in [jlo, jhi] (jhi <= 1 - js), every
+        // G-th row from its group's phase, two rows per step; the grid values
+        // of the next step are loaded before this step's arithmetic
         const int JJ = xin ? (int)cg.jx[kk * cg.NX + (cx <= 0 ? -cx : cx - 1)] : -1;
-        const int jlo = -JJ, jhi = JJ + 1, jend = 1 - js;
-        for (int j = js + cg.grp; j <= jend; j += 2 * cg.G) {
-          const int j2 = j + cg.G;
-          const bool in1 = j >= jlo && j <= jhi;
-          const bool in2 = j2 >= jlo && j2 <= jhi;
-          if (!(in1 || in2))
-            continue;
-          const int j2c = j2 <= jend ? j2 : jend;
-          const T v1 =
-              in1 ? grid_get<N>(grid, zoff + (size_t)map[cg.w + j + cg.cmax] * nx + ig, gstride)
-                  : M::zero();
-          const T v2 =
-              in2 ? grid_get<N>(grid, zoff + (size_t)map[cg.w + j2c + cg.cmax] * nx + ig, gstride)
-                  : M::zero();
+        const int jlo = -JJ, jhi = JJ + 1, G = cg.G;
+        int j = js + cg.grp;
+        if (j < jlo)
+          j += ((jlo - j + G - 1) / G) * G;
+        const size_t base = zoff + ig;
+        auto fetch = [&](int jj, bool ok) -> T {
+          return ok ? grid_get<N>(grid, base + (size_t)map[cg.w + jj + cg.cmax] * nx, gstride)
+                    : M::zero();
+        };
+        bool has1 = j <= jhi, has2 = j + G <= jhi;
+        T v1 = fetch(j, has1), v2 = fetch(j + G, has2);
+        while (has1) {
+          const int jn = j + 2 * G;
+          const bool n1 = jn <= jhi, n2 = jn + G <= jhi;
+          const T v1n = fetch(jn, n1), v2n = fetch(jn + G, n2);
           T p1[PP], p2[PP];
           load_row<T, PP>(pol + (size_t)(cg.w + j + cg.cmax) * PP, p1);
-          load_row<T, PP>(pol + (size_t)(cg.w + j2c + cg.cmax) * PP, p2);
+          load_row<T, PP>(pol + (size_t)(cg.w + (has2 ? j + G : j) + cg.cmax) * PP, p2);
 #pragma unroll
           for (int ly = 0; ly < P; ly++)
             if (ly <= lp)
               wy[ly] = M::fma_acc(M::fma_acc(wy[ly], v1, p1[ly]), v2, p2[ly]);
+          j = jn;
+          has1 = n1;
+          has2 = n2;
+          v1 = v1n;
+          v2 = v2n;
         }
 #pragma unroll
         for (int l = 0; l < P; l++)
@@ -651,7 +660,7 @@ static void launch_ortho_t(const GridArgs &a, bool collocate, int wmax, LaunchCf
   const void *k = pl          ? (const void *)collocate_ortho_pl<N, LPB>
                   : collocate ? (const void *)collocate_ortho<N, LPB>
                               : (const void *)integrate_ortho<N, LPB>;
-  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  set_smem((const void *)k, smem);
   const int nb = cfg.blocks > 0 ? cfg.blocks : cfg_blocks(cfg, persistent_blocks(k, 32 * nw, smem));
   cfg.warps = nw;
   cfg.blocks = nb;

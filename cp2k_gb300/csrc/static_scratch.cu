@@ -228,6 +228,10 @@ GB300_API int grid_gb300_collocate_pgf_product_static(
   off = align256(off + 6 * sizeof(double));
   const size_t o_levels = off;
   off = align256(off + sizeof(LevelSet));
+  std::vector<double> dhtab;
+  build_dh_table(levels, dhtab);
+  const size_t o_dhtab = off;
+  off = align256(off + dhtab.size() * sizeof(double));
   const size_t o_sph = off;
   off = align256(off + sizeof(SphereHdr));
   const size_t o_tab = off;
@@ -248,6 +252,7 @@ GB300_API int grid_gb300_collocate_pgf_product_static(
   const double atoms[6] = {ra[0], ra[1], ra[2], ra[0] + rab[0], ra[1] + rab[1], ra[2] + rab[2]};
   memcpy(&host[o_atoms], atoms, sizeof(atoms));
   memcpy(&host[o_levels], &levels, sizeof(levels));
+  memcpy(&host[o_dhtab], dhtab.data(), dhtab.size() * sizeof(double));
   sph.off = 0;
   memcpy(&host[o_sph], &sph, sizeof(sph));
   if (!tab.empty())
@@ -270,6 +275,7 @@ GB300_API int grid_gb300_collocate_pgf_product_static(
   co.d = dl;
   co.levels = (const LevelSet *)(dev + o_levels);
   co.general_fp64 = 0;
+  co.dhtab = (const double *)(dev + o_dhtab);
   launch_coefficients(co, ARITH_FP64, (int)coef_words(la_max + dl.la_max, lb_max + dl.lb_max), s);
 
   GridArgs ga{};
