@@ -315,11 +315,17 @@ def gpu_arm(args, world, rank, local):
             tuned[prec] = (tl.autotune(100, pab, grids, V, hab, stream=stream), tl.tuned_split())
         torch.cuda.synchronize()
 
-    def run_steps(prec, sched, nsteps):
+    launched = [0, 0]  # kernel counter at the first timed step, launches in timed steps
+
+    def run_steps(prec, sched, nsteps, warm=1):
+        # a precision or schedule switch may rebuild work queues on the host:
+        # `warm` untimed steps run first so that no timed step pays for it
         tl.set_precision(prec)
         tl.set_schedule(sched)
         times = []
-        for _ in range(nsteps):
+        for i in range(warm + nsteps):
+            if i == warm:
+                launched[0] = G.kernel_launches()
             flush.zero_()
             torch.cuda.synchronize()
             with torch.cuda.stream(stream):
@@ -329,7 +335,9 @@ def gpu_arm(args, world, rank, local):
                 tl.integrate_device(V, hab, stream=stream)
                 e[1].record(stream)
             torch.cuda.synchronize()
-            times.append(e[0].elapsed_time(e[1]))
+            if i >= warm:
+                times.append(e[0].elapsed_time(e[1]))
+        launched[1] = G.kernel_launches() - launched[0]
         return times
 
     # warm-up all paths, then the timed regions
@@ -337,14 +345,13 @@ def gpu_arm(args, world, rank, local):
     run_steps(G.MIXED, G.SCHEDULE_SIZE, max(1, min(args.warmup, 2)))
     run_steps(G.FP64, G.SCHEDULE_SIZE, max(1, min(args.warmup, 2)))
     run_steps(G.FP32, sched_mixed, max(1, min(args.warmup, 2)))
-    launches0 = G.kernel_launches()
     barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         torch.cuda.nvtx.range_push("timed_mixed")  # lets a profiler select this region
         t_mixed = run_steps(G.MIXED, sched_mixed, args.steps)
         torch.cuda.nvtx.range_pop()
-    launches = G.kernel_launches() - launches0
+    launches = launched[1]
     torch.cuda.synchronize()
     barrier(world)
     rho_mixed = [g.clone() for g in grids]

@@ -276,6 +276,7 @@ struct Mode { // everything that depends on the l shifts of a call
   std::vector<Queue> queues; // launch order
   int coef_words = 0;      // per-warp shared memory words of coefficient/post
   int sched_version = -1;
+  uint8_t *d_fp32 = nullptr; // per task: 1 if the mixed mode runs it in plain FP32
 };
 
 struct TaskList {
@@ -530,6 +531,8 @@ static void free_device(TaskList *t) {
   for (auto &kv : t->modes) {
     if (kv.second.d_coef_off)
       cudaFree(kv.second.d_coef_off);
+    if (kv.second.d_fp32)
+      cudaFree(kv.second.d_fp32);
     for (auto &q : kv.second.queues)
       if (q.d_idx)
         cudaFree(q.d_idx);
@@ -866,7 +869,9 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
 namespace gb300 {
 
 static Mode &get_mode(TaskList *t, const LDiffs &d) {
-  const int key = mode_key(d);
+  // one mode per (l shifts, precision): switching the precision back and forth
+  // reuses the queues built for each
+  const int key = mode_key(d) * 4 + t->precision;
   auto it = t->modes.find(key);
   if (it != t->modes.end() && it->second.sched_version == t->sched_version)
     return it->second;
@@ -894,6 +899,7 @@ static Mode &get_mode(TaskList *t, const LDiffs &d) {
   // work queues, descending cost
   // work queues: (general, lp bucket, FP32 class, size class), descending cost
   std::map<int, std::vector<std::pair<double, int>>> items;
+  std::vector<uint8_t> fp32(std::max(t->ntasks, 1), 0);
   for (int s = 0; s < t->ntasks; s++) {
     const TaskDesc &k = t->tasks[s];
     if (k.flags & TF_SKIP)
@@ -905,6 +911,7 @@ static Mode &get_mode(TaskList *t, const LDiffs &d) {
     const int g = (k.flags & TF_GENERAL) ? 1 : 0;
     const int cls = (t->precision == GRID_GB300_MIXED && t->gbound[s] <= t->mixed_threshold)
                         ? 1 : 0;
+    fp32[s] = (uint8_t)cls;
     const int ext = g == 0 ? 2 * t->sph[k.sphere].cmax + 2 : k.imax[1] - k.center[1] + 1;
     const int sz = ext <= t->small_extent[t->precision] ? 0 : 1;
     double cost;
@@ -961,6 +968,9 @@ static Mode &get_mode(TaskList *t, const LDiffs &d) {
     q.d_idx = dalloc_copy(idx);
     m.queues.push_back(q);
   }
+  if (m.d_fp32)
+    cudaFree(m.d_fp32);
+  m.d_fp32 = dalloc_copy(fp32);
   m.sched_version = t->sched_version;
   t->gen++;
   return m;
@@ -1078,7 +1088,8 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
                   t->contract_words};
   launch_decontract(ca, s);
   CoefArgs co{t->d_tasks, t->d_subs, m.d_coef_off, t->d_atom_pos, t->d_pab_cart, t->d_coef,
-              t->ntasks, func, d, t->d_levels, arith == ARITH_MIXED ? 1 : 0, t->d_dhtab};
+              t->ntasks, func, d, t->d_levels, arith == ARITH_MIXED ? 1 : 0, t->d_dhtab,
+              arith == ARITH_MIXED ? m.d_fp32 : nullptr};
   launch_coefficients(co, arith, m.coef_words, s);
   record_phase(t, 1, s);
   for (int l = 0; l < t->nlevels; l++) {
@@ -1199,7 +1210,8 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
     CK(cudaMemsetAsync(virial, 0, sizeof(double) * 9, s));
   PostArgs pa{t->d_tasks, t->d_subs, m.d_coef_off, t->d_coef_int,
               need_pab ? t->d_pab_cart : nullptr, t->d_hab_cart, t->d_atom_pos, forces, virial,
-              t->ntasks, tau ? 1 : 0, d, t->d_levels, t->d_dhtab};
+              t->ntasks, tau ? 1 : 0, d, t->d_levels, t->d_dhtab,
+              arith == ARITH_MIXED ? m.d_fp32 : nullptr};
   launch_post(pa, arith, m.coef_words, s);
   CK(cudaMemsetAsync(hab, 0, sizeof(double) * (size_t)t->buffer_len, s));
   ContractArgs cb{t->d_subs, (int)t->subs.size(), t->d_sphi, nullptr, hab, t->d_hab_cart,
@@ -1477,10 +1489,8 @@ GB300_API void grid_gb300_set_precision(const grid_gb300_task_list *task_list, i
       precision != GRID_GB300_FP32)
     fail("unknown precision mode %d", precision);
   TaskList *t = TL(task_list);
-  if (t->precision != precision) {
-    t->precision = precision;
-    t->sched_version++; // queues depend on the precision split
-  }
+  // queues are kept per precision (get_mode); nothing to rebuild here
+  t->precision = precision;
 }
 
 GB300_API int grid_gb300_get_precision(const grid_gb300_task_list *task_list) {

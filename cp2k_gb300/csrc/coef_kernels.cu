@@ -148,6 +148,14 @@ __device__ void prep_one(int f, Orb a, Orb b, T za, T zb, T p, const CabW<T> &w)
   }
 }
 
+// A group of lanes working on one task: the whole warp, or half of it for
+// small tasks (two tasks per warp keep more lanes busy).
+struct Grp {
+  int lane, n;   // lane within the group, group size (16 or 32)
+  unsigned mask; // the group's lanes in the warp
+  __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+};
+
 // ------------------------------------------------------------------------
 // Binomial expansion tables alpha[dir][lxb][lxa][l]: coefficient of (x-p)^l
 // in (x-a)^lxa (x-b)^lxb  (grid_ref_collint.h:838-861)
@@ -156,12 +164,12 @@ __constant__ float c_binom[GB300_LP_MAX + 1][GB300_LP_MAX + 1];
 
 template <typename T>
 __device__ void fill_alpha(T *alpha, int la, int lb, int lp, const double ra[3],
-                           const double rb[3], const double rp[3], int lane) {
+                           const double rb[3], const double rp[3], const Grp &g) {
   const int na = la + 1, nb = lb + 1, P = lp + 1;
-  for (int e = lane; e < 3 * na * nb * P; e += 32)
+  for (int e = g.lane; e < 3 * na * nb * P; e += g.n)
     alpha[e] = T(0);
-  __syncwarp();
-  for (int e = lane; e < 3 * na * nb; e += 32) {
+  g.sync();
+  for (int e = g.lane; e < 3 * na * nb; e += g.n) {
     const int d = e / (na * nb), r = e % (na * nb), xb = r / na, xa = r % na;
     const T pa = T(rp[d] - ra[d]), pb = T(rp[d] - rb[d]);
     T *al = alpha + ((size_t)(d * nb + xb) * na + xa) * P;
@@ -176,7 +184,7 @@ __device__ void fill_alpha(T *alpha, int la, int lb, int lp, const double ra[3],
       powa *= pa;
     }
   }
-  __syncwarp();
+  g.sync();
 }
 
 // sum over C_ab entries of one C_xyz monomial (or the adjoint), gathering
@@ -294,6 +302,8 @@ __device__ __forceinline__ void store_coef(void *out, size_t i, U v, bool as_fp6
   } else if constexpr (std::is_same<Tout, dfloat>::value) {
     if constexpr (std::is_same<U, dfloat>::value)
       ((dfloat *)out)[i] = v;
+    else if constexpr (std::is_same<U, float>::value)
+      ((dfloat *)out)[i] = dfloat{v, 0.f};
     else
       ((dfloat *)out)[i] = df_make(to_double(v));
   } else if constexpr (std::is_same<Tout, float>::value && std::is_same<U, float>::value) {
@@ -307,7 +317,7 @@ __device__ __forceinline__ void store_coef(void *out, size_t i, U v, bool as_fp6
 // coefficients of one task (one warp): P_ab -> C_ab -> C_xyz (-> C_ijk)
 // ------------------------------------------------------------------------
 template <typename U, typename Tout>
-__device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *ws, int lane,
+__device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *ws, const Grp &g,
                           bool as_fp64) {
   const SubblockDesc sb = a.subs[d.subblock];
   const int la_max = d.la_max + a.d.la_max, lb_max = d.lb_max + a.d.lb_max;
@@ -318,31 +328,31 @@ __device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *w
   U *alpha = (U *)((double *)cab + (size_t)n1 * n2);
   U *cxyz = (U *)((double *)alpha + 3 * (size_t)(la_max + 1) * (lb_max + 1) * (lp + 1));
   U *cijk = (U *)((double *)cxyz + ncoset(lp));
-  for (int e = lane; e < n1 * n2; e += 32)
+  for (int e = g.lane; e < n1 * n2; e += g.n)
     cabd[e] = 0.0;
-  __syncwarp();
+  g.sync();
   // P_ab -> C_ab in FP64 (grid_prepare_pab.h; a few operations per element)
   const CabW<double> w{cabd, n1};
   const double *pab = a.pab_cart + sb.cart_offset;
   const int na = ncoset(d.la_max) - ncoset(d.la_min - 1);
   const int nb = ncoset(d.lb_max) - ncoset(d.lb_min - 1);
-  for (int e = lane; e < na * nb; e += 32) {
+  for (int e = g.lane; e < na * nb; e += g.n) {
     const int ia = ncoset(d.la_min - 1) + e % na, ib = ncoset(d.lb_min - 1) + e / na;
     const double p = pab[(size_t)(d.o2 + ib) * sb.ncoa + d.o1 + ia];
     prep_one<double>(a.func, orb_of_index(ia), orb_of_index(ib), d.zeta, d.zetb, p, w);
   }
-  __syncwarp();
-  for (int e = lane; e < n1 * n2; e += 32)
+  g.sync();
+  for (int e = g.lane; e < n1 * n2; e += g.n)
     cab[e] = U(cabd[e]);
   const double *ra = a.atom_pos + 3 * d.iatom;
   double rb[3];
   for (int i = 0; i < 3; i++)
     rb[i] = ra[i] + d.rab[i];
-  fill_alpha<U>(alpha, la_max, lb_max, lp, ra, rb, d.rp, lane);
+  fill_alpha<U>(alpha, la_max, lb_max, lp, ra, rb, d.rp, g);
   const U pref = U(d.prefexp * ((d.iatom == d.jatom) ? 1.0 : 2.0));
   const int nco = ncoset(lp);
   const bool general = d.flags & TF_GENERAL;
-  for (int e = lane; e < nco; e += 32) {
+  for (int e = g.lane; e < nco; e += g.n) {
     int pz, py, px;
     decode_cidx(e, lp, pz, py, px);
     const U v = cab_cxyz_term<U>(cab, n1, alpha, la_max, lb_max, lp, px, py, pz) * pref;
@@ -355,36 +365,41 @@ __device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *w
   }
   if constexpr (!std::is_same<U, dfloat>::value) {
     if (general) {
-      __syncwarp();
-      for (int e = lane; e < nco; e += 32) {
+      g.sync();
+      for (int e = g.lane; e < nco; e += g.n) {
         int lz, ly, lx;
         decode_cidx(e, lp, lz, ly, lx);
         cxyz_cijk_term<U>(true, a.dhtab, d.level, lp, lx, ly, lz, cxyz[e], cijk, nullptr);
       }
-      __syncwarp();
-      for (int e = lane; e < nco; e += 32)
+      g.sync();
+      for (int e = g.lane; e < nco; e += g.n)
         store_coef<Tout, U>(a.coef, (size_t)a.coef_off[t] + e, cijk[e], as_fp64);
     }
   }
-  __syncwarp();
+  g.sync();
 }
 
 // U: working type of ortho tasks; general tasks run in FP64 when U is dfloat
 template <typename U, typename Tout>
-__global__ void __launch_bounds__(128) coefficients_kernel(CoefArgs a, int words_per_warp) {
+__global__ void __launch_bounds__(128) coefficients_kernel(CoefArgs a, int words_per_group,
+                                                           int gsize) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  double *ws = (double *)smem + (size_t)(threadIdx.x >> 5) * words_per_warp;
-  for (int t = gw; t < a.ntasks; t += nwarps) {
+  const int ng = 32 / gsize, half = lane / gsize;
+  const Grp g{lane % gsize, gsize, gsize == 32 ? FULL : ((1u << gsize) - 1) << (half * gsize)};
+  const int gid = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * ng + half;
+  const int ngroups = ((gridDim.x * blockDim.x) >> 5) * ng;
+  double *ws = (double *)smem + (size_t)((threadIdx.x >> 5) * ng + half) * words_per_group;
+  for (int t = gid; t < a.ntasks; t += ngroups) {
     const TaskDesc d = a.tasks[t];
     if (d.flags & TF_SKIP)
       continue;
     if (std::is_same<U, dfloat>::value && (d.flags & TF_GENERAL))
-      coef_task<double, Tout>(a, t, d, ws, lane, a.general_fp64);
+      coef_task<double, Tout>(a, t, d, ws, g, a.general_fp64);
+    else if (std::is_same<U, dfloat>::value && a.task_fp32 && a.task_fp32[t])
+      coef_task<float, Tout>(a, t, d, ws, g, false); // FP32 task of the mixed mode
     else
-      coef_task<U, Tout>(a, t, d, ws, lane, false);
+      coef_task<U, Tout>(a, t, d, ws, g, false);
   }
 }
 
@@ -435,7 +450,7 @@ __device__ T vab(const VabCtx<T> &x, bool tau, int kind, int i, int j, Orb a, Or
 }
 
 template <typename U>
-__device__ void post_task(const PostArgs &a, int t, const TaskDesc &d, double *ws, int lane,
+__device__ void post_task(const PostArgs &a, int t, const TaskDesc &d, double *ws, const Grp &g,
                           double f[6], double v[9]) {
   const SubblockDesc sb = a.subs[d.subblock];
   const int la_max = d.la_max + a.d.la_max, lb_max = d.lb_max + a.d.lb_max;
@@ -448,41 +463,41 @@ __device__ void post_task(const PostArgs &a, int t, const TaskDesc &d, double *w
   const int nco = ncoset(lp);
   const double *src = a.coef + a.coef_off[t];
   const bool general = d.flags & TF_GENERAL;
-  for (int e = lane; e < nco; e += 32) {
+  for (int e = g.lane; e < nco; e += g.n) {
     if (general)
       cijk[e] = U(src[e]);
     else
       cxyz[e] = U(src[e]);
   }
-  __syncwarp();
+  g.sync();
   if constexpr (!std::is_same<U, dfloat>::value) {
     if (general) {
-      for (int e = lane; e < nco; e += 32) {
+      for (int e = g.lane; e < nco; e += g.n) {
         int lz, ly, lx;
         decode_cidx(e, lp, lz, ly, lx);
         cxyz[e] = cxyz_cijk_term<U>(false, a.dhtab, d.level, lp, lx, ly, lz, U(0), nullptr, cijk);
       }
-      __syncwarp();
+      g.sync();
     }
   }
   const double *ra = a.atom_pos + 3 * d.iatom;
   double rb[3];
   for (int i = 0; i < 3; i++)
     rb[i] = ra[i] + d.rab[i];
-  fill_alpha<U>(alpha, la_max, lb_max, lp, ra, rb, d.rp, lane);
+  fill_alpha<U>(alpha, la_max, lb_max, lp, ra, rb, d.rp, g);
   const U pref = U(d.prefexp);
-  for (int e = lane; e < m1 * m2; e += 32) {
+  for (int e = g.lane; e < m1 * m2; e += g.n) {
     const Orb oa = orb_of_index(e % m1), ob = orb_of_index(e / m1);
     cab[e] = cxyz_cab_term<U>(cxyz, alpha, la_max, lb_max, lp, oa, ob) * pref;
   }
-  __syncwarp();
+  g.sync();
   VabCtx<U> x{cab, m1, U(d.zeta), U(d.zetb), {U(d.rab[0]), U(d.rab[1]), U(d.rab[2])}};
   const bool tau = a.compute_tau;
   const int na = ncoset(d.la_max) - ncoset(d.la_min - 1);
   const int nb = ncoset(d.lb_max) - ncoset(d.lb_min - 1);
   const double *pab = a.pab_cart ? a.pab_cart + sb.cart_offset : nullptr;
   double *hab = a.hab_cart + sb.cart_offset;
-  for (int e = lane; e < na * nb; e += 32) {
+  for (int e = g.lane; e < na * nb; e += g.n) {
     const int ia = ncoset(d.la_min - 1) + e % na, ib = ncoset(d.lb_min - 1) + e / na;
     const Orb oa = orb_of_index(ia), ob = orb_of_index(ib);
     const size_t el = (size_t)(d.o2 + ib) * sb.ncoa + d.o1 + ia;
@@ -501,38 +516,43 @@ __device__ void post_task(const PostArgs &a, int t, const TaskDesc &d, double *w
                                  to_double(vab<U>(x, tau, V_VB, i, j, oa, ob)));
     }
   }
-  __syncwarp();
+  g.sync();
 }
 
 template <typename U>
-__global__ void __launch_bounds__(128) post_kernel(PostArgs a, int words_per_warp) {
+__global__ void __launch_bounds__(128) post_kernel(PostArgs a, int words_per_group, int gsize) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ double vir_cta[9];
   const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  double *ws = (double *)smem + (size_t)(threadIdx.x >> 5) * words_per_warp;
+  const int ng = 32 / gsize, half = lane / gsize;
+  const Grp g{lane % gsize, gsize, gsize == 32 ? FULL : ((1u << gsize) - 1) << (half * gsize)};
+  const int gid = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * ng + half;
+  const int ngroups = ((gridDim.x * blockDim.x) >> 5) * ng;
+  double *ws = (double *)smem + (size_t)((threadIdx.x >> 5) * ng + half) * words_per_group;
   if (threadIdx.x < 9)
     vir_cta[threadIdx.x] = 0.0;
   __syncthreads();
-  for (int t = gw; t < a.ntasks; t += nwarps) {
+  for (int t = gid; t < a.ntasks; t += ngroups) {
     const TaskDesc d = a.tasks[t];
     if (d.flags & TF_SKIP)
       continue;
     double f[6] = {0, 0, 0, 0, 0, 0}, v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     if (std::is_same<U, dfloat>::value && (d.flags & TF_GENERAL))
-      post_task<double>(a, t, d, ws, lane, f, v);
+      post_task<double>(a, t, d, ws, g, f, v);
+    else if (std::is_same<U, dfloat>::value && a.task_fp32 && a.task_fp32[t])
+      post_task<float>(a, t, d, ws, g, f, v); // FP32 task of the mixed mode
     else
-      post_task<U>(a, t, d, ws, lane, f, v);
+      post_task<U>(a, t, d, ws, g, f, v);
     const double scale = (d.iatom == d.jatom) ? 1.0 : 2.0;
+    // sums over the group's lanes (xor offsets below the group size stay inside it)
     if (a.forces) {
       for (int i = 0; i < 6; i++) {
         double s = f[i];
-        for (int o = 16; o > 0; o >>= 1)
-          s += __shfl_xor_sync(FULL, s, o);
+        for (int o = gsize / 2; o > 0; o >>= 1)
+          s += __shfl_xor_sync(g.mask, s, o);
         f[i] = s;
       }
-      if (lane == 0)
+      if (g.lane == 0)
         for (int i = 0; i < 3; i++) {
           atomicAdd(&a.forces[3 * d.iatom + i], scale * f[i]);
           atomicAdd(&a.forces[3 * d.jatom + i], scale * f[3 + i]);
@@ -541,11 +561,11 @@ __global__ void __launch_bounds__(128) post_kernel(PostArgs a, int words_per_war
     if (a.virial) {
       for (int i = 0; i < 9; i++) {
         double s = v[i];
-        for (int o = 16; o > 0; o >>= 1)
-          s += __shfl_xor_sync(FULL, s, o);
+        for (int o = gsize / 2; o > 0; o >>= 1)
+          s += __shfl_xor_sync(g.mask, s, o);
         v[i] = s;
       }
-      if (lane == 0)
+      if (g.lane == 0)
         for (int i = 0; i < 9; i++)
           atomicAdd(&vir_cta[i], scale * v[i]);
     }
@@ -685,16 +705,20 @@ void launch_contract_hab(const ContractArgs &a, cudaStream_t s) {
   count_launch();
 }
 
+// two tasks per warp (groups of 16 lanes) while the per-task work is small
+constexpr int kSmallTaskWords = 1024;
+
 template <typename U, typename Tout>
-static void launch_coef_t(const CoefArgs &a, int words_per_warp, cudaStream_t s) {
-  const size_t per_warp = (size_t)words_per_warp * 8;
+static void launch_coef_t(const CoefArgs &a, int words_per_group, cudaStream_t s) {
+  const int gsize = words_per_group <= kSmallTaskWords ? 16 : 32;
+  const size_t per_warp = (size_t)words_per_group * 8 * (32 / gsize);
   const int nw = warps_for(per_warp);
   if (nw < 1)
     return launch_error("coefficients: angular momenta too large for shared memory");
   const size_t smem = nw * per_warp;
   auto k = coefficients_kernel<U, Tout>;
   set_smem((const void *)k, smem);
-  k<<<grid_size_for(a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_warp);
+  k<<<grid_size_for(a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_group, gsize);
   count_launch();
 }
 
@@ -711,15 +735,16 @@ void launch_coefficients(const CoefArgs &a, int arith, int words_per_warp, cudaS
 }
 
 template <typename U>
-static void launch_post_t(const PostArgs &a, int words_per_warp, cudaStream_t s) {
-  const size_t per_warp = (size_t)words_per_warp * 8;
+static void launch_post_t(const PostArgs &a, int words_per_group, cudaStream_t s) {
+  const int gsize = words_per_group <= kSmallTaskWords ? 16 : 32;
+  const size_t per_warp = (size_t)words_per_group * 8 * (32 / gsize);
   const int nw = warps_for(per_warp);
   if (nw < 1)
     return launch_error("post-processing: angular momenta too large for shared memory");
   const size_t smem = nw * per_warp;
   auto k = post_kernel<U>;
   set_smem((const void *)k, smem);
-  k<<<grid_size_for(a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_warp);
+  k<<<grid_size_for(a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_group, gsize);
   count_launch();
 }
 

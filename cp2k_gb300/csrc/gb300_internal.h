@@ -150,6 +150,7 @@ struct CoefArgs {
   const LevelSet *levels; // device copy
   int general_fp64;       // write general-path coefficients as FP64
   const double *dhtab;    // factorials and step-vector powers (build_dh_table)
+  const uint8_t *task_fp32; // mixed mode: 1 for tasks of the FP32 class (or null)
 };
 
 struct GridArgs {
@@ -192,6 +193,7 @@ struct PostArgs {
   LDiffs d;
   const LevelSet *levels;
   const double *dhtab; // factorials and step-vector powers (build_dh_table)
+  const uint8_t *task_fp32; // mixed mode: 1 for tasks of the FP32 class (or null)
 };
 
 struct ContractArgs {
