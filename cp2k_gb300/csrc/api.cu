@@ -308,7 +308,7 @@ struct TaskList {
   std::vector<double> gbound;    // per task bound of |contribution| for |P| <= 1
   std::vector<float2> seeds;     // per task [3][6] dfloat recurrence seeds (ortho)
   float2 *d_seeds = nullptr;
-  double mixed_threshold = 1.0;  // mixed path: tasks with gbound <= this run FP32
+  double mixed_threshold = 0.3;  // mixed path: tasks with gbound <= this run FP32
   std::vector<int> npts_local;   // [nlevels][3]
   size_t cart_total = 0;
   int contract_words = 1;
@@ -422,6 +422,62 @@ void build_sphere(const LevelDesc &L, double disr, SphereHdr &h, std::vector<int
           last = jj;
       jx[(size_t)kk * NX + ii] = (int16_t)last;
     }
+  // integrate lane plan: split the x range into nc chunks of sw lanes and
+  // give each chunk n[c] row groups (floor(32 / sw) groups in all), so that
+  // lanes of short edge columns are not idle while central columns finish;
+  // cost = sum over planes of the slowest group's rows, minimised over nc
+  h.iplan = 0;
+  {
+    const int W = 2 * NX; // x in [lb0, 1 - lb0]
+    if (W <= 32) {
+      auto len = [&](int kk, int x) { // rows of column x on plane kk
+        const int ii = x <= 0 ? -x : x - 1;
+        return 2 * (jx[(size_t)kk * NX + ii] + 1);
+      };
+      long long best = -1;
+      for (int nc = 1; nc <= 4; nc++) {
+        const int sw = (W + nc - 1) / nc, gt = 32 / sw;
+        if (gt < nc || (nc > 1 && (nc - 1) * sw >= W))
+          continue;
+        int n[4] = {1, 1, 1, 1};
+        auto cost = [&](const int *nn) {
+          long long c = 0;
+          for (int kk = 0; kk < K; kk++) {
+            int m = 0;
+            for (int ci = 0; ci < nc; ci++) {
+              int ml = 0;
+              for (int x = h.lb[0] + ci * sw; x < h.lb[0] + (ci + 1) * sw && x <= 1 - h.lb[0]; x++)
+                ml = std::max(ml, len(kk, x));
+              m = std::max(m, (ml + nn[ci] - 1) / nn[ci]);
+            }
+            c += m;
+          }
+          return c;
+        };
+        for (int extra = gt - nc; extra > 0; extra--) { // greedy: where it helps most
+          int bc = 0;
+          long long bv = -1;
+          for (int ci = 0; ci < nc; ci++) {
+            n[ci]++;
+            const long long v = cost(n);
+            n[ci]--;
+            if (bv < 0 || v < bv) {
+              bv = v;
+              bc = ci;
+            }
+          }
+          n[bc]++;
+        }
+        const long long c = cost(n);
+        if (best < 0 || c < best) {
+          best = c;
+          h.iplan = sw | (nc << 6);
+          for (int ci = 0; ci < nc; ci++)
+            h.iplan |= n[ci] << (9 + 5 * ci);
+        }
+      }
+    }
+  }
   for (int kk = 0; kk < K; kk++)
     tab.push_back((int16_t)js[kk]);
   for (int kk = 0; kk < K; kk++)
@@ -472,19 +528,21 @@ void build_sphere_points(SphereHdr &h, const std::vector<int16_t> &tab, std::vec
     fail("sphere point lists exceed int offsets");
 }
 
-// Upper bound of |a Gaussian-product contribution| for |P_ab| <= 1: the
-// prefactor times, per direction, the sum over the binomial expansion
-// coefficients of (x-a)^i (x-b)^j about p of max_x |x^n exp(-zetp x^2)|
-// = (n / (2 e zetp))^(n/2).  Used to pick FP32 or double-float per task.
+// Upper bound of |a Gaussian-product contribution| to any point for
+// Cartesian density-matrix elements |P_ab| <= 1: the prefactor times the sum,
+// over the Cartesian pairs (a, b) of the task's sets, of the product over the
+// three directions of B[a_d][b_d] = sum_n |alpha_n| max_x |x^n exp(-zetp x^2)|
+// with alpha the binomial expansion of (x-A)^i (x-B)^j about P and
+// max_x |x^n exp(-z x^2)| = (n / (2 e z))^(n/2).  Used to pick FP32 or
+// double-float per task.
 static double contribution_bound(const TaskDesc &d, const double *ra) {
   const int la = d.la_max, lb = d.lb_max;
   double m[2 * GB300_LMAX + 2];
   for (int n = 0; n <= la + lb; n++)
     m[n] = n == 0 ? 1.0 : pow(n / (2.0 * M_E * d.zetp), 0.5 * n);
-  double g = d.prefexp * ((d.iatom == d.jatom) ? 1.0 : 2.0);
+  double B[3][GB300_LMAX + 1][GB300_LMAX + 1];
   for (int dir = 0; dir < 3; dir++) {
     const double pa = d.rp[dir] - ra[dir], pb = d.rp[dir] - (ra[dir] + d.rab[dir]);
-    double s = 0.0;
     for (int xa = 0; xa <= la; xa++)
       for (int xb = 0; xb <= lb; xb++) {
         double al[2 * GB300_LMAX + 2] = {0};
@@ -497,12 +555,25 @@ static double contribution_bound(const TaskDesc &d, const double *ra) {
           }
           ca = ca * (xa - k) / (k + 1);
         }
+        double s = 0.0;
         for (int n = 0; n <= xa + xb; n++)
           s += fabs(al[n]) * m[n];
+        B[dir][xa][xb] = s;
       }
-    g *= s;
   }
-  return g;
+  double g = 0.0;
+  for (int l1 = d.la_min; l1 <= la; l1++)
+    for (int ax = 0; ax <= l1; ax++)
+      for (int ay = 0; ay <= l1 - ax; ay++) {
+        const int az = l1 - ax - ay;
+        for (int l2 = d.lb_min; l2 <= lb; l2++)
+          for (int bx = 0; bx <= l2; bx++)
+            for (int by = 0; by <= l2 - bx; by++) {
+              const int bz = l2 - bx - by;
+              g += B[0][ax][bx] * B[1][ay][by] * B[2][az][bz];
+            }
+      }
+  return g * d.prefexp * ((d.iatom == d.jatom) ? 1.0 : 2.0);
 }
 
 template <typename T> static T *dalloc_copy(const std::vector<T> &v) {

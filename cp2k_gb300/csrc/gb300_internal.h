@@ -80,6 +80,10 @@ struct SphereHdr {
   int off; // into the int16 table: [K] jstart, [K] row offsets, istart rows
   int jxo; // relative offset of the [K][1-lb[0]] table of last row index per x
   int plo; // point lists: index of this sphere's plane offsets in sph_ploff (-1: none)
+  // integrate lane plan for cubes up to 32 wide (0: none): x-chunk width sw
+  // (bits 0-5), number of chunks nc (bits 6-8), row groups per chunk n[c]
+  // (5 bits each from bit 9)
+  int iplan;
 };
 
 struct LevelDesc {

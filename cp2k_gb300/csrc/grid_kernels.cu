@@ -530,11 +530,32 @@ __global__ void __launch_bounds__(128, LPB <= 4 ? 5 : 1) integrate_ortho(GridArg
     const void *grid = a.grids_in[d.level];
     const int gstride = a.grid_stride;
     const size_t nx = L.npts_local[0], nxy = nx * L.npts_local[1];
-    const bool lane_on = cg.grp < cg.G;
+    // lanes: x chunks of sub-warps, rows of a plane split over the groups
+    // of a chunk; the sphere's plan (cubes up to 32 wide) sizes the chunks
+    // and gives central chunks, whose columns are longer, more groups
+    const int ip = a.sph[d.sphere].iplan;
+    int sub = cg.sub, phase = cg.grp, nph = cg.G, xstep = cg.SW, cbase = 0;
+    bool on = cg.grp < cg.G;
+    if (ip) {
+      const int sw = ip & 63, nc = (ip >> 6) & 7, gi = lane / sw;
+      sub = lane % sw;
+      on = false;
+      for (int c = 0, base = 0; c < nc; c++) {
+        const int nn = (ip >> (9 + 5 * c)) & 31;
+        if (!on && gi < base + nn) {
+          phase = gi - base;
+          nph = nn;
+          cbase = c * sw;
+          on = true;
+        }
+        base += nn;
+      }
+      xstep = cg.x_hi - cg.x_lo + 1; // one pass covers every chunk
+    }
 
-    for (int xc = cg.x_lo; xc <= cg.x_hi; xc += cg.SW) {
-      const int cx = xc + cg.sub;
-      const bool xin = lane_on && cx <= cg.x_hi;
+    for (int xc = cg.x_lo; xc <= cg.x_hi; xc += xstep) {
+      const int cx = xc + cbase + sub;
+      const bool xin = on && cx <= cg.x_hi;
       const int ig = map[(xin ? cx : cg.x_lo) + cg.cmax];
       T ayz[NYZ]; // [lz][ly], lz + ly <= LPB
 #pragma unroll
@@ -553,8 +574,8 @@ __global__ void __launch_bounds__(128, LPB <= 4 ? 5 : 1) integrate_ortho(GridArg
         // G-th row from its group's phase, two rows per step; the grid values
         // of the next step are loaded before this step's arithmetic
         const int JJ = xin ? (int)cg.jx[kk * cg.NX + (cx <= 0 ? -cx : cx - 1)] : -1;
-        const int jlo = -JJ, jhi = JJ + 1, G = cg.G;
-        int j = js + cg.grp;
+        const int jlo = -JJ, jhi = JJ + 1, G = nph;
+        int j = js + phase;
         if (j < jlo)
           j += ((jlo - j + G - 1) / G) * G;
         const size_t base = zoff + ig;
@@ -623,7 +644,7 @@ __global__ void __launch_bounds__(128, LPB <= 4 ? 5 : 1) integrate_ortho(GridArg
           acc[e] += M::to_double(s);
         }
         __syncwarp();
-        if (xc + cg.SW <= cg.x_hi) { // another x-chunk follows: rebuild the tables
+        if (xc + xstep <= cg.x_hi) { // another x-chunk follows: rebuild the tables
           fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane, a.seeds + (size_t)t * 18);
           __syncwarp();
         }

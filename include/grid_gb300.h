@@ -270,7 +270,7 @@ void grid_gb300_set_schedule(const grid_gb300_task_list *task_list,
  * polynomial maxima, for density-matrix elements of magnitude <= 1) is at
  * most `threshold` run in plain FP32, the others in double-float
  * (orthorhombic kernels) or FP64 (general kernels).  0 runs no task in plain
- * FP32.  Default 1. */
+ * FP32.  Default 0.3. */
 void grid_gb300_set_mixed_threshold(const grid_gb300_task_list *task_list,
                                     double threshold);
 /* Share of the tasks (and of their grid points) that the mixed path

@@ -97,7 +97,7 @@ def test_tasklist_fp64(G, O, name, scale, funcs, tol):
 # measured on seeded inputs (uniform [-1, 1] density-matrix blocks and
 # potential), max |d| / max(1, |ref|) unless noted:
 #   MIXED, default split (tasks with contribution bound <= 1 in FP32, the rest
-#       in double-float):                  rho, hab <= 1e-6, forces <= 1e-6
+#       in double-float):                  rho, hab <= 1e-6, forces <= 1e-5
 #   MIXED, threshold 0 (all double-float): rho, hab <= 1e-9, forces <= 1e-7
 #   FP32 (plain FP32 per-point work):      max |d| / max |ref| <= 2e-6
 @pytest.mark.parametrize("name,scale", [("c1_64atoms", 0.3), ("c2_512atoms", 0.08),
@@ -112,7 +112,7 @@ def test_reduced_precision_bounds(G, O, name, scale):
     h_ref, f_ref, _ = ot.integrate(V, pab, forces=True)
     gmax = max(float(np.abs(g).max()) for g in g_ref)
     hmax = float(np.abs(h_ref).max())
-    for prec, tau, tol_rel, tol_f, tol_max in ((G.MIXED, None, 1e-6, 1e-6, None),
+    for prec, tau, tol_rel, tol_f, tol_max in ((G.MIXED, None, 1e-6, 1e-5, None),
                                                 (G.MIXED, 0.0, 1e-9, 1e-7, None),
                                                 (G.FP32, None, None, None, 2e-6)):
         tl = G.GridTaskList(inp, precision=prec)
