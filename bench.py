@@ -258,9 +258,10 @@ def measure_fp32_peak(torch):
 # beside each figure (dram__bytes_read.sum + dram__bytes_write.sum); the
 # bench cannot run ncu itself.  Keys: kernel label as in "roofline.kernel".
 NCU_TRAFFIC = {
-    # profiles/grid_kernels_c2_512atoms_mixed.md (2 launches each, mean)
-    "collocate_ortho<dfloat,4>": 0.5 * ((57.029 + 32.069) + (407.416 + 1458.588)) * 1e6,
-    "integrate_ortho<dfloat,4>": 0.5 * ((39.392 + 0.917) + (322.533 + 42.050)) * 1e6,
+    # profiles/grid_kernels_c2_512atoms_mixed.md (2 launches each, mean);
+    # the double-float collocation runs the point-list kernel
+    "collocate_ortho<dfloat,4>": 0.5 * ((55.521 + 17.446) + (296.367 + 888.955)) * 1e6,
+    "integrate_ortho<dfloat,4>": 0.5 * ((37.712 + 1.315) + (244.637 + 67.789)) * 1e6,
 }
 
 
