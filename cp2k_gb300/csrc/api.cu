@@ -295,6 +295,7 @@ struct TaskList {
   std::vector<int> sph_pts, sph_ploff; // point lists of the spheres
   std::vector<long long> points; // per task (block order)
   std::vector<float> model_cost; // per task, empty unless a model was applied
+  double model_bin = 0.2;        // width of the log-time bins of the model schedule
   std::vector<float> features;   // per task [6]: cost-model inputs (block order)
   bool task_timing = false;      // record clock64 cycles per task
   bool launch_timing = false;    // record CUDA events around every grid launch
@@ -988,9 +989,14 @@ static Mode &get_mode(TaskList *t, const LDiffs &d) {
     double cost;
     if (t->schedule == GRID_GB300_SCHEDULE_INPUT)
       cost = -(double)k.orig;
-    else if (t->schedule == GRID_GB300_SCHEDULE_MODEL && !t->model_cost.empty())
-      cost = t->model_cost[s];
-    else
+    else if (t->schedule == GRID_GB300_SCHEDULE_MODEL && !t->model_cost.empty()) {
+      // predicted log time, quantised into bins; inside a bin the size order
+      // keeps tasks of one sphere together (their point lists stay in cache)
+      const double size = (double)t->points[s] * (lp + 1) + 64.0 * (lp + 1) * (lp + 2);
+      const double bin = t->model_bin > 0.0 ? floor(t->model_cost[s] / t->model_bin)
+                                            : (double)t->model_cost[s];
+      cost = t->model_bin > 0.0 ? bin + size / (size + 1.0e12) : bin;
+    } else
       cost = (double)t->points[s] * (lp + 1) + 64.0 * (lp + 1) * (lp + 2);
     items[((g * kNumBuckets + b) * 2 + cls) * 2 + sz].push_back({cost, s});
   }
@@ -1161,7 +1167,19 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
   CoefArgs co{t->d_tasks, t->d_subs, m.d_coef_off, t->d_atom_pos, t->d_pab_cart, t->d_coef,
               t->ntasks, func, d, t->d_levels, arith == ARITH_MIXED ? 1 : 0, t->d_dhtab,
               arith == ARITH_MIXED ? m.d_fp32 : nullptr};
-  launch_coefficients(co, arith, m.coef_words, s);
+  if (arith == ARITH_MIXED) {
+    // one launch per work queue, each in the working type of its class: the
+    // kernels stay small (instruction cache) and need no per-task branch
+    for (const Queue &q : m.queues) {
+      co.order = q.d_idx;
+      co.norder = q.n;
+      launch_coefficients_mixed(co, q.general ? (int)ARITH_FP64 : q.fp32 ? (int)ARITH_FP32
+                                                                          : (int)ARITH_MIXED,
+                                m.coef_words, s);
+    }
+  } else {
+    launch_coefficients(co, arith, m.coef_words, s);
+  }
   record_phase(t, 1, s);
   for (int l = 0; l < t->nlevels; l++) {
     const int *n = &t->npts_local[3 * l];
@@ -1283,7 +1301,17 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
               need_pab ? t->d_pab_cart : nullptr, t->d_hab_cart, t->d_atom_pos, forces, virial,
               t->ntasks, tau ? 1 : 0, d, t->d_levels, t->d_dhtab,
               arith == ARITH_MIXED ? m.d_fp32 : nullptr};
-  launch_post(pa, arith, m.coef_words, s);
+  if (arith == ARITH_MIXED) {
+    for (const Queue &q : m.queues) {
+      pa.order = q.d_idx;
+      pa.norder = q.n;
+      launch_post_mixed(pa, q.general ? (int)ARITH_FP64 : q.fp32 ? (int)ARITH_FP32
+                                                                  : (int)ARITH_MIXED,
+                        m.coef_words, s);
+    }
+  } else {
+    launch_post(pa, arith, m.coef_words, s);
+  }
   CK(cudaMemsetAsync(hab, 0, sizeof(double) * (size_t)t->buffer_len, s));
   ContractArgs cb{t->d_subs, (int)t->subs.size(), t->d_sphi, nullptr, hab, t->d_hab_cart,
                   t->contract_words};
@@ -1841,6 +1869,15 @@ GB300_API void grid_gb300_set_collocate_variant(const grid_gb300_task_list *task
   t->coll_variant = variant;
   t->tuned.clear();
   t->gen++;
+}
+
+GB300_API void grid_gb300_set_model_bin_width(const grid_gb300_task_list *task_list,
+                                              double width) {
+  if (!(width >= 0.0))
+    fail("model bin width must be >= 0");
+  TaskList *t = TL(task_list);
+  t->model_bin = width;
+  t->sched_version++;
 }
 
 GB300_API int grid_gb300_tuned_split(const grid_gb300_task_list *task_list) {

@@ -390,16 +390,19 @@ __global__ void __launch_bounds__(128) coefficients_kernel(CoefArgs a, int words
   const int gid = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * ng + half;
   const int ngroups = ((gridDim.x * blockDim.x) >> 5) * ng;
   double *ws = (double *)smem + (size_t)((threadIdx.x >> 5) * ng + half) * words_per_group;
-  for (int t = gid; t < a.ntasks; t += ngroups) {
+  const int nt = a.order ? a.norder : a.ntasks;
+  for (int i = gid; i < nt; i += ngroups) {
+    const int t = a.order ? a.order[i] : i;
     const TaskDesc d = a.tasks[t];
     if (d.flags & TF_SKIP)
       continue;
+    const bool fp64_out = (d.flags & TF_GENERAL) && a.general_fp64;
     if (std::is_same<U, dfloat>::value && (d.flags & TF_GENERAL))
-      coef_task<double, Tout>(a, t, d, ws, g, a.general_fp64);
+      coef_task<double, Tout>(a, t, d, ws, g, fp64_out);
     else if (std::is_same<U, dfloat>::value && a.task_fp32 && a.task_fp32[t])
       coef_task<float, Tout>(a, t, d, ws, g, false); // FP32 task of the mixed mode
     else
-      coef_task<U, Tout>(a, t, d, ws, g, false);
+      coef_task<U, Tout>(a, t, d, ws, g, fp64_out);
   }
 }
 
@@ -532,7 +535,9 @@ __global__ void __launch_bounds__(128) post_kernel(PostArgs a, int words_per_gro
   if (threadIdx.x < 9)
     vir_cta[threadIdx.x] = 0.0;
   __syncthreads();
-  for (int t = gid; t < a.ntasks; t += ngroups) {
+  const int nt = a.order ? a.norder : a.ntasks;
+  for (int i = gid; i < nt; i += ngroups) {
+    const int t = a.order ? a.order[i] : i;
     const TaskDesc d = a.tasks[t];
     if (d.flags & TF_SKIP)
       continue;
@@ -718,8 +723,21 @@ static void launch_coef_t(const CoefArgs &a, int words_per_group, cudaStream_t s
   const size_t smem = nw * per_warp;
   auto k = coefficients_kernel<U, Tout>;
   set_smem((const void *)k, smem);
-  k<<<grid_size_for(a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_group, gsize);
+  k<<<grid_size_for(a.order ? a.norder : a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_group,
+                                                                            gsize);
   count_launch();
+}
+
+void launch_coefficients_mixed(const CoefArgs &a, int work, int words_per_warp, cudaStream_t s) {
+  if ((a.order ? a.norder : a.ntasks) == 0)
+    return;
+  upload_binomials();
+  if (work == ARITH_FP32)
+    launch_coef_t<float, dfloat>(a, words_per_warp, s);
+  else if (work == ARITH_FP64)
+    launch_coef_t<double, dfloat>(a, words_per_warp, s);
+  else
+    launch_coef_t<dfloat, dfloat>(a, words_per_warp, s);
 }
 
 void launch_coefficients(const CoefArgs &a, int arith, int words_per_warp, cudaStream_t s) {
@@ -744,8 +762,21 @@ static void launch_post_t(const PostArgs &a, int words_per_group, cudaStream_t s
   const size_t smem = nw * per_warp;
   auto k = post_kernel<U>;
   set_smem((const void *)k, smem);
-  k<<<grid_size_for(a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_group, gsize);
+  k<<<grid_size_for(a.order ? a.norder : a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_group,
+                                                                            gsize);
   count_launch();
+}
+
+void launch_post_mixed(const PostArgs &a, int work, int words_per_warp, cudaStream_t s) {
+  if ((a.order ? a.norder : a.ntasks) == 0)
+    return;
+  upload_binomials();
+  if (work == ARITH_FP32)
+    launch_post_t<float>(a, words_per_warp, s);
+  else if (work == ARITH_FP64)
+    launch_post_t<double>(a, words_per_warp, s);
+  else
+    launch_post_t<dfloat>(a, words_per_warp, s);
 }
 
 void launch_post(const PostArgs &a, int arith, int words_per_warp, cudaStream_t s) {

@@ -155,6 +155,8 @@ struct CoefArgs {
   int general_fp64;       // write general-path coefficients as FP64
   const double *dhtab;    // factorials and step-vector powers (build_dh_table)
   const uint8_t *task_fp32; // mixed mode: 1 for tasks of the FP32 class (or null)
+  const int *order;         // if set, only these tasks (norder of them)
+  int norder;
 };
 
 struct GridArgs {
@@ -198,6 +200,8 @@ struct PostArgs {
   const LevelSet *levels;
   const double *dhtab; // factorials and step-vector powers (build_dh_table)
   const uint8_t *task_fp32; // mixed mode: 1 for tasks of the FP32 class (or null)
+  const int *order;         // if set, only these tasks (norder of them)
+  int norder;
 };
 
 struct ContractArgs {
@@ -213,6 +217,12 @@ size_t coef_words(int la, int lb);
 
 void launch_decontract(const ContractArgs &a, cudaStream_t s);
 void launch_contract_hab(const ContractArgs &a, cudaStream_t s);
+// mixed mode, one work queue at a time: the queue's tasks (a.order) in the
+// working type of their class, `work` = ARITH_FP32 (float), ARITH_MIXED
+// (double-float) or ARITH_FP64 (general-path tasks); coefficients are stored
+// as double-float pairs, general-path ones in FP64
+void launch_coefficients_mixed(const CoefArgs &a, int work, int max_smem_words, cudaStream_t s);
+void launch_post_mixed(const PostArgs &a, int work, int max_smem_words, cudaStream_t s);
 void launch_coefficients(const CoefArgs &a, int arith, int max_smem_words,
                          cudaStream_t s);
 // `extent` is the largest cube width (2*cmax+2) of the queue for the

@@ -108,6 +108,7 @@ def lib():
         L.grid_gb300_autotune.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp]
         L.grid_gb300_autotune.restype = C.c_double
         L.grid_gb300_set_collocate_variant.argtypes = [vp, C.c_int]
+        L.grid_gb300_set_model_bin_width.argtypes = [vp, C.c_double]
         L.grid_gb300_tuned_split.argtypes = [vp]
         L.grid_gb300_tuned_split.restype = C.c_int
         L.grid_gb300_set_launch_timing.argtypes = [vp, C.c_int]
@@ -377,6 +378,9 @@ class GridTaskList:
         """0: row walk, 1: point list, -1: by arithmetic
         (grid_gb300_set_collocate_variant)."""
         lib().grid_gb300_set_collocate_variant(self.impl, int(variant))
+
+    def set_model_bin_width(self, width: float):
+        lib().grid_gb300_set_model_bin_width(self.impl, float(width))
 
     def tuned_split(self) -> int:
         return int(lib().grid_gb300_tuned_split(self.impl))

@@ -421,6 +421,12 @@ void grid_gb300_cost_model_adam(float *params, const float *grad, float *m,
  * norm = {mean[6], scale[6]} (NULL: none). */
 void grid_gb300_cost_model_predict(const float *params, const float *x, int n,
                                    const float *norm, float *y, void *stream);
+/* GRID_GB300_SCHEDULE_MODEL orders each queue by the predicted log time
+ * quantised into bins of this width (default 0.2), and by the analytic size
+ * inside a bin, which keeps tasks of one sphere together; 0 orders by the raw
+ * prediction. */
+void grid_gb300_set_model_bin_width(const grid_gb300_task_list *task_list,
+                                    double width);
 /* Predicts the cost of every task of the list with the given parameters
  * and normalisation (device pointers) and uses it for
  * GRID_GB300_SCHEDULE_MODEL.  Synchronises `stream`. */
