@@ -276,7 +276,6 @@ struct Mode { // everything that depends on the l shifts of a call
   std::vector<Queue> queues; // launch order
   int coef_words = 0;      // per-warp shared memory words of coefficient/post
   int sched_version = -1;
-  uint8_t *d_fp32 = nullptr; // per task: 1 if the mixed mode runs it in plain FP32
 };
 
 struct TaskList {
@@ -320,6 +319,8 @@ struct TaskList {
   int16_t *d_sph_tab = nullptr;
   int *d_sph_pts = nullptr, *d_sph_ploff = nullptr;
   double *d_dhtab = nullptr;
+  float *d_dhtab_f = nullptr;
+  float2 *d_dhtab_df = nullptr;
   double *d_atom_pos = nullptr;
   double *d_sphi = nullptr;
   LevelSet *d_levels = nullptr;
@@ -500,12 +501,23 @@ void build_dh_table(const LevelSet &ls, std::vector<double> &tab) {
     tab[kPowN + n] = 1.0 / f;
   }
   for (int l = 0; l < ls.nlevels; l++)
-    for (int c = 0; c < 9; c++) {
-      double p = 1.0;
-      for (int n = 0; n < kPowN; n++) {
-        tab[2 * kPowN + ((size_t)l * 9 + c) * kPowN + n] = p;
-        p *= ls.lv[l].dh[c];
+    for (int c = 0; c < 3; c++) {
+      double pw[3][kPowN];
+      for (int d = 0; d < 3; d++) {
+        double p = 1.0;
+        for (int n = 0; n < kPowN; n++) {
+          pw[d][n] = p;
+          p *= ls.lv[l].dh[3 * d + c];
+        }
       }
+      double *W = &tab[2 * kPowN + ((size_t)l * 3 + c) * kNW];
+      for (int n = 0; n <= GB300_LP_MAX; n++)
+        for (int i = 0; i <= n; i++)
+          for (int j = 0; j <= n - i; j++) {
+            const int k = n - i - j;
+            W[coset(i, j, k)] = pw[0][i] * pw[1][j] * pw[2][k] *
+                                (tab[kPowN + i] * tab[kPowN + j] * tab[kPowN + k]);
+          }
     }
 }
 
@@ -588,7 +600,8 @@ template <typename T> static T *dalloc_copy(const std::vector<T> &v) {
 
 static void free_device(TaskList *t) {
   void *ptrs[] = {t->d_seeds, t->d_tasks, t->d_subs, t->d_sph, t->d_sph_tab, t->d_sph_pts,
-                  t->d_sph_ploff, t->d_dhtab, t->d_atom_pos, t->d_sphi,
+                  t->d_sph_ploff, t->d_dhtab, t->d_dhtab_f, t->d_dhtab_df, t->d_atom_pos,
+                  t->d_sphi,
                   t->d_levels, t->d_pab_cart, t->d_hab_cart, t->d_coef, t->d_coef_int,
                   t->d_forces, t->d_virial, t->d_counters, t->d_error, t->d_cycles};
   for (void *p : ptrs)
@@ -603,8 +616,6 @@ static void free_device(TaskList *t) {
   for (auto &kv : t->modes) {
     if (kv.second.d_coef_off)
       cudaFree(kv.second.d_coef_off);
-    if (kv.second.d_fp32)
-      cudaFree(kv.second.d_fp32);
     for (auto &q : kv.second.queues)
       if (q.d_idx)
         cudaFree(q.d_idx);
@@ -920,6 +931,14 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
     std::vector<double> dt;
     build_dh_table(t->levels, dt);
     t->d_dhtab = dalloc_copy(dt);
+    std::vector<float> df(dt.size());
+    std::vector<float2> dd(dt.size());
+    for (size_t k = 0; k < dt.size(); k++) {
+      df[k] = (float)dt[k];
+      dd[k] = make_float2(df[k], (float)(dt[k] - (double)df[k]));
+    }
+    t->d_dhtab_f = dalloc_copy(df);
+    t->d_dhtab_df = dalloc_copy(dd);
   }
   t->d_sph_ploff = dalloc_copy(t->sph_ploff);
   t->d_atom_pos = dalloc_copy(std::vector<double>(atom_positions, atom_positions + 3 * natoms));
@@ -971,7 +990,6 @@ static Mode &get_mode(TaskList *t, const LDiffs &d) {
   // work queues, descending cost
   // work queues: (general, lp bucket, FP32 class, size class), descending cost
   std::map<int, std::vector<std::pair<double, int>>> items;
-  std::vector<uint8_t> fp32(std::max(t->ntasks, 1), 0);
   for (int s = 0; s < t->ntasks; s++) {
     const TaskDesc &k = t->tasks[s];
     if (k.flags & TF_SKIP)
@@ -983,7 +1001,6 @@ static Mode &get_mode(TaskList *t, const LDiffs &d) {
     const int g = (k.flags & TF_GENERAL) ? 1 : 0;
     const int cls = (t->precision == GRID_GB300_MIXED && t->gbound[s] <= t->mixed_threshold)
                         ? 1 : 0;
-    fp32[s] = (uint8_t)cls;
     const int ext = g == 0 ? 2 * t->sph[k.sphere].cmax + 2 : k.imax[1] - k.center[1] + 1;
     const int sz = ext <= t->small_extent[t->precision] ? 0 : 1;
     double cost;
@@ -1045,9 +1062,6 @@ static Mode &get_mode(TaskList *t, const LDiffs &d) {
     q.d_idx = dalloc_copy(idx);
     m.queues.push_back(q);
   }
-  if (m.d_fp32)
-    cudaFree(m.d_fp32);
-  m.d_fp32 = dalloc_copy(fp32);
   m.sched_version = t->sched_version;
   t->gen++;
   return m;
@@ -1164,18 +1178,28 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
   ContractArgs ca{t->d_subs, (int)t->subs.size(), t->d_sphi, pab, nullptr, t->d_pab_cart,
                   t->contract_words};
   launch_decontract(ca, s);
-  CoefArgs co{t->d_tasks, t->d_subs, m.d_coef_off, t->d_atom_pos, t->d_pab_cart, t->d_coef,
-              t->ntasks, func, d, t->d_levels, arith == ARITH_MIXED ? 1 : 0, t->d_dhtab,
-              arith == ARITH_MIXED ? m.d_fp32 : nullptr};
+  CoefArgs co{};
+  co.tasks = t->d_tasks;
+  co.subs = t->d_subs;
+  co.coef_off = m.d_coef_off;
+  co.atom_pos = t->d_atom_pos;
+  co.pab_cart = t->d_pab_cart;
+  co.coef = t->d_coef;
+  co.ntasks = t->ntasks;
+  co.func = func;
+  co.d = d;
+  co.levels = t->d_levels;
+  co.general_fp64 = arith == ARITH_MIXED ? 1 : 0;
+  co.dhtab = t->d_dhtab;
+  co.dhtab_f = t->d_dhtab_f;
+  co.dhtab_df = t->d_dhtab_df;
   if (arith == ARITH_MIXED) {
     // one launch per work queue, each in the working type of its class: the
     // kernels stay small (instruction cache) and need no per-task branch
     for (const Queue &q : m.queues) {
       co.order = q.d_idx;
       co.norder = q.n;
-      launch_coefficients_mixed(co, q.general ? (int)ARITH_FP64 : q.fp32 ? (int)ARITH_FP32
-                                                                          : (int)ARITH_MIXED,
-                                m.coef_words, s);
+      launch_coefficients_mixed(co, q.fp32 ? (int)ARITH_FP32 : (int)ARITH_MIXED, m.coef_words, s);
     }
   } else {
     launch_coefficients(co, arith, m.coef_words, s);
@@ -1299,15 +1323,13 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
     CK(cudaMemsetAsync(virial, 0, sizeof(double) * 9, s));
   PostArgs pa{t->d_tasks, t->d_subs, m.d_coef_off, t->d_coef_int,
               need_pab ? t->d_pab_cart : nullptr, t->d_hab_cart, t->d_atom_pos, forces, virial,
-              t->ntasks, tau ? 1 : 0, d, t->d_levels, t->d_dhtab,
-              arith == ARITH_MIXED ? m.d_fp32 : nullptr};
+              t->ntasks, tau ? 1 : 0, d, t->d_levels, t->d_dhtab, t->d_dhtab_f, t->d_dhtab_df,
+              nullptr, 0};
   if (arith == ARITH_MIXED) {
     for (const Queue &q : m.queues) {
       pa.order = q.d_idx;
       pa.norder = q.n;
-      launch_post_mixed(pa, q.general ? (int)ARITH_FP64 : q.fp32 ? (int)ARITH_FP32
-                                                                  : (int)ARITH_MIXED,
-                        m.coef_words, s);
+      launch_post_mixed(pa, q.fp32 ? (int)ARITH_FP32 : (int)ARITH_MIXED, m.coef_words, s);
     }
   } else {
     launch_post(pa, arith, m.coef_words, s);

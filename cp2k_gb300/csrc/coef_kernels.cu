@@ -238,45 +238,84 @@ __device__ T cxyz_cab_term(const T *cxyz, const T *alpha, int la, int lb, int lp
   return s;
 }
 
-// C_xyz term (lx, ly, lz) <-> C_ijk through x_c = sum_d u_d dh[d][c]
-// (grid_ref_collint.h:698-762): the multinomial expansion of
-// x^lx y^ly z^lz in the lattice coordinates, with the powers of the step
-// vectors and the (inverse) factorials taken from a table (`tab`: n!, 1/n!,
-// then this level's dh[c]^n) so that the innermost loop has no division and
-// no power or factorial loop.  forward: scatter cxyz[e] into cijk (smem
-// atomics); adjoint: gather cijk into the returned value.
+// General path: C_xyz (Cartesian, about P) <-> C_ijk (lattice indices)
+// through x_c = sum_d u_d dh[d][c] (grid_ref_collint.h:698-762).  x^lx y^ly
+// z^lz expands into the product of three multinomials; with the weights
+// W_c(i, j, k) = dh[0][c]^i dh[1][c]^j dh[2][c]^k / (i! j! k!) from a table
+// (build_dh_table) the monomial (lx, ly, lz) maps onto the lattice monomial
+// (i, j, k) = sum over the directions' splits with weight
+// lx! ly! lz! W_x W_y W_z.  Both directions are written as gathers (one
+// output per lane, no atomics) in the arithmetic type T of the kernel, with
+// the table in that type.
+template <typename T> __device__ __forceinline__ const T *dh_tab(const double *d, const float *f,
+                                                                 const float2 *df);
+template <> __device__ __forceinline__ const double *dh_tab<double>(const double *d, const float *,
+                                                                    const float2 *) {
+  return d;
+}
+template <> __device__ __forceinline__ const float *dh_tab<float>(const double *, const float *f,
+                                                                  const float2 *) {
+  return f;
+}
+template <> __device__ __forceinline__ const dfloat *dh_tab<dfloat>(const double *, const float *,
+                                                                    const float2 *df) {
+  return reinterpret_cast<const dfloat *>(df);
+}
+
+// adjoint: C_xyz[lx, ly, lz] from C_ijk
 template <typename T>
-__device__ T cxyz_cijk_term(bool forward, const double *tab, int level, int lp, int lx, int ly,
-                            int lz, T cval, T *cijk_scatter, const T *cijk_gather) {
-  const double *F = tab, *IF = tab + kPowN;
-  const double *pw = tab + 2 * kPowN + (size_t)level * 9 * kPowN;
-  const double fl = F[lx] * F[ly] * F[lz];
-  const double cv = forward ? to_double(cval) * fl : fl;
-  double acc = 0.0;
+__device__ T cxyz_from_cijk(const T *tab, int level, int lp, int lx, int ly, int lz,
+                            const T *cijk) {
+  using M = Num<T>;
+  const T *F = tab;
+  const T *Wx = tab + 2 * kPowN + (size_t)level * 3 * kNW, *Wy = Wx + kNW, *Wz = Wy + kNW;
+  T acc = M::zero();
   for (int ix = 0; ix <= lx; ix++)
     for (int jx = 0; jx <= lx - ix; jx++) {
       const int kx = lx - ix - jx;
-      const double wx = pw[0 * kPowN + ix] * pw[3 * kPowN + jx] * pw[6 * kPowN + kx] *
-                        (IF[ix] * IF[jx] * IF[kx]) * cv;
+      const T wx = Wx[coset(ix, jx, kx)];
       for (int iy = 0; iy <= ly; iy++)
         for (int jy = 0; jy <= ly - iy; jy++) {
           const int ky = ly - iy - jy;
-          const double wxy = wx * pw[1 * kPowN + iy] * pw[4 * kPowN + jy] * pw[7 * kPowN + ky] *
-                             (IF[iy] * IF[jy] * IF[ky]);
+          const T wxy = M::mul(wx, Wy[coset(iy, jy, ky)]);
+          T sz = M::zero();
           for (int iz = 0; iz <= lz; iz++)
             for (int jz = 0; jz <= lz - iz; jz++) {
               const int kz = lz - iz - jz;
-              const int e = cidx(kx + ky + kz, jx + jy + jz, ix + iy + iz, lp);
-              const double wgt = wxy * pw[2 * kPowN + iz] * pw[5 * kPowN + jz] *
-                                 pw[8 * kPowN + kz] * (IF[iz] * IF[jz] * IF[kz]);
-              if (forward)
-                atomicAdd(&cijk_scatter[e], T(wgt));
-              else
-                acc += wgt * to_double(cijk_gather[e]);
+              sz = M::fma_acc(sz, Wz[coset(iz, jz, kz)],
+                              cijk[cidx(kx + ky + kz, jx + jy + jz, ix + iy + iz, lp)]);
             }
+          acc = M::fma_acc(acc, wxy, M::norm(sz));
         }
     }
-  return T(acc);
+  return M::mul(M::norm(acc), M::mul(M::mul(F[lx], F[ly]), F[lz]));
+}
+
+// forward: C_ijk[iu, ju, ku] (lattice exponents of directions 0, 1, 2) from
+// g[e] = lx! ly! lz! C_xyz[e]
+template <typename T>
+__device__ T cijk_from_cxyz(const T *tab, int level, int lp, int iu, int ju, int ku,
+                            const T *g) {
+  using M = Num<T>;
+  const T *Wx = tab + 2 * kPowN + (size_t)level * 3 * kNW, *Wy = Wx + kNW, *Wz = Wy + kNW;
+  T acc = M::zero();
+  for (int ix = 0; ix <= iu; ix++)
+    for (int jx = 0; jx <= ju; jx++)
+      for (int kx = 0; kx <= ku; kx++) {
+        const T wx = Wx[coset(ix, jx, kx)];
+        for (int iy = 0; iy <= iu - ix; iy++)
+          for (int jy = 0; jy <= ju - jx; jy++) {
+            T s = M::zero();
+            for (int ky = 0; ky <= ku - kx; ky++) {
+              const int iz = iu - ix - iy, jz = ju - jx - jy, kz = ku - kx - ky;
+              const T w = M::mul(Wy[coset(iy, jy, ky)], Wz[coset(iz, jz, kz)]);
+              s = M::fma_acc(s, w,
+                             g[cidx(iz + jz + kz, iy + jy + ky, ix + jx + kx, lp)]);
+            }
+            acc = M::fma_acc(acc, wx, M::norm(s));
+          }
+      }
+  return M::norm(acc);
 }
 
 // Per-warp shared memory of the coefficient / post kernels in 8-byte words:
@@ -363,23 +402,28 @@ __device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *w
       store_coef<Tout, U>(a.coef, (size_t)a.coef_off[t] + e, v, false);
     }
   }
-  if constexpr (!std::is_same<U, dfloat>::value) {
-    if (general) {
-      g.sync();
-      for (int e = g.lane; e < nco; e += g.n) {
-        int lz, ly, lx;
-        decode_cidx(e, lp, lz, ly, lx);
-        cxyz_cijk_term<U>(true, a.dhtab, d.level, lp, lx, ly, lz, cxyz[e], cijk, nullptr);
-      }
-      g.sync();
-      for (int e = g.lane; e < nco; e += g.n)
-        store_coef<Tout, U>(a.coef, (size_t)a.coef_off[t] + e, cijk[e], as_fp64);
+  if (general) {
+    using M = Num<U>;
+    const U *tab = dh_tab<U>(a.dhtab, a.dhtab_f, a.dhtab_df);
+    g.sync();
+    for (int e = g.lane; e < nco; e += g.n) { // g = lx! ly! lz! C_xyz, in place
+      int lz, ly, lx;
+      decode_cidx(e, lp, lz, ly, lx);
+      cxyz[e] = M::mul(cxyz[e], M::mul(M::mul(tab[lx], tab[ly]), tab[lz]));
+    }
+    g.sync();
+    for (int e = g.lane; e < nco; e += g.n) {
+      int ku, ju, iu;
+      decode_cidx(e, lp, ku, ju, iu);
+      store_coef<Tout, U>(a.coef, (size_t)a.coef_off[t] + e,
+                          cijk_from_cxyz<U>(tab, d.level, lp, iu, ju, ku, cxyz), as_fp64);
     }
   }
   g.sync();
 }
 
-// U: working type of ortho tasks; general tasks run in FP64 when U is dfloat
+// U: working type of the tasks (the mixed mode launches one kernel per work
+// queue, each in the type of its class)
 template <typename U, typename Tout>
 __global__ void __launch_bounds__(128) coefficients_kernel(CoefArgs a, int words_per_group,
                                                            int gsize) {
@@ -396,13 +440,8 @@ __global__ void __launch_bounds__(128) coefficients_kernel(CoefArgs a, int words
     const TaskDesc d = a.tasks[t];
     if (d.flags & TF_SKIP)
       continue;
-    const bool fp64_out = (d.flags & TF_GENERAL) && a.general_fp64;
-    if (std::is_same<U, dfloat>::value && (d.flags & TF_GENERAL))
-      coef_task<double, Tout>(a, t, d, ws, g, fp64_out);
-    else if (std::is_same<U, dfloat>::value && a.task_fp32 && a.task_fp32[t])
-      coef_task<float, Tout>(a, t, d, ws, g, false); // FP32 task of the mixed mode
-    else
-      coef_task<U, Tout>(a, t, d, ws, g, fp64_out);
+    // general-path coefficients of the mixed mode are stored in FP64
+    coef_task<U, Tout>(a, t, d, ws, g, (d.flags & TF_GENERAL) && a.general_fp64);
   }
 }
 
@@ -473,15 +512,14 @@ __device__ void post_task(const PostArgs &a, int t, const TaskDesc &d, double *w
       cxyz[e] = U(src[e]);
   }
   g.sync();
-  if constexpr (!std::is_same<U, dfloat>::value) {
-    if (general) {
-      for (int e = g.lane; e < nco; e += g.n) {
-        int lz, ly, lx;
-        decode_cidx(e, lp, lz, ly, lx);
-        cxyz[e] = cxyz_cijk_term<U>(false, a.dhtab, d.level, lp, lx, ly, lz, U(0), nullptr, cijk);
-      }
-      g.sync();
+  if (general) {
+    const U *tab = dh_tab<U>(a.dhtab, a.dhtab_f, a.dhtab_df);
+    for (int e = g.lane; e < nco; e += g.n) {
+      int lz, ly, lx;
+      decode_cidx(e, lp, lz, ly, lx);
+      cxyz[e] = cxyz_from_cijk<U>(tab, d.level, lp, lx, ly, lz, cijk);
     }
+    g.sync();
   }
   const double *ra = a.atom_pos + 3 * d.iatom;
   double rb[3];
@@ -542,12 +580,7 @@ __global__ void __launch_bounds__(128) post_kernel(PostArgs a, int words_per_gro
     if (d.flags & TF_SKIP)
       continue;
     double f[6] = {0, 0, 0, 0, 0, 0}, v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    if (std::is_same<U, dfloat>::value && (d.flags & TF_GENERAL))
-      post_task<double>(a, t, d, ws, g, f, v);
-    else if (std::is_same<U, dfloat>::value && a.task_fp32 && a.task_fp32[t])
-      post_task<float>(a, t, d, ws, g, f, v); // FP32 task of the mixed mode
-    else
-      post_task<U>(a, t, d, ws, g, f, v);
+    post_task<U>(a, t, d, ws, g, f, v);
     const double scale = (d.iatom == d.jatom) ? 1.0 : 2.0;
     // sums over the group's lanes (xor offsets below the group size stay inside it)
     if (a.forces) {

@@ -153,9 +153,10 @@ struct CoefArgs {
   LDiffs d;
   const LevelSet *levels; // device copy
   int general_fp64;       // write general-path coefficients as FP64
-  const double *dhtab;    // factorials and step-vector powers (build_dh_table)
-  const uint8_t *task_fp32; // mixed mode: 1 for tasks of the FP32 class (or null)
-  const int *order;         // if set, only these tasks (norder of them)
+  const double *dhtab;     // general-path transform table (build_dh_table), FP64
+  const float *dhtab_f;    // the same in FP32 (FP32 kernels)
+  const float2 *dhtab_df;  // the same as double-float pairs (mixed kernels)
+  const int *order;        // if set, only these tasks (norder of them)
   int norder;
 };
 
@@ -198,9 +199,10 @@ struct PostArgs {
   int compute_tau;
   LDiffs d;
   const LevelSet *levels;
-  const double *dhtab; // factorials and step-vector powers (build_dh_table)
-  const uint8_t *task_fp32; // mixed mode: 1 for tasks of the FP32 class (or null)
-  const int *order;         // if set, only these tasks (norder of them)
+  const double *dhtab;     // general-path transform table (build_dh_table), FP64
+  const float *dhtab_f;    // the same in FP32
+  const float2 *dhtab_df;  // the same as double-float pairs
+  const int *order;        // if set, only these tasks (norder of them)
   int norder;
 };
 
@@ -303,7 +305,11 @@ void build_sphere_points(SphereHdr &h, const std::vector<int16_t> &tab, std::vec
 // Table for the general path's C_xyz <-> C_ijk transform: n! and 1/n! for
 // n < kPowN, then per level the powers dh[c]^n (c = 0..8 row-major, n < kPowN)
 constexpr int kPowN = GB300_LP_MAX + 1;
-inline size_t dh_table_size(int nlevels) { return 2 * kPowN + (size_t)nlevels * 9 * kPowN; }
+constexpr int kNW = (GB300_LP_MAX + 1) * (GB300_LP_MAX + 2) * (GB300_LP_MAX + 3) / 6;
+// n!, 1/n! (kPowN each), then per level and Cartesian direction c the
+// multinomial weights W_c(i, j, k) = dh[0][c]^i dh[1][c]^j dh[2][c]^k / (i! j! k!)
+// at coset(i, j, k), i + j + k <= GB300_LP_MAX
+inline size_t dh_table_size(int nlevels) { return 2 * kPowN + (size_t)nlevels * 3 * kNW; }
 void build_dh_table(const LevelSet &ls, std::vector<double> &tab);
 
 // counts launches for grid_gb300_kernel_launches()
