@@ -203,8 +203,10 @@ class GridTaskList:
     ``api="cp2k"`` goes through grid_create_task_list & co. (the CP2K surface),
     ``api="backend"`` through grid_gb300_* (what CP2K's dispatcher binds)."""
 
-    def __init__(self, inp: TaskListInputs, precision: int = FP64,
-                 schedule: int = SCHEDULE_SIZE, api: str = "backend"):
+    def __init__(self, inp: TaskListInputs, precision: int | None = FP64,
+                 schedule: int | None = SCHEDULE_SIZE, api: str = "backend"):
+        # precision / schedule None: keep what the library chose at creation
+        # (at the CP2K surface the environment may set the precision)
         L = lib()
         self.inp = inp
         self.api = api
@@ -228,8 +230,10 @@ class GridTaskList:
            C.cast(self._bs, C.c_void_p), *[_p(a) for a in lists], *[_p(a) for a in levels],
            C.byref(self.h))
         self.impl = self._impl_handle()
-        self.set_precision(precision)
-        self.set_schedule(schedule)
+        if precision is not None:
+            self.set_precision(precision)
+        if schedule is not None:
+            self.set_schedule(schedule)
         self._pab = None
         self._hab = None
         self._grids = None
