@@ -46,7 +46,7 @@ template <typename N, int LPB> struct OrthoSmem {
   }
   // collocate: tables, coefficients, C_xy, periodic maps
   static __host__ __device__ size_t bytes_coll(int wmax) {
-    size_t b = sizeof(T) * (3 * (size_t)wmax * PP + ncoset(LPB) + ntri(LPB));
+    size_t b = sizeof(T) * (3 * (size_t)wmax * PP + ntri(LPB) * P + ntri(LPB));
     b += sizeof(int) * 3 * (size_t)wmax;
     b += 64; // alignment slack
     return (b + 15) & ~size_t(15);
@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
   unsigned char *ws = smem + (threadIdx.x >> 5) * OrthoSmem<N, LPB>::bytes_coll(wmax);
   T *pol = (T *)ws;
   T *coef = pol + 3 * (size_t)wmax * PP;
-  T *cxy = coef + ncoset(LPB);
+  T *cxy = coef + ntri(LPB) * P;
   int *map = (int *)(cxy + ntri(LPB));
   const T *coefs = (const T *)a.coef;
 
@@ -256,15 +256,26 @@ __global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
         atomicOr(a.error, 1);
       continue;
     }
-    const int nco = ncoset(lp), ntr = ntri(lp);
-    if constexpr (std::is_same<T, float>::value) {
-      const float *csrc = (const float *)a.coef + (size_t)a.coef_off[t] * a.coef_stride;
-      for (int e = lane; e < nco; e += 32)
-        coef[e] = csrc[(size_t)e * a.coef_stride];
-    } else {
-      const T *csrc = coefs + a.coef_off[t];
-      for (int e = lane; e < nco; e += 32)
-        coef[e] = csrc[e];
+    const int ntr = ntri(lp);
+    // coefficients regrouped as coef[(ly, lx)][lz], zero beyond lz = lp-ly-lx,
+    // so that the per-plane z fold is a plain loop
+    for (int r = lane; r < ntr * P; r += 32) {
+      const int e = r / P, lz = r - e * P;
+      int ly = 0, rem = e;
+      while (rem > lp - ly) {
+        rem -= lp - ly + 1;
+        ly++;
+      }
+      const int lx = rem;
+      T v = M::zero();
+      if (lz <= lp - ly - lx) {
+        const size_t ci = (size_t)a.coef_off[t] + cidx(lz, ly, lx, lp);
+        if constexpr (std::is_same<T, float>::value)
+          v = ((const float *)a.coef)[ci * a.coef_stride];
+        else
+          v = coefs[ci];
+      }
+      coef[r] = v;
     }
     fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane, a.seeds + (size_t)t * 18);
     __syncwarp();
@@ -287,15 +298,12 @@ __global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
         // C_xy[ly][lx] = sum_lz C_xyz[lz][ly][lx] pol_z[lz](k)
         const T *pz = pol + (size_t)(2 * cg.w + k + cg.cmax) * PP;
         for (int e = lane; e < ntr; e += 32) {
-          int ly = 0, rem = e;
-          while (rem > lp - ly) {
-            rem -= lp - ly + 1;
-            ly++;
-          }
-          const int lx = rem;
+          const T *cr = coef + e * P;
           T s = M::zero();
-          for (int lz = 0; lz <= lp - ly - lx; lz++)
-            s = M::fma_acc(s, coef[cidx(lz, ly, lx, lp)], pz[lz]);
+#pragma unroll
+          for (int lz = 0; lz < P; lz++)
+            if (lz <= lp)
+              s = M::fma_acc(s, cr[lz], pz[lz]);
           cxy[e] = M::norm(s);
         }
         __syncwarp();
@@ -371,7 +379,7 @@ __global__ void __launch_bounds__(128) collocate_ortho_pl(GridArgs a, int wmax) 
   T *pol = (T *)ws;
   T *qt = pol + 3 * (size_t)wmax * PP;
   T *coef = qt + (size_t)wmax * PP;
-  T *cxy = coef + ncoset(LPB);
+  T *cxy = coef + ntri(LPB) * P;
   int *map = (int *)(cxy + ntri(LPB));
   const T *coefs = (const T *)a.coef;
 
@@ -394,15 +402,26 @@ __global__ void __launch_bounds__(128) collocate_ortho_pl(GridArgs a, int wmax) 
         atomicOr(a.error, 1);
       continue;
     }
-    const int nco = ncoset(lp), ntr = ntri(lp);
-    if constexpr (std::is_same<T, float>::value) {
-      const float *csrc = (const float *)a.coef + (size_t)a.coef_off[t] * a.coef_stride;
-      for (int e = lane; e < nco; e += 32)
-        coef[e] = csrc[(size_t)e * a.coef_stride];
-    } else {
-      const T *csrc = coefs + a.coef_off[t];
-      for (int e = lane; e < nco; e += 32)
-        coef[e] = csrc[e];
+    const int ntr = ntri(lp);
+    // coefficients regrouped as coef[(ly, lx)][lz], zero beyond lz = lp-ly-lx,
+    // so that the per-plane z fold is a plain loop
+    for (int r = lane; r < ntr * P; r += 32) {
+      const int e = r / P, lz = r - e * P;
+      int ly = 0, rem = e;
+      while (rem > lp - ly) {
+        rem -= lp - ly + 1;
+        ly++;
+      }
+      const int lx = rem;
+      T v = M::zero();
+      if (lz <= lp - ly - lx) {
+        const size_t ci = (size_t)a.coef_off[t] + cidx(lz, ly, lx, lp);
+        if constexpr (std::is_same<T, float>::value)
+          v = ((const float *)a.coef)[ci * a.coef_stride];
+        else
+          v = coefs[ci];
+      }
+      coef[r] = v;
     }
     fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane, a.seeds + (size_t)t * 18);
     __syncwarp();
@@ -417,15 +436,12 @@ __global__ void __launch_bounds__(128) collocate_ortho_pl(GridArgs a, int wmax) 
       // C_xy[ly][lx] = sum_lz C_xyz[lz][ly][lx] pol_z[lz](k)
       const T *pz = pol + (size_t)(2 * cg.w + k + cg.cmax) * PP;
       for (int e = lane; e < ntr; e += 32) {
-        int ly = 0, rem = e;
-        while (rem > lp - ly) {
-          rem -= lp - ly + 1;
-          ly++;
-        }
-        const int lx = rem;
+        const T *cr = coef + e * P;
         T s = M::zero();
-        for (int lz = 0; lz <= lp - ly - lx; lz++)
-          s = M::fma_acc(s, coef[cidx(lz, ly, lx, lp)], pz[lz]);
+#pragma unroll
+        for (int lz = 0; lz < P; lz++)
+          if (lz <= lp)
+            s = M::fma_acc(s, cr[lz], pz[lz]);
         cxy[e] = M::norm(s);
       }
       __syncwarp();
