@@ -330,6 +330,7 @@ struct TaskList {
   double *d_coef_int = nullptr; // integrated coefficients
   size_t coef_int_cap = 0;
   void *d_gridsplit[GB300_MAX_LEVELS] = {}; // integrate: V as float / float2
+  float *d_gridhi[GB300_MAX_LEVELS] = {};    // mixed integrate: V high words, dense
   float *d_gridlo[GB300_MAX_LEVELS] = {};   // collocate: low words (mixed)
   double *d_forces = nullptr, *d_virial = nullptr;
   int *d_counters = nullptr; // one per queue launch
@@ -610,6 +611,8 @@ static void free_device(TaskList *t) {
   for (int l = 0; l < GB300_MAX_LEVELS; l++) {
     if (t->d_gridsplit[l])
       cudaFree(t->d_gridsplit[l]);
+    if (t->d_gridhi[l])
+      cudaFree(t->d_gridhi[l]);
     if (t->d_gridlo[l])
       cudaFree(t->d_gridlo[l]);
   }
@@ -1274,7 +1277,12 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
         CK(cudaMalloc(&t->d_gridsplit[l], sizeof(float2) * np));
         t->gen++;
       }
-      launch_grid_split(grids[l], t->d_gridsplit[l], np, arith, s);
+      if (arith == ARITH_MIXED && !t->d_gridhi[l]) {
+        CK(cudaMalloc((void **)&t->d_gridhi[l], sizeof(float) * np));
+        t->gen++;
+      }
+      launch_grid_split(grids[l], t->d_gridsplit[l], np, arith, s,
+                        arith == ARITH_MIXED ? t->d_gridhi[l] : nullptr);
     }
   if (need_pab) {
     ContractArgs ca{t->d_subs, (int)t->subs.size(), t->d_sphi, pab, nullptr, t->d_pab_cart,
@@ -1305,11 +1313,14 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
     ga.queue = q.d_idx;
     ga.nqueue = q.n;
     ga.counter = t->d_counters + qi++;
-    ga.grid_stride = q.fp32 ? 2 : 1;
-    // the general path's double-float class runs in FP64 in the mixed mode
+    ga.grid_stride = 1;
+    // FP64: the grid; mixed: float2 pairs, dense high words for the FP32
+    // class, and the FP64 grid for the general path's double-float class
     for (int l = 0; l < t->nlevels; l++)
       ga.grids_in[l] = (arith == ARITH_FP64 || (q.general && arith == ARITH_MIXED && !q.fp32))
-                           ? (const void *)grids[l] : (const void *)t->d_gridsplit[l];
+                           ? (const void *)grids[l]
+                       : (arith == ARITH_MIXED && q.fp32) ? (const void *)t->d_gridhi[l]
+                                                          : (const void *)t->d_gridsplit[l];
     grid_launch(t, q, 1, q.fp32 ? (int)ARITH_FP32 : arith, ga, s);
     grid_library_counter_add(kBucketLp[q.bucket], GRID_BACKEND_GB300,
                              q.general ? GRID_INTEGRATE_GENERAL : GRID_INTEGRATE_ORTHO, q.n);

@@ -276,7 +276,7 @@ void launch_post(const PostArgs &a, int arith, int max_smem_words,
                  cudaStream_t s);
 // V grid -> float (ARITH_FP32) or float2 hi/lo pairs (ARITH_MIXED)
 void launch_grid_split(const double *src, void *dst, size_t n, int arith,
-                       cudaStream_t s);
+                       cudaStream_t s, float *hi = nullptr);
 // g += (double)lo
 void launch_grid_fold_lo(double *g, const float *lo, size_t n, cudaStream_t s);
 

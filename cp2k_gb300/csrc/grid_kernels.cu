@@ -752,7 +752,7 @@ void launch_integrate(const GridArgs &a, int arith, bool general, int bucket, in
 // grid conversions around the mixed paths
 // ------------------------------------------------------------------------
 __global__ void grid_split_kernel(const double *__restrict__ src, void *__restrict__ dst,
-                                  size_t n, int arith) {
+                                  size_t n, int arith, float *__restrict__ hi) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
     const double v = src[i];
@@ -761,6 +761,8 @@ __global__ void grid_split_kernel(const double *__restrict__ src, void *__restri
     } else {
       const float h = (float)v;
       ((float2 *)dst)[i] = make_float2(h, (float)(v - (double)h));
+      if (hi) // dense high words for the mixed mode's FP32 tasks
+        hi[i] = h;
     }
   }
 }
@@ -777,10 +779,11 @@ static int grid_blocks(size_t n) {
   return (int)(nb > 152 * 16 ? 152 * 16 : (nb ? nb : 1));
 }
 
-void launch_grid_split(const double *src, void *dst, size_t n, int arith, cudaStream_t s) {
+void launch_grid_split(const double *src, void *dst, size_t n, int arith, cudaStream_t s,
+                       float *hi) {
   if (n == 0)
     return;
-  grid_split_kernel<<<grid_blocks(n), 256, 0, s>>>(src, dst, n, arith);
+  grid_split_kernel<<<grid_blocks(n), 256, 0, s>>>(src, dst, n, arith, hi);
   count_launch();
 }
 
