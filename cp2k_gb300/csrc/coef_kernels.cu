@@ -19,6 +19,8 @@
 #include <cstdio>
 #include <type_traits>
 
+#include <algorithm>
+
 #include "gb300_internal.h"
 #include "numeric.cuh"
 
@@ -151,10 +153,29 @@ __device__ void prep_one(int f, Orb a, Orb b, T za, T zb, T p, const CabW<T> &w)
 // A group of lanes working on one task: the whole warp, or half of it for
 // small tasks (two tasks per warp keep more lanes busy).
 struct Grp {
-  int lane, n;   // lane within the group, group size (16 or 32)
-  unsigned mask; // the group's lanes in the warp
-  __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+  int lane, n;   // lane within the group, group size (16, 32, or the CTA)
+  unsigned mask; // the group's lanes in the warp (groups up to 32 lanes)
+  __device__ __forceinline__ void sync() const {
+    if (n > 32)
+      __syncthreads(); // the group is the whole CTA
+    else
+      __syncwarp(mask);
+  }
 };
+
+// Group layout of a CTA: gsize 16 (two tasks per warp), 32 (one per warp) or
+// blockDim.x (one large task per CTA).
+struct GrpLayout {
+  Grp g;
+  int gid, ngroups, slot; // first task, stride, shared-memory slot in the CTA
+};
+__device__ __forceinline__ GrpLayout grp_layout(int gsize) {
+  const int tid = threadIdx.x, per_cta = blockDim.x / gsize, gi = tid / gsize;
+  const int sub = (tid & 31) / (gsize < 32 ? gsize : 32);
+  const unsigned mask = gsize >= 32 ? 0xffffffffu : ((1u << gsize) - 1) << (sub * gsize);
+  return GrpLayout{Grp{tid % gsize, gsize, mask}, (int)blockIdx.x * per_cta + gi,
+                   (int)gridDim.x * per_cta, gi};
+}
 
 // ------------------------------------------------------------------------
 // Binomial expansion tables alpha[dir][lxb][lxa][l]: coefficient of (x-p)^l
@@ -428,12 +449,10 @@ template <typename U, typename Tout>
 __global__ void __launch_bounds__(128) coefficients_kernel(CoefArgs a, int words_per_group,
                                                            int gsize) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int lane = threadIdx.x & 31;
-  const int ng = 32 / gsize, half = lane / gsize;
-  const Grp g{lane % gsize, gsize, gsize == 32 ? FULL : ((1u << gsize) - 1) << (half * gsize)};
-  const int gid = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * ng + half;
-  const int ngroups = ((gridDim.x * blockDim.x) >> 5) * ng;
-  double *ws = (double *)smem + (size_t)((threadIdx.x >> 5) * ng + half) * words_per_group;
+  const GrpLayout gl = grp_layout(gsize);
+  const Grp &g = gl.g;
+  const int gid = gl.gid, ngroups = gl.ngroups;
+  double *ws = (double *)smem + (size_t)gl.slot * words_per_group;
   const int nt = a.order ? a.norder : a.ntasks;
   for (int i = gid; i < nt; i += ngroups) {
     const int t = a.order ? a.order[i] : i;
@@ -565,11 +584,11 @@ __global__ void __launch_bounds__(128) post_kernel(PostArgs a, int words_per_gro
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ double vir_cta[9];
   const int lane = threadIdx.x & 31;
-  const int ng = 32 / gsize, half = lane / gsize;
-  const Grp g{lane % gsize, gsize, gsize == 32 ? FULL : ((1u << gsize) - 1) << (half * gsize)};
-  const int gid = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * ng + half;
-  const int ngroups = ((gridDim.x * blockDim.x) >> 5) * ng;
-  double *ws = (double *)smem + (size_t)((threadIdx.x >> 5) * ng + half) * words_per_group;
+  const GrpLayout gl = grp_layout(gsize);
+  const Grp &g = gl.g;
+  const int gid = gl.gid, ngroups = gl.ngroups;
+  const int wsz = gsize < 32 ? gsize : 32; // lanes of a group within one warp
+  double *ws = (double *)smem + (size_t)gl.slot * words_per_group;
   if (threadIdx.x < 9)
     vir_cta[threadIdx.x] = 0.0;
   __syncthreads();
@@ -582,15 +601,16 @@ __global__ void __launch_bounds__(128) post_kernel(PostArgs a, int words_per_gro
     double f[6] = {0, 0, 0, 0, 0, 0}, v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     post_task<U>(a, t, d, ws, g, f, v);
     const double scale = (d.iatom == d.jatom) ? 1.0 : 2.0;
-    // sums over the group's lanes (xor offsets below the group size stay inside it)
+    // sums over each warp's part of the group (xor offsets below the part
+    // size stay inside it); the first lane of each part adds its sum
     if (a.forces) {
       for (int i = 0; i < 6; i++) {
         double s = f[i];
-        for (int o = gsize / 2; o > 0; o >>= 1)
+        for (int o = wsz / 2; o > 0; o >>= 1)
           s += __shfl_xor_sync(g.mask, s, o);
         f[i] = s;
       }
-      if (g.lane == 0)
+      if (lane % wsz == 0)
         for (int i = 0; i < 3; i++) {
           atomicAdd(&a.forces[3 * d.iatom + i], scale * f[i]);
           atomicAdd(&a.forces[3 * d.jatom + i], scale * f[3 + i]);
@@ -599,11 +619,11 @@ __global__ void __launch_bounds__(128) post_kernel(PostArgs a, int words_per_gro
     if (a.virial) {
       for (int i = 0; i < 9; i++) {
         double s = v[i];
-        for (int o = gsize / 2; o > 0; o >>= 1)
+        for (int o = wsz / 2; o > 0; o >>= 1)
           s += __shfl_xor_sync(g.mask, s, o);
         v[i] = s;
       }
-      if (g.lane == 0)
+      if (lane % wsz == 0)
         for (int i = 0; i < 9; i++)
           atomicAdd(&vir_cta[i], scale * v[i]);
     }
@@ -743,21 +763,40 @@ void launch_contract_hab(const ContractArgs &a, cudaStream_t s) {
   count_launch();
 }
 
-// two tasks per warp (groups of 16 lanes) while the per-task work is small
-constexpr int kSmallTaskWords = 1024;
+// two tasks per warp (groups of 16 lanes) while the per-task work is small;
+// one task per 4-warp CTA when its shared memory would leave an SM with few
+// warps (high angular momenta)
+constexpr int kSmallTaskWords = 1024, kLargeTaskWords = 4096;
+
+struct GroupLaunch {
+  int gsize, threads, grid;
+  size_t smem;
+};
+static GroupLaunch group_launch(int words_per_group, int ntasks) {
+  GroupLaunch L{};
+  if (words_per_group > kLargeTaskWords) {
+    L.gsize = L.threads = 128;
+    L.smem = (size_t)words_per_group * 8;
+    L.grid = std::max(1, std::min(ntasks, 152 * 32));
+    return L;
+  }
+  L.gsize = words_per_group <= kSmallTaskWords ? 16 : 32;
+  const size_t per_warp = (size_t)words_per_group * 8 * (32 / L.gsize);
+  const int nw = warps_for(per_warp);
+  L.threads = 32 * nw;
+  L.smem = nw * per_warp;
+  L.grid = nw < 1 ? 0 : grid_size_for(ntasks, nw);
+  return L;
+}
 
 template <typename U, typename Tout>
 static void launch_coef_t(const CoefArgs &a, int words_per_group, cudaStream_t s) {
-  const int gsize = words_per_group <= kSmallTaskWords ? 16 : 32;
-  const size_t per_warp = (size_t)words_per_group * 8 * (32 / gsize);
-  const int nw = warps_for(per_warp);
-  if (nw < 1)
+  const GroupLaunch L = group_launch(words_per_group, a.order ? a.norder : a.ntasks);
+  if (L.grid < 1 || L.smem > kSmemBudget)
     return launch_error("coefficients: angular momenta too large for shared memory");
-  const size_t smem = nw * per_warp;
   auto k = coefficients_kernel<U, Tout>;
-  set_smem((const void *)k, smem);
-  k<<<grid_size_for(a.order ? a.norder : a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_group,
-                                                                            gsize);
+  set_smem((const void *)k, L.smem);
+  k<<<L.grid, L.threads, L.smem, s>>>(a, words_per_group, L.gsize);
   count_launch();
 }
 
@@ -787,16 +826,12 @@ void launch_coefficients(const CoefArgs &a, int arith, int words_per_warp, cudaS
 
 template <typename U>
 static void launch_post_t(const PostArgs &a, int words_per_group, cudaStream_t s) {
-  const int gsize = words_per_group <= kSmallTaskWords ? 16 : 32;
-  const size_t per_warp = (size_t)words_per_group * 8 * (32 / gsize);
-  const int nw = warps_for(per_warp);
-  if (nw < 1)
+  const GroupLaunch L = group_launch(words_per_group, a.order ? a.norder : a.ntasks);
+  if (L.grid < 1 || L.smem > kSmemBudget)
     return launch_error("post-processing: angular momenta too large for shared memory");
-  const size_t smem = nw * per_warp;
   auto k = post_kernel<U>;
-  set_smem((const void *)k, smem);
-  k<<<grid_size_for(a.order ? a.norder : a.ntasks, nw), 32 * nw, smem, s>>>(a, words_per_group,
-                                                                            gsize);
+  set_smem((const void *)k, L.smem);
+  k<<<L.grid, L.threads, L.smem, s>>>(a, words_per_group, L.gsize);
   count_launch();
 }
 

@@ -20,6 +20,7 @@
 #include <cmath>
 
 #include "gb300_internal.h"
+#include "numeric.cuh"
 
 namespace gb300 {
 
@@ -284,7 +285,10 @@ __global__ void __launch_bounds__(128) collocate_general(GridArgs a, int njmax) 
               v += q[jl] * pj;
             pj *= djt;
           }
-          atomicAdd(gplane + (size_t)jg * nx + ig, (double)(v * gauss));
+          if constexpr (sizeof(T) == 8)
+            atomicAdd(gplane + (size_t)jg * nx + ig, (double)(v * gauss));
+          else // integer-pipe conversion: the FP64 pipe is the scarce one
+            atomicAdd(gplane + (size_t)jg * nx + ig, f2d_exact((float)(v * gauss)));
         }
         __syncwarp();
       }
