@@ -587,7 +587,7 @@ __global__ void __launch_bounds__(128, LPB <= 4 ? 5 : 1) integrate_ortho(GridArg
         for (int l = 0; l < P; l++)
           wy[l] = M::zero();
         // this lane's rows of the plane: j in [jlo, jhi] (jhi <= 1 - js), every
-        // G-th row from its group's phase, two rows per step; the grid values
+        // G-th row from its group's phase, R rows per step; the grid values
         // of the next step are loaded before this step's arithmetic
         const int JJ = xin ? (int)cg.jx[kk * cg.NX + (cx <= 0 ? -cx : cx - 1)] : -1;
         const int jlo = -JJ, jhi = JJ + 1, G = nph;
@@ -599,24 +599,40 @@ __global__ void __launch_bounds__(128, LPB <= 4 ? 5 : 1) integrate_ortho(GridArg
           return ok ? grid_get<N>(grid, base + (size_t)map[cg.w + jj + cg.cmax] * nx, gstride)
                     : M::zero();
         };
-        bool has1 = j <= jhi, has2 = j + G <= jhi;
-        T v1 = fetch(j, has1), v2 = fetch(j + G, has2);
-        while (has1) {
-          const int jn = j + 2 * G;
-          const bool n1 = jn <= jhi, n2 = jn + G <= jhi;
-          const T v1n = fetch(jn, n1), v2n = fetch(jn + G, n2);
-          T p1[PP], p2[PP];
-          load_row<T, PP>(pol + (size_t)(cg.w + j + cg.cmax) * PP, p1);
-          load_row<T, PP>(pol + (size_t)(cg.w + (has2 ? j + G : j) + cg.cmax) * PP, p2);
+        // R rows per step (4 in FP32, whose arithmetic is too short to hide
+        // the L2 latency of 2 loads in flight; 2 otherwise)
+        constexpr int R = std::is_same<N, float>::value ? 4 : 2;
+        bool has[R];
+        T v[R];
 #pragma unroll
-          for (int ly = 0; ly < P; ly++)
-            if (ly <= lp)
-              wy[ly] = M::fma_acc(M::fma_acc(wy[ly], v1, p1[ly]), v2, p2[ly]);
+        for (int r = 0; r < R; r++) {
+          has[r] = j + r * G <= jhi;
+          v[r] = fetch(j + r * G, has[r]);
+        }
+        while (has[0]) {
+          const int jn = j + R * G;
+          bool hn[R];
+          T vn[R];
+#pragma unroll
+          for (int r = 0; r < R; r++) {
+            hn[r] = jn + r * G <= jhi;
+            vn[r] = fetch(jn + r * G, hn[r]);
+          }
+#pragma unroll
+          for (int r = 0; r < R; r++) {
+            T pr[PP];
+            load_row<T, PP>(pol + (size_t)(cg.w + (has[r] ? j + r * G : j) + cg.cmax) * PP, pr);
+#pragma unroll
+            for (int ly = 0; ly < P; ly++)
+              if (ly <= lp)
+                wy[ly] = M::fma_acc(wy[ly], v[r], pr[ly]);
+          }
           j = jn;
-          has1 = n1;
-          has2 = n2;
-          v1 = v1n;
-          v2 = v2n;
+#pragma unroll
+          for (int r = 0; r < R; r++) {
+            has[r] = hn[r];
+            v[r] = vn[r];
+          }
         }
 #pragma unroll
         for (int l = 0; l < P; l++)
