@@ -962,10 +962,16 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
 
 namespace gb300 {
 
-static Mode &get_mode(TaskList *t, const LDiffs &d) {
-  // one mode per (l shifts, precision): switching the precision back and forth
-  // reuses the queues built for each
-  const int key = mode_key(d) * 4 + t->precision;
+// phase 0 collocate, 1 integrate, 2 integrate with tau
+static Mode &get_mode(TaskList *t, const LDiffs &d, int phase) {
+  // one mode per (l shifts, precision, phase): switching the precision back
+  // and forth reuses the queues built for each
+  const int key = (mode_key(d) * 4 + t->precision) * 3 + phase;
+  // derivatives of the Gaussians (derivative densities; the gradients of tau)
+  // multiply the contributions by up to (2 zeta + l + 1) per unit of
+  // angular-momentum shift, with cancellation in the sums; the FP32 class
+  // then uses the bound scaled by that factor
+  const int dshift = phase == 0 ? d.la_max + d.lb_max : phase == 2 ? 2 : 0;
   auto it = t->modes.find(key);
   if (it != t->modes.end() && it->second.sched_version == t->sched_version)
     return it->second;
@@ -1002,8 +1008,10 @@ static Mode &get_mode(TaskList *t, const LDiffs &d) {
     if (b < 0)
       fail("contraction order lp=%d exceeds %d", lp, GB300_LP_MAX);
     const int g = (k.flags & TF_GENERAL) ? 1 : 0;
-    const int cls = (t->precision == GRID_GB300_MIXED && t->gbound[s] <= t->mixed_threshold)
-                        ? 1 : 0;
+    double gb = t->gbound[s];
+    if (dshift > 0)
+      gb *= pow(2.0 * std::max(k.zeta, k.zetb) + std::max(k.la_max, k.lb_max) + 1.0, dshift);
+    const int cls = (t->precision == GRID_GB300_MIXED && gb <= t->mixed_threshold) ? 1 : 0;
     const int ext = g == 0 ? 2 * t->sph[k.sphere].cmax + 2 : k.imax[1] - k.center[1] + 1;
     const int sz = ext <= t->small_extent[t->precision] ? 0 : 1;
     double cost;
@@ -1173,7 +1181,7 @@ static void begin_call(TaskList *t, cudaStream_t s) {
 static void run_collocate(TaskList *t, int func, const double *pab, double *const *grids,
                           cudaStream_t s) {
   const LDiffs d = func_ldiffs(func);
-  Mode &m = get_mode(t, d);
+  Mode &m = get_mode(t, d, 0);
   const int arith = t->precision;
   t->gen += ensure(&t->d_coef, &t->coef_cap, m.coef_total * (arith == ARITH_FP32 ? 4 : 8));
   begin_call(t, s);
@@ -1263,7 +1271,7 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
 static void run_integrate(TaskList *t, bool tau, const double *pab, const double *const *grids,
                           double *hab, double *forces, double *virial, cudaStream_t s) {
   const LDiffs d = integrate_ldiffs(forces != nullptr, virial != nullptr, tau);
-  Mode &m = get_mode(t, d);
+  Mode &m = get_mode(t, d, tau ? 2 : 1);
   const int arith = t->precision;
   const bool need_pab = forces != nullptr || virial != nullptr;
   t->gen += ensure((void **)&t->d_coef_int, &t->coef_int_cap, m.coef_total * 8);

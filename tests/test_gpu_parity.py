@@ -209,3 +209,27 @@ def test_collocate_variants_agree(G, O, prec):
         assert max(rel_diff(a, b) for a, b in zip(out[1], ref)) < TOL_GRID
         ot.close()
     tl.close()
+
+
+@pytest.mark.parametrize("name,scale", [("c1_64atoms", 0.3), ("c3_256atoms_triclinic", 0.1)])
+def test_mixed_all_functions_tau_virial(G, O, name, scale):
+    """The mixed mode on every family of grid_func (derivative shifts of the
+    density) and on integration with tau and virial, against the FP64 oracle
+    within the mixed mode's stated bounds."""
+    from cp2k_gb300 import workload as W
+    inp = W.config(name, scale=scale, seed=23)
+    pab = W.density_blocks(inp)
+    V = W.potential_grids(inp)
+    ot = O.OracleTaskList(inp)
+    tl = G.GridTaskList(inp, precision=G.MIXED)
+    for func in (200, 301, 411, 501, 602, 703, 801, 902, 905, 1003):
+        g = tl.collocate(func, pab)
+        r = ot.collocate(func, pab)
+        assert max(rel_diff(a, b) for a, b in zip(g, r)) < 1e-6, func
+    h, f, v = tl.integrate(V, pab, compute_tau=True, forces=True, virial=True)
+    ho, fo, vo = ot.integrate(V, pab, compute_tau=True, forces=True, virial=True)
+    assert rel_diff(h, ho) < 1e-6
+    assert rel_diff(f, fo) < 1e-5
+    assert rel_diff(v, vo) < 1e-5
+    tl.close()
+    ot.close()
