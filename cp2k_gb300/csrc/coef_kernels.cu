@@ -339,10 +339,10 @@ __device__ T cijk_from_cxyz(const T *tab, int level, int lp, int iu, int ju, int
   return M::norm(acc);
 }
 
-// Per-warp shared memory of the coefficient / post kernels in 8-byte words:
-// cab (FP64) [n2][n1], cab in the working type, alpha, cxyz, cijk.
+// Per-group shared memory of the coefficient / post kernels in 8-byte words:
+// cab [n2][n1] (FP64, then the working type in place), alpha, cxyz, cijk.
 __host__ __device__ inline size_t coef_smem_words(int n1, int n2, int la, int lb, int lp) {
-  return 2 * (size_t)n1 * n2 + 3 * (size_t)(la + 1) * (lb + 1) * (lp + 1) +
+  return (size_t)n1 * n2 + 3 * (size_t)(la + 1) * (lb + 1) * (lp + 1) +
          2 * (size_t)ncoset(lp) + 8;
 }
 
@@ -384,8 +384,8 @@ __device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *w
   const int lp = la_max + lb_max;
   const int n1 = ncoset(la_max), n2 = ncoset(lb_max);
   double *cabd = ws;
-  U *cab = (U *)(cabd + (size_t)n1 * n2);
-  U *alpha = (U *)((double *)cab + (size_t)n1 * n2);
+  U *cab = (U *)cabd; // converted in place after the FP64 accumulation
+  U *alpha = (U *)(cabd + (size_t)n1 * n2);
   U *cxyz = (U *)((double *)alpha + 3 * (size_t)(la_max + 1) * (lb_max + 1) * (lp + 1));
   U *cijk = (U *)((double *)cxyz + ncoset(lp));
   for (int e = g.lane; e < n1 * n2; e += g.n)
@@ -402,8 +402,23 @@ __device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *w
     prep_one<double>(a.func, orb_of_index(ia), orb_of_index(ib), d.zeta, d.zetb, p, w);
   }
   g.sync();
-  for (int e = g.lane; e < n1 * n2; e += g.n)
-    cab[e] = U(cabd[e]);
+  if constexpr (sizeof(U) == sizeof(double)) {
+    for (int e = g.lane; e < n1 * n2; e += g.n) { // each lane rewrites only its own slots
+      const double v = cabd[e];
+      cab[e] = U(v);
+    }
+  } else {
+    // 4-byte U, in ascending chunks of g.n elements: the values of chunk k
+    // land in doubles below (k+1) g.n / 2, all of which were read by then
+    for (int base = 0; base < n1 * n2; base += g.n) {
+      const int e = base + g.lane;
+      const double v = e < n1 * n2 ? cabd[e] : 0.0;
+      g.sync();
+      if (e < n1 * n2)
+        cab[e] = U(v);
+    }
+  }
+  g.sync();
   const double *ra = a.atom_pos + 3 * d.iatom;
   double rb[3];
   for (int i = 0; i < 3; i++)

@@ -233,3 +233,32 @@ def test_mixed_all_functions_tau_virial(G, O, name, scale):
     assert rel_diff(v, vo) < 1e-5
     tl.close()
     ot.close()
+
+
+@pytest.mark.parametrize("lmax,random_sphi,funcs,tau", [
+    (6, False, (100, 200), False),   # forces + virial: la = 8, lb = 7, lp = 15
+    (5, False, (100, 200, 801), True),  # DXDX la = lb = 7; tau + virial la = 8, lb = 7
+    (3, True, (100, 200, 801), True),
+])
+def test_high_l_and_contraction_fp64(G, O, lmax, random_sphi, funcs, tau):
+    """Sets up to l = 6 and random orthonormal contraction matrices (sphi),
+    against the oracle. The cases reach the largest shifted angular momenta
+    whose per-task coefficient block (cab, alpha, cxyz) fits the 200 KB of
+    shared memory of one CTA: la = 8 with lb = 7."""
+    from cp2k_gb300 import workload as W
+    inp = W.config("c1_64atoms", scale=0.12, seed=41, random_sphi=random_sphi,
+                   elements=[(1.0, [lmax, 1])], zet=(0.3, 20.0))
+    pab = W.density_blocks(inp)
+    V = W.potential_grids(inp)
+    tl = G.GridTaskList(inp, precision=G.FP64)
+    ot = O.OracleTaskList(inp)
+    for func in funcs:
+        e = max(rel_diff(a, b) for a, b in zip(tl.collocate(func, pab), ot.collocate(func, pab)))
+        assert e < 1e-11, (func, e)
+    h1, f1, v1 = tl.integrate(V, pab, compute_tau=tau, forces=True, virial=True)
+    h2, f2, v2 = ot.integrate(V, pab, compute_tau=tau, forces=True, virial=True)
+    assert rel_diff(h1, h2) < 1e-11
+    assert rel_diff(f1, f2) < TOL_DERIV
+    assert rel_diff(v1, v2) < TOL_DERIV
+    tl.close()
+    ot.close()
