@@ -1200,7 +1200,6 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
   co.func = func;
   co.d = d;
   co.levels = t->d_levels;
-  co.general_fp64 = arith == ARITH_MIXED ? 1 : 0;
   co.dhtab = t->d_dhtab;
   co.dhtab_f = t->d_dhtab_f;
   co.dhtab_df = t->d_dhtab_df;
@@ -1322,11 +1321,10 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
     ga.nqueue = q.n;
     ga.counter = t->d_counters + qi++;
     ga.grid_stride = 1;
-    // FP64: the grid; mixed: float2 pairs, dense high words for the FP32
-    // class, and the FP64 grid for the general path's double-float class
+    // FP64: the grid; mixed: float2 pairs for the double-float class, dense
+    // high words for the FP32 class
     for (int l = 0; l < t->nlevels; l++)
-      ga.grids_in[l] = (arith == ARITH_FP64 || (q.general && arith == ARITH_MIXED && !q.fp32))
-                           ? (const void *)grids[l]
+      ga.grids_in[l] = arith == ARITH_FP64                  ? (const void *)grids[l]
                        : (arith == ARITH_MIXED && q.fp32) ? (const void *)t->d_gridhi[l]
                                                           : (const void *)t->d_gridsplit[l];
     grid_launch(t, q, 1, q.fp32 ? (int)ARITH_FP32 : arith, ga, s);

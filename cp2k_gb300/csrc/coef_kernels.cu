@@ -356,10 +356,8 @@ __device__ __forceinline__ Orb orb_of_index(int i) {
 
 // store of one coefficient in the grid kernels' arithmetic
 template <typename Tout, typename U>
-__device__ __forceinline__ void store_coef(void *out, size_t i, U v, bool as_fp64) {
-  if (as_fp64) {
-    ((double *)out)[i] = to_double(v);
-  } else if constexpr (std::is_same<Tout, dfloat>::value) {
+__device__ __forceinline__ void store_coef(void *out, size_t i, U v) {
+  if constexpr (std::is_same<Tout, dfloat>::value) {
     if constexpr (std::is_same<U, dfloat>::value)
       ((dfloat *)out)[i] = v;
     else if constexpr (std::is_same<U, float>::value)
@@ -377,8 +375,7 @@ __device__ __forceinline__ void store_coef(void *out, size_t i, U v, bool as_fp6
 // coefficients of one task (one warp): P_ab -> C_ab -> C_xyz (-> C_ijk)
 // ------------------------------------------------------------------------
 template <typename U, typename Tout>
-__device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *ws, const Grp &g,
-                          bool as_fp64) {
+__device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *ws, const Grp &g) {
   const SubblockDesc sb = a.subs[d.subblock];
   const int la_max = d.la_max + a.d.la_max, lb_max = d.lb_max + a.d.lb_max;
   const int lp = la_max + lb_max;
@@ -435,7 +432,7 @@ __device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *w
       cxyz[e] = v;
       cijk[e] = U(0);
     } else {
-      store_coef<Tout, U>(a.coef, (size_t)a.coef_off[t] + e, v, false);
+      store_coef<Tout, U>(a.coef, (size_t)a.coef_off[t] + e, v);
     }
   }
   if (general) {
@@ -452,7 +449,7 @@ __device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *w
       int ku, ju, iu;
       decode_cidx(e, lp, ku, ju, iu);
       store_coef<Tout, U>(a.coef, (size_t)a.coef_off[t] + e,
-                          cijk_from_cxyz<U>(tab, d.level, lp, iu, ju, ku, cxyz), as_fp64);
+                          cijk_from_cxyz<U>(tab, d.level, lp, iu, ju, ku, cxyz));
     }
   }
   g.sync();
@@ -474,8 +471,7 @@ __global__ void __launch_bounds__(128) coefficients_kernel(CoefArgs a, int words
     const TaskDesc d = a.tasks[t];
     if (d.flags & TF_SKIP)
       continue;
-    // general-path coefficients of the mixed mode are stored in FP64
-    coef_task<U, Tout>(a, t, d, ws, g, (d.flags & TF_GENERAL) && a.general_fp64);
+    coef_task<U, Tout>(a, t, d, ws, g);
   }
 }
 

@@ -152,7 +152,6 @@ struct CoefArgs {
   int func;
   LDiffs d;
   const LevelSet *levels; // device copy
-  int general_fp64;       // write general-path coefficients as FP64
   const double *dhtab;     // general-path transform table (build_dh_table), FP64
   const float *dhtab_f;    // the same in FP32 (FP32 kernels)
   const float2 *dhtab_df;  // the same as double-float pairs (mixed kernels)

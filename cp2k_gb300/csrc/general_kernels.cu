@@ -13,11 +13,13 @@
 // split, grid_ref_collint.h:358-367): e_ki per lane and plane, e_jk per row
 // (precomputed per plane in shared memory), e_ij by a multiplicative
 // recurrence along j.  FP32 path evaluates exp(-zetp r^2) per point from
-// cube-local Cartesian offsets.
+// cube-local Cartesian offsets.  The double-float path (mixed mode) evaluates
+// it per point in dfloat (df_exp_neg), see collocate_general_df.
 #include <cuda_runtime.h>
 
 #include <climits>
 #include <cmath>
+#include <type_traits>
 
 #include "gb300_internal.h"
 #include "numeric.cuh"
@@ -127,7 +129,7 @@ __device__ __forceinline__ void plane_rows(int k, const GenTask &g, const LevelD
     if (gmap(j, 1, g, L) >= 0)
       rb = row_bounds(j, k, g, radius);
     rows[r] = rb;
-    if (sizeof(T) == 8) {
+    if constexpr (std::is_same<T, double>::value) {
       const double dj = (double)j - g.gp[1];
       ejk[r] = exp(-zetp * (dj * dj * g.hh[1] + 2.0 * dj * dk * g.h12));
     }
@@ -169,10 +171,10 @@ __global__ void __launch_bounds__(128) collocate_general(GridArgs a, int njmax) 
     }
     const int nco = ncoset(lp), ntr = ntri(lp);
     if (sizeof(T) == 4 && a.coef_stride == 2) {
-      // FP32 task of the mixed mode: general-path coefficients are stored in FP64
-      const double *csrc = (const double *)a.coef + a.coef_off[t];
+      // FP32 task of the mixed mode: the high words of the dfloat coefficients
+      const float *csrc = (const float *)a.coef + 2 * (size_t)a.coef_off[t];
       for (int e = lane; e < nco; e += 32)
-        coef[e] = (T)csrc[e];
+        coef[e] = (T)csrc[2 * e];
     } else {
       const T *csrc = coefs + a.coef_off[t];
       for (int e = lane; e < nco; e += 32)
@@ -468,6 +470,347 @@ __global__ void __launch_bounds__(128) integrate_general(GridArgs a, int njmax) 
   }
 }
 
+// ------------------------------------------------------------------------
+// double-float (mixed mode) general kernels
+//
+// Same point set and polynomial as above, in dfloat arithmetic on the FP32
+// pipes. The Gaussian is evaluated per point by df_exp_neg, from the
+// exponent in completed-square form along the lane's j line:
+//   zetp |r_ik + dj h1|^2 = A u^2 + x_perp,   u = dj - dj*,  A = zetp |h1|^2,
+// where r_ik = di h0 + dk h2, dj* = -(r_ik . h1) / |h1|^2 and x_perp =
+// zetp |r_ik|^2 - A dj*^2 >= 0. Both terms are non-negative, so the exponent
+// carries no cancellation. The FP64 work left is per lane and plane (the
+// line constants) and per row (the row bounds).
+// ------------------------------------------------------------------------
+
+// 2^(-j/64), j = 0..63, as dfloat pairs (the table of df_exp_neg)
+__device__ __forceinline__ void fill_exp2_table(float2 *tab) {
+  for (int j = threadIdx.x; j < 64; j += blockDim.x) {
+    const double v = exp2(-(double)j / 64.0);
+    const float h = (float)v;
+    tab[j] = make_float2(h, (float)(v - (double)h));
+  }
+  __syncthreads();
+}
+
+struct DfLine {
+  dfloat c0; // dj - dj* at the box's first row
+  dfloat xp; // x_perp
+};
+
+__device__ __forceinline__ DfLine df_line(double di, double dk, const GenTask &g, double zetp,
+                                          double inv_hh1, double fj0) {
+  double rc[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++)
+    rc[c] = di * g.h[c] + dk * g.h[6 + c];
+  const double rh = rc[0] * g.h[3] + rc[1] * g.h[4] + rc[2] * g.h[5];
+  const double rr = rc[0] * rc[0] + rc[1] * rc[1] + rc[2] * rc[2];
+  const double djs = -rh * inv_hh1;
+  return DfLine{df_make(fj0 - djs), df_make(fmax(zetp * (rr - rh * rh * inv_hh1), 0.0))};
+}
+
+// Gaussian at row offset rf (rows from the box's first row) of the line
+__device__ __forceinline__ dfloat df_gauss(const DfLine &L, dfloat A, float rf, const float2 *tab) {
+  const dfloat u = df_add1(L.c0, rf);
+  return df_exp_neg(df_fma(L.xp, df_mul(A, u), u), tab);
+}
+
+template <int LPB>
+__global__ void __launch_bounds__(128) collocate_general_df(GridArgs a, int njmax) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ float2 tab[64];
+  fill_exp2_table(tab);
+  constexpr int P = LPB + 1;
+  using S = GenSmem<dfloat, LPB>;
+  const int lane = threadIdx.x & 31;
+  unsigned char *ws = smem + (threadIdx.x >> 5) * S::bytes(njmax);
+  double *ejk = (double *)ws + ncoset(LPB);
+  dfloat *coef = (dfloat *)(ejk + njmax);
+  dfloat *cij = coef + ncoset(LPB);
+  dfloat *red = cij + ntri(LPB);
+  int2 *rows = (int2 *)(((uintptr_t)(red + 32 * S::red_stride()) + 7) & ~uintptr_t(7));
+  const dfloat *coefs = (const dfloat *)a.coef;
+
+  for (;;) {
+    int qi = 0;
+    if (lane == 0)
+      qi = atomicAdd(a.counter, 1);
+    qi = __shfl_sync(FULL, qi, 0);
+    if (qi >= a.nqueue)
+      break;
+    const int t = a.queue[qi];
+    const long long t0 = clock64();
+    const TaskDesc d = a.tasks[t];
+    const LevelDesc &L = a.levels.lv[d.level];
+    GenTask g;
+    gen_setup(d, L, g);
+    const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
+    const int nj = g.imax[1] - g.imin[1] + 1;
+    if (nj > njmax || lp > LPB) {
+      if (lane == 0)
+        atomicOr(a.error, 1);
+      continue;
+    }
+    const int nco = ncoset(lp), ntr = ntri(lp);
+    for (int e = lane; e < nco; e += 32)
+      coef[e] = coefs[a.coef_off[t] + e];
+    double *grid = a.grids[d.level];
+    float *glo = a.grids_lo[d.level];
+    const size_t nx = L.npts_local[0], nxy = nx * L.npts_local[1];
+    const int width = g.imax[0] - g.imin[0] + 1;
+    const int SW = width <= 8 ? 8 : (width <= 16 ? 16 : 32);
+    const int G = 32 / SW, sub = lane % SW, grp = lane / SW;
+    const double zetp = d.zetp, inv_hh1 = 1.0 / g.hh[1];
+    const double fj0 = (double)g.imin[1] - g.gp[1];
+    const dfloat A = df_make(zetp * g.hh[1]), dj0 = df_make(fj0);
+
+    for (int xc = g.imin[0]; xc <= g.imax[0]; xc += SW) {
+      const int i = xc + sub;
+      const bool xin = i <= g.imax[0];
+      const int ig = xin ? gmap(i, 0, g, L) : -1;
+      const double di = (double)i - g.gp[0];
+      dfloat px[P];
+      {
+        const dfloat dd = df_make(di);
+        dfloat p{1.f, 0.f};
+#pragma unroll
+        for (int l = 0; l < P; l++) {
+          px[l] = p;
+          p = df_mul(p, dd);
+        }
+      }
+      for (int k = g.imin[2]; k <= g.imax[2]; k++) {
+        const int kg = gmap(k, 2, g, L);
+        if (kg < 0)
+          continue;
+        const double dk = (double)k - g.gp[2];
+        plane_rows<dfloat>(k, g, L, d.radius, zetp, rows, ejk, lane);
+        // C_ij = sum_kl C_ijk dk^kl (Horner in kl)
+        const dfloat dkd = df_make(dk);
+        for (int e = lane; e < ntr; e += 32) {
+          int jl = 0, rem = e;
+          while (rem > lp - jl) {
+            rem -= lp - jl + 1;
+            jl++;
+          }
+          const int il = rem;
+          dfloat s{0.f, 0.f};
+          for (int kl = lp - jl - il; kl >= 0; kl--)
+            s = df_fma(coef[cidx(kl, jl, il, lp)], s, dkd);
+          cij[e] = s;
+        }
+        __syncwarp();
+        dfloat q[P];
+#pragma unroll
+        for (int jl = 0; jl < P; jl++) {
+          dfloat s{0.f, 0.f};
+          if (jl <= lp) {
+            const dfloat *row = cij + jl * (lp + 1) - (jl * (jl - 1)) / 2;
+#pragma unroll
+            for (int il = 0; il < P; il++)
+              if (il <= lp - jl)
+                s = df_fma_acc(s, row[il], px[il]);
+          }
+          q[jl] = df_norm(s);
+        }
+        const DfLine line = df_line(di, dk, g, zetp, inv_hh1, fj0);
+        double *gplane = grid + (size_t)kg * nxy;
+        float *lplane = glo + (size_t)kg * nxy;
+        for (int j0 = g.imin[1]; j0 <= g.imax[1]; j0 += G) {
+          const int j = j0 + grp;
+          if (j > g.imax[1] || ig < 0)
+            continue;
+          const int2 rb = rows[j - g.imin[1]];
+          if (i < rb.x || i > rb.y)
+            continue;
+          const int jg = gmap(j, 1, g, L); // >= 0 since rb non-empty
+          const float rf = (float)(j - g.imin[1]);
+          const dfloat gauss = df_gauss(line, A, rf, tab);
+          const dfloat dj = df_add1(dj0, rf);
+          dfloat v{0.f, 0.f};
+#pragma unroll
+          for (int jl = P - 1; jl >= 0; jl--)
+            if (jl <= lp)
+              v = df_fma(q[jl], v, dj);
+          const dfloat val = df_mul(v, gauss);
+          const size_t idx = (size_t)jg * nx + ig;
+          atomicAdd(gplane + idx, f2d_exact(val.h));
+          atomicAdd(lplane + idx, val.l);
+        }
+        __syncwarp();
+      }
+    }
+    if (a.task_cycles && lane == 0)
+      a.task_cycles[t] = clock64() - t0;
+    __syncwarp();
+  }
+}
+
+// acc + b without renormalisation (the sum of a long run is renormalised once)
+__device__ __forceinline__ dfloat df_acc(dfloat acc, dfloat b) {
+  const float s = acc.h + b.h;
+  const float bb = s - acc.h;
+  return dfloat{s, ((acc.h - (s - bb)) + (b.h - bb)) + (acc.l + b.l)};
+}
+
+template <int LPB>
+__global__ void __launch_bounds__(128) integrate_general_df(GridArgs a, int njmax) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ float2 tab[64];
+  fill_exp2_table(tab);
+  constexpr int P = LPB + 1;
+  constexpr int NKJ = (LPB + 1) * (LPB + 2) / 2;
+  using S = GenSmem<dfloat, LPB>;
+  const int lane = threadIdx.x & 31;
+  unsigned char *ws = smem + (threadIdx.x >> 5) * S::bytes(njmax);
+  double *acc = (double *)ws;
+  double *ejk = acc + ncoset(LPB);
+  dfloat *red = (dfloat *)(ejk + njmax) + ncoset(LPB) + ntri(LPB);
+  int2 *rows = (int2 *)(((uintptr_t)(red + 32 * S::red_stride()) + 7) & ~uintptr_t(7));
+  double *out = (double *)a.coef_out;
+
+  for (;;) {
+    int qi = 0;
+    if (lane == 0)
+      qi = atomicAdd(a.counter, 1);
+    qi = __shfl_sync(FULL, qi, 0);
+    if (qi >= a.nqueue)
+      break;
+    const int t = a.queue[qi];
+    const long long t0 = clock64();
+    const TaskDesc d = a.tasks[t];
+    const LevelDesc &L = a.levels.lv[d.level];
+    GenTask g;
+    gen_setup(d, L, g);
+    const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
+    const int nj = g.imax[1] - g.imin[1] + 1;
+    if (nj > njmax || lp > LPB) {
+      if (lane == 0)
+        atomicOr(a.error, 1);
+      continue;
+    }
+    const int nco = ncoset(lp);
+    for (int e = lane; e < nco; e += 32)
+      acc[e] = 0.0;
+    __syncwarp();
+    // the (hi, lo) float pairs of the split grid
+    const float2 *grid = (const float2 *)a.grids_in[d.level];
+    const size_t nx = L.npts_local[0], nxy = nx * L.npts_local[1];
+    const int width = g.imax[0] - g.imin[0] + 1;
+    const int SW = width <= 8 ? 8 : (width <= 16 ? 16 : 32);
+    const int G = 32 / SW, sub = lane % SW, grp = lane / SW;
+    const double zetp = d.zetp, inv_hh1 = 1.0 / g.hh[1];
+    const double fj0 = (double)g.imin[1] - g.gp[1];
+    const dfloat A = df_make(zetp * g.hh[1]), dj0 = df_make(fj0);
+
+    for (int xc = g.imin[0]; xc <= g.imax[0]; xc += SW) {
+      const int i = xc + sub;
+      const bool xin = i <= g.imax[0];
+      const int ig = xin ? gmap(i, 0, g, L) : -1;
+      const double di = (double)i - g.gp[0];
+      dfloat akj[NKJ];
+#pragma unroll
+      for (int e = 0; e < NKJ; e++)
+        akj[e] = dfloat{0.f, 0.f};
+
+      for (int k = g.imin[2]; k <= g.imax[2]; k++) {
+        const int kg = gmap(k, 2, g, L);
+        if (kg < 0)
+          continue;
+        const double dk = (double)k - g.gp[2];
+        plane_rows<dfloat>(k, g, L, d.radius, zetp, rows, ejk, lane);
+        __syncwarp();
+        const DfLine line = df_line(di, dk, g, zetp, inv_hh1, fj0);
+        dfloat wj[P];
+#pragma unroll
+        for (int l = 0; l < P; l++)
+          wj[l] = dfloat{0.f, 0.f};
+        const float2 *gplane = grid + (size_t)kg * nxy;
+        for (int j0 = g.imin[1]; j0 <= g.imax[1]; j0 += G) {
+          const int j = j0 + grp;
+          if (j > g.imax[1] || ig < 0)
+            continue;
+          const int2 rb = rows[j - g.imin[1]];
+          if (i < rb.x || i > rb.y)
+            continue;
+          const int jg = gmap(j, 1, g, L);
+          const float rf = (float)(j - g.imin[1]);
+          const float2 gv = __ldg(gplane + (size_t)jg * nx + ig);
+          dfloat pj = df_mul(dfloat{gv.x, gv.y}, df_gauss(line, A, rf, tab));
+          const dfloat dj = df_add1(dj0, rf);
+#pragma unroll
+          for (int jl = 0; jl < P; jl++) {
+            if (jl <= lp)
+              wj[jl] = df_acc(wj[jl], pj);
+            if (jl < P - 1)
+              pj = df_mul(pj, dj);
+          }
+        }
+        __syncwarp();
+        const dfloat dkd = df_make(dk);
+        dfloat pk{1.f, 0.f};
+#pragma unroll
+        for (int kl = 0; kl < P; kl++) {
+          if (kl > lp)
+            break;
+#pragma unroll
+          for (int jl = 0; jl < P; jl++)
+            if (jl <= lp - kl) {
+              dfloat &x = akj[kl * P - (kl * (kl - 1)) / 2 + jl];
+              x = df_fma_acc(x, df_norm(wj[jl]), pk);
+            }
+          pk = df_mul(pk, dkd);
+        }
+      }
+      // fold i and reduce over the warp through shared memory
+      {
+        constexpr int RS = S::red_stride();
+        dfloat *rl = red + lane * RS;
+#pragma unroll
+        for (int e = 0; e < NKJ; e++)
+          rl[e] = df_norm(akj[e]);
+        const dfloat dd = df_make(di);
+        dfloat pi = xin ? dfloat{1.f, 0.f} : dfloat{0.f, 0.f};
+#pragma unroll
+        for (int l = 0; l < P; l++) {
+          rl[NKJ + l] = pi;
+          pi = df_mul(pi, dd);
+        }
+        __syncwarp();
+        for (int e = lane; e < nco; e += 32) {
+          int kl, jl, il;
+          decode_cidx(e, lp, kl, jl, il);
+          const int kj = kl * P - (kl * (kl - 1)) / 2 + jl;
+          dfloat s{0.f, 0.f};
+#pragma unroll 8
+          for (int r = 0; r < 32; r++)
+            s = df_fma_acc(s, red[r * RS + kj], red[r * RS + NKJ + il]);
+          acc[e] += to_double(df_norm(s));
+        }
+        __syncwarp();
+      }
+    }
+    __syncwarp();
+    double *dst = out + a.coef_off[t];
+    for (int e = lane; e < nco; e += 32)
+      dst[e] = acc[e];
+    if (a.task_cycles && lane == 0)
+      a.task_cycles[t] = clock64() - t0;
+    __syncwarp();
+  }
+}
+
+template <typename T, int LPB>
+const void *gen_kernel(bool collocate) {
+  if constexpr (std::is_same<T, dfloat>::value)
+    return collocate ? (const void *)collocate_general_df<LPB>
+                     : (const void *)integrate_general_df<LPB>;
+  else
+    return collocate ? (const void *)collocate_general<T, LPB>
+                     : (const void *)integrate_general<T, LPB>;
+}
+
 template <typename T, int LPB>
 void launch_gen(const GridArgs &a, bool collocate, int njmax, LaunchCfg &cfg, cudaStream_t s) {
   const size_t per_warp = GenSmem<T, LPB>::bytes(njmax);
@@ -477,26 +820,34 @@ void launch_gen(const GridArgs &a, bool collocate, int njmax, LaunchCfg &cfg, cu
   if (cfg.warps > 0 && cfg.warps < nw)
     nw = cfg.warps;
   const size_t smem = nw * per_warp;
-  const void *k = collocate ? (const void *)collocate_general<T, LPB>
-                            : (const void *)integrate_general<T, LPB>;
-  set_smem((const void *)k, smem);
+  const void *k = gen_kernel<T, LPB>(collocate);
+  set_smem(k, smem);
   const int nb = cfg.blocks > 0 ? cfg.blocks : cfg_blocks(cfg, persistent_blocks(k, 32 * nw, smem));
   cfg.warps = nw;
   cfg.blocks = nb;
-  if (collocate)
-    collocate_general<T, LPB><<<nb, 32 * nw, smem, s>>>(a, njmax);
-  else
-    integrate_general<T, LPB><<<nb, 32 * nw, smem, s>>>(a, njmax);
+  if constexpr (std::is_same<T, dfloat>::value) {
+    if (collocate)
+      collocate_general_df<LPB><<<nb, 32 * nw, smem, s>>>(a, njmax);
+    else
+      integrate_general_df<LPB><<<nb, 32 * nw, smem, s>>>(a, njmax);
+  } else {
+    if (collocate)
+      collocate_general<T, LPB><<<nb, 32 * nw, smem, s>>>(a, njmax);
+    else
+      integrate_general<T, LPB><<<nb, 32 * nw, smem, s>>>(a, njmax);
+  }
   count_launch();
 }
 
-void launch_gen_any(const GridArgs &a, bool collocate, bool fp32, int lpb, int njmax,
+void launch_gen_any(const GridArgs &a, bool collocate, int arith, int lpb, int njmax,
                     LaunchCfg &cfg, cudaStream_t s) {
   switch (lpb) {
 #define GB_CASE(LP)                                                            \
   case LP:                                                                     \
-    if (fp32)                                                                  \
+    if (arith == ARITH_FP32)                                                   \
       launch_gen<float, LP>(a, collocate, njmax, cfg, s);                      \
+    else if (arith == ARITH_MIXED)                                             \
+      launch_gen<dfloat, LP>(a, collocate, njmax, cfg, s);                     \
     else                                                                       \
       launch_gen<double, LP>(a, collocate, njmax, cfg, s);                     \
     break;
@@ -509,12 +860,12 @@ void launch_gen_any(const GridArgs &a, bool collocate, bool fp32, int lpb, int n
 
 void launch_collocate_general_impl(const GridArgs &a, int arith, int lpb, int njmax,
                                    LaunchCfg &cfg, cudaStream_t s) {
-  launch_gen_any(a, true, arith == ARITH_FP32, lpb, njmax, cfg, s);
+  launch_gen_any(a, true, arith, lpb, njmax, cfg, s);
 }
 
 void launch_integrate_general_impl(const GridArgs &a, int arith, int lpb, int njmax,
                                    LaunchCfg &cfg, cudaStream_t s) {
-  launch_gen_any(a, false, arith == ARITH_FP32, lpb, njmax, cfg, s);
+  launch_gen_any(a, false, arith, lpb, njmax, cfg, s);
 }
 
 } // namespace gb300

@@ -106,6 +106,61 @@ __device__ __forceinline__ double to_double(dfloat a) { return (double)a.h + (do
 __device__ __forceinline__ double to_double(double a) { return a; }
 __device__ __forceinline__ double to_double(float a) { return (double)a; }
 
+// a + b for plain floats, exact (Knuth's TwoSum)
+__device__ __forceinline__ dfloat df_two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return dfloat{s, (a - (s - bb)) + (b - bb)};
+}
+
+// a + b with b a plain float
+__device__ __forceinline__ dfloat df_add1(dfloat a, float b) {
+  const dfloat s = df_two_sum(a.h, b);
+  const float t = s.l + a.l;
+  const float h = s.h + t;
+  return dfloat{h, t - (h - s.h)};
+}
+
+// exp(-x) for a dfloat x >= 0, to ~1e-14 relative for x <= 40, following
+// Tang's table-driven method (P. T. P. Tang, ACM TOMS 15 (1989) 144-157):
+//   x = k ln2/64 + t, |t| <= ln2/128,  exp(-x) = 2^(-k/64) exp(-t),
+// with k = 64 m + j, 2^(-j/64) from a 64-entry dfloat table (tab[j]) and
+// exp(-t) from its Taylor polynomial to degree 5 (remainder below 4e-17).
+// ln2/64 is split Cody-Waite style into L0 (11 significant bits, so k L0 is
+// exact for k < 2^13) and two smaller parts.  Results below 2^-126 are
+// returned as zero.
+namespace dfexp {
+constexpr double kL = 0.69314718055994530942 / 64.0;
+constexpr float kL0 = (float)((double)(long long)(kL * 131072.0 + 0.5) / 131072.0);
+constexpr float kL1 = (float)(kL - (double)kL0);
+constexpr float kL2 = (float)(kL - (double)kL0 - (double)kL1);
+constexpr float kInvL = (float)(64.0 / 0.69314718055994530942);
+} // namespace dfexp
+
+__device__ __forceinline__ dfloat df_exp_neg(dfloat x, const float2 *tab) {
+  if (!(x.h < 87.0f))
+    return dfloat{0.f, 0.f};
+  const float kf = rintf(x.h * dfexp::kInvL);
+  const int k = (int)kf;
+  // t = x - k ln2/64
+  const float th = fmaf(-kf, dfexp::kL0, x.h); // exact (Sterbenz)
+  dfloat t = df_two_sum(th, x.l);
+  const float p = kf * dfexp::kL1;
+  const float pe = fmaf(kf, dfexp::kL1, -p) + kf * dfexp::kL2;
+  t = df_add(t, dfloat{-p, -pe});
+  // exp(s), s = -t: 1 + s + s^2 (1/2 + s (1/6 + s (1/24 + s/120)))
+  const dfloat s{-t.h, -t.l};
+  const float c = fmaf(s.h, fmaf(s.h, 1.0f / 120.0f, 1.0f / 24.0f), 1.0f / 6.0f);
+  const dfloat u = df_two_sum(0.5f, s.h * c);
+  dfloat r = df_add(s, df_mul(df_mul(s, s), u));
+  r = df_add(dfloat{1.f, 0.f}, r);
+  const float2 tj = tab[k & 63];
+  r = df_mul(r, dfloat{tj.x, tj.y});
+  const int m = k >> 6;
+  const float sc = __int_as_float((127 - m) << 23); // 2^-m, m <= 125
+  return dfloat{r.h * sc, r.l * sc};
+}
+
 __device__ __forceinline__ dfloat df_shfl_xor(dfloat v, int o) {
   return dfloat{__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
 }

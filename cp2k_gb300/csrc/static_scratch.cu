@@ -274,7 +274,6 @@ GB300_API int grid_gb300_collocate_pgf_product_static(
   co.func = func;
   co.d = dl;
   co.levels = (const LevelSet *)(dev + o_levels);
-  co.general_fp64 = 0;
   co.dhtab = (const double *)(dev + o_dhtab);
   launch_coefficients(co, ARITH_FP64, (int)coef_words(la_max + dl.la_max, lb_max + dl.lb_max), s);
 
