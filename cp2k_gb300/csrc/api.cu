@@ -492,34 +492,43 @@ void build_sphere(const LevelDesc &L, double disr, SphereHdr &h, std::vector<int
   tab.insert(tab.end(), jx.begin(), jx.end());
 }
 
+// LU factorisation with partial pivoting of M[c][d] = dh[d][c] per level:
+// P M = L D U with L unit lower, U unit upper, (P x)_i = x_pi(i)
 void build_dh_table(const LevelSet &ls, std::vector<double> &tab) {
   tab.assign(dh_table_size(ls.nlevels), 0.0);
-  double f = 1.0;
-  for (int n = 0; n < kPowN; n++) {
-    if (n > 1)
-      f *= n;
-    tab[n] = f;
-    tab[kPowN + n] = 1.0 / f;
-  }
-  for (int l = 0; l < ls.nlevels; l++)
-    for (int c = 0; c < 3; c++) {
-      double pw[3][kPowN];
-      for (int d = 0; d < 3; d++) {
-        double p = 1.0;
-        for (int n = 0; n < kPowN; n++) {
-          pw[d][n] = p;
-          p *= ls.lv[l].dh[3 * d + c];
-        }
+  for (int l = 0; l < ls.nlevels; l++) {
+    double A[3][3];
+    int pi[3] = {0, 1, 2};
+    for (int c = 0; c < 3; c++)
+      for (int d = 0; d < 3; d++)
+        A[c][d] = ls.lv[l].dh[3 * d + c];
+    for (int k = 0; k < 3; k++) {
+      int p = k;
+      for (int i = k + 1; i < 3; i++)
+        if (std::fabs(A[i][k]) > std::fabs(A[p][k]))
+          p = i;
+      if (A[p][k] == 0.0)
+        fail("singular grid spacing matrix on level %d", l);
+      std::swap(A[k], A[p]);
+      std::swap(pi[k], pi[p]);
+      for (int i = k + 1; i < 3; i++) {
+        A[i][k] /= A[k][k];
+        for (int j = k + 1; j < 3; j++)
+          A[i][j] -= A[i][k] * A[k][j];
       }
-      double *W = &tab[2 * kPowN + ((size_t)l * 3 + c) * kNW];
-      for (int n = 0; n <= GB300_LP_MAX; n++)
-        for (int i = 0; i <= n; i++)
-          for (int j = 0; j <= n - i; j++) {
-            const int k = n - i - j;
-            W[coset(i, j, k)] = pw[0][i] * pw[1][j] * pw[2][k] *
-                                (tab[kPowN + i] * tab[kPowN + j] * tab[kPowN + k]);
-          }
     }
+    double *t = &tab[(size_t)l * kLatTab];
+    for (int i = 0; i < 3; i++) {
+      t[i] = pi[i];
+      t[6 + i] = A[i][i];
+    }
+    t[3] = A[1][0];
+    t[4] = A[2][0];
+    t[5] = A[2][1];
+    t[9] = A[0][2] / A[0][0];
+    t[10] = A[1][2] / A[1][1];
+    t[11] = A[0][1] / A[0][0];
+  }
 }
 
 void build_sphere_points(SphereHdr &h, const std::vector<int16_t> &tab, std::vector<int> &pts,

@@ -259,15 +259,22 @@ __device__ T cxyz_cab_term(const T *cxyz, const T *alpha, int la, int lb, int lp
   return s;
 }
 
-// General path: C_xyz (Cartesian, about P) <-> C_ijk (lattice indices)
-// through x_c = sum_d u_d dh[d][c] (grid_ref_collint.h:698-762).  x^lx y^ly
-// z^lz expands into the product of three multinomials; with the weights
-// W_c(i, j, k) = dh[0][c]^i dh[1][c]^j dh[2][c]^k / (i! j! k!) from a table
-// (build_dh_table) the monomial (lx, ly, lz) maps onto the lattice monomial
-// (i, j, k) = sum over the directions' splits with weight
-// lx! ly! lz! W_x W_y W_z.  Both directions are written as gathers (one
-// output per lane, no atomics) in the arithmetic type T of the kernel, with
-// the table in that type.
+// General path: C_xyz (Cartesian, about P) <-> C_ijk (lattice indices).
+// The polynomial p(r) in Cartesian offsets becomes q(u) = p(M u) in lattice
+// offsets, M[c][d] = dh[d][c] (grid_ref_collint.h:698-762 expands every
+// monomial into the product of three multinomials).  Here M is factorised on
+// the host, per level, with partial pivoting, M = P^T L D U, and the change of
+// variables runs as eight elementary substitutions, each a gather over the
+// coefficient vector (one output per lane, no atomics):
+//   permutation  x = P^T y         q[e] = p[l] with l[pi(i)] = e[i]
+//   shear        y_r = z_r + b z_c  q[e] = sum_k C(e_r + k, k) b^k p[e + k (^r - ^c)]
+//   scaling      y_r = d_r z_r      q[e] = p[e] d_0^e_0 d_1^e_1 d_2^e_2
+// in the order P^T, L = S(1,0) S(2,0) S(2,1), D, U = S(0,2) S(1,2) S(0,1).
+// A shear costs ncoset(lp) (mean exponent + 1) terms, against the
+// O(lp^6) terms of the full multinomial expansion.  Integrate applies the
+// transposed steps in reverse order.  The table (build_dh_table) holds per
+// level: pi (3 entries), L10, L20, L21, D0, D1, D2, U02, U12, U01, in the
+// arithmetic type T of the kernel.
 template <typename T> __device__ __forceinline__ const T *dh_tab(const double *d, const float *f,
                                                                  const float2 *df);
 template <> __device__ __forceinline__ const double *dh_tab<double>(const double *d, const float *,
@@ -283,60 +290,121 @@ template <> __device__ __forceinline__ const dfloat *dh_tab<dfloat>(const double
   return reinterpret_cast<const dfloat *>(df);
 }
 
-// adjoint: C_xyz[lx, ly, lz] from C_ijk
-template <typename T>
-__device__ T cxyz_from_cijk(const T *tab, int level, int lp, int lx, int ly, int lz,
-                            const T *cijk) {
-  using M = Num<T>;
-  const T *F = tab;
-  const T *Wx = tab + 2 * kPowN + (size_t)level * 3 * kNW, *Wy = Wx + kNW, *Wz = Wy + kNW;
-  T acc = M::zero();
-  for (int ix = 0; ix <= lx; ix++)
-    for (int jx = 0; jx <= lx - ix; jx++) {
-      const int kx = lx - ix - jx;
-      const T wx = Wx[coset(ix, jx, kx)];
-      for (int iy = 0; iy <= ly; iy++)
-        for (int jy = 0; jy <= ly - iy; jy++) {
-          const int ky = ly - iy - jy;
-          const T wxy = M::mul(wx, Wy[coset(iy, jy, ky)]);
-          T sz = M::zero();
-          for (int iz = 0; iz <= lz; iz++)
-            for (int jz = 0; jz <= lz - iz; jz++) {
-              const int kz = lz - iz - jz;
-              sz = M::fma_acc(sz, Wz[coset(iz, jz, kz)],
-                              cijk[cidx(kx + ky + kz, jx + jy + jz, ix + iy + iz, lp)]);
-            }
-          acc = M::fma_acc(acc, wxy, M::norm(sz));
-        }
-    }
-  return M::mul(M::norm(acc), M::mul(M::mul(F[lx], F[ly]), F[lz]));
+__device__ __forceinline__ int pick3(int i, int a, int b, int c) {
+  return i == 0 ? a : (i == 1 ? b : c);
 }
 
-// forward: C_ijk[iu, ju, ku] (lattice exponents of directions 0, 1, 2) from
-// g[e] = lx! ly! lz! C_xyz[e]
+// shear y_r = z_r + b z_c (adjoint: its transpose) from in to out
 template <typename T>
-__device__ T cijk_from_cxyz(const T *tab, int level, int lp, int iu, int ju, int ku,
-                            const T *g) {
+__device__ void lat_shear(const T *in, T *out, int lp, int r, int c, T b, bool adjoint,
+                          const Grp &g) {
   using M = Num<T>;
-  const T *Wx = tab + 2 * kPowN + (size_t)level * 3 * kNW, *Wy = Wx + kNW, *Wz = Wy + kNW;
-  T acc = M::zero();
-  for (int ix = 0; ix <= iu; ix++)
-    for (int jx = 0; jx <= ju; jx++)
-      for (int kx = 0; kx <= ku; kx++) {
-        const T wx = Wx[coset(ix, jx, kx)];
-        for (int iy = 0; iy <= iu - ix; iy++)
-          for (int jy = 0; jy <= ju - jx; jy++) {
-            T s = M::zero();
-            for (int ky = 0; ky <= ku - kx; ky++) {
-              const int iz = iu - ix - iy, jz = ju - jx - jy, kz = ku - kx - ky;
-              const T w = M::mul(Wy[coset(iy, jy, ky)], Wz[coset(iz, jz, kz)]);
-              s = M::fma_acc(s, w,
-                             g[cidx(iz + jz + kz, iy + jy + ky, ix + jx + kx, lp)]);
-            }
-            acc = M::fma_acc(acc, wx, M::norm(s));
-          }
+  const int n = ncoset(lp);
+  // source exponents move by k (d0, d1, d2) per term
+  const int s = adjoint ? -1 : 1;
+  const int d0 = s * ((r == 0) - (c == 0)), d1 = s * ((r == 1) - (c == 1)),
+            d2 = s * ((r == 2) - (c == 2));
+  for (int e = g.lane; e < n; e += g.n) {
+    int l2, l1, l0;
+    decode_cidx(e, lp, l2, l1, l0);
+    const int lr = pick3(r, l0, l1, l2);
+    const int kmax = adjoint ? lr : pick3(c, l0, l1, l2);
+    T acc = M::zero(), pw = T(1);
+    for (int k = 0; k <= kmax; k++) {
+      const float cb = adjoint ? c_binom[lr][k] : c_binom[lr + k][k];
+      acc = M::fma_acc(acc, M::mul(pw, T(cb)),
+                       in[cidx(l2 + k * d2, l1 + k * d1, l0 + k * d0, lp)]);
+      pw = M::mul(pw, b);
+    }
+    out[e] = M::norm(acc);
+  }
+}
+
+template <typename T>
+__device__ void lat_scale(const T *in, T *out, int lp, const T *dd, const Grp &g) {
+  using M = Num<T>;
+  const int n = ncoset(lp);
+  for (int e = g.lane; e < n; e += g.n) {
+    int l2, l1, l0;
+    decode_cidx(e, lp, l2, l1, l0);
+    T v = in[e];
+    for (int k = 0; k < l0; k++)
+      v = M::mul(v, dd[0]);
+    for (int k = 0; k < l1; k++)
+      v = M::mul(v, dd[1]);
+    for (int k = 0; k < l2; k++)
+      v = M::mul(v, dd[2]);
+    out[e] = v;
+  }
+}
+
+// permutation (forward: q[e] = p[l], l[pi(i)] = e[i]; adjoint: its inverse)
+template <typename T>
+__device__ void lat_perm(const T *in, T *out, int lp, const int pi[3], bool adjoint,
+                         const Grp &g) {
+  const int n = ncoset(lp);
+  for (int e = g.lane; e < n; e += g.n) {
+    int e2, e1, e0;
+    decode_cidx(e, lp, e2, e1, e0);
+    int l0, l1, l2;
+    if (!adjoint) {
+      // l[pi(i)] = e[i]
+      l0 = pick3(pi[0] == 0 ? 0 : (pi[1] == 0 ? 1 : 2), e0, e1, e2);
+      l1 = pick3(pi[0] == 1 ? 0 : (pi[1] == 1 ? 1 : 2), e0, e1, e2);
+      l2 = pick3(pi[0] == 2 ? 0 : (pi[1] == 2 ? 1 : 2), e0, e1, e2);
+    } else {
+      // l[i] = e[pi(i)]
+      l0 = pick3(pi[0], e0, e1, e2);
+      l1 = pick3(pi[1], e0, e1, e2);
+      l2 = pick3(pi[2], e0, e1, e2);
+    }
+    out[e] = in[cidx(l2, l1, l0, lp)];
+  }
+}
+
+// C_ijk (forward) or C_xyz (adjoint) from the vector in a; b is scratch of
+// the same size.  Returns the buffer holding the result (a or b).
+template <typename T>
+__device__ T *lattice_transform(const T *tab, int level, int lp, bool adjoint, T *a, T *b,
+                                const Grp &g) {
+  const T *t = tab + (size_t)level * kLatTab;
+  const int pi[3] = {(int)Num<T>::to_double(t[0]), (int)Num<T>::to_double(t[1]),
+                     (int)Num<T>::to_double(t[2])};
+  // forward steps: perm, S(1,0,L10), S(2,0,L20), S(2,1,L21), D, S(0,2,U02),
+  // S(1,2,U12), S(0,1,U01)
+  const int sr[6] = {1, 2, 2, 0, 1, 0}, sc[6] = {0, 0, 1, 2, 2, 1};
+  const int sb[6] = {3, 4, 5, 9, 10, 11};
+  T *x = a, *y = b;
+  auto swap = [&]() {
+    T *tmp = x;
+    x = y;
+    y = tmp;
+    g.sync();
+  };
+  if (!adjoint) {
+    lat_perm<T>(x, y, lp, pi, false, g);
+    swap();
+    for (int s = 0; s < 6; s++) {
+      if (s == 3) {
+        lat_scale<T>(x, y, lp, t + 6, g);
+        swap();
       }
-  return M::norm(acc);
+      lat_shear<T>(x, y, lp, sr[s], sc[s], t[sb[s]], false, g);
+      swap();
+    }
+  } else {
+    for (int s = 5; s >= 0; s--) {
+      lat_shear<T>(x, y, lp, sr[s], sc[s], t[sb[s]], true, g);
+      swap();
+      if (s == 3) {
+        lat_scale<T>(x, y, lp, t + 6, g);
+        swap();
+      }
+    }
+    lat_perm<T>(x, y, lp, pi, true, g);
+    swap();
+  }
+  return x;
 }
 
 // Per-group shared memory of the coefficient / post kernels in 8-byte words:
@@ -428,29 +496,17 @@ __device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *w
     int pz, py, px;
     decode_cidx(e, lp, pz, py, px);
     const U v = cab_cxyz_term<U>(cab, n1, alpha, la_max, lb_max, lp, px, py, pz) * pref;
-    if (general) {
+    if (general)
       cxyz[e] = v;
-      cijk[e] = U(0);
-    } else {
+    else
       store_coef<Tout, U>(a.coef, (size_t)a.coef_off[t] + e, v);
-    }
   }
   if (general) {
-    using M = Num<U>;
-    const U *tab = dh_tab<U>(a.dhtab, a.dhtab_f, a.dhtab_df);
     g.sync();
-    for (int e = g.lane; e < nco; e += g.n) { // g = lx! ly! lz! C_xyz, in place
-      int lz, ly, lx;
-      decode_cidx(e, lp, lz, ly, lx);
-      cxyz[e] = M::mul(cxyz[e], M::mul(M::mul(tab[lx], tab[ly]), tab[lz]));
-    }
-    g.sync();
-    for (int e = g.lane; e < nco; e += g.n) {
-      int ku, ju, iu;
-      decode_cidx(e, lp, ku, ju, iu);
-      store_coef<Tout, U>(a.coef, (size_t)a.coef_off[t] + e,
-                          cijk_from_cxyz<U>(tab, d.level, lp, iu, ju, ku, cxyz));
-    }
+    const U *cl = lattice_transform<U>(dh_tab<U>(a.dhtab, a.dhtab_f, a.dhtab_df), d.level, lp,
+                                       false, cxyz, cijk, g);
+    for (int e = g.lane; e < nco; e += g.n)
+      store_coef<Tout, U>(a.coef, (size_t)a.coef_off[t] + e, cl[e]);
   }
   g.sync();
 }
@@ -542,15 +598,9 @@ __device__ void post_task(const PostArgs &a, int t, const TaskDesc &d, double *w
       cxyz[e] = U(src[e]);
   }
   g.sync();
-  if (general) {
-    const U *tab = dh_tab<U>(a.dhtab, a.dhtab_f, a.dhtab_df);
-    for (int e = g.lane; e < nco; e += g.n) {
-      int lz, ly, lx;
-      decode_cidx(e, lp, lz, ly, lx);
-      cxyz[e] = cxyz_from_cijk<U>(tab, d.level, lp, lx, ly, lz, cijk);
-    }
-    g.sync();
-  }
+  const U *cx = general ? lattice_transform<U>(dh_tab<U>(a.dhtab, a.dhtab_f, a.dhtab_df),
+                                               d.level, lp, true, cijk, cxyz, g)
+                        : cxyz;
   const double *ra = a.atom_pos + 3 * d.iatom;
   double rb[3];
   for (int i = 0; i < 3; i++)
@@ -559,7 +609,7 @@ __device__ void post_task(const PostArgs &a, int t, const TaskDesc &d, double *w
   const U pref = U(d.prefexp);
   for (int e = g.lane; e < m1 * m2; e += g.n) {
     const Orb oa = orb_of_index(e % m1), ob = orb_of_index(e / m1);
-    cab[e] = cxyz_cab_term<U>(cxyz, alpha, la_max, lb_max, lp, oa, ob) * pref;
+    cab[e] = cxyz_cab_term<U>(cx, alpha, la_max, lb_max, lp, oa, ob) * pref;
   }
   g.sync();
   VabCtx<U> x{cab, m1, U(d.zeta), U(d.zetb), {U(d.rab[0]), U(d.rab[1]), U(d.rab[2])}};

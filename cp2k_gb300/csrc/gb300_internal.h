@@ -301,14 +301,11 @@ void build_sphere(const LevelDesc &L, double disr, SphereHdr &h,
 void build_sphere_points(SphereHdr &h, const std::vector<int16_t> &tab, std::vector<int> &pts,
                          std::vector<int> &ploff);
 
-// Table for the general path's C_xyz <-> C_ijk transform: n! and 1/n! for
-// n < kPowN, then per level the powers dh[c]^n (c = 0..8 row-major, n < kPowN)
-constexpr int kPowN = GB300_LP_MAX + 1;
-constexpr int kNW = (GB300_LP_MAX + 1) * (GB300_LP_MAX + 2) * (GB300_LP_MAX + 3) / 6;
-// n!, 1/n! (kPowN each), then per level and Cartesian direction c the
-// multinomial weights W_c(i, j, k) = dh[0][c]^i dh[1][c]^j dh[2][c]^k / (i! j! k!)
-// at coset(i, j, k), i + j + k <= GB300_LP_MAX
-inline size_t dh_table_size(int nlevels) { return 2 * kPowN + (size_t)nlevels * 3 * kNW; }
+// Table for the general path's C_xyz <-> C_ijk transform: per level the
+// pivoted factorisation M = P^T L D U of M[c][d] = dh[d][c] as kLatTab
+// values: pi(0..2), L10, L20, L21, D0, D1, D2, U02, U12, U01
+constexpr int kLatTab = 12;
+inline size_t dh_table_size(int nlevels) { return (size_t)nlevels * kLatTab; }
 void build_dh_table(const LevelSet &ls, std::vector<double> &tab);
 
 // counts launches for grid_gb300_kernel_launches()
