@@ -217,23 +217,17 @@ __device__ T cab_cxyz_term(const T *cab, int n1, const T *alpha, int la, int lb,
   auto A = [&](int d, int xb, int xa, int l) {
     return alpha[((size_t)(d * nb + xb) * na + xa) * P + l];
   };
+  // loop bounds visit only the pairs with a_d + b_d >= p_d
   T s = T(0);
   for (int az = 0; az <= la; az++)
-    for (int bz = 0; bz <= lb; bz++) {
-      if (az + bz < pz)
-        continue;
+    for (int bz = max(0, pz - az); bz <= lb; bz++) {
       const T wz = A(2, bz, az, pz);
       for (int ay = 0; ay <= la - az; ay++)
-        for (int by = 0; by <= lb - bz; by++) {
-          if (ay + by < py)
-            continue;
+        for (int by = max(0, py - ay); by <= lb - bz; by++) {
           const T wyz = wz * A(1, by, ay, py);
           for (int ax = 0; ax <= la - az - ay; ax++)
-            for (int bx = 0; bx <= lb - bz - by; bx++) {
-              if (ax + bx < px)
-                continue;
+            for (int bx = max(0, px - ax); bx <= lb - bz - by; bx++)
               s += wyz * A(0, bx, ax, px) * cab[coset(bx, by, bz) * n1 + coset(ax, ay, az)];
-            }
         }
     }
   return s;

@@ -59,6 +59,34 @@ def test_sample_task_fp64(G, O, name):
     ot.close()
 
 
+@pytest.mark.parametrize("name", SAMPLE_TASKS)
+def test_sample_task_double_float(G, O, name):
+    """Each recorded CP2K task in the mixed mode with every task in the
+    double-float class (threshold 0): the orthorhombic and the general
+    double-float kernels, border masks included (general_subpatch*,
+    general_overflow), within the mixed mode's stated bounds (1e-9 for grids
+    and hab, 1e-7 for forces and virial)."""
+    from cp2k_gb300.tasklist import single_task_list
+    d = load_digests()[name]
+    t = digest_task(d)
+    inp = single_task_list(t)
+    tl = G.GridTaskList(inp, precision=G.MIXED)
+    tl.set_mixed_threshold(0.0)
+    ot = O.OracleTaskList(inp)
+    pab_c = (0.5 * t["rscale"] * t["pab"]).ravel()
+    g_ora = ot.collocate(t["func"], pab_c)[0]
+    assert rel_diff(tl.collocate(t["func"], pab_c)[0], g_ora) < 1e-9
+    tau = t["func"] == 200
+    pab_i = (0.5 * t["pab"]).ravel()
+    hab, f, v = tl.integrate([g_ora], pab_i, compute_tau=tau, forces=True, virial=True)
+    hab_o, f_o, v_o = ot.integrate([g_ora], pab_i, compute_tau=tau, forces=True, virial=True)
+    assert rel_diff(hab, hab_o) < 1e-9
+    assert rel_diff(f, f_o) < 1e-7
+    assert rel_diff(v, v_o) < 1e-7
+    tl.close()
+    ot.close()
+
+
 # The triclinic l<=4 case with compute_tau reaches contraction order 11 on
 # |hab| ~ 2e3: two FP64 evaluation orders differ there by up to ~7e-12
 # relative (the oracle and CP2K's REF backend themselves differ by 1.3e-12),
