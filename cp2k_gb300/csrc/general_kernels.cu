@@ -115,18 +115,93 @@ __device__ __forceinline__ int2 row_bounds(int j, int k, const GenTask &g, doubl
                    (int)floor(__dmul_rn(__dadd_rn(-b, sq), inv2a)));
 }
 
+// The same bounds from a double-float evaluation, when that evaluation
+// decides them: it carries an error bound (first order, with generous
+// constants; eps below covers the dfloat arithmetic, the rounding of the
+// inputs and the reference's own FP64 rounding) and answers only when the
+// sign of the discriminant and both roots' floor/ceil are certain under it.
+// Otherwise the caller falls back to row_bounds.  This keeps the visited
+// points identical while moving the per-row work off the FP64 pipe.
+struct RowFast {
+  dfloat base[3], h0[3], h1[3], h2[3]; // v_c = base_c + j h1_c + k h2_c
+  dfloat a4, inv2a, r2;                // 4 |h0|^2, 1 / (2 |h0|^2), radius^2
+  float a, habs0;                      // |h0|^2, sum_c |h0_c|
+};
+
+__device__ __forceinline__ void row_fast_setup(const GenTask &g, double radius, RowFast &f) {
+  double a = 0.0;
+  float habs0 = 0.f;
+  for (int c = 0; c < 3; c++) {
+    f.base[c] = df_make(-g.gp[0] * g.h[c] - g.gp[1] * g.h[3 + c] - g.gp[2] * g.h[6 + c]);
+    f.h0[c] = df_make(g.h[c]);
+    f.h1[c] = df_make(g.h[3 + c]);
+    f.h2[c] = df_make(g.h[6 + c]);
+    a += g.h[c] * g.h[c];
+    habs0 += fabsf((float)g.h[c]);
+  }
+  f.a4 = df_make(4.0 * a);
+  f.inv2a = df_make(1.0 / (2.0 * a));
+  f.r2 = df_make(radius * radius);
+  f.a = (float)a;
+  f.habs0 = habs0;
+}
+
+// true with the bounds in rb when decided, false when the caller must use
+// the FP64 evaluation
+__device__ __forceinline__ bool row_bounds_fast(int j, int k, const RowFast &f, int2 &rb) {
+  constexpr float eps = 1.0e-12f;
+  const float fj = (float)j, fk = (float)k;
+  dfloat b{0.f, 0.f}, c{-f.r2.h, -f.r2.l};
+  float vs = 0.f, vv = 0.f;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const dfloat v = df_fma1(df_fma1(f.base[i], f.h1[i], fj), f.h2[i], fk);
+    vs += fabsf(f.base[i].h) + fabsf(fj * f.h1[i].h) + fabsf(fk * f.h2[i].h);
+    vv += v.h * v.h;
+    b = df_fma(b, v, f.h0[i]);
+    c = df_fma(c, v, v);
+  }
+  b = dfloat{2.f * b.h, 2.f * b.l};
+  const dfloat disc = df_fma(df_mul(dfloat{-f.a4.h, -f.a4.l}, c), b, b);
+  const float ab = fabsf(b.h), r2 = f.r2.h;
+  const float db = eps * (2.f * vs * f.habs0 + ab);
+  const float dc = eps * (2.f * vs * vs + vv + r2);
+  const float dd = 2.f * ab * db + f.a4.h * dc + eps * (ab * ab + f.a4.h * (vv + r2));
+  if (disc.h <= -2.f * dd) {
+    rb = make_int2(1, 0);
+    return true;
+  }
+  if (disc.h <= 2.f * dd)
+    return false;
+  // dfloat square root: one Newton step from the FP32 root
+  const float s0 = sqrtf(disc.h);
+  const float corr = (fmaf(-s0, s0, disc.h) + disc.l) * (0.5f / s0);
+  const dfloat sq = df_two_sum(s0, corr);
+  const float ds = dd / sqrtf(disc.h - dd) + eps * s0;
+  const float dx = (db + ds + eps * (ab + s0)) * f.inv2a.h;
+  const dfloat nb{-b.h, -b.l};
+  const dfloat x1 = df_mul(df_add(nb, dfloat{-sq.h, -sq.l}), f.inv2a);
+  const dfloat x2 = df_mul(df_add(nb, sq), f.inv2a);
+  const float m1 = 2.f * dx + eps * fabsf(x1.h) + fabsf(x1.l);
+  const float m2 = 2.f * dx + eps * fabsf(x2.h) + fabsf(x2.l);
+  if (fabsf(x1.h - rintf(x1.h)) <= m1 || fabsf(x2.h - rintf(x2.h)) <= m2)
+    return false;
+  rb = make_int2((int)ceilf(x1.h), (int)floorf(x2.h));
+  return true;
+}
+
 // Per-plane preparation shared by collocate and integrate: row bounds (and
 // for FP64 the e_jk factors) for every j of the box.
 template <typename T>
 __device__ __forceinline__ void plane_rows(int k, const GenTask &g, const LevelDesc &L,
                                            double radius, double zetp, int2 *rows,
-                                           double *ejk, int lane) {
+                                           double *ejk, int lane, const RowFast &f) {
   const int nj = g.imax[1] - g.imin[1] + 1;
   const double dk = (double)k - g.gp[2];
   for (int r = lane; r < nj; r += 32) {
     const int j = g.imin[1] + r;
     int2 rb = make_int2(1, 0);
-    if (gmap(j, 1, g, L) >= 0)
+    if (gmap(j, 1, g, L) >= 0 && !row_bounds_fast(j, k, f, rb))
       rb = row_bounds(j, k, g, radius);
     rows[r] = rb;
     if constexpr (std::is_same<T, double>::value) {
@@ -162,6 +237,8 @@ __global__ void __launch_bounds__(128) collocate_general(GridArgs a, int njmax) 
     const LevelDesc &L = a.levels.lv[d.level];
     GenTask g;
     gen_setup(d, L, g);
+    RowFast rowf;
+    row_fast_setup(g, d.radius, rowf);
     const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
     const int nj = g.imax[1] - g.imin[1] + 1;
     if (nj > njmax || lp > LPB) {
@@ -219,7 +296,7 @@ __global__ void __launch_bounds__(128) collocate_general(GridArgs a, int njmax) 
         if (kg < 0)
           continue;
         const double dk = (double)k - g.gp[2];
-        plane_rows<T>(k, g, L, d.radius, zetp, rows, ejk, lane);
+        plane_rows<T>(k, g, L, d.radius, zetp, rows, ejk, lane, rowf);
         // C_ij = sum_kl C_ijk dk^kl
         for (int e = lane; e < ntr; e += 32) {
           int jl = 0, rem = e;
@@ -329,6 +406,8 @@ __global__ void __launch_bounds__(128) integrate_general(GridArgs a, int njmax) 
     const LevelDesc &L = a.levels.lv[d.level];
     GenTask g;
     gen_setup(d, L, g);
+    RowFast rowf;
+    row_fast_setup(g, d.radius, rowf);
     const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
     const int nj = g.imax[1] - g.imin[1] + 1;
     if (nj > njmax || lp > LPB) {
@@ -373,7 +452,7 @@ __global__ void __launch_bounds__(128) integrate_general(GridArgs a, int njmax) 
         if (kg < 0)
           continue;
         const double dk = (double)k - g.gp[2];
-        plane_rows<T>(k, g, L, d.radius, zetp, rows, ejk, lane);
+        plane_rows<T>(k, g, L, d.radius, zetp, rows, ejk, lane, rowf);
         __syncwarp();
         const double eki = (sizeof(T) == 8)
                                ? exp(-zetp * (dk * dk * g.hh[2] + 2.0 * dk * di * g.h20))
@@ -545,6 +624,8 @@ __global__ void __launch_bounds__(128) collocate_general_df(GridArgs a, int njma
     const LevelDesc &L = a.levels.lv[d.level];
     GenTask g;
     gen_setup(d, L, g);
+    RowFast rowf;
+    row_fast_setup(g, d.radius, rowf);
     const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
     const int nj = g.imax[1] - g.imin[1] + 1;
     if (nj > njmax || lp > LPB) {
@@ -585,7 +666,7 @@ __global__ void __launch_bounds__(128) collocate_general_df(GridArgs a, int njma
         if (kg < 0)
           continue;
         const double dk = (double)k - g.gp[2];
-        plane_rows<dfloat>(k, g, L, d.radius, zetp, rows, ejk, lane);
+        plane_rows<dfloat>(k, g, L, d.radius, zetp, rows, ejk, lane, rowf);
         // C_ij = sum_kl C_ijk dk^kl (Horner in kl)
         const dfloat dkd = df_make(dk);
         for (int e = lane; e < ntr; e += 32) {
@@ -683,6 +764,8 @@ __global__ void __launch_bounds__(128) integrate_general_df(GridArgs a, int njma
     const LevelDesc &L = a.levels.lv[d.level];
     GenTask g;
     gen_setup(d, L, g);
+    RowFast rowf;
+    row_fast_setup(g, d.radius, rowf);
     const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
     const int nj = g.imax[1] - g.imin[1] + 1;
     if (nj > njmax || lp > LPB) {
@@ -719,7 +802,7 @@ __global__ void __launch_bounds__(128) integrate_general_df(GridArgs a, int njma
         if (kg < 0)
           continue;
         const double dk = (double)k - g.gp[2];
-        plane_rows<dfloat>(k, g, L, d.radius, zetp, rows, ejk, lane);
+        plane_rows<dfloat>(k, g, L, d.radius, zetp, rows, ejk, lane, rowf);
         __syncwarp();
         const DfLine line = df_line(di, dk, g, zetp, inv_hh1, fj0);
         dfloat wj[P];
