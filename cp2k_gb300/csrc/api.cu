@@ -248,6 +248,10 @@ namespace gb300 {
 struct Queue {
   int *d_idx = nullptr;
   int n = 0;
+  // general path: grid work items (task, first plane | planes << 16), large
+  // boxes split by planes over several warps; null when no task is split
+  int2 *d_items = nullptr;
+  int nitems = 0;
   int extent = 0; // ortho: max cube width; general: max j-range
   int general = 0, bucket = 0;
   int fp32 = 0; // mixed path: this queue runs in plain FP32
@@ -628,9 +632,12 @@ static void free_device(TaskList *t) {
   for (auto &kv : t->modes) {
     if (kv.second.d_coef_off)
       cudaFree(kv.second.d_coef_off);
-    for (auto &q : kv.second.queues)
+    for (auto &q : kv.second.queues) {
       if (q.d_idx)
         cudaFree(q.d_idx);
+      if (q.d_items)
+        cudaFree(q.d_items);
+    }
   }
   for (auto &e : t->ev)
     if (e)
@@ -1037,9 +1044,12 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase) {
       cost = (double)t->points[s] * (lp + 1) + 64.0 * (lp + 1) * (lp + 2);
     items[((g * kNumBuckets + b) * 2 + cls) * 2 + sz].push_back({cost, s});
   }
-  for (auto &q : m.queues)
+  for (auto &q : m.queues) {
     if (q.d_idx)
       cudaFree(q.d_idx);
+    if (q.d_items)
+      cudaFree(q.d_items);
+  }
   m.queues.clear();
   // heavier classes first: large cubes, then the arithmetic of the mode, FP32 last
   std::vector<int> keys;
@@ -1080,6 +1090,29 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase) {
     q.n = (int)idx.size();
     q.extent = ext;
     q.d_idx = dalloc_copy(idx);
+    if (q.general) {
+      // boxes of many points are split by planes (kSlicePoints points and at
+      // least kSlicePlanes planes per item), so a few large tasks still
+      // spread over the GPU; slices stay in the task's cost order
+      std::vector<int2> items;
+      bool split = false;
+      for (int s : idx) {
+        const TaskDesc &k = t->tasks[s];
+        const int nk = k.imax[2] - k.center[2] + 1;
+        const long long by_pts = (t->points[s] + kSlicePoints - 1) / kSlicePoints;
+        const int ns = (int)std::max<long long>(
+            1, std::min<long long>(by_pts, (nk + kSlicePlanes - 1) / kSlicePlanes));
+        split |= ns > 1;
+        for (int c = 0; c < ns; c++) {
+          const int k0 = (int)((long long)nk * c / ns), k1 = (int)((long long)nk * (c + 1) / ns);
+          items.push_back(make_int2(s, k0 | ((k1 - k0) << 16)));
+        }
+      }
+      if (split) {
+        q.nitems = (int)items.size();
+        q.d_items = dalloc_copy(items);
+      }
+    }
     m.queues.push_back(q);
   }
   m.sched_version = t->sched_version;
@@ -1165,6 +1198,7 @@ static void grid_launch(TaskList *t, const Queue &q, int phase, int arith, const
     in.general = q.general;
     in.lp_bucket = kBucketLp[q.bucket];
     in.ntasks = q.n;
+    in.work_items = q.d_items ? q.nitems : q.n;
     in.warps_per_block = cfg.warps;
     in.blocks = cfg.blocks;
     in.points = q.points;
@@ -1259,7 +1293,8 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
   int qi = 0;
   for (const Queue &q : m.queues) {
     ga.queue = q.d_idx;
-    ga.nqueue = q.n;
+    ga.items = q.d_items;
+    ga.nqueue = q.d_items ? q.nitems : q.n;
     ga.counter = t->d_counters + qi++;
     ga.coef_stride = q.fp32 ? 2 : 1;
     grid_launch(t, q, 0, q.fp32 ? (int)ARITH_FP32 : arith, ga, s);
@@ -1306,6 +1341,12 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
     launch_decontract(ca, s);
   }
   CK(cudaMemsetAsync(t->d_counters, 0, sizeof(int) * 64, s));
+  // split general tasks add their planes' partial coefficients
+  bool any_split = false;
+  for (const Queue &q : m.queues)
+    any_split |= q.d_items != nullptr;
+  if (any_split)
+    CK(cudaMemsetAsync(t->d_coef_int, 0, m.coef_total * 8, s));
   record_phase(t, 1, s);
   GridArgs ga{};
   ga.coef_stride = 1;
@@ -1327,7 +1368,8 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
   int qi = 0;
   for (const Queue &q : m.queues) {
     ga.queue = q.d_idx;
-    ga.nqueue = q.n;
+    ga.items = q.d_items;
+    ga.nqueue = q.d_items ? q.nitems : q.n;
     ga.counter = t->d_counters + qi++;
     ga.grid_stride = 1;
     // FP64: the grid; mixed: float2 pairs for the double-float class, dense

@@ -162,7 +162,8 @@ struct CoefArgs {
 struct GridArgs {
   const TaskDesc *tasks;
   const int *queue;
-  int nqueue;
+  const int2 *items;      // general path: (task, first plane | planes << 16), or null
+  int nqueue;             // tasks, or work items when items is set
   int *counter;           // work counter, zeroed before launch
   const int *coef_off;
   const void *coef;       // T* (collocate) ; double* out (integrate)
@@ -305,6 +306,9 @@ void build_sphere_points(SphereHdr &h, const std::vector<int16_t> &tab, std::vec
 // pivoted factorisation M = P^T L D U of M[c][d] = dh[d][c] as kLatTab
 // values: pi(0..2), L10, L20, L21, D0, D1, D2, U02, U12, U01
 constexpr int kLatTab = 12;
+// splitting of large general-path boxes into plane ranges (work items)
+constexpr long long kSlicePoints = 16384;
+constexpr int kSlicePlanes = 4;
 inline size_t dh_table_size(int nlevels) { return (size_t)nlevels * kLatTab; }
 void build_dh_table(const LevelSet &ls, std::vector<double> &tab);
 

@@ -86,6 +86,18 @@ __device__ __forceinline__ void gen_setup(const TaskDesc &d, const LevelDesc &L,
   g.h20 = dot(2, 0);
 }
 
+// one work item: a task, or a range of its box's planes
+struct WorkItem {
+  int t, k0, nk;
+};
+__device__ __forceinline__ WorkItem work_item(const GridArgs &a, int qi) {
+  if (a.items) {
+    const int2 it = a.items[qi];
+    return WorkItem{it.x, it.y & 0xffff, it.y >> 16};
+  }
+  return WorkItem{a.queue[qi], 0, INT_MAX / 2};
+}
+
 // grid index along dir for lattice index c, or -1 when outside the bounds
 __device__ __forceinline__ int gmap(int c, int dir, const GenTask &g, const LevelDesc &L) {
   const int v = imod(c - L.shift[dir], L.npts_global[dir]);
@@ -231,12 +243,14 @@ __global__ void __launch_bounds__(128) collocate_general(GridArgs a, int njmax) 
     qi = __shfl_sync(FULL, qi, 0);
     if (qi >= a.nqueue)
       break;
-    const int t = a.queue[qi];
+    const WorkItem w = work_item(a, qi);
+    const int t = w.t;
     const long long t0 = clock64();
     const TaskDesc d = a.tasks[t];
     const LevelDesc &L = a.levels.lv[d.level];
     GenTask g;
     gen_setup(d, L, g);
+    const int k_lo = g.imin[2] + w.k0, k_hi = min(g.imax[2], g.imin[2] + w.k0 + w.nk - 1);
     RowFast rowf;
     row_fast_setup(g, d.radius, rowf);
     const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
@@ -291,7 +305,7 @@ __global__ void __launch_bounds__(128) collocate_general(GridArgs a, int njmax) 
       for (int c = 0; c < 3; c++)
         rx[c] = (float)(di * g.h[c]);
 
-      for (int k = g.imin[2]; k <= g.imax[2]; k++) {
+      for (int k = k_lo; k <= k_hi; k++) {
         const int kg = gmap(k, 2, g, L);
         if (kg < 0)
           continue;
@@ -372,8 +386,8 @@ __global__ void __launch_bounds__(128) collocate_general(GridArgs a, int njmax) 
         __syncwarp();
       }
     }
-    if (a.task_cycles && lane == 0)
-      a.task_cycles[t] = clock64() - t0;
+    if (a.task_cycles && lane == 0) // summed over the task's work items
+      atomicAdd((unsigned long long *)&a.task_cycles[t], (unsigned long long)(clock64() - t0));
     __syncwarp();
   }
 }
@@ -400,12 +414,14 @@ __global__ void __launch_bounds__(128) integrate_general(GridArgs a, int njmax) 
     qi = __shfl_sync(FULL, qi, 0);
     if (qi >= a.nqueue)
       break;
-    const int t = a.queue[qi];
+    const WorkItem w = work_item(a, qi);
+    const int t = w.t;
     const long long t0 = clock64();
     const TaskDesc d = a.tasks[t];
     const LevelDesc &L = a.levels.lv[d.level];
     GenTask g;
     gen_setup(d, L, g);
+    const int k_lo = g.imin[2] + w.k0, k_hi = min(g.imax[2], g.imin[2] + w.k0 + w.nk - 1);
     RowFast rowf;
     row_fast_setup(g, d.radius, rowf);
     const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
@@ -447,7 +463,7 @@ __global__ void __launch_bounds__(128) integrate_general(GridArgs a, int njmax) 
       for (int e = 0; e < NKJ; e++)
         akj[e] = T(0);
 
-      for (int k = g.imin[2]; k <= g.imax[2]; k++) {
+      for (int k = k_lo; k <= k_hi; k++) {
         const int kg = gmap(k, 2, g, L);
         if (kg < 0)
           continue;
@@ -541,10 +557,14 @@ __global__ void __launch_bounds__(128) integrate_general(GridArgs a, int njmax) 
     }
     __syncwarp();
     double *dst = out + a.coef_off[t];
-    for (int e = lane; e < nco; e += 32)
-      dst[e] = acc[e];
-    if (a.task_cycles && lane == 0)
-      a.task_cycles[t] = clock64() - t0;
+    for (int e = lane; e < nco; e += 32) {
+      if (a.items) // plane ranges of one task add up (the buffer is zeroed)
+        atomicAdd(dst + e, acc[e]);
+      else
+        dst[e] = acc[e];
+    }
+    if (a.task_cycles && lane == 0) // summed over the task's work items
+      atomicAdd((unsigned long long *)&a.task_cycles[t], (unsigned long long)(clock64() - t0));
     __syncwarp();
   }
 }
@@ -618,12 +638,14 @@ __global__ void __launch_bounds__(128) collocate_general_df(GridArgs a, int njma
     qi = __shfl_sync(FULL, qi, 0);
     if (qi >= a.nqueue)
       break;
-    const int t = a.queue[qi];
+    const WorkItem w = work_item(a, qi);
+    const int t = w.t;
     const long long t0 = clock64();
     const TaskDesc d = a.tasks[t];
     const LevelDesc &L = a.levels.lv[d.level];
     GenTask g;
     gen_setup(d, L, g);
+    const int k_lo = g.imin[2] + w.k0, k_hi = min(g.imax[2], g.imin[2] + w.k0 + w.nk - 1);
     RowFast rowf;
     row_fast_setup(g, d.radius, rowf);
     const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
@@ -661,7 +683,7 @@ __global__ void __launch_bounds__(128) collocate_general_df(GridArgs a, int njma
           p = df_mul(p, dd);
         }
       }
-      for (int k = g.imin[2]; k <= g.imax[2]; k++) {
+      for (int k = k_lo; k <= k_hi; k++) {
         const int kg = gmap(k, 2, g, L);
         if (kg < 0)
           continue;
@@ -722,8 +744,8 @@ __global__ void __launch_bounds__(128) collocate_general_df(GridArgs a, int njma
         __syncwarp();
       }
     }
-    if (a.task_cycles && lane == 0)
-      a.task_cycles[t] = clock64() - t0;
+    if (a.task_cycles && lane == 0) // summed over the task's work items
+      atomicAdd((unsigned long long *)&a.task_cycles[t], (unsigned long long)(clock64() - t0));
     __syncwarp();
   }
 }
@@ -758,12 +780,14 @@ __global__ void __launch_bounds__(128) integrate_general_df(GridArgs a, int njma
     qi = __shfl_sync(FULL, qi, 0);
     if (qi >= a.nqueue)
       break;
-    const int t = a.queue[qi];
+    const WorkItem w = work_item(a, qi);
+    const int t = w.t;
     const long long t0 = clock64();
     const TaskDesc d = a.tasks[t];
     const LevelDesc &L = a.levels.lv[d.level];
     GenTask g;
     gen_setup(d, L, g);
+    const int k_lo = g.imin[2] + w.k0, k_hi = min(g.imax[2], g.imin[2] + w.k0 + w.nk - 1);
     RowFast rowf;
     row_fast_setup(g, d.radius, rowf);
     const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
@@ -797,7 +821,7 @@ __global__ void __launch_bounds__(128) integrate_general_df(GridArgs a, int njma
       for (int e = 0; e < NKJ; e++)
         akj[e] = dfloat{0.f, 0.f};
 
-      for (int k = g.imin[2]; k <= g.imax[2]; k++) {
+      for (int k = k_lo; k <= k_hi; k++) {
         const int kg = gmap(k, 2, g, L);
         if (kg < 0)
           continue;
@@ -876,10 +900,14 @@ __global__ void __launch_bounds__(128) integrate_general_df(GridArgs a, int njma
     }
     __syncwarp();
     double *dst = out + a.coef_off[t];
-    for (int e = lane; e < nco; e += 32)
-      dst[e] = acc[e];
-    if (a.task_cycles && lane == 0)
-      a.task_cycles[t] = clock64() - t0;
+    for (int e = lane; e < nco; e += 32) {
+      if (a.items) // plane ranges of one task add up (the buffer is zeroed)
+        atomicAdd(dst + e, acc[e]);
+      else
+        dst[e] = acc[e];
+    }
+    if (a.task_cycles && lane == 0) // summed over the task's work items
+      atomicAdd((unsigned long long *)&a.task_cycles[t], (unsigned long long)(clock64() - t0));
     __syncwarp();
   }
 }

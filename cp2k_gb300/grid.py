@@ -134,7 +134,7 @@ class LaunchInfo(C.Structure):
     _fields_ = [("phase", C.c_int), ("precision", C.c_int), ("general", C.c_int),
                 ("lp_bucket", C.c_int), ("ntasks", C.c_int), ("warps_per_block", C.c_int),
                 ("blocks", C.c_int), ("points", C.c_longlong), ("flops", C.c_double),
-                ("ms", C.c_double)]
+                ("ms", C.c_double), ("work_items", C.c_int)]
 
 
 def kernel_launches() -> int:
@@ -272,7 +272,7 @@ class GridTaskList:
     def launch_timings(self):
         """Per grid-kernel launch of the last call (launch timing enabled):
         list of dicts with phase, precision, general, lp_bucket, ntasks,
-        warps_per_block, blocks, points, flops, ms."""
+        warps_per_block, blocks, points, flops, ms, work_items."""
         n = lib().grid_gb300_launch_timings(self.impl, 0, None)
         arr = (LaunchInfo * max(n, 1))()
         lib().grid_gb300_launch_timings(self.impl, n, C.cast(arr, C.c_void_p))

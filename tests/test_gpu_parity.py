@@ -290,3 +290,33 @@ def test_high_l_and_contraction_fp64(G, O, lmax, random_sphi, funcs, tau):
     assert rel_diff(v1, v2) < TOL_DERIV
     tl.close()
     ot.close()
+
+
+def test_general_boxes_split_by_planes(G, O):
+    """Large general-path boxes are split into plane ranges, each a work item
+    of its own (integrate adds the ranges' partial coefficients); the split
+    runs give the oracle's results, in FP64 and in the double-float class."""
+    from cp2k_gb300 import workload as W
+    inp = W.config("c3_256atoms_triclinic", scale=0.12, seed=13)
+    pab = W.density_blocks(inp)
+    V = W.potential_grids(inp)
+    ot = O.OracleTaskList(inp)
+    g_ref = ot.collocate(100, pab)
+    h_ref, f_ref, v_ref = ot.integrate(V, pab, forces=True, virial=True)
+    for prec, tol, tol_d in ((G.FP64, 1e-11, TOL_DERIV), (G.MIXED, 1e-9, 1e-7)):
+        tl = G.GridTaskList(inp, precision=prec)
+        if prec == G.MIXED:
+            tl.set_mixed_threshold(0.0)
+        tl.set_launch_timing(True)
+        g = tl.collocate(100, pab)
+        info = [i for i in tl.launch_timings() if i["general"]]
+        assert any(i["work_items"] > i["ntasks"] for i in info)
+        assert max(rel_diff(a, b) for a, b in zip(g, g_ref)) < tol
+        h, f, v = tl.integrate(V, pab, forces=True, virial=True)
+        info = [i for i in tl.launch_timings() if i["general"]]
+        assert any(i["work_items"] > i["ntasks"] for i in info)
+        assert rel_diff(h, h_ref) < tol
+        assert rel_diff(f, f_ref) < tol_d
+        assert rel_diff(v, v_ref) < tol_d
+        tl.close()
+    ot.close()
