@@ -281,8 +281,8 @@ void launch_grid_split(const double *src, void *dst, size_t n, int arith,
 void launch_grid_fold_lo(double *g, const float *lo, size_t n, cudaStream_t s);
 
 // lp bucket limits of the templated grid kernels
-constexpr int kNumBuckets = 4;
-constexpr int kBucketLp[kNumBuckets] = {4, 6, 9, 16};
+constexpr int kNumBuckets = 5;
+constexpr int kBucketLp[kNumBuckets] = {4, 6, 9, 12, 16};
 inline int bucket_of(int lp) {
   for (int b = 0; b < kNumBuckets; b++)
     if (lp <= kBucketLp[b])

@@ -39,9 +39,10 @@ template <typename T> __device__ __forceinline__ T wsum(T v) {
 
 template <typename T, int LPB> struct GenSmem {
   static constexpr int P = LPB + 1;
-  static __host__ __device__ constexpr int red_stride() {
-    return ((P * (P + 1)) / 2 + P) | 1;
-  }
+  // the integrate fold passes KC (kl, jl) rows at a time
+  static constexpr int NKJ = (P * (P + 1)) / 2;
+  static constexpr int KC = NKJ < 32 ? NKJ : 32;
+  static __host__ __device__ constexpr int red_stride() { return (KC + P) | 1; }
   static __host__ __device__ size_t bytes(int nj) {
     size_t b = sizeof(double) * ncoset(LPB) + sizeof(double) * (size_t)nj; // acc, ejk
     b += sizeof(T) * (ncoset(LPB) + ntri(LPB));                            // coef, cij
@@ -528,31 +529,38 @@ __global__ void __launch_bounds__(128) integrate_general(GridArgs a, int njmax) 
           pk *= (T)dk;
         }
       }
-      // fold i and reduce over the warp through shared memory
+      // fold i and reduce over the warp through shared memory, KC rows of
+      // akj per pass
       {
-        constexpr int RS = GenSmem<T, LPB>::red_stride();
+        constexpr int KC = GenSmem<T, LPB>::KC, RS = GenSmem<T, LPB>::red_stride();
         T *rl = red + lane * RS;
-#pragma unroll
-        for (int e = 0; e < NKJ; e++)
-          rl[e] = akj[e];
         T pi = xin ? T(1) : T(0);
 #pragma unroll
         for (int l = 0; l < P; l++) {
-          rl[NKJ + l] = pi;
+          rl[KC + l] = pi;
           pi *= (T)di;
         }
-        __syncwarp();
-        for (int e = lane; e < nco; e += 32) {
-          int kl, jl, il;
-          decode_cidx(e, lp, kl, jl, il);
-          const int kj = kl * P - (kl * (kl - 1)) / 2 + jl;
-          T s = T(0);
+#pragma unroll
+        for (int c0 = 0; c0 < NKJ; c0 += KC) {
+#pragma unroll
+          for (int c = 0; c < KC; c++)
+            if (c0 + c < NKJ)
+              rl[c] = akj[c0 + c];
+          __syncwarp();
+          for (int e = lane; e < nco; e += 32) {
+            int kl, jl, il;
+            decode_cidx(e, lp, kl, jl, il);
+            const int kj = kl * P - (kl * (kl - 1)) / 2 + jl - c0;
+            if (kj < 0 || kj >= KC)
+              continue;
+            T s = T(0);
 #pragma unroll 8
-          for (int r = 0; r < 32; r++)
-            s += red[r * RS + kj] * red[r * RS + NKJ + il];
-          acc[e] += (double)s;
+            for (int r = 0; r < 32; r++)
+              s += red[r * RS + kj] * red[r * RS + KC + il];
+            acc[e] += (double)s;
+          }
+          __syncwarp();
         }
-        __syncwarp();
       }
     }
     __syncwarp();
@@ -870,32 +878,39 @@ __global__ void __launch_bounds__(128) integrate_general_df(GridArgs a, int njma
           pk = df_mul(pk, dkd);
         }
       }
-      // fold i and reduce over the warp through shared memory
+      // fold i and reduce over the warp through shared memory, KC rows of
+      // akj per pass
       {
-        constexpr int RS = S::red_stride();
+        constexpr int KC = S::KC, RS = S::red_stride();
         dfloat *rl = red + lane * RS;
-#pragma unroll
-        for (int e = 0; e < NKJ; e++)
-          rl[e] = df_norm(akj[e]);
         const dfloat dd = df_make(di);
         dfloat pi = xin ? dfloat{1.f, 0.f} : dfloat{0.f, 0.f};
 #pragma unroll
         for (int l = 0; l < P; l++) {
-          rl[NKJ + l] = pi;
+          rl[KC + l] = pi;
           pi = df_mul(pi, dd);
         }
-        __syncwarp();
-        for (int e = lane; e < nco; e += 32) {
-          int kl, jl, il;
-          decode_cidx(e, lp, kl, jl, il);
-          const int kj = kl * P - (kl * (kl - 1)) / 2 + jl;
-          dfloat s{0.f, 0.f};
+#pragma unroll
+        for (int c0 = 0; c0 < NKJ; c0 += KC) {
+#pragma unroll
+          for (int c = 0; c < KC; c++)
+            if (c0 + c < NKJ)
+              rl[c] = df_norm(akj[c0 + c]);
+          __syncwarp();
+          for (int e = lane; e < nco; e += 32) {
+            int kl, jl, il;
+            decode_cidx(e, lp, kl, jl, il);
+            const int kj = kl * P - (kl * (kl - 1)) / 2 + jl - c0;
+            if (kj < 0 || kj >= KC)
+              continue;
+            dfloat s{0.f, 0.f};
 #pragma unroll 8
-          for (int r = 0; r < 32; r++)
-            s = df_fma_acc(s, red[r * RS + kj], red[r * RS + NKJ + il]);
-          acc[e] += to_double(df_norm(s));
+            for (int r = 0; r < 32; r++)
+              s = df_fma_acc(s, red[r * RS + kj], red[r * RS + KC + il]);
+            acc[e] += to_double(df_norm(s));
+          }
+          __syncwarp();
         }
-        __syncwarp();
       }
     }
     __syncwarp();
@@ -962,7 +977,7 @@ void launch_gen_any(const GridArgs &a, bool collocate, int arith, int lpb, int n
     else                                                                       \
       launch_gen<double, LP>(a, collocate, njmax, cfg, s);                     \
     break;
-    GB_CASE(4) GB_CASE(6) GB_CASE(9) GB_CASE(16)
+    GB_CASE(4) GB_CASE(6) GB_CASE(9) GB_CASE(12) GB_CASE(16)
 #undef GB_CASE
   }
 }

@@ -750,6 +750,7 @@ static void launch_grid(const GridArgs &a, int arith, bool general, bool colloca
   case 4: launch_ortho_lp<4>(a, arith, collocate, extent, cfg, s); break;
   case 6: launch_ortho_lp<6>(a, arith, collocate, extent, cfg, s); break;
   case 9: launch_ortho_lp<9>(a, arith, collocate, extent, cfg, s); break;
+  case 12: launch_ortho_lp<12>(a, arith, collocate, extent, cfg, s); break;
   case 16: launch_ortho_lp<16>(a, arith, collocate, extent, cfg, s); break;
   }
 }

@@ -368,7 +368,7 @@ typedef struct {
   int precision;      /* arithmetic of the launch: GRID_GB300_FP64 / _MIXED
                          (double-float) / _FP32 */
   int general;        /* 1: general (non-orthorhombic or border) kernel */
-  int lp_bucket;      /* lp limit of the kernel instance (4, 6, 9, 16) */
+  int lp_bucket;      /* lp limit of the kernel instance (4, 6, 9, 12, 16) */
   int ntasks;         /* tasks in the launch */
   int warps_per_block;
   int blocks;
