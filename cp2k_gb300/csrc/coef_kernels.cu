@@ -20,6 +20,8 @@
 #include <type_traits>
 
 #include <algorithm>
+#include <cstdint>
+#include <vector>
 
 #include "gb300_internal.h"
 #include "numeric.cuh"
@@ -182,6 +184,24 @@ __device__ __forceinline__ GrpLayout grp_layout(int gsize) {
 // in (x-a)^lxa (x-b)^lxb  (grid_ref_collint.h:838-861)
 // ------------------------------------------------------------------------
 __constant__ float c_binom[GB300_LP_MAX + 1][GB300_LP_MAX + 1];
+
+// Entry orders of the transforms' per-lane loops, per (la, lb) with la, lb
+// < kOrdL: lanes of a warp take consecutive entries, and their loops have
+// very different trip counts (1 to ~10^3 terms), so the entries are sorted
+// by their number of terms, longest first; neighbouring lanes then run
+// loops of similar length.  Kind 0: the C_ab entries (a, b) of the post
+// kernel, index ib * ncoset(la) + ia, (a_x + b_x + 1)(a_y + b_y + 1)
+// (a_z + b_z + 1) terms.  Kind 1: the C_xyz outputs p (cidx order) of the
+// coefficient kernel, #{(a, b): a + b >= p componentwise} terms.
+constexpr int kOrdL = 9;
+constexpr int kOrderWords = 495 * 495 + kOrdL * kOrdL * 969;
+__device__ uint16_t g_order[kOrderWords];
+__constant__ int c_order_off[2][kOrdL][kOrdL];
+
+__device__ __forceinline__ const uint16_t *entry_order(int kind, int la, int lb) {
+  return (la < kOrdL && lb < kOrdL) ? g_order + c_order_off[kind][la][lb] : nullptr;
+}
+
 
 template <typename T>
 __device__ void fill_alpha(T *alpha, int la, int lb, int lp, const double ra[3],
@@ -486,7 +506,9 @@ __device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *w
   const U pref = U(d.prefexp * ((d.iatom == d.jatom) ? 1.0 : 2.0));
   const int nco = ncoset(lp);
   const bool general = d.flags & TF_GENERAL;
-  for (int e = g.lane; e < nco; e += g.n) {
+  const uint16_t *ord = entry_order(1, la_max, lb_max);
+  for (int i = g.lane; i < nco; i += g.n) {
+    const int e = ord ? ord[i] : i;
     int pz, py, px;
     decode_cidx(e, lp, pz, py, px);
     const U v = cab_cxyz_term<U>(cab, n1, alpha, la_max, lb_max, lp, px, py, pz) * pref;
@@ -601,7 +623,9 @@ __device__ void post_task(const PostArgs &a, int t, const TaskDesc &d, double *w
     rb[i] = ra[i] + d.rab[i];
   fill_alpha<U>(alpha, la_max, lb_max, lp, ra, rb, d.rp, g);
   const U pref = U(d.prefexp);
-  for (int e = g.lane; e < m1 * m2; e += g.n) {
+  const uint16_t *ord = entry_order(0, la_max, lb_max);
+  for (int i = g.lane; i < m1 * m2; i += g.n) {
+    const int e = ord ? ord[i] : i;
     const Orb oa = orb_of_index(e % m1), ob = orb_of_index(e / m1);
     cab[e] = cxyz_cab_term<U>(cx, alpha, la_max, lb_max, lp, oa, ob) * pref;
   }
@@ -778,10 +802,66 @@ int grid_size_for(int nwarps_needed, int warps_per_cta = 4) {
 
 } // namespace
 
+static void upload_orders() {
+  std::vector<uint16_t> tab;
+  std::vector<int> off(2 * kOrdL * kOrdL);
+  std::vector<int> ox, oy, oz; // orbital of Cartesian index
+  for (int l = 0; l < kOrdL; l++)
+    for (int lx = l; lx >= 0; lx--)
+      for (int lz = 0; lz <= l - lx; lz++) {
+        ox.push_back(lx);
+        oy.push_back(l - lx - lz);
+        oz.push_back(lz);
+      }
+  for (size_t i = 0; i < ox.size(); i++)
+    if (coset(ox[i], oy[i], oz[i]) != (int)i)
+      return launch_error("entry orders: orbital order mismatch");
+  std::vector<std::pair<long long, int>> v;
+  auto push_sorted = [&]() {
+    std::stable_sort(v.begin(), v.end(), [](const std::pair<long long, int> &x,
+                                            const std::pair<long long, int> &y) {
+      return x.first > y.first;
+    });
+    for (auto &p : v)
+      tab.push_back((uint16_t)p.second);
+  };
+  for (int la = 0; la < kOrdL; la++)
+    for (int lb = 0; lb < kOrdL; lb++) {
+      const int m1 = ncoset(la), m2 = ncoset(lb), lp = la + lb;
+      off[(0 * kOrdL + la) * kOrdL + lb] = (int)tab.size();
+      v.clear();
+      for (int ib = 0; ib < m2; ib++)
+        for (int ia = 0; ia < m1; ia++)
+          v.push_back({(long long)(ox[ia] + ox[ib] + 1) * (oy[ia] + oy[ib] + 1) *
+                           (oz[ia] + oz[ib] + 1),
+                       ib * m1 + ia});
+      push_sorted();
+      off[(1 * kOrdL + la) * kOrdL + lb] = (int)tab.size();
+      v.clear();
+      for (int e = 0; e < ncoset(lp); e++) {
+        int pz, py, px;
+        decode_cidx(e, lp, pz, py, px);
+        long long n = 0;
+        for (int ia = 0; ia < m1; ia++) {
+          const int q = std::max(px - ox[ia], 0) + std::max(py - oy[ia], 0) +
+                        std::max(pz - oz[ia], 0);
+          n += ncoset(lb - q);
+        }
+        v.push_back({n, e});
+      }
+      push_sorted();
+    }
+  if (tab.size() > (size_t)kOrderWords)
+    return launch_error("entry orders: table exceeds its size");
+  cudaMemcpyToSymbol(g_order, tab.data(), tab.size() * sizeof(uint16_t));
+  cudaMemcpyToSymbol(c_order_off, off.data(), off.size() * sizeof(int));
+}
+
 static void upload_binomials() {
   static bool done = false;
   if (done)
     return;
+  upload_orders();
   float b[GB300_LP_MAX + 1][GB300_LP_MAX + 1] = {};
   for (int n = 0; n <= GB300_LP_MAX; n++) {
     b[n][0] = 1.f;
