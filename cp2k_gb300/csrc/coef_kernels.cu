@@ -253,21 +253,34 @@ __device__ T cab_cxyz_term(const T *cab, int n1, const T *alpha, int la, int lb,
   return s;
 }
 
-// C_ab entry (a, b) from C_xyz (integrate adjoint of the above)
+// C_ab entry (a, b) from C_xyz (integrate adjoint of the above).  The
+// (px, py, pz) terms run as one flat loop with carries, so lanes whose
+// entries have equally many terms (the entry order sorts them so) keep the
+// same control flow whatever the shape of their index ranges.
 template <typename T>
 __device__ T cxyz_cab_term(const T *cxyz, const T *alpha, int la, int lb, int lp, Orb a,
                            Orb b) {
   const int na = la + 1, nb = lb + 1, P = lp + 1;
-  auto A = [&](int d, int xb, int xa, int l) {
-    return alpha[((size_t)(d * nb + xb) * na + xa) * P + l];
-  };
+  const T *ax = alpha + ((size_t)(0 * nb + b.l[0]) * na + a.l[0]) * P;
+  const T *ay = alpha + ((size_t)(1 * nb + b.l[1]) * na + a.l[1]) * P;
+  const T *az = alpha + ((size_t)(2 * nb + b.l[2]) * na + a.l[2]) * P;
+  const int nx = a.l[0] + b.l[0] + 1, ny = a.l[1] + b.l[1] + 1, nz = a.l[2] + b.l[2] + 1;
+  const int n = nx * ny * nz;
+  int px = 0, py = 0, pz = 0, row = cidx(0, 0, 0, lp);
+  T wyz = ay[0] * az[0];
   T s = T(0);
-  for (int pz = 0; pz <= a.l[2] + b.l[2]; pz++) {
-    const T wz = A(2, b.l[2], a.l[2], pz);
-    for (int py = 0; py <= a.l[1] + b.l[1]; py++) {
-      const T wyz = wz * A(1, b.l[1], a.l[1], py);
-      for (int px = 0; px <= a.l[0] + b.l[0]; px++)
-        s += wyz * A(0, b.l[0], a.l[0], px) * cxyz[cidx(pz, py, px, lp)];
+  for (int t = 0; t < n; t++) {
+    s += wyz * ax[px] * cxyz[row + px];
+    if (++px == nx) {
+      px = 0;
+      if (++py == ny) {
+        py = 0;
+        ++pz;
+      }
+      if (pz < nz) {
+        wyz = ay[py] * az[pz];
+        row = cidx(pz, py, 0, lp);
+      }
     }
   }
   return s;
