@@ -519,7 +519,9 @@ __device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *w
   const U pref = U(d.prefexp * ((d.iatom == d.jatom) ? 1.0 : 2.0));
   const int nco = ncoset(lp);
   const bool general = d.flags & TF_GENERAL;
-  const uint16_t *ord = entry_order(1, la_max, lb_max);
+  // (at low lp the outputs' term counts differ little and the plain order
+  // keeps the stores contiguous)
+  const uint16_t *ord = lp >= 6 ? entry_order(1, la_max, lb_max) : nullptr;
   for (int i = g.lane; i < nco; i += g.n) {
     const int e = ord ? ord[i] : i;
     int pz, py, px;
