@@ -252,6 +252,7 @@ struct Queue {
   // boxes split by planes over several warps; null when no task is split
   int2 *d_items = nullptr;
   int nitems = 0;
+  int iwidth = 0; // general path: widest box in i
   int extent = 0; // ortho: max cube width; general: max j-range
   int general = 0, bucket = 0;
   int fp32 = 0; // mixed path: this queue runs in plain FP32
@@ -1084,8 +1085,10 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase) {
       q.flops += 2.0 * (lpk + 1) * (double)t->points[idx[i]];
       if (q.general == 0)
         ext = std::max(ext, 2 * t->sph[k.sphere].cmax + 2);
-      else
+      else {
         ext = std::max(ext, k.imax[1] - k.center[1] + 1);
+        q.iwidth = std::max(q.iwidth, k.imax[0] - k.center[0] + 1);
+      }
     }
     q.n = (int)idx.size();
     q.extent = ext;
@@ -1294,6 +1297,7 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
   for (const Queue &q : m.queues) {
     ga.queue = q.d_idx;
     ga.items = q.d_items;
+    ga.iwidth = q.iwidth;
     ga.nqueue = q.d_items ? q.nitems : q.n;
     ga.counter = t->d_counters + qi++;
     ga.coef_stride = q.fp32 ? 2 : 1;
@@ -1369,6 +1373,7 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
   for (const Queue &q : m.queues) {
     ga.queue = q.d_idx;
     ga.items = q.d_items;
+    ga.iwidth = q.iwidth;
     ga.nqueue = q.d_items ? q.nitems : q.n;
     ga.counter = t->d_counters + qi++;
     ga.grid_stride = 1;

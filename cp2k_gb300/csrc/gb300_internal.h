@@ -163,6 +163,7 @@ struct GridArgs {
   const TaskDesc *tasks;
   const int *queue;
   const int2 *items;      // general path: (task, first plane | planes << 16), or null
+  int iwidth;             // general path: widest box of the queue in i
   int nqueue;             // tasks, or work items when items is set
   int *counter;           // work counter, zeroed before launch
   const int *coef_off;

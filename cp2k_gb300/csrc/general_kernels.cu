@@ -927,6 +927,238 @@ __global__ void __launch_bounds__(128) integrate_general_df(GridArgs a, int njma
   }
 }
 
+// ------------------------------------------------------------------------
+// point-list collocation, general path (FP32 and double-float)
+//
+// The kernels above bind lanes to i and walk the box's rows: lanes whose i
+// lies outside the sphere's row idle, and the sphere fills about half of
+// the box.  Here the warp first builds, per plane, the clipped i-range of
+// every row and their prefix offsets, and per i of the box the x-folded
+// polynomial Q[i][jl] = sum_il C_ij[jl][il] di^il and the Gaussian's line
+// constants; then it walks the plane's points in row-major order, 32
+// consecutive points per step.  Same points and arithmetic as
+// collocate_general_df / collocate_general<float>.
+// ------------------------------------------------------------------------
+template <typename T, int LPB> struct PlSmem {
+  static constexpr int P = LPB + 1;
+  static __host__ __device__ size_t bytes(int nj, int iw) {
+    size_t b = sizeof(T) * (ncoset(LPB) + ntri(LPB) + (size_t)iw * P); // coef, cij, Q
+    b = (b + 15) & ~size_t(15);
+    b += sizeof(float4) * (size_t)iw;                                   // line constants
+    b += sizeof(int) * (size_t)iw;                                      // grid index of i
+    b = (b + 7) & ~size_t(7);
+    b += sizeof(int2) * (size_t)nj + sizeof(int) * (2 * (size_t)nj + 1); // rows, jg, offsets
+    return (b + 15) & ~size_t(15);
+  }
+};
+
+template <typename T, int LPB>
+__global__ void __launch_bounds__(128) collocate_general_pl(GridArgs a, int njmax) {
+  constexpr bool DF = std::is_same<T, dfloat>::value;
+  using M = Num<T>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ float2 tab[64];
+  fill_exp2_table(tab);
+  constexpr int P = LPB + 1;
+  const int iw = a.iwidth;
+  const int lane = threadIdx.x & 31;
+  unsigned char *ws = smem + (threadIdx.x >> 5) * PlSmem<T, LPB>::bytes(njmax, iw);
+  T *coef = (T *)ws;
+  T *cij = coef + ncoset(LPB);
+  T *Q = cij + ntri(LPB); // [iw][P]
+  float4 *lin = (float4 *)(((uintptr_t)(Q + (size_t)iw * P) + 15) & ~uintptr_t(15));
+  int *igx = (int *)(lin + iw);
+  int2 *rows = (int2 *)(((uintptr_t)(igx + iw) + 7) & ~uintptr_t(7));
+  int *jgr = (int *)(rows + njmax);
+  int *off = jgr + njmax; // [njmax + 1]
+
+  for (;;) {
+    int qi = 0;
+    if (lane == 0)
+      qi = atomicAdd(a.counter, 1);
+    qi = __shfl_sync(FULL, qi, 0);
+    if (qi >= a.nqueue)
+      break;
+    const WorkItem w = work_item(a, qi);
+    const int t = w.t;
+    const long long t0 = clock64();
+    const TaskDesc d = a.tasks[t];
+    const LevelDesc &L = a.levels.lv[d.level];
+    GenTask g;
+    gen_setup(d, L, g);
+    RowFast rowf;
+    row_fast_setup(g, d.radius, rowf);
+    const int k_lo = g.imin[2] + w.k0, k_hi = min(g.imax[2], g.imin[2] + w.k0 + w.nk - 1);
+    const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
+    const int nj = g.imax[1] - g.imin[1] + 1;
+    const int width = g.imax[0] - g.imin[0] + 1;
+    if (nj > njmax || lp > LPB || width > iw) {
+      if (lane == 0)
+        atomicOr(a.error, 1);
+      continue;
+    }
+    const int nco = ncoset(lp), ntr = ntri(lp);
+    if constexpr (DF) {
+      const dfloat *csrc = (const dfloat *)a.coef + a.coef_off[t];
+      for (int e = lane; e < nco; e += 32)
+        coef[e] = csrc[e];
+    } else if (a.coef_stride == 2) { // FP32 class of the mixed mode: high words
+      const float *csrc = (const float *)a.coef + 2 * (size_t)a.coef_off[t];
+      for (int e = lane; e < nco; e += 32)
+        coef[e] = csrc[2 * e];
+    } else {
+      const float *csrc = (const float *)a.coef + a.coef_off[t];
+      for (int e = lane; e < nco; e += 32)
+        coef[e] = csrc[e];
+    }
+    for (int x = lane; x < width; x += 32)
+      igx[x] = gmap(g.imin[0] + x, 0, g, L);
+    double *grid = a.grids[d.level];
+    float *glo = a.grids_lo[d.level];
+    const size_t nx = L.npts_local[0], nxy = nx * L.npts_local[1];
+    const double zetp = d.zetp, inv_hh1 = 1.0 / g.hh[1];
+    const double fj0 = (double)g.imin[1] - g.gp[1];
+    const dfloat A = df_make(zetp * g.hh[1]), dj0 = df_make(fj0);
+    const float fj0f = (float)fj0, zetpf = (float)zetp;
+    const float h1f[3] = {(float)g.h[3], (float)g.h[4], (float)g.h[5]};
+
+    for (int k = k_lo; k <= k_hi; k++) {
+      const int kg = gmap(k, 2, g, L);
+      if (kg < 0)
+        continue;
+      const double dk = (double)k - g.gp[2];
+      plane_rows<T>(k, g, L, d.radius, zetp, rows, nullptr, lane, rowf);
+      __syncwarp();
+      // clipped i-range per row, the row's grid index, exclusive offsets
+      int total = 0;
+      for (int r0 = 0; r0 < nj; r0 += 32) {
+        const int r = r0 + lane;
+        int len = 0;
+        if (r < nj) {
+          const int2 rb = rows[r];
+          const int i0 = max(rb.x, g.imin[0]), i1 = min(rb.y, g.imax[0]);
+          len = max(0, i1 - i0 + 1);
+          rows[r] = make_int2(i0, i1);
+          jgr[r] = len > 0 ? gmap(g.imin[1] + r, 1, g, L) : -1;
+        }
+        int inc = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(FULL, inc, o);
+          if (lane >= o)
+            inc += y;
+        }
+        if (r < nj)
+          off[r] = total + inc - len;
+        total += __shfl_sync(FULL, inc, 31);
+      }
+      if (lane == 0)
+        off[nj] = total;
+      // C_ij = sum_kl C_ijk dk^kl (Horner in kl)
+      const T dkt = M::from(dk);
+      for (int e = lane; e < ntr; e += 32) {
+        int jl = 0, rem = e;
+        while (rem > lp - jl) {
+          rem -= lp - jl + 1;
+          jl++;
+        }
+        const int il = rem;
+        T s = M::zero();
+        for (int kl = lp - jl - il; kl >= 0; kl--)
+          s = M::fma(coef[cidx(kl, jl, il, lp)], s, dkt);
+        cij[e] = s;
+      }
+      __syncwarp();
+      // per i of the box: Q[i][jl] and the Gaussian's line constants
+      for (int x = lane; x < width; x += 32) {
+        const double di = (double)(g.imin[0] + x) - g.gp[0];
+        T px[P];
+        {
+          const T dd = M::from(di);
+          T p = T(1);
+#pragma unroll
+          for (int l = 0; l < P; l++) {
+            px[l] = p;
+            p = M::mul(p, dd);
+          }
+        }
+#pragma unroll
+        for (int jl = 0; jl < P; jl++) {
+          T s = M::zero();
+          if (jl <= lp) {
+            const T *row = cij + jl * (lp + 1) - (jl * (jl - 1)) / 2;
+#pragma unroll
+            for (int il = 0; il < P; il++)
+              if (il <= lp - jl)
+                s = M::fma_acc(s, row[il], px[il]);
+          }
+          Q[(size_t)x * P + jl] = M::norm(s);
+        }
+        if constexpr (DF) {
+          const DfLine ln = df_line(di, dk, g, zetp, inv_hh1, fj0);
+          lin[x] = make_float4(ln.c0.h, ln.c0.l, ln.xp.h, ln.xp.l);
+        } else {
+          float rk[3];
+#pragma unroll
+          for (int c = 0; c < 3; c++)
+            rk[c] = (float)(di * g.h[c]) + (float)(dk * g.h[6 + c]);
+          lin[x] = make_float4(rk[0], rk[1], rk[2], 0.f);
+        }
+      }
+      __syncwarp();
+      double *gplane = grid + (size_t)kg * nxy;
+      int r = 0;
+      for (int p0 = 0; p0 < total; p0 += 32) {
+        const int p = p0 + lane;
+        if (p >= total)
+          continue;
+        while (off[r + 1] <= p)
+          r++;
+        const int i = rows[r].x + (p - off[r]);
+        const int x = i - g.imin[0];
+        const int ig = igx[x];
+        if (ig < 0)
+          continue;
+        const T *q = Q + (size_t)x * P;
+        const float4 lv = lin[x];
+        const float rf = (float)r;
+        const size_t idx = (size_t)jgr[r] * nx + ig;
+        if constexpr (DF) {
+          const dfloat gauss = df_gauss(DfLine{dfloat{lv.x, lv.y}, dfloat{lv.z, lv.w}}, A, rf, tab);
+          const dfloat dj = df_add1(dj0, rf);
+          dfloat v{0.f, 0.f};
+#pragma unroll
+          for (int jl = P - 1; jl >= 0; jl--)
+            if (jl <= lp)
+              v = df_fma(q[jl], v, dj);
+          const dfloat val = df_mul(v, gauss);
+          atomicAdd(gplane + idx, f2d_exact(val.h));
+          atomicAdd(glo + (size_t)kg * nxy + idx, val.l);
+        } else {
+          const float djf = rf + fj0f;
+          float r2 = 0.f;
+          const float rk[3] = {lv.x, lv.y, lv.z};
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            const float rc = fmaf(djf, h1f[c], rk[c]);
+            r2 = fmaf(rc, rc, r2);
+          }
+          float v = 0.f;
+#pragma unroll
+          for (int jl = P - 1; jl >= 0; jl--)
+            if (jl <= lp)
+              v = fmaf(v, djf, q[jl]);
+          atomicAdd(gplane + idx, f2d_exact(v * expf(-zetpf * r2)));
+        }
+      }
+      __syncwarp();
+    }
+    if (a.task_cycles && lane == 0) // summed over the task's work items
+      atomicAdd((unsigned long long *)&a.task_cycles[t], (unsigned long long)(clock64() - t0));
+    __syncwarp();
+  }
+}
+
 template <typename T, int LPB>
 const void *gen_kernel(bool collocate) {
   if constexpr (std::is_same<T, dfloat>::value)
@@ -939,13 +1171,30 @@ const void *gen_kernel(bool collocate) {
 
 template <typename T, int LPB>
 void launch_gen(const GridArgs &a, bool collocate, int njmax, LaunchCfg &cfg, cudaStream_t s) {
-  const size_t per_warp = GenSmem<T, LPB>::bytes(njmax);
+  // variant 1: point-list collocation (FP32 and double-float)
+  constexpr bool can_pl = !std::is_same<T, double>::value;
+  const bool pl = can_pl && collocate && cfg.variant == 1;
+  const size_t per_warp =
+      pl ? PlSmem<T, LPB>::bytes(njmax, a.iwidth) : GenSmem<T, LPB>::bytes(njmax);
   int nw = warps_for(per_warp);
   if (nw < 1)
     return launch_error("general path: box too large for shared memory");
   if (cfg.warps > 0 && cfg.warps < nw)
     nw = cfg.warps;
   const size_t smem = nw * per_warp;
+  if constexpr (can_pl) {
+    if (pl) {
+      const void *k = (const void *)collocate_general_pl<T, LPB>;
+      set_smem(k, smem);
+      const int nb =
+          cfg.blocks > 0 ? cfg.blocks : cfg_blocks(cfg, persistent_blocks(k, 32 * nw, smem));
+      cfg.warps = nw;
+      cfg.blocks = nb;
+      collocate_general_pl<T, LPB><<<nb, 32 * nw, smem, s>>>(a, njmax);
+      count_launch();
+      return;
+    }
+  }
   const void *k = gen_kernel<T, LPB>(collocate);
   set_smem(k, smem);
   const int nb = cfg.blocks > 0 ? cfg.blocks : cfg_blocks(cfg, persistent_blocks(k, 32 * nw, smem));

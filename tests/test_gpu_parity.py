@@ -239,6 +239,38 @@ def test_collocate_variants_agree(G, O, prec):
     tl.close()
 
 
+@pytest.mark.parametrize("prec,tau", [(1, 0.0), (1, None), (2, None)])
+def test_general_collocate_variants_agree(G, O, prec, tau):
+    """The general path's lane-per-i kernels (variant 0) and point-list
+    kernels (variant 1) visit the same points: double-float grids agree to
+    the order of the additions, FP32 grids to FP32 rounding (the point-list
+    kernel evaluates the polynomial in Horner form); the point-list
+    double-float grids match the oracle within the mixed mode's bound."""
+    from cp2k_gb300 import workload as W
+    inp = W.config("c3_256atoms_triclinic", scale=0.12, seed=33)
+    pab = W.density_blocks(inp)
+    tl = G.GridTaskList(inp, precision=prec)
+    if tau is not None:
+        tl.set_mixed_threshold(tau)
+    out = []
+    for v in (0, 1):
+        tl.set_collocate_variant(v)
+        out.append(tl.collocate(100, pab))
+    if prec == G.FP32:
+        gmax = max(float(np.abs(g).max()) for g in out[0])
+        assert max(float(np.abs(a - b).max()) for a, b in zip(*out)) / gmax < 2e-6
+    else:
+        tol = 1e-10 if tau == 0.0 else 1e-6
+        for a, b in zip(*out):
+            assert rel_diff(a, b) < tol
+    if tau == 0.0:
+        ot = O.OracleTaskList(inp)
+        ref = ot.collocate(100, pab)
+        assert max(rel_diff(a, b) for a, b in zip(out[1], ref)) < 1e-9
+        ot.close()
+    tl.close()
+
+
 @pytest.mark.parametrize("name,scale", [("c1_64atoms", 0.3), ("c3_256atoms_triclinic", 0.1)])
 def test_mixed_all_functions_tau_virial(G, O, name, scale):
     """The mixed mode on every family of grid_func (derivative shifts of the
