@@ -1176,9 +1176,11 @@ static cudaEvent_t pool_event(TaskList *t, size_t i) {
 static void grid_launch(TaskList *t, const Queue &q, int phase, int arith, const GridArgs &ga,
                         cudaStream_t s) {
   LaunchCfg cfg;
-  // automatic: the point-list kernel pays off where the per-point arithmetic
-  // is expensive (FP64, double-float), the row walk for plain FP32
-  cfg.variant = t->coll_variant >= 0 ? t->coll_variant : (arith == ARITH_FP32 ? 0 : 1);
+  // automatic: on the orthorhombic path the point-list kernel pays off where
+  // the per-point arithmetic is expensive (FP64, double-float), the row walk
+  // for plain FP32; on the general path (box around the sphere) the point
+  // list wins in every arithmetic that has one (FP32, double-float)
+  cfg.variant = t->coll_variant >= 0 ? t->coll_variant : ((q.general || arith != ARITH_FP32) ? 1 : 0);
   auto it = t->tuned.find(std::make_tuple(t->precision, phase, q.key));
   if (it != t->tuned.end())
     cfg = it->second;
