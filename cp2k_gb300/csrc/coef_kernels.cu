@@ -202,6 +202,18 @@ __device__ __forceinline__ const uint16_t *entry_order(int kind, int la, int lb)
   return (la < kOrdL && lb < kOrdL) ? g_order + c_order_off[kind][la][lb] : nullptr;
 }
 
+// Term lists of the C_ab -> C_xyz gather for la, lb < kTermL: for output e
+// (cidx order) the terms g_terms[g_tstart[e] .. g_tstart[e + 1]), each the
+// C_ab index (x low 16 bits), the alpha offsets of z (x high 16 bits), x
+// (y low) and y (y high) in the [3][lb + 1][la + 1][lp + 1] alpha table.
+// The gather then costs a packed load and four shared-memory loads per term
+// instead of the index arithmetic of the nested loops.
+constexpr int kTermL = 4;
+constexpr int kTermWords = 40000, kTStartWords = kTermL * kTermL * 100;
+__device__ uint2 g_terms[kTermWords];
+__device__ int g_tstart[kTStartWords];
+__constant__ int c_tstart_off[kTermL][kTermL];
+
 
 template <typename T>
 __device__ void fill_alpha(T *alpha, int la, int lb, int lp, const double ra[3],
@@ -526,7 +538,18 @@ __device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *w
     const int e = ord ? ord[i] : i;
     int pz, py, px;
     decode_cidx(e, lp, pz, py, px);
-    const U v = cab_cxyz_term<U>(cab, n1, alpha, la_max, lb_max, lp, px, py, pz) * pref;
+    U v;
+    if (la_max < kTermL && lb_max < kTermL) {
+      const int *ts = g_tstart + c_tstart_off[la_max][lb_max];
+      U acc = U(0);
+      for (int q = ts[e]; q < ts[e + 1]; q++) {
+        const uint2 w = g_terms[q];
+        acc += alpha[w.x >> 16] * alpha[w.y & 0xffffu] * alpha[w.y >> 16] * cab[w.x & 0xffffu];
+      }
+      v = acc * pref;
+    } else {
+      v = cab_cxyz_term<U>(cab, n1, alpha, la_max, lb_max, lp, px, py, pz) * pref;
+    }
     if (general)
       cxyz[e] = v;
     else
@@ -868,6 +891,38 @@ static void upload_orders() {
     }
   if (tab.size() > (size_t)kOrderWords)
     return launch_error("entry orders: table exceeds its size");
+  // term lists of the C_ab -> C_xyz gather
+  std::vector<uint2> terms;
+  std::vector<int> tstart;
+  int toff[kTermL][kTermL];
+  for (int la = 0; la < kTermL; la++)
+    for (int lb = 0; lb < kTermL; lb++) {
+      const int m1 = ncoset(la), m2 = ncoset(lb), lp = la + lb, P = lp + 1;
+      const int na = la + 1, nb = lb + 1;
+      toff[la][lb] = (int)tstart.size();
+      auto aoff = [&](int d, int xb, int xa, int l) { return ((d * nb + xb) * na + xa) * P + l; };
+      for (int e = 0; e < ncoset(lp); e++) {
+        int pz, py, px;
+        decode_cidx(e, lp, pz, py, px);
+        tstart.push_back((int)terms.size());
+        for (int ib = 0; ib < m2; ib++)
+          for (int ia = 0; ia < m1; ia++) {
+            if (ox[ia] + ox[ib] < px || oy[ia] + oy[ib] < py || oz[ia] + oz[ib] < pz)
+              continue;
+            const unsigned ci = (unsigned)(ib * m1 + ia);
+            const unsigned az = (unsigned)aoff(2, oz[ib], oz[ia], pz);
+            const unsigned axo = (unsigned)aoff(0, ox[ib], ox[ia], px);
+            const unsigned ayo = (unsigned)aoff(1, oy[ib], oy[ia], py);
+            terms.push_back(make_uint2(ci | (az << 16), axo | (ayo << 16)));
+          }
+      }
+      tstart.push_back((int)terms.size());
+    }
+  if (terms.size() > (size_t)kTermWords || tstart.size() > (size_t)kTStartWords)
+    return launch_error("term lists: table exceeds its size");
+  cudaMemcpyToSymbol(g_terms, terms.data(), terms.size() * sizeof(uint2));
+  cudaMemcpyToSymbol(g_tstart, tstart.data(), tstart.size() * sizeof(int));
+  cudaMemcpyToSymbol(c_tstart_off, toff, sizeof(toff));
   cudaMemcpyToSymbol(g_order, tab.data(), tab.size() * sizeof(uint16_t));
   cudaMemcpyToSymbol(c_order_off, off.data(), off.size() * sizeof(int));
 }
