@@ -544,7 +544,7 @@ __device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *w
       U acc = U(0);
       for (int q = ts[e]; q < ts[e + 1]; q++) {
         const uint2 w = g_terms[q];
-        acc += alpha[w.x >> 16] * alpha[w.y & 0xffffu] * alpha[w.y >> 16] * cab[w.x & 0xffffu];
+        acc += alpha[w.x >> 16] * alpha[w.y >> 16] * alpha[w.y & 0xffffu] * cab[w.x & 0xffffu];
       }
       v = acc * pref;
     } else {
@@ -905,16 +905,19 @@ static void upload_orders() {
         int pz, py, px;
         decode_cidx(e, lp, pz, py, px);
         tstart.push_back((int)terms.size());
-        for (int ib = 0; ib < m2; ib++)
-          for (int ia = 0; ia < m1; ia++) {
-            if (ox[ia] + ox[ib] < px || oy[ia] + oy[ib] < py || oz[ia] + oz[ib] < pz)
-              continue;
-            const unsigned ci = (unsigned)(ib * m1 + ia);
-            const unsigned az = (unsigned)aoff(2, oz[ib], oz[ia], pz);
-            const unsigned axo = (unsigned)aoff(0, ox[ib], ox[ia], px);
-            const unsigned ayo = (unsigned)aoff(1, oy[ib], oy[ia], py);
-            terms.push_back(make_uint2(ci | (az << 16), axo | (ayo << 16)));
-          }
+        // the order of cab_cxyz_term's loops
+        for (int az = 0; az <= la; az++)
+          for (int bz = std::max(0, pz - az); bz <= lb; bz++)
+            for (int ay = 0; ay <= la - az; ay++)
+              for (int by = std::max(0, py - ay); by <= lb - bz; by++)
+                for (int ax = 0; ax <= la - az - ay; ax++)
+                  for (int bx = std::max(0, px - ax); bx <= lb - bz - by; bx++) {
+                    const unsigned ci = (unsigned)(coset(bx, by, bz) * m1 + coset(ax, ay, az));
+                    const unsigned azo = (unsigned)aoff(2, bz, az, pz);
+                    const unsigned axo = (unsigned)aoff(0, bx, ax, px);
+                    const unsigned ayo = (unsigned)aoff(1, by, ay, py);
+                    terms.push_back(make_uint2(ci | (azo << 16), axo | (ayo << 16)));
+                  }
       }
       tstart.push_back((int)terms.size());
     }
