@@ -120,6 +120,42 @@ def test_schedule_from_recorded_timings(CM):
     tl.close()
 
 
+def test_model_beats_size_cost_prediction(CM):
+    """The learned model's gain over the analytic size cost: on held-out
+    tasks it predicts log(task time) with a lower mean squared error than
+    the size cost's best affine fit in log space (fitted on the same
+    training tasks), and ranks the tasks at least as well."""
+    import torch
+    from cp2k_gb300 import grid as G
+    from cp2k_gb300 import workload as W
+    from cp2k_gb300.costmodel_eval import size_cost, spearman
+    inp = W.config("c2_512atoms", scale=0.25, seed=23)
+    pab = torch.tensor(W.density_blocks(inp), device="cuda")
+    V = [torch.tensor(v, device="cuda") for v in W.potential_grids(inp)]
+    grids = [torch.empty(n, dtype=torch.float64, device="cuda") for n in inp.grid_sizes()]
+    hab = torch.empty(inp.buffer_size, dtype=torch.float64, device="cuda")
+    tl = G.GridTaskList(inp, precision=G.MIXED)
+    tl.collocate_device(100, pab, grids)
+    tl.integrate_device(V, hab)
+    X, T, ok = CM.collect_timings(tl, pab, V, grids, hab, steps=2)
+    pts, lp = tl.sizes()
+    S = np.log(size_cost(pts, lp)[ok])
+    rng = np.random.default_rng(1)
+    perm = rng.permutation(len(T))
+    ntr = int(0.8 * len(T))
+    tr, va = perm[:ntr], perm[ntr:]
+    m = CM.CostModel(seed=3)
+    m.train(X[tr], T[tr], epochs=30, batch=1024)
+    pred = m.predict(X[va])
+    mse_model = float(np.mean((pred - T[va]) ** 2))
+    A = np.vstack([S[tr], np.ones(ntr)]).T
+    coef = np.linalg.lstsq(A, T[tr], rcond=None)[0]
+    mse_size = float(np.mean((coef[0] * S[va] + coef[1] - T[va]) ** 2))
+    assert mse_model < mse_size, (mse_model, mse_size)
+    assert spearman(pred, T[va]) >= spearman(S[va], T[va]) - 0.01
+    tl.close()
+
+
 def test_launch_timings_cover_all_tasks(CM):
     import torch
     from cp2k_gb300 import grid as G
