@@ -87,6 +87,32 @@ def test_sample_task_double_float(G, O, name):
     ot.close()
 
 
+@pytest.mark.parametrize("name", SAMPLE_TASKS)
+def test_sample_task_fp32(G, O, name):
+    """Each recorded CP2K task in plain FP32 (orthorhombic and general FP32
+    kernels, border masks included): max |d| / max |ref| <= 1e-5 for the
+    grid and hab.  (Single tasks are looser than the workloads' 2e-6: the
+    l2200 task, whose polynomial has only l = 2 terms in both factors,
+    cancels to 3.2e-6.)"""
+    from cp2k_gb300.tasklist import single_task_list
+    d = load_digests()[name]
+    t = digest_task(d)
+    inp = single_task_list(t)
+    tl = G.GridTaskList(inp, precision=G.FP32)
+    ot = O.OracleTaskList(inp)
+    pab_c = (0.5 * t["rscale"] * t["pab"]).ravel()
+    g_ora = ot.collocate(t["func"], pab_c)[0]
+    g = tl.collocate(t["func"], pab_c)[0]
+    assert float(np.abs(g - g_ora).max()) <= 1e-5 * float(np.abs(g_ora).max())
+    tau = t["func"] == 200
+    pab_i = (0.5 * t["pab"]).ravel()
+    hab, _, _ = tl.integrate([g_ora], pab_i, compute_tau=tau)
+    hab_o, _, _ = ot.integrate([g_ora], pab_i, compute_tau=tau)
+    assert float(np.abs(hab - hab_o).max()) <= 1e-5 * float(np.abs(hab_o).max())
+    tl.close()
+    ot.close()
+
+
 # The triclinic l<=4 case with compute_tau reaches contraction order 11 on
 # |hab| ~ 2e3: two FP64 evaluation orders differ there by up to ~7e-12
 # relative (the oracle and CP2K's REF backend themselves differ by 1.3e-12),
