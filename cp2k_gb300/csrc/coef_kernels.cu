@@ -674,12 +674,20 @@ __device__ void post_task(const PostArgs &a, int t, const TaskDesc &d, double *w
   const int nb = ncoset(d.lb_max) - ncoset(d.lb_min - 1);
   const double *pab = a.pab_cart ? a.pab_cart + sb.cart_offset : nullptr;
   double *hab = a.hab_cart + sb.cart_offset;
+  // With tau, forces and virial are linear in the density matrix: the tau
+  // shifts move onto it once (P', below), and the plain formulas then run
+  // once per entry of P' instead of twelve times per pair.  P' lives in the
+  // alpha / C_xyz / C_ijk area, free once C_ab is built.
+  const int n1p = ncoset(d.la_max + 1), n2p = ncoset(d.lb_max + 1);
+  const bool tau_fv = tau && (a.forces || a.virial) &&
+                      (size_t)n1p * n2p <= 3 * (size_t)(la_max + 1) * (lb_max + 1) * (lp + 1) +
+                                               2 * (size_t)ncoset(lp);
   for (int e = g.lane; e < na * nb; e += g.n) {
     const int ia = ncoset(d.la_min - 1) + e % na, ib = ncoset(d.lb_min - 1) + e / na;
     const Orb oa = orb_of_index(ia), ob = orb_of_index(ib);
     const size_t el = (size_t)(d.o2 + ib) * sb.ncoa + d.o1 + ia;
     atomicAdd(&hab[el], to_double(vab<U>(x, tau, V_HAB, 0, 0, oa, ob)));
-    if (a.forces || a.virial) {
+    if ((a.forces || a.virial) && !tau_fv) {
       const double p = pab[el];
       if (a.forces)
         for (int i = 0; i < 3; i++) {
@@ -691,6 +699,57 @@ __device__ void post_task(const PostArgs &a, int t, const TaskDesc &d, double *w
           for (int j = 0; j < 3; j++)
             v[i * 3 + j] += p * (to_double(vab<U>(x, tau, V_VA, i, j, oa, ob)) +
                                  to_double(vab<U>(x, tau, V_VB, i, j, oa, ob)));
+    }
+  }
+  if (tau_fv) {
+    // P'(a', b') = sum_k of the four tau terms' weights times P at the
+    // shifted pair that maps onto (a', b'):
+    //   0.5 (a'_k + 1)(b'_k + 1) P(a' + 1_k, b' + 1_k)
+    //   - zeta_a (b'_k + 1) P(a' - 1_k, b' + 1_k)      (a'_k >= 1)
+    //   - zeta_b (a'_k + 1) P(a' + 1_k, b' - 1_k)      (b'_k >= 1)
+    //   + 2 zeta_a zeta_b P(a' - 1_k, b' - 1_k)        (a'_k, b'_k >= 1)
+    // with P zero outside the task's block (the inverse of vab's tau sum).
+    double *pp = (double *)alpha;
+    const int ia0 = ncoset(d.la_min - 1), ia1 = ncoset(d.la_max);
+    const int ib0 = ncoset(d.lb_min - 1), ib1 = ncoset(d.lb_max);
+    auto P = [&](Orb oa, Orb ob) -> double {
+      const int ia = oidx(oa), ib = oidx(ob);
+      if (ia < ia0 || ia >= ia1 || ib < ib0 || ib >= ib1)
+        return 0.0;
+      return pab[(size_t)(d.o2 + ib) * sb.ncoa + d.o1 + ia];
+    };
+    g.sync(); // every lane is done with alpha and C_xyz
+    for (int e = g.lane; e < n1p * n2p; e += g.n) {
+      const Orb oa = orb_of_index(e % n1p), ob = orb_of_index(e / n1p);
+      double s = 0.0;
+      for (int k = 0; k < 3; k++) {
+        const double ak = oa.l[k], bk = ob.l[k];
+        s += 0.5 * (ak + 1.0) * (bk + 1.0) * P(up(k, oa), up(k, ob));
+        if (oa.l[k] >= 1)
+          s -= d.zeta * (bk + 1.0) * P(dn(k, oa), up(k, ob));
+        if (ob.l[k] >= 1)
+          s -= d.zetb * (ak + 1.0) * P(up(k, oa), dn(k, ob));
+        if (oa.l[k] >= 1 && ob.l[k] >= 1)
+          s += 2.0 * d.zeta * d.zetb * P(dn(k, oa), dn(k, ob));
+      }
+      pp[e] = s;
+    }
+    g.sync();
+    for (int e = g.lane; e < n1p * n2p; e += g.n) {
+      const double p = pp[e];
+      if (p == 0.0)
+        continue;
+      const Orb oa = orb_of_index(e % n1p), ob = orb_of_index(e / n1p);
+      if (a.forces)
+        for (int i = 0; i < 3; i++) {
+          f[i] += p * to_double(vab_plain<U>(x, V_FA, i, 0, oa, ob));
+          f[3 + i] += p * to_double(vab_plain<U>(x, V_FB, i, 0, oa, ob));
+        }
+      if (a.virial)
+        for (int i = 0; i < 3; i++)
+          for (int j = 0; j < 3; j++)
+            v[i * 3 + j] += p * (to_double(vab_plain<U>(x, V_VA, i, j, oa, ob)) +
+                                 to_double(vab_plain<U>(x, V_VB, i, j, oa, ob)));
     }
   }
   g.sync();
