@@ -43,8 +43,12 @@ template <typename T, int LPB> struct GenSmem {
   static constexpr int NKJ = (P * (P + 1)) / 2;
   static constexpr int KC = NKJ < 32 ? NKJ : 32;
   static __host__ __device__ constexpr int red_stride() { return (KC + P) | 1; }
+  // the e_jk table of the FP64 Gaussian (none in the FP32 / dfloat kernels)
+  static __host__ __device__ constexpr int ejk_words(int nj) {
+    return std::is_same<T, double>::value ? nj : 0;
+  }
   static __host__ __device__ size_t bytes(int nj) {
-    size_t b = sizeof(double) * ncoset(LPB) + sizeof(double) * (size_t)nj; // acc, ejk
+    size_t b = sizeof(double) * ncoset(LPB) + sizeof(double) * (size_t)ejk_words(nj); // acc, ejk
     b += sizeof(T) * (ncoset(LPB) + ntri(LPB));                            // coef, cij
     b += sizeof(T) * 32 * (size_t)red_stride();                            // fold
     b += sizeof(int2) * (size_t)nj;                                         // row bounds
@@ -231,7 +235,7 @@ __global__ void __launch_bounds__(128) collocate_general(GridArgs a, int njmax) 
   const int lane = threadIdx.x & 31;
   unsigned char *ws = smem + (threadIdx.x >> 5) * GenSmem<T, LPB>::bytes(njmax);
   double *ejk = (double *)ws + ncoset(LPB);
-  T *coef = (T *)(ejk + njmax);
+  T *coef = (T *)(ejk + GenSmem<T, LPB>::ejk_words(njmax));
   T *cij = coef + ncoset(LPB);
   T *red = cij + ntri(LPB);
   int2 *rows = (int2 *)(((uintptr_t)(red + 32 * GenSmem<T, LPB>::red_stride()) + 7) & ~uintptr_t(7));
@@ -402,7 +406,7 @@ __global__ void __launch_bounds__(128) integrate_general(GridArgs a, int njmax) 
   unsigned char *ws = smem + (threadIdx.x >> 5) * GenSmem<T, LPB>::bytes(njmax);
   double *acc = (double *)ws;
   double *ejk = acc + ncoset(LPB);
-  T *coef = (T *)(ejk + njmax);
+  T *coef = (T *)(ejk + GenSmem<T, LPB>::ejk_words(njmax));
   T *cij = coef + ncoset(LPB);
   T *red = cij + ntri(LPB);
   int2 *rows = (int2 *)(((uintptr_t)(red + 32 * GenSmem<T, LPB>::red_stride()) + 7) & ~uintptr_t(7));
@@ -633,7 +637,7 @@ __global__ void __launch_bounds__(128) collocate_general_df(GridArgs a, int njma
   const int lane = threadIdx.x & 31;
   unsigned char *ws = smem + (threadIdx.x >> 5) * S::bytes(njmax);
   double *ejk = (double *)ws + ncoset(LPB);
-  dfloat *coef = (dfloat *)(ejk + njmax);
+  dfloat *coef = (dfloat *)(ejk + S::ejk_words(njmax));
   dfloat *cij = coef + ncoset(LPB);
   dfloat *red = cij + ntri(LPB);
   int2 *rows = (int2 *)(((uintptr_t)(red + 32 * S::red_stride()) + 7) & ~uintptr_t(7));
@@ -777,7 +781,7 @@ __global__ void __launch_bounds__(128) integrate_general_df(GridArgs a, int njma
   unsigned char *ws = smem + (threadIdx.x >> 5) * S::bytes(njmax);
   double *acc = (double *)ws;
   double *ejk = acc + ncoset(LPB);
-  dfloat *red = (dfloat *)(ejk + njmax) + ncoset(LPB) + ntri(LPB);
+  dfloat *red = (dfloat *)(ejk + S::ejk_words(njmax)) + ncoset(LPB) + ntri(LPB);
   int2 *rows = (int2 *)(((uintptr_t)(red + 32 * S::red_stride()) + 7) & ~uintptr_t(7));
   double *out = (double *)a.coef_out;
 
