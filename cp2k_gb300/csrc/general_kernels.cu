@@ -7,7 +7,10 @@
 // 424-463).  Those bounds are computed in FP64 with explicitly rounded
 // operations (no FMA contraction) so the visited points are exactly the
 // reference's.  Mapping onto the warp as in the orthorhombic kernels: lane <->
-// i, planes k and rows j sequential, per-point lp+1 FMAs.
+// i, planes k and rows j sequential, per-point lp+1 FMAs; collocation also
+// has a point-list form (collocate_general_pl) whose lanes take consecutive
+// points of a plane.  Large boxes arrive as several work items, each a
+// range of planes.
 //
 // Gaussian: FP64 path uses the reference's three pair factors (Mathieu's
 // split, grid_ref_collint.h:358-367): e_ki per lane and plane, e_jk per row
