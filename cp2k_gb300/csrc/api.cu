@@ -1093,18 +1093,33 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase) {
     q.n = (int)idx.size();
     q.extent = ext;
     q.d_idx = dalloc_copy(idx);
-    if (q.general) {
-      // boxes of many points are split by planes (kSlicePoints points and at
-      // least kSlicePlanes planes per item), so a few large tasks still
-      // spread over the GPU; slices stay in the task's cost order
+    {
+      // Large tasks are split by planes into several work items, so that a
+      // few of them do not keep single warps busy while the GPU idles.
+      // General path: boxes of more than kSlicePoints points, in items of at
+      // least kSlicePlanes planes.  Orthorhombic path: tasks of more than
+      // twice the queue's balanced share per resident warp, in items of half
+      // that share (at least kOrthoSliceMin points and two planes).
+      const double share = (double)q.points / kNominalWarps;
+      const long long target =
+          std::max<long long>(kOrthoSliceMin, (long long)(0.5 * share));
       std::vector<int2> items;
       bool split = false;
       for (int s : idx) {
         const TaskDesc &k = t->tasks[s];
-        const int nk = k.imax[2] - k.center[2] + 1;
-        const long long by_pts = (t->points[s] + kSlicePoints - 1) / kSlicePoints;
-        const int ns = (int)std::max<long long>(
-            1, std::min<long long>(by_pts, (nk + kSlicePlanes - 1) / kSlicePlanes));
+        int nk, ns;
+        if (q.general) {
+          nk = k.imax[2] - k.center[2] + 1;
+          const long long by_pts = (t->points[s] + kSlicePoints - 1) / kSlicePoints;
+          ns = (int)std::max<long long>(
+              1, std::min<long long>(by_pts, (nk + kSlicePlanes - 1) / kSlicePlanes));
+        } else {
+          nk = 2 - 2 * t->sph[k.sphere].lb[2];
+          ns = 1;
+          if (t->points[s] > 2 * target)
+            ns = (int)std::min<long long>(nk / 2, (t->points[s] + target - 1) / target);
+          ns = std::max(ns, 1);
+        }
         split |= ns > 1;
         for (int c = 0; c < ns; c++) {
           const int k0 = (int)((long long)nk * c / ns), k1 = (int)((long long)nk * (c + 1) / ns);

@@ -307,9 +307,27 @@ void build_sphere_points(SphereHdr &h, const std::vector<int16_t> &tab, std::vec
 // pivoted factorisation M = P^T L D U of M[c][d] = dh[d][c] as kLatTab
 // values: pi(0..2), L10, L20, L21, D0, D1, D2, U02, U12, U01
 constexpr int kLatTab = 12;
+#ifdef __CUDACC__
+// one work item of a grid launch: a task, or a range of its planes (k0 planes
+// past the first, nk of them)
+struct WorkItem {
+  int t, k0, nk;
+};
+__device__ __forceinline__ WorkItem work_item(const GridArgs &a, int qi) {
+  if (a.items) {
+    const int2 it = a.items[qi];
+    return WorkItem{it.x, it.y & 0xffff, it.y >> 16};
+  }
+  return WorkItem{a.queue[qi], 0, 1 << 20};
+}
+#endif
+
 // splitting of large general-path boxes into plane ranges (work items)
 constexpr long long kSlicePoints = 16384;
 constexpr int kSlicePlanes = 4;
+// orthorhombic tasks: split past twice the queue's share per resident warp
+constexpr double kNominalWarps = 152.0 * 16.0;
+constexpr long long kOrthoSliceMin = 4096;
 inline size_t dh_table_size(int nlevels) { return (size_t)nlevels * kLatTab; }
 void build_dh_table(const LevelSet &ls, std::vector<double> &tab);
 

@@ -94,18 +94,6 @@ __device__ __forceinline__ void gen_setup(const TaskDesc &d, const LevelDesc &L,
   g.h20 = dot(2, 0);
 }
 
-// one work item: a task, or a range of its box's planes
-struct WorkItem {
-  int t, k0, nk;
-};
-__device__ __forceinline__ WorkItem work_item(const GridArgs &a, int qi) {
-  if (a.items) {
-    const int2 it = a.items[qi];
-    return WorkItem{it.x, it.y & 0xffff, it.y >> 16};
-  }
-  return WorkItem{a.queue[qi], 0, INT_MAX / 2};
-}
-
 // grid index along dir for lattice index c, or -1 when outside the bounds
 __device__ __forceinline__ int gmap(int c, int dir, const GenTask &g, const LevelDesc &L) {
   const int v = imod(c - L.shift[dir], L.npts_global[dir]);

@@ -245,12 +245,14 @@ __global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
     qi = __shfl_sync(FULL, qi, 0);
     if (qi >= a.nqueue)
       break;
-    const int t = a.queue[qi];
+    const WorkItem w = work_item(a, qi);
+    const int t = w.t;
     const long long t0 = clock64();
     const TaskDesc d = a.tasks[t];
     const LevelDesc &L = a.levels.lv[d.level];
     const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
     const CubeGeo cg = cube_geo(a.sph[d.sphere], a.sph_tab, lane);
+    const int k_lo = cg.lb2 + w.k0, k_hi = min(1 - cg.lb2, cg.lb2 + w.k0 + w.nk - 1);
     if (cg.w > wmax || lp > LPB) { // the host sized the work arrays; never expected
       if (lane == 0)
         atomicOr(a.error, 1);
@@ -292,7 +294,7 @@ __global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
       load_row<T, PP>(pol + (size_t)((xin ? cx : cg.x_lo) + cg.cmax) * PP, px);
       const int ig = map[(xin ? cx : cg.x_lo) + cg.cmax];
 
-      for (int k = cg.lb2; k <= 1 - cg.lb2; k++) {
+      for (int k = k_lo; k <= k_hi; k++) {
         const int kk = k <= 0 ? -k : k - 1;
         const int js = cg.tab[kk];
         // C_xy[ly][lx] = sum_lz C_xyz[lz][ly][lx] pol_z[lz](k)
@@ -351,7 +353,7 @@ __global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
       }
     }
     if (a.task_cycles && lane == 0)
-      a.task_cycles[t] = clock64() - t0;
+      atomicAdd((unsigned long long *)&a.task_cycles[t], (unsigned long long)(clock64() - t0));
     __syncwarp();
   }
 }
@@ -390,13 +392,15 @@ __global__ void __launch_bounds__(128) collocate_ortho_pl(GridArgs a, int wmax) 
     qi = __shfl_sync(FULL, qi, 0);
     if (qi >= a.nqueue)
       break;
-    const int t = a.queue[qi];
+    const WorkItem w = work_item(a, qi);
+    const int t = w.t;
     const long long t0 = clock64();
     const TaskDesc d = a.tasks[t];
     const LevelDesc &L = a.levels.lv[d.level];
     const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
     const SphereHdr &H = a.sph[d.sphere];
     const CubeGeo cg = cube_geo(H, a.sph_tab, lane);
+    const int k_lo = cg.lb2 + w.k0, k_hi = min(1 - cg.lb2, cg.lb2 + w.k0 + w.nk - 1);
     if (cg.w > wmax || lp > LPB || H.plo < 0) { // the host sized the work arrays
       if (lane == 0)
         atomicOr(a.error, 1);
@@ -431,7 +435,7 @@ __global__ void __launch_bounds__(128) collocate_ortho_pl(GridArgs a, int wmax) 
     const size_t nx = L.npts_local[0], nxy = nx * L.npts_local[1];
     const int *ploff = a.sph_ploff + H.plo;
 
-    for (int k = cg.lb2; k <= 1 - cg.lb2; k++) {
+    for (int k = k_lo; k <= k_hi; k++) {
       const int kk = k <= 0 ? -k : k - 1;
       // C_xy[ly][lx] = sum_lz C_xyz[lz][ly][lx] pol_z[lz](k)
       const T *pz = pol + (size_t)(2 * cg.w + k + cg.cmax) * PP;
@@ -495,7 +499,7 @@ __global__ void __launch_bounds__(128) collocate_ortho_pl(GridArgs a, int wmax) 
       __syncwarp();
     }
     if (a.task_cycles && lane == 0)
-      a.task_cycles[t] = clock64() - t0;
+      atomicAdd((unsigned long long *)&a.task_cycles[t], (unsigned long long)(clock64() - t0));
     __syncwarp();
   }
 }
@@ -526,12 +530,14 @@ __global__ void __launch_bounds__(128, LPB <= 4 ? 5 : 1) integrate_ortho(GridArg
     qi = __shfl_sync(FULL, qi, 0);
     if (qi >= a.nqueue)
       break;
-    const int t = a.queue[qi];
+    const WorkItem w = work_item(a, qi);
+    const int t = w.t;
     const long long t0 = clock64();
     const TaskDesc d = a.tasks[t];
     const LevelDesc &L = a.levels.lv[d.level];
     const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
     const CubeGeo cg = cube_geo(a.sph[d.sphere], a.sph_tab, lane);
+    const int k_lo = cg.lb2 + w.k0, k_hi = min(1 - cg.lb2, cg.lb2 + w.k0 + w.nk - 1);
     if (cg.w > wmax || lp > LPB) {
       if (lane == 0)
         atomicOr(a.error, 1);
@@ -578,7 +584,7 @@ __global__ void __launch_bounds__(128, LPB <= 4 ? 5 : 1) integrate_ortho(GridArg
       for (int e = 0; e < NYZ; e++)
         ayz[e] = M::zero();
 
-      for (int k = cg.lb2; k <= 1 - cg.lb2; k++) {
+      for (int k = k_lo; k <= k_hi; k++) {
         const int kk = k <= 0 ? -k : k - 1;
         const int js = cg.tab[kk];
         const size_t zoff = (size_t)map[2 * cg.w + k + cg.cmax] * nxy;
@@ -685,9 +691,12 @@ __global__ void __launch_bounds__(128, LPB <= 4 ? 5 : 1) integrate_ortho(GridArg
     __syncwarp();
     double *dst = out + a.coef_off[t];
     for (int e = lane; e < nco; e += 32)
-      dst[e] = acc[e];
+      if (a.items) // plane ranges of one task add up (the buffer is zeroed)
+        atomicAdd(dst + e, acc[e]);
+      else
+        dst[e] = acc[e];
     if (a.task_cycles && lane == 0)
-      a.task_cycles[t] = clock64() - t0;
+      atomicAdd((unsigned long long *)&a.task_cycles[t], (unsigned long long)(clock64() - t0));
     __syncwarp();
   }
 }
