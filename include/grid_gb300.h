@@ -375,8 +375,8 @@ typedef struct {
   long long points;   /* grid points the tasks visit */
   double flops;       /* sum over tasks of 2 (lp+1) points */
   double ms;          /* CUDA-event duration on the launching stream */
-  int work_items;     /* work items: the tasks, or for the general path the
-                         plane ranges that large boxes are split into */
+  int work_items;     /* work items: the tasks, counting a large task split
+                         into plane ranges once per range */
 } grid_gb300_launch_info;
 void grid_gb300_set_launch_timing(const grid_gb300_task_list *task_list,
                                   int enable);

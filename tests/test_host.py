@@ -51,6 +51,35 @@ def test_header_declares_the_cp2k_surface():
         assert name in d, name
 
 
+def test_struct_layouts_match_ctypes(tmp_path):
+    """The ctypes mirrors of the header's structs (offload_buffer,
+    grid_gb300_launch_info) have the C compiler's size and field offsets."""
+    import ctypes as C
+    from cp2k_gb300 import grid as G
+    structs = {"offload_buffer": G.OffloadBuffer, "grid_gb300_launch_info": G.LaunchInfo}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "grid_gb300.h"',
+             'int main(void) {']
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'  printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ['  return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    seen = {}
+    for line in out.splitlines():
+        cname, field, value = line.split()
+        seen[(cname, field)] = int(value)
+    for cname, py in structs.items():
+        assert seen[(cname, "sizeof")] == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert seen[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
 def test_library_exports_every_declared_symbol(grid_lib):
     out = subprocess.run(["nm", "-D", "--defined-only", grid_lib], capture_output=True,
                          text=True, check=True).stdout
