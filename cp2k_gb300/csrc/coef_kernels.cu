@@ -207,7 +207,10 @@ __device__ __forceinline__ const uint16_t *entry_order(int kind, int la, int lb)
 // C_ab index (x low 16 bits), the alpha offsets of z (x high 16 bits), x
 // (y low) and y (y high) in the [3][lb + 1][la + 1][lp + 1] alpha table.
 // The gather then costs a packed load and four shared-memory loads per term
-// instead of the index arithmetic of the nested loops.
+// instead of the index arithmetic of the nested loops.  The terms keep the
+// loops' order and the products their factor order, so the sums are those
+// of cab_cxyz_term to the last bit (the energy of the mixed mode is
+// sensitive to the FP32 class's summation order at the 1e-10 level).
 constexpr int kTermL = 4;
 constexpr int kTermWords = 40000, kTStartWords = kTermL * kTermL * 100;
 __device__ uint2 g_terms[kTermWords];
