@@ -208,9 +208,9 @@ __device__ __forceinline__ const uint16_t *entry_order(int kind, int la, int lb)
 // (y low) and y (y high) in the [3][lb + 1][la + 1][lp + 1] alpha table.
 // The gather then costs a packed load and four shared-memory loads per term
 // instead of the index arithmetic of the nested loops.  The terms keep the
-// loops' order and the products their factor order, so the sums are those
-// of cab_cxyz_term to the last bit (the energy of the mixed mode is
-// sensitive to the FP32 class's summation order at the 1e-10 level).
+// loops' order and the products their factor order, so the sums follow
+// cab_cxyz_term's rounding (the mixed mode's energy error moved from 1e-10
+// to 9e-10 Ha/atom with a different term order).
 constexpr int kTermL = 4;
 constexpr int kTermWords = 40000, kTStartWords = kTermL * kTermL * 100;
 __device__ uint2 g_terms[kTermWords];
