@@ -13,6 +13,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <thread>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
@@ -565,23 +567,35 @@ void build_sphere_points(SphereHdr &h, const std::vector<int16_t> &tab, std::vec
 // double-float per task.
 static double contribution_bound(const TaskDesc &d, const double *ra) {
   const int la = d.la_max, lb = d.lb_max;
+  // binomial coefficients, once
+  static const auto binom = [] {
+    std::array<std::array<double, GB300_LMAX + 1>, GB300_LMAX + 1> c{};
+    for (int n = 0; n <= GB300_LMAX; n++) {
+      c[n][0] = 1.0;
+      for (int k = 1; k <= n; k++)
+        c[n][k] = c[n - 1][k - 1] + (k <= n - 1 ? c[n - 1][k] : 0.0);
+    }
+    return c;
+  }();
   double m[2 * GB300_LMAX + 2];
   for (int n = 0; n <= la + lb; n++)
     m[n] = n == 0 ? 1.0 : pow(n / (2.0 * M_E * d.zetp), 0.5 * n);
   double B[3][GB300_LMAX + 1][GB300_LMAX + 1];
   for (int dir = 0; dir < 3; dir++) {
     const double pa = d.rp[dir] - ra[dir], pb = d.rp[dir] - (ra[dir] + d.rab[dir]);
+    double ppa[GB300_LMAX + 1], ppb[GB300_LMAX + 1];
+    ppa[0] = ppb[0] = 1.0;
+    for (int k = 1; k <= GB300_LMAX; k++) {
+      ppa[k] = ppa[k - 1] * pa;
+      ppb[k] = ppb[k - 1] * pb;
+    }
     for (int xa = 0; xa <= la; xa++)
       for (int xb = 0; xb <= lb; xb++) {
         double al[2 * GB300_LMAX + 2] = {0};
-        double ca = 1.0;
         for (int k = 0; k <= xa; k++) {
-          double cb = 1.0;
-          for (int q = 0; q <= xb; q++) {
-            al[xa - k + xb - q] += ca * cb * pow(pa, k) * pow(pb, q);
-            cb = cb * (xb - q) / (q + 1);
-          }
-          ca = ca * (xa - k) / (k + 1);
+          const double wa = binom[xa][k] * ppa[k];
+          for (int q = 0; q <= xb; q++)
+            al[xa - k + xb - q] += wa * binom[xb][q] * ppb[q];
         }
         double s = 0.0;
         for (int n = 0; n <= xa + xb; n++)
@@ -659,6 +673,26 @@ static bool sphi_is_identity(const grid_basis_set *b, int iset) {
       if (b->sphi[(size_t)(s0 + r) * b->maxco + c] != (r == c ? 1.0 : 0.0))
         return false;
   return true;
+}
+
+// Runs body(i) for i in [0, n) on the host's cores, in contiguous chunks.
+template <typename F> static void parallel_for(int n, const F &body) {
+  const int nt = (int)std::max(1u, std::min(std::thread::hardware_concurrency(), 64u));
+  const int chunks = n < 4096 ? 1 : nt;
+  if (chunks == 1) {
+    for (int i = 0; i < n; i++)
+      body(i);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (int c = 0; c < chunks; c++)
+    th.emplace_back([&, c] {
+      const int i0 = (int)((long long)n * c / chunks), i1 = (int)((long long)n * (c + 1) / chunks);
+      for (int i = i0; i < i1; i++)
+        body(i);
+    });
+  for (auto &x : th)
+    x.join();
 }
 
 static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nkinds,
@@ -755,10 +789,11 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
       norms *= sqrt(h[3 * r] * h[3 * r] + h[3 * r + 1] * h[3 * r + 1] + h[3 * r + 2] * h[3 * r + 2]);
     skew = norms > 0.0 ? 1.0 - fabs(det) / norms : 0.0;
   }
-  std::map<std::pair<int, long long>, int> sphere_of;
-  std::vector<long long> sphere_points;
-  long long maxbuf = 0;
-  for (int s = 0; s < ntasks; s++) {
+  // Phase 1, in parallel over the tasks: everything a task needs that does
+  // not depend on the shared sphere tables (geometry, seeds, general-path
+  // boxes and point counts, class bounds, most features).
+  std::vector<long long> nrad_of(ntasks, -1); // ortho tasks: discretised radius
+  parallel_for(ntasks, [&](int s) {
     const int i = order[s];
     TaskDesc &d = t->tasks[s];
     memset(&d, 0, sizeof(d));
@@ -805,27 +840,7 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
         d.roff[k] = d.rp[k] - ((double)d.center[k]) * L.dh[k * 4];
       }
       const double drmin = fmin(L.dh[0], fmin(L.dh[4], L.dh[8]));
-      const double nrad = fmax(1.0, ceil(d.radius / drmin));
-      const auto key = std::make_pair(lev, (long long)nrad);
-      auto it = sphere_of.find(key);
-      if (it == sphere_of.end()) {
-        SphereHdr h;
-        long long np = 0;
-        build_sphere(L, drmin * nrad, h, t->sph_tab, np);
-        build_sphere_points(h, t->sph_tab, t->sph_pts, t->sph_ploff);
-        t->sph.push_back(h);
-        sphere_points.push_back(np);
-        it = sphere_of.emplace(key, (int)t->sph.size() - 1).first;
-      }
-      d.sphere = it->second;
-      const SphereHdr &h = t->sph[d.sphere];
-      for (int k = 0; k < 3; k++)
-        if (L.npts_global[k] != L.npts_local[k]) { // grid_ref_collint.h:247-255
-          const int off = imod(d.center[k] + h.lb[k] - L.shift[k], L.npts_global[k]) - h.lb[k];
-          if (!(off + 1 - h.lb[k] < L.npts_local[k] && off + h.lb[k] >= 0))
-            fail("task %d: cube does not fit into the local grid of level %d", i, lev);
-        }
-      t->points[s] = sphere_points[d.sphere];
+      nrad_of[s] = (long long)fmax(1.0, ceil(d.radius / drmin));
       // FP64 seeds of the dfloat Gaussian recurrences (grid_kernels.cu)
       for (int dir = 0; dir < 3; dir++) {
         const double h = L.dh[dir * 4], r = d.roff[dir], z = d.zetp;
@@ -884,20 +899,59 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
       t->points[s] = np;
     }
     t->gbound[s] = contribution_bound(d, atom_positions + 3 * ia);
-    {
-      float *f = &t->features[(size_t)s * 6];
-      f[0] = (float)d.la_max;
-      f[1] = (float)d.lb_max;
-      f[2] = (float)(zeta + zetb);
-      if (d.flags & TF_SKIP)
-        f[3] = 0.f;
-      else if (d.flags & TF_GENERAL)
-        f[3] = 0.5f * (float)std::max(d.imax[0] - d.center[0],
-                                      std::max(d.imax[1] - d.center[1], d.imax[2] - d.center[2]));
-      else
-        f[3] = (float)t->sph[d.sphere].cmax;
-      f[4] = (float)L.dh_max;
-      f[5] = (float)skew;
+    float *fe = &t->features[(size_t)s * 6];
+    fe[0] = (float)d.la_max;
+    fe[1] = (float)d.lb_max;
+    fe[2] = (float)(zeta + zetb);
+    if (d.flags & TF_SKIP)
+      fe[3] = 0.f;
+    else if (d.flags & TF_GENERAL)
+      fe[3] = 0.5f * (float)std::max(d.imax[0] - d.center[0],
+                                     std::max(d.imax[1] - d.center[1], d.imax[2] - d.center[2]));
+    fe[4] = (float)L.dh_max;
+    fe[5] = (float)skew;
+  });
+  // Phase 2, in task order: the sphere tables of the orthorhombic tasks
+  // (shared, built on first use) and the subblocks.
+  std::vector<std::vector<char>> sphi_identity(nkinds); // per kind and set
+  for (int kd = 0; kd < nkinds; kd++)
+    for (int st = 0; st < basis_sets[kd]->nset; st++)
+      sphi_identity[kd].push_back(sphi_is_identity(basis_sets[kd], st) ? 1 : 0);
+  std::map<std::pair<int, long long>, int> sphere_of;
+  std::vector<long long> sphere_points;
+  long long maxbuf = 0;
+  for (int s = 0; s < ntasks; s++) {
+    const int i = order[s];
+    TaskDesc &d = t->tasks[s];
+    const int lev = d.level, ia = d.iatom, ja = d.jatom;
+    const int iset = iset_list[i] - 1, jset = jset_list[i] - 1;
+    const grid_basis_set *bi = basis_sets[atom_kinds[ia] - 1];
+    const grid_basis_set *bj = basis_sets[atom_kinds[ja] - 1];
+    const LevelDesc &L = t->levels.lv[lev];
+    if (nrad_of[s] >= 0) {
+      const double drmin = fmin(L.dh[0], fmin(L.dh[4], L.dh[8]));
+      const long long nrad = nrad_of[s];
+      const auto key = std::make_pair(lev, nrad);
+      auto it = sphere_of.find(key);
+      if (it == sphere_of.end()) {
+        SphereHdr h;
+        long long np = 0;
+        build_sphere(L, drmin * (double)nrad, h, t->sph_tab, np);
+        build_sphere_points(h, t->sph_tab, t->sph_pts, t->sph_ploff);
+        t->sph.push_back(h);
+        sphere_points.push_back(np);
+        it = sphere_of.emplace(key, (int)t->sph.size() - 1).first;
+      }
+      d.sphere = it->second;
+      const SphereHdr &h = t->sph[d.sphere];
+      for (int k = 0; k < 3; k++)
+        if (L.npts_global[k] != L.npts_local[k]) { // grid_ref_collint.h:247-255
+          const int off = imod(d.center[k] + h.lb[k] - L.shift[k], L.npts_global[k]) - h.lb[k];
+          if (!(off + 1 - h.lb[k] < L.npts_local[k] && off + h.lb[k] >= 0))
+            fail("task %d: cube does not fit into the local grid of level %d", i, lev);
+        }
+      t->points[s] = sphere_points[d.sphere];
+      t->features[(size_t)s * 6 + 3] = (float)h.cmax;
     }
     // subblock bookkeeping
     const int bn = block_num_list[i] - 1;
@@ -921,7 +975,7 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
       sb.sphia = (int)(sphi_off[atom_kinds[ia] - 1] + (long long)sb.sgfa * bi->maxco);
       sb.sphib = (int)(sphi_off[atom_kinds[ja] - 1] + (long long)sb.sgfb * bj->maxco);
       sb.transpose = ia <= ja;
-      sb.identity = sphi_is_identity(bi, iset) && sphi_is_identity(bj, jset);
+      sb.identity = sphi_identity[atom_kinds[ia] - 1][iset] && sphi_identity[atom_kinds[ja] - 1][jset];
       sb.iatom = ia;
       sb.jatom = ja;
       sb.first_task = s;
