@@ -83,7 +83,7 @@ def build_grid(force: bool = False, verbose_ptxas: bool = False) -> str:
 
     with ThreadPoolExecutor(max_workers=max(1, len(cu))) as ex:
         list(ex.map(compile_one, zip(cu, objs)))
-    _run([nvcc, *ARCH, "-shared", "-o", GRID_LIB, *objs, "-lcudart", "-lcuda"])
+    _run([nvcc, *ARCH, "-shared", "-o", GRID_LIB, *objs, "-lcudart", "-lcuda", "-lpthread"])
     return GRID_LIB
 
 
