@@ -763,15 +763,29 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
     if (!(radius_list[i] >= 0.0) || !std::isfinite(radius_list[i]))
       fail("task %d: invalid radius %g", i, radius_list[i]);
   }
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-    if (block_num_list[a] != block_num_list[b])
-      return block_num_list[a] < block_num_list[b];
-    if (iset_list[a] != iset_list[b])
-      return iset_list[a] < iset_list[b];
-    if (jset_list[a] != jset_list[b])
-      return jset_list[a] < jset_list[b];
-    return level_list[a] < level_list[b];
-  });
+  // stable order by (block, iset, jset, level): sort packed keys with the
+  // input index as the last key
+  {
+    struct Key {
+      int block, iset, jset, level, i;
+    };
+    std::vector<Key> keys(ntasks);
+    for (int i = 0; i < ntasks; i++)
+      keys[i] = Key{block_num_list[i], iset_list[i], jset_list[i], level_list[i], i};
+    std::sort(keys.begin(), keys.end(), [](const Key &a, const Key &b) {
+      if (a.block != b.block)
+        return a.block < b.block;
+      if (a.iset != b.iset)
+        return a.iset < b.iset;
+      if (a.jset != b.jset)
+        return a.jset < b.jset;
+      if (a.level != b.level)
+        return a.level < b.level;
+      return a.i < b.i;
+    });
+    for (int i = 0; i < ntasks; i++)
+      order[i] = keys[i].i;
+  }
   // ---- tasks, subblocks, sphere tables
   t->tasks.resize(ntasks);
   t->points.assign(ntasks, 0);
