@@ -931,7 +931,7 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
   for (int kd = 0; kd < nkinds; kd++)
     for (int st = 0; st < basis_sets[kd]->nset; st++)
       sphi_identity[kd].push_back(sphi_is_identity(basis_sets[kd], st) ? 1 : 0);
-  std::map<std::pair<int, long long>, int> sphere_of;
+  std::vector<std::vector<int>> sphere_of(nlevels); // [level][nrad] -> sphere, or -1
   std::vector<long long> sphere_points;
   long long maxbuf = 0;
   for (int s = 0; s < ntasks; s++) {
@@ -945,18 +945,19 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
     if (nrad_of[s] >= 0) {
       const double drmin = fmin(L.dh[0], fmin(L.dh[4], L.dh[8]));
       const long long nrad = nrad_of[s];
-      const auto key = std::make_pair(lev, nrad);
-      auto it = sphere_of.find(key);
-      if (it == sphere_of.end()) {
+      std::vector<int> &known = sphere_of[lev];
+      if ((long long)known.size() <= nrad)
+        known.resize((size_t)nrad + 1, -1);
+      if (known[nrad] < 0) {
         SphereHdr h;
         long long np = 0;
         build_sphere(L, drmin * (double)nrad, h, t->sph_tab, np);
         build_sphere_points(h, t->sph_tab, t->sph_pts, t->sph_ploff);
         t->sph.push_back(h);
         sphere_points.push_back(np);
-        it = sphere_of.emplace(key, (int)t->sph.size() - 1).first;
+        known[nrad] = (int)t->sph.size() - 1;
       }
-      d.sphere = it->second;
+      d.sphere = known[nrad];
       const SphereHdr &h = t->sph[d.sphere];
       for (int k = 0; k < 3; k++)
         if (L.npts_global[k] != L.npts_local[k]) { // grid_ref_collint.h:247-255
