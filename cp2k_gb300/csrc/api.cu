@@ -677,7 +677,9 @@ static bool sphi_is_identity(const grid_basis_set *b, int iset) {
 
 // Runs body(i) for i in [0, n) on the host's cores, in contiguous chunks.
 template <typename F> static void parallel_for(int n, const F &body) {
-  const int nt = (int)std::max(1u, std::min(std::thread::hardware_concurrency(), 64u));
+  int nt = (int)std::max(1u, std::min(std::thread::hardware_concurrency(), 64u));
+  if (const char *e = getenv("GRID_GB300_HOST_THREADS")) // testing: fix the thread count
+    nt = std::max(1, std::min(atoi(e), 64));
   const int chunks = n < 4096 ? 1 : nt;
   if (chunks == 1) {
     for (int i = 0; i < n; i++)
@@ -704,7 +706,7 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
                         const int *block_num_list, const double *radius_list,
                         const double *rab_list, const int *npts_global, const int *npts_local,
                         const int *shift_local, const int *border_width, const double *dh,
-                        const double *dh_inv) {
+                        const double *dh_inv, bool host_only = false) {
   TaskList *t = new TaskList();
   t->ortho = ortho;
   t->ntasks = ntasks;
@@ -1006,6 +1008,8 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
     d.subblock = (int)t->subs.size() - 1;
   }
   t->buffer_len = maxbuf;
+  if (host_only) // grid_gb300_host_digest: the host preparation alone
+    return t;
   // ---- upload
   CK(cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking));
   for (auto &e : t->ev)
@@ -1536,6 +1540,50 @@ GB300_API void grid_gb300_create_task_list(
   t->precision = prec;
   t->schedule = sched;
   *task_list = t;
+}
+
+// FNV-1a over the bytes of a vector of plain structs
+template <typename V> static unsigned long long fnv_bytes(const V &v) {
+  unsigned long long h = 1469598103934665603ull;
+  const unsigned char *p = (const unsigned char *)v.data();
+  for (size_t i = 0; i < v.size() * sizeof(v[0]); i++) {
+    h ^= p[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+GB300_API void grid_gb300_host_digest(
+    const bool orthorhombic, const int ntasks, const int nlevels, const int natoms,
+    const int nkinds, const int nblocks, const int *block_offsets, const double *atom_positions,
+    const int *atom_kinds, const grid_basis_set **basis_sets, const int *level_list,
+    const int *iatom_list, const int *jatom_list, const int *iset_list, const int *jset_list,
+    const int *ipgf_list, const int *jpgf_list, const int *border_mask_list,
+    const int *block_num_list, const double *radius_list, const double *rab_list,
+    const int *npts_global, const int *npts_local, const int *shift_local,
+    const int *border_width, const double *dh, const double *dh_inv,
+    unsigned long long digest[12]) {
+  TaskList *t = create(orthorhombic, ntasks, nlevels, natoms, nkinds, nblocks, block_offsets,
+                       atom_positions, atom_kinds, basis_sets, level_list, iatom_list,
+                       jatom_list, iset_list, jset_list, ipgf_list, jpgf_list,
+                       border_mask_list, block_num_list, radius_list, rab_list, npts_global,
+                       npts_local, shift_local, border_width, dh, dh_inv, true);
+  digest[0] = fnv_bytes(t->tasks);
+  digest[1] = fnv_bytes(t->seeds);
+  digest[2] = fnv_bytes(t->gbound);
+  digest[3] = fnv_bytes(t->features);
+  digest[4] = fnv_bytes(t->points);
+  digest[5] = fnv_bytes(t->subs);
+  digest[6] = fnv_bytes(t->sph);
+  digest[7] = fnv_bytes(t->sph_tab);
+  digest[8] = fnv_bytes(t->sph_pts);
+  digest[9] = fnv_bytes(t->sph_ploff);
+  digest[10] = (unsigned long long)t->cart_total;
+  unsigned long long n32 = 0;
+  for (double g : t->gbound)
+    n32 += g <= 0.3;
+  digest[11] = n32;
+  delete t;
 }
 
 GB300_API void grid_gb300_free_task_list(grid_gb300_task_list *task_list) {

@@ -197,6 +197,31 @@ class BasisSet:
             pass
 
 
+def host_digest(inp: TaskListInputs) -> np.ndarray:
+    """grid_gb300_host_digest: hashes of the host-side task-list preparation
+    (no GPU needed); 12 unsigned 64-bit words."""
+    L = lib()
+    basis = [BasisSet(b) for b in inp.basis_sets]
+    bs = (C.c_void_p * max(1, len(basis)))(*[b.h.value for b in basis])
+    i32 = lambda a: np.ascontiguousarray(a, np.int32)
+    f64 = lambda a: np.ascontiguousarray(a, np.float64)
+    head = [i32(inp.block_offsets), f64(inp.atom_positions), i32(inp.atom_kinds)]
+    lists = [i32(inp.level_list), i32(inp.iatom_list), i32(inp.jatom_list),
+             i32(inp.iset_list), i32(inp.jset_list), i32(inp.ipgf_list), i32(inp.jpgf_list),
+             i32(inp.border_mask_list), i32(inp.block_num_list), f64(inp.radius_list),
+             f64(inp.rab_list)]
+    levels = [i32(inp.npts_global), i32(inp.npts_local), i32(inp.shift_local),
+              i32(inp.border_width), f64(inp.dh), f64(inp.dh_inv)]
+    out = np.zeros(12, np.uint64)
+    L.grid_gb300_host_digest(bool(inp.orthorhombic), inp.ntasks, inp.nlevels, inp.natoms,
+                             inp.nkinds, inp.nblocks, *[_p(a) for a in head],
+                             C.cast(bs, C.c_void_p), *[_p(a) for a in lists],
+                             *[_p(a) for a in levels], _p(out))
+    for b in basis:
+        b.free()
+    return out
+
+
 class GridTaskList:
     """A GB300 task list for ``TaskListInputs`` (see cp2k_gb300.tasklist).
 

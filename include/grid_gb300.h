@@ -467,6 +467,26 @@ const char *grid_gb300_static_scratch_error(void);
 /* Last error message recorded by the library ("" if none). */
 const char *grid_gb300_last_error(void);
 
+/* ---- testing ---------------------------------------------------------------
+ * Runs the host-side preparation of grid_gb300_create_task_list (ordering,
+ * per-task geometry, seeds, class bounds, features, sphere tables,
+ * subblocks) without touching the GPU, and returns FNV-1a hashes of the
+ * prepared arrays: digest[0..9] tasks, seeds, class bounds, features, point
+ * counts, subblocks, sphere headers, sphere tables, sphere points, point
+ * offsets; digest[10] the Cartesian scratch size; digest[11] the number of
+ * tasks whose class bound is <= 0.3.  The preparation runs on the host's
+ * cores; GRID_GB300_HOST_THREADS fixes their number. */
+void grid_gb300_host_digest(
+    const bool orthorhombic, const int ntasks, const int nlevels, const int natoms,
+    const int nkinds, const int nblocks, const int *block_offsets, const double *atom_positions,
+    const int *atom_kinds, const grid_basis_set **basis_sets, const int *level_list,
+    const int *iatom_list, const int *jatom_list, const int *iset_list, const int *jset_list,
+    const int *ipgf_list, const int *jpgf_list, const int *border_mask_list,
+    const int *block_num_list, const double *radius_list, const double *rab_list,
+    const int *npts_global, const int *npts_local, const int *shift_local,
+    const int *border_width, const double *dh, const double *dh_inv,
+    unsigned long long digest[12]);
+
 #ifdef __cplusplus
 }
 #endif

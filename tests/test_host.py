@@ -80,6 +80,24 @@ def test_struct_layouts_match_ctypes(tmp_path):
             assert seen[(cname, f)] == getattr(py, f).offset, (cname, f)
 
 
+@pytest.mark.parametrize("name,scale", [("c2_512atoms", 0.3), ("c3_256atoms_triclinic", 0.5)])
+def test_host_preparation_independent_of_threads(grid_lib, name, scale, monkeypatch):
+    """The host-side task-list preparation runs on several threads: its
+    arrays (hashed by grid_gb300_host_digest, no GPU needed) are the same
+    with one thread as with eight, and the class split is non-trivial."""
+    from cp2k_gb300 import grid as G
+    from cp2k_gb300 import workload as W
+    inp = W.config(name, scale=scale, seed=3)
+    assert inp.ntasks > 4096  # large enough for the threaded path
+    monkeypatch.setenv("GRID_GB300_HOST_THREADS", "1")
+    one = G.host_digest(inp)
+    monkeypatch.setenv("GRID_GB300_HOST_THREADS", "8")
+    eight = G.host_digest(inp)
+    assert np.array_equal(one, eight)
+    assert one[10] > 0                     # Cartesian scratch
+    assert 0 < one[11] < inp.ntasks        # FP32-class tasks at the default bound
+
+
 def test_library_exports_every_declared_symbol(grid_lib):
     out = subprocess.run(["nm", "-D", "--defined-only", grid_lib], capture_output=True,
                          text=True, check=True).stdout
