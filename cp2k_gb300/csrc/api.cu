@@ -39,6 +39,7 @@ static std::atomic<long long> g_launches{0};
 void count_launch(int n) { g_launches += n; }
 static std::atomic<const char *> g_launch_error{nullptr};
 void launch_error(const char *msg) { g_launch_error = msg; }
+const char *take_launch_error() { return g_launch_error.exchange(nullptr); }
 
 static std::mutex g_err_mu;
 static char g_last_error[512] = "";
@@ -856,7 +857,8 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
         d.roff[k] = d.rp[k] - ((double)d.center[k]) * L.dh[k * 4];
       }
       const double drmin = fmin(L.dh[0], fmin(L.dh[4], L.dh[8]));
-      nrad_of[s] = (long long)fmax(1.0, ceil(d.radius / drmin));
+      // clamped before the cast; radii past the int16 tables fail later
+      nrad_of[s] = (long long)fmin(fmax(1.0, ceil(d.radius / drmin)), 1e9);
       // FP64 seeds of the dfloat Gaussian recurrences (grid_kernels.cu)
       for (int dir = 0; dir < 3; dir++) {
         const double h = L.dh[dir * 4], r = d.roff[dir], z = d.zetp;
@@ -948,6 +950,11 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
       const double drmin = fmin(L.dh[0], fmin(L.dh[4], L.dh[8]));
       const long long nrad = nrad_of[s];
       std::vector<int> &known = sphere_of[lev];
+      // the sphere tables hold int16 offsets: radii past 32767 grid steps
+      // cannot be tabulated (and must not size this lookup)
+      if (nrad > 32767)
+        fail("task %d: radius %g spans more than 32767 grid steps of level %d", i,
+             radius_list[i], lev);
       if ((long long)known.size() <= nrad)
         known.resize((size_t)nrad + 1, -1);
       if (known[nrad] < 0) {
@@ -1223,7 +1230,7 @@ static int ensure(void **p, size_t *cap, size_t bytes) {
 }
 
 static void check_device_error(TaskList *t) {
-  if (const char *m = g_launch_error.exchange(nullptr))
+  if (const char *m = take_launch_error())
     fail("%s", m);
   int err = 0;
   CK(cudaMemcpy(&err, t->d_error, sizeof(int), cudaMemcpyDeviceToHost));

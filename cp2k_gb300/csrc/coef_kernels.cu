@@ -1129,6 +1129,11 @@ void launch_post(const PostArgs &a, int arith, int words_per_warp, cudaStream_t 
     launch_post_t<double>(a, words_per_warp, s);
 }
 
+bool coefficients_fit(int words_per_group) {
+  const GroupLaunch L = group_launch(words_per_group, 1);
+  return L.grid >= 1 && L.smem <= kSmemBudget;
+}
+
 size_t coef_words(int la, int lb) {
   return coef_smem_words(ncoset(la), ncoset(lb), la, lb, la + lb);
 }

@@ -261,6 +261,15 @@ inline void launch_integrate(const GridArgs &a, int arith, bool general, int buc
   c.blocks = nblocks;
   launch_integrate(a, arith, general, bucket, extent, c, s);
 }
+// Host-side checks that a launch of the grid kernels (`iwidth`: the general
+// point-list kernel's box width) or of the coefficient kernel fits the
+// shared-memory budget; the launch wrappers refuse what does not fit through
+// launch_error().
+bool grid_launch_fits(int arith, bool general, bool collocate, int bucket, int extent,
+                      int variant, int iwidth);
+bool general_launch_fits(int arith, bool collocate, int lpb, int njmax, int variant,
+                         int iwidth);
+bool coefficients_fit(int words_per_group);
 // general path: FP64 for ARITH_FP64 and ARITH_MIXED, FP32 for ARITH_FP32
 void launch_collocate_general_impl(const GridArgs &a, int arith, int lpb,
                                    int njmax, LaunchCfg &cfg, cudaStream_t s);
@@ -336,6 +345,8 @@ void count_launch(int n = 1);
 // records a launch-configuration error; the host call fails after the launch
 // sequence (reported like a device error)
 void launch_error(const char *msg);
+// returns and clears the message recorded by launch_error (nullptr if none)
+const char *take_launch_error();
 
 // learned cost model (mlp_kernels.cu)
 int mlp_nparams();

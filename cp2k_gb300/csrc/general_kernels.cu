@@ -1226,7 +1226,30 @@ void launch_gen_any(const GridArgs &a, bool collocate, int arith, int lpb, int n
   }
 }
 
+template <typename T, int LPB>
+size_t gen_per_warp(bool collocate, int njmax, int variant, int iwidth) {
+  constexpr bool can_pl = !std::is_same<T, double>::value;
+  return can_pl && collocate && variant == 1 ? PlSmem<T, LPB>::bytes(njmax, iwidth)
+                                             : GenSmem<T, LPB>::bytes(njmax);
+}
+
 } // namespace
+
+bool general_launch_fits(int arith, bool collocate, int lpb, int njmax, int variant, int iwidth) {
+  size_t pw = 0;
+  switch (lpb) {
+#define GB_CASE(LP)                                                            \
+  case LP:                                                                     \
+    pw = arith == ARITH_FP32    ? gen_per_warp<float, LP>(collocate, njmax, variant, iwidth)  \
+         : arith == ARITH_MIXED ? gen_per_warp<dfloat, LP>(collocate, njmax, variant, iwidth) \
+                                : gen_per_warp<double, LP>(collocate, njmax, variant, iwidth); \
+    break;
+    GB_CASE(4) GB_CASE(6) GB_CASE(9) GB_CASE(12) GB_CASE(16)
+#undef GB_CASE
+  default: return false;
+  }
+  return warps_for(pw) >= 1;
+}
 
 void launch_collocate_general_impl(const GridArgs &a, int arith, int lpb, int njmax,
                                    LaunchCfg &cfg, cudaStream_t s) {

@@ -764,6 +764,39 @@ static void launch_grid(const GridArgs &a, int arith, bool general, bool colloca
   }
 }
 
+template <typename N, int LPB>
+static size_t ortho_per_warp(bool collocate, int variant, int wmax) {
+  return collocate && variant == 1 ? OrthoSmem<N, LPB>::bytes_coll_pl(wmax)
+         : collocate               ? OrthoSmem<N, LPB>::bytes_coll(wmax)
+                                   : OrthoSmem<N, LPB>::bytes_int(wmax);
+}
+
+template <int LPB>
+static size_t ortho_per_warp_lp(int arith, bool collocate, int variant, int wmax) {
+  if (arith == ARITH_FP64)
+    return ortho_per_warp<double, LPB>(collocate, variant, wmax);
+  if (arith == ARITH_FP32)
+    return ortho_per_warp<float, LPB>(collocate, variant, wmax);
+  return ortho_per_warp<dfloat, LPB>(collocate, variant, wmax);
+}
+
+bool grid_launch_fits(int arith, bool general, bool collocate, int bucket, int extent,
+                      int variant, int iwidth) {
+  if (bucket < 0 || bucket >= kNumBuckets || extent < 1)
+    return false;
+  if (general)
+    return general_launch_fits(arith, collocate, kBucketLp[bucket], extent, variant, iwidth);
+  size_t pw = 0;
+  switch (kBucketLp[bucket]) {
+  case 4: pw = ortho_per_warp_lp<4>(arith, collocate, variant, extent); break;
+  case 6: pw = ortho_per_warp_lp<6>(arith, collocate, variant, extent); break;
+  case 9: pw = ortho_per_warp_lp<9>(arith, collocate, variant, extent); break;
+  case 12: pw = ortho_per_warp_lp<12>(arith, collocate, variant, extent); break;
+  case 16: pw = ortho_per_warp_lp<16>(arith, collocate, variant, extent); break;
+  }
+  return warps_for(pw) >= 1;
+}
+
 void launch_collocate(const GridArgs &a, int arith, bool general, int bucket, int extent,
                       LaunchCfg &cfg, cudaStream_t s) {
   launch_grid(a, arith, general, true, bucket, extent, cfg, s);

@@ -1,14 +1,15 @@
 // Allocation-free single-task collocation.
 //
-// Some callers cannot allocate device memory while they run: code executing
-// inside a CUDA graph that is being captured or replayed, memory-pool
-// allocators that hand out one fixed arena, embedded drivers that forbid
-// cudaMalloc after start-up.  grid_gb300_collocate_pgf_product_static lets
-// them collocate one primitive pair with device buffers they already own:
-// every piece of per-call scratch (the task descriptor, sphere bounds,
-// polynomial coefficients, work counters) lives in one file-scope
-// __device__ array of fixed size, kStaticScratchBytes, that every GPU which
-// loads this library holds until the process exits.
+// Some callers cannot allocate device memory while they run: a program that
+// reserved all of the GPU's memory for its own pool at start-up and hands out
+// pieces of that arena only, and drivers that forbid cudaMalloc/cudaFree after
+// initialisation because those calls can synchronise the whole device and
+// stall every other stream.  grid_gb300_collocate_pgf_product_static lets them
+// collocate one primitive pair with device buffers they already own: every
+// piece of per-call scratch (the task descriptor, sphere bounds, polynomial
+// coefficients, work counters) lives in one file-scope __device__ array of
+// fixed size, kStaticScratchBytes, that every GPU which loads this library
+// holds until the process exits.
 //
 // The array is shared by all calls: each call overwrites what the previous
 // one left (the work counter and error word are reset by the call itself),
@@ -16,6 +17,12 @@
 // ordering) race on it.  The first call on a device resolves the array's
 // device address with cudaGetSymbolAddress, so that first call should come
 // before any stream capture.
+//
+// Errors are found on the host before anything is copied or launched: the
+// scratch layout, the coefficient kernel's and the grid kernel's shared-
+// memory budgets.  The grid kernel's own per-task size check (an error word
+// in the scratch array) cannot trigger for a launch planned from this one
+// task, and it is not read back, which would need a synchronisation.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -38,7 +45,8 @@ namespace {
 
 std::mutex g_mu;
 void *g_addr[64] = {}; // device address of g_static_scratch per device ordinal
-char g_err[256] = "";
+// the last error of a call, per calling host thread
+thread_local char g_err[256] = "";
 
 int set_error(const char *msg) {
   snprintf(g_err, sizeof(g_err), "%s", msg);
@@ -243,6 +251,12 @@ GB300_API int grid_gb300_collocate_pgf_product_static(
   if (off > kStaticScratchBytes)
     return set_error("task needs more scratch than the static array holds "
                      "(grid_gb300_static_scratch_bytes)");
+  const int coef_w = (int)coef_words(la_max + dl.la_max, lb_max + dl.lb_max);
+  if (!coefficients_fit(coef_w))
+    return set_error("angular momenta too large for the coefficient kernel's shared memory");
+  if (!grid_launch_fits(ARITH_FP64, general, true, bucket_of(lp), extent, 0, 0))
+    return set_error(general ? "general path: box too large for shared memory"
+                             : "orthorhombic path: cube too large for shared memory");
 
   std::vector<unsigned char> host(o_coef, 0);
   memcpy(&host[o_task], &d, sizeof(d));
@@ -275,7 +289,11 @@ GB300_API int grid_gb300_collocate_pgf_product_static(
   co.d = dl;
   co.levels = (const LevelSet *)(dev + o_levels);
   co.dhtab = (const double *)(dev + o_dhtab);
-  launch_coefficients(co, ARITH_FP64, (int)coef_words(la_max + dl.la_max, lb_max + dl.lb_max), s);
+  launch_coefficients(co, ARITH_FP64, coef_w, s);
+  if (const char *m = take_launch_error())
+    return set_error(m);
+  if (cudaGetLastError() != cudaSuccess)
+    return set_error("coefficient kernel launch failed");
 
   GridArgs ga{};
   ga.tasks = (const TaskDesc *)(dev + o_task);
@@ -294,7 +312,9 @@ GB300_API int grid_gb300_collocate_pgf_product_static(
   ga.coef_stride = 1;
   ga.grid_stride = 1;
   launch_collocate(ga, ARITH_FP64, general, bucket_of(lp), extent, 1, s);
+  if (const char *m = take_launch_error())
+    return set_error(m);
   if (cudaGetLastError() != cudaSuccess)
-    return set_error("kernel launch failed");
+    return set_error("grid kernel launch failed");
   return 0;
 }

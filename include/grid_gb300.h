@@ -437,8 +437,9 @@ void grid_gb300_apply_cost_model(const grid_gb300_task_list *task_list,
                                  void *stream);
 
 /* Allocation-free collocation of one primitive pair, for callers that
- * cannot allocate device memory at call time (inside CUDA-graph capture, under
- * a fixed memory arena, in drivers that forbid cudaMalloc after start-up).
+ * cannot allocate device memory at call time (a program that gave the GPU's
+ * memory to its own fixed arena at start-up, drivers that forbid cudaMalloc
+ * after initialisation because it can synchronise the whole device).
  * No counterpart in CP2K; the arguments mean what they mean for
  * grid_cpu_collocate_pgf_product (src/grid/cpu/grid_cpu_collocate.h), with
  * pab ([n2][n1]) and grid (npts_local, x fastest; collocated values are
@@ -450,8 +451,10 @@ void grid_gb300_apply_cost_model(const grid_gb300_task_list *task_list,
  * whose kernels overlap on the GPU race, calls on one stream are ordered.
  * The first call on a device looks up the array's address and should come
  * before any stream capture.  Returns 0, or nonzero with a message in
- * grid_gb300_static_scratch_error() when the task needs more scratch than
- * the array holds or an argument is out of range. */
+ * grid_gb300_static_scratch_error() (the calling thread's last message) when
+ * the task needs more scratch than the array holds, its cube or box exceeds
+ * the kernels' shared memory, or an argument is out of range; these checks
+ * run on the host before anything is copied or launched. */
 int grid_gb300_collocate_pgf_product_static(
     const bool orthorhombic, const int border_mask, const int func,
     const int la_max, const int la_min, const int lb_max, const int lb_min,

@@ -1,9 +1,10 @@
 """The allocation-free entry point grid_gb300_collocate_pgf_product_static.
 
-Callers that cannot allocate device memory while they run (code inside CUDA
-graph capture, fixed memory arenas, drivers that forbid cudaMalloc after
-start-up) collocate single primitive pairs through it; its scratch is one
-static device array shared by all calls.  Each recorded CP2K task is
+Callers that cannot allocate device memory while they run (a program that
+gave the GPU's memory to its own fixed arena at start-up, drivers that forbid
+cudaMalloc after initialisation because it can synchronise the device)
+collocate single primitive pairs through it; its scratch is one static device
+array shared by all calls.  Each recorded CP2K task is
 collocated twice in a row through it (through the C ABI) and both results are
 compared with the task-list entry point (grid_gb300_collocate_device_async on
 a one-task list) at the FP64 tolerance of the other parity tests.  This file
@@ -67,3 +68,36 @@ def test_static_scratch_rejects_oversized_task():
     assert G.collocate_pgf_product_static(t2, pab, out) != 0
     torch.cuda.synchronize()
     assert float(out.abs().max()) == 0.0
+
+
+def test_static_scratch_rejects_box_beyond_shared_memory():
+    """A general-path task (border mask set) whose index box fits the static
+    array but not the grid kernel's shared memory is refused on the host with
+    a message, and a task-list call made afterwards still runs and matches the
+    oracle (no stale launch error is left behind)."""
+    import torch
+    from cp2k_gb300 import grid as G
+    from cp2k_gb300.tasklist import single_task_list
+    from oracle import oracle as O
+
+    base = digest_task(load_digests()["ortho_density_l0000"])
+    t = dict(base)
+    h = 0.01
+    t["dh"] = [[h, 0, 0], [0, h, 0], [0, 0, h]]
+    t["dh_inv"] = [[1 / h, 0, 0], [0, 1 / h, 0], [0, 0, 1 / h]]
+    t["radius"] = 200.0  # 40,000 points along j: per-warp tables > 200 KB
+    t["border_mask"] = 1
+    t["npts_global"] = t["npts_local"] = [64, 64, 64]
+    pab = torch.tensor(np.ascontiguousarray(t["pab"]).ravel(), device="cuda")
+    out = torch.zeros(8, dtype=torch.float64, device="cuda")
+    assert G.collocate_pgf_product_static(t, pab, out) != 0
+    assert b"shared memory" in G.lib().grid_gb300_static_scratch_error()
+    torch.cuda.synchronize()
+    assert float(out.abs().max()) == 0.0
+    inp = single_task_list(base)
+    tl = G.GridTaskList(inp, precision=G.FP64)
+    ot = O.OracleTaskList(inp)
+    pab_c = (0.5 * base["rscale"] * base["pab"]).ravel()
+    assert rel_diff(tl.collocate(base["func"], pab_c)[0], ot.collocate(base["func"], pab_c)[0]) < 1e-12
+    tl.close()
+    ot.close()
