@@ -11,18 +11,23 @@ grid_integrate_task_list (hab only), as one SCF iteration does.
   e2e        the same step through the CP2K C ABI with host offload buffers
              (H2D pab + V grids, D2H rho grids + hab inside the timed region);
   fp64_*     the plain FP64 path timed the same way;
-  errors     mixed vs the FP64 path on the same inputs (the FP64 path is
-             pinned to the oracle at 1e-12 by the test-suite);
-  roofline   the dominant grid kernel (largest share of a mixed step, from
-             per-launch CUDA events) against measured peaks;
-  cpu_baseline  the oracle (FP64 C restatement of CP2K's REF backend) on the
-             host cores, on a bounded random sample of the tasks, scaled to a
-             full step by grid points.
+  errors     mixed / FP64 / FP32 against the oracle's FP64 results on the
+             same inputs (and mixed against the FP64 path);
+  roofline   the dominant grid kernel of the mixed step (largest total time
+             from per-launch CUDA events) against the measured HBM roof, and
+             against the CUDA-core FMA roof that binds it (roofline_fp32);
+             roofline_fp64 the same for the FP64 step;
+  cpu_baseline  whole SCF steps of the oracle (FP64 C restatement of CP2K's
+             REF backend) on all host cores;
+  triclinic_256atoms_forces_virial, c5_6144atoms_forces
+             the other workloads' mixed and FP64 steps with forces (and
+             virial), errors against the oracle, the oracle's step time and
+             the task-list creation time (--no-secondary skips them).
 
---impl reference times the reference's CPU implementation of the path (the
-oracle port, all host threads) on the same workload and prints the same
-metric.  Under torchrun every rank runs an independent replica (the path has
-no data exchange on one GPU); rank 0 prints the max over ranks.
+--impl reference times whole SCF steps of the reference's CPU implementation
+of the path (the oracle port, all host threads) on the same workload and
+prints the same metric.  Under torchrun every rank runs an independent replica
+(the path has no data exchange on one GPU); rank 0 prints the max over ranks.
 """
 from __future__ import annotations
 
@@ -149,52 +154,33 @@ def barrier(world: int):
 
 
 # --------------------------------------------------------------------------
-# CPU baseline: the oracle on a bounded sample
+# CPU baseline: whole SCF steps of the oracle
 # --------------------------------------------------------------------------
-def cpu_sample_time(inp, pab, V, target_s: float = 1.0, seed: int = 0):
-    """Times the oracle's collocate + integrate on a random subset of tasks and
-    scales to the whole task list by grid points visited."""
-    from cp2k_gb300.tasklist import TaskListInputs
+def oracle_steps(inp, pab, V, nsteps: int, warmup: int = 0, forces: bool = False,
+                 virial: bool = False):
+    """Times whole SCF steps (collocate GRID_FUNC_AB + integrate) of the oracle
+    -- the FP64 C restatement of CP2K's REF backend -- on all host threads.
+    Task-list creation is outside the timed region, as it is for the GPU.
+    Returns (ms per step list, rho, hab, forces, virial) of the last step."""
     from oracle import oracle as O
 
-    full = O.OracleTaskList(inp)
-    pts, _ = full.count_points(100)
-    full.close()
-    total = float(pts.sum())
-    rng = np.random.default_rng(seed)
-    keys = ("level_list", "iatom_list", "jatom_list", "iset_list", "jset_list", "ipgf_list",
-            "jpgf_list", "border_mask_list", "block_num_list", "radius_list", "rab_list")
-
-    def timed(frac):
-        sel = np.sort(rng.choice(inp.ntasks, size=max(1, int(frac * inp.ntasks)), replace=False))
-        sub = TaskListInputs(**{**inp.__dict__, **{k: getattr(inp, k)[sel] for k in keys}})
-        tl = O.OracleTaskList(sub)
+    ot = O.OracleTaskList(inp)
+    times, out = [], None
+    for i in range(warmup + nsteps):
         t0 = time.perf_counter()
-        tl.collocate(100, pab)
-        tl.integrate(V)
-        dt = time.perf_counter() - t0
-        tl.close()
-        return sel, dt
+        rho = ot.collocate(100, pab)
+        hab, f, v = ot.integrate(V, pab if (forces or virial) else None, forces=forces,
+                                 virial=virial)
+        dt = (time.perf_counter() - t0) * 1e3
+        if i >= warmup:
+            times.append(dt)
+        out = (rho, hab, f, v)
+    ot.close()
+    return times, out
 
-    # two independent samples, the second twice the size of the first, fit
-    # t = t_fixed + t_per_point * points so that per-call costs (thread-local
-    # grid reduction) are not scaled up with the points
-    frac = 0.002
-    sel, dt = timed(frac)
-    while dt < 0.5 * target_s and frac < 0.25:
-        frac = min(0.25, frac * min(8.0, target_s / max(dt, 1e-3)))
-        sel, dt = timed(frac)
-    sel1, dt1 = timed(frac)
-    sel2, dt2 = timed(min(1.0, 2 * frac))
-    p1, p2 = float(pts[sel1].sum()), float(pts[sel2].sum())
-    per_pt = max((dt2 - dt1) / max(p2 - p1, 1.0), dt2 / max(p2, 1.0) * 0.5)
-    fixed = max(0.0, dt1 - per_pt * p1)
-    ms = (fixed + per_pt * total) * 1e3
-    sel, dt, sample_pts = sel2, dt2, p2
-    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return ms, threads, (f"{len(sel)} of {inp.ntasks} tasks ({sample_pts / total * 100:.2f}% of "
-                         f"grid points) in {dt:.2f} s and a half-size sample; fixed + per-point cost "
-                         f"fitted and scaled to all grid points")
+
+def host_threads() -> int:
+    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
 
 
 def reference_arm(args, world, rank):
@@ -207,22 +193,18 @@ def reference_arm(args, world, rank):
     inp = W.config(WORKLOAD)
     pab = W.density_blocks(inp)
     V = W.potential_grids(inp)
-    vals = []
-    for _ in range(max(1, args.warmup)):
-        cpu_sample_time(inp, pab, V)
-    for k in range(args.steps):
-        ms, threads, sample = cpu_sample_time(inp, pab, V, seed=k)
-        vals.append(ms)
-    v = float(np.mean(vals))
+    times, _ = oracle_steps(inp, pab, V, args.steps, args.warmup)
+    v = float(np.mean(times))
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "ms",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": v, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": CONFIG,
-        "cpu_baseline": {"value": v, "unit": "ms", "cores": threads, "kind": "port",
-                         "sample": sample + "; oracle = C restatement of CP2K's REF backend "
-                                            "(CP2K's sources, needed to build its own CPU "
-                                            "backend, are not present on the GPU host)"},
+        "cpu_baseline": {"value": v, "unit": "ms", "cores": host_threads(), "kind": "port",
+                         "sample": f"{args.steps} whole SCF steps of the workload ({inp.ntasks} "
+                                   f"tasks each), mean; oracle = C restatement of CP2K's REF "
+                                   f"backend (CP2K's own CPU backend cannot be built on the GPU "
+                                   f"host: its sources are not there)"},
         "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -231,19 +213,19 @@ def reference_arm(args, world, rank):
 # --------------------------------------------------------------------------
 # GPU arm
 # --------------------------------------------------------------------------
-def measure_fp32_peak(torch):
-    """CUDA-core FP32 FMA peak as cuBLAS SGEMM reaches it (TF32 disabled)."""
+def measure_peak(torch, dtype, n):
+    """cuBLAS GEMM throughput (TFLOP/s) in `dtype` with TF32 off: the CUDA-core
+    FP32 FMA peak (float32) or the FP64 peak (float64) of this GPU."""
     prev = torch.backends.cuda.matmul.allow_tf32
     torch.backends.cuda.matmul.allow_tf32 = False
-    n = 8192
-    a = torch.randn(n, n, device="cuda")
-    b = torch.randn(n, n, device="cuda")
+    a = torch.randn(n, n, device="cuda", dtype=dtype)
+    b = torch.randn(n, n, device="cuda", dtype=dtype)
     for _ in range(2):
         torch.mm(a, b)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     best = 0.0
-    for _ in range(5):
+    for _ in range(3):
         e0.record()
         torch.mm(a, b)
         e1.record()
@@ -254,14 +236,13 @@ def measure_fp32_peak(torch):
     return best
 
 
-# DRAM bytes per launch of the dominant kernels, from the ncu capture named
-# beside each figure (dram__bytes_read.sum + dram__bytes_write.sum); the
-# bench cannot run ncu itself.  Keys: kernel label as in "roofline.kernel".
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# dominant kernels of the 512-atom mixed and FP64 steps, from one ncu capture
+# of this workload (two launches per kernel, mean); the bench cannot run ncu
+# itself.  Keys: kernel label as in "roofline.kernel".
 NCU_TRAFFIC = {
-    # profiles/grid_kernels_c2_512atoms_mixed.md (2 launches each, mean);
-    # the double-float collocation runs the point-list kernel
-    "collocate_ortho<dfloat,4>": 0.5 * ((55.521 + 17.446) + (296.367 + 888.955)) * 1e6,
-    "integrate_ortho<dfloat,4>": 0.5 * ((37.712 + 1.315) + (244.637 + 67.789)) * 1e6,
+    "integrate_ortho<dfloat,4>": None,
+    "integrate_ortho<double,4>": None,
 }
 
 
@@ -283,6 +264,151 @@ def load_cost_model(torch):
         return CM.CostModel.from_bytes(fh.read()), os.path.relpath(path, ROOT)
 
 
+def kernel_times(torch, tl, G, prec, sched, step, flush, nsteps=3):
+    """Per grid-kernel launch CUDA events (recorded on the launching stream)
+    over `nsteps` steps: label -> {ms: [...], points, flops, launches, phase}
+    and the total visited points per phase."""
+    tl.set_precision(prec)
+    tl.set_schedule(sched)
+    tl.set_launch_timing(True)
+    per, phase_points = {}, [0.0, 0.0]
+    for _ in range(nsteps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        infos = step()
+        for i in infos:
+            k = per.setdefault(_kernel_label(i), {"ms": [], "points": 0.0, "flops": 0.0,
+                                                  "launches": 0, "phase": i["phase"]})
+            k["ms"].append(i["ms"])
+            k["points"] += i["points"]
+            k["flops"] += i["flops"]
+            k["launches"] += 1
+            phase_points[i["phase"]] += i["points"]
+    tl.set_launch_timing(False)
+    return per, phase_points
+
+
+def roofline_objects(per, phase_points, field_points, peaks, peak_kind, fp_peak, fp_kind, arith):
+    """The dominant kernel (largest total time) against the HBM roof and
+    against the CUDA-core FMA roof of its arithmetic.
+
+    Algorithmic HBM bytes of a step: every grid point written once by the
+    collocate phase (8 B FP64 grid, plus 4 B of FP32 low words in the mixed
+    mode) or read once by the integrate phase (8 B: FP64 or hi/lo float
+    pairs); a launch is charged the share of its phase's visited points that
+    it visits.  Algorithmic flops of a launch: 2 (lp + 1) per visited point
+    (the separable inner-loop minimum)."""
+    dom = max(per, key=lambda k: sum(per[k]["ms"]))
+    d = per[dom]
+    avg_ms = float(np.mean(d["ms"]))
+    if d["phase"] == 0:
+        bpp = 12.0 if arith == "mixed" else 8.0
+    else:
+        bpp = 8.0
+    share = d["points"] / max(phase_points[d["phase"]], 1.0)
+    alg_bytes = bpp * field_points * share
+    alg_flops = d["flops"] / d["launches"]
+    gbs = alg_bytes / (avg_ms * 1e-3) / 1e9
+    tf = alg_flops / (avg_ms * 1e-3) / 1e12
+    traffic = NCU_TRAFFIC.get(dom)
+    hbm = {"bound": "hbm", "achieved": gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+           "frac": gbs / peaks.get("hbm_gbs", 1.0), "traffic": traffic, "kernel": dom,
+           "launch_ms": avg_ms, "launches_per_step": d["launches"] / 3.0,
+           "algorithmic_bytes_per_launch": alg_bytes, "peak_kind": peak_kind,
+           "binding": False}
+    fma = {"bound": "fp32_fma" if arith != "fp64" else "fp64_fma", "achieved": tf,
+           "peak": fp_peak, "unit": "TFLOP/s", "frac": tf / fp_peak, "peak_kind": fp_kind,
+           "kernel": dom, "launch_ms": avg_ms, "flops_per_launch": alg_flops, "binding": True}
+    share_k = {k: sum(v["ms"]) / sum(sum(x["ms"]) for x in per.values())
+               for k, v in sorted(per.items(), key=lambda kv: -sum(kv[1]["ms"]))}
+    return hbm, fma, share_k
+
+
+def field_energy(rho, V, inp):
+    dvol = [abs(float(np.linalg.det(d_))) for d_ in inp.dh]
+    return sum(float((np.asarray(g) * np.asarray(v)).sum()) * dv for g, v, dv in zip(rho, V, dvol))
+
+
+def errors_vs(rho, hab, rho_ref, hab_ref, V, inp, f=None, f_ref=None, vir=None, vir_ref=None):
+    """The reference's measure max |d| / max(1, |ref|) for rho, hab, forces,
+    virial; max |d| / max |rho|; Tr(V rho) energy error per atom (Ha)."""
+    rel = lambda a, b: float(np.max(np.abs(np.asarray(a) - np.asarray(b))
+                                    / np.maximum(1.0, np.abs(np.asarray(b)))))
+    out = {
+        "rho_max_rel_ref_measure": max(rel(a, b) for a, b in zip(rho, rho_ref)),
+        "rho_max_abs_over_max_rho": max(float(np.abs(np.asarray(a) - np.asarray(b)).max())
+                                        for a, b in zip(rho, rho_ref))
+        / max(float(np.abs(np.asarray(b)).max()) for b in rho_ref),
+        "energy_ha_per_atom": abs(field_energy(rho, V, inp) - field_energy(rho_ref, V, inp))
+        / inp.natoms,
+        "hab_max_rel": rel(hab, hab_ref),
+    }
+    if f is not None:
+        out["forces_max_rel"] = rel(f, f_ref)
+    if vir is not None:
+        out["virial_max_rel"] = rel(vir, vir_ref)
+    return out
+
+
+def secondary_case(torch, G, W, name, forces, virial, nsteps, cpu_steps, flush):
+    """Mixed and FP64 step times (device-resident, default launch shapes, size
+    schedule) of another workload, with forces / virial as its configuration
+    asks, errors against the oracle's FP64 results, the oracle's own step
+    time on the host cores, and the task-list creation time."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    t0 = time.perf_counter()
+    inp = W.config(name)
+    pab_h = W.density_blocks(inp)
+    V_h = W.potential_grids(inp)
+    gen_s = time.perf_counter() - t0
+    pab = torch.tensor(pab_h, device=dev)
+    V = [torch.tensor(v, device=dev) for v in V_h]
+    grids = [torch.empty(n, dtype=torch.float64, device=dev) for n in inp.grid_sizes()]
+    hab = torch.empty(inp.buffer_size, dtype=torch.float64, device=dev)
+    f = torch.empty((inp.natoms, 3), dtype=torch.float64, device=dev) if forces else None
+    vir = torch.empty((3, 3), dtype=torch.float64, device=dev) if virial else None
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tl = G.GridTaskList(inp, api="cp2k")
+    torch.cuda.synchronize()
+    create_s = time.perf_counter() - t0
+    stream = torch.cuda.Stream(device=dev)
+    res, outs = {"ntasks": inp.ntasks, "forces": forces, "virial": virial,
+                 "task_list_create_s": create_s, "workload_generate_s": gen_s}, {}
+    for prec, key in ((G.MIXED, "mixed"), (G.FP64, "fp64")):
+        tl.set_precision(prec)
+        times = []
+        for i in range(1 + nsteps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            with torch.cuda.stream(stream):
+                e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+                e[0].record(stream)
+                tl.collocate_device(100, pab, grids, stream=stream)
+                tl.integrate_device(V, hab, pab_dev=pab if (forces or virial) else None,
+                                    forces_dev=f, virial_dev=vir, stream=stream)
+                e[1].record(stream)
+            torch.cuda.synchronize()
+            if i:
+                times.append(e[0].elapsed_time(e[1]))
+        res[f"{key}_ms_per_step"] = float(np.mean(times))
+        outs[key] = ([g.cpu().numpy() for g in grids], hab.cpu().numpy(),
+                     f.cpu().numpy() if f is not None else None,
+                     vir.cpu().numpy() if vir is not None else None)
+    res["speedup_vs_fp64"] = res["fp64_ms_per_step"] / res["mixed_ms_per_step"]
+    tl.close()
+    del pab, V, grids, hab, f, vir
+    torch.cuda.empty_cache()
+    ctimes, ref = oracle_steps(inp, pab_h, V_h, cpu_steps, 0, forces=forces, virial=virial)
+    res["cpu_baseline"] = {"value": float(np.mean(ctimes)), "unit": "ms", "cores": host_threads(),
+                           "kind": "port", "sample": f"{cpu_steps} whole SCF step(s)"}
+    for key in ("mixed", "fp64"):
+        rho, h, ff, vv = outs[key]
+        res[f"errors_{key}_vs_oracle"] = errors_vs(rho, h, ref[0], ref[1], V_h, inp, ff, ref[2],
+                                                   vv, ref[3])
+    return res
+
+
 def gpu_arm(args, world, rank, local):
     import torch
 
@@ -299,7 +425,11 @@ def gpu_arm(args, world, rank, local):
     grids = [torch.empty(n, dtype=torch.float64, device=dev) for n in inp.grid_sizes()]
     hab = torch.empty(inp.buffer_size, dtype=torch.float64, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
     tl = G.GridTaskList(inp, api="cp2k")
+    torch.cuda.synchronize()
+    create_s = time.perf_counter() - t0
     stream = torch.cuda.Stream(device=dev)
     model, model_path = load_cost_model(torch)
     if model is not None:
@@ -317,6 +447,14 @@ def gpu_arm(args, world, rank, local):
         torch.cuda.synchronize()
 
     launched = [0, 0]  # kernel counter at the first timed step, launches in timed steps
+
+    def one_step():
+        with torch.cuda.stream(stream):
+            tl.collocate_device(100, pab, grids, stream=stream)
+        infos = tl.launch_timings()
+        with torch.cuda.stream(stream):
+            tl.integrate_device(V, hab, stream=stream)
+        return infos + tl.launch_timings()
 
     def run_steps(prec, sched, nsteps, warm=1):
         # a precision or schedule switch may rebuild work queues on the host:
@@ -355,8 +493,8 @@ def gpu_arm(args, world, rank, local):
     launches = launched[1]
     torch.cuda.synchronize()
     barrier(world)
-    rho_mixed = [g.clone() for g in grids]
-    hab_mixed = hab.clone()
+    rho_mixed = [g.cpu().numpy() for g in grids]
+    hab_mixed = hab.cpu().numpy()
     # the same step replayed as one CUDA graph
     graph = tl.capture_step(100, pab, grids, V, hab, stream=stream)
     t_graph = []
@@ -374,81 +512,30 @@ def gpu_arm(args, world, rank, local):
     graph.free()
     t_size = run_steps(G.MIXED, G.SCHEDULE_SIZE, max(1, min(args.steps, 5)))
     t_fp64 = run_steps(G.FP64, G.SCHEDULE_SIZE, max(1, min(args.steps, 3)))
-    rho64 = [g.clone() for g in grids]
-    hab64 = hab.clone()
+    rho64 = [g.cpu().numpy() for g in grids]
+    hab64 = hab.cpu().numpy()
     t_fp32 = run_steps(G.FP32, sched_mixed, max(1, min(args.steps, 5)))
-    rho32 = [g.clone() for g in grids]
-    hab32 = hab.clone()
+    rho32 = [g.cpu().numpy() for g in grids]
+    hab32 = hab.cpu().numpy()
 
     ms_mixed = max_over_ranks(float(np.mean(t_mixed)), world)
     ms_size = max_over_ranks(float(np.mean(t_size)), world)
     ms_fp64 = max_over_ranks(float(np.mean(t_fp64)), world)
     ms_fp32 = max_over_ranks(float(np.mean(t_fp32)), world)
 
-    # per-launch CUDA events of one mixed step (outside the timed region):
-    # the dominant kernel is the one with the largest total time
-    tl.set_precision(G.MIXED)
-    tl.set_schedule(sched_mixed)
-    tl.set_launch_timing(True)
-    per_kernel = {}
-    for _ in range(3):
-        flush.zero_()
-        torch.cuda.synchronize()
-        with torch.cuda.stream(stream):
-            tl.collocate_device(100, pab, grids, stream=stream)
-        infos = tl.launch_timings()
-        with torch.cuda.stream(stream):
-            tl.integrate_device(V, hab, stream=stream)
-        infos = infos + tl.launch_timings()
-        for i in infos:
-            k = per_kernel.setdefault(_kernel_label(i), {"ms": [], "points": 0.0, "flops": 0.0,
-                                                         "launches": 0})
-            k["ms"].append(i["ms"])
-            k["points"] += i["points"]
-            k["flops"] += i["flops"]
-            k["launches"] += 1
-    tl.set_launch_timing(False)
-    dom = max(per_kernel, key=lambda k: sum(per_kernel[k]["ms"]))
-    d = per_kernel[dom]
-    avg_ms = float(np.mean(d["ms"]))
-    # algorithmic HBM bytes of one launch: every grid point written once
-    # (collocate: FP64 grid, 8 B, plus the FP32 low-word grid for double-float,
-    # 4 B) or read once (integrate: float2 / double 8 B, float 4 B); the many
-    # per-task visits of a point are L2 traffic, not HBM traffic
-    arith = dom.split("<")[1].split(",")[0]
-    if dom.startswith("collocate"):
-        bytes_per_point = 12.0 if arith == "dfloat" else 8.0
-    else:
-        bytes_per_point = 4.0 if arith == "float" else 8.0
-    alg_bytes = bytes_per_point * float(sum(inp.grid_sizes()))
-    visit_bytes = bytes_per_point * d["points"] / d["launches"]
-    alg_flops = d["flops"] / d["launches"]
-    kernel_share = {k: sum(v["ms"]) / sum(sum(x["ms"]) for x in per_kernel.values())
-                    for k, v in sorted(per_kernel.items(), key=lambda kv: -sum(kv[1]["ms"]))}
-
-    # errors of the mixed / FP32 paths against the FP64 path
-    dvol = [abs(float(np.linalg.det(d_))) for d_ in inp.dh]
-    e64 = sum(float((g * v).sum()) * dv for g, v, dv in zip(rho64, V, dvol))
-
-    def errors(rho, habx):
-        e = sum(float((g * v).sum()) * dv for g, v, dv in zip(rho, V, dvol))
-        return {
-            "rho_max_rel_ref_measure": max(
-                float(((a - b).abs() / b.abs().clamp(min=1.0)).max()) for a, b in zip(rho, rho64)),
-            "rho_max_abs_over_max_rho": max(float((a - b).abs().max()) for a, b in zip(rho, rho64))
-            / max(float(b.abs().max()) for b in rho64),
-            "energy_ha_per_atom": abs(e - e64) / inp.natoms,
-            "hab_max_rel": float((habx - hab64).abs().max()) / max(1.0, float(hab64.abs().max())),
-        }
-
-    err_mixed = errors(rho_mixed, hab_mixed)
-    err_fp32 = errors(rho32, hab32)
-
+    # per-launch CUDA events of mixed and FP64 steps (outside the timed region)
     peaks, peak_kind = _peaks()
-    fp32_peak = measure_fp32_peak(torch)
-    achieved_gbs = alg_bytes / (avg_ms * 1e-3) / 1e9
-    achieved_tf = alg_flops / (avg_ms * 1e-3) / 1e12
-    traffic = NCU_TRAFFIC.get(dom)
+    fp32_peak = measure_peak(torch, torch.float32, 8192)
+    fp64_peak = measure_peak(torch, torch.float64, 4096)
+    field_points = float(sum(inp.grid_sizes()))
+    per_m, pp_m = kernel_times(torch, tl, G, G.MIXED, sched_mixed, one_step, flush)
+    roof_hbm, roof_fp32, share_mixed = roofline_objects(
+        per_m, pp_m, field_points, peaks, peak_kind, fp32_peak,
+        "measured cuBLAS SGEMM (TF32 off) on this GPU", "mixed")
+    per_d, pp_d = kernel_times(torch, tl, G, G.FP64, G.SCHEDULE_SIZE, one_step, flush)
+    roof_hbm64, roof_fp64, share_fp64 = roofline_objects(
+        per_d, pp_d, field_points, peaks, peak_kind, fp64_peak,
+        "measured cuBLAS DGEMM on this GPU", "fp64")
 
     # e2e through the CP2K C ABI with host offload buffers: inputs are placed
     # in the pinned host buffers once (as CP2K fills them); each timed step
@@ -465,16 +552,27 @@ def gpu_arm(args, world, rank, local):
         tl.integrate(copy_out=False)
         e2e.append((time.perf_counter() - t0) * 1e3)
     e2e_ms = max_over_ranks(float(np.mean(e2e)), world)
-    grid_pts = float(sum(inp.grid_sizes()))
-    h2d = 8 * inp.buffer_size + 8 * int(grid_pts)  # pab + V grids
-    d2h = 8 * int(grid_pts) + 8 * inp.buffer_size  # rho grids + hab
+    h2d = 8 * inp.buffer_size + 8 * int(field_points)  # pab + V grids
+    d2h = 8 * int(field_points) + 8 * inp.buffer_size  # rho grids + hab
+    tl.close()
+    del pab, V, grids, hab
+    torch.cuda.empty_cache()
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        ms, threads, sample = cpu_sample_time(inp, pab_h, V_h)
-        cpu = {"value": ms, "unit": "ms", "cores": threads, "kind": "port", "sample": sample}
-
+    line = None
     if rank == 0:
+        # the oracle: whole FP64 SCF steps on the host cores (CPU baseline),
+        # and the FP64 reference results the errors are measured against
+        cpu, err_oracle = None, {}
+        if world == 1 and not args.no_cpu_baseline:
+            ctimes, ref = oracle_steps(inp, pab_h, V_h, 3, 0)
+            cpu = {"value": float(np.mean(ctimes)), "unit": "ms", "cores": host_threads(),
+                   "kind": "port",
+                   "sample": f"3 whole SCF steps of the workload ({inp.ntasks} tasks each), mean"}
+            err_oracle = {
+                "mixed": errors_vs(rho_mixed, hab_mixed, ref[0], ref[1], V_h, inp),
+                "fp64": errors_vs(rho64, hab64, ref[0], ref[1], V_h, inp),
+                "fp32": errors_vs(rho32, hab32, ref[0], ref[1], V_h, inp),
+            }
         line = {
             "metric": METRIC, "value": ms_mixed, "unit": "ms", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_mixed,
@@ -491,28 +589,33 @@ def gpu_arm(args, world, rank, local):
                          for p, v in tuned.items()},
             "cost_model_gain": ms_size / ms_mixed - 1.0,
             "fp32_ms_per_step": ms_fp32, "fp32_speedup_vs_fp64": ms_fp64 / ms_fp32,
-            "errors_mixed_vs_fp64": err_mixed,
-            "errors_fp32_vs_fp64": err_fp32,
-            "targets": {"speedup_vs_fp64": 3.0, "rho_max_rel": 1e-6, "energy_ha_per_atom": 1e-8},
-            "kernel_share_mixed": kernel_share,
-            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks.get("hbm_gbs"),
-                         "unit": "GB/s", "frac": achieved_gbs / peaks.get("hbm_gbs", 1.0),
-                         "traffic": traffic, "kernel": dom, "launch_ms": avg_ms,
-                         "algorithmic_bytes_per_launch": alg_bytes,
-                         "grid_visit_bytes_per_launch": visit_bytes,
-                         "peak_kind": peak_kind},
-            "roofline_fp32": {"bound": "fp32_fma", "achieved": achieved_tf, "peak": fp32_peak,
-                              "unit": "TFLOP/s", "frac": achieved_tf / fp32_peak,
-                              "peak_kind": "measured cuBLAS SGEMM (TF32 off) on this GPU",
-                              "kernel": dom, "flops_per_launch": alg_flops},
+            "errors_mixed_vs_oracle": err_oracle.get("mixed"),
+            "errors_fp64_vs_oracle": err_oracle.get("fp64"),
+            "errors_fp32_vs_oracle": err_oracle.get("fp32"),
+            "errors_mixed_vs_fp64": errors_vs(rho_mixed, hab_mixed, rho64, hab64, V_h, inp),
+            "targets": {"speedup_vs_fp64": 3.0, "rho_max_rel": 1e-6, "energy_ha_per_atom": 1e-8,
+                        "fp64_rel": 1e-12},
+            "kernel_share_mixed": share_mixed,
+            "kernel_share_fp64": share_fp64,
+            "roofline": roof_hbm,
+            "roofline_fp32": roof_fp32,
+            "roofline_fp64": roof_fp64,
+            "roofline_fp64_hbm": roof_hbm64,
+            "task_list_create_s": create_s,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
         }
+    # secondary workloads (reported beside the headline, not part of it)
+    if rank == 0 and world == 1 and not args.no_secondary:
+        line["triclinic_256atoms_forces_virial"] = secondary_case(
+            torch, G, W, "c3_256atoms_triclinic", True, True, 5, 2, flush)
+        line["c5_6144atoms_forces"] = secondary_case(
+            torch, G, W, "c5_6144atoms", True, False, 3, 1, flush)
+    if rank == 0:
         print(json.dumps(line), flush=True)
-    tl.close()
 
 
 def main():
@@ -522,6 +625,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the triclinic and 6144-atom lines")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

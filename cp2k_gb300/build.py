@@ -49,7 +49,8 @@ def _run(cmd: list[str]) -> None:
 def build_workload(force: bool = False) -> str:
     src = os.path.join(CSRC, "workload.c")
     if force or _stale(WORKLOAD_LIB, [src]):
-        _run(["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-o", WORKLOAD_LIB, src, "-lm"])
+        _run(["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-ffp-contract=off", "-o", WORKLOAD_LIB,
+              src, "-lm"])
     return WORKLOAD_LIB
 
 

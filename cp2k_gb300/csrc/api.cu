@@ -22,6 +22,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <numeric>
 #include <string>
@@ -1533,10 +1534,26 @@ GB300_API void grid_gb300_create_task_list(
     const int *npts_global, const int *npts_local, const int *shift_local,
     const int *border_width, const double *dh, const double *dh_inv,
     grid_gb300_task_list **task_list) {
-  int prec = GRID_GB300_FP64, sched = GRID_GB300_SCHEDULE_SIZE;
-  if (*task_list) { // re-creation keeps the caller's settings
-    prec = TL(*task_list)->precision;
-    sched = TL(*task_list)->schedule;
+  // Re-creation through an existing handle (CP2K does this at every change
+  // of geometry, src/grid/grid_task_list.c:42-63) keeps the caller's
+  // settings: precision, schedule, mixed threshold, collocate variant, model
+  // bin width, tuned launch shapes and timing switches.  Per-task data (model
+  // predictions, timings) belong to the old geometry and are dropped; the
+  // learned schedule falls back to the size order until a model is applied.
+  struct Kept {
+    int precision, schedule, coll_variant;
+    double mixed_threshold, model_bin;
+    int small_extent[3];
+    std::map<std::tuple<int, int, int>, LaunchCfg> tuned;
+    bool launch_timing, task_timing;
+  };
+  std::unique_ptr<Kept> kept;
+  if (*task_list) {
+    const TaskList *o = TL(*task_list);
+    kept.reset(new Kept{o->precision, o->schedule, o->coll_variant, o->mixed_threshold,
+                        o->model_bin, {o->small_extent[0], o->small_extent[1],
+                                       o->small_extent[2]},
+                        o->tuned, o->launch_timing, o->task_timing});
     grid_gb300_free_task_list(*task_list);
   }
   TaskList *t = create(orthorhombic, ntasks, nlevels, natoms, nkinds, nblocks, block_offsets,
@@ -1544,8 +1561,20 @@ GB300_API void grid_gb300_create_task_list(
                        jatom_list, iset_list, jset_list, ipgf_list, jpgf_list,
                        border_mask_list, block_num_list, radius_list, rab_list, npts_global,
                        npts_local, shift_local, border_width, dh, dh_inv);
-  t->precision = prec;
-  t->schedule = sched;
+  t->precision = GRID_GB300_FP64;
+  t->schedule = GRID_GB300_SCHEDULE_SIZE;
+  if (kept) {
+    t->precision = kept->precision;
+    t->schedule = kept->schedule;
+    t->coll_variant = kept->coll_variant;
+    t->mixed_threshold = kept->mixed_threshold;
+    t->model_bin = kept->model_bin;
+    for (int i = 0; i < 3; i++)
+      t->small_extent[i] = kept->small_extent[i];
+    t->tuned = kept->tuned;
+    t->launch_timing = kept->launch_timing;
+    t->task_timing = kept->task_timing;
+  }
   *task_list = t;
 }
 

@@ -232,9 +232,21 @@ class GridTaskList:
                  schedule: int | None = SCHEDULE_SIZE, api: str = "backend"):
         # precision / schedule None: keep what the library chose at creation
         # (at the CP2K surface the environment may set the precision)
-        L = lib()
-        self.inp = inp
         self.api = api
+        self.h = C.c_void_p()
+        self._create(inp)
+        if precision is not None:
+            self.set_precision(precision)
+        if schedule is not None:
+            self.set_schedule(schedule)
+
+    def _create(self, inp: TaskListInputs):
+        """grid_create_task_list (or grid_gb300_create_task_list) into self.h;
+        a non-NULL handle is re-created in place, as CP2K does at every change
+        of geometry (src/grid/grid_task_list.c:42-63)."""
+        L = lib()
+        old_basis = getattr(self, "basis", [])
+        self.inp = inp
         self.basis = [BasisSet(b) for b in inp.basis_sets]
         self._bs = (C.c_void_p * max(1, len(self.basis)))(*[b.h.value for b in self.basis])
         i32 = lambda a: np.ascontiguousarray(a, np.int32)
@@ -248,20 +260,27 @@ class GridTaskList:
                   i32(inp.border_width), f64(inp.dh), f64(inp.dh_inv)]
         self._arrays += lists + levels
         self.npts_local = levels[1]
-        self.h = C.c_void_p()
-        fn = L.grid_create_task_list if api == "cp2k" else L.grid_gb300_create_task_list
+        fn = L.grid_create_task_list if self.api == "cp2k" else L.grid_gb300_create_task_list
         fn(bool(inp.orthorhombic), inp.ntasks, inp.nlevels, inp.natoms, inp.nkinds,
            inp.nblocks, _p(self._arrays[0]), _p(self._arrays[1]), _p(self._arrays[2]),
            C.cast(self._bs, C.c_void_p), *[_p(a) for a in lists], *[_p(a) for a in levels],
            C.byref(self.h))
         self.impl = self._impl_handle()
-        if precision is not None:
-            self.set_precision(precision)
-        if schedule is not None:
-            self.set_schedule(schedule)
+        # the list kept pointers to the old basis sets until now
+        for b in old_basis:
+            b.free()
+        for buf in ([getattr(self, "_pab", None), getattr(self, "_hab", None)]
+                    + list(getattr(self, "_grids", None) or [])):
+            if buf is not None:
+                buf.free()
         self._pab = None
         self._hab = None
         self._grids = None
+
+    def recreate(self, inp: TaskListInputs):
+        """Re-create the task list through its existing handle for new inputs
+        (a moved geometry); the backend keeps the settings made on it."""
+        self._create(inp)
 
     def _impl_handle(self):
         if self.api == "cp2k":

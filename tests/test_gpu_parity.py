@@ -113,13 +113,15 @@ def test_sample_task_fp32(G, O, name):
     ot.close()
 
 
-# The triclinic l<=4 case with compute_tau reaches contraction order 11 on
-# |hab| ~ 2e3: two FP64 evaluation orders differ there by up to ~7e-12
-# relative (the oracle and CP2K's REF backend themselves differ by 1.3e-12),
-# so its bound is 1e-11.
+# Reduced-size variants of the workloads (seed 5 at full size is in
+# test_parity_fullsize.py).  The triclinic l<=4 case with compute_tau reaches
+# contraction order 11 on |hab| ~ 2e3: two FP64 evaluation orders differ
+# there by up to ~7e-12 relative (on the full-size workload CP2K's REF
+# backend and the oracle themselves differ by 1.7e-12,
+# tests/golden/fp64_spread.json), so its bound is 1e-11.
 @pytest.mark.parametrize("name,scale,funcs,tol", [
-    ("c1_64atoms", 0.3, (100, 200, 302, 412, 503, 602, 703, 801, 902, 906, 1003), 5e-12),
-    ("c2_512atoms", 0.08, (100,), 5e-12),
+    ("c1_64atoms", 0.3, (100, 200, 302, 412, 503, 602, 703, 801, 902, 906, 1003), TOL_GRID),
+    ("c2_512atoms", 0.08, (100,), TOL_GRID),
     ("c3_256atoms_triclinic", 0.12, (100, 200), 1e-11),
 ])
 def test_tasklist_fp64(G, O, name, scale, funcs, tol):
@@ -150,8 +152,8 @@ def test_tasklist_fp64(G, O, name, scale, funcs, tol):
 # Stated error bounds of the reduced-precision paths against the FP64 oracle,
 # measured on seeded inputs (uniform [-1, 1] density-matrix blocks and
 # potential), max |d| / max(1, |ref|) unless noted:
-#   MIXED, default split (tasks with contribution bound <= 1 in FP32, the rest
-#       in double-float):                  rho, hab <= 1e-6, forces <= 1e-5
+#   MIXED, default split (tasks with contribution bound <= 0.3 in FP32, the
+#       rest in double-float):             rho, hab <= 1e-6, forces <= 1e-5
 #   MIXED, threshold 0 (all double-float): rho, hab <= 1e-9, forces <= 1e-7
 #   FP32 (plain FP32 per-point work):      max |d| / max |ref| <= 2e-6
 @pytest.mark.parametrize("name,scale", [("c1_64atoms", 0.3), ("c2_512atoms", 0.08),
@@ -203,9 +205,10 @@ def test_cp2k_surface_and_empty_list(G):
     tl.close()
 
 
-def test_recreate_and_schedules_agree(G, O):
-    """Re-creating a task list and reordering its work queue leave the FP64
-    results within rounding."""
+def test_schedules_agree(G, O):
+    """Reordering the work queues (size order, input order) leaves the FP64
+    results within rounding.  (Re-creation through an existing handle is
+    tested in test_parity_fullsize.py.)"""
     from cp2k_gb300 import workload as W
     inp = W.config("c1_64atoms", scale=0.2, seed=4)
     pab = W.density_blocks(inp)
