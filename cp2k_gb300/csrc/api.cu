@@ -1065,11 +1065,11 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase) {
   // one mode per (l shifts, precision, phase): switching the precision back
   // and forth reuses the queues built for each
   const int key = (mode_key(d) * 4 + t->precision) * 3 + phase;
-  // derivatives of the Gaussians (derivative densities; the gradients of tau)
-  // multiply the contributions by up to (2 zeta + l + 1) per unit of
-  // angular-momentum shift, with cancellation in the sums; the FP32 class
-  // then uses the bound scaled by that factor
-  const int dshift = phase == 0 ? d.la_max + d.lb_max : phase == 2 ? 2 : 0;
+  // derivatives of the Gaussians (derivative densities; the gradients of tau;
+  // the forces and virial of an integration) multiply the contributions by up
+  // to (2 zeta + l + 1) per unit of angular-momentum shift, with cancellation
+  // in the sums; the FP32 class then uses the bound scaled by that factor
+  const int dshift = phase == 0 ? d.la_max + d.lb_max : phase == 2 ? 2 : d.la_max;
   auto it = t->modes.find(key);
   if (it != t->modes.end() && it->second.sched_version == t->sched_version)
     return it->second;

@@ -11,7 +11,25 @@ import os
 
 import numpy as np
 
-REFERENCE_ROOT = os.environ.get("CP2K_REFERENCE_ROOT", "/root/reference")
+
+
+def _reference_root() -> str:
+    """The CP2K source tree: CP2K_REFERENCE_ROOT, else the location the
+    oracle's Makefile builds the reference library from."""
+    root = os.environ.get("CP2K_REFERENCE_ROOT")
+    if root:
+        return root
+    oracle_dir = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle")
+    try:
+        import subprocess
+        r = subprocess.run(["make", "-s", "-C", oracle_dir, "print-ref-root"],
+                           capture_output=True, text=True, timeout=30)
+        return r.stdout.strip()
+    except Exception:
+        return ""
+
+
+REFERENCE_ROOT = _reference_root()
 SAMPLE_DIR = os.path.join(REFERENCE_ROOT, "src", "grid", "sample_tasks")
 GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 DIGEST_FILE = os.path.join(GOLDEN_DIR, "sample_task_digests.json.gz")
