@@ -552,6 +552,16 @@ def gpu_arm(args, world, rank, local):
         tl.integrate(copy_out=False)
         e2e.append((time.perf_counter() - t0) * 1e3)
     e2e_ms = max_over_ranks(float(np.mean(e2e)), world)
+    # the same with the copies in one piece each (no overlap with the kernels)
+    tl.set_copy_chunks(1)
+    e2e1 = []
+    for _ in range(max(3, min(args.steps, 5))):
+        t0 = time.perf_counter()
+        tl.collocate(100, copy_out=False)
+        tl.integrate(copy_out=False)
+        e2e1.append((time.perf_counter() - t0) * 1e3)
+    tl.set_copy_chunks(3)
+    e2e_one_piece = max_over_ranks(float(np.mean(e2e1[1:])), world)
     h2d = 8 * inp.buffer_size + 8 * int(field_points)  # pab + V grids
     d2h = 8 * int(field_points) + 8 * inp.buffer_size  # rho grids + hab
     tl.close()
@@ -605,6 +615,7 @@ def gpu_arm(args, world, rank, local):
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
+            "e2e_copies_in_one_piece_ms": e2e_one_piece,
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
         }

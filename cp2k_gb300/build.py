@@ -1,6 +1,7 @@
 """In-tree build of the package's native libraries.
 
-* ``libgb300grid.so``  -- the CUDA backend and its C ABI (nvcc, sm_103a only);
+* ``libgb300grid.so``  -- the CUDA backend and its C ABI (nvcc, sm_103a only;
+  linked with cuFFT for the plane-wave transfer of the level grids);
 * ``libgb300workload.so`` -- the host-only synthetic task-list generator (gcc).
 
 Both land next to this file (``cp2k_gb300/``) and are git-ignored.  Builds run
@@ -84,7 +85,8 @@ def build_grid(force: bool = False, verbose_ptxas: bool = False) -> str:
 
     with ThreadPoolExecutor(max_workers=max(1, len(cu))) as ex:
         list(ex.map(compile_one, zip(cu, objs)))
-    _run([nvcc, *ARCH, "-shared", "-o", GRID_LIB, *objs, "-lcudart", "-lcuda", "-lpthread"])
+    _run([nvcc, *ARCH, "-shared", "-o", GRID_LIB, *objs, "-lcudart", "-lcuda", "-lcufft",
+          "-lpthread"])
     return GRID_LIB
 
 

@@ -249,6 +249,17 @@ GB300_API const char *grid_gb300_last_error(void) { return g_last_error; }
 // ===========================================================================
 namespace gb300 {
 
+// Copy chunks of the host-buffer calls: subblock ranges in block order,
+// chunk c holding subblocks [sub_lo[c], sub_lo[c+1]) and the block-buffer
+// elements [el_lo[c], el_lo[c+1]) (which partition the buffer).
+struct CopyChunks {
+  int n = 1;
+  std::vector<int> sub_lo;
+  std::vector<long long> el_lo;
+};
+constexpr int kMaxQueues = 256;          // queue launches per call (work counters)
+constexpr int kQueueKeys = 2 * kNumBuckets * 2 * 2; // (general, bucket, class, size)
+
 struct Queue {
   int *d_idx = nullptr;
   int n = 0;
@@ -261,6 +272,7 @@ struct Queue {
   int general = 0, bucket = 0;
   int fp32 = 0; // mixed path: this queue runs in plain FP32
   int key = 0;          // (general, bucket, FP32 class, size class)
+  int base = 0;         // key of the tuned launch shapes
   long long points = 0; // grid points the queue's tasks visit
   double flops = 0.0;   // 2 (lp+1) points summed over the tasks
 };
@@ -283,7 +295,13 @@ struct Mode { // everything that depends on the l shifts of a call
   int *d_coef_off = nullptr;
   size_t coef_total = 0;
   std::vector<Queue> queues; // launch order
+  // host-buffer calls (nch > 1): per copy chunk and FP32 class (mixed mode)
+  // the tasks whose coefficients (collocate) or post-processing (integrate)
+  // depend on that chunk of pab / hab
+  std::vector<int *> d_chunk_idx; // [chunk * 2 + class]
+  std::vector<int> chunk_n;
   int coef_words = 0;      // per-warp shared memory words of coefficient/post
+  int transform = -1;      // transform variant the words were sized for
   int sched_version = -1;
 };
 
@@ -314,6 +332,7 @@ struct TaskList {
   std::map<std::tuple<int, int, int>, LaunchCfg> tuned; // (precision, phase, queue key) -> shape
   int small_extent[3] = {kSmallExtent, kSmallExtent, kSmallExtent}; // per precision
   int coll_variant = -1; // orthorhombic collocate lanes: 0 row walk, 1 point list, -1 by arith
+  int transform_variant = -1; // C_ab <-> C_xyz: 0 direct, 1 staged, -1 by l (uses_staged)
   std::vector<double> gbound;    // per task bound of |contribution| for |P| <= 1
   std::vector<float2> seeds;     // per task [3][6] dfloat recurrence seeds (ortho)
   float2 *d_seeds = nullptr;
@@ -342,7 +361,13 @@ struct TaskList {
   float *d_gridhi[GB300_MAX_LEVELS] = {};    // mixed integrate: V high words, dense
   float *d_gridlo[GB300_MAX_LEVELS] = {};   // collocate: low words (mixed)
   double *d_forces = nullptr, *d_virial = nullptr;
-  int *d_counters = nullptr; // one per queue launch
+  int *d_counters = nullptr; // one per queue launch (kMaxQueues)
+  // host-buffer calls: pab / hab copies in pieces that overlap the kernels
+  int copy_chunks = 3;
+  CopyChunks chunks;
+  int chunks_for = -1; // copy_chunks the chunks were computed for
+  cudaStream_t copy_stream = nullptr;
+  std::vector<cudaEvent_t> copy_ev;
   int *d_error = nullptr;
   long long *d_cycles = nullptr;
   cudaStream_t stream = nullptr;
@@ -649,6 +674,9 @@ static void free_device(TaskList *t) {
   for (auto &kv : t->modes) {
     if (kv.second.d_coef_off)
       cudaFree(kv.second.d_coef_off);
+    for (int *p : kv.second.d_chunk_idx)
+      if (p)
+        cudaFree(p);
     for (auto &q : kv.second.queues) {
       if (q.d_idx)
         cudaFree(q.d_idx);
@@ -663,6 +691,10 @@ static void free_device(TaskList *t) {
     cudaEventDestroy(e);
   if (t->stream)
     cudaStreamDestroy(t->stream);
+  for (auto &e : t->copy_ev)
+    cudaEventDestroy(e);
+  if (t->copy_stream)
+    cudaStreamDestroy(t->copy_stream);
 }
 
 static bool sphi_is_identity(const grid_basis_set *b, int iset) {
@@ -1050,7 +1082,7 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
   CK(cudaMalloc((void **)&t->d_hab_cart, sizeof(double) * std::max<size_t>(t->cart_total, 1)));
   CK(cudaMalloc((void **)&t->d_forces, sizeof(double) * 3 * std::max(natoms, 1)));
   CK(cudaMalloc((void **)&t->d_virial, sizeof(double) * 9));
-  CK(cudaMalloc((void **)&t->d_counters, sizeof(int) * 64));
+  CK(cudaMalloc((void **)&t->d_counters, sizeof(int) * kMaxQueues));
   CK(cudaMalloc((void **)&t->d_error, sizeof(int)));
   CK(cudaMemset(t->d_error, 0, sizeof(int)));
   return t;
@@ -1061,10 +1093,11 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
 namespace gb300 {
 
 // phase 0 collocate, 1 integrate, 2 integrate with tau
-static Mode &get_mode(TaskList *t, const LDiffs &d, int phase) {
-  // one mode per (l shifts, precision, phase): switching the precision back
-  // and forth reuses the queues built for each
-  const int key = (mode_key(d) * 4 + t->precision) * 3 + phase;
+static Mode &get_mode(TaskList *t, const LDiffs &d, int phase, int nch = 1) {
+  // one mode per (l shifts, precision, phase, copy chunks): switching the
+  // precision back and forth reuses the queues built for each; with nch > 1
+  // (host-buffer calls, t->chunks) every queue holds the tasks of one chunk
+  const int key = ((mode_key(d) * 4 + t->precision) * 3 + phase) * 8 + nch;
   // derivatives of the Gaussians (derivative densities; the gradients of tau;
   // the forces and virial of an integration) multiply the contributions by up
   // to (2 zeta + l + 1) per unit of angular-momentum shift, with cancellation
@@ -1078,25 +1111,37 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase) {
   if (m.d_coef_off == nullptr) {
     m.coef_off.resize(t->ntasks);
     size_t off = 0;
-    int words = 4;
     for (int s = 0; s < t->ntasks; s++) {
       const TaskDesc &k = t->tasks[s];
       const int la = k.la_max + d.la_max, lb = k.lb_max + d.lb_max;
       m.coef_off[s] = (int)off;
-      if (!(k.flags & TF_SKIP)) {
+      if (!(k.flags & TF_SKIP))
         off += ncoset(la + lb);
-        words = std::max(words, (int)coef_words(la, lb));
-      }
       if (off > (size_t)INT32_MAX)
         fail("coefficient buffer exceeds int offsets");
     }
     m.coef_total = off;
-    m.coef_words = words;
     m.d_coef_off = dalloc_copy(m.coef_off);
   }
-  // work queues, descending cost
+  {
+    // shared memory of the coefficient / post kernels (depends on the
+    // transform variant, so it is redone whenever the mode is rebuilt)
+    int words = 4;
+    for (int s = 0; s < t->ntasks; s++) {
+      const TaskDesc &k = t->tasks[s];
+      if (k.flags & TF_SKIP)
+        continue;
+      const int la = k.la_max + d.la_max, lb = k.lb_max + d.lb_max;
+      // collocate: the coefficient kernel (forward); integrate: the post kernel
+      words = std::max(words, (int)coef_words(la, lb, uses_staged(t->transform_variant, la, lb,
+                                                                  phase == 0)));
+    }
+    m.coef_words = words;
+    m.transform = t->transform_variant;
+  }
   // work queues: (general, lp bucket, FP32 class, size class), descending cost
   std::map<int, std::vector<std::pair<double, int>>> items;
+  std::vector<char> task_cls(t->ntasks, -1); // FP32 class, -1: skipped
   for (int s = 0; s < t->ntasks; s++) {
     const TaskDesc &k = t->tasks[s];
     if (k.flags & TF_SKIP)
@@ -1124,6 +1169,7 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase) {
       cost = t->model_bin > 0.0 ? bin + size / (size + 1.0e12) : bin;
     } else
       cost = (double)t->points[s] * (lp + 1) + 64.0 * (lp + 1) * (lp + 2);
+    task_cls[s] = (char)cls;
     items[((g * kNumBuckets + b) * 2 + cls) * 2 + sz].push_back({cost, s});
   }
   for (auto &q : m.queues) {
@@ -1133,6 +1179,27 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase) {
       cudaFree(q.d_items);
   }
   m.queues.clear();
+  for (int *p : m.d_chunk_idx)
+    if (p)
+      cudaFree(p);
+  m.d_chunk_idx.clear();
+  m.chunk_n.clear();
+  if (nch > 1) {
+    // tasks are in subblock order: chunk c's tasks are those of its subblocks
+    for (int c = 0; c < nch; c++) {
+      const int sa = t->chunks.sub_lo[c], sb = t->chunks.sub_lo[c + 1];
+      const int t0 = sa < (int)t->subs.size() ? t->subs[sa].first_task : t->ntasks;
+      const int t1 = sb < (int)t->subs.size() ? t->subs[sb].first_task : t->ntasks;
+      for (int cls = 0; cls < 2; cls++) {
+        std::vector<int> idx;
+        for (int s = t0; s < t1; s++)
+          if (task_cls[s] == cls)
+            idx.push_back(s);
+        m.chunk_n.push_back((int)idx.size());
+        m.d_chunk_idx.push_back(idx.empty() ? nullptr : dalloc_copy(idx));
+      }
+    }
+  }
   // heavier classes first: large cubes, then the arithmetic of the mode, FP32 last
   std::vector<int> keys;
   for (auto &kv : items)
@@ -1153,9 +1220,10 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase) {
     });
     Queue q;
     q.key = key;
-    q.general = key / (2 * 2 * kNumBuckets);
-    q.bucket = (key / 4) % kNumBuckets;
-    q.fp32 = (key >> 1) & 1;
+    q.base = key % kQueueKeys;
+    q.general = q.base / (2 * 2 * kNumBuckets);
+    q.bucket = (q.base / 4) % kNumBuckets;
+    q.fp32 = (q.base >> 1) & 1;
     std::vector<int> idx(v.size());
     int ext = 1;
     for (size_t i = 0; i < v.size(); i++) {
@@ -1277,7 +1345,7 @@ static void grid_launch(TaskList *t, const Queue &q, int phase, int arith, const
   // for plain FP32; on the general path (box around the sphere) the point
   // list wins in every arithmetic that has one (FP32, double-float)
   cfg.variant = t->coll_variant >= 0 ? t->coll_variant : ((q.general || arith != ARITH_FP32) ? 1 : 0);
-  auto it = t->tuned.find(std::make_tuple(t->precision, phase, q.key));
+  auto it = t->tuned.find(std::make_tuple(t->precision, phase, q.base));
   if (it != t->tuned.end())
     cfg = it->second;
   LaunchRecord rec;
@@ -1305,7 +1373,7 @@ static void grid_launch(TaskList *t, const Queue &q, int phase, int arith, const
     in.points = q.points;
     in.flops = q.flops;
     in.ms = 0.0;
-    rec.key = q.key;
+    rec.key = q.base;
     t->launches.push_back(rec);
   }
 }
@@ -1322,17 +1390,41 @@ static void begin_call(TaskList *t, cudaStream_t s) {
   }
 }
 
+// Host-buffer calls: the copies of one call run on the list's copy stream in
+// the pieces of a CopyChunks, overlapping the kernels of earlier pieces.
+struct HostCopy {
+  const CopyChunks *ch = nullptr;
+  cudaStream_t cs = nullptr;       // copy stream
+  const cudaEvent_t *ready = nullptr;  // collocate: pab chunk c is on the device
+  const cudaEvent_t *vready = nullptr; // integrate: V of level l is on the device
+  cudaEvent_t pab_ready = nullptr;     // integrate: pab (forces / virial) is on the device
+  const cudaEvent_t *done = nullptr;   // integrate: hab chunk c is final on the device
+  double *hab_host = nullptr;          // integrate: where hab chunk c goes
+};
+
 static void run_collocate(TaskList *t, int func, const double *pab, double *const *grids,
-                          cudaStream_t s) {
+                          cudaStream_t s, const HostCopy *hc = nullptr) {
   const LDiffs d = func_ldiffs(func);
-  Mode &m = get_mode(t, d, 0);
+  const int nch = hc ? hc->ch->n : 1;
+  Mode &m = get_mode(t, d, 0, nch);
   const int arith = t->precision;
   t->gen += ensure(&t->d_coef, &t->coef_cap, m.coef_total * (arith == ARITH_FP32 ? 4 : 8));
   begin_call(t, s);
   record_phase(t, 0, s);
-  ContractArgs ca{t->d_subs, (int)t->subs.size(), t->d_sphi, pab, nullptr, t->d_pab_cart,
-                  t->contract_words};
-  launch_decontract(ca, s);
+  // the grids are overwritten (grid_ref_task_list.c:418-424)
+  for (int l = 0; l < t->nlevels; l++) {
+    const int *n = &t->npts_local[3 * l];
+    const size_t np = (size_t)n[0] * n[1] * n[2];
+    CK(cudaMemsetAsync(grids[l], 0, sizeof(double) * np, s));
+    if (arith == ARITH_MIXED) {
+      if (!t->d_gridlo[l]) {
+        CK(cudaMalloc((void **)&t->d_gridlo[l], sizeof(float) * np));
+        t->gen++;
+      }
+      CK(cudaMemsetAsync(t->d_gridlo[l], 0, sizeof(float) * np, s));
+    }
+  }
+  CK(cudaMemsetAsync(t->d_counters, 0, sizeof(int) * kMaxQueues, s));
   CoefArgs co{};
   co.tasks = t->d_tasks;
   co.subs = t->d_subs;
@@ -1347,31 +1439,7 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
   co.dhtab = t->d_dhtab;
   co.dhtab_f = t->d_dhtab_f;
   co.dhtab_df = t->d_dhtab_df;
-  if (arith == ARITH_MIXED) {
-    // one launch per work queue, each in the working type of its class: the
-    // kernels stay small (instruction cache) and need no per-task branch
-    for (const Queue &q : m.queues) {
-      co.order = q.d_idx;
-      co.norder = q.n;
-      launch_coefficients_mixed(co, q.fp32 ? (int)ARITH_FP32 : (int)ARITH_MIXED, m.coef_words, s);
-    }
-  } else {
-    launch_coefficients(co, arith, m.coef_words, s);
-  }
-  record_phase(t, 1, s);
-  for (int l = 0; l < t->nlevels; l++) {
-    const int *n = &t->npts_local[3 * l];
-    const size_t np = (size_t)n[0] * n[1] * n[2];
-    CK(cudaMemsetAsync(grids[l], 0, sizeof(double) * np, s));
-    if (arith == ARITH_MIXED) {
-      if (!t->d_gridlo[l]) {
-        CK(cudaMalloc((void **)&t->d_gridlo[l], sizeof(float) * np));
-        t->gen++;
-      }
-      CK(cudaMemsetAsync(t->d_gridlo[l], 0, sizeof(float) * np, s));
-    }
-  }
-  CK(cudaMemsetAsync(t->d_counters, 0, sizeof(int) * 64, s));
+  co.transform = m.transform;
   GridArgs ga{};
   ga.coef_stride = 1;
   ga.grid_stride = 1;
@@ -1391,17 +1459,59 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
   ga.task_cycles = t->task_timing ? t->d_cycles : nullptr;
   ga.seeds = t->d_seeds;
   ga.error = t->d_error;
+  // pab -> Cartesian -> coefficients, piece by piece where the host-buffer
+  // call copies pab in pieces (each waits for its piece only)
+  for (int c = 0; c < nch; c++) {
+    int s0 = 0, ns = (int)t->subs.size();
+    if (hc) { // this piece of pab is on the device
+      CK(cudaStreamWaitEvent(s, hc->ready[c], 0));
+      s0 = hc->ch->sub_lo[c];
+      ns = hc->ch->sub_lo[c + 1] - s0;
+    }
+    ContractArgs ca{t->d_subs + s0, ns, t->d_sphi, pab, nullptr, t->d_pab_cart,
+                    t->contract_words};
+    launch_decontract(ca, s);
+    if (nch > 1) {
+      for (int cls = 0; cls < 2; cls++) {
+        co.order = m.d_chunk_idx[2 * c + cls];
+        co.norder = m.chunk_n[2 * c + cls];
+        if (co.norder == 0)
+          continue;
+        if (arith == ARITH_MIXED)
+          launch_coefficients_mixed(co, cls ? (int)ARITH_FP32 : (int)ARITH_MIXED, m.coef_words,
+                                    s);
+        else
+          launch_coefficients(co, arith, m.coef_words, s);
+      }
+    } else if (arith == ARITH_MIXED) {
+      // one launch per work queue, each in the working type of its class: the
+      // kernels stay small (instruction cache) and need no per-task branch
+      for (const Queue &q : m.queues) {
+        co.order = q.d_idx;
+        co.norder = q.n;
+        launch_coefficients_mixed(co, q.fp32 ? (int)ARITH_FP32 : (int)ARITH_MIXED, m.coef_words,
+                                  s);
+      }
+    } else {
+      launch_coefficients(co, arith, m.coef_words, s);
+    }
+  }
+  record_phase(t, 1, s);
   int qi = 0;
-  for (const Queue &q : m.queues) {
-    ga.queue = q.d_idx;
-    ga.items = q.d_items;
-    ga.iwidth = q.iwidth;
-    ga.nqueue = q.d_items ? q.nitems : q.n;
-    ga.counter = t->d_counters + qi++;
-    ga.coef_stride = q.fp32 ? 2 : 1;
-    grid_launch(t, q, 0, q.fp32 ? (int)ARITH_FP32 : arith, ga, s);
-    grid_library_counter_add(kBucketLp[q.bucket], GRID_BACKEND_GB300,
-                             q.general ? GRID_COLLOCATE_GENERAL : GRID_COLLOCATE_ORTHO, q.n);
+  {
+    for (const Queue &q : m.queues) {
+      ga.queue = q.d_idx;
+      ga.items = q.d_items;
+      ga.iwidth = q.iwidth;
+      ga.nqueue = q.d_items ? q.nitems : q.n;
+      if (qi >= kMaxQueues)
+        fail("more than %d work queues in one call", kMaxQueues);
+      ga.counter = t->d_counters + qi++;
+      ga.coef_stride = q.fp32 ? 2 : 1;
+      grid_launch(t, q, 0, q.fp32 ? (int)ARITH_FP32 : arith, ga, s);
+      grid_library_counter_add(kBucketLp[q.bucket], GRID_BACKEND_GB300,
+                               q.general ? GRID_COLLOCATE_GENERAL : GRID_COLLOCATE_ORTHO, q.n);
+    }
   }
   if (arith == ARITH_MIXED)
     for (int l = 0; l < t->nlevels; l++) {
@@ -1414,9 +1524,11 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
 }
 
 static void run_integrate(TaskList *t, bool tau, const double *pab, const double *const *grids,
-                          double *hab, double *forces, double *virial, cudaStream_t s) {
+                          double *hab, double *forces, double *virial, cudaStream_t s,
+                          const HostCopy *hc = nullptr) {
   const LDiffs d = integrate_ldiffs(forces != nullptr, virial != nullptr, tau);
-  Mode &m = get_mode(t, d, tau ? 2 : 1);
+  const int nch = hc ? hc->ch->n : 1;
+  Mode &m = get_mode(t, d, tau ? 2 : 1, nch);
   const int arith = t->precision;
   const bool need_pab = forces != nullptr || virial != nullptr;
   t->gen += ensure((void **)&t->d_coef_int, &t->coef_int_cap, m.coef_total * 8);
@@ -1434,21 +1546,35 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
         CK(cudaMalloc((void **)&t->d_gridhi[l], sizeof(float) * np));
         t->gen++;
       }
+      if (hc)
+        CK(cudaStreamWaitEvent(s, hc->vready[l], 0));
       launch_grid_split(grids[l], t->d_gridsplit[l], np, arith, s,
                         arith == ARITH_MIXED ? t->d_gridhi[l] : nullptr);
     }
+  else if (hc)
+    for (int l = 0; l < t->nlevels; l++)
+      CK(cudaStreamWaitEvent(s, hc->vready[l], 0));
   if (need_pab) {
+    if (hc)
+      CK(cudaStreamWaitEvent(s, hc->pab_ready, 0));
     ContractArgs ca{t->d_subs, (int)t->subs.size(), t->d_sphi, pab, nullptr, t->d_pab_cart,
                     t->contract_words};
     launch_decontract(ca, s);
   }
-  CK(cudaMemsetAsync(t->d_counters, 0, sizeof(int) * 64, s));
+  CK(cudaMemsetAsync(t->d_counters, 0, sizeof(int) * kMaxQueues, s));
   // split general tasks add their planes' partial coefficients
   bool any_split = false;
   for (const Queue &q : m.queues)
     any_split |= q.d_items != nullptr;
   if (any_split)
     CK(cudaMemsetAsync(t->d_coef_int, 0, m.coef_total * 8, s));
+  CK(cudaMemsetAsync(t->d_hab_cart, 0, sizeof(double) * std::max<size_t>(t->cart_total, 1), s));
+  if (forces)
+    CK(cudaMemsetAsync(forces, 0, sizeof(double) * 3 * t->natoms, s));
+  if (virial)
+    CK(cudaMemsetAsync(virial, 0, sizeof(double) * 9, s));
+  // hab is overwritten (grid_ref_task_list.c:672-678)
+  CK(cudaMemsetAsync(hab, 0, sizeof(double) * (size_t)t->buffer_len, s));
   record_phase(t, 1, s);
   GridArgs ga{};
   ga.coef_stride = 1;
@@ -1460,55 +1586,79 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
   ga.sph_tab = t->d_sph_tab;
   ga.sph_pts = t->d_sph_pts;
   ga.sph_ploff = t->d_sph_ploff;
-  for (int l = 0; l < t->nlevels; l++)
-    ga.grids_in[l] = arith != ARITH_FP64 ? (const void *)t->d_gridsplit[l] : (const void *)grids[l];
   ga.levels = t->levels;
   ga.d = d;
   ga.task_cycles = t->task_timing ? t->d_cycles : nullptr;
   ga.seeds = t->d_seeds;
   ga.error = t->d_error;
-  int qi = 0;
-  for (const Queue &q : m.queues) {
-    ga.queue = q.d_idx;
-    ga.items = q.d_items;
-    ga.iwidth = q.iwidth;
-    ga.nqueue = q.d_items ? q.nitems : q.n;
-    ga.counter = t->d_counters + qi++;
-    ga.grid_stride = 1;
-    // FP64: the grid; mixed: float2 pairs for the double-float class, dense
-    // high words for the FP32 class
-    for (int l = 0; l < t->nlevels; l++)
-      ga.grids_in[l] = arith == ARITH_FP64                  ? (const void *)grids[l]
-                       : (arith == ARITH_MIXED && q.fp32) ? (const void *)t->d_gridhi[l]
-                                                          : (const void *)t->d_gridsplit[l];
-    grid_launch(t, q, 1, q.fp32 ? (int)ARITH_FP32 : arith, ga, s);
-    grid_library_counter_add(kBucketLp[q.bucket], GRID_BACKEND_GB300,
-                             q.general ? GRID_INTEGRATE_GENERAL : GRID_INTEGRATE_ORTHO, q.n);
-  }
-  CK(cudaGetLastError());
-  record_phase(t, 2, s);
-  CK(cudaMemsetAsync(t->d_hab_cart, 0, sizeof(double) * std::max<size_t>(t->cart_total, 1), s));
-  if (forces)
-    CK(cudaMemsetAsync(forces, 0, sizeof(double) * 3 * t->natoms, s));
-  if (virial)
-    CK(cudaMemsetAsync(virial, 0, sizeof(double) * 9, s));
   PostArgs pa{t->d_tasks, t->d_subs, m.d_coef_off, t->d_coef_int,
               need_pab ? t->d_pab_cart : nullptr, t->d_hab_cart, t->d_atom_pos, forces, virial,
               t->ntasks, tau ? 1 : 0, d, t->d_levels, t->d_dhtab, t->d_dhtab_f, t->d_dhtab_df,
-              nullptr, 0};
-  if (arith == ARITH_MIXED) {
-    for (const Queue &q : m.queues) {
-      pa.order = q.d_idx;
-      pa.norder = q.n;
-      launch_post_mixed(pa, q.fp32 ? (int)ARITH_FP32 : (int)ARITH_MIXED, m.coef_words, s);
+              nullptr, 0, m.transform};
+  int qi = 0;
+  for (const Queue &q : m.queues) {
+    {
+      ga.queue = q.d_idx;
+      ga.items = q.d_items;
+      ga.iwidth = q.iwidth;
+      ga.nqueue = q.d_items ? q.nitems : q.n;
+      if (qi >= kMaxQueues)
+        fail("more than %d work queues in one call", kMaxQueues);
+      ga.counter = t->d_counters + qi++;
+      ga.grid_stride = 1;
+      // FP64: the grid; mixed: float2 pairs for the double-float class, dense
+      // high words for the FP32 class
+      for (int l = 0; l < t->nlevels; l++)
+        ga.grids_in[l] = arith == ARITH_FP64                  ? (const void *)grids[l]
+                         : (arith == ARITH_MIXED && q.fp32) ? (const void *)t->d_gridhi[l]
+                                                            : (const void *)t->d_gridsplit[l];
+      grid_launch(t, q, 1, q.fp32 ? (int)ARITH_FP32 : arith, ga, s);
+      grid_library_counter_add(kBucketLp[q.bucket], GRID_BACKEND_GB300,
+                               q.general ? GRID_INTEGRATE_GENERAL : GRID_INTEGRATE_ORTHO, q.n);
     }
-  } else {
-    launch_post(pa, arith, m.coef_words, s);
   }
-  CK(cudaMemsetAsync(hab, 0, sizeof(double) * (size_t)t->buffer_len, s));
-  ContractArgs cb{t->d_subs, (int)t->subs.size(), t->d_sphi, nullptr, hab, t->d_hab_cart,
-                  t->contract_words};
-  launch_contract_hab(cb, s);
+  record_phase(t, 2, s);
+  // integrated coefficients -> hab (forces, virial), piece by piece where the
+  // host-buffer call copies hab out in pieces: the largest piece first, so
+  // that the copy left after the last kernel is the smallest one
+  for (int ci = nch - 1; ci >= 0; ci--) {
+    if (nch > 1) {
+      for (int cls = 0; cls < 2; cls++) {
+        pa.order = m.d_chunk_idx[2 * ci + cls];
+        pa.norder = m.chunk_n[2 * ci + cls];
+        if (pa.norder == 0)
+          continue;
+        if (arith == ARITH_MIXED)
+          launch_post_mixed(pa, cls ? (int)ARITH_FP32 : (int)ARITH_MIXED, m.coef_words, s);
+        else
+          launch_post(pa, arith, m.coef_words, s);
+      }
+    } else if (arith == ARITH_MIXED) {
+      for (const Queue &q : m.queues) {
+        pa.order = q.d_idx;
+        pa.norder = q.n;
+        launch_post_mixed(pa, q.fp32 ? (int)ARITH_FP32 : (int)ARITH_MIXED, m.coef_words, s);
+      }
+    } else {
+      launch_post(pa, arith, m.coef_words, s);
+    }
+    int s0 = 0, ns = (int)t->subs.size();
+    if (hc) {
+      s0 = hc->ch->sub_lo[ci];
+      ns = hc->ch->sub_lo[ci + 1] - s0;
+    }
+    ContractArgs cb{t->d_subs + s0, ns, t->d_sphi, nullptr, hab, t->d_hab_cart,
+                    t->contract_words};
+    launch_contract_hab(cb, s);
+    if (hc) { // this piece of hab is final: copy it out behind the next kernels
+      CK(cudaEventRecord(hc->done[ci], s));
+      CK(cudaStreamWaitEvent(hc->cs, hc->done[ci], 0));
+      const long long e0 = hc->ch->el_lo[ci], e1 = hc->ch->el_lo[ci + 1];
+      if (e1 > e0)
+        CK(cudaMemcpyAsync(hc->hab_host + e0, hab + e0, sizeof(double) * (size_t)(e1 - e0),
+                           cudaMemcpyDeviceToHost, hc->cs));
+    }
+  }
   CK(cudaGetLastError());
   record_phase(t, 3, s);
 }
@@ -1541,7 +1691,7 @@ GB300_API void grid_gb300_create_task_list(
   // predictions, timings) belong to the old geometry and are dropped; the
   // learned schedule falls back to the size order until a model is applied.
   struct Kept {
-    int precision, schedule, coll_variant;
+    int precision, schedule, coll_variant, transform_variant, copy_chunks;
     double mixed_threshold, model_bin;
     int small_extent[3];
     std::map<std::tuple<int, int, int>, LaunchCfg> tuned;
@@ -1550,7 +1700,8 @@ GB300_API void grid_gb300_create_task_list(
   std::unique_ptr<Kept> kept;
   if (*task_list) {
     const TaskList *o = TL(*task_list);
-    kept.reset(new Kept{o->precision, o->schedule, o->coll_variant, o->mixed_threshold,
+    kept.reset(new Kept{o->precision, o->schedule, o->coll_variant, o->transform_variant,
+                        o->copy_chunks, o->mixed_threshold,
                         o->model_bin, {o->small_extent[0], o->small_extent[1],
                                        o->small_extent[2]},
                         o->tuned, o->launch_timing, o->task_timing});
@@ -1567,6 +1718,8 @@ GB300_API void grid_gb300_create_task_list(
     t->precision = kept->precision;
     t->schedule = kept->schedule;
     t->coll_variant = kept->coll_variant;
+    t->transform_variant = kept->transform_variant;
+    t->copy_chunks = kept->copy_chunks;
     t->mixed_threshold = kept->mixed_threshold;
     t->model_bin = kept->model_bin;
     for (int i = 0; i < 3; i++)
@@ -1665,6 +1818,66 @@ GB300_API void grid_gb300_integrate_device_async(const grid_gb300_task_list *tas
   run_integrate(t, compute_tau, pab_blocks, grids, hab_blocks, forces, virial, s);
 }
 
+// Copy chunks of the host-buffer calls: t->copy_chunks pieces whose sizes
+// grow 1 : 2 : 4 ... in block order, cut at block starts.  One piece where
+// the blocks' ranges in the buffer are not in subblock order.
+static const CopyChunks &get_chunks(TaskList *t) {
+  if (t->chunks_for == t->copy_chunks)
+    return t->chunks;
+  const int nsubs = (int)t->subs.size();
+  CopyChunks c;
+  c.sub_lo = {0, nsubs};
+  c.el_lo = {0, t->buffer_len};
+  const int want = std::max(1, std::min(t->copy_chunks, 7));
+  bool ok = nsubs > 0 && t->buffer_len > 0;
+  std::vector<long long> bstart(nsubs);
+  long long prev_end = 0;
+  for (int i = 0; i < nsubs && ok; i++) {
+    const SubblockDesc &sb = t->subs[i];
+    bstart[i] = sb.block_offset;
+    if (i > 0 && sb.block_offset == t->subs[i - 1].block_offset)
+      continue; // another subblock of the same block
+    if (sb.block_offset < prev_end)
+      ok = false;
+    prev_end = (long long)sb.block_offset + (long long)sb.nsgfa * sb.nsgfb;
+  }
+  if (ok && want > 1) {
+    std::vector<int> sub_lo = {0};
+    std::vector<long long> el_lo = {0};
+    const double denom = (double)((1 << want) - 1);
+    for (int k = 1; k < want; k++) {
+      const long long target = (long long)((double)((1 << k) - 1) / denom * t->buffer_len);
+      int i = sub_lo.back() + 1;
+      while (i < nsubs && (bstart[i] < target || bstart[i] == bstart[i - 1]))
+        i++;
+      if (i >= nsubs)
+        break;
+      sub_lo.push_back(i);
+      el_lo.push_back(bstart[i]);
+    }
+    sub_lo.push_back(nsubs);
+    el_lo.push_back(t->buffer_len);
+    c.sub_lo = sub_lo;
+    c.el_lo = el_lo;
+  }
+  c.n = (int)c.sub_lo.size() - 1;
+  t->chunks = c;
+  t->chunks_for = t->copy_chunks;
+  return t->chunks;
+}
+
+// the copy stream and `n` timing-free events of a host-buffer call
+static cudaEvent_t *copy_events(TaskList *t, size_t n) {
+  if (!t->copy_stream)
+    CK(cudaStreamCreateWithFlags(&t->copy_stream, cudaStreamNonBlocking));
+  while (t->copy_ev.size() < n) {
+    cudaEvent_t e;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    t->copy_ev.push_back(e);
+  }
+  return t->copy_ev.data();
+}
+
 GB300_API void grid_gb300_collocate_task_list(const grid_gb300_task_list *task_list,
                                               const enum grid_func func, const int nlevels,
                                               const offload_buffer *pab_blocks,
@@ -1678,12 +1891,33 @@ GB300_API void grid_gb300_collocate_task_list(const grid_gb300_task_list *task_l
     return;
   }
   cudaStream_t s = t->stream;
-  CK(cudaMemcpyAsync(pab_blocks->device_buffer, pab_blocks->host_buffer, pab_blocks->size,
-                     cudaMemcpyHostToDevice, s));
   double *g[GB300_MAX_LEVELS];
   for (int l = 0; l < nlevels; l++)
     g[l] = grids[l]->device_buffer;
-  run_collocate(t, func, pab_blocks->device_buffer, g, s);
+  const CopyChunks &ch = get_chunks(t);
+  if (ch.n > 1 && (long long)(pab_blocks->size / sizeof(double)) >= t->buffer_len) {
+    // pab in pieces on the copy stream; piece c's kernels start once it landed
+    cudaEvent_t *ev = copy_events(t, (size_t)ch.n + 1);
+    CK(cudaEventRecord(ev[ch.n], s)); // earlier work on the list's stream is done
+    CK(cudaStreamWaitEvent(t->copy_stream, ev[ch.n], 0));
+    for (int c = 0; c < ch.n; c++) {
+      const long long e0 = ch.el_lo[c], e1 = ch.el_lo[c + 1];
+      if (e1 > e0)
+        CK(cudaMemcpyAsync(pab_blocks->device_buffer + e0, pab_blocks->host_buffer + e0,
+                           sizeof(double) * (size_t)(e1 - e0), cudaMemcpyHostToDevice,
+                           t->copy_stream));
+      CK(cudaEventRecord(ev[c], t->copy_stream));
+    }
+    HostCopy hc;
+    hc.ch = &ch;
+    hc.cs = t->copy_stream;
+    hc.ready = ev;
+    run_collocate(t, func, pab_blocks->device_buffer, g, s, &hc);
+  } else {
+    CK(cudaMemcpyAsync(pab_blocks->device_buffer, pab_blocks->host_buffer, pab_blocks->size,
+                       cudaMemcpyHostToDevice, s));
+    run_collocate(t, func, pab_blocks->device_buffer, g, s);
+  }
   for (int l = 0; l < nlevels; l++)
     CK(cudaMemcpyAsync(grids[l]->host_buffer, grids[l]->device_buffer, grids[l]->size,
                        cudaMemcpyDeviceToHost, s));
@@ -1716,25 +1950,66 @@ GB300_API void grid_gb300_integrate_task_list(const grid_gb300_task_list *task_l
          hab_blocks->size / sizeof(double), t->buffer_len);
   cudaStream_t s = t->stream;
   const double *g[GB300_MAX_LEVELS];
-  for (int l = 0; l < nlevels; l++) {
-    CK(cudaMemcpyAsync(grids[l]->device_buffer, grids[l]->host_buffer, grids[l]->size,
-                       cudaMemcpyHostToDevice, s));
+  for (int l = 0; l < nlevels; l++)
     g[l] = grids[l]->device_buffer;
+  const bool need_pab = pab_blocks && (forces || virial);
+  const CopyChunks &ch = get_chunks(t);
+  if (ch.n > 1) {
+    // V levels and pab in on the copy stream, hab out in pieces behind the
+    // kernels of the next piece
+    cudaEvent_t *ev = copy_events(t, (size_t)(2 * ch.n + nlevels + 2));
+    cudaEvent_t *vready = ev, *done = ev + nlevels, start = ev[nlevels + ch.n],
+                pab_ready = ev[nlevels + ch.n + 1];
+    CK(cudaEventRecord(start, s));
+    CK(cudaStreamWaitEvent(t->copy_stream, start, 0));
+    for (int l = 0; l < nlevels; l++) {
+      CK(cudaMemcpyAsync(grids[l]->device_buffer, grids[l]->host_buffer, grids[l]->size,
+                         cudaMemcpyHostToDevice, t->copy_stream));
+      CK(cudaEventRecord(vready[l], t->copy_stream));
+    }
+    if (need_pab)
+      CK(cudaMemcpyAsync(pab_blocks->device_buffer, pab_blocks->host_buffer, pab_blocks->size,
+                         cudaMemcpyHostToDevice, t->copy_stream));
+    CK(cudaEventRecord(pab_ready, t->copy_stream));
+    HostCopy hc;
+    hc.ch = &ch;
+    hc.cs = t->copy_stream;
+    hc.vready = vready;
+    hc.pab_ready = pab_ready;
+    hc.done = done;
+    hc.hab_host = hab_blocks->host_buffer;
+    run_integrate(t, compute_tau, pab_blocks ? pab_blocks->device_buffer : nullptr, g,
+                  hab_blocks->device_buffer, forces ? t->d_forces : nullptr,
+                  virial ? t->d_virial : nullptr, s, &hc);
+    // the reference zeroes the whole hab buffer; past the task list's blocks
+    // nothing is computed
+    if (hab_blocks->size > sizeof(double) * (size_t)t->buffer_len)
+      memset(hab_blocks->host_buffer + t->buffer_len, 0,
+             hab_blocks->size - sizeof(double) * (size_t)t->buffer_len);
+  } else {
+    for (int l = 0; l < nlevels; l++)
+      CK(cudaMemcpyAsync(grids[l]->device_buffer, grids[l]->host_buffer, grids[l]->size,
+                         cudaMemcpyHostToDevice, s));
+    if (need_pab)
+      CK(cudaMemcpyAsync(pab_blocks->device_buffer, pab_blocks->host_buffer, pab_blocks->size,
+                         cudaMemcpyHostToDevice, s));
+    run_integrate(t, compute_tau, pab_blocks ? pab_blocks->device_buffer : nullptr, g,
+                  hab_blocks->device_buffer, forces ? t->d_forces : nullptr,
+                  virial ? t->d_virial : nullptr, s);
+    CK(cudaMemcpyAsync(hab_blocks->host_buffer, hab_blocks->device_buffer,
+                       sizeof(double) * (size_t)t->buffer_len, cudaMemcpyDeviceToHost, s));
+    if (hab_blocks->size > sizeof(double) * (size_t)t->buffer_len)
+      memset(hab_blocks->host_buffer + t->buffer_len, 0,
+             hab_blocks->size - sizeof(double) * (size_t)t->buffer_len);
   }
-  if (pab_blocks && (forces || virial))
-    CK(cudaMemcpyAsync(pab_blocks->device_buffer, pab_blocks->host_buffer, pab_blocks->size,
-                       cudaMemcpyHostToDevice, s));
-  run_integrate(t, compute_tau, pab_blocks ? pab_blocks->device_buffer : nullptr, g,
-                hab_blocks->device_buffer, forces ? t->d_forces : nullptr,
-                virial ? t->d_virial : nullptr, s);
-  CK(cudaMemcpyAsync(hab_blocks->host_buffer, hab_blocks->device_buffer, hab_blocks->size,
-                     cudaMemcpyDeviceToHost, s));
   if (forces)
     CK(cudaMemcpyAsync(forces, t->d_forces, sizeof(double) * 3 * t->natoms,
                        cudaMemcpyDeviceToHost, s));
   if (virial)
     CK(cudaMemcpyAsync(virial, t->d_virial, sizeof(double) * 9, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  if (t->copy_stream)
+    CK(cudaStreamSynchronize(t->copy_stream));
   read_timings(t);
   check_device_error(t);
 }
@@ -2093,7 +2368,7 @@ GB300_API double grid_gb300_autotune(const grid_gb300_task_list *task_list, int 
           cfg.warps = cands[c].warps;
           cfg.occupancy = cands[c].occ;
           cfg.variant = cands[c].variant;
-          t->tuned[std::make_tuple(prec, phase, q.key)] = cfg;
+          t->tuned[std::make_tuple(prec, phase, q.base)] = cfg;
         }
     std::map<std::pair<int, int>, double> ms;
     for (int r = 0; r < 2; r++) {
@@ -2134,6 +2409,23 @@ GB300_API void grid_gb300_set_collocate_variant(const grid_gb300_task_list *task
   t->coll_variant = variant;
   t->tuned.clear();
   t->gen++;
+}
+
+GB300_API void grid_gb300_set_copy_chunks(const grid_gb300_task_list *task_list, int chunks) {
+  if (chunks < 1 || chunks > 7)
+    fail("copy chunks must be in 1..7, got %d", chunks);
+  TL(task_list)->copy_chunks = chunks;
+}
+
+GB300_API void grid_gb300_set_transform_variant(const grid_gb300_task_list *task_list,
+                                               int variant) {
+  if (variant < -1 || variant > 1)
+    fail("unknown transform variant %d", variant);
+  TaskList *t = TL(task_list);
+  if (t->transform_variant != variant) {
+    t->transform_variant = variant;
+    t->sched_version++; // the modes' shared-memory sizes depend on it
+  }
 }
 
 GB300_API void grid_gb300_set_model_bin_width(const grid_gb300_task_list *task_list,

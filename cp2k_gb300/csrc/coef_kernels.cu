@@ -449,12 +449,7 @@ __device__ T *lattice_transform(const T *tab, int level, int lp, bool adjoint, T
   return x;
 }
 
-// Per-group shared memory of the coefficient / post kernels in 8-byte words:
-// cab [n2][n1] (FP64, then the working type in place), alpha, cxyz, cijk.
-__host__ __device__ inline size_t coef_smem_words(int n1, int n2, int la, int lb, int lp) {
-  return (size_t)n1 * n2 + 3 * (size_t)(la + 1) * (lb + 1) * (lp + 1) +
-         2 * (size_t)ncoset(lp) + 8;
-}
+
 
 // Decode the Cartesian index i (0 .. ncoset(lmax)-1) into an orbital.
 __device__ __forceinline__ Orb orb_of_index(int i) {
@@ -462,6 +457,136 @@ __device__ __forceinline__ Orb orb_of_index(int i) {
   while (ncoset(l) <= i)
     l++;
   return orb_of(l, i - ncoset(l - 1));
+}
+
+// ------------------------------------------------------------------------
+// Staged transforms: the C_ab <-> C_xyz change of basis one direction at a
+// time.  C_xyz[p] = sum_{a,b} C_ab[a,b] prod_d alpha_d[b_d][a_d][p_d] is
+// evaluated as three small contractions, x, then y, then z:
+//   T1[(ay,az),(by,bz)][px] = sum_{ax,bx} C_ab[a,b] alpha_x[bx][ax][px]
+//   T2[az][bz][(px,py)]     = sum_{ay,by} T1[(ay,az),(by,bz)][px] alpha_y[by][ay][py]
+//   C_xyz[(px,py,pz)]        = sum_{az,bz} T2[az][bz][(px,py)] alpha_z[bz][az][pz]
+// and the integrate adjoint in reverse (z, y, x).  A direct gather costs
+// each output prod_d (a_d + b_d + 1)-style sums over all (a, b) pairs; the
+// stages cost about a quarter of that at la = lb = 4 (the reference's own
+// cab_to_cxyz, grid_ref_collint.h:827-911, runs the nested loops directly).
+// Index helpers: pairs (u, v) with u + v <= L in the order of u + v, then v.
+// ------------------------------------------------------------------------
+__device__ __forceinline__ int pidx(int u, int v) {
+  const int s = u + v;
+  return (s * (s + 1)) / 2 + v;
+}
+__device__ __forceinline__ void pdecode(int i, int &u, int &v) {
+  int s = 0;
+  while (((s + 1) * (s + 2)) / 2 <= i)
+    s++;
+  v = i - (s * (s + 1)) / 2;
+  u = s - v;
+}
+
+template <typename T>
+__device__ void cab_to_cxyz_staged(const T *cab, int n1, const T *alpha, int la, int lb, int lp,
+                                   T *t1, T *t2, T *cxyz, T pref, const uint16_t *ord,
+                                   const Grp &g) {
+  using M = Num<T>;
+  const int na = la + 1, nb = lb + 1, P = lp + 1, npa = ntri(la), npb = ntri(lb),
+            nt = ntri(lp);
+  auto A = [&](int d, int xb, int xa) { return alpha + ((size_t)(d * nb + xb) * na + xa) * P; };
+  // x: T1[(ay,az),(by,bz)][px]
+  for (int e = g.lane; e < npa * npb * P; e += g.n) {
+    const int px = e % P, r = e / P, ipb = r % npb, ipa = r / npb;
+    int ay, az, by, bz;
+    pdecode(ipa, ay, az);
+    pdecode(ipb, by, bz);
+    const int ra = la - ay - az, rb = lb - by - bz;
+    T acc = M::zero();
+    if (px <= ra + rb)
+      for (int ax = 0; ax <= ra; ax++)
+        for (int bx = px > ax ? px - ax : 0; bx <= rb; bx++)
+          acc = M::fma_acc(acc, A(0, bx, ax)[px],
+                           cab[coset(bx, by, bz) * n1 + coset(ax, ay, az)]);
+    t1[e] = M::norm(acc);
+  }
+  g.sync();
+  // y: T2[az][bz][(px,py)]
+  for (int e = g.lane; e < na * nb * nt; e += g.n) {
+    const int it = e % nt, r = e / nt, bz = r % nb, az = r / nb;
+    int px, py;
+    pdecode(it, px, py);
+    T acc = M::zero();
+    if (px + py <= (la - az) + (lb - bz))
+      for (int ay = 0; ay <= la - az; ay++)
+        for (int by = py > ay ? py - ay : 0; by <= lb - bz; by++)
+          if (px <= (la - ay - az) + (lb - by - bz))
+            acc = M::fma_acc(acc, A(1, by, ay)[py],
+                             t1[((size_t)pidx(ay, az) * npb + pidx(by, bz)) * P + px]);
+    t2[e] = M::norm(acc);
+  }
+  g.sync();
+  // z: C_xyz
+  for (int i = g.lane; i < ncoset(lp); i += g.n) {
+    const int e = ord ? ord[i] : i;
+    int pz, py, px;
+    decode_cidx(e, lp, pz, py, px);
+    T acc = M::zero();
+    for (int az = 0; az <= la; az++)
+      for (int bz = pz > az ? pz - az : 0; bz <= lb; bz++)
+        if (px + py <= (la - az) + (lb - bz))
+          acc = M::fma_acc(acc, A(2, bz, az)[pz], t2[(size_t)(az * nb + bz) * nt + pidx(px, py)]);
+    cxyz[e] = M::mul(M::norm(acc), pref);
+  }
+}
+
+template <typename T>
+__device__ void cxyz_to_cab_staged(const T *cxyz, const T *alpha, int la, int lb, int lp,
+                                   T *t1, T *t2, T *cab, int m1, T pref, const Grp &g) {
+  using M = Num<T>;
+  const int na = la + 1, nb = lb + 1, P = lp + 1, npa = ntri(la), npb = ntri(lb),
+            nt = ntri(lp);
+  auto A = [&](int d, int xb, int xa) { return alpha + ((size_t)(d * nb + xb) * na + xa) * P; };
+  // z: T2[az][bz][(px,py)] = sum_pz alpha_z C_xyz
+  for (int e = g.lane; e < na * nb * nt; e += g.n) {
+    const int it = e % nt, r = e / nt, bz = r % nb, az = r / nb;
+    int px, py;
+    pdecode(it, px, py);
+    T acc = M::zero();
+    if (px + py <= (la - az) + (lb - bz)) {
+      const T *al = A(2, bz, az);
+      const int pzmax = az + bz < lp - px - py ? az + bz : lp - px - py;
+      for (int pz = 0; pz <= pzmax; pz++)
+        acc = M::fma_acc(acc, al[pz], cxyz[cidx(pz, py, px, lp)]);
+    }
+    t2[e] = M::norm(acc);
+  }
+  g.sync();
+  // y: T1[(ay,az),(by,bz)][px] = sum_py alpha_y T2
+  for (int e = g.lane; e < npa * npb * P; e += g.n) {
+    const int px = e % P, r = e / P, ipb = r % npb, ipa = r / npb;
+    int ay, az, by, bz;
+    pdecode(ipa, ay, az);
+    pdecode(ipb, by, bz);
+    T acc = M::zero();
+    if (px <= (la - ay - az) + (lb - by - bz)) {
+      const T *al = A(1, by, ay);
+      const T *src = t2 + (size_t)(az * nb + bz) * nt;
+      for (int py = 0; py <= ay + by; py++)
+        acc = M::fma_acc(acc, al[py], src[pidx(px, py)]);
+    }
+    t1[e] = M::norm(acc);
+  }
+  g.sync();
+  // x: C_ab[a,b] = sum_px alpha_x T1
+  const int m2 = ncoset(lb);
+  for (int e = g.lane; e < m1 * m2; e += g.n) {
+    const Orb oa = orb_of_index(e % m1), ob = orb_of_index(e / m1);
+    const T *al = A(0, ob.l[0], oa.l[0]);
+    const T *src =
+        t1 + ((size_t)pidx(oa.l[1], oa.l[2]) * npb + pidx(ob.l[1], ob.l[2])) * P;
+    T acc = M::zero();
+    for (int px = 0; px <= oa.l[0] + ob.l[0]; px++)
+      acc = M::fma_acc(acc, al[px], src[px]);
+    cab[e] = M::mul(M::norm(acc), pref);
+  }
 }
 
 // store of one coefficient in the grid kernels' arithmetic
@@ -537,6 +662,19 @@ __device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *w
   // (at low lp the outputs' term counts differ little and the plain order
   // keeps the stores contiguous)
   const uint16_t *ord = lp >= 6 ? entry_order(1, la_max, lb_max) : nullptr;
+  if (uses_staged(a.transform, la_max, lb_max, true)) {
+    U *t1 = (U *)((double *)cijk + nco);
+    U *t2 = (U *)((double *)t1 + (size_t)ntri(la_max) * ntri(lb_max) * (lp + 1));
+    cab_to_cxyz_staged<U>(cab, n1, alpha, la_max, lb_max, lp, t1, t2, cxyz, pref, ord, g);
+    g.sync();
+    const U *cl = general ? lattice_transform<U>(dh_tab<U>(a.dhtab, a.dhtab_f, a.dhtab_df),
+                                                 d.level, lp, false, cxyz, cijk, g)
+                          : cxyz;
+    for (int e = g.lane; e < nco; e += g.n)
+      store_coef<Tout, U>(a.coef, (size_t)a.coef_off[t] + e, cl[e]);
+    g.sync();
+    return;
+  }
   for (int i = g.lane; i < nco; i += g.n) {
     const int e = ord ? ord[i] : i;
     int pz, py, px;
@@ -591,45 +729,66 @@ __global__ void __launch_bounds__(128) coefficients_kernel(CoefArgs a, int words
 // ------------------------------------------------------------------------
 // post: integrated C_xyz -> C_ab -> hab / forces / virial (one warp per task)
 // ------------------------------------------------------------------------
+// Cartesian orbitals by coset index with neighbour tables, so that the
+// derivative terms of the post kernel look their orbitals up instead of
+// recomputing coset indices: g_orb_lxyz[i] = lx | ly << 4 | lz << 8,
+// g_orb_up[d][i] the index of the orbital + 1_d, g_orb_dn[d][i] of the
+// orbital - 1_d (the orbital itself where its d component is 0, as dn()).
+constexpr int kOrbL = 12;                                     // orbitals with l < kOrbL
+constexpr int kOrbN = kOrbL * (kOrbL + 1) * (kOrbL + 2) / 6; // their number
+__device__ uint16_t g_orb_lxyz[kOrbN];
+__device__ uint16_t g_orb_up[3][kOrbN];
+__device__ uint16_t g_orb_dn[3][kOrbN];
+struct OI {
+  int i;
+};
+__device__ __forceinline__ int ocomp(OI a, int d) {
+  return (__ldg(&g_orb_lxyz[a.i]) >> (4 * d)) & 15;
+}
+__device__ __forceinline__ OI oup(int d, OI a) { return OI{__ldg(&g_orb_up[d][a.i])}; }
+__device__ __forceinline__ OI odn(int d, OI a) { return OI{__ldg(&g_orb_dn[d][a.i])}; }
+
 template <typename T> struct VabCtx {
   const T *c;
   int m1;
   T za, zb;
   T rab[3];
-  __device__ __forceinline__ T g(Orb a, Orb b) const { return c[oidx(b) * m1 + oidx(a)]; }
+  __device__ __forceinline__ T g(OI a, OI b) const { return c[b.i * m1 + a.i]; }
 };
 
 enum { V_HAB, V_FA, V_FB, V_VA, V_VB };
 
 template <typename T>
-__device__ T vab_plain(const VabCtx<T> &x, int kind, int i, int j, Orb a, Orb b) {
+__device__ T vab_plain(const VabCtx<T> &x, int kind, int i, int j, OI a, OI b) {
   switch (kind) {
   case V_HAB:
     return x.g(a, b);
   case V_FA:
-    return T(2) * x.za * x.g(up(i, a), b) - T(a.l[i]) * x.g(dn(i, a), b);
+    return T(2) * x.za * x.g(oup(i, a), b) - T(ocomp(a, i)) * x.g(odn(i, a), b);
   case V_FB:
-    return T(2) * x.zb * (x.g(up(i, a), b) - x.rab[i] * x.g(a, b)) - T(b.l[i]) * x.g(a, dn(i, b));
+    return T(2) * x.zb * (x.g(oup(i, a), b) - x.rab[i] * x.g(a, b)) -
+           T(ocomp(b, i)) * x.g(a, odn(i, b));
   case V_VA:
-    return T(2) * x.za * x.g(up(i, up(j, a)), b) - T(a.l[j]) * x.g(up(i, dn(j, a)), b);
+    return T(2) * x.za * x.g(oup(i, oup(j, a)), b) - T(ocomp(a, j)) * x.g(oup(i, odn(j, a)), b);
   default:
     return T(2) * x.zb *
-               (x.g(up(i, up(j, a)), b) - x.g(up(i, a), b) * x.rab[j] -
-                x.g(up(j, a), b) * x.rab[i] + x.g(a, b) * x.rab[j] * x.rab[i]) -
-           T(b.l[j]) * x.g(a, up(i, dn(j, b)));
+               (x.g(oup(i, oup(j, a)), b) - x.g(oup(i, a), b) * x.rab[j] -
+                x.g(oup(j, a), b) * x.rab[i] + x.g(a, b) * x.rab[j] * x.rab[i]) -
+           T(ocomp(b, j)) * x.g(a, oup(i, odn(j, b)));
   }
 }
 
 template <typename T>
-__device__ T vab(const VabCtx<T> &x, bool tau, int kind, int i, int j, Orb a, Orb b) {
+__device__ T vab(const VabCtx<T> &x, bool tau, int kind, int i, int j, OI a, OI b) {
   if (!tau)
     return vab_plain(x, kind, i, j, a, b);
   T s = T(0);
   for (int k = 0; k < 3; k++) {
-    s += T(0.5) * T(a.l[k] * b.l[k]) * vab_plain(x, kind, i, j, dn(k, a), dn(k, b));
-    s -= x.za * T(b.l[k]) * vab_plain(x, kind, i, j, up(k, a), dn(k, b));
-    s -= T(a.l[k]) * x.zb * vab_plain(x, kind, i, j, dn(k, a), up(k, b));
-    s += T(2) * x.za * x.zb * vab_plain(x, kind, i, j, up(k, a), up(k, b));
+    const int ak = ocomp(a, k), bk = ocomp(b, k);
+    s += T(0.5) * T(ak * bk) * vab_plain(x, kind, i, j, odn(k, a), odn(k, b));
+    s -= x.za * T(bk) * vab_plain(x, kind, i, j, oup(k, a), odn(k, b));
+    s -= T(ak) * x.zb * vab_plain(x, kind, i, j, odn(k, a), oup(k, b));
+    s += T(2) * x.za * x.zb * vab_plain(x, kind, i, j, oup(k, a), oup(k, b));
   }
   return s;
 }
@@ -664,11 +823,17 @@ __device__ void post_task(const PostArgs &a, int t, const TaskDesc &d, double *w
     rb[i] = ra[i] + d.rab[i];
   fill_alpha<U>(alpha, la_max, lb_max, lp, ra, rb, d.rp, g);
   const U pref = U(d.prefexp);
-  const uint16_t *ord = entry_order(0, la_max, lb_max);
-  for (int i = g.lane; i < m1 * m2; i += g.n) {
-    const int e = ord ? ord[i] : i;
-    const Orb oa = orb_of_index(e % m1), ob = orb_of_index(e / m1);
-    cab[e] = cxyz_cab_term<U>(cx, alpha, la_max, lb_max, lp, oa, ob) * pref;
+  if (uses_staged(a.transform, la_max, lb_max, false)) {
+    U *t1 = (U *)((double *)cijk + nco);
+    U *t2 = (U *)((double *)t1 + (size_t)ntri(la_max) * ntri(lb_max) * (lp + 1));
+    cxyz_to_cab_staged<U>(cx, alpha, la_max, lb_max, lp, t1, t2, cab, m1, pref, g);
+  } else {
+    const uint16_t *ord = entry_order(0, la_max, lb_max);
+    for (int i = g.lane; i < m1 * m2; i += g.n) {
+      const int e = ord ? ord[i] : i;
+      const Orb oa = orb_of_index(e % m1), ob = orb_of_index(e / m1);
+      cab[e] = cxyz_cab_term<U>(cx, alpha, la_max, lb_max, lp, oa, ob) * pref;
+    }
   }
   g.sync();
   VabCtx<U> x{cab, m1, U(d.zeta), U(d.zetb), {U(d.rab[0]), U(d.rab[1]), U(d.rab[2])}};
@@ -685,23 +850,32 @@ __device__ void post_task(const PostArgs &a, int t, const TaskDesc &d, double *w
   const bool tau_fv = tau && (a.forces || a.virial) &&
                       (size_t)n1p * n2p <= 3 * (size_t)(la_max + 1) * (lb_max + 1) * (lp + 1) +
                                                2 * (size_t)ncoset(lp);
+  // forces and virial accumulate per lane in the working type (the FP64 pipe
+  // is the scarce unit on GB300) and reach FP64 once per task
+  using M = Num<U>;
+  U fu[6], vu[9];
+  for (int i = 0; i < 6; i++)
+    fu[i] = M::zero();
+  for (int i = 0; i < 9; i++)
+    vu[i] = M::zero();
   for (int e = g.lane; e < na * nb; e += g.n) {
     const int ia = ncoset(d.la_min - 1) + e % na, ib = ncoset(d.lb_min - 1) + e / na;
-    const Orb oa = orb_of_index(ia), ob = orb_of_index(ib);
+    const OI oa{ia}, ob{ib};
     const size_t el = (size_t)(d.o2 + ib) * sb.ncoa + d.o1 + ia;
     atomicAdd(&hab[el], to_double(vab<U>(x, tau, V_HAB, 0, 0, oa, ob)));
     if ((a.forces || a.virial) && !tau_fv) {
-      const double p = pab[el];
+      const U p = M::from(pab[el]);
       if (a.forces)
         for (int i = 0; i < 3; i++) {
-          f[i] += p * to_double(vab<U>(x, tau, V_FA, i, 0, oa, ob));
-          f[3 + i] += p * to_double(vab<U>(x, tau, V_FB, i, 0, oa, ob));
+          fu[i] = M::fma_acc(fu[i], p, vab<U>(x, tau, V_FA, i, 0, oa, ob));
+          fu[3 + i] = M::fma_acc(fu[3 + i], p, vab<U>(x, tau, V_FB, i, 0, oa, ob));
         }
       if (a.virial)
         for (int i = 0; i < 3; i++)
           for (int j = 0; j < 3; j++)
-            v[i * 3 + j] += p * (to_double(vab<U>(x, tau, V_VA, i, j, oa, ob)) +
-                                 to_double(vab<U>(x, tau, V_VB, i, j, oa, ob)));
+            vu[i * 3 + j] = M::fma_acc(vu[i * 3 + j], p,
+                                       M::add(vab<U>(x, tau, V_VA, i, j, oa, ob),
+                                              vab<U>(x, tau, V_VB, i, j, oa, ob)));
     }
   }
   if (tau_fv) {
@@ -739,22 +913,30 @@ __device__ void post_task(const PostArgs &a, int t, const TaskDesc &d, double *w
     }
     g.sync();
     for (int e = g.lane; e < n1p * n2p; e += g.n) {
-      const double p = pp[e];
-      if (p == 0.0)
+      const double pd = pp[e];
+      if (pd == 0.0)
         continue;
-      const Orb oa = orb_of_index(e % n1p), ob = orb_of_index(e / n1p);
+      const U p = M::from(pd);
+      const OI oa{e % n1p}, ob{e / n1p};
       if (a.forces)
         for (int i = 0; i < 3; i++) {
-          f[i] += p * to_double(vab_plain<U>(x, V_FA, i, 0, oa, ob));
-          f[3 + i] += p * to_double(vab_plain<U>(x, V_FB, i, 0, oa, ob));
+          fu[i] = M::fma_acc(fu[i], p, vab_plain<U>(x, V_FA, i, 0, oa, ob));
+          fu[3 + i] = M::fma_acc(fu[3 + i], p, vab_plain<U>(x, V_FB, i, 0, oa, ob));
         }
       if (a.virial)
         for (int i = 0; i < 3; i++)
           for (int j = 0; j < 3; j++)
-            v[i * 3 + j] += p * (to_double(vab_plain<U>(x, V_VA, i, j, oa, ob)) +
-                                 to_double(vab_plain<U>(x, V_VB, i, j, oa, ob)));
+            vu[i * 3 + j] = M::fma_acc(vu[i * 3 + j], p,
+                                       M::add(vab_plain<U>(x, V_VA, i, j, oa, ob),
+                                              vab_plain<U>(x, V_VB, i, j, oa, ob)));
     }
   }
+  if (a.forces)
+    for (int i = 0; i < 6; i++)
+      f[i] += to_double(M::norm(fu[i]));
+  if (a.virial)
+    for (int i = 0; i < 9; i++)
+      v[i] += to_double(M::norm(vu[i]));
   g.sync();
 }
 
@@ -810,6 +992,88 @@ __global__ void __launch_bounds__(128) post_kernel(PostArgs a, int words_per_gro
   __syncthreads();
   if (a.virial && threadIdx.x < 9)
     atomicAdd(&a.virial[threadIdx.x], vir_cta[threadIdx.x]);
+}
+
+// ------------------------------------------------------------------------
+// post of one task of the single-task integrate (FP64, one CTA): C_xyz ->
+// C_ab -> hab, the forces and virials of atoms a and b separately, and the
+// derivative blocks hdab, hadb, a_hdab, all accumulated into the caller's
+// arrays (src/grid/ref/grid_ref_integrate.c:81-145)
+// ------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) pgf_post_kernel(PgfPostArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ double red[27];
+  const Grp g{(int)threadIdx.x, (int)blockDim.x, 0xffffffffu};
+  const TaskDesc d = *a.task;
+  const int la_max = d.la_max + a.d.la_max, lb_max = d.lb_max + a.d.lb_max;
+  const int lp = la_max + lb_max;
+  const int m1 = ncoset(la_max), m2 = ncoset(lb_max), nco = ncoset(lp);
+  double *ws = (double *)smem;
+  double *cab = ws;
+  double *alpha = ws + (size_t)m1 * m2;
+  double *cxyz = alpha + 3 * (size_t)(la_max + 1) * (lb_max + 1) * (lp + 1);
+  double *cijk = cxyz + nco;
+  const bool general = d.flags & TF_GENERAL;
+  for (int e = g.lane; e < nco; e += g.n)
+    (general ? cijk : cxyz)[e] = a.coef[e];
+  if (threadIdx.x < 27)
+    red[threadIdx.x] = 0.0;
+  g.sync();
+  const double *cx = general ? lattice_transform<double>(a.dhtab, d.level, lp, true, cijk, cxyz, g)
+                             : cxyz;
+  double rb[3];
+  for (int i = 0; i < 3; i++)
+    rb[i] = a.atom_pos[i] + d.rab[i];
+  fill_alpha<double>(alpha, la_max, lb_max, lp, a.atom_pos, rb, d.rp, g);
+  for (int e = g.lane; e < m1 * m2; e += g.n)
+    cab[e] = cxyz_cab_term<double>(cx, alpha, la_max, lb_max, lp, orb_of_index(e % m1),
+                                   orb_of_index(e / m1)) *
+             d.prefexp;
+  g.sync();
+  const VabCtx<double> x{cab, m1, d.zeta, d.zetb, {d.rab[0], d.rab[1], d.rab[2]}};
+  const bool tau = a.compute_tau;
+  const int na = ncoset(d.la_max) - ncoset(d.la_min - 1);
+  const int nb = ncoset(d.lb_max) - ncoset(d.lb_min - 1);
+  double acc[27]; // forces a, b; virials a, b
+  for (int i = 0; i < 27; i++)
+    acc[i] = 0.0;
+  for (int e = g.lane; e < na * nb; e += g.n) {
+    const int ia = ncoset(d.la_min - 1) + e % na, ib = ncoset(d.lb_min - 1) + e / na;
+    const OI oa{ia}, ob{ib};
+    const size_t el = (size_t)(d.o2 + ib) * a.n1 + d.o1 + ia;
+    a.hab[el] += vab<double>(x, tau, V_HAB, 0, 0, oa, ob);
+    const double p = a.pab ? a.pab[el] : 0.0;
+    for (int i = 0; i < 3; i++) {
+      if (a.forces) {
+        acc[i] += p * vab<double>(x, tau, V_FA, i, 0, oa, ob);
+        acc[3 + i] += p * vab<double>(x, tau, V_FB, i, 0, oa, ob);
+      }
+      if (a.virials)
+        for (int j = 0; j < 3; j++) {
+          acc[6 + i * 3 + j] += p * vab<double>(x, tau, V_VA, i, j, oa, ob);
+          acc[15 + i * 3 + j] += p * vab<double>(x, tau, V_VB, i, j, oa, ob);
+        }
+      if (a.hdab)
+        a.hdab[el * 3 + i] += vab_plain<double>(x, V_FA, i, 0, oa, ob);
+      if (a.hadb)
+        a.hadb[el * 3 + i] += vab_plain<double>(x, V_FB, i, 0, oa, ob);
+      if (a.a_hdab)
+        for (int j = 0; j < 3; j++)
+          a.a_hdab[(el * 3 + i) * 3 + j] += vab_plain<double>(x, V_VA, i, j, oa, ob);
+    }
+  }
+  for (int i = 0; i < 27; i++) {
+    double v = acc[i];
+    for (int o = 16; o > 0; o >>= 1)
+      v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0)
+      atomicAdd(&red[i], v);
+  }
+  __syncthreads();
+  if (threadIdx.x < 6 && a.forces)
+    a.forces[threadIdx.x] += red[threadIdx.x];
+  if (threadIdx.x < 18 && a.virials)
+    a.virials[threadIdx.x] += red[6 + threadIdx.x];
 }
 
 // ------------------------------------------------------------------------
@@ -916,6 +1180,29 @@ static void upload_orders() {
   for (size_t i = 0; i < ox.size(); i++)
     if (coset(ox[i], oy[i], oz[i]) != (int)i)
       return launch_error("entry orders: orbital order mismatch");
+  {
+    // orbital tables of the post kernel's derivative terms
+    static uint16_t lxyz[kOrbN], upt[3][kOrbN], dnt[3][kOrbN];
+    int i = 0;
+    for (int l = 0; l < kOrbL; l++)
+      for (int lx = l; lx >= 0; lx--)
+        for (int lz = 0; lz <= l - lx; lz++, i++) {
+          const int c[3] = {lx, l - lx - lz, lz};
+          lxyz[i] = (uint16_t)(c[0] | (c[1] << 4) | (c[2] << 8));
+          for (int d = 0; d < 3; d++) {
+            int u[3] = {c[0], c[1], c[2]}, w[3] = {c[0], c[1], c[2]};
+            u[d] += 1;
+            w[d] = w[d] > 0 ? w[d] - 1 : 0;
+            upt[d][i] = (uint16_t)coset(u[0], u[1], u[2]);
+            dnt[d][i] = (uint16_t)coset(w[0], w[1], w[2]);
+          }
+        }
+    if (i != kOrbN)
+      return launch_error("orbital tables: size mismatch");
+    cudaMemcpyToSymbol(g_orb_lxyz, lxyz, sizeof(lxyz));
+    cudaMemcpyToSymbol(g_orb_up, upt, sizeof(upt));
+    cudaMemcpyToSymbol(g_orb_dn, dnt, sizeof(dnt));
+  }
   std::vector<std::pair<long long, int>> v;
   auto push_sorted = [&]() {
     std::stable_sort(v.begin(), v.end(), [](const std::pair<long long, int> &x,
@@ -1134,8 +1421,19 @@ bool coefficients_fit(int words_per_group) {
   return L.grid >= 1 && L.smem <= kSmemBudget;
 }
 
-size_t coef_words(int la, int lb) {
-  return coef_smem_words(ncoset(la), ncoset(lb), la, lb, la + lb);
+void launch_pgf_post(const PgfPostArgs &a, cudaStream_t s) {
+  upload_binomials();
+  const size_t smem = sizeof(double) * (size_t)a.words;
+  if (smem > kSmemBudget)
+    return launch_error("single-task post-processing: angular momenta too large for shared memory");
+  set_smem((const void *)pgf_post_kernel, smem);
+  pgf_post_kernel<<<1, 128, smem, s>>>(a);
+  count_launch();
+}
+
+size_t coef_words(int la, int lb, bool staged) {
+  return coef_smem_words(ncoset(la), ncoset(lb), la, lb, la + lb) +
+         (staged ? staged_words(la, lb, la + lb) : 0);
 }
 
 } // namespace gb300

@@ -157,6 +157,7 @@ struct CoefArgs {
   const float2 *dhtab_df;  // the same as double-float pairs (mixed kernels)
   const int *order;        // if set, only these tasks (norder of them)
   int norder;
+  int transform;           // C_ab -> C_xyz: see uses_staged()
 };
 
 struct GridArgs {
@@ -205,7 +206,28 @@ struct PostArgs {
   const float2 *dhtab_df;  // the same as double-float pairs
   const int *order;        // if set, only these tasks (norder of them)
   int norder;
+  int transform;           // C_xyz -> C_ab: see uses_staged()
 };
+
+// single-task integrate (grid_cpu_integrate_pgf_product): one task's post
+// processing, every output accumulated (FP64; all pointers device memory)
+struct PgfPostArgs {
+  const TaskDesc *task;
+  const double *atom_pos; // ra[3]
+  const double *coef;     // integrated C_xyz (C_ijk on the general path)
+  const double *dhtab;    // general-path transform table
+  LDiffs d;               // the integrate shifts
+  int compute_tau;
+  int n1;                 // leading dimension of the [n2][n1] blocks
+  const double *pab;      // or null
+  double *hab;
+  double *forces;         // [2][3] or null
+  double *virials;        // [2][3][3] or null
+  double *hdab, *hadb;    // [n2][n1][3] or null
+  double *a_hdab;         // [n2][n1][3][3] or null
+  int words;              // shared-memory doubles (coef_words)
+};
+void launch_pgf_post(const PgfPostArgs &a, cudaStream_t s);
 
 struct ContractArgs {
   const SubblockDesc *subs;
@@ -216,7 +238,32 @@ struct ContractArgs {
   double *cart;         // Cartesian scratch
   int words;            // per-warp shared-memory doubles (largest work array)
 };
-size_t coef_words(int la, int lb);
+// Per-group shared memory of the coefficient / post kernels in 8-byte words:
+// cab [n2][n1] (FP64, then the working type in place), alpha, cxyz, cijk.
+__host__ __device__ inline size_t coef_smem_words(int n1, int n2, int la, int lb, int lp) {
+  return (size_t)n1 * n2 + 3 * (size_t)(la + 1) * (lb + 1) * (lp + 1) +
+         2 * (size_t)ncoset(lp) + 8;
+}
+// the staged transforms' T1 and T2, after those
+__host__ __device__ inline size_t staged_words(int la, int lb, int lp) {
+  return (size_t)ntri(la) * ntri(lb) * (lp + 1) + (size_t)(la + 1) * (lb + 1) * ntri(lp);
+}
+// C_ab <-> C_xyz transform of a task with (shifted) angular momenta la, lb
+// in the coefficient kernel (forward) or the post kernel (adjoint): the
+// staged per-direction contractions (true) or the direct gather.
+// variant 0: direct, 1: staged, -1: staged forward where la or lb >= 3 and
+// direct in the adjoint (whose outputs, the C_ab entries, each gather only
+// their own non-zero terms); staged only where its scratch fits one CTA's
+// shared memory (200 KB).
+__host__ __device__ inline bool uses_staged(int variant, int la, int lb, bool forward) {
+  const int lp = la + lb;
+  if (coef_smem_words(ncoset(la), ncoset(lb), la, lb, lp) + staged_words(la, lb, lp) >
+      (size_t)(200 * 1024 / 8))
+    return false;
+  return variant == 1 || (variant < 0 && forward && (la >= 3 || lb >= 3));
+}
+// per-group shared-memory words of the coefficient / post kernels for a task
+size_t coef_words(int la, int lb, bool staged = false);
 
 void launch_decontract(const ContractArgs &a, cudaStream_t s);
 void launch_contract_hab(const ContractArgs &a, cudaStream_t s);

@@ -508,7 +508,8 @@ __global__ void __launch_bounds__(128) collocate_ortho_pl(GridArgs a, int wmax) 
 // integrate, orthorhombic (adjoint of collocate_ortho)
 // ------------------------------------------------------------------------
 template <typename N, int LPB>
-__global__ void __launch_bounds__(128, LPB <= 4 ? 5 : 1) integrate_ortho(GridArgs a, int wmax) {
+__global__ void __launch_bounds__(128, LPB <= 4 ? (std::is_same<N, float>::value ? 8 : 5) : 1)
+    integrate_ortho(GridArgs a, int wmax) {
   using T = typename Num<N>::T;
   using M = Num<N>;
   extern __shared__ __align__(16) unsigned char smem[];

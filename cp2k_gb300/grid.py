@@ -109,6 +109,8 @@ def lib():
         L.grid_gb300_autotune.restype = C.c_double
         L.grid_gb300_set_collocate_variant.argtypes = [vp, C.c_int]
         L.grid_gb300_set_model_bin_width.argtypes = [vp, C.c_double]
+        L.grid_gb300_set_transform_variant.argtypes = [vp, C.c_int]
+        L.grid_gb300_set_copy_chunks.argtypes = [vp, C.c_int]
         L.grid_gb300_tuned_split.argtypes = [vp]
         L.grid_gb300_tuned_split.restype = C.c_int
         L.grid_gb300_set_launch_timing.argtypes = [vp, C.c_int]
@@ -427,6 +429,17 @@ class GridTaskList:
         (grid_gb300_set_collocate_variant)."""
         lib().grid_gb300_set_collocate_variant(self.impl, int(variant))
 
+    def set_transform_variant(self, variant: int):
+        """C_ab <-> C_xyz transform: 0 direct, 1 staged, -1 staged in the
+        coefficient kernel only
+        (grid_gb300_set_transform_variant)."""
+        lib().grid_gb300_set_transform_variant(self.impl, int(variant))
+
+    def set_copy_chunks(self, chunks: int):
+        """Pieces of the pab / hab copies of the host-buffer calls
+        (grid_gb300_set_copy_chunks)."""
+        lib().grid_gb300_set_copy_chunks(self.impl, int(chunks))
+
     def set_model_bin_width(self, width: float):
         lib().grid_gb300_set_model_bin_width(self.impl, float(width))
 
@@ -518,3 +531,109 @@ def _stream(stream):
     if hasattr(stream, "cuda_stream"):
         return C.c_void_p(stream.cuda_stream)
     return C.c_void_p(int(stream))
+
+
+class PwTransfer:
+    """Device-resident transfer of the level grids to the plane-wave grid and
+    back (grid_gb300_pw_*): density_rs2pw / potential_pw2rs of CP2K's
+    src/pw_env/rs_pw_interface.F on torch CUDA float64 tensors."""
+
+    def __init__(self, npts):
+        L = lib()
+        if not hasattr(L, "_pw_bound"):
+            L.grid_gb300_pw_create.argtypes = [C.c_int, vp, C.POINTER(vp)]
+            L.grid_gb300_pw_free.argtypes = [vp]
+            L.grid_gb300_pw_density_rs2pw.argtypes = [vp, vp, vp, vp, vp]
+            L.grid_gb300_pw_potential_pw2rs.argtypes = [vp, vp, vp, vp]
+            L._pw_bound = True
+        self.npts = [tuple(int(x) for x in n) for n in npts]
+        arr = np.ascontiguousarray(np.array(self.npts, np.int32).ravel())
+        self.h = C.c_void_p()
+        L.grid_gb300_pw_create(len(self.npts), _p(arr), C.byref(self.h))
+
+    def density_rs2pw(self, rs_grids, rho=None, rho_gspace=None, stream=None):
+        ptrs = (C.c_void_p * len(rs_grids))(*[g.data_ptr() for g in rs_grids])
+        dp = lambda x: C.c_void_p(x.data_ptr()) if x is not None else None
+        lib().grid_gb300_pw_density_rs2pw(self.h, C.cast(ptrs, C.c_void_p), dp(rho),
+                                          dp(rho_gspace), _stream(stream))
+
+    def potential_pw2rs(self, v_rspace, rs_grids, stream=None):
+        ptrs = (C.c_void_p * len(rs_grids))(*[g.data_ptr() for g in rs_grids])
+        lib().grid_gb300_pw_potential_pw2rs(self.h, C.c_void_p(v_rspace.data_ptr()),
+                                            C.cast(ptrs, C.c_void_p), _stream(stream))
+
+    def close(self):
+        if self.h:
+            lib().grid_gb300_pw_free(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _pgf_bind(L):
+    if hasattr(L, "_pgf_bound"):
+        return
+    L.grid_cpu_collocate_pgf_product.argtypes = (
+        [C.c_bool, C.c_int, C.c_int] + [C.c_int] * 4 + [C.c_double] * 3 + [vp] * 8
+        + [C.c_double] + [C.c_int] * 4 + [vp, vp])
+    L.grid_cpu_integrate_pgf_product.argtypes = (
+        [C.c_bool, C.c_bool, C.c_int] + [C.c_int] * 4 + [C.c_double] * 2 + [vp] * 8
+        + [C.c_double] + [C.c_int] * 4 + [vp] * 8)
+    L._pgf_bound = True
+
+
+def _task_arrays(t):
+    f64 = lambda x: np.ascontiguousarray(x, np.float64)
+    i32 = lambda x: np.ascontiguousarray(x, np.int32)
+    return [f64(t["dh"]), f64(t["dh_inv"]), f64(t["ra"]), f64(t["rab"]), i32(t["npts_global"]),
+            i32(t["npts_local"]), i32(t["shift_local"]), i32(t["border_width"])]
+
+
+def collocate_pgf_product(t: dict, grid: np.ndarray = None) -> np.ndarray:
+    """grid_cpu_collocate_pgf_product (CP2K's single-task collocate, run on the
+    GPU) for a task description dict (keys as a CP2K .task file); the values
+    are added into `grid` (zeros if not given), which is returned."""
+    L = lib()
+    _pgf_bind(L)
+    nl = t["npts_local"]
+    if grid is None:
+        grid = np.zeros(int(nl[0] * nl[1] * nl[2]))
+    grid = np.ascontiguousarray(grid, np.float64)
+    arrs = _task_arrays(t)
+    pab = np.ascontiguousarray(t["pab"], np.float64)
+    L.grid_cpu_collocate_pgf_product(
+        bool(t["orthorhombic"]), int(t["border_mask"]), int(t["func"]), t["la_max"], t["la_min"],
+        t["lb_max"], t["lb_min"], t["zeta"], t["zetb"], t["rscale"], *[_p(a) for a in arrs],
+        t["radius"], t["o1"], t["o2"], t["n1"], t["n2"], _p(pab), _p(grid))
+    return grid
+
+
+def integrate_pgf_product(t: dict, grid: np.ndarray, compute_tau: bool, forces: bool = True,
+                          virial: bool = True, derivatives: bool = False):
+    """grid_cpu_integrate_pgf_product (CP2K's single-task integrate, run on the
+    GPU); returns (hab, forces[2][3], virials[2][3][3]) and, with
+    derivatives, also (hdab, hadb, a_hdab)."""
+    L = lib()
+    _pgf_bind(L)
+    hab = np.zeros((t["n2"], t["n1"]))
+    f = np.zeros((2, 3)) if forces else None
+    v = np.zeros((2, 3, 3)) if virial else None
+    hd = np.zeros((t["n2"], t["n1"], 3)) if derivatives else None
+    ha = np.zeros((t["n2"], t["n1"], 3)) if derivatives else None
+    ahd = np.zeros((t["n2"], t["n1"], 3, 3)) if derivatives else None
+    pab = np.ascontiguousarray(t["pab"], np.float64) if (forces or virial) else None
+    g = np.ascontiguousarray(grid, np.float64)
+    arrs = _task_arrays(t)
+    pp = lambda a: _p(a) if a is not None else None
+    L.grid_cpu_integrate_pgf_product(
+        bool(t["orthorhombic"]), bool(compute_tau), int(t["border_mask"]), t["la_max"],
+        t["la_min"], t["lb_max"], t["lb_min"], t["zeta"], t["zetb"], *[_p(a) for a in arrs],
+        t["radius"], t["o1"], t["o2"], t["n1"], t["n2"], _p(g), _p(hab), pp(pab), pp(f), pp(v),
+        pp(hd), pp(ha), pp(ahd))
+    if derivatives:
+        return hab, f, v, hd, ha, ahd
+    return hab, f, v

@@ -42,6 +42,8 @@ def main():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--forces", action="store_true")
     ap.add_argument("--virial", action="store_true")
+    ap.add_argument("--transform", type=int, default=-1, choices=[-1, 0, 1],
+                    help="C_ab <-> C_xyz transform: 0 direct, 1 staged, -1 staged forward")
     ap.add_argument("--compare", action="store_true",
                     help="also run FP64 and print times and errors as one JSON line")
     args = ap.parse_args()
@@ -55,6 +57,7 @@ def main():
     tl = G.GridTaskList(inp, precision=PRECISIONS[args.precision])
     if args.threshold is not None:
         tl.set_mixed_threshold(args.threshold)
+    tl.set_transform_variant(args.transform)
     s = torch.cuda.current_stream()
     if not args.compare:
         for step in range(args.steps):
@@ -69,7 +72,8 @@ def main():
         return
 
     res = {"config": args.config, "scale": args.scale, "ntasks": inp.ntasks,
-           "precision": args.precision, "forces": args.forces, "virial": args.virial}
+           "precision": args.precision, "forces": args.forces, "virial": args.virial,
+           "transform": args.transform}
     out = {}
     for name, prec in (("fp64", G.FP64), (args.precision, PRECISIONS[args.precision])):
         tl.set_precision(prec)

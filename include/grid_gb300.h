@@ -338,6 +338,19 @@ void grid_gb300_set_collocate_variant(const grid_gb300_task_list *task_list,
 /* Cube width separating the small- and large-cube queues at the current
  * precision (default 34). */
 int grid_gb300_tuned_split(const grid_gb300_task_list *task_list);
+/* Host-buffer calls (grid_gb300_collocate_task_list / _integrate_task_list
+ * and the CP2K surface) move pab in and hab out in `chunks` pieces (1..7,
+ * default 3) on a copy stream, sizes growing 1 : 2 : 4 in block order, so
+ * that the copies overlap the kernels of other pieces.  No counterpart in
+ * CP2K (src/grid/gpu/grid_gpu_context.cu:509, 528, 645 copy whole buffers). */
+void grid_gb300_set_copy_chunks(const grid_gb300_task_list *task_list, int chunks);
+/* C_ab <-> C_xyz change of basis of the coefficient and post kernels: 0 the
+ * direct gather over all (a, b) pairs, 1 the staged per-direction
+ * contractions (x, then y, then z), -1 (default) staged in the coefficient
+ * kernel where la or lb >= 3 and direct in the post kernel.
+ * No counterpart in CP2K (src/grid/ref/grid_ref_collint.h:827-911 runs the
+ * direct loops); both give the same results up to rounding. */
+void grid_gb300_set_transform_variant(const grid_gb300_task_list *task_list, int variant);
 
 /* CUDA-graph capture of one SCF step on device buffers: collocate(func)
  * into rho_grids, then integrate v_grids into hab (forces / virial optional,
@@ -436,6 +449,32 @@ void grid_gb300_apply_cost_model(const grid_gb300_task_list *task_list,
                                  const float *params, const float *norm,
                                  void *stream);
 
+/* ---- single tasks (src/grid/grid_api.F:145, 318 bind these by name) ------
+ * grid_cpu_collocate_pgf_product (src/grid/cpu/grid_cpu_collocate.h) and
+ * grid_cpu_integrate_pgf_product (src/grid/cpu/grid_cpu_integrate.h): one
+ * primitive pair on host buffers, same arguments and meaning; the work runs
+ * on the GPU in FP64 (the block and the whole grid go to the device and
+ * back; every output is accumulated into, as the reference does).  pab, hab:
+ * [n2][n1]; forces [2][3] and virials [2][3][3] of atoms a and b; hdab,
+ * hadb [n2][n1][3] and a_hdab [n2][n1][3][3] (not with compute_tau).
+ * Synchronous; calls from several threads are serialised. */
+void grid_cpu_collocate_pgf_product(
+    const bool orthorhombic, const int border_mask, const enum grid_func func,
+    const int la_max, const int la_min, const int lb_max, const int lb_min,
+    const double zeta, const double zetb, const double rscale, const double *dh,
+    const double *dh_inv, const double *ra, const double *rab, const int *npts_global,
+    const int *npts_local, const int *shift_local, const int *border_width,
+    const double radius, const int o1, const int o2, const int n1, const int n2,
+    const double *pab, double *grid);
+void grid_cpu_integrate_pgf_product(
+    const bool orthorhombic, const bool compute_tau, const int border_mask, const int la_max,
+    const int la_min, const int lb_max, const int lb_min, const double zeta, const double zetb,
+    const double *dh, const double *dh_inv, const double *ra, const double *rab,
+    const int *npts_global, const int *npts_local, const int *shift_local,
+    const int *border_width, const double radius, const int o1, const int o2, const int n1,
+    const int n2, const double *grid, double *hab, const double *pab, double *forces,
+    double *virials, double *hdab, double *hadb, double *a_hdab);
+
 /* Allocation-free collocation of one primitive pair, for callers that
  * cannot allocate device memory at call time (a program that gave the GPU's
  * memory to its own fixed arena at start-up, drivers that forbid cudaMalloc
@@ -466,6 +505,30 @@ int grid_gb300_collocate_pgf_product_static(
     const double *pab, double *grid, void *stream);
 size_t grid_gb300_static_scratch_bytes(void);
 const char *grid_gb300_static_scratch_error(void);
+
+/* ---- plane-wave transfer of the multigrid levels (device resident) -------
+ * The steps either side of collocate / integrate in a Quickstep SCF cycle:
+ * density_rs2pw (src/pw_env/rs_pw_interface.F:64-136) and potential_pw2rs
+ * (:151-228) with the default interpolation (pw_interp) on replicated grids,
+ * so that rho -> plane-wave grid -> potential -> level grids stays in device
+ * memory.  npts: [nlevels][3] (x, y, z) points per level, finest first; all
+ * arrays device pointers, grids x fastest ([nz][ny][nx]); G-space arrays the
+ * full complex box of the finest level (re, im pairs of doubles) in FFT
+ * order, coefficients normalised by the number of points as the reference's
+ * forward transform does.  Work is enqueued on `stream`. */
+typedef struct grid_gb300_pw_transfer grid_gb300_pw_transfer;
+void grid_gb300_pw_create(const int nlevels, const int *npts, grid_gb300_pw_transfer **handle);
+void grid_gb300_pw_free(grid_gb300_pw_transfer *handle);
+/* rho (finest grid, may be NULL) and rho_gspace (may be NULL) from the
+ * collocated level grids: the sum over levels of their spectra on the
+ * finest grid's frequencies, transformed back to real space. */
+void grid_gb300_pw_density_rs2pw(grid_gb300_pw_transfer *handle, const double *const *rs_grids,
+                                 double *rho, void *rho_gspace, void *stream);
+/* The potential on every level grid from the potential on the finest grid:
+ * the finest level copies it, coarser levels take its coefficients at their
+ * frequencies, transform back and scale by dvol(level) / dvol(finest). */
+void grid_gb300_pw_potential_pw2rs(grid_gb300_pw_transfer *handle, const double *v_rspace,
+                                   double *const *rs_grids, void *stream);
 
 /* Last error message recorded by the library ("" if none). */
 const char *grid_gb300_last_error(void);

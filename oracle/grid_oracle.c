@@ -844,9 +844,12 @@ void oracle_integrate_pgf_product(
     const double *rab, const int *npts_global, const int *npts_local,
     const int *shift_local, const int *border_width, double radius, int o1,
     int o2, int n1, int n2, const double *grid, double *hab,
-    const double *pab, double *forces, double *virials) {
+    const double *pab, double *forces, double *virials, double *hdab,
+    double *hadb, double *a_hdab) {
   (void)n2;
-  const bool do_f = forces != NULL, do_v = virials != NULL;
+  /* grid_ref_integrate.c:56-57: the derivative blocks need the same shifts */
+  const bool do_f = forces != NULL || hdab != NULL || hadb != NULL,
+             do_v = virials != NULL || a_hdab != NULL;
   /* process_get_ldiffs, grid_process_vab.h:222-251 */
   int amax_d = 0, amin_d = 0, bmax_d = 0, bmin_d = 0;
   if (do_f || do_v) {
@@ -876,14 +879,24 @@ void oracle_integrate_pgf_product(
               const orb b = {{bx, by, lb - bx - by}};
               const size_t e = (size_t)(o2 + o_idx(b)) * n1 + o1 + o_idx(a);
               hab[e] += vab(&x, compute_tau, V_HAB, 0, 0, a, b);
-              if (do_f) {
+              /* grid_ref_integrate.c:121-145 (no tau) */
+              for (int i = 0; i < 3; i++) {
+                if (hdab != NULL)
+                  hdab[e * 3 + i] += vab(&x, false, V_FA, i, 0, a, b);
+                if (hadb != NULL)
+                  hadb[e * 3 + i] += vab(&x, false, V_FB, i, 0, a, b);
+                if (a_hdab != NULL)
+                  for (int j = 0; j < 3; j++)
+                    a_hdab[(e * 3 + i) * 3 + j] += vab(&x, false, V_VA, i, j, a, b);
+              }
+              if (forces != NULL) {
                 const double p = pab[e];
                 for (int i = 0; i < 3; i++) {
                   forces[i] += p * vab(&x, compute_tau, V_FA, i, 0, a, b);
                   forces[3 + i] += p * vab(&x, compute_tau, V_FB, i, 0, a, b);
                 }
               }
-              if (do_v) {
+              if (virials != NULL) {
                 const double p = pab[e];
                 for (int i = 0; i < 3; i++)
                   for (int j = 0; j < 3; j++) {
@@ -1220,7 +1233,7 @@ void oracle_integrate_task_list(const void *p, bool compute_tau, int natoms,
                 &t->shift_local[3 * level], &t->border_width[3 * level],
                 k->radius, (k->ipgf - 1) * s.ncoseta, (k->jpgf - 1) * s.ncosetb,
                 s.ncoa, s.ncob, grids[level], hab, need_pab ? pab : NULL,
-                forces ? f : NULL, virial ? v : NULL);
+                forces ? f : NULL, virial ? v : NULL, NULL, NULL, NULL);
           }
           store_hab(ib, jb, iset, jset, ia <= ja, hab, block);
         }

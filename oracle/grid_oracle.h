@@ -63,7 +63,8 @@ void oracle_integrate_task_list(const void *task_list, bool compute_tau,
 /* Single-task entry points with the argument meaning of
  * grid_ref_collocate_pgf_product / grid_ref_integrate_pgf_product
  * (src/grid/ref/grid_ref_collocate.h, grid_ref_integrate.h).
- * pab/hab are [n2][n1]; forces [2][3]; virials [2][3][3]. */
+ * pab/hab are [n2][n1]; forces [2][3]; virials [2][3][3]; hdab, hadb
+ * [n2][n1][3] and a_hdab [n2][n1][3][3] (may be NULL). */
 void oracle_collocate_pgf_product(
     bool orthorhombic, int border_mask, int func, int la_max, int la_min,
     int lb_max, int lb_min, double zeta, double zetb, double rscale,
@@ -79,7 +80,8 @@ void oracle_integrate_pgf_product(
     const double *rab, const int *npts_global, const int *npts_local,
     const int *shift_local, const int *border_width, double radius, int o1,
     int o2, int n1, int n2, const double *grid, double *hab,
-    const double *pab, double *forces, double *virials);
+    const double *pab, double *forces, double *virials, double *hdab,
+    double *hadb, double *a_hdab);
 
 /* Number of grid points the oracle's loops visit for every task of the list
  * (in the caller's task order), with the cube-to-grid contraction order lp

@@ -55,7 +55,7 @@ def lib():
             L.oracle_integrate_pgf_product.argtypes = (
                 [C.c_bool, C.c_bool, C.c_int] + [C.c_int] * 4 + [C.c_double] * 2
                 + [_dp] * 4 + [_ip] * 4 + [C.c_double] + [C.c_int] * 4
-                + [_dp, _dp, vp, vp, vp])
+                + [_dp, _dp, vp, vp, vp, vp, vp, vp])
             L.oracle_count_task_points.restype = C.c_longlong
             L.oracle_count_task_points.argtypes = [vp, C.c_int, vp, vp]
             _LIB = L
@@ -92,11 +92,16 @@ def collocate_pgf_product(t: dict) -> np.ndarray:
 
 
 def integrate_pgf_product(t: dict, grid: np.ndarray, compute_tau: bool,
-                          forces: bool = True, virial: bool = True):
-    """Integrate one task; returns (hab[n2][n1], forces[2][3], virials[2][3][3])."""
+                          forces: bool = True, virial: bool = True, derivatives: bool = False):
+    """Integrate one task; returns (hab[n2][n1], forces[2][3], virials[2][3][3])
+    and, with derivatives=True, also (hdab[n2][n1][3], hadb[n2][n1][3],
+    a_hdab[n2][n1][3][3]) (grid_ref_integrate.c:121-145; not with tau)."""
     hab = np.zeros((t["n2"], t["n1"]), dtype=np.float64)
     f = np.zeros((2, 3)) if forces else None
     v = np.zeros((2, 3, 3)) if virial else None
+    hd = np.zeros((t["n2"], t["n1"], 3)) if derivatives else None
+    ha = np.zeros((t["n2"], t["n1"], 3)) if derivatives else None
+    ahd = np.zeros((t["n2"], t["n1"], 3, 3)) if derivatives else None
     pab = _f64(t["pab"]) if (forces or virial) else None
     lib().oracle_integrate_pgf_product(
         bool(t["orthorhombic"]), bool(compute_tau), int(t["border_mask"]),
@@ -104,7 +109,9 @@ def integrate_pgf_product(t: dict, grid: np.ndarray, compute_tau: bool,
         _f64(t["dh"]), _f64(t["dh_inv"]), _f64(t["ra"]), _f64(t["rab"]),
         _i32(t["npts_global"]), _i32(t["npts_local"]), _i32(t["shift_local"]),
         _i32(t["border_width"]), t["radius"], t["o1"], t["o2"], t["n1"], t["n2"],
-        _f64(grid), hab, _ptr(pab), _ptr(f), _ptr(v))
+        _f64(grid), hab, _ptr(pab), _ptr(f), _ptr(v), _ptr(hd), _ptr(ha), _ptr(ahd))
+    if derivatives:
+        return hab, f, v, hd, ha, ahd
     return hab, f, v
 
 

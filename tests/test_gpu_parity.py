@@ -381,3 +381,73 @@ def test_general_boxes_split_by_planes(G, O):
         assert rel_diff(v, v_ref) < tol_d
         tl.close()
     ot.close()
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2])
+@pytest.mark.parametrize("case", ["tricl", "ortho_l3"])
+def test_transform_variants_agree(G, O, prec, case):
+    """The staged (x, then y, then z) and the direct C_ab <-> C_xyz transforms
+    of the coefficient and post kernels give the oracle's results: FP64 to
+    the bounds of the FP64 tests, the double-float class (threshold 0) to
+    1e-9 / 1e-7, FP32 to 1e-5 of the maximum (its stated accuracy; sets up to
+    l = 3 cancel more than the workloads' l <= 2); collocation of rho and of the
+    tau density, integration with tau, forces and virial."""
+    from cp2k_gb300 import workload as W
+    if case == "tricl":
+        inp = W.config("c3_256atoms_triclinic", scale=0.1, seed=35)
+    else:
+        inp = W.config("c1_64atoms", scale=0.2, seed=36, elements=[(1.0, [3, 2])])
+    pab = W.density_blocks(inp)
+    V = W.potential_grids(inp)
+    ot = O.OracleTaskList(inp)
+    ref = {f: ot.collocate(f, pab) for f in (100, 200)}
+    h_ref, f_ref, v_ref = ot.integrate(V, pab, compute_tau=True, forces=True, virial=True)
+    ot.close()
+    tl = G.GridTaskList(inp, precision=prec)
+    if prec == G.MIXED:
+        tl.set_mixed_threshold(0.0)
+    tol = {G.FP64: (1e-11, TOL_DERIV), G.MIXED: (1e-9, 1e-7)}
+    for variant in (0, 1):
+        tl.set_transform_variant(variant)
+        for f in (100, 200):
+            g = tl.collocate(f, pab)
+            if prec == G.FP32:
+                gmax = max(float(np.abs(r).max()) for r in ref[f])
+                assert max(float(np.abs(a - b).max()) for a, b in zip(g, ref[f])) / gmax < 1e-5
+            else:
+                assert max(rel_diff(a, b) for a, b in zip(g, ref[f])) < tol[prec][0], (variant, f)
+        h, fo, vi = tl.integrate(V, pab, compute_tau=True, forces=True, virial=True)
+        if prec == G.FP32:
+            assert float(np.abs(h - h_ref).max()) / float(np.abs(h_ref).max()) < 1e-5
+        else:
+            assert rel_diff(h, h_ref) < tol[prec][0], variant
+            assert rel_diff(fo, f_ref) < tol[prec][1], variant
+            assert rel_diff(vi, v_ref) < tol[prec][1], variant
+    tl.close()
+
+
+@pytest.mark.parametrize("api", ["cp2k", "backend"])
+def test_copy_chunks_agree(G, O, api):
+    """Host-buffer calls copy pab in and hab out in pieces that overlap the
+    kernels (grid_gb300_set_copy_chunks); 1, 2 and 3 pieces give the oracle's
+    results, and hab entries past the task list's blocks come back zeroed."""
+    from cp2k_gb300 import workload as W
+    inp = W.config("c2_512atoms", scale=0.1, seed=37)
+    pab = W.density_blocks(inp)
+    V = W.potential_grids(inp)
+    ot = O.OracleTaskList(inp)
+    g_ref = ot.collocate(100, pab)
+    h_ref, f_ref, v_ref = ot.integrate(V, pab, forces=True, virial=True)
+    ot.close()
+    tl = G.GridTaskList(inp, precision=G.FP64, api=api)
+    for chunks in (1, 2, 3):
+        tl.set_copy_chunks(chunks)
+        g = tl.collocate(100, pab)
+        assert max(rel_diff(a, b) for a, b in zip(g, g_ref)) < TOL_GRID, chunks
+        _, hab_buf, _ = tl.host_buffers()
+        hab_buf.host[:] = 7.0  # stale values must not survive
+        h, f, v = tl.integrate(V, pab, forces=True, virial=True)
+        assert rel_diff(h, h_ref) < TOL_GRID, chunks
+        assert rel_diff(f, f_ref) < TOL_DERIV
+        assert rel_diff(v, v_ref) < TOL_DERIV
+    tl.close()

@@ -138,3 +138,58 @@ def test_adjointness(O):
     rhs = float(np.dot(pab * w, hab))
     assert abs(lhs - rhs) <= 1e-10 * max(1.0, abs(lhs))
     tl.close()
+
+
+def _ref_integrate_pgf(t, grid, tau, derivatives):
+    """CP2K's grid_ref_integrate_pgf_product (src/grid/ref/grid_ref_integrate.c:
+    44-152) from the reference library built from its sources."""
+    import ctypes as C
+
+    from oracle import refgrid as R
+    L = R.lib()  # loads the library and runs grid_library_init
+    fn = L.grid_ref_integrate_pgf_product
+    f64 = lambda a: np.ascontiguousarray(a, np.float64)
+    i32 = lambda a: np.ascontiguousarray(a, np.int32)
+    p = lambda a: a.ctypes.data_as(C.c_void_p) if a is not None else None
+    fn.argtypes = ([C.c_bool, C.c_bool, C.c_int] + [C.c_int] * 4 + [C.c_double] * 2
+                   + [C.c_void_p] * 8 + [C.c_double] + [C.c_int] * 4 + [C.c_void_p] * 8)
+    hab = np.zeros((t["n2"], t["n1"]))
+    f, v = np.zeros((2, 3)), np.zeros((2, 3, 3))
+    hd = np.zeros((t["n2"], t["n1"], 3)) if derivatives else None
+    ha = np.zeros((t["n2"], t["n1"], 3)) if derivatives else None
+    ahd = np.zeros((t["n2"], t["n1"], 3, 3)) if derivatives else None
+    arrs = [f64(t["dh"]), f64(t["dh_inv"]), f64(t["ra"]), f64(t["rab"]),
+            i32(t["npts_global"]), i32(t["npts_local"]), i32(t["shift_local"]),
+            i32(t["border_width"])]
+    pab = f64(t["pab"])
+    g = f64(grid)
+    fn(bool(t["orthorhombic"]), bool(tau), int(t["border_mask"]), t["la_max"], t["la_min"],
+       t["lb_max"], t["lb_min"], t["zeta"], t["zetb"], *[p(a) for a in arrs], t["radius"],
+       t["o1"], t["o2"], t["n1"], t["n2"], p(g), p(hab), p(pab), p(f), p(v), p(hd), p(ha),
+       p(ahd))
+    return hab, f, v, hd, ha, ahd
+
+
+@pytest.mark.parametrize("name", ["ortho_density_l0122", "ortho_density_l3333",
+                                  "general_density", "general_subpatch16", "ortho_tau"])
+def test_oracle_pgf_derivative_blocks_vs_reference_library(O, name):
+    """The single-task integrate's optional outputs -- hdab, hadb, a_hdab
+    (d hab / d a, d hab / d b, the virial of hab) and the separate virials of
+    atoms a and b -- against CP2K's REF library on the recorded tasks."""
+    from oracle import refgrid as R
+    if not R.available():
+        pytest.skip("CP2K's reference library is not built here")
+    t = digest_task(load_digests()[name])
+    grid = O.collocate_pgf_product(t)
+    tau = t["func"] == 200
+    got = O.integrate_pgf_product(t, grid, tau, derivatives=not tau)
+    exp = _ref_integrate_pgf(t, grid, tau, derivatives=not tau)
+    # hab at the reference's 1e-12; forces and virials at its 1e-8
+    # (src/grid/grid_replay.c:445, 481, 495: weighed by 1e-4), which also
+    # bounds the derivative blocks built from the same terms
+    assert rel_diff(got[0], exp[0]) < 1e-12
+    assert rel_diff(got[1], exp[1]) < 1e-8
+    assert rel_diff(got[2], exp[2]) < 1e-8
+    if not tau:
+        for a, b in zip(got[3:], exp[3:]):
+            assert rel_diff(a, b) < 1e-8
