@@ -241,8 +241,8 @@ def measure_peak(torch, dtype, n):
 # of this workload (two launches per kernel, mean); the bench cannot run ncu
 # itself.  Keys: kernel label as in "roofline.kernel".
 NCU_TRAFFIC = {
-    "integrate_ortho<dfloat,4>": None,
-    "integrate_ortho<double,4>": None,
+    "integrate_ortho<dfloat,4>": 0.5 * ((37.778 + 1.220) + (244.241 + 62.083)) * 1e6,
+    "integrate_ortho<double,4>": 0.5 * ((35.777 + 0.760) + (594.138 + 123.159)) * 1e6,
 }
 
 

@@ -377,7 +377,7 @@ __global__ void __launch_bounds__(128) collocate_general(GridArgs a, int njmax) 
           if constexpr (sizeof(T) == 8)
             atomicAdd(gplane + (size_t)jg * nx + ig, (double)(v * gauss));
           else // integer-pipe conversion: the FP64 pipe is the scarce one
-            atomicAdd(gplane + (size_t)jg * nx + ig, f2d_exact((float)(v * gauss)));
+            atomicAdd(gplane + (size_t)jg * nx + ig, f2d_grid((float)(v * gauss)));
         }
         __syncwarp();
       }
@@ -741,7 +741,7 @@ __global__ void __launch_bounds__(128) collocate_general_df(GridArgs a, int njma
               v = df_fma(q[jl], v, dj);
           const dfloat val = df_mul(v, gauss);
           const size_t idx = (size_t)jg * nx + ig;
-          atomicAdd(gplane + idx, f2d_exact(val.h));
+          atomicAdd(gplane + idx, f2d_grid(val.h));
           atomicAdd(lplane + idx, val.l);
         }
         __syncwarp();
@@ -1127,7 +1127,7 @@ __global__ void __launch_bounds__(128) collocate_general_pl(GridArgs a, int njma
             if (jl <= lp)
               v = df_fma(q[jl], v, dj);
           const dfloat val = df_mul(v, gauss);
-          atomicAdd(gplane + idx, f2d_exact(val.h));
+          atomicAdd(gplane + idx, f2d_grid(val.h));
           atomicAdd(glo + (size_t)kg * nxy + idx, val.l);
         } else {
           const float djf = rf + fj0f;
@@ -1143,7 +1143,7 @@ __global__ void __launch_bounds__(128) collocate_general_pl(GridArgs a, int njma
           for (int jl = P - 1; jl >= 0; jl--)
             if (jl <= lp)
               v = fmaf(v, djf, q[jl]);
-          atomicAdd(gplane + idx, f2d_exact(v * expf(-zetpf * r2)));
+          atomicAdd(gplane + idx, f2d_grid(v * expf(-zetpf * r2)));
         }
       }
       __syncwarp();

@@ -171,10 +171,10 @@ template <typename N>
 __device__ __forceinline__ void grid_add(double *g, float *glo, size_t i,
                                          typename Num<N>::T v) {
   if constexpr (std::is_same<N, dfloat>::value) {
-    atomicAdd(g + i, f2d_exact(v.h));
+    atomicAdd(g + i, f2d_grid(v.h));
     atomicAdd(glo + i, v.l);
   } else if constexpr (std::is_same<N, float>::value) {
-    atomicAdd(g + i, f2d_exact(v));
+    atomicAdd(g + i, f2d_grid(v));
   } else {
     atomicAdd(g + i, v);
   }
@@ -508,8 +508,7 @@ __global__ void __launch_bounds__(128) collocate_ortho_pl(GridArgs a, int wmax) 
 // integrate, orthorhombic (adjoint of collocate_ortho)
 // ------------------------------------------------------------------------
 template <typename N, int LPB>
-__global__ void __launch_bounds__(128, LPB <= 4 ? (std::is_same<N, float>::value ? 8 : 5) : 1)
-    integrate_ortho(GridArgs a, int wmax) {
+__global__ void __launch_bounds__(128, LPB <= 4 ? 5 : 1) integrate_ortho(GridArgs a, int wmax) {
   using T = typename Num<N>::T;
   using M = Num<N>;
   extern __shared__ __align__(16) unsigned char smem[];

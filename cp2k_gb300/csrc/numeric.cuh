@@ -181,6 +181,16 @@ __device__ __forceinline__ double f2d_exact(float x) {
   return __hiloint2double((int)hi, (int)lo);
 }
 
+// FP32 -> FP64 for the grid atomics: exact for every normal float, in four
+// integer operations (the exponent rebias of f2d_exact without its zero and
+// subnormal branch).  Zero and subnormal inputs (|x| < 1.2e-38) become
+// doubles of magnitude below 1.2e-38, far under any value the grids resolve.
+__device__ __forceinline__ double f2d_grid(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned hi = (((u >> 3) & 0x0fffffffu) + 0x38000000u) | (u & 0x80000000u);
+  return __hiloint2double((int)hi, (int)(u << 29));
+}
+
 // ---------------------------------------------------------------------------
 // uniform interface over double / float / dfloat
 // ---------------------------------------------------------------------------
