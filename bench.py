@@ -511,6 +511,10 @@ def gpu_arm(args, world, rank, local):
     graph_kernels = graph.kernels
     graph.free()
     t_size = run_steps(G.MIXED, G.SCHEDULE_SIZE, max(1, min(args.steps, 5)))
+    # the queue launches of each phase on one stream (no tail overlap)
+    tl.set_queue_streams(1)
+    t_one_stream = run_steps(G.MIXED, sched_mixed, max(1, min(args.steps, 5)))
+    tl.set_queue_streams(2)
     t_fp64 = run_steps(G.FP64, G.SCHEDULE_SIZE, max(1, min(args.steps, 3)))
     rho64 = [g.cpu().numpy() for g in grids]
     hab64 = hab.cpu().numpy()
@@ -593,6 +597,8 @@ def gpu_arm(args, world, rank, local):
                        "cost_model": model_path},
             "fp64_ms_per_step": ms_fp64, "speedup_vs_fp64": ms_fp64 / ms_mixed,
             "mixed_size_schedule_ms_per_step": ms_size,
+            "mixed_one_queue_stream_ms_per_step": max_over_ranks(float(np.mean(t_one_stream)),
+                                                                 world),
             "mixed_cuda_graph_ms_per_step": max_over_ranks(float(np.mean(t_graph)), world),
             "cuda_graph_kernels": int(graph_kernels),
             "autotune": {{0: "fp64", 1: "mixed", 2: "fp32"}[p]: {"grid_ms": v[0], "size_split": v[1]}

@@ -368,6 +368,11 @@ struct TaskList {
   int chunks_for = -1; // copy_chunks the chunks were computed for
   cudaStream_t copy_stream = nullptr;
   std::vector<cudaEvent_t> copy_ev;
+  // the independent grid launches of a phase alternate over this many
+  // streams, so that one launch's tail overlaps the next one's start
+  int queue_streams = 2;
+  cudaStream_t aux_stream = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   int *d_error = nullptr;
   long long *d_cycles = nullptr;
   cudaStream_t stream = nullptr;
@@ -695,6 +700,12 @@ static void free_device(TaskList *t) {
     cudaEventDestroy(e);
   if (t->copy_stream)
     cudaStreamDestroy(t->copy_stream);
+  if (t->fork_ev)
+    cudaEventDestroy(t->fork_ev);
+  if (t->join_ev)
+    cudaEventDestroy(t->join_ev);
+  if (t->aux_stream)
+    cudaStreamDestroy(t->aux_stream);
 }
 
 static bool sphi_is_identity(const grid_basis_set *b, int iset) {
@@ -1378,6 +1389,35 @@ static void grid_launch(TaskList *t, const Queue &q, int phase, int arith, const
   }
 }
 
+// Grid launches of one phase are independent (each its own tasks and work
+// counter; the grids take atomic adds): with two queue streams they
+// alternate between the caller's stream and an auxiliary one, forked from
+// and joined back into the caller's stream around the phase.  Per-launch
+// timing keeps them on one stream.
+static bool two_queue_streams(const TaskList *t) {
+  return t->queue_streams > 1 && !t->launch_timing;
+}
+static void fork_queues(TaskList *t, cudaStream_t s) {
+  if (!two_queue_streams(t))
+    return;
+  if (!t->aux_stream) {
+    CK(cudaStreamCreateWithFlags(&t->aux_stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&t->fork_ev, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&t->join_ev, cudaEventDisableTiming));
+  }
+  CK(cudaEventRecord(t->fork_ev, s));
+  CK(cudaStreamWaitEvent(t->aux_stream, t->fork_ev, 0));
+}
+static cudaStream_t queue_stream(const TaskList *t, cudaStream_t s, int i) {
+  return (two_queue_streams(t) && (i & 1)) ? t->aux_stream : s;
+}
+static void join_queues(TaskList *t, cudaStream_t s) {
+  if (!two_queue_streams(t))
+    return;
+  CK(cudaEventRecord(t->join_ev, t->aux_stream));
+  CK(cudaStreamWaitEvent(s, t->join_ev, 0));
+}
+
 static void begin_call(TaskList *t, cudaStream_t s) {
   if (!t->capturing)
     t->launches.clear();
@@ -1498,6 +1538,7 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
   }
   record_phase(t, 1, s);
   int qi = 0;
+  fork_queues(t, s);
   {
     for (const Queue &q : m.queues) {
       ga.queue = q.d_idx;
@@ -1508,11 +1549,12 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
         fail("more than %d work queues in one call", kMaxQueues);
       ga.counter = t->d_counters + qi++;
       ga.coef_stride = q.fp32 ? 2 : 1;
-      grid_launch(t, q, 0, q.fp32 ? (int)ARITH_FP32 : arith, ga, s);
+      grid_launch(t, q, 0, q.fp32 ? (int)ARITH_FP32 : arith, ga, queue_stream(t, s, qi));
       grid_library_counter_add(kBucketLp[q.bucket], GRID_BACKEND_GB300,
                                q.general ? GRID_COLLOCATE_GENERAL : GRID_COLLOCATE_ORTHO, q.n);
     }
   }
+  join_queues(t, s);
   if (arith == ARITH_MIXED)
     for (int l = 0; l < t->nlevels; l++) {
       const int *n = &t->npts_local[3 * l];
@@ -1596,6 +1638,7 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
               t->ntasks, tau ? 1 : 0, d, t->d_levels, t->d_dhtab, t->d_dhtab_f, t->d_dhtab_df,
               nullptr, 0, m.transform};
   int qi = 0;
+  fork_queues(t, s);
   for (const Queue &q : m.queues) {
     {
       ga.queue = q.d_idx;
@@ -1612,11 +1655,12 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
         ga.grids_in[l] = arith == ARITH_FP64                  ? (const void *)grids[l]
                          : (arith == ARITH_MIXED && q.fp32) ? (const void *)t->d_gridhi[l]
                                                             : (const void *)t->d_gridsplit[l];
-      grid_launch(t, q, 1, q.fp32 ? (int)ARITH_FP32 : arith, ga, s);
+      grid_launch(t, q, 1, q.fp32 ? (int)ARITH_FP32 : arith, ga, queue_stream(t, s, qi));
       grid_library_counter_add(kBucketLp[q.bucket], GRID_BACKEND_GB300,
                                q.general ? GRID_INTEGRATE_GENERAL : GRID_INTEGRATE_ORTHO, q.n);
     }
   }
+  join_queues(t, s);
   record_phase(t, 2, s);
   // integrated coefficients -> hab (forces, virial), piece by piece where the
   // host-buffer call copies hab out in pieces: the largest piece first, so
@@ -1691,7 +1735,7 @@ GB300_API void grid_gb300_create_task_list(
   // predictions, timings) belong to the old geometry and are dropped; the
   // learned schedule falls back to the size order until a model is applied.
   struct Kept {
-    int precision, schedule, coll_variant, transform_variant, copy_chunks;
+    int precision, schedule, coll_variant, transform_variant, copy_chunks, queue_streams;
     double mixed_threshold, model_bin;
     int small_extent[3];
     std::map<std::tuple<int, int, int>, LaunchCfg> tuned;
@@ -1701,7 +1745,7 @@ GB300_API void grid_gb300_create_task_list(
   if (*task_list) {
     const TaskList *o = TL(*task_list);
     kept.reset(new Kept{o->precision, o->schedule, o->coll_variant, o->transform_variant,
-                        o->copy_chunks, o->mixed_threshold,
+                        o->copy_chunks, o->queue_streams, o->mixed_threshold,
                         o->model_bin, {o->small_extent[0], o->small_extent[1],
                                        o->small_extent[2]},
                         o->tuned, o->launch_timing, o->task_timing});
@@ -1720,6 +1764,7 @@ GB300_API void grid_gb300_create_task_list(
     t->coll_variant = kept->coll_variant;
     t->transform_variant = kept->transform_variant;
     t->copy_chunks = kept->copy_chunks;
+    t->queue_streams = kept->queue_streams;
     t->mixed_threshold = kept->mixed_threshold;
     t->model_bin = kept->model_bin;
     for (int i = 0; i < 3; i++)
@@ -2409,6 +2454,12 @@ GB300_API void grid_gb300_set_collocate_variant(const grid_gb300_task_list *task
   t->coll_variant = variant;
   t->tuned.clear();
   t->gen++;
+}
+
+GB300_API void grid_gb300_set_queue_streams(const grid_gb300_task_list *task_list, int n) {
+  if (n < 1 || n > 2)
+    fail("queue streams must be 1 or 2, got %d", n);
+  TL(task_list)->queue_streams = n;
 }
 
 GB300_API void grid_gb300_set_copy_chunks(const grid_gb300_task_list *task_list, int chunks) {

@@ -111,6 +111,7 @@ def lib():
         L.grid_gb300_set_model_bin_width.argtypes = [vp, C.c_double]
         L.grid_gb300_set_transform_variant.argtypes = [vp, C.c_int]
         L.grid_gb300_set_copy_chunks.argtypes = [vp, C.c_int]
+        L.grid_gb300_set_queue_streams.argtypes = [vp, C.c_int]
         L.grid_gb300_tuned_split.argtypes = [vp]
         L.grid_gb300_tuned_split.restype = C.c_int
         L.grid_gb300_set_launch_timing.argtypes = [vp, C.c_int]
@@ -434,6 +435,11 @@ class GridTaskList:
         coefficient kernel only
         (grid_gb300_set_transform_variant)."""
         lib().grid_gb300_set_transform_variant(self.impl, int(variant))
+
+    def set_queue_streams(self, n: int):
+        """Streams the grid launches of a phase alternate over (1 or 2;
+        grid_gb300_set_queue_streams)."""
+        lib().grid_gb300_set_queue_streams(self.impl, int(n))
 
     def set_copy_chunks(self, chunks: int):
         """Pieces of the pab / hab copies of the host-buffer calls

@@ -344,6 +344,12 @@ int grid_gb300_tuned_split(const grid_gb300_task_list *task_list);
  * that the copies overlap the kernels of other pieces.  No counterpart in
  * CP2K (src/grid/gpu/grid_gpu_context.cu:509, 528, 645 copy whole buffers). */
 void grid_gb300_set_copy_chunks(const grid_gb300_task_list *task_list, int chunks);
+/* The grid-kernel launches of a collocate or integrate (one per work queue,
+ * independent of each other) alternate over n streams (1 or 2, default 2):
+ * the caller's stream and an auxiliary one forked from and joined back into
+ * it, so that the tail of one launch overlaps the start of the next.  With
+ * per-launch timing on they stay on one stream.  No counterpart in CP2K. */
+void grid_gb300_set_queue_streams(const grid_gb300_task_list *task_list, int n);
 /* C_ab <-> C_xyz change of basis of the coefficient and post kernels: 0 the
  * direct gather over all (a, b) pairs, 1 the staged per-direction
  * contractions (x, then y, then z), -1 (default) staged in the coefficient
