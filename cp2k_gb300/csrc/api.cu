@@ -371,6 +371,8 @@ struct TaskList {
   // the independent grid launches of a phase alternate over this many
   // streams, so that one launch's tail overlaps the next one's start
   int queue_streams = 2;
+  // integrate, orthorhombic, FP32 class, lp <= 6: the tensor-core kernel
+  int tc_integrate = 1;
   cudaStream_t aux_stream = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   int *d_error = nullptr;
@@ -1359,6 +1361,7 @@ static void grid_launch(TaskList *t, const Queue &q, int phase, int arith, const
   auto it = t->tuned.find(std::make_tuple(t->precision, phase, q.base));
   if (it != t->tuned.end())
     cfg = it->second;
+  cfg.tensor = t->tc_integrate;
   LaunchRecord rec;
   const bool timed = t->launch_timing && !t->capturing;
   if (timed) {
@@ -1735,7 +1738,8 @@ GB300_API void grid_gb300_create_task_list(
   // predictions, timings) belong to the old geometry and are dropped; the
   // learned schedule falls back to the size order until a model is applied.
   struct Kept {
-    int precision, schedule, coll_variant, transform_variant, copy_chunks, queue_streams;
+    int precision, schedule, coll_variant, transform_variant, copy_chunks, queue_streams,
+        tc_integrate;
     double mixed_threshold, model_bin;
     int small_extent[3];
     std::map<std::tuple<int, int, int>, LaunchCfg> tuned;
@@ -1745,7 +1749,7 @@ GB300_API void grid_gb300_create_task_list(
   if (*task_list) {
     const TaskList *o = TL(*task_list);
     kept.reset(new Kept{o->precision, o->schedule, o->coll_variant, o->transform_variant,
-                        o->copy_chunks, o->queue_streams, o->mixed_threshold,
+                        o->copy_chunks, o->queue_streams, o->tc_integrate, o->mixed_threshold,
                         o->model_bin, {o->small_extent[0], o->small_extent[1],
                                        o->small_extent[2]},
                         o->tuned, o->launch_timing, o->task_timing});
@@ -1765,6 +1769,7 @@ GB300_API void grid_gb300_create_task_list(
     t->transform_variant = kept->transform_variant;
     t->copy_chunks = kept->copy_chunks;
     t->queue_streams = kept->queue_streams;
+    t->tc_integrate = kept->tc_integrate;
     t->mixed_threshold = kept->mixed_threshold;
     t->model_bin = kept->model_bin;
     for (int i = 0; i < 3; i++)
@@ -2454,6 +2459,13 @@ GB300_API void grid_gb300_set_collocate_variant(const grid_gb300_task_list *task
   t->coll_variant = variant;
   t->tuned.clear();
   t->gen++;
+}
+
+GB300_API void grid_gb300_set_tensor_integrate(const grid_gb300_task_list *task_list,
+                                               int enable) {
+  TaskList *t = TL(task_list);
+  t->tc_integrate = enable ? 1 : 0;
+  t->gen++; // captured graphs hold the other kernel
 }
 
 GB300_API void grid_gb300_set_queue_streams(const grid_gb300_task_list *task_list, int n) {

@@ -285,6 +285,7 @@ struct LaunchCfg {
   int blocks = 0; // CTAs (automatic: all that fit on the GPU at once)
   int occupancy = 100; // automatic CTA count: this percentage of all that fit
   int variant = 0;     // collocate, orthorhombic: 0 row walk, 1 point list
+  int tensor = 0;      // integrate, orthorhombic, FP32, lp <= 6: tensor-core kernel
 };
 inline int cfg_blocks(const LaunchCfg &c, int persistent) {
   if (c.blocks > 0)

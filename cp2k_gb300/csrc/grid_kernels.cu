@@ -701,6 +701,248 @@ __global__ void __launch_bounds__(128, LPB <= 4 ? 5 : 1) integrate_ortho(GridArg
   }
 }
 
+// ------------------------------------------------------------------------
+// integrate, orthorhombic, FP32 class, on the tensor cores
+// ------------------------------------------------------------------------
+// The first contraction of the integrate is a dense matrix product per
+// task: T1[(k, j)][lx] = sum_x V(x, j, k) pol_x[lx](x) over the rows (k, j)
+// of the sphere (plane by plane) and the cube's x range, V zero outside the
+// sphere (the reference's point set, grid_ref_collint.h:144-151).  One warp
+// runs it as mma.sync m16n8k8 TF32 tiles (16 rows x 8 x per step, n = 8
+// covers lx <= 7), each operand split into a TF32 high and low part and
+// three products accumulated in FP32 (high*high + high*low + low*high), which
+// keeps about 21 bits of every product.  The rows are folded with
+// pol_y(j) pol_z(k) on the CUDA cores and reduced over the warp once per
+// task.
+template <int LPB> struct TcSmem {
+  static constexpr int PP = 8; // padded<LPB, float>() for LPB <= 7
+  static __host__ __device__ size_t bytes(int wmax) {
+    size_t b = sizeof(float) * 3 * (size_t)wmax * PP; // pol x, y, z
+    b += sizeof(float2) * (size_t)wmax * 8;          // pol_x split hi / lo
+    b += sizeof(int) * 3 * (size_t)wmax;             // periodic maps
+    b += sizeof(int) * ((size_t)wmax + 4);           // row starts of the planes
+    b += 64;
+    return (b + 15) & ~size_t(15);
+  }
+};
+
+__device__ __forceinline__ unsigned f2tf32(float x) {
+  unsigned r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void mma_tf32(float (&c)[4], const unsigned (&a)[4], unsigned b0,
+                                         unsigned b1) {
+  asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 "
+               "{%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};"
+               : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+               : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+template <int LPB>
+__global__ void __launch_bounds__(128) integrate_ortho_tc(GridArgs a, int wmax) {
+  static_assert(LPB <= 7, "one n8 tile holds lx <= 7");
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int P = LPB + 1;
+  constexpr int PP = TcSmem<LPB>::PP;
+  constexpr int NT = (P * (P + 1)) / 2; // (ly, lz) pairs with ly + lz <= LPB
+  const int lane = threadIdx.x & 31, grp = lane >> 2, tq = lane & 3;
+  unsigned char *ws = smem + (threadIdx.x >> 5) * TcSmem<LPB>::bytes(wmax);
+  float *pol = (float *)ws;
+  float2 *pxs = (float2 *)(pol + 3 * (size_t)wmax * PP);
+  int *map = (int *)(pxs + (size_t)wmax * 8);
+  int *starts = map + 3 * wmax;
+  double *out = (double *)a.coef_out;
+
+  for (;;) {
+    int qi = 0;
+    if (lane == 0)
+      qi = atomicAdd(a.counter, 1);
+    qi = __shfl_sync(FULL, qi, 0);
+    if (qi >= a.nqueue)
+      break;
+    const WorkItem w = work_item(a, qi);
+    const int t = w.t;
+    const long long t0 = clock64();
+    const TaskDesc d = a.tasks[t];
+    const LevelDesc &L = a.levels.lv[d.level];
+    const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
+    const CubeGeo cg = cube_geo(a.sph[d.sphere], a.sph_tab, lane);
+    const int k_lo = cg.lb2 + w.k0, k_hi = min(1 - cg.lb2, cg.lb2 + w.k0 + w.nk - 1);
+    if (cg.w > wmax || lp > LPB || k_hi - k_lo + 1 > wmax + 2) {
+      if (lane == 0)
+        atomicOr(a.error, 1);
+      continue;
+    }
+    fill_ortho_tables<float, LPB>(d, L, cg.cmax, lp, pol, map, lane, nullptr);
+    __syncwarp();
+    // pol_x split into TF32 high and low parts, lx >= P (or > lp) zero
+    for (int e = lane; e < cg.w * 8; e += 32) {
+      const int c = e >> 3, l = e & 7;
+      const float v = (l <= lp) ? pol[(size_t)c * PP + l] : 0.f;
+      const unsigned hi = f2tf32(v);
+      const unsigned lo = f2tf32(v - __uint_as_float(hi));
+      pxs[e] = make_float2(__uint_as_float(hi), __uint_as_float(lo));
+    }
+    // first row of every plane k_lo .. k_hi (rows j in [js, 1 - js])
+    const int np = k_hi - k_lo + 1;
+    if (lane == 0) {
+      int r = 0;
+      for (int p = 0; p < np; p++) {
+        const int k = k_lo + p, kk = k <= 0 ? -k : k - 1;
+        starts[p] = r;
+        r += 2 - 2 * cg.tab[kk];
+      }
+      starts[np] = r;
+    }
+    __syncwarp();
+    const int R = starts[np];
+    const float *grid = (const float *)a.grids_in[d.level];
+    const size_t nx = L.npts_local[0], nxy = nx * L.npts_local[1];
+    const int K = 1 - cg.lb2;
+    float acc[2][NT];
+#pragma unroll
+    for (int s2 = 0; s2 < 2; s2++)
+#pragma unroll
+      for (int e = 0; e < NT; e++)
+        acc[s2][e] = 0.f;
+    int pc = 0; // plane cursor (rows only grow)
+    for (int rb = 0; rb < R; rb += 16) {
+      // the two rows of this lane in the tile
+      int kr[2], jr[2], xs[2], xe[2];
+      size_t base[2];
+      bool rv[2];
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int r = rb + grp + 8 * h;
+        rv[h] = r < R;
+        kr[h] = k_lo;
+        jr[h] = 0;
+        xs[h] = 1;
+        xe[h] = 0;
+        base[h] = 0;
+        if (rv[h]) {
+          int p = pc;
+          while (starts[p + 1] <= r)
+            p++;
+          if (h == 0)
+            pc = p;
+          const int k = k_lo + p, kk = k <= 0 ? -k : k - 1;
+          const int js = cg.tab[kk];
+          const int j = js + (r - starts[p]), jj = j <= 0 ? -j : j - 1;
+          const int ist = cg.tab[2 * K + cg.tab[K + kk] + jj];
+          kr[h] = k;
+          jr[h] = j;
+          xs[h] = ist;
+          xe[h] = 1 - ist;
+          base[h] = (size_t)map[2 * cg.w + k + cg.cmax] * nxy +
+                    (size_t)map[cg.w + j + cg.cmax] * nx;
+        }
+      }
+      float c[4] = {0.f, 0.f, 0.f, 0.f};
+      // the row look-ups above diverge; mma.sync.aligned needs the whole warp
+      // converged
+      __syncwarp();
+      // x steps counted up front: written as a loop on xb <= x_hi, this
+      // kernel ran a single step under nvcc 13.0 (measured, lp <= 6 tasks of
+      // 12 and more x points)
+      const int nxs = (cg.x_hi - cg.x_lo + 8) >> 3;
+#pragma unroll 1
+      for (int xs8 = 0; xs8 < nxs; xs8++) {
+        const int xb = cg.x_lo + 8 * xs8;
+        float av[4];
+        float2 bv[2];
+#pragma unroll
+        for (int s2 = 0; s2 < 2; s2++) {
+          const int x = xb + tq + 4 * s2;
+          const bool xin = x <= cg.x_hi;
+          const int mx = xin ? map[x + cg.cmax] : 0;
+          bv[s2] = xin ? pxs[(x + cg.cmax) * 8 + grp] : make_float2(0.f, 0.f);
+#pragma unroll
+          for (int h = 0; h < 2; h++) {
+            const bool in = rv[h] && xin && x >= xs[h] && x <= xe[h];
+            av[h + 2 * s2] = in ? __ldg(grid + base[h] + mx) : 0.f;
+          }
+        }
+        unsigned ahi[4], alo[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          ahi[i] = f2tf32(av[i]);
+          alo[i] = f2tf32(av[i] - __uint_as_float(ahi[i]));
+        }
+        const unsigned b0h = __float_as_uint(bv[0].x), b1h = __float_as_uint(bv[1].x);
+        const unsigned b0l = __float_as_uint(bv[0].y), b1l = __float_as_uint(bv[1].y);
+        __syncwarp();
+        mma_tf32(c, alo, b0h, b1h);
+        mma_tf32(c, ahi, b0l, b1l);
+        mma_tf32(c, ahi, b0h, b1h);
+      }
+      // fold the rows: acc[s][(ly, lz)] += T1[row][lx = 2 tq + s] pol_y[ly](j) pol_z[lz](k)
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        if (!rv[h])
+          continue;
+        const float *py = pol + (size_t)(cg.w + jr[h] + cg.cmax) * PP;
+        const float *pz = pol + (size_t)(2 * cg.w + kr[h] + cg.cmax) * PP;
+#pragma unroll
+        for (int s2 = 0; s2 < 2; s2++) {
+          const int lx = 2 * tq + s2;
+          if (lx > lp)
+            continue;
+          const float v = c[2 * h + s2];
+          int e = 0;
+#pragma unroll
+          for (int ly = 0; ly < P; ly++) {
+            const float u = v * py[ly];
+#pragma unroll
+            for (int lz = 0; lz < P - ly; lz++, e++)
+              if (lx + ly + lz <= lp)
+                acc[s2][e] = fmaf(u, pz[lz], acc[s2][e]);
+          }
+        }
+      }
+    }
+    // sum over the 8 lanes that share tq (the row groups)
+    __syncwarp();
+#pragma unroll
+    for (int s2 = 0; s2 < 2; s2++)
+#pragma unroll
+      for (int e = 0; e < NT; e++) {
+        float v = acc[s2][e];
+        v += __shfl_xor_sync(FULL, v, 4);
+        v += __shfl_xor_sync(FULL, v, 8);
+        v += __shfl_xor_sync(FULL, v, 16);
+        acc[s2][e] = v;
+      }
+    if (grp == 0) {
+      double *dst = out + a.coef_off[t];
+#pragma unroll
+      for (int s2 = 0; s2 < 2; s2++) {
+        const int lx = 2 * tq + s2;
+        if (lx > lp)
+          continue;
+        int e = 0;
+#pragma unroll
+        for (int ly = 0; ly < P; ly++)
+#pragma unroll
+          for (int lz = 0; lz < P - ly; lz++, e++)
+            if (lx + ly + lz <= lp) {
+              const double v = f2d_exact(acc[s2][e]);
+              const int ci = cidx(lz, ly, lx, lp);
+              if (a.items) // plane ranges of one task add up (the buffer is zeroed)
+                atomicAdd(dst + ci, v);
+              else
+                dst[ci] = v;
+            }
+      }
+    }
+    if (a.task_cycles && lane == 0)
+      atomicAdd((unsigned long long *)&a.task_cycles[t], (unsigned long long)(clock64() - t0));
+    __syncwarp();
+  }
+}
+
 } // namespace
 
 // ------------------------------------------------------------------------
@@ -736,8 +978,30 @@ static void launch_ortho_t(const GridArgs &a, bool collocate, int wmax, LaunchCf
 }
 
 template <int LPB>
+static void launch_ortho_tc(const GridArgs &a, int wmax, LaunchCfg &cfg, cudaStream_t s) {
+  const size_t per_warp = TcSmem<LPB>::bytes(wmax);
+  int nw = warps_for(per_warp);
+  if (nw < 1)
+    return launch_error("orthorhombic grid kernel: cube too large for shared memory");
+  if (cfg.warps > 0 && cfg.warps < nw)
+    nw = cfg.warps;
+  const size_t smem = nw * per_warp;
+  const void *k = (const void *)integrate_ortho_tc<LPB>;
+  set_smem(k, smem);
+  const int nb = cfg.blocks > 0 ? cfg.blocks : cfg_blocks(cfg, persistent_blocks(k, 32 * nw, smem));
+  cfg.warps = nw;
+  cfg.blocks = nb;
+  integrate_ortho_tc<LPB><<<nb, 32 * nw, smem, s>>>(a, wmax);
+  count_launch();
+}
+
+template <int LPB>
 static void launch_ortho_lp(const GridArgs &a, int arith, bool collocate, int wmax,
                             LaunchCfg &cfg, cudaStream_t s) {
+  if constexpr (LPB <= 6) {
+    if (!collocate && arith == ARITH_FP32 && cfg.tensor)
+      return launch_ortho_tc<LPB>(a, wmax, cfg, s);
+  }
   if (arith == ARITH_FP64)
     launch_ortho_t<double, LPB>(a, collocate, wmax, cfg, s);
   else if (arith == ARITH_FP32)

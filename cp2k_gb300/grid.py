@@ -112,6 +112,7 @@ def lib():
         L.grid_gb300_set_transform_variant.argtypes = [vp, C.c_int]
         L.grid_gb300_set_copy_chunks.argtypes = [vp, C.c_int]
         L.grid_gb300_set_queue_streams.argtypes = [vp, C.c_int]
+        L.grid_gb300_set_tensor_integrate.argtypes = [vp, C.c_int]
         L.grid_gb300_tuned_split.argtypes = [vp]
         L.grid_gb300_tuned_split.restype = C.c_int
         L.grid_gb300_set_launch_timing.argtypes = [vp, C.c_int]
@@ -435,6 +436,11 @@ class GridTaskList:
         coefficient kernel only
         (grid_gb300_set_transform_variant)."""
         lib().grid_gb300_set_transform_variant(self.impl, int(variant))
+
+    def set_tensor_integrate(self, enable: bool):
+        """FP32-class orthorhombic integration on the tensor cores
+        (grid_gb300_set_tensor_integrate)."""
+        lib().grid_gb300_set_tensor_integrate(self.impl, int(bool(enable)))
 
     def set_queue_streams(self, n: int):
         """Streams the grid launches of a phase alternate over (1 or 2;

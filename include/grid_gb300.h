@@ -350,6 +350,13 @@ void grid_gb300_set_copy_chunks(const grid_gb300_task_list *task_list, int chunk
  * it, so that the tail of one launch overlaps the start of the next.  With
  * per-launch timing on they stay on one stream.  No counterpart in CP2K. */
 void grid_gb300_set_queue_streams(const grid_gb300_task_list *task_list, int n);
+/* Integration of the FP32 class (mixed mode) and of FP32 mode, orthorhombic
+ * tasks with lp <= 6: 1 (default) runs the first contraction, over the x
+ * points of each row of the sphere, as TF32 tensor-core matrix products
+ * (mma.sync m16n8k8, operands split into high and low TF32 parts, three
+ * products, about 21 bits per product); 0 runs the CUDA-core kernel.  No
+ * counterpart in CP2K. */
+void grid_gb300_set_tensor_integrate(const grid_gb300_task_list *task_list, int enable);
 /* C_ab <-> C_xyz change of basis of the coefficient and post kernels: 0 the
  * direct gather over all (a, b) pairs, 1 the staged per-direction
  * contractions (x, then y, then z), -1 (default) staged in the coefficient

@@ -451,3 +451,35 @@ def test_copy_chunks_agree(G, O, api):
         assert rel_diff(f, f_ref) < TOL_DERIV
         assert rel_diff(v, v_ref) < TOL_DERIV
     tl.close()
+
+
+@pytest.mark.parametrize("name,scale", [("c2_512atoms", 0.1), ("c1_64atoms", 0.3)])
+def test_tensor_core_integrate(G, O, name, scale):
+    """The FP32 class's orthorhombic integration on the tensor cores (TF32
+    products, each operand split in two, three products) against the CUDA-core
+    kernel and the oracle: mixed mode within its stated bounds (hab 1e-6,
+    forces 1e-5, relative to max(1, |ref|)), plain FP32 within 1e-5 of the
+    maximum, the two kernels within 2e-6 of each other."""
+    from cp2k_gb300 import workload as W
+    inp = W.config(name, scale=scale, seed=39)
+    pab = W.density_blocks(inp)
+    V = W.potential_grids(inp)
+    ot = O.OracleTaskList(inp)
+    h_ref, f_ref, _ = ot.integrate(V, pab, forces=True)
+    h_only_ref, _, _ = ot.integrate(V)
+    ot.close()
+    for prec in (G.MIXED, G.FP32):
+        tl = G.GridTaskList(inp, precision=prec)
+        res = {}
+        for tc in (0, 1):
+            tl.set_tensor_integrate(tc)
+            res[tc] = (tl.integrate(V)[0],) + tl.integrate(V, pab, forces=True)[:2]
+        hmax = float(np.abs(h_only_ref).max())
+        assert float(np.abs(res[1][0] - res[0][0]).max()) / hmax < 2e-6
+        if prec == G.MIXED:
+            assert rel_diff(res[1][0], h_only_ref) < 1e-6
+            assert rel_diff(res[1][1], h_ref) < 1e-6
+            assert rel_diff(res[1][2], f_ref) < 1e-5
+        else:
+            assert float(np.abs(res[1][0] - h_only_ref).max()) / hmax < 1e-5
+        tl.close()
