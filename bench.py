@@ -435,7 +435,9 @@ def gpu_arm(args, world, rank, local):
     if model is not None:
         with torch.cuda.stream(stream):
             model.apply(tl, stream=stream)
-    sched_mixed = G.SCHEDULE_MODEL if model is not None else G.SCHEDULE_SIZE
+    # the size schedule is the default; the learned model's order is timed
+    # beside it as a diagnostic (it gains within the run-to-run noise)
+    sched_mixed = G.SCHEDULE_SIZE
     # autotuned size split and launch shapes, per precision, on this workload
     tuned = {}
     for prec, sched in ((G.MIXED, sched_mixed), (G.FP64, G.SCHEDULE_SIZE),
@@ -481,7 +483,8 @@ def gpu_arm(args, world, rank, local):
 
     # warm-up all paths, then the timed regions
     run_steps(G.MIXED, sched_mixed, args.warmup)
-    run_steps(G.MIXED, G.SCHEDULE_SIZE, max(1, min(args.warmup, 2)))
+    if model is not None:
+        run_steps(G.MIXED, G.SCHEDULE_MODEL, max(1, min(args.warmup, 2)))
     run_steps(G.FP64, G.SCHEDULE_SIZE, max(1, min(args.warmup, 2)))
     run_steps(G.FP32, sched_mixed, max(1, min(args.warmup, 2)))
     barrier(world)
@@ -510,11 +513,18 @@ def gpu_arm(args, world, rank, local):
         t_graph.append(e[0].elapsed_time(e[1]))
     graph_kernels = graph.kernels
     graph.free()
-    t_size = run_steps(G.MIXED, G.SCHEDULE_SIZE, max(1, min(args.steps, 5)))
+    t_model = (run_steps(G.MIXED, G.SCHEDULE_MODEL, max(1, min(args.steps, 5)))
+               if model is not None else None)
     # the queue launches of each phase on one stream (no tail overlap)
     tl.set_queue_streams(1)
     t_one_stream = run_steps(G.MIXED, sched_mixed, max(1, min(args.steps, 5)))
     tl.set_queue_streams(2)
+    # every double-float task whole (no FP32 outer rows)
+    tl.set_row_split(False)
+    run_steps(G.MIXED, sched_mixed, 1)
+    t_no_row_split = run_steps(G.MIXED, sched_mixed, max(1, min(args.steps, 5)))
+    tl.set_row_split(True)
+    row_split_share = tl.row_split_stats() + (tl.mixed_split()[1],)
     t_fp64 = run_steps(G.FP64, G.SCHEDULE_SIZE, max(1, min(args.steps, 3)))
     rho64 = [g.cpu().numpy() for g in grids]
     hab64 = hab.cpu().numpy()
@@ -523,7 +533,7 @@ def gpu_arm(args, world, rank, local):
     hab32 = hab.cpu().numpy()
 
     ms_mixed = max_over_ranks(float(np.mean(t_mixed)), world)
-    ms_size = max_over_ranks(float(np.mean(t_size)), world)
+    ms_model = max_over_ranks(float(np.mean(t_model)), world) if t_model else None
     ms_fp64 = max_over_ranks(float(np.mean(t_fp64)), world)
     ms_fp32 = max_over_ranks(float(np.mean(t_fp32)), world)
 
@@ -593,17 +603,22 @@ def gpu_arm(args, world, rank, local):
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 pairs (double-float) bulk / f64 accumulate", "data": "synthetic",
             "config": {**CONFIG, "ntasks": inp.ntasks, "parallelism": f"replicas x{world}",
-                       "schedule": "learned cost model" if model is not None else "size",
-                       "cost_model": model_path},
+                       "schedule": "size (longest first)"},
             "fp64_ms_per_step": ms_fp64, "speedup_vs_fp64": ms_fp64 / ms_mixed,
-            "mixed_size_schedule_ms_per_step": ms_size,
+            "mixed_model_schedule_ms_per_step": ms_model,
+            "cost_model": {"params": model_path, "use": "diagnostic; the size schedule is the default"},
             "mixed_one_queue_stream_ms_per_step": max_over_ranks(float(np.mean(t_one_stream)),
                                                                  world),
+            "mixed_no_row_split_ms_per_step": max_over_ranks(float(np.mean(t_no_row_split)),
+                                                             world),
+            "row_split": {"tasks_split": row_split_share[0],
+                          "fp32_share_of_points": row_split_share[1],
+                          "fp32_class_share_of_points": row_split_share[2]},
             "mixed_cuda_graph_ms_per_step": max_over_ranks(float(np.mean(t_graph)), world),
             "cuda_graph_kernels": int(graph_kernels),
             "autotune": {{0: "fp64", 1: "mixed", 2: "fp32"}[p]: {"grid_ms": v[0], "size_split": v[1]}
                          for p, v in tuned.items()},
-            "cost_model_gain": ms_size / ms_mixed - 1.0,
+            "cost_model_gain": (ms_mixed / ms_model - 1.0) if ms_model else None,
             "fp32_ms_per_step": ms_fp32, "fp32_speedup_vs_fp64": ms_fp64 / ms_fp32,
             "errors_mixed_vs_oracle": err_oracle.get("mixed"),
             "errors_fp64_vs_oracle": err_oracle.get("fp64"),

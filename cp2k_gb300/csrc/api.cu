@@ -271,6 +271,7 @@ struct Queue {
   int extent = 0; // ortho: max cube width; general: max j-range
   int general = 0, bucket = 0;
   int fp32 = 0; // mixed path: this queue runs in plain FP32
+  int side = 0; // row split: 0 whole tasks, 1 rows inside the cylinder, 2 rows outside
   int key = 0;          // (general, bucket, FP32 class, size class)
   int base = 0;         // key of the tuned launch shapes
   long long points = 0; // grid points the queue's tasks visit
@@ -303,6 +304,11 @@ struct Mode { // everything that depends on the l shifts of a call
   int coef_words = 0;      // per-warp shared memory words of coefficient/post
   int transform = -1;      // transform variant the words were sized for
   int sched_version = -1;
+  // mixed mode row split: per task squared cylinder radius (kCoreAll: whole
+  // task in its class), on the device for the kernels
+  std::vector<float> core_r2;
+  float *d_core_r2 = nullptr;
+  bool row_split = false; // some task runs split
 };
 
 struct TaskList {
@@ -373,6 +379,8 @@ struct TaskList {
   int queue_streams = 2;
   // integrate, orthorhombic, FP32 class, lp <= 6: the tensor-core kernel
   int tc_integrate = 1;
+  // mixed mode: the outer rows of orthorhombic double-float tasks in FP32
+  int row_split = 1;
   cudaStream_t aux_stream = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   int *d_error = nullptr;
@@ -650,6 +658,104 @@ static double contribution_bound(const TaskDesc &d, const double *ra) {
             }
       }
   return g * d.prefexp * ((d.iatom == d.jatom) ? 1.0 : 2.0);
+}
+
+// Row split of a double-float task (mixed mode, orthorhombic cubes).  A row
+// (j, k) of the cube at distance rho = sqrt(y^2 + z^2) from the Gaussian
+// product's x axis holds contributions of at most
+//   f(rho) = prefactor sum_(a,b) B_x[a_x][b_x] sum_n C_n rho^n exp(-zetp rho^2)
+// for |P_ab| <= 1: B_x is contribution_bound's x factor (maximum over x) and
+// C_n collects the products of the y and z binomial expansions, with
+// |y|^p |z|^q <= rho^(p+q).  Past rho0 = sqrt(nmax / (2 zetp)) every term
+// decreases, so the rows with rho >= rc, f(rc) <= tau, obey the FP32 class's
+// bound and run in FP32; the rows inside stay double-float.  Returns rc^2
+// (bohr^2) and the share of the sphere's points outside, or kCoreAll when
+// that share is under a half (the second pass over the task repeats its
+// table set-up and plane folds; measured on the 512-atom workload, shares
+// from a tenth up split nearly the same tasks and time the same).
+// The outside rows obey the bound tau / kShellMargin rather than tau: their
+// FP32 rounding errors are correlated within a task (one set of rounded
+// coefficients and table values), unlike those of many small FP32-class
+// tasks.  Measured on the 512-atom workload (mixed step, Tr(V rho) error per
+// atom against FP64): margin 1 gives 7.0e-10 Ha, 3 gives 2.8e-10, 10 gives
+// 6.6e-11, and keeping every task whole 1.1e-10; the step takes 20.5, 20.9,
+// 21.4 and 22.3 ms.
+constexpr double kShellMargin = 3.0;
+
+static float core_radius2(const TaskDesc &d, double tau, double *outside) {
+  *outside = 0.0;
+  const int la = d.la_max, lb = d.lb_max, nn = la + lb + 1;
+  double bin[GB300_LMAX + 1][GB300_LMAX + 1] = {};
+  for (int n = 0; n <= GB300_LMAX; n++) {
+    bin[n][0] = 1.0;
+    for (int k = 1; k <= n; k++)
+      bin[n][k] = bin[n - 1][k - 1] + (k <= n - 1 ? bin[n - 1][k] : 0.0);
+  }
+  double m[2 * GB300_LMAX + 2];
+  for (int n = 0; n < nn; n++)
+    m[n] = n == 0 ? 1.0 : pow(n / (2.0 * M_E * d.zetp), 0.5 * n);
+  // |binomial expansion| of (x - A)^xa (x - B)^xb about P, per direction
+  static thread_local double al[3][GB300_LMAX + 1][GB300_LMAX + 1][2 * GB300_LMAX + 2];
+  for (int dir = 0; dir < 3; dir++) {
+    const double pa = d.zetb / d.zetp * d.rab[dir], pb = pa - d.rab[dir];
+    for (int xa = 0; xa <= la; xa++)
+      for (int xb = 0; xb <= lb; xb++) {
+        double *c = al[dir][xa][xb];
+        for (int n = 0; n < nn; n++)
+          c[n] = 0.0;
+        for (int k = 0; k <= xa; k++)
+          for (int q = 0; q <= xb; q++)
+            c[xa - k + xb - q] += bin[xa][k] * pow(pa, k) * bin[xb][q] * pow(pb, q);
+        for (int n = 0; n < nn; n++)
+          c[n] = fabs(c[n]);
+      }
+  }
+  double C[4 * GB300_LMAX + 2] = {};
+  for (int l1 = d.la_min; l1 <= la; l1++)
+    for (int ax = 0; ax <= l1; ax++)
+      for (int ay = 0; ay <= l1 - ax; ay++) {
+        const int az = l1 - ax - ay;
+        for (int l2 = d.lb_min; l2 <= lb; l2++)
+          for (int bx = 0; bx <= l2; bx++)
+            for (int by = 0; by <= l2 - bx; by++) {
+              const int bz = l2 - bx - by;
+              double Bx = 0.0;
+              for (int n = 0; n <= ax + bx; n++)
+                Bx += al[0][ax][bx][n] * m[n];
+              const double *cy = al[1][ay][by], *cz = al[2][az][bz];
+              for (int p = 0; p <= ay + by; p++)
+                for (int q = 0; q <= az + bz; q++)
+                  C[p + q] += Bx * cy[p] * cz[q];
+            }
+      }
+  int nmax = 0;
+  for (int n = 0; n < 2 * nn; n++)
+    if (C[n] > 0.0)
+      nmax = n;
+  const double pref = d.prefexp * ((d.iatom == d.jatom) ? 1.0 : 2.0);
+  auto f = [&](double r) {
+    double poly = 0.0;
+    for (int n = nmax; n >= 0; n--)
+      poly = poly * r + C[n];
+    return pref * poly * exp(-d.zetp * r * r);
+  };
+  const double R = d.radius, r0 = sqrt(nmax / (2.0 * d.zetp));
+  if (r0 >= R || f(R) > tau)
+    return kCoreAll;
+  double lo = r0, hi = R;
+  if (f(r0) > tau) {
+    for (int it = 0; it < 40; it++) {
+      const double mid = 0.5 * (lo + hi);
+      (f(mid) > tau ? lo : hi) = mid;
+    }
+  } else {
+    hi = r0;
+  }
+  const double share = pow(std::max(0.0, 1.0 - hi * hi / (R * R)), 1.5);
+  if (share < 0.5)
+    return kCoreAll;
+  *outside = share;
+  return nextafterf((float)(hi * hi), kCoreAll);
 }
 
 template <typename T> static T *dalloc_copy(const std::vector<T> &v) {
@@ -1152,7 +1258,27 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase, int nch = 1) {
     m.coef_words = words;
     m.transform = t->transform_variant;
   }
-  // work queues: (general, lp bucket, FP32 class, size class), descending cost
+  // row split (mixed mode, orthorhombic double-float tasks): the radius of
+  // the double-float core per task, with the class test's derivative factor
+  const bool split_rows = t->precision == GRID_GB300_MIXED && t->row_split;
+  m.core_r2.assign(t->ntasks, kCoreAll);
+  std::vector<double> outside(t->ntasks, 0.0);
+  if (split_rows)
+    parallel_for(t->ntasks, [&](int s) {
+      const TaskDesc &k = t->tasks[s];
+      if ((k.flags & (TF_SKIP | TF_GENERAL)) != 0)
+        return;
+      double fac = 1.0;
+      if (dshift > 0)
+        fac = pow(2.0 * std::max(k.zeta, k.zetb) + std::max(k.la_max, k.lb_max) + 1.0, dshift);
+      if (t->gbound[s] * fac <= t->mixed_threshold)
+        return; // FP32 class already
+      m.core_r2[s] = core_radius2(k, t->mixed_threshold / (fac * kShellMargin), &outside[s]);
+    });
+  m.row_split = false;
+  // work queues: (general, lp bucket, FP32 class, size class), descending
+  // cost; the outside rows of split tasks in shell queues keyed from
+  // kQueueKeys on
   std::map<int, std::vector<std::pair<double, int>>> items;
   std::vector<char> task_cls(t->ntasks, -1); // FP32 class, -1: skipped
   for (int s = 0; s < t->ntasks; s++) {
@@ -1183,8 +1309,19 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase, int nch = 1) {
     } else
       cost = (double)t->points[s] * (lp + 1) + 64.0 * (lp + 1) * (lp + 2);
     task_cls[s] = (char)cls;
-    items[((g * kNumBuckets + b) * 2 + cls) * 2 + sz].push_back({cost, s});
+    const int key = ((g * kNumBuckets + b) * 2 + cls) * 2 + sz;
+    if (m.core_r2[s] < kCoreAll) {
+      const double out = outside[s];
+      items[key].push_back({cost * (1.0 - out), s});
+      items[kQueueKeys + key + 2].push_back({cost * out, s}); // FP32 class bit set
+      m.row_split = true;
+    } else {
+      items[key].push_back({cost, s});
+    }
   }
+  if (m.d_core_r2)
+    cudaFree(m.d_core_r2);
+  m.d_core_r2 = m.row_split ? dalloc_copy(m.core_r2) : nullptr;
   for (auto &q : m.queues) {
     if (q.d_idx)
       cudaFree(q.d_idx);
@@ -1233,18 +1370,25 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase, int nch = 1) {
     });
     Queue q;
     q.key = key;
-    q.base = key % kQueueKeys;
-    q.general = q.base / (2 * 2 * kNumBuckets);
-    q.bucket = (q.base / 4) % kNumBuckets;
-    q.fp32 = (q.base >> 1) & 1;
+    q.base = key; // shell queues tune apart from the FP32 class's
+    const int kb = key % kQueueKeys;
+    q.general = kb / (2 * 2 * kNumBuckets);
+    q.bucket = (kb / 4) % kNumBuckets;
+    q.fp32 = (kb >> 1) & 1;
     std::vector<int> idx(v.size());
     int ext = 1;
     for (size_t i = 0; i < v.size(); i++) {
       idx[i] = v[i].second;
       const TaskDesc &k = t->tasks[idx[i]];
       const int lpk = k.la_max + d.la_max + k.lb_max + d.lb_max;
-      q.points += t->points[idx[i]];
-      q.flops += 2.0 * (lpk + 1) * (double)t->points[idx[i]];
+      long long pts = t->points[idx[i]]; // of the task's points in this queue
+      if (m.core_r2[idx[i]] < kCoreAll) { // estimated split, the two parts adding up
+        q.side = key >= kQueueKeys ? 2 : 1;
+        const long long in = llround((1.0 - outside[idx[i]]) * (double)pts);
+        pts = key >= kQueueKeys ? pts - in : in;
+      }
+      q.points += pts;
+      q.flops += 2.0 * (lpk + 1) * (double)pts;
       if (q.general == 0)
         ext = std::max(ext, 2 * t->sph[k.sphere].cmax + 2);
       else {
@@ -1362,6 +1506,8 @@ static void grid_launch(TaskList *t, const Queue &q, int phase, int arith, const
   if (it != t->tuned.end())
     cfg = it->second;
   cfg.tensor = t->tc_integrate;
+  if (q.side != 0) // a split task's rows are ranges of the point lists
+    cfg.variant = 1;
   LaunchRecord rec;
   const bool timed = t->launch_timing && !t->capturing;
   if (timed) {
@@ -1530,6 +1676,8 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
       // one launch per work queue, each in the working type of its class: the
       // kernels stay small (instruction cache) and need no per-task branch
       for (const Queue &q : m.queues) {
+        if (q.side == 2) // the core queue computes a split task's coefficients
+          continue;
         co.order = q.d_idx;
         co.norder = q.n;
         launch_coefficients_mixed(co, q.fp32 ? (int)ARITH_FP32 : (int)ARITH_MIXED, m.coef_words,
@@ -1551,10 +1699,15 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
       if (qi >= kMaxQueues)
         fail("more than %d work queues in one call", kMaxQueues);
       ga.counter = t->d_counters + qi++;
+      // FP32 queues read the high words of the coefficient slots (shell
+      // queues: of the split tasks' double-float coefficients)
       ga.coef_stride = q.fp32 ? 2 : 1;
+      ga.core_side = q.side;
+      ga.core_r2 = q.side ? m.d_core_r2 : nullptr;
       grid_launch(t, q, 0, q.fp32 ? (int)ARITH_FP32 : arith, ga, queue_stream(t, s, qi));
-      grid_library_counter_add(kBucketLp[q.bucket], GRID_BACKEND_GB300,
-                               q.general ? GRID_COLLOCATE_GENERAL : GRID_COLLOCATE_ORTHO, q.n);
+      if (q.side != 2)
+        grid_library_counter_add(kBucketLp[q.bucket], GRID_BACKEND_GB300,
+                                 q.general ? GRID_COLLOCATE_GENERAL : GRID_COLLOCATE_ORTHO, q.n);
     }
   }
   join_queues(t, s);
@@ -1608,7 +1761,7 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
   }
   CK(cudaMemsetAsync(t->d_counters, 0, sizeof(int) * kMaxQueues, s));
   // split general tasks add their planes' partial coefficients
-  bool any_split = false;
+  bool any_split = m.row_split; // split tasks: both sides add their coefficients
   for (const Queue &q : m.queues)
     any_split |= q.d_items != nullptr;
   if (any_split)
@@ -1652,6 +1805,9 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
         fail("more than %d work queues in one call", kMaxQueues);
       ga.counter = t->d_counters + qi++;
       ga.grid_stride = 1;
+      ga.core_side = q.side;
+      ga.core_r2 = q.side ? m.d_core_r2 : nullptr;
+      ga.accum = q.side != 0;
       // FP64: the grid; mixed: float2 pairs for the double-float class, dense
       // high words for the FP32 class
       for (int l = 0; l < t->nlevels; l++)
@@ -1659,8 +1815,9 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
                          : (arith == ARITH_MIXED && q.fp32) ? (const void *)t->d_gridhi[l]
                                                             : (const void *)t->d_gridsplit[l];
       grid_launch(t, q, 1, q.fp32 ? (int)ARITH_FP32 : arith, ga, queue_stream(t, s, qi));
-      grid_library_counter_add(kBucketLp[q.bucket], GRID_BACKEND_GB300,
-                               q.general ? GRID_INTEGRATE_GENERAL : GRID_INTEGRATE_ORTHO, q.n);
+      if (q.side != 2)
+        grid_library_counter_add(kBucketLp[q.bucket], GRID_BACKEND_GB300,
+                                 q.general ? GRID_INTEGRATE_GENERAL : GRID_INTEGRATE_ORTHO, q.n);
     }
   }
   join_queues(t, s);
@@ -1682,6 +1839,8 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
       }
     } else if (arith == ARITH_MIXED) {
       for (const Queue &q : m.queues) {
+        if (q.side == 2) // posted with the task's core queue
+          continue;
         pa.order = q.d_idx;
         pa.norder = q.n;
         launch_post_mixed(pa, q.fp32 ? (int)ARITH_FP32 : (int)ARITH_MIXED, m.coef_words, s);
@@ -1739,7 +1898,7 @@ GB300_API void grid_gb300_create_task_list(
   // learned schedule falls back to the size order until a model is applied.
   struct Kept {
     int precision, schedule, coll_variant, transform_variant, copy_chunks, queue_streams,
-        tc_integrate;
+        tc_integrate, row_split;
     double mixed_threshold, model_bin;
     int small_extent[3];
     std::map<std::tuple<int, int, int>, LaunchCfg> tuned;
@@ -1749,7 +1908,8 @@ GB300_API void grid_gb300_create_task_list(
   if (*task_list) {
     const TaskList *o = TL(*task_list);
     kept.reset(new Kept{o->precision, o->schedule, o->coll_variant, o->transform_variant,
-                        o->copy_chunks, o->queue_streams, o->tc_integrate, o->mixed_threshold,
+                        o->copy_chunks, o->queue_streams, o->tc_integrate, o->row_split,
+                        o->mixed_threshold,
                         o->model_bin, {o->small_extent[0], o->small_extent[1],
                                        o->small_extent[2]},
                         o->tuned, o->launch_timing, o->task_timing});
@@ -1770,6 +1930,7 @@ GB300_API void grid_gb300_create_task_list(
     t->copy_chunks = kept->copy_chunks;
     t->queue_streams = kept->queue_streams;
     t->tc_integrate = kept->tc_integrate;
+    t->row_split = kept->row_split;
     t->mixed_threshold = kept->mixed_threshold;
     t->model_bin = kept->model_bin;
     for (int i = 0; i < 3; i++)
@@ -2217,6 +2378,43 @@ GB300_API void grid_gb300_mixed_split(const grid_gb300_task_list *task_list, dou
     *frac_points = pt ? pf / pt : 0.0;
 }
 
+GB300_API void grid_gb300_row_split_stats(const grid_gb300_task_list *task_list,
+                                          double *frac_tasks_split, double *frac_points_fp32) {
+  const TaskList *t = TL(task_list);
+  std::vector<double> out(t->tasks.size(), 0.0);
+  std::vector<char> cls(t->tasks.size(), -1);
+  parallel_for((int)t->tasks.size(), [&](int s) {
+    const TaskDesc &k = t->tasks[s];
+    if (k.flags & TF_SKIP)
+      return;
+    if (t->gbound[s] <= t->mixed_threshold) {
+      cls[s] = 1;
+      return;
+    }
+    cls[s] = 0;
+    if (t->row_split && !(k.flags & TF_GENERAL) &&
+        core_radius2(k, t->mixed_threshold / kShellMargin, &out[s]) >= kCoreAll)
+      out[s] = 0.0;
+  });
+  double nt = 0, ns = 0, pt = 0, pf = 0;
+  for (size_t s = 0; s < t->tasks.size(); s++) {
+    if (cls[s] < 0)
+      continue;
+    nt += 1;
+    pt += (double)t->points[s];
+    if (cls[s] == 1)
+      pf += (double)t->points[s];
+    else if (out[s] > 0.0) {
+      ns += 1;
+      pf += out[s] * (double)t->points[s];
+    }
+  }
+  if (frac_tasks_split)
+    *frac_tasks_split = nt ? ns / nt : 0.0;
+  if (frac_points_fp32)
+    *frac_points_fp32 = pt ? pf / pt : 0.0;
+}
+
 GB300_API void grid_gb300_set_schedule(const grid_gb300_task_list *task_list, int schedule) {
   if (schedule < GRID_GB300_SCHEDULE_SIZE || schedule > GRID_GB300_SCHEDULE_INPUT)
     fail("unknown schedule %d", schedule);
@@ -2466,6 +2664,12 @@ GB300_API void grid_gb300_set_tensor_integrate(const grid_gb300_task_list *task_
   TaskList *t = TL(task_list);
   t->tc_integrate = enable ? 1 : 0;
   t->gen++; // captured graphs hold the other kernel
+}
+
+GB300_API void grid_gb300_set_row_split(const grid_gb300_task_list *task_list, int enable) {
+  TaskList *t = TL(task_list);
+  t->row_split = enable ? 1 : 0;
+  t->sched_version++; // the work queues change
 }
 
 GB300_API void grid_gb300_set_queue_streams(const grid_gb300_task_list *task_list, int n) {

@@ -185,7 +185,42 @@ struct GridArgs {
   const float2 *seeds;    // mixed path: per task [3][6] dfloat recurrence seeds
   long long *task_cycles; // optional per-task timings (clock64)
   int *error;             // device error word
+  // mixed mode, orthorhombic tasks split by rows: per task the squared radius
+  // (bohr^2) of the cylinder around the Gaussian's x axis whose rows (j, k)
+  // run in double-float; the rows outside run in FP32 in a shell queue.
+  // kCoreAll: every row is inside; negative: none is.  Null with core_side 0.
+  const float *core_r2;
+  int core_side; // 0: every row of the task; 1: rows inside; 2: rows outside
+  int accum;     // integrate: add into the (zeroed) coefficient buffer
 };
+
+constexpr float kCoreAll = 3.0e38f;
+
+#ifdef __CUDACC__
+// Rows j of cube plane k inside the cylinder y^2 + z^2 <= r2 around the
+// Gaussian product's x axis (y = j dh_y - roff_y, z = k dh_z - roff_z):
+// [lo, hi], empty when lo > hi.  Every kernel that runs one side of a split
+// task calls this function; it uses round-to-nearest FP32 operations only
+// (no contraction), so the double-float and the FP32 side agree on every row.
+__device__ __forceinline__ void core_rows(float r2, const TaskDesc &d, const LevelDesc &L, int k,
+                                          int &lo, int &hi) {
+  if (r2 >= kCoreAll) {
+    lo = -(1 << 20);
+    hi = 1 << 20;
+    return;
+  }
+  const float z = __fsub_rn(__fmul_rn((float)k, (float)L.dh[8]), (float)d.roff[2]);
+  const float rem = __fsub_rn(r2, __fmul_rn(z, z));
+  if (!(rem >= 0.f)) {
+    lo = 1;
+    hi = 0;
+    return;
+  }
+  const float s = __fsqrt_rn(rem), ry = (float)d.roff[1], iy = (float)L.dh_inv[4];
+  lo = (int)ceilf(__fmul_rn(__fsub_rn(ry, s), iy));
+  hi = (int)floorf(__fmul_rn(__fadd_rn(ry, s), iy));
+}
+#endif
 
 struct PostArgs {
   const TaskDesc *tasks;

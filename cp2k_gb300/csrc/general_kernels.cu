@@ -561,7 +561,7 @@ __global__ void __launch_bounds__(128) integrate_general(GridArgs a, int njmax) 
     __syncwarp();
     double *dst = out + a.coef_off[t];
     for (int e = lane; e < nco; e += 32) {
-      if (a.items) // plane ranges of one task add up (the buffer is zeroed)
+      if (a.items || a.accum) // parts of one task add up (the buffer is zeroed)
         atomicAdd(dst + e, acc[e]);
       else
         dst[e] = acc[e];
@@ -911,7 +911,7 @@ __global__ void __launch_bounds__(128) integrate_general_df(GridArgs a, int njma
     __syncwarp();
     double *dst = out + a.coef_off[t];
     for (int e = lane; e < nco; e += 32) {
-      if (a.items) // plane ranges of one task add up (the buffer is zeroed)
+      if (a.items || a.accum) // parts of one task add up (the buffer is zeroed)
         atomicAdd(dst + e, acc[e]);
       else
         dst[e] = acc[e];

@@ -81,6 +81,49 @@ __device__ __forceinline__ void load_row(const T *src, T (&dst)[PP]) {
     d[i] = s[i];
 }
 
+// The 1-D tables from the Gaussian along each line by the multiplicative
+// recurrence of grid_ref_collint.h:262-293, run in dfloat by 6 lanes (3
+// directions x 2 sides of c = 0) from exponentials the host evaluated in FP64:
+// seed[dir] = {e(0), f_up(0), f_down(0), q, h, -roff} with
+// e(c) = exp(-z (c h - r)^2), e(c +- 1) = e(c) f(c), f(c +- 1) = f(c) q.
+// Stored as dfloat, or (T = float) rounded to FP32: an FP32 table whose
+// relative error does not grow with the exponent z x^2, unlike expf of a
+// rounded argument.
+template <typename T, int LPB, int PP>
+__device__ __forceinline__ void seeded_tables(int w, int cmax, int lp, T *pol, int lane,
+                                              const float2 *seed) {
+  if (lane < 6) {
+    const int dir = lane >> 1, up = lane & 1;
+    const float2 *sd = seed + 6 * dir;
+    dfloat ec = dfloat{sd[0].x, sd[0].y};
+    dfloat f = up ? dfloat{sd[1].x, sd[1].y} : dfloat{sd[2].x, sd[2].y};
+    const dfloat q = dfloat{sd[3].x, sd[3].y};
+    const dfloat hd = dfloat{sd[4].x, sd[4].y}, rd = dfloat{sd[5].x, sd[5].y};
+    const int cend = up ? cmax + 1 : -cmax;
+    for (int cc = 0;; cc += up ? 1 : -1) {
+      if (up || cc != 0) { // c = 0 is written by the up-going lane
+        const dfloat x = df_fma1(rd, hd, (float)cc);
+        dfloat v = ec;
+        T *p = pol + (size_t)(dir * w + cc + cmax) * PP;
+#pragma unroll
+        for (int l = 0; l <= LPB; l++) {
+          if (l > lp)
+            break;
+          if constexpr (std::is_same<T, float>::value)
+            p[l] = v.h;
+          else
+            p[l] = v;
+          v = df_mul(v, x);
+        }
+      }
+      if (cc == cend)
+        break;
+      ec = df_mul(ec, f);
+      f = df_mul(f, q);
+    }
+  }
+}
+
 // 1-D factors pol[dir][c][l] = x_c^l exp(-zetp x_c^2), x_c = c*h - roff,
 // c in [-cmax, cmax+1]; and the periodic maps map[dir][c]
 // (grid_ref_collint.h:259-304).
@@ -112,6 +155,10 @@ __device__ __forceinline__ void fill_ortho_tables(const TaskDesc &d, const Level
       }
     }
   } else if constexpr (std::is_same<T, float>::value) {
+    if (seed) { // rounded from the double-float recurrence below
+      seeded_tables<T, LPB, PP>(w, cmax, lp, pol, lane, seed);
+      return;
+    }
     for (int e = lane; e < 3 * w; e += 32) {
       const int dir = e / w, c = e - dir * w, cc = c - cmax;
       const float x = fmaf((float)cc, (float)L.dh[dir * 4], -(float)d.roff[dir]);
@@ -126,39 +173,19 @@ __device__ __forceinline__ void fill_ortho_tables(const TaskDesc &d, const Level
       }
     }
   } else {
-    // dfloat: the Gaussian along each line by the multiplicative recurrence
-    // of grid_ref_collint.h:262-293, run in dfloat by 6 lanes (3 directions
-    // x 2 sides of c = 0) from exponentials the host evaluated in FP64:
-    // seed[dir] = {e(0), f_up(0), f_down(0), q, h, -roff} with
-    // e(c) = exp(-z (c h - r)^2), e(c +- 1) = e(c) f(c), f(c +- 1) = f(c) q.
-    if (lane < 6) {
-      const int dir = lane >> 1, up = lane & 1;
-      const float2 *sd = seed + 6 * dir;
-      dfloat ec = dfloat{sd[0].x, sd[0].y};
-      dfloat f = up ? dfloat{sd[1].x, sd[1].y} : dfloat{sd[2].x, sd[2].y};
-      const dfloat q = dfloat{sd[3].x, sd[3].y};
-      const dfloat hd = dfloat{sd[4].x, sd[4].y}, rd = dfloat{sd[5].x, sd[5].y};
-      const int cend = up ? cmax + 1 : -cmax;
-      for (int cc = 0;; cc += up ? 1 : -1) {
-        if (up || cc != 0) { // c = 0 is written by the up-going lane
-          const dfloat x = df_fma1(rd, hd, (float)cc);
-          dfloat v = ec;
-          T *p = pol + (size_t)(dir * w + cc + cmax) * PP;
-#pragma unroll
-          for (int l = 0; l <= LPB; l++) {
-            if (l > lp)
-              break;
-            p[l] = v;
-            v = df_mul(v, x);
-          }
-        }
-        if (cc == cend)
-          break;
-        ec = df_mul(ec, f);
-        f = df_mul(f, q);
-      }
-    }
+    seeded_tables<T, LPB, PP>(w, cmax, lp, pol, lane, seed);
   }
+}
+
+// Recurrence seeds of task t for fill_ortho_tables: the double-float kernels
+// always use them; the FP32 kernels only on the outside rows of a split task,
+// whose exponents z x^2 are large (elsewhere expf is as accurate and cheaper)
+template <typename N>
+__device__ __forceinline__ const float2 *table_seed(const GridArgs &a, int t) {
+  if constexpr (std::is_same<N, float>::value)
+    return a.core_side == 2 ? a.seeds + (size_t)t * 18 : nullptr;
+  else
+    return a.seeds + (size_t)t * 18;
 }
 
 // number of (ly, lx) pairs before row ly in a triangle of degree m
@@ -279,7 +306,7 @@ __global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
       }
       coef[r] = v;
     }
-    fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane, a.seeds + (size_t)t * 18);
+    fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane, table_seed<N>(a, t));
     __syncwarp();
 
     double *grid = a.grids[d.level];
@@ -427,7 +454,7 @@ __global__ void __launch_bounds__(128) collocate_ortho_pl(GridArgs a, int wmax) 
       }
       coef[r] = v;
     }
-    fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane, a.seeds + (size_t)t * 18);
+    fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane, table_seed<N>(a, t));
     __syncwarp();
 
     double *grid = a.grids[d.level];
@@ -435,8 +462,39 @@ __global__ void __launch_bounds__(128) collocate_ortho_pl(GridArgs a, int wmax) 
     const size_t nx = L.npts_local[0], nxy = nx * L.npts_local[1];
     const int *ploff = a.sph_ploff + H.plo;
 
+    const float r2 = a.core_side ? a.core_r2[t] : kCoreAll;
     for (int k = k_lo; k <= k_hi; k++) {
       const int kk = k <= 0 ? -k : k - 1;
+      const int n = ploff[kk + 1] - ploff[kk];
+      // the plane's points [f0, f1) and [g0, g1): all of them, or (split
+      // task) the rows inside the cylinder, or the rows outside it, which are
+      // contiguous ranges of the row-major list
+      int f0 = 0, f1 = n, g0 = n, g1 = n;
+      if (a.core_side) {
+        int clo, chi;
+        core_rows(r2, d, L, k, clo, chi);
+        const int js = cg.tab[kk], row0 = cg.tab[cg.K + kk];
+        int before = 0, inside = 0;
+        for (int j = js + lane; j <= 1 - js; j += 32) {
+          const int jj = j <= 0 ? -j : j - 1;
+          const int len = 2 - 2 * cg.tab[2 * cg.K + row0 + jj];
+          if (j < clo)
+            before += len;
+          else if (j <= chi)
+            inside += len;
+        }
+        before = __reduce_add_sync(FULL, before);
+        inside = __reduce_add_sync(FULL, inside);
+        if (a.core_side == 1) {
+          f0 = before;
+          f1 = before + inside;
+        } else {
+          f1 = before;
+          g0 = before + inside;
+        }
+        if (f1 <= f0 && g1 <= g0)
+          continue; // nothing of this plane on this side
+      }
       // C_xy[ly][lx] = sum_lz C_xyz[lz][ly][lx] pol_z[lz](k)
       const T *pz = pol + (size_t)(2 * cg.w + k + cg.cmax) * PP;
       for (int e = lane; e < ntr; e += 32) {
@@ -470,10 +528,11 @@ __global__ void __launch_bounds__(128) collocate_ortho_pl(GridArgs a, int wmax) 
       __syncwarp();
       const size_t zoff = (size_t)map[2 * cg.w + k + cg.cmax] * nxy;
       const int *pts = a.sph_pts + ploff[kk];
-      const int n = ploff[kk + 1] - ploff[kk];
-      for (int f = lane; f < n; f += 64) {
+      for (int rg = 0; rg < 2; rg++) {
+       const int fe = rg ? g1 : f1;
+       for (int f = (rg ? g0 : f0) + lane; f < fe; f += 64) {
         const int f2 = f + 32;
-        const bool two = f2 < n;
+        const bool two = f2 < fe;
         const int pk1 = __ldg(pts + f);
         const int pk2 = two ? __ldg(pts + f2) : pk1;
         const int x1 = (int)(short)(pk1 & 0xffff), j1 = pk1 >> 16;
@@ -495,6 +554,7 @@ __global__ void __launch_bounds__(128) collocate_ortho_pl(GridArgs a, int wmax) 
         if (two)
           grid_add<N>(grid, glo,
                       zoff + (size_t)map[cg.w + j2 + cg.cmax] * nx + map[x2 + cg.cmax], v2);
+       }
       }
       __syncwarp();
     }
@@ -546,9 +606,10 @@ __global__ void __launch_bounds__(128, LPB <= 4 ? 5 : 1) integrate_ortho(GridArg
     const int nco = ncoset(lp);
     for (int e = lane; e < nco; e += 32)
       acc[e] = 0.0;
-    fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane, a.seeds + (size_t)t * 18);
+    fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane, table_seed<N>(a, t));
     __syncwarp();
 
+    const float r2 = a.core_side ? a.core_r2[t] : kCoreAll;
     const void *grid = a.grids_in[d.level];
     const int gstride = a.grid_stride;
     const size_t nx = L.npts_local[0], nxy = nx * L.npts_local[1];
@@ -596,10 +657,20 @@ __global__ void __launch_bounds__(128, LPB <= 4 ? 5 : 1) integrate_ortho(GridArg
         // G-th row from its group's phase, R rows per step; the grid values
         // of the next step are loaded before this step's arithmetic
         const int JJ = xin ? (int)cg.jx[kk * cg.NX + (cx <= 0 ? -cx : cx - 1)] : -1;
-        const int jlo = -JJ, jhi = JJ + 1, G = nph;
-        int j = js + phase;
-        if (j < jlo)
-          j += ((jlo - j + G - 1) / G) * G;
+        int jlo = -JJ, jhi = JJ + 1, jlo2 = 1, jhi2 = 0;
+        if (a.core_side) { // split task: the rows inside, or the two runs outside
+          int clo, chi;
+          core_rows(r2, d, L, k, clo, chi);
+          if (a.core_side == 1) {
+            jlo = max(jlo, clo);
+            jhi = min(jhi, chi);
+          } else {
+            jlo2 = max(jlo, chi + 1);
+            jhi2 = jhi;
+            jhi = min(jhi, clo - 1);
+          }
+        }
+        const int G = nph;
         const size_t base = zoff + ig;
         auto fetch = [&](int jj, bool ok) -> T {
           return ok ? grid_get<N>(grid, base + (size_t)map[cg.w + jj + cg.cmax] * nx, gstride)
@@ -608,36 +679,44 @@ __global__ void __launch_bounds__(128, LPB <= 4 ? 5 : 1) integrate_ortho(GridArg
         // R rows per step (4 in FP32, whose arithmetic is too short to hide
         // the L2 latency of 2 loads in flight; 2 otherwise)
         constexpr int R = std::is_same<N, float>::value ? 4 : 2;
-        bool has[R];
-        T v[R];
-#pragma unroll
-        for (int r = 0; r < R; r++) {
-          has[r] = j + r * G <= jhi;
-          v[r] = fetch(j + r * G, has[r]);
-        }
-        while (has[0]) {
-          const int jn = j + R * G;
-          bool hn[R];
-          T vn[R];
+        for (int sg = 0; sg < 2; sg++) {
+          const int slo = sg ? jlo2 : jlo, shi = sg ? jhi2 : jhi;
+          if (slo > shi)
+            continue;
+          int j = js + phase;
+          if (j < slo)
+            j += ((slo - j + G - 1) / G) * G;
+          bool has[R];
+          T v[R];
 #pragma unroll
           for (int r = 0; r < R; r++) {
-            hn[r] = jn + r * G <= jhi;
-            vn[r] = fetch(jn + r * G, hn[r]);
+            has[r] = j + r * G <= shi;
+            v[r] = fetch(j + r * G, has[r]);
           }
+          while (has[0]) {
+            const int jn = j + R * G;
+            bool hn[R];
+            T vn[R];
 #pragma unroll
-          for (int r = 0; r < R; r++) {
-            T pr[PP];
-            load_row<T, PP>(pol + (size_t)(cg.w + (has[r] ? j + r * G : j) + cg.cmax) * PP, pr);
+            for (int r = 0; r < R; r++) {
+              hn[r] = jn + r * G <= shi;
+              vn[r] = fetch(jn + r * G, hn[r]);
+            }
 #pragma unroll
-            for (int ly = 0; ly < P; ly++)
-              if (ly <= lp)
-                wy[ly] = M::fma_acc(wy[ly], v[r], pr[ly]);
-          }
-          j = jn;
+            for (int r = 0; r < R; r++) {
+              T pr[PP];
+              load_row<T, PP>(pol + (size_t)(cg.w + (has[r] ? j + r * G : j) + cg.cmax) * PP, pr);
 #pragma unroll
-          for (int r = 0; r < R; r++) {
-            has[r] = hn[r];
-            v[r] = vn[r];
+              for (int ly = 0; ly < P; ly++)
+                if (ly <= lp)
+                  wy[ly] = M::fma_acc(wy[ly], v[r], pr[ly]);
+            }
+            j = jn;
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+              has[r] = hn[r];
+              v[r] = vn[r];
+            }
           }
         }
 #pragma unroll
@@ -683,7 +762,7 @@ __global__ void __launch_bounds__(128, LPB <= 4 ? 5 : 1) integrate_ortho(GridArg
         }
         __syncwarp();
         if (xc + xstep <= cg.x_hi) { // another x-chunk follows: rebuild the tables
-          fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane, a.seeds + (size_t)t * 18);
+          fill_ortho_tables<N, LPB>(d, L, cg.cmax, lp, pol, map, lane, table_seed<N>(a, t));
           __syncwarp();
         }
       }
@@ -691,7 +770,7 @@ __global__ void __launch_bounds__(128, LPB <= 4 ? 5 : 1) integrate_ortho(GridArg
     __syncwarp();
     double *dst = out + a.coef_off[t];
     for (int e = lane; e < nco; e += 32)
-      if (a.items) // plane ranges of one task add up (the buffer is zeroed)
+      if (a.items || a.accum) // parts of one task add up (the buffer is zeroed)
         atomicAdd(dst + e, acc[e]);
       else
         dst[e] = acc[e];
@@ -720,7 +799,7 @@ template <int LPB> struct TcSmem {
     size_t b = sizeof(float) * 3 * (size_t)wmax * PP; // pol x, y, z
     b += sizeof(float2) * (size_t)wmax * 8;          // pol_x split hi / lo
     b += sizeof(int) * 3 * (size_t)wmax;             // periodic maps
-    b += sizeof(int) * ((size_t)wmax + 4);           // row starts of the planes
+    b += sizeof(int) * 4 * ((size_t)wmax + 4);       // per plane: first row, row map
     b += 64;
     return (b + 15) & ~size_t(15);
   }
@@ -753,6 +832,7 @@ __global__ void __launch_bounds__(128) integrate_ortho_tc(GridArgs a, int wmax) 
   float2 *pxs = (float2 *)(pol + 3 * (size_t)wmax * PP);
   int *map = (int *)(pxs + (size_t)wmax * 8);
   int *starts = map + 3 * wmax;
+  int *prow = starts + wmax + 4; // per plane: j of row 0, skip at row, rows skipped
   double *out = (double *)a.coef_out;
 
   for (;;) {
@@ -775,7 +855,7 @@ __global__ void __launch_bounds__(128) integrate_ortho_tc(GridArgs a, int wmax) 
         atomicOr(a.error, 1);
       continue;
     }
-    fill_ortho_tables<float, LPB>(d, L, cg.cmax, lp, pol, map, lane, nullptr);
+    fill_ortho_tables<float, LPB>(d, L, cg.cmax, lp, pol, map, lane, table_seed<float>(a, t));
     __syncwarp();
     // pol_x split into TF32 high and low parts, lx >= P (or > lp) zero
     for (int e = lane; e < cg.w * 8; e += 32) {
@@ -785,16 +865,52 @@ __global__ void __launch_bounds__(128) integrate_ortho_tc(GridArgs a, int wmax) 
       const unsigned lo = f2tf32(v - __uint_as_float(hi));
       pxs[e] = make_float2(__uint_as_float(hi), __uint_as_float(lo));
     }
-    // first row of every plane k_lo .. k_hi (rows j in [js, 1 - js])
+    // the rows of every plane k_lo .. k_hi (j in [js, 1 - js]; of a split
+    // task the rows inside or outside the cylinder) numbered plane after
+    // plane: row i of plane p is j = prow[3p] + i (+ prow[3p + 2] from
+    // i = prow[3p + 1] on, stepping over the inside rows)
     const int np = k_hi - k_lo + 1;
-    if (lane == 0) {
-      int r = 0;
-      for (int p = 0; p < np; p++) {
-        const int k = k_lo + p, kk = k <= 0 ? -k : k - 1;
-        starts[p] = r;
-        r += 2 - 2 * cg.tab[kk];
+    const float r2 = a.core_side ? a.core_r2[t] : kCoreAll;
+    {
+      int carry = 0;
+      for (int p0 = 0; p0 < np; p0 += 32) {
+        const int p = p0 + lane;
+        int cnt = 0;
+        if (p < np) {
+          const int k = k_lo + p, kk = k <= 0 ? -k : k - 1, js = cg.tab[kk];
+          int j0 = js, at = 1 << 20, skip = 0;
+          cnt = 2 - 2 * js;
+          if (a.core_side) {
+            int clo, chi;
+            core_rows(r2, d, L, k, clo, chi);
+            const int ilo = max(clo, js), ihi = min(chi, 1 - js);
+            const int inside = max(0, ihi - ilo + 1);
+            if (a.core_side == 1) {
+              j0 = ilo;
+              cnt = inside;
+            } else {
+              at = min(max(clo - js, 0), cnt);
+              skip = inside;
+              cnt -= inside;
+            }
+          }
+          prow[3 * p] = j0;
+          prow[3 * p + 1] = at;
+          prow[3 * p + 2] = skip;
+        }
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(FULL, incl, o);
+          if (lane >= o)
+            incl += y;
+        }
+        if (p < np)
+          starts[p] = carry + incl - cnt;
+        carry += __shfl_sync(FULL, incl, 31);
       }
-      starts[np] = r;
+      if (lane == 0)
+        starts[np] = carry;
     }
     __syncwarp();
     const int R = starts[np];
@@ -829,8 +945,9 @@ __global__ void __launch_bounds__(128) integrate_ortho_tc(GridArgs a, int wmax) 
           if (h == 0)
             pc = p;
           const int k = k_lo + p, kk = k <= 0 ? -k : k - 1;
-          const int js = cg.tab[kk];
-          const int j = js + (r - starts[p]), jj = j <= 0 ? -j : j - 1;
+          const int i = r - starts[p];
+          const int j = prow[3 * p] + i + (i >= prow[3 * p + 1] ? prow[3 * p + 2] : 0);
+          const int jj = j <= 0 ? -j : j - 1;
           const int ist = cg.tab[2 * K + cg.tab[K + kk] + jj];
           kr[h] = k;
           jr[h] = j;
@@ -930,7 +1047,7 @@ __global__ void __launch_bounds__(128) integrate_ortho_tc(GridArgs a, int wmax) 
             if (lx + ly + lz <= lp) {
               const double v = f2d_exact(acc[s2][e]);
               const int ci = cidx(lz, ly, lx, lp);
-              if (a.items) // plane ranges of one task add up (the buffer is zeroed)
+              if (a.items || a.accum) // parts of one task add up (the buffer is zeroed)
                 atomicAdd(dst + ci, v);
               else
                 dst[ci] = v;

@@ -113,6 +113,8 @@ def lib():
         L.grid_gb300_set_copy_chunks.argtypes = [vp, C.c_int]
         L.grid_gb300_set_queue_streams.argtypes = [vp, C.c_int]
         L.grid_gb300_set_tensor_integrate.argtypes = [vp, C.c_int]
+        L.grid_gb300_set_row_split.argtypes = [vp, C.c_int]
+        L.grid_gb300_row_split_stats.argtypes = [vp, vp, vp]
         L.grid_gb300_tuned_split.argtypes = [vp]
         L.grid_gb300_tuned_split.restype = C.c_int
         L.grid_gb300_set_launch_timing.argtypes = [vp, C.c_int]
@@ -441,6 +443,18 @@ class GridTaskList:
         """FP32-class orthorhombic integration on the tensor cores
         (grid_gb300_set_tensor_integrate)."""
         lib().grid_gb300_set_tensor_integrate(self.impl, int(bool(enable)))
+
+    def set_row_split(self, enable: bool):
+        """Mixed mode: run the outer rows of orthorhombic double-float tasks
+        in FP32 (grid_gb300_set_row_split)."""
+        lib().grid_gb300_set_row_split(self.impl, int(bool(enable)))
+
+    def row_split_stats(self):
+        """(share of tasks split, share of grid points in FP32) of a density
+        collocation in the mixed mode (grid_gb300_row_split_stats)."""
+        a, b = C.c_double(), C.c_double()
+        lib().grid_gb300_row_split_stats(self.impl, C.byref(a), C.byref(b))
+        return a.value, b.value
 
     def set_queue_streams(self, n: int):
         """Streams the grid launches of a phase alternate over (1 or 2;

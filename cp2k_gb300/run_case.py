@@ -40,6 +40,8 @@ def main():
     ap.add_argument("--threshold", type=float, default=None,
                     help="mixed path: contribution bound below which tasks run in FP32")
     ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--no-row-split", action="store_true",
+                    help="mixed mode: keep every double-float task whole")
     ap.add_argument("--forces", action="store_true")
     ap.add_argument("--virial", action="store_true")
     ap.add_argument("--transform", type=int, default=-1, choices=[-1, 0, 1],
@@ -58,6 +60,7 @@ def main():
     if args.threshold is not None:
         tl.set_mixed_threshold(args.threshold)
     tl.set_transform_variant(args.transform)
+    tl.set_row_split(not args.no_row_split)
     s = torch.cuda.current_stream()
     if not args.compare:
         for step in range(args.steps):
@@ -100,6 +103,7 @@ def main():
         res["errors"]["virial_max_rel"] = rel(vx, v64)
     if args.precision == "mixed":
         res["fp32_share_tasks"], res["fp32_share_points"] = tl.mixed_split()
+        res["row_split_tasks"], res["fp32_share_points_row_split"] = tl.row_split_stats()
     print(json.dumps(res), flush=True)
     tl.close()
 

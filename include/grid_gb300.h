@@ -357,6 +357,19 @@ void grid_gb300_set_queue_streams(const grid_gb300_task_list *task_list, int n);
  * products, about 21 bits per product); 0 runs the CUDA-core kernel.  No
  * counterpart in CP2K. */
 void grid_gb300_set_tensor_integrate(const grid_gb300_task_list *task_list, int enable);
+/* Mixed mode: 1 (default) splits every orthorhombic double-float task by
+ * rows.  The rows (j, k) farther from the Gaussian product's x axis than the
+ * radius where the task's contribution bound falls to the mixed threshold
+ * run in FP32 (a second, FP32 pass over the task), the rows inside stay
+ * double-float; 0 keeps every task whole in its class.  No counterpart in
+ * CP2K. */
+void grid_gb300_set_row_split(const grid_gb300_task_list *task_list, int enable);
+/* The row split of a density collocation (no derivatives) in the mixed mode
+ * at the current threshold: the share of tasks split, and the share of grid
+ * points computed in FP32 (FP32-class tasks plus the outside rows of split
+ * tasks, the latter estimated from the cylinder's volume share). */
+void grid_gb300_row_split_stats(const grid_gb300_task_list *task_list,
+                                double *frac_tasks_split, double *frac_points_fp32);
 /* C_ab <-> C_xyz change of basis of the coefficient and post kernels: 0 the
  * direct gather over all (a, b) pairs, 1 the staged per-direction
  * contractions (x, then y, then z), -1 (default) staged in the coefficient

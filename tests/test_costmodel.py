@@ -168,7 +168,8 @@ def test_launch_timings_cover_all_tasks(CM):
     tl.collocate_device(100, pab, grids)
     info = tl.launch_timings()
     pts, _ = tl.sizes()
-    assert sum(i["ntasks"] for i in info) == int((pts > 0).sum()) or \
-        sum(i["points"] for i in info) == int(pts.sum())
+    # every task once, or (row split) its two parts, whose points add up
+    assert sum(i["ntasks"] for i in info) >= int((pts > 0).sum())
+    assert sum(i["points"] for i in info) == int(pts.sum())
     assert all(i["ms"] > 0 and i["blocks"] > 0 and i["warps_per_block"] >= 1 for i in info)
     tl.close()

@@ -483,3 +483,47 @@ def test_tensor_core_integrate(G, O, name, scale):
         else:
             assert float(np.abs(res[1][0] - h_only_ref).max()) / hmax < 1e-5
         tl.close()
+
+
+def test_row_split(G, O):
+    """Mixed mode with the outer rows of the double-float tasks in FP32 (the
+    default) on the full 512-atom workload, against the oracle: densities of
+    GRID_FUNC_AB and of a derivative function (DXDX, whose class test carries
+    the derivative factor) within 1e-6 in the reference measure, the
+    Tr(V rho) energy within 1e-8 Ha per atom, hab within 1e-6, forces, virial
+    and tau-integrated hab within 1e-5 (relative to max(1, |ref|)); and the
+    same bounds with every task whole."""
+    from cp2k_gb300 import workload as W
+    inp = W.config("c2_512atoms", seed=5)
+    pab = W.density_blocks(inp)
+    V = W.potential_grids(inp)
+    ot = O.OracleTaskList(inp)
+    tl = G.GridTaskList(inp, precision=G.MIXED)
+    split, fp32_points = tl.row_split_stats()
+    assert split > 0.05 and fp32_points > tl.mixed_split()[1] + 0.1
+    dvol = [abs(float(np.linalg.det(d))) for d in inp.dh]
+    res = {}
+    for on in (1, 0):
+        tl.set_row_split(on)
+        rho = {f: tl.collocate(f, pab) for f in (100, 801)}
+        res[on] = (rho, tl.integrate(V, pab, forces=True, virial=True),
+                   tl.integrate(V, pab, compute_tau=True, forces=True)[:2])
+    for f in (100, 801):
+        ref = ot.collocate(f, pab)
+        for on in (1, 0):
+            assert max(rel_diff(a, b) for a, b in zip(res[on][0][f], ref)) < 1e-6, (f, on)
+            if f == 100:
+                e = [sum(float((a * v).sum()) * dv for a, v, dv in zip(g, V, dvol))
+                     for g in (res[on][0][f], ref)]
+                assert abs(e[0] - e[1]) / inp.natoms < 1e-8, on
+    h2, f2, v2 = ot.integrate(V, pab, forces=True, virial=True)
+    ht2, ft2, _ = ot.integrate(V, pab, compute_tau=True, forces=True)
+    for on in (1, 0):
+        (h1, f1, v1), (ht1, ft1) = res[on][1], res[on][2]
+        assert rel_diff(h1, h2) < 1e-6
+        assert rel_diff(f1, f2) < 1e-5
+        assert rel_diff(v1, v2) < 1e-5
+        assert rel_diff(ht1, ht2) < 1e-5
+        assert rel_diff(ft1, ft2) < 1e-5
+    tl.close()
+    ot.close()
