@@ -14,9 +14,12 @@ grid_integrate_task_list (hab only), as one SCF iteration does.
   errors     mixed / FP64 / FP32 against the oracle's FP64 results on the
              same inputs (and mixed against the FP64 path);
   roofline   the dominant grid kernel of the mixed step (largest total time
-             from per-launch CUDA events) against the measured HBM roof, and
-             against the CUDA-core FMA roof that binds it (roofline_fp32);
+             from per-launch CUDA events; the tensor-core FP32-class
+             integrate) against the measured HBM roof, and its algorithmic
+             flops against the CUDA-core FMA roof (roofline_fp32);
              roofline_fp64 the same for the FP64 step;
+  mixed_no_row_split / mixed_model_schedule / mixed_one_queue_stream
+             the mixed step with one feature switched back (diagnostics);
   cpu_baseline  whole SCF steps of the oracle (FP64 C restatement of CP2K's
              REF backend) on all host cores;
   triclinic_256atoms_forces_virial, c5_6144atoms_forces
@@ -236,13 +239,15 @@ def measure_peak(torch, dtype, n):
     return best
 
 
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
-# dominant kernels of the 512-atom mixed and FP64 steps, from one ncu capture
-# of this workload (two launches per kernel, mean); the bench cannot run ncu
-# itself.  Keys: kernel label as in "roofline.kernel".
-NCU_TRAFFIC = {
-    "integrate_ortho<dfloat,4>": 0.5 * ((37.778 + 1.220) + (244.241 + 62.083)) * 1e6,
-    "integrate_ortho<double,4>": 0.5 * ((35.777 + 0.760) + (594.138 + 123.159)) * 1e6,
+# DRAM bytes per SCF step (dram__bytes_read.sum + dram__bytes_write.sum over
+# the kernel's launches of one step) of the dominant kernels of the 512-atom
+# mixed and FP64 steps, from one ncu capture of this workload at the default
+# launch split; the bench cannot run ncu itself, and divides by its own
+# launches per step.  Keys: kernel label as in "roofline.kernel".
+NCU_TRAFFIC_PER_STEP = {
+    "integrate_ortho_tc<4>": (2.632 + 0.024 + 25.168 + 0.098 + 178.044 + 47.542
+                              + 114.334 + 19.523) * 1e6,
+    "integrate_ortho<double,4>": ((35.777 + 0.760) + (594.138 + 123.159)) * 1e6,
 }
 
 
@@ -250,6 +255,10 @@ def _kernel_label(info):
     prec = {0: "double", 1: "dfloat", 2: "float"}[info["precision"]]
     kind = "general" if info["general"] else "ortho"
     phase = "collocate" if info["phase"] == 0 else "integrate"
+    if (info["phase"] == 1 and prec == "float" and not info["general"]
+            and info["lp_bucket"] <= 6):
+        # FP32-class orthorhombic integration runs on the tensor cores (default)
+        return f"integrate_ortho_tc<{info['lp_bucket']}>"
     return f"{phase}_{kind}<{prec},{info['lp_bucket']}>"
 
 
@@ -304,13 +313,15 @@ def roofline_objects(per, phase_points, field_points, peaks, peak_kind, fp_peak,
     if d["phase"] == 0:
         bpp = 12.0 if arith == "mixed" else 8.0
     else:
-        bpp = 8.0
+        # FP32 kernels of the mixed mode read the dense high words (4 B)
+        bpp = 4.0 if (arith == "mixed" and ("<float" in dom or "_tc<" in dom)) else 8.0
     share = d["points"] / max(phase_points[d["phase"]], 1.0)
     alg_bytes = bpp * field_points * share
     alg_flops = d["flops"] / d["launches"]
     gbs = alg_bytes / (avg_ms * 1e-3) / 1e9
     tf = alg_flops / (avg_ms * 1e-3) / 1e12
-    traffic = NCU_TRAFFIC.get(dom)
+    per_step = NCU_TRAFFIC_PER_STEP.get(dom)
+    traffic = per_step / (d["launches"] / 3.0) if per_step else None
     hbm = {"bound": "hbm", "achieved": gbs, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
            "frac": gbs / peaks.get("hbm_gbs", 1.0), "traffic": traffic, "kernel": dom,
            "launch_ms": avg_ms, "launches_per_step": d["launches"] / 3.0,

@@ -682,9 +682,15 @@ static double contribution_bound(const TaskDesc &d, const double *ra) {
 // 21.4 and 22.3 ms.
 constexpr double kShellMargin = 3.0;
 
-static float core_radius2(const TaskDesc &d, double tau, double *outside) {
+static float core_radius2(const TaskDesc &d, int dla, int dlb, double tau, double *outside) {
   *outside = 0.0;
-  const int la = d.la_max, lb = d.lb_max, nn = la + lb + 1;
+  // the call's l shifts (derivatives) raise the polynomial degree of the
+  // rows' values: the bound runs over the shifted l ranges
+  if (d.la_max + dla > GB300_LMAX || d.lb_max + dlb > GB300_LMAX)
+    return kCoreAll; // past the tables below: keep the task whole
+  const int la = d.la_max + dla, lb = d.lb_max + dlb;
+  const int la_min = std::max(d.la_min - dla, 0), lb_min = std::max(d.lb_min - dlb, 0);
+  const int nn = la + lb + 1;
   double bin[GB300_LMAX + 1][GB300_LMAX + 1] = {};
   for (int n = 0; n <= GB300_LMAX; n++) {
     bin[n][0] = 1.0;
@@ -711,11 +717,11 @@ static float core_radius2(const TaskDesc &d, double tau, double *outside) {
       }
   }
   double C[4 * GB300_LMAX + 2] = {};
-  for (int l1 = d.la_min; l1 <= la; l1++)
+  for (int l1 = la_min; l1 <= la; l1++)
     for (int ax = 0; ax <= l1; ax++)
       for (int ay = 0; ay <= l1 - ax; ay++) {
         const int az = l1 - ax - ay;
-        for (int l2 = d.lb_min; l2 <= lb; l2++)
+        for (int l2 = lb_min; l2 <= lb; l2++)
           for (int bx = 0; bx <= l2; bx++)
             for (int by = 0; by <= l2 - bx; by++) {
               const int bz = l2 - bx - by;
@@ -1273,7 +1279,8 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase, int nch = 1) {
         fac = pow(2.0 * std::max(k.zeta, k.zetb) + std::max(k.la_max, k.lb_max) + 1.0, dshift);
       if (t->gbound[s] * fac <= t->mixed_threshold)
         return; // FP32 class already
-      m.core_r2[s] = core_radius2(k, t->mixed_threshold / (fac * kShellMargin), &outside[s]);
+      m.core_r2[s] = core_radius2(k, d.la_max, d.lb_max, t->mixed_threshold / (fac * kShellMargin),
+                                  &outside[s]);
     });
   m.row_split = false;
   // work queues: (general, lp bucket, FP32 class, size class), descending
@@ -2393,7 +2400,7 @@ GB300_API void grid_gb300_row_split_stats(const grid_gb300_task_list *task_list,
     }
     cls[s] = 0;
     if (t->row_split && !(k.flags & TF_GENERAL) &&
-        core_radius2(k, t->mixed_threshold / kShellMargin, &out[s]) >= kCoreAll)
+        core_radius2(k, 0, 0, t->mixed_threshold / kShellMargin, &out[s]) >= kCoreAll)
       out[s] = 0.0;
   });
   double nt = 0, ns = 0, pt = 0, pf = 0;
