@@ -377,8 +377,9 @@ struct TaskList {
   // the independent grid launches of a phase alternate over this many
   // streams, so that one launch's tail overlaps the next one's start
   int queue_streams = 2;
-  // integrate, orthorhombic, FP32 class, lp <= 6: the tensor-core kernel
+  // orthorhombic, FP32 class, lp <= 6: the tensor-core kernels
   int tc_integrate = 1;
+  int tc_collocate = 0; // measured slower than the CUDA-core collocation
   // mixed mode: the outer rows of orthorhombic double-float tasks in FP32
   int row_split = 1;
   cudaStream_t aux_stream = nullptr;
@@ -1513,6 +1514,10 @@ static void grid_launch(TaskList *t, const Queue &q, int phase, int arith, const
   if (it != t->tuned.end())
     cfg = it->second;
   cfg.tensor = t->tc_integrate;
+  // the tensor-core collocation keeps about 21 bits per product: the mixed
+  // mode's FP32 class (contributions bounded by the threshold) takes it,
+  // plain FP32 mode keeps the CUDA-core kernels' 24
+  cfg.tensor_coll = t->tc_collocate && t->precision == GRID_GB300_MIXED;
   if (q.side != 0) // a split task's rows are ranges of the point lists
     cfg.variant = 1;
   LaunchRecord rec;
@@ -1905,7 +1910,7 @@ GB300_API void grid_gb300_create_task_list(
   // learned schedule falls back to the size order until a model is applied.
   struct Kept {
     int precision, schedule, coll_variant, transform_variant, copy_chunks, queue_streams,
-        tc_integrate, row_split;
+        tc_integrate, tc_collocate, row_split;
     double mixed_threshold, model_bin;
     int small_extent[3];
     std::map<std::tuple<int, int, int>, LaunchCfg> tuned;
@@ -1915,7 +1920,8 @@ GB300_API void grid_gb300_create_task_list(
   if (*task_list) {
     const TaskList *o = TL(*task_list);
     kept.reset(new Kept{o->precision, o->schedule, o->coll_variant, o->transform_variant,
-                        o->copy_chunks, o->queue_streams, o->tc_integrate, o->row_split,
+                        o->copy_chunks, o->queue_streams, o->tc_integrate, o->tc_collocate,
+                        o->row_split,
                         o->mixed_threshold,
                         o->model_bin, {o->small_extent[0], o->small_extent[1],
                                        o->small_extent[2]},
@@ -1937,6 +1943,7 @@ GB300_API void grid_gb300_create_task_list(
     t->copy_chunks = kept->copy_chunks;
     t->queue_streams = kept->queue_streams;
     t->tc_integrate = kept->tc_integrate;
+    t->tc_collocate = kept->tc_collocate;
     t->row_split = kept->row_split;
     t->mixed_threshold = kept->mixed_threshold;
     t->model_bin = kept->model_bin;
@@ -2670,6 +2677,13 @@ GB300_API void grid_gb300_set_tensor_integrate(const grid_gb300_task_list *task_
                                                int enable) {
   TaskList *t = TL(task_list);
   t->tc_integrate = enable ? 1 : 0;
+  t->gen++; // captured graphs hold the other kernel
+}
+
+GB300_API void grid_gb300_set_tensor_collocate(const grid_gb300_task_list *task_list,
+                                               int enable) {
+  TaskList *t = TL(task_list);
+  t->tc_collocate = enable ? 1 : 0;
   t->gen++; // captured graphs hold the other kernel
 }
 

@@ -106,7 +106,7 @@ struct LDiffs {
   int la_max, la_min, lb_max, lb_min;
 };
 
-__host__ __device__ inline int ncoset(int l) {
+__host__ __device__ constexpr int ncoset(int l) {
   return l < 0 ? 0 : (l + 1) * (l + 2) * (l + 3) / 6;
 }
 __host__ __device__ inline int coset(int lx, int ly, int lz) {
@@ -114,7 +114,7 @@ __host__ __device__ inline int coset(int lx, int ly, int lz) {
   return l == 0 ? 0 : ncoset(l - 1) + ((l - lx) * (l - lx + 1)) / 2 + lz;
 }
 // number of (a, b) with a + b <= m
-__host__ __device__ inline int ntri(int m) { return m < 0 ? 0 : (m + 1) * (m + 2) / 2; }
+__host__ __device__ constexpr int ntri(int m) { return m < 0 ? 0 : (m + 1) * (m + 2) / 2; }
 // compact index of x^lx y^ly z^lz in a polynomial of degree <= lp
 __host__ __device__ inline int cidx(int lz, int ly, int lx, int lp) {
   const int m = lp - lz;
@@ -321,6 +321,7 @@ struct LaunchCfg {
   int occupancy = 100; // automatic CTA count: this percentage of all that fit
   int variant = 0;     // collocate, orthorhombic: 0 row walk, 1 point list
   int tensor = 0;      // integrate, orthorhombic, FP32, lp <= 6: tensor-core kernel
+  int tensor_coll = 0; // collocate, orthorhombic, FP32, lp <= 6: tensor-core kernel
 };
 inline int cfg_blocks(const LaunchCfg &c, int persistent) {
   if (c.blocks > 0)

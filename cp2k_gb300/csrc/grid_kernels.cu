@@ -1060,6 +1060,259 @@ __global__ void __launch_bounds__(128) integrate_ortho_tc(GridArgs a, int wmax) 
   }
 }
 
+// ------------------------------------------------------------------------
+// collocate, orthorhombic, FP32 class, on the tensor cores
+// ------------------------------------------------------------------------
+// With the x factor folded into the coefficients once per task,
+//   Q[x][(ly, lz)] = sum_lx C_xyz[lz][ly][lx] pol_x[lx](x),
+// every value of the cube is a product over the (ly, lz) pairs:
+//   rho[x][(j, k)] = sum_(ly,lz) Q[x][(ly, lz)] pol_y[ly](j) pol_z[lz](k).
+// One warp per task runs it as mma.sync m16n8k8 TF32 tiles: 16 x of the cube
+// (M) by 8 rows (j, k) of the sphere (N; the rows of all planes numbered one
+// after another, as in integrate_ortho_tc), the pairs (K, two steps of 8 for
+// lp <= 4, ntri(lp) <= 16).  Both operands are split into TF32 high and low
+// parts and three products accumulated in FP32 (about 21 bits per product).
+// Each lane adds its four results that lie inside the sphere (the
+// reference's point set, grid_ref_collint.h:144-151) to the FP64 grid;
+// points of a tile outside the sphere cost only tensor-core work.  Split
+// tasks (core_side) take their rows inside or outside the cylinder.
+template <int LPB> struct TcCollSmem {
+  static constexpr int PP = 8;
+  static constexpr int NPR = (ntri(LPB) + 7) & ~7; // pairs, padded to k8 steps
+  static __host__ __device__ size_t bytes(int wmax) {
+    size_t b = sizeof(float) * 3 * (size_t)wmax * PP;      // pol x, y, z
+    b += sizeof(float2) * (size_t)wmax * NPR;              // Q[x][pair] hi / lo
+    b += sizeof(float) * ((ncoset(LPB) + 3) & ~3);         // C_xyz of the task
+    b += sizeof(int) * 3 * (size_t)wmax;                   // periodic maps
+    b += sizeof(int) * 4 * ((size_t)wmax + 4);             // per plane: first row, row map
+    b += 64;
+    return (b + 15) & ~size_t(15);
+  }
+};
+
+template <int LPB>
+__global__ void __launch_bounds__(128) collocate_ortho_tc(GridArgs a, int wmax) {
+  static_assert(ntri(LPB) <= 32, "pairs fit four k8 steps");
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int PP = TcCollSmem<LPB>::PP;
+  constexpr int NPR = TcCollSmem<LPB>::NPR;
+  constexpr int KS = NPR / 8; // k8 steps
+  const int lane = threadIdx.x & 31, grp = lane >> 2, tq = lane & 3;
+  unsigned char *ws = smem + (threadIdx.x >> 5) * TcCollSmem<LPB>::bytes(wmax);
+  float *pol = (float *)ws;
+  float2 *qs = (float2 *)(pol + 3 * (size_t)wmax * PP);
+  float *cx = (float *)(qs + (size_t)wmax * NPR);
+  int *map = (int *)(cx + ((ncoset(LPB) + 3) & ~3));
+  int *starts = map + 3 * wmax;
+  int *prow = starts + wmax + 4;
+
+  for (;;) {
+    int qi = 0;
+    if (lane == 0)
+      qi = atomicAdd(a.counter, 1);
+    qi = __shfl_sync(FULL, qi, 0);
+    if (qi >= a.nqueue)
+      break;
+    const WorkItem w = work_item(a, qi);
+    const int t = w.t;
+    const long long t0 = clock64();
+    const TaskDesc d = a.tasks[t];
+    const LevelDesc &L = a.levels.lv[d.level];
+    const int lp = d.la_max + a.d.la_max + d.lb_max + a.d.lb_max;
+    const CubeGeo cg = cube_geo(a.sph[d.sphere], a.sph_tab, lane);
+    const int k_lo = cg.lb2 + w.k0, k_hi = min(1 - cg.lb2, cg.lb2 + w.k0 + w.nk - 1);
+    if (cg.w > wmax || lp > LPB || k_hi - k_lo + 1 > wmax + 2) {
+      if (lane == 0) // the host sized the work arrays; never expected
+        atomicOr(a.error, 1);
+      continue;
+    }
+    const int nco = ncoset(lp), npr = ntri(lp);
+    for (int e = lane; e < nco; e += 32)
+      cx[e] = ((const float *)a.coef)[((size_t)a.coef_off[t] + e) * a.coef_stride];
+    fill_ortho_tables<float, LPB>(d, L, cg.cmax, lp, pol, map, lane, table_seed<float>(a, t));
+    __syncwarp();
+    // Q[x][pair] for every x of the cube, pairs (ly, lz) with ly + lz <= lp in
+    // the order of lz, then ly; padded pairs zero
+    for (int e = lane; e < cg.w * NPR; e += 32) {
+      const int c = e / NPR, pr = e - c * NPR;
+      float v = 0.f;
+      if (pr < npr) {
+        int lz = 0, rem = pr;
+        while (rem > lp - lz) {
+          rem -= lp - lz + 1;
+          lz++;
+        }
+        const int ly = rem;
+        const float *px = pol + (size_t)c * PP;
+#pragma unroll
+        for (int lx = 0; lx <= LPB; lx++)
+          if (lx <= lp - ly - lz)
+            v = fmaf(cx[cidx(lz, ly, lx, lp)], px[lx], v);
+      }
+      const unsigned hi = f2tf32(v);
+      qs[e] = make_float2(__uint_as_float(hi), __uint_as_float(f2tf32(v - __uint_as_float(hi))));
+    }
+    // the rows of planes k_lo .. k_hi (split tasks: inside or outside the
+    // cylinder) numbered plane after plane, as in integrate_ortho_tc
+    const int np = k_hi - k_lo + 1;
+    const float r2 = a.core_side ? a.core_r2[t] : kCoreAll;
+    {
+      int carry = 0;
+      for (int p0 = 0; p0 < np; p0 += 32) {
+        const int p = p0 + lane;
+        int cnt = 0;
+        if (p < np) {
+          const int k = k_lo + p, kk = k <= 0 ? -k : k - 1, js = cg.tab[kk];
+          int j0 = js, at = 1 << 20, skip = 0;
+          cnt = 2 - 2 * js;
+          if (a.core_side) {
+            int clo, chi;
+            core_rows(r2, d, L, k, clo, chi);
+            const int ilo = max(clo, js), ihi = min(chi, 1 - js);
+            const int inside = max(0, ihi - ilo + 1);
+            if (a.core_side == 1) {
+              j0 = ilo;
+              cnt = inside;
+            } else {
+              at = min(max(clo - js, 0), cnt);
+              skip = inside;
+              cnt -= inside;
+            }
+          }
+          prow[3 * p] = j0;
+          prow[3 * p + 1] = at;
+          prow[3 * p + 2] = skip;
+        }
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(FULL, incl, o);
+          if (lane >= o)
+            incl += y;
+        }
+        if (p < np)
+          starts[p] = carry + incl - cnt;
+        carry += __shfl_sync(FULL, incl, 31);
+      }
+      if (lane == 0)
+        starts[np] = carry;
+    }
+    __syncwarp();
+    const int R = starts[np];
+    // this lane's B pairs: 8 s + tq and 8 s + tq + 4 of every k8 step s
+    int ply[2 * KS], plz[2 * KS];
+#pragma unroll
+    for (int i = 0; i < 2 * KS; i++) {
+      const int pr = 8 * (i >> 1) + tq + 4 * (i & 1);
+      int lz = 0, rem = pr;
+      while (rem > lp - lz && lz <= lp) {
+        rem -= lp - lz + 1;
+        lz++;
+      }
+      ply[i] = pr < npr ? rem : -1;
+      plz[i] = lz;
+    }
+    double *grid = a.grids[d.level];
+    const size_t nx = L.npts_local[0], nxy = nx * L.npts_local[1];
+    const int K = cg.K;
+    const int nxt = (cg.x_hi - cg.x_lo + 16) >> 4; // x tiles, counted up front
+    // row r of the numbering -> plane k, row j, cursor pc over the planes
+    auto row_of = [&](int r, int &pc, int &k, int &j) {
+      int p = pc;
+      while (starts[p + 1] <= r)
+        p++;
+      pc = p;
+      const int i = r - starts[p];
+      k = k_lo + p;
+      j = prow[3 * p] + i + (i >= prow[3 * p + 1] ? prow[3 * p + 2] : 0);
+    };
+    int pcb = 0, pco = 0;
+    const int nrt = (R + 7) >> 3;
+#pragma unroll 1
+    for (int rt = 0; rt < nrt; rt++) {
+      // B: pol_y[ly](j) pol_z[lz](k) of row 8 rt + grp for this lane's pairs
+      unsigned bh[2 * KS], bl[2 * KS];
+      {
+        const int r = 8 * rt + grp;
+        float pyz[2 * KS];
+        if (r < R) {
+          int k, j;
+          row_of(r, pcb, k, j);
+          const float *py = pol + (size_t)(cg.w + j + cg.cmax) * PP;
+          const float *pz = pol + (size_t)(2 * cg.w + k + cg.cmax) * PP;
+#pragma unroll
+          for (int i = 0; i < 2 * KS; i++)
+            pyz[i] = ply[i] >= 0 ? py[ply[i]] * pz[plz[i]] : 0.f;
+        } else {
+#pragma unroll
+          for (int i = 0; i < 2 * KS; i++)
+            pyz[i] = 0.f;
+        }
+#pragma unroll
+        for (int i = 0; i < 2 * KS; i++) {
+          bh[i] = f2tf32(pyz[i]);
+          bl[i] = f2tf32(pyz[i] - __uint_as_float(bh[i]));
+        }
+      }
+      // outputs of this lane: rows 8 rt + 2 tq + h
+      int xs[2], xe[2];
+      size_t roff[2];
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int r = 8 * rt + 2 * tq + h;
+        xs[h] = 1;
+        xe[h] = 0;
+        roff[h] = 0;
+        if (r < R) {
+          int k, j;
+          row_of(r, pco, k, j);
+          const int kk = k <= 0 ? -k : k - 1, jj = j <= 0 ? -j : j - 1;
+          const int ist = cg.tab[2 * K + cg.tab[K + kk] + jj];
+          xs[h] = ist;
+          xe[h] = 1 - ist;
+          roff[h] = (size_t)map[2 * cg.w + k + cg.cmax] * nxy +
+                    (size_t)map[cg.w + j + cg.cmax] * nx;
+        }
+      }
+      __syncwarp(); // the look-ups above diverge; mma.sync needs the whole warp
+#pragma unroll 1
+      for (int xt = 0; xt < nxt; xt++) {
+        const int xa = cg.x_lo + 16 * xt + grp, xc = xa + 8;
+        const bool in0 = xa <= cg.x_hi, in1 = xc <= cg.x_hi;
+        float c[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int s8 = 0; s8 < KS; s8++) {
+          const float2 z2 = make_float2(0.f, 0.f);
+          const int p0 = 8 * s8 + tq;
+          const float2 q00 = in0 ? qs[(size_t)(xa + cg.cmax) * NPR + p0] : z2;
+          const float2 q01 = in0 ? qs[(size_t)(xa + cg.cmax) * NPR + p0 + 4] : z2;
+          const float2 q10 = in1 ? qs[(size_t)(xc + cg.cmax) * NPR + p0] : z2;
+          const float2 q11 = in1 ? qs[(size_t)(xc + cg.cmax) * NPR + p0 + 4] : z2;
+          const unsigned ahi[4] = {__float_as_uint(q00.x), __float_as_uint(q10.x),
+                                   __float_as_uint(q01.x), __float_as_uint(q11.x)};
+          const unsigned alo[4] = {__float_as_uint(q00.y), __float_as_uint(q10.y),
+                                   __float_as_uint(q01.y), __float_as_uint(q11.y)};
+          mma_tf32(c, alo, bh[2 * s8], bh[2 * s8 + 1]);
+          mma_tf32(c, ahi, bl[2 * s8], bl[2 * s8 + 1]);
+          mma_tf32(c, ahi, bh[2 * s8], bh[2 * s8 + 1]);
+        }
+        const int mx0 = in0 ? map[xa + cg.cmax] : 0, mx1 = in1 ? map[xc + cg.cmax] : 0;
+        // c0 (xa, row 2tq), c1 (xa, row 2tq+1), c2 (xc, 2tq), c3 (xc, 2tq+1)
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          const int h = i & 1, x = i < 2 ? xa : xc;
+          if (x >= xs[h] && x <= xe[h])
+            atomicAdd(grid + roff[h] + (i < 2 ? mx0 : mx1), f2d_grid(c[i]));
+        }
+        __syncwarp();
+      }
+    }
+    if (a.task_cycles && lane == 0)
+      atomicAdd((unsigned long long *)&a.task_cycles[t], (unsigned long long)(clock64() - t0));
+    __syncwarp();
+  }
+}
+
 } // namespace
 
 // ------------------------------------------------------------------------
@@ -1113,11 +1366,31 @@ static void launch_ortho_tc(const GridArgs &a, int wmax, LaunchCfg &cfg, cudaStr
 }
 
 template <int LPB>
+static void launch_coll_tc(const GridArgs &a, int wmax, LaunchCfg &cfg, cudaStream_t s) {
+  const size_t per_warp = TcCollSmem<LPB>::bytes(wmax);
+  int nw = warps_for(per_warp);
+  if (nw < 1)
+    return launch_error("orthorhombic grid kernel: cube too large for shared memory");
+  if (cfg.warps > 0 && cfg.warps < nw)
+    nw = cfg.warps;
+  const size_t smem = nw * per_warp;
+  const void *k = (const void *)collocate_ortho_tc<LPB>;
+  set_smem(k, smem);
+  const int nb = cfg.blocks > 0 ? cfg.blocks : cfg_blocks(cfg, persistent_blocks(k, 32 * nw, smem));
+  cfg.warps = nw;
+  cfg.blocks = nb;
+  collocate_ortho_tc<LPB><<<nb, 32 * nw, smem, s>>>(a, wmax);
+  count_launch();
+}
+
+template <int LPB>
 static void launch_ortho_lp(const GridArgs &a, int arith, bool collocate, int wmax,
                             LaunchCfg &cfg, cudaStream_t s) {
   if constexpr (LPB <= 6) {
     if (!collocate && arith == ARITH_FP32 && cfg.tensor)
       return launch_ortho_tc<LPB>(a, wmax, cfg, s);
+    if (collocate && arith == ARITH_FP32 && cfg.tensor_coll)
+      return launch_coll_tc<LPB>(a, wmax, cfg, s);
   }
   if (arith == ARITH_FP64)
     launch_ortho_t<double, LPB>(a, collocate, wmax, cfg, s);

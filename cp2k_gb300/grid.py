@@ -114,6 +114,7 @@ def lib():
         L.grid_gb300_set_queue_streams.argtypes = [vp, C.c_int]
         L.grid_gb300_set_tensor_integrate.argtypes = [vp, C.c_int]
         L.grid_gb300_set_row_split.argtypes = [vp, C.c_int]
+        L.grid_gb300_set_tensor_collocate.argtypes = [vp, C.c_int]
         L.grid_gb300_row_split_stats.argtypes = [vp, vp, vp]
         L.grid_gb300_tuned_split.argtypes = [vp]
         L.grid_gb300_tuned_split.restype = C.c_int
@@ -443,6 +444,11 @@ class GridTaskList:
         """FP32-class orthorhombic integration on the tensor cores
         (grid_gb300_set_tensor_integrate)."""
         lib().grid_gb300_set_tensor_integrate(self.impl, int(bool(enable)))
+
+    def set_tensor_collocate(self, enable: bool):
+        """FP32-class orthorhombic collocation on the tensor cores
+        (grid_gb300_set_tensor_collocate)."""
+        lib().grid_gb300_set_tensor_collocate(self.impl, int(bool(enable)))
 
     def set_row_split(self, enable: bool):
         """Mixed mode: run the outer rows of orthorhombic double-float tasks

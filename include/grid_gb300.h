@@ -357,6 +357,13 @@ void grid_gb300_set_queue_streams(const grid_gb300_task_list *task_list, int n);
  * products, about 21 bits per product); 0 runs the CUDA-core kernel.  No
  * counterpart in CP2K. */
 void grid_gb300_set_tensor_integrate(const grid_gb300_task_list *task_list, int enable);
+/* 1: in the mixed mode, FP32-class orthorhombic collocation with lp <= 6 on
+ * the tensor cores (16 x by 8 rows of the sphere per mma.sync m16n8k8 tile,
+ * the (ly, lz) pairs as the contraction, operands split as above, about 21
+ * bits per product); 0 (default) runs the CUDA-core kernels, which are
+ * faster on the measured workloads.  Plain FP32 mode always runs the
+ * CUDA-core kernels.  No counterpart in CP2K. */
+void grid_gb300_set_tensor_collocate(const grid_gb300_task_list *task_list, int enable);
 /* Mixed mode: 1 (default) splits every orthorhombic double-float task by
  * rows.  The rows (j, k) farther from the Gaussian product's x axis than the
  * radius where the task's contribution bound falls to the mixed threshold

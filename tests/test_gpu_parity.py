@@ -527,3 +527,59 @@ def test_row_split(G, O):
         assert rel_diff(ft1, ft2) < 1e-5
     tl.close()
     ot.close()
+
+
+# the tensor-core collocation keeps about 21 bits per product (TF32 high and
+# low parts, three products): eight times the FP32 bound of the CUDA-core
+# kernels where a task's polynomial cancels
+TOL_TC_COLL = 8e-5
+
+
+@pytest.mark.parametrize("name,scale", [("c2_512atoms", 0.1), ("c1_64atoms", 0.3)])
+def test_tensor_core_collocate(G, O, name, scale):
+    """The mixed mode's FP32-class orthorhombic collocation on the tensor
+    cores (opt-in) against the CUDA-core kernels and the oracle: both
+    within the mixed mode's bound (rho 1e-6 in the reference measure, shells
+    of split tasks included), and within 2e-6 of each other; and with every
+    task in the FP32 class (threshold 1e30) within TOL_TC_COLL of the largest
+    density value."""
+    from cp2k_gb300 import workload as W
+    inp = W.config(name, scale=scale, seed=43)
+    pab = W.density_blocks(inp)
+    ot = O.OracleTaskList(inp)
+    ref = ot.collocate(100, pab)
+    ot.close()
+    rmax = max(float(np.abs(r).max()) for r in ref)
+    tl = G.GridTaskList(inp, precision=G.MIXED)
+    res = {}
+    for tc in (0, 1):
+        tl.set_tensor_collocate(tc)
+        res[tc] = tl.collocate(100, pab)
+        assert max(rel_diff(a, b) for a, b in zip(res[tc], ref)) < 1e-6, tc
+    assert max(float(np.abs(a - b).max()) for a, b in zip(res[1], res[0])) / rmax < 2e-6
+    tl.set_mixed_threshold(1e30)
+    tl.set_tensor_collocate(1)
+    g = tl.collocate(100, pab)
+    assert max(float(np.abs(a - b).max()) for a, b in zip(g, ref)) / rmax < TOL_TC_COLL
+    tl.close()
+
+
+@pytest.mark.parametrize("name", sorted(SAMPLE_TASKS))
+def test_tensor_core_collocate_sample_tasks(G, O, name):
+    """Every sample task collocated with the tensor-core kernel (mixed mode,
+    threshold 1e30: every task in the FP32 class; the kernel takes the
+    orthorhombic tasks with lp <= 6, the others run the CUDA-core kernels):
+    max |d| / max |ref| <= TOL_TC_COLL against the oracle."""
+    from cp2k_gb300.tasklist import single_task_list
+    t = digest_task(load_digests()[name])
+    inp = single_task_list(t)
+    tl = G.GridTaskList(inp, precision=G.MIXED)
+    tl.set_mixed_threshold(1e30)
+    tl.set_tensor_collocate(True)
+    ot = O.OracleTaskList(inp)
+    pab_c = (0.5 * t["rscale"] * t["pab"]).ravel()
+    g_ora = ot.collocate(t["func"], pab_c)[0]
+    g = tl.collocate(t["func"], pab_c)[0]
+    assert float(np.abs(g - g_ora).max()) <= TOL_TC_COLL * float(np.abs(g_ora).max())
+    tl.close()
+    ot.close()
