@@ -726,10 +726,10 @@ static float core_radius2(const TaskDesc &d, int dla, int dlb, double tau, doubl
           for (int bx = 0; bx <= l2; bx++)
             for (int by = 0; by <= l2 - bx; by++) {
               const int bz = l2 - bx - by;
+              const double *cx = al[0][ax][bx], *cy = al[1][ay][by], *cz = al[2][az][bz];
               double Bx = 0.0;
               for (int n = 0; n <= ax + bx; n++)
-                Bx += al[0][ax][bx][n] * m[n];
-              const double *cy = al[1][ay][by], *cz = al[2][az][bz];
+                Bx += cx[n] * m[n];
               for (int p = 0; p <= ay + by; p++)
                 for (int q = 0; q <= az + bz; q++)
                   C[p + q] += Bx * cy[p] * cz[q];
@@ -1273,6 +1273,10 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase, int nch = 1) {
   if (split_rows)
     parallel_for(t->ntasks, [&](int s) {
       const TaskDesc &k = t->tasks[s];
+      // general-path tasks stay whole: their kernels' cost is dominated by
+      // per-row set-up (the ellipsoid's row bounds), which a second pass
+      // repeats (measured on the triclinic workload: collocation 5.9 ms
+      // whole, 7.4 ms split)
       if ((k.flags & (TF_SKIP | TF_GENERAL)) != 0)
         return;
       double fac = 1.0;

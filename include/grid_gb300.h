@@ -366,10 +366,10 @@ void grid_gb300_set_tensor_integrate(const grid_gb300_task_list *task_list, int 
 void grid_gb300_set_tensor_collocate(const grid_gb300_task_list *task_list, int enable);
 /* Mixed mode: 1 (default) splits every orthorhombic double-float task by
  * rows.  The rows (j, k) farther from the Gaussian product's x axis than the
- * radius where the task's contribution bound falls to the mixed threshold
- * run in FP32 (a second, FP32 pass over the task), the rows inside stay
- * double-float; 0 keeps every task whole in its class.  No counterpart in
- * CP2K. */
+ * radius where the task's contribution bound falls to a third of the mixed
+ * threshold run in FP32 (a second, FP32 pass over the task), the rows inside
+ * stay double-float; 0 keeps every task whole in its class.  General-path
+ * tasks stay whole.  No counterpart in CP2K. */
 void grid_gb300_set_row_split(const grid_gb300_task_list *task_list, int enable);
 /* The row split of a density collocation (no derivatives) in the mixed mode
  * at the current threshold: the share of tasks split, and the share of grid
