@@ -15,8 +15,7 @@
 // one left (the work counter and error word are reset by the call itself),
 // and two calls whose kernels overlap on the GPU (different streams without
 // ordering) race on it.  The first call on a device resolves the array's
-// device address with cudaGetSymbolAddress, so that first call should come
-// before any stream capture.
+// device address with cudaGetSymbolAddress and keeps it.
 //
 // Errors are found on the host before anything is copied or launched: the
 // scratch layout, the coefficient kernel's and the grid kernel's shared-
