@@ -958,22 +958,32 @@ __global__ void __launch_bounds__(128) integrate_ortho_tc(GridArgs a, int wmax) 
         }
       }
       float c[4] = {0.f, 0.f, 0.f, 0.f};
+      // the tile's x range: the union of its rows' ranges (short rows of the
+      // sphere's outer planes need fewer steps than the cube's width)
+      int xmn = 1 << 20, xmx = -(1 << 20);
+#pragma unroll
+      for (int h = 0; h < 2; h++)
+        if (rv[h]) {
+          xmn = min(xmn, xs[h]);
+          xmx = max(xmx, xe[h]);
+        }
       // the row look-ups above diverge; mma.sync.aligned needs the whole warp
-      // converged
-      __syncwarp();
+      // converged (the reductions reconverge it)
+      xmn = max(__reduce_min_sync(FULL, xmn), cg.x_lo);
+      xmx = min(__reduce_max_sync(FULL, xmx), cg.x_hi);
       // x steps counted up front: written as a loop on xb <= x_hi, this
       // kernel ran a single step under nvcc 13.0 (measured, lp <= 6 tasks of
       // 12 and more x points)
-      const int nxs = (cg.x_hi - cg.x_lo + 8) >> 3;
+      const int nxs = xmx >= xmn ? (xmx - xmn + 8) >> 3 : 0;
 #pragma unroll 1
       for (int xs8 = 0; xs8 < nxs; xs8++) {
-        const int xb = cg.x_lo + 8 * xs8;
+        const int xb = xmn + 8 * xs8;
         float av[4];
         float2 bv[2];
 #pragma unroll
         for (int s2 = 0; s2 < 2; s2++) {
           const int x = xb + tq + 4 * s2;
-          const bool xin = x <= cg.x_hi;
+          const bool xin = x <= xmx;
           const int mx = xin ? map[x + cg.cmax] : 0;
           bv[s2] = xin ? pxs[(x + cg.cmax) * 8 + grp] : make_float2(0.f, 0.f);
 #pragma unroll
