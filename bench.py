@@ -315,8 +315,10 @@ def roofline_objects(per, phase_points, field_points, peaks, peak_kind, fp_peak,
     else:
         # FP32 kernels of the mixed mode read the dense high words (4 B)
         bpp = 4.0 if (arith == "mixed" and ("<float" in dom or "_tc<" in dom)) else 8.0
+    # the kernel's share of the phase's visited points (all its launches of
+    # a step), spread over its launches per step
     share = d["points"] / max(phase_points[d["phase"]], 1.0)
-    alg_bytes = bpp * field_points * share
+    alg_bytes = bpp * field_points * share / (d["launches"] / 3.0)
     alg_flops = d["flops"] / d["launches"]
     gbs = alg_bytes / (avg_ms * 1e-3) / 1e9
     tf = alg_flops / (avg_ms * 1e-3) / 1e12
