@@ -1971,6 +1971,38 @@ template <typename V> static unsigned long long fnv_bytes(const V &v) {
   return h;
 }
 
+GB300_API double grid_gb300_row_split_radius2(int la_min, int la_max, int lb_min, int lb_max,
+                                              double zeta, double zetb, const double *rab,
+                                              double radius, int same_atom, int dla, int dlb,
+                                              double tau, double *outside) {
+  if (la_min < 0 || la_max < la_min || lb_min < 0 || lb_max < lb_min || la_max > GB300_LMAX ||
+      lb_max > GB300_LMAX || !(zeta > 0.0) || !(zetb > 0.0) || !(radius > 0.0) || dla < 0 ||
+      dlb < 0)
+    fail("grid_gb300_row_split_radius2: invalid arguments");
+  TaskDesc d{};
+  d.la_min = (int8_t)la_min;
+  d.la_max = (int8_t)la_max;
+  d.lb_min = (int8_t)lb_min;
+  d.lb_max = (int8_t)lb_max;
+  d.zeta = zeta;
+  d.zetb = zetb;
+  d.zetp = zeta + zetb;
+  double r2 = 0.0;
+  for (int i = 0; i < 3; i++) {
+    d.rab[i] = rab[i];
+    r2 += rab[i] * rab[i];
+  }
+  d.prefexp = exp(-zeta * zetb / d.zetp * r2);
+  d.radius = radius;
+  d.iatom = 0;
+  d.jatom = same_atom ? 0 : 1;
+  double out = 0.0;
+  const float c2 = core_radius2(d, dla, dlb, tau, &out);
+  if (outside)
+    *outside = out;
+  return (double)c2;
+}
+
 GB300_API void grid_gb300_host_digest(
     const bool orthorhombic, const int ntasks, const int nlevels, const int natoms,
     const int nkinds, const int nblocks, const int *block_offsets, const double *atom_positions,

@@ -377,6 +377,18 @@ void grid_gb300_set_row_split(const grid_gb300_task_list *task_list, int enable)
  * tasks, the latter estimated from the cylinder's volume share). */
 void grid_gb300_row_split_stats(const grid_gb300_task_list *task_list,
                                 double *frac_tasks_split, double *frac_points_fp32);
+/* The row split's core for one primitive pair (host only, no GPU; for tests
+ * and tuning): the squared radius (bohr^2) of the cylinder around the
+ * Gaussian product's x axis outside which every row's contributions are at
+ * most tau for density-matrix entries of magnitude <= 1 (the factor 2 of
+ * pairs of different atoms included), with the l ranges raised by dla, dlb
+ * (the derivatives of a call); *outside receives the share of the sphere's
+ * points outside it.  Returns 3e38 when the pair stays whole.  Aborts on
+ * invalid arguments. */
+double grid_gb300_row_split_radius2(int la_min, int la_max, int lb_min, int lb_max,
+                                    double zeta, double zetb, const double *rab,
+                                    double radius, int same_atom, int dla, int dlb,
+                                    double tau, double *outside);
 /* C_ab <-> C_xyz change of basis of the coefficient and post kernels: 0 the
  * direct gather over all (a, b) pairs, 1 the staged per-direction
  * contractions (x, then y, then z), -1 (default) staged in the coefficient
