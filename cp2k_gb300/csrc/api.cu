@@ -1522,8 +1522,6 @@ static void grid_launch(TaskList *t, const Queue &q, int phase, int arith, const
   // mode's FP32 class (contributions bounded by the threshold) takes it,
   // plain FP32 mode keeps the CUDA-core kernels' 24
   cfg.tensor_coll = t->tc_collocate && t->precision == GRID_GB300_MIXED;
-  if (q.side != 0) // a split task's rows are ranges of the point lists
-    cfg.variant = 1;
   LaunchRecord rec;
   const bool timed = t->launch_timing && !t->capturing;
   if (timed) {

@@ -250,7 +250,10 @@ __device__ __forceinline__ CubeGeo cube_geo(const SphereHdr &H, const int16_t *s
 // ------------------------------------------------------------------------
 // collocate, orthorhombic
 // ------------------------------------------------------------------------
-template <typename N, int LPB>
+// SPLIT: the launch runs one side of split tasks (a.core_side), whose rows
+// are limited per plane; a template flag, so that whole-task launches keep
+// the plain row loop (this kernel is bound by instruction issue)
+template <typename N, int LPB, bool SPLIT = false>
 __global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
   using T = typename Num<N>::T;
   using M = Num<N>;
@@ -313,6 +316,7 @@ __global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
     float *glo = a.grids_lo[d.level];
     const size_t nx = L.npts_local[0], nxy = nx * L.npts_local[1];
     const bool lane_on = cg.grp < cg.G;
+    const float r2 = SPLIT ? a.core_r2[t] : kCoreAll;
 
     for (int xc = cg.x_lo; xc <= cg.x_hi; xc += cg.SW) {
       const int cx = xc + cg.sub;
@@ -354,11 +358,27 @@ __global__ void __launch_bounds__(128) collocate_ortho(GridArgs a, int wmax) {
         const size_t zoff = (size_t)map[2 * cg.w + k + cg.cmax] * nxy;
         // rows of this lane's x on the plane: j in [jlo, jhi]
         const int JJ = xin ? (int)cg.jx[kk * cg.NX + (cx <= 0 ? -cx : cx - 1)] : -1;
-        const int jlo = -JJ, jhi = JJ + 1, jend = 1 - js;
+        int jlo = -JJ, jhi = JJ + 1, xlo = 1, xhi = 0; // rows [xlo, xhi] left out
+        const int jend = 1 - js;
+        if constexpr (SPLIT) { // the rows inside the cylinder, or those outside
+          int clo, chi;
+          core_rows(r2, d, L, k, clo, chi);
+          if (a.core_side == 1) {
+            jlo = max(jlo, clo);
+            jhi = min(jhi, chi);
+          } else {
+            xlo = clo;
+            xhi = chi;
+          }
+        }
         for (int j = js + cg.grp; j <= jend; j += 2 * cg.G) {
           const int j2 = j + cg.G;
-          const bool in1 = j >= jlo && j <= jhi;
-          const bool in2 = j2 >= jlo && j2 <= jhi;
+          bool in1 = j >= jlo && j <= jhi;
+          bool in2 = j2 >= jlo && j2 <= jhi;
+          if constexpr (SPLIT) {
+            in1 = in1 && (j < xlo || j > xhi);
+            in2 = in2 && (j2 < xlo || j2 > xhi);
+          }
           if (!(in1 || in2))
             continue;
           const int j2c = j2 <= jend ? j2 : jend;
@@ -1331,7 +1351,10 @@ __global__ void __launch_bounds__(128) collocate_ortho_tc(GridArgs a, int wmax) 
 template <typename N, int LPB>
 static void launch_ortho_t(const GridArgs &a, bool collocate, int wmax, LaunchCfg &cfg,
                            cudaStream_t s) {
-  const bool pl = collocate && cfg.variant == 1;
+  // split tasks' sides: the row walk has an FP32 instance for them, the
+  // other arithmetics take the point lists
+  const bool split = a.core_side != 0;
+  const bool pl = collocate && (cfg.variant == 1 || (split && !std::is_same<N, float>::value));
   const size_t per_warp = pl ? OrthoSmem<N, LPB>::bytes_coll_pl(wmax)
                           : collocate ? OrthoSmem<N, LPB>::bytes_coll(wmax)
                                       : OrthoSmem<N, LPB>::bytes_int(wmax);
@@ -1341,7 +1364,9 @@ static void launch_ortho_t(const GridArgs &a, bool collocate, int wmax, LaunchCf
   if (cfg.warps > 0 && cfg.warps < nw)
     nw = cfg.warps;
   const size_t smem = nw * per_warp;
-  const void *k = pl          ? (const void *)collocate_ortho_pl<N, LPB>
+  const bool rw_split = collocate && !pl && split; // FP32 only, see above
+  const void *k = pl         ? (const void *)collocate_ortho_pl<N, LPB>
+                  : rw_split ? (const void *)collocate_ortho<N, LPB, std::is_same<N, float>::value>
                   : collocate ? (const void *)collocate_ortho<N, LPB>
                               : (const void *)integrate_ortho<N, LPB>;
   set_smem((const void *)k, smem);
@@ -1350,6 +1375,8 @@ static void launch_ortho_t(const GridArgs &a, bool collocate, int wmax, LaunchCf
   cfg.blocks = nb;
   if (pl)
     collocate_ortho_pl<N, LPB><<<nb, 32 * nw, smem, s>>>(a, wmax);
+  else if (rw_split)
+    collocate_ortho<N, LPB, std::is_same<N, float>::value><<<nb, 32 * nw, smem, s>>>(a, wmax);
   else if (collocate)
     collocate_ortho<N, LPB><<<nb, 32 * nw, smem, s>>>(a, wmax);
   else
