@@ -943,11 +943,16 @@ __global__ void __launch_bounds__(128) integrate_ortho_tc(GridArgs a, int wmax) 
 #pragma unroll
       for (int e = 0; e < NT; e++)
         acc[s2][e] = 0.f;
+    // x indices of the grid: linear over the cube's x range unless the cube
+    // wraps around the periodic grid there (then through the map)
+    const int mx0 = map[cg.cmax];
+    const bool linx = map[cg.x_hi + cg.cmax] - map[cg.x_lo + cg.cmax] == cg.x_hi - cg.x_lo;
     int pc = 0; // plane cursor (rows only grow)
     for (int rb = 0; rb < R; rb += 16) {
-      // the two rows of this lane in the tile
+      // the two rows of this lane in the tile; rows past the end get an
+      // empty x range [1 << 28, 1 << 28 - 1] for the unsigned range test
       int kr[2], jr[2], xs[2], xe[2];
-      size_t base[2];
+      const float *rowp[2];
       bool rv[2];
 #pragma unroll
       for (int h = 0; h < 2; h++) {
@@ -955,9 +960,9 @@ __global__ void __launch_bounds__(128) integrate_ortho_tc(GridArgs a, int wmax) 
         rv[h] = r < R;
         kr[h] = k_lo;
         jr[h] = 0;
-        xs[h] = 1;
-        xe[h] = 0;
-        base[h] = 0;
+        xs[h] = 1 << 28;
+        xe[h] = (1 << 28) - 1;
+        rowp[h] = grid;
         if (rv[h]) {
           int p = pc;
           while (starts[p + 1] <= r)
@@ -973,7 +978,7 @@ __global__ void __launch_bounds__(128) integrate_ortho_tc(GridArgs a, int wmax) 
           jr[h] = j;
           xs[h] = ist;
           xe[h] = 1 - ist;
-          base[h] = (size_t)map[2 * cg.w + k + cg.cmax] * nxy +
+          rowp[h] = grid + (size_t)map[2 * cg.w + k + cg.cmax] * nxy +
                     (size_t)map[cg.w + j + cg.cmax] * nx;
         }
       }
@@ -1004,19 +1009,23 @@ __global__ void __launch_bounds__(128) integrate_ortho_tc(GridArgs a, int wmax) 
         for (int s2 = 0; s2 < 2; s2++) {
           const int x = xb + tq + 4 * s2;
           const bool xin = x <= xmx;
-          const int mx = xin ? map[x + cg.cmax] : 0;
+          int mx = mx0 + x;
+          if (!linx) // warp-uniform
+            mx = xin ? map[x + cg.cmax] : 0;
           bv[s2] = xin ? pxs[(x + cg.cmax) * 8 + grp] : make_float2(0.f, 0.f);
 #pragma unroll
-          for (int h = 0; h < 2; h++) {
-            const bool in = rv[h] && xin && x >= xs[h] && x <= xe[h];
-            av[h + 2 * s2] = in ? __ldg(grid + base[h] + mx) : 0.f;
+          for (int h = 0; h < 2; h++) { // x in [xs, xe]: the row's points (xe <= xmx)
+            const bool in = (unsigned)(x - xs[h]) <= (unsigned)(xe[h] - xs[h]);
+            av[h + 2 * s2] = in ? __ldg(rowp[h] + mx) : 0.f;
           }
         }
+        // TF32 high part by truncation (the low 13 bits cleared), low part
+        // the exact remainder (the tensor cores read its top 19 bits)
         unsigned ahi[4], alo[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-          ahi[i] = f2tf32(av[i]);
-          alo[i] = f2tf32(av[i] - __uint_as_float(ahi[i]));
+          ahi[i] = __float_as_uint(av[i]) & 0xffffe000u;
+          alo[i] = __float_as_uint(av[i] - __uint_as_float(ahi[i]));
         }
         const unsigned b0h = __float_as_uint(bv[0].x), b1h = __float_as_uint(bv[1].x);
         const unsigned b0l = __float_as_uint(bv[0].y), b1l = __float_as_uint(bv[1].y);
