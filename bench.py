@@ -245,8 +245,10 @@ def measure_peak(torch, dtype, n):
 # launch split; the bench cannot run ncu itself, and divides by its own
 # launches per step.  Keys: kernel label as in "roofline.kernel".
 NCU_TRAFFIC_PER_STEP = {
-    "integrate_ortho_tc<4>": (2.632 + 0.024 + 25.168 + 0.098 + 178.044 + 47.542
-                              + 114.334 + 19.523) * 1e6,
+    "integrate_ortho_tc<4>": (2.641 + 0.024 + 25.110 + 0.087 + 176.468 + 47.204
+                              + 114.270 + 19.439) * 1e6,
+    "collocate_ortho<float,4>": (3.380 + 0.050 + 32.582 + 7.295 + 261.180 + 1072.604
+                                 + 143.043 + 393.604) * 1e6,
     "integrate_ortho<double,4>": ((35.777 + 0.760) + (594.138 + 123.159)) * 1e6,
 }
 
@@ -311,7 +313,8 @@ def roofline_objects(per, phase_points, field_points, peaks, peak_kind, fp_peak,
     d = per[dom]
     avg_ms = float(np.mean(d["ms"]))
     if d["phase"] == 0:
-        bpp = 12.0 if arith == "mixed" else 8.0
+        # FP64 grid RMW; the double-float class adds its FP32 low words
+        bpp = 12.0 if (arith == "mixed" and "<dfloat" in dom) else 8.0
     else:
         # FP32 kernels of the mixed mode read the dense high words (4 B)
         bpp = 4.0 if (arith == "mixed" and ("<float" in dom or "_tc<" in dom)) else 8.0
