@@ -1,7 +1,10 @@
 // Multigrid transfer between the realspace level grids and the plane-wave
-// grid, kept on the device, so that collocate -> FFT / Poisson -> integrate
-// stays in HBM (CP2K: src/pw_env/rs_pw_interface.F:64-136 density_rs2pw and
-// :151-228 potential_pw2rs with the default pw_interp, replicated grids; the
+// grid, and the periodic Hartree solve between them, kept on the device, so
+// that collocate -> FFT -> Poisson -> integrate stays in HBM (CP2K:
+// src/pw_env/rs_pw_interface.F:64-136 density_rs2pw and :151-228
+// potential_pw2rs with the default pw_interp, replicated grids;
+// src/pw/pw_poisson_types.F:316-320 the periodic influence function 4 pi /
+// |G|^2 and src/pw/pw_poisson_methods.F:363-367 the Hartree energy; the
 // reference's GPU FFT helpers are src/pw/gpu/pw_gpu_kernels.cu).
 //
 // Conventions of the reference's pw layer, restated:
@@ -115,6 +118,50 @@ __global__ void spectrum_cut(const double2 *__restrict__ fine, Box fb, double2 *
   }
 }
 
+// 2 pi times the reciprocal vectors b_d (rows), b_d . a_e = delta_de
+struct Recip {
+  double b[3][3];
+};
+
+// v(G) = 4 pi rho(G) / |G|^2, zero at G = 0; the sum of |rho(G)|^2 4 pi /
+// |G|^2 into esum (when given), by block partial sums
+__global__ void poisson_kernel(const double2 *rho, double2 *v, Box bx, // may alias
+                               Recip r, double *esum) {
+  __shared__ double part[8];
+  const size_t n = (size_t)bx.n[0] * bx.n[1] * bx.n[2];
+  double local = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int ax = (int)(i % bx.n[0]), ay = (int)((i / bx.n[0]) % bx.n[1]),
+              az = (int)(i / ((size_t)bx.n[0] * bx.n[1]));
+    const double f[3] = {(double)freq_of(ax, bx.n[0]), (double)freq_of(ay, bx.n[1]),
+                         (double)freq_of(az, bx.n[2])};
+    double g2 = 0.0;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const double gc = f[0] * r.b[0][c] + f[1] * r.b[1][c] + f[2] * r.b[2][c];
+      g2 += gc * gc;
+    }
+    const double2 p = rho[i];
+    const double k = g2 > 0.0 ? 4.0 * M_PI / g2 : 0.0;
+    v[i] = make_double2(k * p.x, k * p.y);
+    local += k * (p.x * p.x + p.y * p.y);
+  }
+  if (!esum)
+    return;
+  for (int o = 16; o > 0; o >>= 1)
+    local += __shfl_xor_sync(0xffffffffu, local, o);
+  if ((threadIdx.x & 31) == 0)
+    part[threadIdx.x >> 5] = local;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sacc = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++)
+      sacc += part[w];
+    atomicAdd(esum, sacc);
+  }
+}
+
 int blocks_for(size_t n) {
   const size_t b = (n + 255) / 256;
   return (int)(b < 152 * 8 ? (b ? b : 1) : 152 * 8);
@@ -127,6 +174,7 @@ using namespace gb300;
 
 struct grid_gb300_pw_transfer {
   int nlevels = 0;
+  double *d_esum = nullptr;      // Hartree energy sum of the Poisson solve
   std::vector<Box> box;          // per level
   std::vector<size_t> npts;      // per level
   std::vector<cufftHandle> plan; // per level, Z2Z
@@ -165,6 +213,8 @@ GB300_API void grid_gb300_pw_free(grid_gb300_pw_transfer *h) {
     cufftDestroy(h->plan[l]);
     cudaFree(h->work[l]);
   }
+  if (h->d_esum)
+    cudaFree(h->d_esum);
   delete h;
 }
 
@@ -226,3 +276,54 @@ GB300_API void grid_gb300_pw_potential_pw2rs(grid_gb300_pw_transfer *h, const do
   }
   CKC(cudaGetLastError());
 }
+
+GB300_API void grid_gb300_pw_poisson(grid_gb300_pw_transfer *h, const double *dh,
+                                     const void *rho_gspace, void *v_gspace, double *v_rspace,
+                                     double *energy, void *stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  const Box &b = h->box[0];
+  // hmat: columns are the cell vectors a_d = n_d dh[d][:]
+  double hm[3][3];
+  for (int c = 0; c < 3; c++)
+    for (int d = 0; d < 3; d++)
+      hm[c][d] = b.n[d] * dh[3 * d + c];
+  const double det = hm[0][0] * (hm[1][1] * hm[2][2] - hm[1][2] * hm[2][1]) -
+                     hm[0][1] * (hm[1][0] * hm[2][2] - hm[1][2] * hm[2][0]) +
+                     hm[0][2] * (hm[1][0] * hm[2][1] - hm[1][1] * hm[2][0]);
+  if (!(fabs(det) > 0.0))
+    pw_fail("Poisson solve: singular cell", 0);
+  // inverse by cofactors: inv[e][c] = cof[c][e] / det; 2 pi b_e = 2 pi inv[e][:]
+  Recip r;
+  for (int e = 0; e < 3; e++)
+    for (int c = 0; c < 3; c++) {
+      const int c1 = (c + 1) % 3, c2 = (c + 2) % 3, e1 = (e + 1) % 3, e2 = (e + 2) % 3;
+      const double cof = hm[c1][e1] * hm[c2][e2] - hm[c1][e2] * hm[c2][e1];
+      r.b[e][c] = 2.0 * M_PI * cof / det;
+    }
+  if (energy) {
+    if (!h->d_esum)
+      CKC(cudaMalloc((void **)&h->d_esum, sizeof(double)));
+    CKC(cudaMemsetAsync(h->d_esum, 0, sizeof(double), s));
+  }
+  poisson_kernel<<<blocks_for(h->npts[0]), 256, 0, s>>>(
+      (const double2 *)rho_gspace, (double2 *)v_gspace, b, r, energy ? h->d_esum : nullptr);
+  count_launch();
+  CKC(cudaGetLastError());
+  if (v_rspace) { // G space -> realspace on the finest grid (no scale)
+    double2 *w = h->work[0];
+    CKF(cufftSetStream(h->plan[0], s));
+    CKC(cudaMemcpyAsync(w, v_gspace, sizeof(double2) * h->npts[0], cudaMemcpyDeviceToDevice, s));
+    CKF(cufftExecZ2Z(h->plan[0], (cufftDoubleComplex *)w, (cufftDoubleComplex *)w,
+                     CUFFT_INVERSE));
+    complex_to_real<<<blocks_for(h->npts[0]), 256, 0, s>>>(w, v_rspace, h->npts[0], 1.0);
+    count_launch();
+    CKC(cudaGetLastError());
+  }
+  if (energy) {
+    double sum = 0.0;
+    CKC(cudaMemcpyAsync(&sum, h->d_esum, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CKC(cudaStreamSynchronize(s));
+    *energy = 0.5 * fabs(det) * sum;
+  }
+}
+

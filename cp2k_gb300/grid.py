@@ -577,6 +577,7 @@ class PwTransfer:
             L.grid_gb300_pw_free.argtypes = [vp]
             L.grid_gb300_pw_density_rs2pw.argtypes = [vp, vp, vp, vp, vp]
             L.grid_gb300_pw_potential_pw2rs.argtypes = [vp, vp, vp, vp]
+            L.grid_gb300_pw_poisson.argtypes = [vp, vp, vp, vp, vp, vp, vp]
             L._pw_bound = True
         self.npts = [tuple(int(x) for x in n) for n in npts]
         arr = np.ascontiguousarray(np.array(self.npts, np.int32).ravel())
@@ -593,6 +594,18 @@ class PwTransfer:
         ptrs = (C.c_void_p * len(rs_grids))(*[g.data_ptr() for g in rs_grids])
         lib().grid_gb300_pw_potential_pw2rs(self.h, C.c_void_p(v_rspace.data_ptr()),
                                             C.cast(ptrs, C.c_void_p), _stream(stream))
+
+    def poisson(self, dh, rho_gspace, v_gspace, v_rspace=None, energy=False, stream=None):
+        """Periodic Hartree solve in G space (grid_gb300_pw_poisson), with v in
+        real space when a tensor is given; returns the Hartree energy when
+        asked for (synchronising)."""
+        dh = np.ascontiguousarray(dh, np.float64).reshape(9)
+        e = C.c_double(0.0)
+        lib().grid_gb300_pw_poisson(
+            self.h, _p(dh), C.c_void_p(rho_gspace.data_ptr()), C.c_void_p(v_gspace.data_ptr()),
+            C.c_void_p(v_rspace.data_ptr()) if v_rspace is not None else None,
+            C.byref(e) if energy else None, _stream(stream))
+        return e.value if energy else None
 
     def close(self):
         if self.h:

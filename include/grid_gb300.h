@@ -574,6 +574,20 @@ void grid_gb300_pw_density_rs2pw(grid_gb300_pw_transfer *handle, const double *c
  * frequencies, transform back and scale by dvol(level) / dvol(finest). */
 void grid_gb300_pw_potential_pw2rs(grid_gb300_pw_transfer *handle, const double *v_rspace,
                                    double *const *rs_grids, void *stream);
+/* Periodic Hartree solve on the finest grid's G-space box (the layout of
+ * rho_gspace above): v(G) = 4 pi rho(G) / |G|^2, v(0) = 0, with G = 2 pi
+ * sum_d f_d b_d over the grid's frequencies and b_d the reciprocal vectors
+ * of the cell whose vectors are a_d = n_d dh[d][:] (dh: the finest level's
+ * spacing matrix, row d the step along lattice vector d; n_d its points)
+ * (src/pw/pw_poisson_types.F:316-320, PERIODIC3D).  rho_gspace and v_gspace
+ * may be the same buffer.  v_rspace (may be NULL) receives v on the finest
+ * grid in real space, ready for grid_gb300_pw_potential_pw2rs.  energy
+ * (host, may be NULL) receives the Hartree energy 0.5 Omega sum
+ * conj(rho(G)) v(G) (src/pw/pw_poisson_methods.F:363-367); asking for it
+ * synchronises the stream. */
+void grid_gb300_pw_poisson(grid_gb300_pw_transfer *handle, const double *dh,
+                           const void *rho_gspace, void *v_gspace, double *v_rspace,
+                           double *energy, void *stream);
 
 /* Last error message recorded by the library ("" if none). */
 const char *grid_gb300_last_error(void);

@@ -12,6 +12,10 @@ the default interpolation (pw_interp):
   * potential_pw2rs (:151-228): the finest level copies the potential;
     coarser levels take its G-space coefficients at their frequencies
     (pw_copy), transform back and scale by dvol(level) / dvol(finest).
+  * poisson: the periodic Hartree solve in G space
+    (src/pw/pw_poisson_types.F:316-320, influence function 4 pi / |G|^2 with
+    G = 0 set to zero; src/pw/pw_poisson_methods.F:363-367, the Hartree
+    energy 0.5 * pw_integral_ab(rho_G, v_G) = 0.5 Omega sum conj(rho_G) v_G).
 A grid of n points holds the frequencies -n/2 .. n/2 - 1
 (src/pw/pw_grid_info.F:247-254).  Grids are [nz][ny][nx] arrays (x
 fastest), given flat or shaped.
@@ -58,3 +62,36 @@ def potential_pw2rs(npts, v_rspace):
         r = np.real(np.fft.ifftn(c) * c.size)
         out.append(r * (v.size / r.size))
     return out
+
+
+def cell_of(dh, npts):
+    """hmat (columns: the cell vectors) of a grid with spacing matrix dh (row
+    d: the step along lattice vector d) and npts = (nx, ny, nz) points."""
+    dh = np.asarray(dh, np.float64).reshape(3, 3)
+    return np.stack([npts[d] * dh[d] for d in range(3)], axis=1)
+
+
+def g_vectors(dh, npts):
+    """Cartesian G vectors [nz][ny][nx][3] of the grid's frequencies:
+    G = 2 pi sum_d f_d b_d, b_d the rows of inv(hmat) (b_d . a_e = delta)."""
+    hinv = np.linalg.inv(cell_of(dh, npts))
+    f = [np.where(np.arange(n) < (n + 1) // 2, np.arange(n), np.arange(n) - n) for n in npts]
+    fz, fy, fx = np.meshgrid(f[2], f[1], f[0], indexing="ij")
+    return 2.0 * np.pi * (fx[..., None] * hinv[0] + fy[..., None] * hinv[1]
+                          + fz[..., None] * hinv[2])
+
+
+def poisson(rho_g, dh, npts):
+    """v(G) = 4 pi rho(G) / |G|^2 (zero at G = 0) and the Hartree energy
+    0.5 Omega sum conj(rho(G)) v(G)."""
+    g = g_vectors(dh, npts)
+    g2 = (g ** 2).sum(-1)
+    rho_g = np.asarray(rho_g, np.complex128).reshape(g2.shape)
+    inf = np.zeros_like(g2)
+    nz = g2 > 0
+    inf[nz] = 4.0 * np.pi / g2[nz]
+    v = rho_g * inf
+    omega = abs(np.linalg.det(cell_of(dh, npts)))
+    e = 0.5 * omega * float(np.real(np.sum(np.conj(rho_g) * v)))
+    return v, e
+
