@@ -20,6 +20,8 @@ grid_integrate_task_list (hab only), as one SCF iteration does.
              roofline_fp64 the same for the FP64 step;
   mixed_no_row_split / mixed_model_schedule / mixed_one_queue_stream
              the mixed step with one feature switched back (diagnostics);
+  hartree_step_on_device  collocate -> plane waves -> Hartree potential ->
+             level grids -> integrate, every buffer on the device;
   cpu_baseline  whole SCF steps of the oracle (FP64 C restatement of CP2K's
              REF backend) on all host cores;
   triclinic_256atoms_forces_virial, c5_6144atoms_forces
@@ -366,6 +368,43 @@ def errors_vs(rho, hab, rho_ref, hab_ref, V, inp, f=None, f_ref=None, vir=None, 
     return out
 
 
+def hartree_step(torch, G, tl, inp, pab, grids, hab, stream, flush, nsteps):
+    """One Hartree step kept on the device, mixed mode: collocate ->
+    density_rs2pw -> periodic Poisson solve -> potential_pw2rs -> integrate
+    (CUDA events on the stream, L2 flushed before each step), with the share
+    of the plane-wave part."""
+    npts = [tuple(int(x) for x in n) for n in inp.npts_local]
+    dh = np.asarray(inp.dh[0], np.float64).reshape(3, 3)
+    pw = G.PwTransfer(npts)
+    n0 = int(np.prod(npts[0]))
+    dev = grids[0].device
+    g = torch.empty(2 * n0, dtype=torch.float64, device=dev)
+    tl.set_precision(G.MIXED)
+    times, pw_times = [], []
+    for i in range(nsteps + 1):
+        flush.zero_()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            e[0].record(stream)
+            tl.collocate_device(100, pab, grids, stream=stream)
+            e[1].record(stream)
+            pw.density_rs2pw(grids, None, g, stream=stream)
+            pw.poisson(dh, g, g, stream=stream)
+            pw.potential_g2rs(g, grids, stream=stream)
+            e[2].record(stream)
+            tl.integrate_device(grids, hab, stream=stream)
+            e[3].record(stream)
+        torch.cuda.synchronize()
+        if i:
+            times.append(e[0].elapsed_time(e[3]))
+            pw_times.append(e[1].elapsed_time(e[2]))
+    pw.close()
+    return {"ms_per_step": float(np.mean(times)), "plane_wave_ms": float(np.mean(pw_times)),
+            "steps": "collocate, density_rs2pw, Poisson (Hartree) in G space, "
+                     "potential_g2rs, integrate; all buffers on the device"}
+
+
 def secondary_case(torch, G, W, name, forces, virial, nsteps, cpu_steps, flush):
     """Mixed and FP64 step times (device-resident, default launch shapes, size
     schedule) of another workload, with forces / virial as its configuration
@@ -547,6 +586,8 @@ def gpu_arm(args, world, rank, local):
     t_fp32 = run_steps(G.FP32, sched_mixed, max(1, min(args.steps, 5)))
     rho32 = [g.cpu().numpy() for g in grids]
     hab32 = hab.cpu().numpy()
+    hartree = hartree_step(torch, G, tl, inp, pab, grids, hab, stream, flush,
+                           max(1, min(args.steps, 5)))
 
     ms_mixed = max_over_ranks(float(np.mean(t_mixed)), world)
     ms_model = max_over_ranks(float(np.mean(t_model)), world) if t_model else None
@@ -627,6 +668,7 @@ def gpu_arm(args, world, rank, local):
                                                                  world),
             "mixed_no_row_split_ms_per_step": max_over_ranks(float(np.mean(t_no_row_split)),
                                                              world),
+            "hartree_step_on_device": hartree,
             "row_split": {"tasks_split": row_split_share[0],
                           "fp32_share_of_points": row_split_share[1],
                           "fp32_class_share_of_points": row_split_share[2]},

@@ -118,6 +118,22 @@ __global__ void spectrum_cut(const double2 *__restrict__ fine, Box fb, double2 *
   }
 }
 
+// out = the spectrum of Re(inverse transform of v): (v(f) + conj(v(-f))) / 2,
+// -f taken on the same grid (the Nyquist frequency -n/2 is its own partner)
+__global__ void hermitian_part(const double2 *__restrict__ v, double2 *__restrict__ out, Box b) {
+  const size_t n = (size_t)b.n[0] * b.n[1] * b.n[2];
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int ax = (int)(i % b.n[0]), ay = (int)((i / b.n[0]) % b.n[1]),
+              az = (int)(i / ((size_t)b.n[0] * b.n[1]));
+    const int px = index_of(-freq_of(ax, b.n[0]), b.n[0]) % b.n[0];
+    const int py = index_of(-freq_of(ay, b.n[1]), b.n[1]) % b.n[1];
+    const int pz = index_of(-freq_of(az, b.n[2]), b.n[2]) % b.n[2];
+    const double2 a = v[i], c = v[((size_t)pz * b.n[1] + py) * b.n[0] + px];
+    out[i] = make_double2(0.5 * (a.x + c.x), 0.5 * (a.y - c.y));
+  }
+}
+
 // 2 pi times the reciprocal vectors b_d (rows), b_d . a_e = delta_de
 struct Recip {
   double b[3][3];
@@ -274,6 +290,36 @@ GB300_API void grid_gb300_pw_potential_pw2rs(grid_gb300_pw_transfer *h, const do
         w, rs_grids[l], h->npts[l], (double)h->npts[0] / (double)h->npts[l]);
     count_launch(2);
   }
+  CKC(cudaGetLastError());
+}
+
+GB300_API void grid_gb300_pw_potential_g2rs(grid_gb300_pw_transfer *h, const void *v_gspace,
+                                            double *const *rs_grids, void *stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  const int L = h->nlevels;
+  // the spectrum of the real potential on the finest grid (what
+  // potential_pw2rs's forward transform of it would give)
+  double2 *w0 = h->work[0];
+  hermitian_part<<<blocks_for(h->npts[0]), 256, 0, s>>>((const double2 *)v_gspace, w0, h->box[0]);
+  count_launch();
+  // coarser levels first (they read w0): the coefficients at their
+  // frequencies, as potential_pw2rs
+  for (int l = 1; l < L; l++) {
+    CKF(cufftSetStream(h->plan[l], s));
+    double2 *w = h->work[l];
+    spectrum_cut<<<blocks_for(h->npts[l]), 256, 0, s>>>(w0, h->box[0], w, h->box[l], 1.0);
+    CKF(cufftExecZ2Z(h->plan[l], (cufftDoubleComplex *)w, (cufftDoubleComplex *)w,
+                     CUFFT_INVERSE));
+    complex_to_real<<<blocks_for(h->npts[l]), 256, 0, s>>>(
+        w, rs_grids[l], h->npts[l], (double)h->npts[0] / (double)h->npts[l]);
+    count_launch(2);
+  }
+  // the finest level: back to real space (no scale)
+  CKF(cufftSetStream(h->plan[0], s));
+  CKF(cufftExecZ2Z(h->plan[0], (cufftDoubleComplex *)w0, (cufftDoubleComplex *)w0,
+                   CUFFT_INVERSE));
+  complex_to_real<<<blocks_for(h->npts[0]), 256, 0, s>>>(w0, rs_grids[0], h->npts[0], 1.0);
+  count_launch();
   CKC(cudaGetLastError());
 }
 

@@ -578,6 +578,7 @@ class PwTransfer:
             L.grid_gb300_pw_density_rs2pw.argtypes = [vp, vp, vp, vp, vp]
             L.grid_gb300_pw_potential_pw2rs.argtypes = [vp, vp, vp, vp]
             L.grid_gb300_pw_poisson.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+            L.grid_gb300_pw_potential_g2rs.argtypes = [vp, vp, vp, vp]
             L._pw_bound = True
         self.npts = [tuple(int(x) for x in n) for n in npts]
         arr = np.ascontiguousarray(np.array(self.npts, np.int32).ravel())
@@ -594,6 +595,13 @@ class PwTransfer:
         ptrs = (C.c_void_p * len(rs_grids))(*[g.data_ptr() for g in rs_grids])
         lib().grid_gb300_pw_potential_pw2rs(self.h, C.c_void_p(v_rspace.data_ptr()),
                                             C.cast(ptrs, C.c_void_p), _stream(stream))
+
+    def potential_g2rs(self, v_gspace, rs_grids, stream=None):
+        """The level grids from the finest grid's G-space coefficients
+        (grid_gb300_pw_potential_g2rs)."""
+        ptrs = (C.c_void_p * len(rs_grids))(*[g.data_ptr() for g in rs_grids])
+        lib().grid_gb300_pw_potential_g2rs(self.h, C.c_void_p(v_gspace.data_ptr()),
+                                           C.cast(ptrs, C.c_void_p), _stream(stream))
 
     def poisson(self, dh, rho_gspace, v_gspace, v_rspace=None, energy=False, stream=None):
         """Periodic Hartree solve in G space (grid_gb300_pw_poisson), with v in

@@ -574,6 +574,11 @@ void grid_gb300_pw_density_rs2pw(grid_gb300_pw_transfer *handle, const double *c
  * frequencies, transform back and scale by dvol(level) / dvol(finest). */
 void grid_gb300_pw_potential_pw2rs(grid_gb300_pw_transfer *handle, const double *v_rspace,
                                    double *const *rs_grids, void *stream);
+/* potential_pw2rs from the finest grid's G-space coefficients (the layout
+ * of rho_gspace above, e.g. grid_gb300_pw_poisson's v_gspace): the same
+ * level grids without the forward transform of the finest grid. */
+void grid_gb300_pw_potential_g2rs(grid_gb300_pw_transfer *handle, const void *v_gspace,
+                                  double *const *rs_grids, void *stream);
 /* Periodic Hartree solve on the finest grid's G-space box (the layout of
  * rho_gspace above): v(G) = 4 pi rho(G) / |G|^2, v(0) = 0, with G = 2 pi
  * sum_d f_d b_d over the grid's frequencies and b_d the reciprocal vectors

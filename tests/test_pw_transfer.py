@@ -142,5 +142,12 @@ def test_hartree_step_on_device():
     assert abs(e - e_h) <= 1e-10 * abs(e_h)
     h = hab.cpu().numpy()
     assert float(np.abs(h - hab_h).max()) <= 1e-10 * max(1.0, float(np.abs(hab_h).max()))
+    # the same potential on the level grids straight from v(G) (one FFT
+    # fewer than the host chain's real-space round trip: the same 1e-10)
+    lv = [torch.empty_like(x) for x in grids]
+    pw.potential_g2rs(g, lv)
+    torch.cuda.synchronize()
+    for a, b in zip(lv, V_l):
+        assert float(np.abs(a.cpu().numpy() - b.ravel()).max()) <= 1e-10 * float(np.abs(b).max())
     pw.close()
     tl.close()
