@@ -281,24 +281,29 @@ __device__ T cxyz_cab_term(const T *cxyz, const T *alpha, int la, int lb, int lp
   const T *az = alpha + ((size_t)(2 * nb + b.l[2]) * na + a.l[2]) * P;
   const int nx = a.l[0] + b.l[0] + 1, ny = a.l[1] + b.l[1] + 1, nz = a.l[2] + b.l[2] + 1;
   const int n = nx * ny * nz;
+  // the x terms of a C_xyz row as a running dot product (one fused
+  // multiply-add per term), folded in with alpha_y alpha_z at the row's end
+  using M = Num<T>;
   int px = 0, py = 0, pz = 0, row = cidx(0, 0, 0, lp);
-  T wyz = ay[0] * az[0];
-  T s = T(0);
+  T wyz = M::norm(ay[0] * az[0]);
+  T s = M::zero(), d = M::zero();
   for (int t = 0; t < n; t++) {
-    s += wyz * ax[px] * cxyz[row + px];
+    d = M::fma_acc(d, ax[px], cxyz[row + px]);
     if (++px == nx) {
+      s = M::fma_acc(s, wyz, M::norm(d));
+      d = M::zero();
       px = 0;
       if (++py == ny) {
         py = 0;
         ++pz;
       }
       if (pz < nz) {
-        wyz = ay[py] * az[pz];
+        wyz = M::norm(ay[py] * az[pz]);
         row = cidx(pz, py, 0, lp);
       }
     }
   }
-  return s;
+  return M::norm(s);
 }
 
 // General path: C_xyz (Cartesian, about P) <-> C_ijk (lattice indices).
