@@ -62,6 +62,8 @@ typedef struct {
       *block_num;                    /* [ntasks] */
   double *radius, *rab;              /* [ntasks], [ntasks][3] */
   double dh[WL_MAX_LEVELS][3][3], dh_inv[WL_MAX_LEVELS][3][3];
+  int nimg[3];  /* periodic images searched per cell vector: -nimg..nimg */
+  double rmax;  /* pair distance cut (bohr) */
 } wl_out;
 
 /* --------------------------------------------------------------- random -- */
@@ -220,6 +222,110 @@ static void random_orthogonal(int n, uint64_t *s, double *q) {
   }
 }
 
+/* The task arrays for the atom positions in o->atom_positions: every atom
+ * pair i <= j, every periodic image within rmax, every primitive pair that
+ * passes the prefactor screen, in that order.  Replaces any earlier arrays. */
+static void build_tasks(wl_out *o, const wl_params *p) {
+  const int na = o->natoms;
+  const int maxpgf_all = o->maxpgf_all;
+  void *old[] = {o->block_offsets, o->level, o->iatom, o->jatom, o->iset, o->jset,
+                 o->ipgf, o->jpgf, o->border_mask, o->block_num, o->radius, o->rab};
+  for (size_t q = 0; q < sizeof(old) / sizeof(old[0]); q++)
+    free(old[q]);
+  /* image range from the most diffuse possible product */
+  const double ln_eps = log(1.0 / p->eps);
+  const double rmax = sqrt(ln_eps / (0.5 * p->zet_min));
+  double cinv[3][3];
+  inv3(p->cell, cinv);
+  int nimg[3];
+  for (int d = 0; d < 3; d++) {
+    const double h = sqrt(cinv[0][d] * cinv[0][d] + cinv[1][d] * cinv[1][d] +
+                          cinv[2][d] * cinv[2][d]);
+    nimg[d] = (int)ceil(rmax * h) + 1;
+    o->nimg[d] = nimg[d];
+  }
+  o->rmax = rmax;
+  vec vi[9], vr = {0, 0, 0, sizeof(double)}, vrab = {0, 0, 0, 3 * sizeof(double)},
+             vblk = {0, 0, 0, sizeof(int)};
+  for (int q = 0; q < 9; q++) {
+    vi[q].p = NULL;
+    vi[q].n = vi[q].cap = 0;
+    vi[q].elem = sizeof(int);
+  }
+  long long offset = 0;
+  int nblocks = 0;
+  for (int i = 0; i < na; i++) {
+    const double *ra = &o->atom_positions[3 * i];
+    for (int j = i; j < na; j++) {
+      const double *rj = &o->atom_positions[3 * j];
+      int block = 0;
+      for (int n0i = -nimg[0]; n0i <= nimg[0]; n0i++)
+        for (int n1i = -nimg[1]; n1i <= nimg[1]; n1i++)
+          for (int n2i = -nimg[2]; n2i <= nimg[2]; n2i++) {
+            if (i == j) { /* same atom: image 0 and one of each +/- pair */
+              const int lex = n0i != 0 ? n0i : (n1i != 0 ? n1i : n2i);
+              if (lex < 0)
+                continue;
+            }
+            double rab[3];
+            for (int d = 0; d < 3; d++)
+              rab[d] = rj[d] - ra[d] + n0i * p->cell[0][d] + n1i * p->cell[1][d] +
+                       n2i * p->cell[2][d];
+            const double rab2 = rab[0] * rab[0] + rab[1] * rab[1] + rab[2] * rab[2];
+            if (rab2 > rmax * rmax)
+              continue;
+            for (int is = 0; is < o->nset[i]; is++)
+            for (int ip = 0; ip < o->npgf[o->set_off[i] + is]; ip++) {
+              const int gi = o->set_off[i] + is;
+              const double za = o->zet[(size_t)gi * maxpgf_all + ip];
+              for (int js = 0; js < o->nset[j]; js++)
+              for (int jp = 0; jp < o->npgf[o->set_off[j] + js]; jp++) {
+                const int gj = o->set_off[j] + js;
+                const double zb = o->zet[(size_t)gj * maxpgf_all + jp];
+                const double zetp = za + zb, f = zb / zetp;
+                const double pref = exp(-za * f * rab2);
+                if (!(pref > p->eps))
+                  continue;
+                double rp[3], rb[3];
+                for (int d = 0; d < 3; d++) {
+                  rp[d] = ra[d] + f * rab[d];
+                  rb[d] = ra[d] + rab[d];
+                }
+                const double radius = exp_radius_very_extended(
+                    o->lmax[gi], o->lmax[gj], ra, rb, rp, zetp, p->eps, pref);
+                if (!block) {
+                  block = ++nblocks;
+                  const int off = (int)offset;
+                  vpush(&vblk, &off);
+                  offset += (long long)o->nsgf[i] * o->nsgf[j];
+                }
+                const int v[9] = {grid_level(p, zetp), i + 1, j + 1, is + 1, js + 1,
+                                  ip + 1, jp + 1, 0, block};
+                for (int q = 0; q < 9; q++)
+                  vpush(&vi[q], &v[q]);
+                vpush(&vr, &radius);
+                vpush(&vrab, rab);
+              }
+            }
+          }
+    }
+  }
+  if (offset > 2147483647LL) {
+    fprintf(stderr, "workload: block buffer exceeds int offsets\n");
+    abort();
+  }
+  o->ntasks = (int)vr.n;
+  o->nblocks = nblocks;
+  o->buffer_size = offset;
+  o->block_offsets = vblk.p;
+  int **dst[9] = {&o->level, &o->iatom, &o->jatom, &o->iset, &o->jset,
+                  &o->ipgf, &o->jpgf, &o->border_mask, &o->block_num};
+  for (int q = 0; q < 9; q++)
+    *dst[q] = vi[q].p;
+  o->radius = vr.p;
+  o->rab = vrab.p;
+}
+
 wl_out *wl_generate(const wl_params *p) {
   if (p->nlevels < 1 || p->nlevels > WL_MAX_LEVELS || p->nelem < 1 ||
       p->nelem > WL_MAX_ELEM || p->natoms < 1)
@@ -326,98 +432,19 @@ wl_out *wl_generate(const wl_params *p) {
         o->dh[l][a][b] = p->cell[a][b] / p->npts[l][a];
     inv3(o->dh[l], o->dh_inv[l]);
   }
-  /* image range from the most diffuse possible product */
-  const double ln_eps = log(1.0 / p->eps);
-  const double rmax = sqrt(ln_eps / (0.5 * p->zet_min));
-  double cinv[3][3];
-  inv3(p->cell, cinv);
-  int nimg[3];
-  for (int d = 0; d < 3; d++) {
-    const double h = sqrt(cinv[0][d] * cinv[0][d] + cinv[1][d] * cinv[1][d] +
-                          cinv[2][d] * cinv[2][d]);
-    nimg[d] = (int)ceil(rmax * h) + 1;
-  }
-  vec vi[9], vr = {0, 0, 0, sizeof(double)}, vrab = {0, 0, 0, 3 * sizeof(double)},
-             vblk = {0, 0, 0, sizeof(int)};
-  for (int q = 0; q < 9; q++) {
-    vi[q].p = NULL;
-    vi[q].n = vi[q].cap = 0;
-    vi[q].elem = sizeof(int);
-  }
-  long long offset = 0;
-  int nblocks = 0;
-  for (int i = 0; i < na; i++) {
-    const double *ra = &o->atom_positions[3 * i];
-    for (int j = i; j < na; j++) {
-      const double *rj = &o->atom_positions[3 * j];
-      int block = 0;
-      for (int n0i = -nimg[0]; n0i <= nimg[0]; n0i++)
-        for (int n1i = -nimg[1]; n1i <= nimg[1]; n1i++)
-          for (int n2i = -nimg[2]; n2i <= nimg[2]; n2i++) {
-            if (i == j) { /* same atom: image 0 and one of each +/- pair */
-              const int lex = n0i != 0 ? n0i : (n1i != 0 ? n1i : n2i);
-              if (lex < 0)
-                continue;
-            }
-            double rab[3];
-            for (int d = 0; d < 3; d++)
-              rab[d] = rj[d] - ra[d] + n0i * p->cell[0][d] + n1i * p->cell[1][d] +
-                       n2i * p->cell[2][d];
-            const double rab2 = rab[0] * rab[0] + rab[1] * rab[1] + rab[2] * rab[2];
-            if (rab2 > rmax * rmax)
-              continue;
-            for (int is = 0; is < o->nset[i]; is++)
-            for (int ip = 0; ip < o->npgf[o->set_off[i] + is]; ip++) {
-              const int gi = o->set_off[i] + is;
-              const double za = o->zet[(size_t)gi * maxpgf_all + ip];
-              for (int js = 0; js < o->nset[j]; js++)
-              for (int jp = 0; jp < o->npgf[o->set_off[j] + js]; jp++) {
-                const int gj = o->set_off[j] + js;
-                const double zb = o->zet[(size_t)gj * maxpgf_all + jp];
-                const double zetp = za + zb, f = zb / zetp;
-                const double pref = exp(-za * f * rab2);
-                if (!(pref > p->eps))
-                  continue;
-                double rp[3], rb[3];
-                for (int d = 0; d < 3; d++) {
-                  rp[d] = ra[d] + f * rab[d];
-                  rb[d] = ra[d] + rab[d];
-                }
-                const double radius = exp_radius_very_extended(
-                    o->lmax[gi], o->lmax[gj], ra, rb, rp, zetp, p->eps, pref);
-                if (!block) {
-                  block = ++nblocks;
-                  const int off = (int)offset;
-                  vpush(&vblk, &off);
-                  offset += (long long)o->nsgf[i] * o->nsgf[j];
-                }
-                const int v[9] = {grid_level(p, zetp), i + 1, j + 1, is + 1, js + 1,
-                                  ip + 1, jp + 1, 0, block};
-                for (int q = 0; q < 9; q++)
-                  vpush(&vi[q], &v[q]);
-                vpush(&vr, &radius);
-                vpush(&vrab, rab);
-              }
-            }
-          }
-    }
-  }
-  if (offset > 2147483647LL) {
-    fprintf(stderr, "workload: block buffer exceeds int offsets\n");
-    abort();
-  }
-  o->ntasks = (int)vr.n;
-  o->nblocks = nblocks;
-  o->buffer_size = offset;
-  o->block_offsets = vblk.p;
-  int **dst[9] = {&o->level, &o->iatom, &o->jatom, &o->iset, &o->jset,
-                  &o->ipgf, &o->jpgf, &o->border_mask, &o->block_num};
-  for (int q = 0; q < 9; q++)
-    *dst[q] = vi[q].p;
-  o->radius = vr.p;
-  o->rab = vrab.p;
+  build_tasks(o, p);
   free(elem);
   return o;
+}
+
+/* Rebuild the task arrays of o for new atom positions ([natoms][3], bohr),
+ * keeping its basis sets: the task list of a moved geometry. */
+int wl_retask(wl_out *o, const wl_params *p, const double *positions) {
+  if (!o || !p || !positions || p->natoms != o->natoms)
+    return 1;
+  memcpy(o->atom_positions, positions, sizeof(double) * 3 * (size_t)o->natoms);
+  build_tasks(o, p);
+  return 0;
 }
 
 void wl_free(wl_out *o) {

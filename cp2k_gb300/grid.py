@@ -284,6 +284,47 @@ class GridTaskList:
         self._hab = None
         self._grids = None
 
+    @classmethod
+    def from_generator(cls, gen: "TaskGenerator", positions=None, precision: int | None = FP64,
+                       schedule: int | None = SCHEDULE_SIZE, existing: "GridTaskList" = None):
+        """A backend task list from the generator's last run through
+        grid_gb300_taskgen_create_task_list; ``existing`` is re-created in
+        place (its settings kept), as at a change of geometry."""
+        inp = gen.inputs(positions)
+        self = existing if existing is not None else cls.__new__(cls)
+        if existing is None:
+            self.api = "backend"
+            self.h = C.c_void_p()
+        old_basis = getattr(self, "basis", [])
+        self.inp = inp
+        self.basis = [BasisSet(b) for b in inp.basis_sets]
+        self._bs = (C.c_void_p * max(1, len(self.basis)))(*[b.h.value for b in self.basis])
+        i32 = lambda a: np.ascontiguousarray(a, np.int32)
+        f64 = lambda a: np.ascontiguousarray(a, np.float64)
+        levels = [i32(inp.npts_global), i32(inp.npts_local), i32(inp.shift_local),
+                  i32(inp.border_width), f64(inp.dh), f64(inp.dh_inv)]
+        self._arrays = levels
+        self.npts_local = levels[1]
+        lib().grid_gb300_taskgen_create_task_list(gen.h, bool(inp.orthorhombic), inp.nlevels,
+                                                  C.cast(self._bs, C.c_void_p),
+                                                  *[_p(a) for a in levels], C.byref(self.h))
+        self.impl = self.h
+        for b in old_basis:
+            b.free()
+        for buf in ([getattr(self, "_pab", None), getattr(self, "_hab", None)]
+                    + list(getattr(self, "_grids", None) or [])):
+            if buf is not None:
+                buf.free()
+        self._pab = None
+        self._hab = None
+        self._grids = None
+        if existing is None:
+            if precision is not None:
+                self.set_precision(precision)
+            if schedule is not None:
+                self.set_schedule(schedule)
+        return self
+
     def recreate(self, inp: TaskListInputs):
         """Re-create the task list through its existing handle for new inputs
         (a moved geometry); the backend keeps the settings made on it."""
@@ -563,6 +604,158 @@ def _stream(stream):
     if hasattr(stream, "cuda_stream"):
         return C.c_void_p(stream.cuda_stream)
     return C.c_void_p(int(stream))
+
+
+def _bind_taskgen(L):
+    if hasattr(L, "_tg_bound"):
+        return
+    vp = C.c_void_p
+    L.grid_gb300_taskgen_create.argtypes = ([C.c_int, C.c_int] + [vp] * 5 + [C.c_int, vp, vp, vp]
+                                            + [C.c_double, C.c_double, C.c_int, vp, C.c_double,
+                                               C.POINTER(vp)])
+    L.grid_gb300_taskgen_free.argtypes = [vp]
+    L.grid_gb300_taskgen_run.argtypes = [vp, vp, C.c_int, vp, vp, vp, vp]
+    L.grid_gb300_taskgen_arrays.argtypes = [vp] + [vp] * 12
+    L.grid_gb300_taskgen_copy.argtypes = [vp] + [vp] * 12
+    L.grid_gb300_taskgen_create_task_list.argtypes = [vp, C.c_bool, C.c_int] + [vp] * 8
+    L.grid_gb300_pack_blocks.argtypes = [C.c_longlong] + [vp] * 6
+    L.grid_gb300_unpack_blocks.argtypes = [C.c_longlong] + [vp] * 6
+    L.grid_gb300_find_blocks.restype = C.c_longlong
+    L.grid_gb300_find_blocks.argtypes = [C.c_longlong, vp, vp, vp, C.c_longlong, vp, vp, vp, vp]
+    L._tg_bound = True
+
+
+_TASK_INT_FIELDS = ["level_list", "iatom_list", "jatom_list", "iset_list", "jset_list",
+                    "ipgf_list", "jpgf_list", "border_mask_list", "block_num_list"]
+
+
+class TaskGenerator:
+    """Task-list generation on the device (grid_gb300_taskgen_*): the work of
+    Quickstep's generate_qs_task_list (src/task_list_methods.F:117-501) for
+    a geometry, with the basis and screening of ``like`` (a TaskListInputs
+    from cp2k_gb300.workload, whose ``meta`` holds the cell, level cutoffs,
+    rel_cutoff, eps, image range and pair cut)."""
+
+    def __init__(self, like: TaskListInputs):
+        L = lib()
+        _bind_taskgen(L)
+        m = like.meta
+        self.like = like
+        bs = like.basis_sets
+        self.maxpgf = max(int(b.maxpgf) for b in bs)
+        nset = np.array([b.nset for b in bs], np.int32)
+        nsgf = np.array([b.nsgf for b in bs], np.int32)
+        lmax = np.concatenate([np.asarray(b.lmax, np.int32) for b in bs]).astype(np.int32)
+        npgf = np.concatenate([np.asarray(b.npgf, np.int32) for b in bs]).astype(np.int32)
+        zet = np.zeros((int(nset.sum()), self.maxpgf))
+        r = 0
+        for b in bs:
+            z = np.asarray(b.zet, np.float64).reshape(b.nset, -1)
+            zet[r:r + b.nset, :z.shape[1]] = z
+            r += b.nset
+        kinds = np.ascontiguousarray(like.atom_kinds, np.int32)
+        cell = np.ascontiguousarray(np.asarray(m["cell_bohr"], np.float64).reshape(3, 3))
+        nimg = np.ascontiguousarray(m["nimg"], np.int32)
+        cut = np.ascontiguousarray(m["cutoffs_ry"], np.float64)
+        self._keep = [kinds, nset, nsgf, lmax, npgf, zet, cell, nimg, cut]
+        self.h = C.c_void_p()
+        L.grid_gb300_taskgen_create(like.natoms, len(bs), _p(kinds), _p(nset), _p(nsgf),
+                                    _p(lmax), _p(npgf), self.maxpgf, _p(zet), _p(cell),
+                                    _p(nimg), float(m["rmax"]), float(m["eps"]),
+                                    len(cut), _p(cut), float(m["rel_cutoff"]),
+                                    C.byref(self.h))
+        self.ntasks = self.nblocks = self.buffer_size = 0
+        self.positions = None
+
+    def run(self, positions, stream=None):
+        """Generate for ``positions`` ([natoms][3] bohr: numpy, or a torch
+        CUDA float64 tensor); returns (ntasks, nblocks, buffer_size)."""
+        nt, nb, bsz = C.c_int(), C.c_int(), C.c_longlong()
+        if hasattr(positions, "data_ptr"):
+            self.positions = None
+            lib().grid_gb300_taskgen_run(self.h, C.c_void_p(positions.data_ptr()), 1,
+                                         _stream(stream), C.byref(nt), C.byref(nb),
+                                         C.byref(bsz))
+        else:
+            pos = np.ascontiguousarray(positions, np.float64).reshape(-1, 3)
+            self.positions = pos
+            lib().grid_gb300_taskgen_run(self.h, _p(pos), 0, _stream(stream), C.byref(nt),
+                                         C.byref(nb), C.byref(bsz))
+        self.ntasks, self.nblocks, self.buffer_size = nt.value, nb.value, bsz.value
+        return self.ntasks, self.nblocks, self.buffer_size
+
+    def device_arrays(self) -> dict:
+        """Device addresses of the last run's arrays."""
+        ptrs = [C.c_void_p() for _ in range(12)]
+        lib().grid_gb300_taskgen_arrays(self.h, *[C.byref(x) for x in ptrs])
+        names = _TASK_INT_FIELDS + ["radius_list", "rab_list", "block_offsets"]
+        return {k: v.value for k, v in zip(names, ptrs)}
+
+    def host_arrays(self) -> dict:
+        nt, nb = self.ntasks, self.nblocks
+        out = {k: np.zeros(nt, np.int32) for k in _TASK_INT_FIELDS}
+        out["radius_list"] = np.zeros(nt)
+        out["rab_list"] = np.zeros((nt, 3))
+        out["block_offsets"] = np.zeros(nb, np.int32)
+        lib().grid_gb300_taskgen_copy(self.h, *[_p(out[k]) for k in _TASK_INT_FIELDS],
+                                      _p(out["radius_list"]), _p(out["rab_list"]),
+                                      _p(out["block_offsets"]))
+        return out
+
+    def inputs(self, positions=None) -> TaskListInputs:
+        """``like`` with the last run's task arrays (and ``positions``)."""
+        import dataclasses
+        a = self.host_arrays()
+        pos = self.positions if positions is None else positions
+        if pos is None:
+            raise ValueError("positions of a device run must be given")
+        return dataclasses.replace(self.like, nblocks=self.nblocks,
+                                   buffer_size=self.buffer_size,
+                                   atom_positions=np.asarray(pos, np.float64).reshape(-1, 3),
+                                   **a)
+
+    def free(self):
+        if self.h:
+            lib().grid_gb300_taskgen_free(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def pack_blocks(src_offsets, dst_offsets, sizes, src, dst, stream=None):
+    """rs_pack_buffer on torch CUDA tensors: dst[dst_off[b]:+sizes[b]] =
+    src[src_off[b]:+sizes[b]] (src_offsets int64, dst_offsets / sizes int32)."""
+    L = lib()
+    _bind_taskgen(L)
+    d = lambda t: C.c_void_p(t.data_ptr())
+    L.grid_gb300_pack_blocks(int(sizes.numel()), d(src_offsets), d(dst_offsets), d(sizes),
+                             d(src), d(dst), _stream(stream))
+
+
+def unpack_blocks(buffer_offsets, block_offsets, sizes, buffer, blocks, stream=None):
+    """rs_unpack_buffer on torch CUDA tensors: blocks[block_off[b]:+sizes[b]]
+    += buffer[buffer_off[b]:+sizes[b]] (buffer_offsets / sizes int32,
+    block_offsets int64)."""
+    L = lib()
+    _bind_taskgen(L)
+    d = lambda t: C.c_void_p(t.data_ptr())
+    L.grid_gb300_unpack_blocks(int(sizes.numel()), d(buffer_offsets), d(block_offsets),
+                               d(sizes), d(buffer), d(blocks), _stream(stream))
+
+
+def find_blocks(key_rows, key_cols, key_offsets, rows, cols, offsets, stream=None) -> int:
+    """Block look-up by (row, col) in keys sorted by row then column (torch
+    CUDA tensors; offsets int64, -1 where absent); returns the misses."""
+    L = lib()
+    _bind_taskgen(L)
+    d = lambda t: C.c_void_p(t.data_ptr())
+    return int(L.grid_gb300_find_blocks(int(key_rows.numel()), d(key_rows), d(key_cols),
+                                        d(key_offsets), int(rows.numel()), d(rows), d(cols),
+                                        d(offsets), _stream(stream)))
 
 
 class PwTransfer:

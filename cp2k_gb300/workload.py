@@ -49,6 +49,7 @@ class _Out(C.Structure):
         ("ipgf", _ip), ("jpgf", _ip), ("border_mask", _ip), ("block_num", _ip),
         ("radius", _dp), ("rab", _dp),
         ("dh", C.c_double * (_MAXL * 9)), ("dh_inv", C.c_double * (_MAXL * 9)),
+        ("nimg", C.c_int * 3), ("rmax", C.c_double),
     ]
 
 
@@ -62,6 +63,8 @@ def _lib():
         L.wl_generate.restype = C.POINTER(_Out)
         L.wl_generate.argtypes = [C.POINTER(_Params)]
         L.wl_free.argtypes = [C.POINTER(_Out)]
+        L.wl_retask.restype = C.c_int
+        L.wl_retask.argtypes = [C.POINTER(_Out), C.POINTER(_Params), C.c_void_p]
         _LIB = L
     return _LIB
 
@@ -125,9 +128,11 @@ def make_cell(spec) -> np.ndarray:
 
 def generate(natoms: int, cell: np.ndarray, npts, elements, zet, seed: int = 1,
              rel_cutoff: float = 40.0, eps: float = 1e-10, random_sphi: bool = False,
-             cutoffs=None) -> TaskListInputs:
+             cutoffs=None, positions=None) -> TaskListInputs:
     """Build a task list.  ``npts`` is a list of per-level point counts (int or
-    3-tuple), finest first; ``elements`` a list of (fraction, [set lmax...])."""
+    3-tuple), finest first; ``elements`` a list of (fraction, [set lmax...]).
+    ``positions`` ([natoms][3], bohr) replaces the seeded atom positions
+    (same basis sets): the task list of a moved geometry."""
     npts = [(n, n, n) if np.isscalar(n) else tuple(n) for n in npts]
     cell = np.asarray(cell, np.float64)
     p = _Params()
@@ -158,9 +163,14 @@ def generate(natoms: int, cell: np.ndarray, npts, elements, zet, seed: int = 1,
     if not op:
         raise ValueError("invalid workload parameters")
     try:
+        if positions is not None:
+            pos = np.ascontiguousarray(positions, np.float64).reshape(natoms, 3)
+            if L.wl_retask(op, C.byref(p), pos.ctypes.data_as(C.c_void_p)) != 0:
+                raise ValueError("positions do not match the workload")
         o = op.contents
         return _to_inputs(o, cell, npts, cut, dict(natoms=natoms, seed=seed, zet=zet,
-                                                   elements=elements, rel_cutoff=rel_cutoff))
+                                                   elements=elements, rel_cutoff=rel_cutoff,
+                                                   eps=eps, nimg=list(o.nimg), rmax=o.rmax))
     finally:
         L.wl_free(op)
 
@@ -223,10 +233,11 @@ def _to_inputs(o, cell, npts, cutoffs, meta) -> TaskListInputs:
 
 
 def config(name: str, seed: int = 1, scale: float = 1.0, random_sphi: bool = False,
-           **overrides) -> TaskListInputs:
+           positions=None, **overrides) -> TaskListInputs:
     """A named benchmark configuration.  ``scale`` < 1 shrinks the atom count,
     the cell edge (at fixed density) and the grid point counts (at fixed
-    spacing) for quick parity runs."""
+    spacing) for quick parity runs.  ``positions`` moves the atoms (see
+    ``generate``)."""
     c = dict(CONFIGS[name])
     c.update(overrides)
     natoms = max(2, int(round(c["natoms"] * scale)))
@@ -235,7 +246,7 @@ def config(name: str, seed: int = 1, scale: float = 1.0, random_sphi: bool = Fal
     npts = [max(8, int(round(n * lin))) for n in c["npts"]]
     cutoffs = _cutoffs(cell, [(n, n, n) for n in c["npts"]])
     return generate(natoms, cell * lin, npts, c["elements"], c["zet"], seed=seed,
-                    random_sphi=random_sphi, cutoffs=cutoffs)
+                    random_sphi=random_sphi, cutoffs=cutoffs, positions=positions)
 
 
 def density_blocks(inp: TaskListInputs, seed: int = 2) -> np.ndarray:

@@ -594,6 +594,81 @@ void grid_gb300_pw_poisson(grid_gb300_pw_transfer *handle, const double *dh,
                            const void *rho_gspace, void *v_gspace, double *v_rspace,
                            double *energy, void *stream);
 
+/* ---- task-list generation and block packing on the device ---------------
+ * Replaces, for one geometry, the work of Quickstep's generate_qs_task_list
+ * (src/task_list_methods.F:117-501; task_list_inner_loop :652-719,
+ * compute_pgf_properties :738-800, the API arrays :507-618): every atom pair
+ * i <= j and periodic image n (-nimages[d] .. nimages[d] along cell vector d;
+ * for i == j image 0 and one of each +/- n pair) with |rab| <= rmax, every
+ * primitive pair (iset, ipgf, jset, jpgf) whose Gaussian-product prefactor
+ * exp(-zeta zetb / zetp |rab|^2) exceeds eps, in that order; the level of
+ * gaussian_gridlevel (src/pw_env/gaussian_gridlevels.F:147-167, cutoff[] in
+ * the units of zetp * rel_cutoff, finest first); the radius of
+ * exp_radius_very_extended (src/aobasis/ao_util.F:207-290); one block per
+ * atom pair with tasks, numbered in pair order, at offset sum nsgf(i)
+ * nsgf(j) of the blocks before it.  The basis is uploaded once; runs take
+ * new positions (a moved geometry) and leave the arrays of
+ * grid_create_task_list (1-based indices, rab [ntasks][3]) in device memory.
+ * Sets and primitives: set_lmax and set_npgf hold every kind's sets, kind
+ * after kind ([sum nset]); zet [sum nset][maxpgf].  Cell rows are the cell
+ * vectors (bohr).  Invalid arguments abort with a message. */
+typedef void grid_gb300_task_generator;
+void grid_gb300_taskgen_create(
+    const int natoms, const int nkinds, const int *atom_kinds, const int *nset,
+    const int *nsgf, const int *set_lmax, const int *set_npgf, const int maxpgf,
+    const double *zet, const double *cell, const int *nimages, const double rmax,
+    const double eps, const int nlevels, const double *cutoff, const double rel_cutoff,
+    grid_gb300_task_generator **generator);
+void grid_gb300_taskgen_free(grid_gb300_task_generator *generator);
+/* Generates the task list for atom_positions ([natoms][3], bohr; a device
+ * pointer when on_device != 0, else host); returns the task and block counts
+ * and the pab buffer length (doubles).  Synchronises the stream. */
+void grid_gb300_taskgen_run(grid_gb300_task_generator *generator,
+                            const double *atom_positions, const int on_device,
+                            void *stream, int *ntasks, int *nblocks,
+                            long long *buffer_size);
+/* Device pointers of the last run's arrays (valid until the next run or
+ * free); any argument may be NULL. */
+void grid_gb300_taskgen_arrays(const grid_gb300_task_generator *generator,
+                               int **level, int **iatom, int **jatom, int **iset,
+                               int **jset, int **ipgf, int **jpgf, int **border_mask,
+                               int **block_num, double **radius, double **rab,
+                               int **block_offsets);
+/* The same arrays copied to host memory (caller-sized: ntasks, 3 ntasks for
+ * rab, nblocks for block_offsets); any argument may be NULL. */
+void grid_gb300_taskgen_copy(const grid_gb300_task_generator *generator, int *level,
+                             int *iatom, int *jatom, int *iset, int *jset, int *ipgf,
+                             int *jpgf, int *border_mask, int *block_num, double *radius,
+                             double *rab, int *block_offsets);
+/* grid_gb300_create_task_list on the last run's arrays and positions (a
+ * non-NULL *task_list is re-created in place, keeping its settings). */
+void grid_gb300_taskgen_create_task_list(
+    grid_gb300_task_generator *generator, const bool orthorhombic, const int nlevels,
+    const grid_basis_set **basis_sets, const int *npts_global, const int *npts_local,
+    const int *shift_local, const int *border_width, const double *dh, const double *dh_inv,
+    grid_gb300_task_list **task_list);
+/* rs_pack_buffer (src/task_list_methods.F:2593-2619) on device memory: block
+ * b, sizes[b] doubles at src + src_offsets[b], is copied to dst +
+ * dst_offsets[b] (the task list's block offsets).  Enqueued on `stream`. */
+void grid_gb300_pack_blocks(const long long nblocks, const long long *src_offsets,
+                            const int *dst_offsets, const int *sizes, const double *src,
+                            double *dst, void *stream);
+/* rs_unpack_buffer (:2625-2674): blocks[block_offsets[b] + k] +=
+ * buffer[buffer_offsets[b] + k] for k < sizes[b].  The target blocks must
+ * not overlap (one entry per block, as in the reference's atom-pair list). */
+void grid_gb300_unpack_blocks(const long long nblocks, const int *buffer_offsets,
+                              const long long *block_offsets, const int *sizes,
+                              const double *buffer, double *blocks, void *stream);
+/* dbcsr_get_block_p for many blocks at once: offsets[q] = key_offsets[k] for
+ * the key k with (key_rows[k], key_cols[k]) == (rows[q], cols[q]), keys
+ * sorted by row, then column; -1 where absent.  Returns the number of
+ * absent blocks (the reference asserts found); synchronises the stream.
+ * All arrays are device pointers. */
+long long grid_gb300_find_blocks(const long long nkeys, const int *key_rows,
+                                 const int *key_cols, const long long *key_offsets,
+                                 const long long nquery, const int *rows, const int *cols,
+                                 long long *offsets, void *stream);
+
 /* Last error message recorded by the library ("" if none). */
 const char *grid_gb300_last_error(void);
 
