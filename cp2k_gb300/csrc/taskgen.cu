@@ -18,12 +18,17 @@
 //   * one block per atom pair with tasks, numbered in pair order, its buffer
 //     offset the running sum of nsgf(i) * nsgf(j).
 // The host generator (csrc/workload.c) runs the same loops in C; every array
-// made here equals its array element for element.  The double-precision
-// expressions are evaluated in the host code's order with explicitly rounded
-// operations (no contraction into FMAs), the single-precision exponential as
-// exp in double rounded once to float (the correctly rounded value but for
-// inputs within 2^-29 of a rounding boundary), and integer powers by
-// repeated multiplication (Fortran's r**l).
+// made here equals its array element for element.  Every comparison that
+// decides the outcome (distance cut, prefactor screen, the bisection's
+// g(r) < threshold) is first taken in single precision, with a margin above
+// the rounding of both sides (GB300's FP64 rate is a small fraction of its
+// FP32 rate); inside the margin the exact double expression decides, in the
+// host code's order with explicitly rounded operations (no contraction into
+// FMAs), the single-precision exponential as exp in double rounded once to
+// float (the correctly rounded value but for inputs within 2^-29 of a
+// rounding boundary), and integer powers by repeated multiplication
+// (Fortran's r**l).  The values written (rab, radius) are always exact
+// double results.
 //
 // Kernels: one warp per atom pair counts the tasks of its images (lanes over
 // images); a three-phase scan turns the counts into task offsets and block
@@ -80,6 +85,9 @@ struct TgParams {
   int nlevels;
   double cutoff[kTgMaxLevels];
   int maxpgf;
+  // single-precision copies for the screening decisions
+  float cellf[3][3], cellnorm[3], rmaxf, leps;
+  const float *zetf;   // [nsets][maxpgf]
   const double *pos;   // [natoms][3]
   const int *kind;     // [natoms], 0-based
   const int *set_off;  // [nkinds]
@@ -107,8 +115,9 @@ __device__ __forceinline__ long long row_start(long long i, long long n) {
   return i * n - i * (i - 1) / 2;
 }
 __device__ void pair_of(long long p, int n, int &i, int &j) {
-  const double b = 2.0 * n + 1.0;
-  long long r = (long long)((b - sqrt(fmax(b * b - 8.0 * (double)p, 0.0))) * 0.5);
+  // estimate in single precision, then exact integer corrections
+  const float b = 2.0f * n + 1.0f;
+  long long r = (long long)((b - sqrtf(fmaxf(b * b - 8.0f * (float)p, 0.0f))) * 0.5f);
   r = r < 0 ? 0 : (r > n - 1 ? n - 1 : r);
   while (r > 0 && row_start(r, n) > p)
     r--;
@@ -144,7 +153,20 @@ __device__ __forceinline__ double image_rab(const TgParams &P, const double ra[3
   return dadd(dadd(dmul(rab[0], rab[0]), dmul(rab[1], rab[1])), dmul(rab[2], rab[2]));
 }
 
-__device__ __forceinline__ bool passes(const TgParams &P, double za, double zb, double rab2) {
+// Decisions are taken in single precision where a margin of 1e-3 (in the
+// exponent) covers every rounding of both sides, and by the exact double
+// expression inside that band: the outcome is the host's.
+constexpr float kMargin = 1e-3f;
+
+// exp(-za zb / (za + zb) rab2) > eps
+__device__ __forceinline__ bool passes(const TgParams &P, double za, double zb, float zaf,
+                                       float zbf, double rab2, float rab2f) {
+  const float y = -zaf * (zbf / (zaf + zbf)) * rab2f;
+  const float diff = y - P.leps;
+  if (diff > kMargin)
+    return true;
+  if (diff < -kMargin)
+    return false;
   const double zetp = dadd(za, zb), f = ddiv(zb, zetp);
   const double pref = exp(dmul(dmul(-za, f), rab2));
   return pref > P.eps;
@@ -153,26 +175,60 @@ __device__ __forceinline__ bool passes(const TgParams &P, double za, double zb, 
 // tasks of one image of the pair (ki, kj): primitive pairs that pass
 __device__ int image_tasks(const TgParams &P, int ki, int kj, double rab2) {
   int c = 0;
+  const float rab2f = __double2float_rn(rab2);
   const int si0 = P.set_off[ki], sj0 = P.set_off[kj];
   for (int is = 0; is < P.nset[ki]; is++)
     for (int ip = 0; ip < P.npgf[si0 + is]; ip++) {
-      const double za = P.zet[(size_t)(si0 + is) * P.maxpgf + ip];
+      const size_t ia = (size_t)(si0 + is) * P.maxpgf + ip;
+      const double za = P.zet[ia];
+      const float zaf = P.zetf[ia];
       for (int js = 0; js < P.nset[kj]; js++)
-        for (int jp = 0; jp < P.npgf[sj0 + js]; jp++)
-          c += passes(P, za, P.zet[(size_t)(sj0 + js) * P.maxpgf + jp], rab2);
+        for (int jp = 0; jp < P.npgf[sj0 + js]; jp++) {
+          const size_t ib = (size_t)(sj0 + js) * P.maxpgf + jp;
+          c += passes(P, za, P.zet[ib], zaf, P.zetf[ib], rab2, rab2f);
+        }
     }
   return c;
 }
 
-// tasks of image `img` of pair (i, j) (0 outside the cut or skipped)
-__device__ int lane_image_tasks(const TgParams &P, int i, int j, int img, double rab[3],
-                                double &rab2) {
+// an atom pair's positions: exact, and their difference in single precision
+struct PairPos {
+  double ra[3], rj[3];
+  float df[3];
+};
+__device__ __forceinline__ PairPos pair_pos(const TgParams &P, int i, int j) {
+  PairPos q;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    q.ra[d] = P.pos[3 * i + d];
+    q.rj[d] = P.pos[3 * j + d];
+    q.df[d] = __double2float_rn(dsub(q.rj[d], q.ra[d]));
+  }
+  return q;
+}
+
+// tasks of image `img` of pair (i, j) (0 outside the cut or skipped); the
+// distance cut is tried in single precision first with a margin above its
+// rounding error
+__device__ int lane_image_tasks(const TgParams &P, int i, int j, const PairPos &q, int img,
+                                double rab[3], double &rab2) {
   int n[3];
   if (!image_of(P, img, i == j, n))
     return 0;
-  const double ra[3] = {P.pos[3 * i], P.pos[3 * i + 1], P.pos[3 * i + 2]};
-  const double rj[3] = {P.pos[3 * j], P.pos[3 * j + 1], P.pos[3 * j + 2]};
-  rab2 = image_rab(P, ra, rj, n, rab);
+  float rf2 = 0.0f;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const float x = q.df[d] + (float)n[0] * P.cellf[0][d] + (float)n[1] * P.cellf[1][d] +
+                    (float)n[2] * P.cellf[2][d];
+    rf2 += x * x;
+  }
+  const float span = P.rmaxf + fabsf(q.df[0]) + fabsf(q.df[1]) + fabsf(q.df[2]) +
+                     fabsf((float)n[0]) * P.cellnorm[0] + fabsf((float)n[1]) * P.cellnorm[1] +
+                     fabsf((float)n[2]) * P.cellnorm[2];
+  const float lim = P.rmaxf + 1e-5f * span + 1e-6f;
+  if (rf2 > lim * lim)
+    return 0;
+  rab2 = image_rab(P, q.ra, q.rj, n, rab);
   if (rab2 > dmul(P.rmax, P.rmax))
     return 0;
   return image_tasks(P, P.kind[i], P.kind[j], rab2);
@@ -186,10 +242,11 @@ __global__ void __launch_bounds__(256) pair_count_kernel(TgParams P, int *__rest
   for (long long p = w0; p < P.npairs; p += nw) {
     int i, j;
     pair_of(p, P.natoms, i, j);
+    const PairPos q = pair_pos(P, i, j);
     int c = 0;
     for (int img = lane; img < P.nimages; img += 32) {
       double rab[3], rab2;
-      c += lane_image_tasks(P, i, j, img, rab, rab2);
+      c += lane_image_tasks(P, i, j, q, img, rab, rab2);
     }
     c = __reduce_add_sync(0xffffffffu, c);
     if (lane == 0)
@@ -353,11 +410,12 @@ __global__ void __launch_bounds__(256)
   for (long long b = w0; b < nblocks; b += nw) {
     const int i = pair_i[b], j = pair_j[b];
     const int ki = P.kind[i], kj = P.kind[j];
+    const PairPos q = pair_pos(P, i, j);
     long long base = task0[b];
     for (int img0 = 0; img0 < P.nimages; img0 += 32) {
       const int img = img0 + lane;
       double rab[3] = {0.0, 0.0, 0.0}, rab2 = 0.0;
-      const int c = img < P.nimages ? lane_image_tasks(P, i, j, img, rab, rab2) : 0;
+      const int c = img < P.nimages ? lane_image_tasks(P, i, j, q, img, rab, rab2) : 0;
       int inc = c;
 #pragma unroll
       for (int o2 = 1; o2 < 32; o2 <<= 1) {
@@ -369,14 +427,18 @@ __global__ void __launch_bounds__(256)
       base += __shfl_sync(0xffffffffu, inc, 31);
       if (c == 0)
         continue;
+      const float rab2f = __double2float_rn(rab2);
       const int si0 = P.set_off[ki], sj0 = P.set_off[kj];
       for (int is = 0; is < P.nset[ki]; is++)
         for (int ip = 0; ip < P.npgf[si0 + is]; ip++) {
-          const double za = P.zet[(size_t)(si0 + is) * P.maxpgf + ip];
+          const size_t ia = (size_t)(si0 + is) * P.maxpgf + ip;
+          const double za = P.zet[ia];
+          const float zaf = P.zetf[ia];
           for (int js = 0; js < P.nset[kj]; js++)
             for (int jp = 0; jp < P.npgf[sj0 + js]; jp++) {
-              const double zb = P.zet[(size_t)(sj0 + js) * P.maxpgf + jp];
-              if (!passes(P, za, zb, rab2))
+              const size_t ib = (size_t)(sj0 + js) * P.maxpgf + jp;
+              const double zb = P.zet[ib];
+              if (!passes(P, za, zb, zaf, P.zetf[ib], rab2, rab2f))
                 continue;
               o.level[t] = grid_level(P, dadd(za, zb));
               o.iatom[t] = i + 1;
@@ -407,6 +469,32 @@ __device__ __forceinline__ double g_eval(double d, double a, double r, int l) {
   return dmul(dmul(d, e), pw);
 }
 
+__device__ __forceinline__ float log_of(double v) {
+  const float f = __double2float_rn(v);
+  return (f > 1e-30f && f < 1e30f) ? logf(f) : __double2float_rn(log(v));
+}
+
+// g_eval(d, a, r, l) < t: in single precision on the logarithms, ln d - a r^2
+// + l ln r against ln t, where the margin decides; else g_eval itself.  Below
+// exp(-87) the single-precision exponential is subnormal or zero, so there the
+// comparison uses e^-87 as an upper bound and defers to g_eval otherwise.
+struct Below {
+  double d, a, t;
+  int l;
+  float af, ld, lt;
+  __device__ bool operator()(double r) const {
+    const float rf = __double2float_rn(r);
+    const float x = -af * rf * rf;
+    const float xe = fmaxf(x, -87.0f);
+    const float diff = ld + xe + (l ? (float)l * logf(rf) : 0.0f) - lt;
+    if (diff < -kMargin)
+      return true;
+    if (x > -87.0f && diff > kMargin)
+      return false;
+    return g_eval(d, a, r, l) < t;
+  }
+};
+
 // smallest radius past which d exp(-a r^2) r^l stays below t (ao_util.F:95-180)
 __device__ double exp_radius(int l, double alpha, double threshold, double prefactor,
                              double epsabs, double rlow) {
@@ -418,15 +506,13 @@ __device__ double exp_radius(int l, double alpha, double threshold, double prefa
     return radius;
   double r = fmax(__dsqrt_rn(ddiv(dmul(0.5, (double)l), a)), radius);
   const double d = fabs(prefactor);
-  double g = d;
-  if (l != 0)
-    g = g_eval(d, a, r, l);
-  if (g < t)
+  const Below below{d, a, t, l, __double2float_rn(a), log_of(d), log_of(t)};
+  if (l != 0 ? below(r) : d < t)
     return radius;
   radius = dadd(dmul(r, 2.0), 1.0);
   int i;
   for (i = 1; i <= itermax; i++) {
-    if (g_eval(d, a, radius, l) < t)
+    if (below(radius))
       break;
     r = radius;
     radius = dadd(dmul(r, 2.0), 1.0);
@@ -436,15 +522,19 @@ __device__ double exp_radius(int l, double alpha, double threshold, double prefa
     const double rd = dsub(radius, r);
     if (rd < epsabs || rd == dr)
       return radius;
-    double s[2];
-    for (int k = 0; k < 2; k++)
-      s[k] = dadd(r, dmul(rd, contract[k]));
-    for (int k = 0; k < 2; k++) {
-      if (g_eval(d, a, s[k], l) < t) {
-        radius = s[k];
-        break;
-      }
-      r = s[k];
+    // the two contraction points of [r, radius), the second only when the
+    // first is above
+    const double r0 = r;
+    const double s0 = dadd(r0, dmul(rd, contract[0]));
+    if (below(s0)) {
+      radius = s0;
+    } else {
+      r = s0;
+      const double s1 = dadd(r0, dmul(rd, contract[1]));
+      if (below(s1))
+        radius = s1;
+      else
+        r = s1;
     }
     dr = rd;
   }
@@ -616,6 +706,7 @@ struct TaskGenerator {
   int *d_kind = nullptr, *d_set_off = nullptr, *d_nset = nullptr, *d_nsgf = nullptr;
   int *d_lmax = nullptr, *d_npgf = nullptr;
   double *d_zet = nullptr, *d_pos = nullptr;
+  float *d_zetf = nullptr;
   // work
   int *d_cnt = nullptr;
   size_t cap_cnt = 0;
@@ -733,6 +824,19 @@ GB300_API void grid_gb300_taskgen_create(
   for (int l = 0; l < nlevels; l++)
     P.cutoff[l] = cutoff[l];
   P.maxpgf = maxpgf;
+  for (int a = 0; a < 3; a++) {
+    double nrm = 0.0;
+    for (int b = 0; b < 3; b++) {
+      P.cellf[a][b] = (float)cell[3 * a + b];
+      nrm += cell[3 * a + b] * cell[3 * a + b];
+    }
+    P.cellnorm[a] = (float)std::sqrt(nrm);
+  }
+  P.rmaxf = (float)rmax;
+  P.leps = (float)std::log(eps);
+  std::vector<float> zetf((size_t)nsets * maxpgf);
+  for (size_t q = 0; q < zetf.size(); q++)
+    zetf[q] = (float)zet[q];
   auto up = [](auto *&dst, const auto *src, size_t n) {
     CKT(cudaMalloc((void **)&dst, std::max<size_t>(n, 1) * sizeof(*src)));
     if (n)
@@ -745,6 +849,7 @@ GB300_API void grid_gb300_taskgen_create(
   up(g->d_lmax, set_lmax, nsets);
   up(g->d_npgf, set_npgf, nsets);
   up(g->d_zet, zet, (size_t)nsets * maxpgf);
+  up(g->d_zetf, zetf.data(), zetf.size());
   CKT(cudaMalloc((void **)&g->d_pos, sizeof(double) * 3 * natoms));
   CKT(cudaMallocHost((void **)&g->h_tot, sizeof(V2)));
   P.pos = g->d_pos;
@@ -755,6 +860,7 @@ GB300_API void grid_gb300_taskgen_create(
   P.lmax = g->d_lmax;
   P.npgf = g->d_npgf;
   P.zet = g->d_zet;
+  P.zetf = g->d_zetf;
   *generator = g;
 }
 
@@ -764,7 +870,7 @@ GB300_API void grid_gb300_taskgen_free(grid_gb300_task_generator *generator) {
   if (!g)
     return;
   void *d[] = {g->d_kind, g->d_set_off, g->d_nset, g->d_nsgf, g->d_lmax, g->d_npgf,
-               g->d_zet, g->d_pos, g->d_cnt, g->d_partial, g->d_pair_i, g->d_pair_j,
+               g->d_zet, g->d_zetf, g->d_pos, g->d_cnt, g->d_partial, g->d_pair_i, g->d_pair_j,
                g->d_size, g->d_task0, g->d_radius, g->d_rab, g->d_block_offsets};
   for (void *p : d)
     if (p)
