@@ -22,6 +22,10 @@ grid_integrate_task_list (hab only), as one SCF iteration does.
              the mixed step with one feature switched back (diagnostics);
   hartree_step_on_device  collocate -> plane waves -> Hartree potential ->
              level grids -> integrate, every buffer on the device;
+  task_generation  the geometry's task list generated on the device against
+             the host generator (time, equality), the task list created from
+             it, and the pab blocks packed from / added back to a block store
+             on the device (GB/s against the measured HBM roof);
   cpu_baseline  whole SCF steps of the oracle (FP64 C restatement of CP2K's
              REF backend) on all host cores;
   triclinic_256atoms_forces_virial, c5_6144atoms_forces
@@ -405,6 +409,76 @@ def hartree_step(torch, G, tl, inp, pab, grids, hab, stream, flush, nsteps):
                      "potential_g2rs, integrate; all buffers on the device"}
 
 
+def task_generation(torch, G, inp, host_s, pab=None, flush=None, peaks=None, reps=5):
+    """The workload's task list generated on the device (grid_gb300_taskgen_run:
+    the screening, radii, levels and block offsets of CP2K's
+    generate_qs_task_list) against the host generator's arrays, the task list
+    created from it; with `pab`, the density-matrix blocks gathered on the
+    device from a block store into the pab buffer (rs_pack_buffer) and added
+    back (rs_unpack_buffer), against the HBM roof."""
+    gen = G.TaskGenerator(inp)
+    gen.run(inp.atom_positions)
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        gen.run(inp.atom_positions)
+        ts.append((time.perf_counter() - t0) * 1e3)
+    arrays = gen.host_arrays()
+    equal = all(np.array_equal(np.asarray(getattr(inp, k)).reshape(v.shape), v)
+                for k, v in arrays.items())
+    t0 = time.perf_counter()
+    tl2 = G.GridTaskList.from_generator(gen, precision=None, schedule=None)
+    create_s = time.perf_counter() - t0
+    tl2.close()
+    gen.free()
+    res = {"ntasks": inp.ntasks, "device_ms": float(np.median(ts)),
+           "host_generator_s": host_s, "arrays_equal_host_generator": bool(equal),
+           "create_task_list_from_device_arrays_s": create_s,
+           "timing": "wall clock of the whole call (positions upload, 5 kernels, 2 reads of "
+                     "the totals), median of %d" % reps}
+    if pab is None:
+        return res
+    # a block store: the task list's blocks at shuffled places in one arena
+    dev = pab.device
+    blk = inp.block_num_list - 1
+    first = np.unique(blk, return_index=True)[1]
+    nsgf = np.array([inp.basis_sets[k - 1].nsgf for k in inp.atom_kinds])
+    sizes = (nsgf[inp.iatom_list[first] - 1] * nsgf[inp.jatom_list[first] - 1]).astype(np.int32)
+    perm = np.random.default_rng(0).permutation(len(sizes))
+    store_off = np.zeros(len(sizes), np.int64)
+    store_off[perm] = np.concatenate([[0], np.cumsum(sizes[perm].astype(np.int64))[:-1]])
+    t = lambda a: torch.tensor(np.ascontiguousarray(a), device=dev)
+    d_store_off, d_sizes = t(store_off), t(sizes)
+    d_boff = t(np.ascontiguousarray(inp.block_offsets, np.int32))
+    store = torch.zeros(int(sizes.astype(np.int64).sum()), dtype=torch.float64, device=dev)
+    G.unpack_blocks(d_boff, d_store_off, d_sizes, pab, store)
+    out = torch.empty_like(pab)
+    moved = 8.0 * float(sizes.astype(np.int64).sum())
+    for name, fn, nbytes in (
+            ("pack", lambda: G.pack_blocks(d_store_off, d_boff, d_sizes, store, out), 2 * moved),
+            ("unpack", lambda: G.unpack_blocks(d_boff, d_store_off, d_sizes, pab, store),
+             3 * moved)):
+        fn()
+        times = []
+        for _ in range(reps):
+            flush.zero_()
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            torch.cuda.synchronize()
+            e[0].record()
+            fn()
+            e[1].record()
+            torch.cuda.synchronize()
+            times.append(e[0].elapsed_time(e[1]))
+        ms = float(np.median(times))
+        gbs = nbytes / ms * 1e-6
+        res[name] = {"ms": ms, "bytes": nbytes, "gbs": gbs,
+                     "frac_of_measured_hbm": gbs / peaks.get("hbm_gbs", 1.0)}
+    res["pack"]["equal"] = bool(torch.equal(out, pab))
+    del store, out
+    torch.cuda.empty_cache()
+    return res
+
+
 def secondary_case(torch, G, W, name, forces, virial, nsteps, cpu_steps, flush):
     """Mixed and FP64 step times (device-resident, default launch shapes, size
     schedule) of another workload, with forces / virial as its configuration
@@ -413,6 +487,7 @@ def secondary_case(torch, G, W, name, forces, virial, nsteps, cpu_steps, flush):
     dev = torch.device("cuda", torch.cuda.current_device())
     t0 = time.perf_counter()
     inp = W.config(name)
+    host_gen_s = time.perf_counter() - t0
     pab_h = W.density_blocks(inp)
     V_h = W.potential_grids(inp)
     gen_s = time.perf_counter() - t0
@@ -451,6 +526,7 @@ def secondary_case(torch, G, W, name, forces, virial, nsteps, cpu_steps, flush):
                      f.cpu().numpy() if f is not None else None,
                      vir.cpu().numpy() if vir is not None else None)
     res["speedup_vs_fp64"] = res["fp64_ms_per_step"] / res["mixed_ms_per_step"]
+    res["task_generation"] = task_generation(torch, G, inp, host_gen_s)
     tl.close()
     del pab, V, grids, hab, f, vir
     torch.cuda.empty_cache()
@@ -472,7 +548,9 @@ def gpu_arm(args, world, rank, local):
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    t0 = time.perf_counter()
     inp = W.config(WORKLOAD)
+    host_gen_s = time.perf_counter() - t0
     pab_h = W.density_blocks(inp)
     V_h = W.potential_grids(inp)
     pab = torch.tensor(pab_h, device=dev)
@@ -588,6 +666,7 @@ def gpu_arm(args, world, rank, local):
     hab32 = hab.cpu().numpy()
     hartree = hartree_step(torch, G, tl, inp, pab, grids, hab, stream, flush,
                            max(1, min(args.steps, 5)))
+    taskgen = task_generation(torch, G, inp, host_gen_s, pab, flush, _peaks()[0])
 
     ms_mixed = max_over_ranks(float(np.mean(t_mixed)), world)
     ms_model = max_over_ranks(float(np.mean(t_model)), world) if t_model else None
@@ -669,6 +748,7 @@ def gpu_arm(args, world, rank, local):
             "mixed_no_row_split_ms_per_step": max_over_ranks(float(np.mean(t_no_row_split)),
                                                              world),
             "hartree_step_on_device": hartree,
+            "task_generation": taskgen,
             "row_split": {"tasks_split": row_split_share[0],
                           "fp32_share_of_points": row_split_share[1],
                           "fp32_class_share_of_points": row_split_share[2]},
