@@ -30,10 +30,11 @@
 // (Fortran's r**l).  The values written (rab, radius) are always exact
 // double results.
 //
-// Kernels: one warp per atom pair counts the tasks of its images (lanes over
-// images); a three-phase scan turns the counts into task offsets and block
-// numbers; one warp per block writes its tasks in order; one thread per task
-// finds the radius.  Two synchronisations per run read back the totals.
+// Kernels: one thread per atom pair counts the tasks of its images (only the
+// images whose lattice box can reach the distance cut are visited); a
+// three-phase scan turns the counts into task offsets and block numbers; one
+// thread per block writes its tasks in order; one thread per task finds the
+// radius.  Two synchronisations per run read back the totals.
 //
 // Packing is rs_pack_buffer / rs_unpack_buffer (src/task_list_methods.F:
 // 2593-2674) on device memory: blocks gathered from a block store into the
@@ -79,7 +80,6 @@ struct TgParams {
   int natoms;
   long long npairs;
   int nimg[3];
-  int nimages;
   double cell[3][3];
   double rmax, eps, rel_cutoff;
   int nlevels;
@@ -87,6 +87,7 @@ struct TgParams {
   int maxpgf;
   // single-precision copies for the screening decisions
   float cellf[3][3], cellnorm[3], rmaxf, leps;
+  float cinvf[3][3], hf[3];  // inverse cell; column norms (reciprocal lengths)
   const float *zetf;   // [nsets][maxpgf]
   const double *pos;   // [natoms][3]
   const int *kind;     // [natoms], 0-based
@@ -97,6 +98,20 @@ struct TgParams {
   const int *npgf;     // [nsets]
   const double *zet;   // [nsets][maxpgf]
 };
+
+struct BinomTable {
+  double v[kTgMaxL + 1][kTgMaxL + 1];
+};
+constexpr BinomTable make_binom() {
+  BinomTable t{};
+  for (int n = 0; n <= kTgMaxL; n++) {
+    t.v[n][0] = 1.0;
+    for (int k = 1; k <= n; k++)
+      t.v[n][k] = t.v[n][k - 1] * (n - k + 1) / k;
+  }
+  return t;
+}
+__constant__ BinomTable kBinom = make_binom();
 
 struct TgOut {
   int *level, *iatom, *jatom, *iset, *jset, *ipgf, *jpgf, *border_mask, *block_num;
@@ -125,21 +140,6 @@ __device__ void pair_of(long long p, int n, int &i, int &j) {
     r++;
   i = (int)r;
   j = (int)(r + (p - row_start(r, n)));
-}
-
-// image index -> (n0, n1, n2), n2 fastest; false when the image is skipped
-// for a diagonal pair
-__device__ __forceinline__ bool image_of(const TgParams &P, int img, bool diag, int n[3]) {
-  const int w2 = 2 * P.nimg[2] + 1, w1 = 2 * P.nimg[1] + 1;
-  n[2] = img % w2 - P.nimg[2];
-  n[1] = (img / w2) % w1 - P.nimg[1];
-  n[0] = img / (w2 * w1) - P.nimg[0];
-  if (diag) {
-    const int lex = n[0] != 0 ? n[0] : (n[1] != 0 ? n[1] : n[2]);
-    if (lex < 0)
-      return false;
-  }
-  return true;
 }
 
 // rab of image n and |rab|^2, in the host code's order of operations
@@ -207,50 +207,69 @@ __device__ __forceinline__ PairPos pair_pos(const TgParams &P, int i, int j) {
   return q;
 }
 
-// tasks of image `img` of pair (i, j) (0 outside the cut or skipped); the
-// distance cut is tried in single precision first with a margin above its
-// rounding error
-__device__ int lane_image_tasks(const TgParams &P, int i, int j, const PairPos &q, int img,
-                                double rab[3], double &rab2) {
-  int n[3];
-  if (!image_of(P, img, i == j, n))
-    return 0;
-  float rf2 = 0.0f;
+// The images n of pair (i, j) within the distance cut, in the host's order
+// (n0, n1, n2 lexicographic; for i == j image 0 and the images whose first
+// non-zero index is positive), f(n, rab, rab2) for each.  Only the box of
+// lattice coordinates that can reach the cut is searched:
+// |u_k + n_k| <= rmax |b_k| with u the pair's difference in lattice
+// coordinates and b_k the reciprocal vectors, widened above the rounding of
+// the single-precision bounds.  Each candidate is tried against the cut in
+// single precision with a margin, then exactly.
+template <class F>
+__device__ __forceinline__ void for_images(const TgParams &P, int i, int j, const PairPos &q,
+                                           F &&f) {
+  int lo[3], hi[3];
 #pragma unroll
-  for (int d = 0; d < 3; d++) {
-    const float x = q.df[d] + (float)n[0] * P.cellf[0][d] + (float)n[1] * P.cellf[1][d] +
-                    (float)n[2] * P.cellf[2][d];
-    rf2 += x * x;
+  for (int k = 0; k < 3; k++) {
+    const float u = q.df[0] * P.cinvf[0][k] + q.df[1] * P.cinvf[1][k] + q.df[2] * P.cinvf[2][k];
+    const float w = P.rmaxf * P.hf[k];
+    const float m = 1e-4f + 1e-6f * (fabsf(u) + w);
+    const float nk = (float)P.nimg[k];
+    lo[k] = (int)fminf(fmaxf(ceilf(-u - w - m), -nk), nk + 1.0f);
+    hi[k] = (int)fminf(fmaxf(floorf(-u + w + m), -nk - 1.0f), nk);
   }
-  const float span = P.rmaxf + fabsf(q.df[0]) + fabsf(q.df[1]) + fabsf(q.df[2]) +
-                     fabsf((float)n[0]) * P.cellnorm[0] + fabsf((float)n[1]) * P.cellnorm[1] +
-                     fabsf((float)n[2]) * P.cellnorm[2];
-  const float lim = P.rmaxf + 1e-5f * span + 1e-6f;
-  if (rf2 > lim * lim)
-    return 0;
-  rab2 = image_rab(P, q.ra, q.rj, n, rab);
-  if (rab2 > dmul(P.rmax, P.rmax))
-    return 0;
-  return image_tasks(P, P.kind[i], P.kind[j], rab2);
+  const double rmax2 = dmul(P.rmax, P.rmax);
+  for (int n0 = lo[0]; n0 <= hi[0]; n0++)
+    for (int n1 = lo[1]; n1 <= hi[1]; n1++)
+      for (int n2 = lo[2]; n2 <= hi[2]; n2++) {
+        const int n[3] = {n0, n1, n2};
+        if (i == j) {
+          const int lex = n0 != 0 ? n0 : (n1 != 0 ? n1 : n2);
+          if (lex < 0)
+            continue;
+        }
+        float rf2 = 0.0f;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          const float x = q.df[d] + (float)n0 * P.cellf[0][d] + (float)n1 * P.cellf[1][d] +
+                          (float)n2 * P.cellf[2][d];
+          rf2 += x * x;
+        }
+        const float span = P.rmaxf + fabsf(q.df[0]) + fabsf(q.df[1]) + fabsf(q.df[2]) +
+                           fabsf((float)n0) * P.cellnorm[0] + fabsf((float)n1) * P.cellnorm[1] +
+                           fabsf((float)n2) * P.cellnorm[2];
+        const float lim = P.rmaxf + 1e-5f * span + 1e-6f;
+        if (rf2 > lim * lim)
+          continue;
+        double rab[3];
+        const double rab2 = image_rab(P, q.ra, q.rj, n, rab);
+        if (rab2 > rmax2)
+          continue;
+        f(rab, rab2);
+      }
 }
 
-// one warp per atom pair: number of tasks over all images
+// one thread per atom pair: number of tasks over its images
 __global__ void __launch_bounds__(256) pair_count_kernel(TgParams P, int *__restrict__ cnt) {
-  const int lane = threadIdx.x & 31;
-  const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long p = w0; p < P.npairs; p += nw) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < P.npairs;
+       p += (long long)gridDim.x * blockDim.x) {
     int i, j;
     pair_of(p, P.natoms, i, j);
     const PairPos q = pair_pos(P, i, j);
+    const int ki = P.kind[i], kj = P.kind[j];
     int c = 0;
-    for (int img = lane; img < P.nimages; img += 32) {
-      double rab[3], rab2;
-      c += lane_image_tasks(P, i, j, q, img, rab, rab2);
-    }
-    c = __reduce_add_sync(0xffffffffu, c);
-    if (lane == 0)
-      cnt[p] = c;
+    for_images(P, i, j, q, [&](const double *, double rab2) { c += image_tasks(P, ki, kj, rab2); });
+    cnt[p] = c;
   }
 }
 
@@ -399,36 +418,20 @@ __device__ int grid_level(const TgParams &P, double zetp) {
   return lev;
 }
 
-// one warp per block: the tasks of the block's pair, images in order
+// one thread per block: the tasks of the block's pair, images in order
 __global__ void __launch_bounds__(256)
     fill_tasks_kernel(TgParams P, long long nblocks, const int *__restrict__ pair_i,
                       const int *__restrict__ pair_j, const long long *__restrict__ task0,
                       TgOut o) {
-  const int lane = threadIdx.x & 31;
-  const long long w0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long b = w0; b < nblocks; b += nw) {
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < nblocks;
+       b += (long long)gridDim.x * blockDim.x) {
     const int i = pair_i[b], j = pair_j[b];
     const int ki = P.kind[i], kj = P.kind[j];
     const PairPos q = pair_pos(P, i, j);
-    long long base = task0[b];
-    for (int img0 = 0; img0 < P.nimages; img0 += 32) {
-      const int img = img0 + lane;
-      double rab[3] = {0.0, 0.0, 0.0}, rab2 = 0.0;
-      const int c = img < P.nimages ? lane_image_tasks(P, i, j, q, img, rab, rab2) : 0;
-      int inc = c;
-#pragma unroll
-      for (int o2 = 1; o2 < 32; o2 <<= 1) {
-        const int u = __shfl_up_sync(0xffffffffu, inc, o2);
-        if (lane >= o2)
-          inc += u;
-      }
-      long long t = base + inc - c;
-      base += __shfl_sync(0xffffffffu, inc, 31);
-      if (c == 0)
-        continue;
+    long long t = task0[b];
+    const int si0 = P.set_off[ki], sj0 = P.set_off[kj];
+    for_images(P, i, j, q, [&](const double *rab, double rab2) {
       const float rab2f = __double2float_rn(rab2);
-      const int si0 = P.set_off[ki], sj0 = P.set_off[kj];
       for (int is = 0; is < P.nset[ki]; is++)
         for (int ip = 0; ip < P.npgf[si0 + is]; ip++) {
           const size_t ia = (size_t)(si0 + is) * P.maxpgf + ip;
@@ -455,7 +458,7 @@ __global__ void __launch_bounds__(256)
               t++;
             }
         }
-    }
+    });
   }
 }
 
@@ -567,6 +570,15 @@ __global__ void __launch_bounds__(128) radius_kernel(TgParams P, long long ntask
     rad_a = __dsqrt_rn(rad_a);
     rad_b = __dsqrt_rn(rad_b);
     const int la = P.lmax[gi], lb = P.lmax[gj];
+    // the powers rad^i and the binomials of the host's recurrences (there
+    // s1 = s1 rad from 1, and bin (n - i) / (i + 1), whose every step is an
+    // exact integer, i.e. the binomial coefficients of the table)
+    double pa[kTgMaxL + 1], pb[kTgMaxL + 1];
+    pa[0] = pb[0] = 1.0;
+    for (int k = 1; k <= la; k++)
+      pa[k] = dmul(pa[k - 1], rad_a);
+    for (int k = 1; k <= lb; k++)
+      pb[k] = dmul(pb[k - 1], rad_b);
     double poly[kTgPoly];
     for (int k = 0; k <= la + lb; k++)
       poly[k] = 0.0;
@@ -575,18 +587,12 @@ __global__ void __launch_bounds__(128) radius_kernel(TgParams P, long long ntask
         double coef[kTgPoly];
         for (int k = 0; k <= lxa + lxb; k++)
           coef[k] = 0.0;
-        double bini = 1.0, s1 = 1.0;
-        for (int ii = 0; ii <= lxa; ii++) {
-          double binj = 1.0, s2 = 1.0;
+        for (int ii = 0; ii <= lxa; ii++)
           for (int jj = 0; jj <= lxb; jj++) {
             const int k = lxa + lxb - ii - jj;
-            coef[k] = dadd(coef[k], dmul(dmul(dmul(bini, binj), s1), s2));
-            binj = ddiv(dmul(binj, (double)(lxb - jj)), (double)(jj + 1));
-            s2 = dmul(s2, rad_b);
+            const double bb = dmul(kBinom.v[lxa][ii], kBinom.v[lxb][jj]);
+            coef[k] = dadd(coef[k], dmul(dmul(bb, pa[ii]), pb[jj]));
           }
-          bini = ddiv(dmul(bini, (double)(lxa - ii)), (double)(ii + 1));
-          s1 = dmul(s1, rad_a);
-        }
         for (int k = 0; k <= lxa + lxb; k++)
           poly[k] = fmax(poly[k], coef[k]);
       }
@@ -683,6 +689,11 @@ int warp_grid(long long nwarps) {
   const long long cap = 152LL * 16;
   const long long blocks = (nwarps + 7) / 8;
   return (int)std::max(1LL, std::min(blocks, cap));
+}
+
+int thread_grid(long long n) {
+  const long long cap = 152LL * 32;
+  return (int)std::max(1LL, std::min((n + 255) / 256, cap));
 }
 
 template <class T> void grow(T *&p, size_t &cap, size_t n) {
@@ -808,12 +819,8 @@ GB300_API void grid_gb300_taskgen_create(
   TgParams &P = g->P;
   P.natoms = natoms;
   P.npairs = (long long)natoms * (natoms + 1) / 2;
-  int nimg = 1;
-  for (int d = 0; d < 3; d++) {
+  for (int d = 0; d < 3; d++)
     P.nimg[d] = nimages[d];
-    nimg *= 2 * nimages[d] + 1;
-  }
-  P.nimages = nimg;
   for (int a = 0; a < 3; a++)
     for (int b = 0; b < 3; b++)
       P.cell[a][b] = cell[3 * a + b];
@@ -831,6 +838,29 @@ GB300_API void grid_gb300_taskgen_create(
       nrm += cell[3 * a + b] * cell[3 * a + b];
     }
     P.cellnorm[a] = (float)std::sqrt(nrm);
+  }
+  {
+    // inverse of the cell (rows: cell vectors), for the image boxes
+    const double *m = cell;
+    const double det = m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+                       m[2] * (m[3] * m[7] - m[4] * m[6]);
+    if (!(std::fabs(det) > 0.0))
+      tg_fail("singular cell", 0);
+    double inv[3][3];
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 3; c++) {
+        // cofactor of (c, r) over det
+        const int r1 = (c + 1) % 3, r2 = (c + 2) % 3, c1 = (r + 1) % 3, c2 = (r + 2) % 3;
+        inv[r][c] = (m[3 * r1 + c1] * m[3 * r2 + c2] - m[3 * r1 + c2] * m[3 * r2 + c1]) / det;
+      }
+    for (int k = 0; k < 3; k++) {
+      double h = 0.0;
+      for (int r = 0; r < 3; r++) {
+        P.cinvf[r][k] = (float)inv[r][k];
+        h += inv[r][k] * inv[r][k];
+      }
+      P.hf[k] = (float)std::sqrt(h);
+    }
   }
   P.rmaxf = (float)rmax;
   P.leps = (float)std::log(eps);
@@ -903,7 +933,7 @@ GB300_API void grid_gb300_taskgen_run(grid_gb300_task_generator *generator,
   }
   // 1. tasks per atom pair
   grow(g->d_cnt, g->cap_cnt, (size_t)P.npairs);
-  pair_count_kernel<<<warp_grid(P.npairs), 256, 0, s>>>(P, g->d_cnt);
+  pair_count_kernel<<<thread_grid(P.npairs), 256, 0, s>>>(P, g->d_cnt);
   count_launch();
   CKT(cudaGetLastError());
   // 2. task offsets and block numbers of the pairs with tasks
@@ -931,7 +961,7 @@ GB300_API void grid_gb300_taskgen_run(grid_gb300_task_generator *generator,
   grow(g->d_rab, g->cap_rab, (size_t)g->ntasks * 3);
   const TgOut o = g->out();
   if (g->nblocks > 0) {
-    fill_tasks_kernel<<<warp_grid(g->nblocks), 256, 0, s>>>(P, g->nblocks, g->d_pair_i,
+    fill_tasks_kernel<<<thread_grid(g->nblocks), 256, 0, s>>>(P, g->nblocks, g->d_pair_i,
                                                             g->d_pair_j, g->d_task0, o);
     count_launch();
   }

@@ -4,7 +4,9 @@ resident), e.g. as the workload of a profiler:
     python -m cp2k_gb300.run_case --config c2_512atoms --scale 0.5 \\
         --precision mixed --steps 2
 
-Prints the per-phase kernel times of every step.  With --compare the step is
+Prints the per-phase kernel times of every step.  --taskgen instead runs the
+device task-list generator (and the block packing) on the configuration's
+geometry.  With --compare the step is
 also run in FP64 on the same inputs, and one JSON line reports the median
 step times (CUDA events) of both and the errors of the chosen precision
 against FP64: max relative rho (reference measure), Tr(V rho) energy per
@@ -32,6 +34,31 @@ def _step(tl, pab, V, grids, hab, f, vir, s):
     return e0.elapsed_time(e1)
 
 
+def _taskgen(inp, steps):
+    import time
+    gen = G.TaskGenerator(inp)
+    ms = []
+    for _ in range(max(1, steps)):
+        t0 = time.perf_counter()
+        gen.run(inp.atom_positions)
+        ms.append((time.perf_counter() - t0) * 1e3)
+    a = gen.host_arrays()
+    equal = all(np.array_equal(np.asarray(getattr(inp, k)).reshape(v.shape), v)
+                for k, v in a.items())
+    # pab blocks from a block store holding them in task-list order
+    boff = torch.tensor(np.ascontiguousarray(inp.block_offsets, np.int32), device="cuda")
+    sizes = np.diff(np.append(inp.block_offsets.astype(np.int64), inp.buffer_size))
+    src = torch.tensor(W.density_blocks(inp), device="cuda")
+    dst = torch.empty_like(src)
+    G.pack_blocks(boff.to(torch.int64), boff, torch.tensor(sizes.astype(np.int32), device="cuda"),
+                  src, dst)
+    torch.cuda.synchronize()
+    print(json.dumps({"ntasks": gen.ntasks, "nblocks": gen.nblocks, "run_ms": ms,
+                      "arrays_equal_host_generator": bool(equal),
+                      "pack_equal": bool(torch.equal(src, dst))}), flush=True)
+    gen.free()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--config", default="c2_512atoms", choices=sorted(W.CONFIGS))
@@ -48,8 +75,14 @@ def main():
                     help="C_ab <-> C_xyz transform: 0 direct, 1 staged, -1 staged forward")
     ap.add_argument("--compare", action="store_true",
                     help="also run FP64 and print times and errors as one JSON line")
+    ap.add_argument("--taskgen", action="store_true",
+                    help="generate the task list on the device --steps times (and pack the "
+                         "pab blocks once), check it against the host generator, print times")
     args = ap.parse_args()
     inp = W.config(args.config, scale=args.scale)
+    if args.taskgen:
+        _taskgen(inp, args.steps)
+        return
     pab = torch.tensor(W.density_blocks(inp), device="cuda")
     V = [torch.tensor(v, device="cuda") for v in W.potential_grids(inp)]
     grids = [torch.empty(n, dtype=torch.float64, device="cuda") for n in inp.grid_sizes()]
