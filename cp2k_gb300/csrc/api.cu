@@ -274,6 +274,7 @@ struct Queue {
   int side = 0; // row split: 0 whole tasks, 1 rows inside the cylinder, 2 rows outside
   int key = 0;          // (general, bucket, FP32 class, size class)
   int base = 0;         // key of the tuned launch shapes
+  int chunk = 0;        // host-buffer calls: the copy chunk whose tasks it holds
   long long points = 0; // grid points the queue's tasks visit
   double flops = 0.0;   // 2 (lp+1) points summed over the tasks
 };
@@ -1362,6 +1363,19 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase, int nch = 1) {
       }
     }
   }
+  // host-buffer calls: each copy chunk gets queues of its own tasks, so that
+  // a chunk's grid kernels run while the next chunk is copied
+  std::vector<int> chunk_of;
+  if (nch > 1) {
+    chunk_of.assign(t->ntasks, 0);
+    for (int c = 0; c < nch; c++) {
+      const int sa = t->chunks.sub_lo[c], sb = t->chunks.sub_lo[c + 1];
+      const int t0 = sa < (int)t->subs.size() ? t->subs[sa].first_task : t->ntasks;
+      const int t1 = sb < (int)t->subs.size() ? t->subs[sb].first_task : t->ntasks;
+      for (int s = t0; s < t1; s++)
+        chunk_of[s] = c;
+    }
+  }
   // heavier classes first: large cubes, then the arithmetic of the mode, FP32 last
   std::vector<int> keys;
   for (auto &kv : items)
@@ -1374,13 +1388,25 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase, int nch = 1) {
       return sx > sy;
     return x < y;
   });
+  for (auto &kv : items)
+    std::stable_sort(kv.second.begin(), kv.second.end(),
+                     [](const std::pair<double, int> &x, const std::pair<double, int> &y) {
+                       return x.first > y.first;
+                     });
+  for (int qc = 0; qc < (nch > 1 ? nch : 1); qc++)
   for (int key : keys) {
-    auto &v = items[key];
-    std::stable_sort(v.begin(), v.end(), [](const std::pair<double, int> &x,
-                                            const std::pair<double, int> &y) {
-      return x.first > y.first;
-    });
+    std::vector<std::pair<double, int>> v;
+    if (nch > 1) {
+      for (const auto &e : items[key])
+        if (chunk_of[e.second] == qc)
+          v.push_back(e);
+      if (v.empty())
+        continue;
+    } else {
+      v.swap(items[key]);
+    }
     Queue q;
+    q.chunk = qc;
     q.key = key;
     q.base = key; // shell queues tune apart from the FP32 class's
     const int kb = key % kQueueKeys;
@@ -1662,8 +1688,35 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
   ga.task_cycles = t->task_timing ? t->d_cycles : nullptr;
   ga.seeds = t->d_seeds;
   ga.error = t->d_error;
+  int qi = 0;
+  auto launch_queues = [&](int chunk) {
+    fork_queues(t, s);
+    for (const Queue &q : m.queues) {
+      if (chunk >= 0 && q.chunk != chunk)
+        continue;
+      ga.queue = q.d_idx;
+      ga.items = q.d_items;
+      ga.iwidth = q.iwidth;
+      ga.nqueue = q.d_items ? q.nitems : q.n;
+      if (qi >= kMaxQueues)
+        fail("more than %d work queues in one call", kMaxQueues);
+      ga.counter = t->d_counters + qi++;
+      // FP32 queues read the high words of the coefficient slots (shell
+      // queues: of the split tasks' double-float coefficients)
+      ga.coef_stride = q.fp32 ? 2 : 1;
+      ga.core_side = q.side;
+      ga.core_r2 = q.side ? m.d_core_r2 : nullptr;
+      grid_launch(t, q, 0, q.fp32 ? (int)ARITH_FP32 : arith, ga, queue_stream(t, s, qi));
+      if (q.side != 2)
+        grid_library_counter_add(kBucketLp[q.bucket], GRID_BACKEND_GB300,
+                                 q.general ? GRID_COLLOCATE_GENERAL : GRID_COLLOCATE_ORTHO, q.n);
+    }
+    join_queues(t, s);
+  };
   // pab -> Cartesian -> coefficients, piece by piece where the host-buffer
-  // call copies pab in pieces (each waits for its piece only)
+  // call copies pab in pieces (each waits for its piece only); there each
+  // piece's grid kernels follow its coefficients, while the next piece is
+  // still being copied
   for (int c = 0; c < nch; c++) {
     int s0 = 0, ns = (int)t->subs.size();
     if (hc) { // this piece of pab is on the device
@@ -1700,31 +1753,13 @@ static void run_collocate(TaskList *t, int func, const double *pab, double *cons
     } else {
       launch_coefficients(co, arith, m.coef_words, s);
     }
+    if (c == 0)
+      record_phase(t, 1, s);
+    if (nch > 1)
+      launch_queues(c);
   }
-  record_phase(t, 1, s);
-  int qi = 0;
-  fork_queues(t, s);
-  {
-    for (const Queue &q : m.queues) {
-      ga.queue = q.d_idx;
-      ga.items = q.d_items;
-      ga.iwidth = q.iwidth;
-      ga.nqueue = q.d_items ? q.nitems : q.n;
-      if (qi >= kMaxQueues)
-        fail("more than %d work queues in one call", kMaxQueues);
-      ga.counter = t->d_counters + qi++;
-      // FP32 queues read the high words of the coefficient slots (shell
-      // queues: of the split tasks' double-float coefficients)
-      ga.coef_stride = q.fp32 ? 2 : 1;
-      ga.core_side = q.side;
-      ga.core_r2 = q.side ? m.d_core_r2 : nullptr;
-      grid_launch(t, q, 0, q.fp32 ? (int)ARITH_FP32 : arith, ga, queue_stream(t, s, qi));
-      if (q.side != 2)
-        grid_library_counter_add(kBucketLp[q.bucket], GRID_BACKEND_GB300,
-                                 q.general ? GRID_COLLOCATE_GENERAL : GRID_COLLOCATE_ORTHO, q.n);
-    }
-  }
-  join_queues(t, s);
+  if (nch == 1)
+    launch_queues(-1);
   if (arith == ARITH_MIXED)
     for (int l = 0; l < t->nlevels; l++) {
       const int *n = &t->npts_local[3 * l];
@@ -1808,9 +1843,11 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
               t->ntasks, tau ? 1 : 0, d, t->d_levels, t->d_dhtab, t->d_dhtab_f, t->d_dhtab_df,
               nullptr, 0, m.transform};
   int qi = 0;
-  fork_queues(t, s);
-  for (const Queue &q : m.queues) {
-    {
+  auto launch_queues = [&](int chunk) {
+    fork_queues(t, s);
+    for (const Queue &q : m.queues) {
+      if (chunk >= 0 && q.chunk != chunk)
+        continue;
       ga.queue = q.d_idx;
       ga.items = q.d_items;
       ga.iwidth = q.iwidth;
@@ -1833,13 +1870,23 @@ static void run_integrate(TaskList *t, bool tau, const double *pab, const double
         grid_library_counter_add(kBucketLp[q.bucket], GRID_BACKEND_GB300,
                                  q.general ? GRID_INTEGRATE_GENERAL : GRID_INTEGRATE_ORTHO, q.n);
     }
+    join_queues(t, s);
+  };
+  if (nch == 1) {
+    launch_queues(-1);
+    record_phase(t, 2, s);
   }
-  join_queues(t, s);
-  record_phase(t, 2, s);
   // integrated coefficients -> hab (forces, virial), piece by piece where the
   // host-buffer call copies hab out in pieces: the largest piece first, so
-  // that the copy left after the last kernel is the smallest one
+  // that the copy left after the last kernel is the smallest one; there each
+  // piece's grid kernels run first, so that its copy overlaps the next
+  // piece's grid kernels
   for (int ci = nch - 1; ci >= 0; ci--) {
+    if (nch > 1) {
+      launch_queues(ci);
+      if (ci == nch - 1)
+        record_phase(t, 2, s);
+    }
     if (nch > 1) {
       for (int cls = 0; cls < 2; cls++) {
         pa.order = m.d_chunk_idx[2 * ci + cls];
