@@ -775,6 +775,7 @@ def gpu_arm(args, world, rank, local):
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "e2e_copies_in_one_piece_ms": e2e_one_piece,
+            "e2e_steps_ms": [round(x, 3) for x in e2e],
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
         }
