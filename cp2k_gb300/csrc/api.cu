@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <thread>
 #include <array>
 #include <atomic>
@@ -297,6 +298,11 @@ struct Mode { // everything that depends on the l shifts of a call
   int *d_coef_off = nullptr;
   size_t coef_total = 0;
   std::vector<Queue> queues; // launch order
+  int *d_qidx = nullptr;     // every queue's task indices (queues point into it)
+  int2 *d_qitems = nullptr;  // every split queue's work items
+  // what the queues depend on: l shifts, precision, derivative factor, copy
+  // chunks (not the phase)
+  std::tuple<int, int, int, int> qsig{-1, -1, -1, -1};
   // host-buffer calls (nch > 1): per copy chunk and FP32 class (mixed mode)
   // the tasks whose coefficients (collocate) or post-processing (integrate)
   // depend on that chunk of pab / hab
@@ -313,6 +319,10 @@ struct Mode { // everything that depends on the l shifts of a call
 };
 
 struct TaskList {
+  // row-split radii and outside shares per (l shifts, derivative factor,
+  // threshold), shared by the modes that need the same ones
+  std::map<std::tuple<int, int, int, double>, std::pair<std::vector<float>, std::vector<double>>>
+      core_cache;
   bool empty = false;
   bool ortho = true;
   int ntasks = 0, nlevels = 0, natoms = 0, nkinds = 0, nblocks = 0;
@@ -706,6 +716,12 @@ static float core_radius2(const TaskDesc &d, int dla, int dlb, double tau, doubl
   static thread_local double al[3][GB300_LMAX + 1][GB300_LMAX + 1][2 * GB300_LMAX + 2];
   for (int dir = 0; dir < 3; dir++) {
     const double pa = d.zetb / d.zetp * d.rab[dir], pb = pa - d.rab[dir];
+    double ppa[GB300_LMAX + 1], ppb[GB300_LMAX + 1];
+    ppa[0] = ppb[0] = 1.0;
+    for (int k = 1; k <= std::max(la, lb); k++) {
+      ppa[k] = ppa[k - 1] * pa;
+      ppb[k] = ppb[k - 1] * pb;
+    }
     for (int xa = 0; xa <= la; xa++)
       for (int xb = 0; xb <= lb; xb++) {
         double *c = al[dir][xa][xb];
@@ -713,7 +729,7 @@ static float core_radius2(const TaskDesc &d, int dla, int dlb, double tau, doubl
           c[n] = 0.0;
         for (int k = 0; k <= xa; k++)
           for (int q = 0; q <= xb; q++)
-            c[xa - k + xb - q] += bin[xa][k] * pow(pa, k) * bin[xb][q] * pow(pb, q);
+            c[xa - k + xb - q] += bin[xa][k] * ppa[k] * bin[xb][q] * ppb[q];
         for (int n = 0; n < nn; n++)
           c[n] = fabs(c[n]);
       }
@@ -752,7 +768,9 @@ static float core_radius2(const TaskDesc &d, int dla, int dlb, double tau, doubl
     return kCoreAll;
   double lo = r0, hi = R;
   if (f(r0) > tau) {
-    for (int it = 0; it < 40; it++) {
+    // 26 halvings leave hi within 2^-26 R above the crossing (the radius is
+    // kept as a float, rounded up)
+    for (int it = 0; it < 26; it++) {
       const double mid = 0.5 * (lo + hi);
       (f(mid) > tau ? lo : hi) = mid;
     }
@@ -798,12 +816,12 @@ static void free_device(TaskList *t) {
     for (int *p : kv.second.d_chunk_idx)
       if (p)
         cudaFree(p);
-    for (auto &q : kv.second.queues) {
-      if (q.d_idx)
-        cudaFree(q.d_idx);
-      if (q.d_items)
-        cudaFree(q.d_items);
-    }
+    if (kv.second.d_qidx)
+      cudaFree(kv.second.d_qidx);
+    if (kv.second.d_qitems)
+      cudaFree(kv.second.d_qitems);
+    if (kv.second.d_core_r2)
+      cudaFree(kv.second.d_core_r2);
   }
   for (auto &e : t->ev)
     if (e)
@@ -836,11 +854,34 @@ static bool sphi_is_identity(const grid_basis_set *b, int iset) {
   return true;
 }
 
-// Runs body(i) for i in [0, n) on the host's cores, in contiguous chunks.
-template <typename F> static void parallel_for(int n, const F &body) {
+// GRID_GB300_HOST_TIMING set: the host phases of task-list creation and of
+// the work-queue construction, in ms since the start of the call, on stderr
+struct HostPhases {
+  bool on;
+  const char *what;
+  std::chrono::steady_clock::time_point t0;
+  explicit HostPhases(const char *w)
+      : on(getenv("GRID_GB300_HOST_TIMING") != nullptr), what(w),
+        t0(std::chrono::steady_clock::now()) {}
+  void mark(const char *phase) const {
+    if (on)
+      fprintf(stderr, "grid_gb300 host %s: %s %.2f ms\n", what, phase,
+              std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0)
+                  .count());
+  }
+};
+
+// host threads for the preparation (GRID_GB300_HOST_THREADS fixes it)
+static int host_threads() {
   int nt = (int)std::max(1u, std::min(std::thread::hardware_concurrency(), 64u));
   if (const char *e = getenv("GRID_GB300_HOST_THREADS")) // testing: fix the thread count
     nt = std::max(1, std::min(atoi(e), 64));
+  return nt;
+}
+
+// Runs body(i) for i in [0, n) on the host's cores, in contiguous chunks.
+template <typename F> static void parallel_for(int n, const F &body) {
+  const int nt = host_threads();
   const int chunks = n < 4096 ? 1 : nt;
   if (chunks == 1) {
     for (int i = 0; i < n; i++)
@@ -858,6 +899,66 @@ template <typename F> static void parallel_for(int n, const F &body) {
     x.join();
 }
 
+// Runs body(i) for i in [0, n) on the host's cores, items taken one at a
+// time (for few items of uneven cost).
+template <typename F> static void parallel_items(int n, const F &body) {
+  const int nt = std::min(host_threads(), n);
+  if (nt <= 1) {
+    for (int i = 0; i < n; i++)
+      body(i);
+    return;
+  }
+  std::atomic<int> next{0};
+  std::vector<std::thread> th;
+  for (int c = 0; c < nt; c++)
+    th.emplace_back([&] {
+      for (int i = next++; i < n; i = next++)
+        body(i);
+    });
+  for (auto &x : th)
+    x.join();
+}
+
+// std::sort on the host's cores: chunks sorted in parallel, then merged
+// pairwise in rounds.  With a comparator that orders no two elements equal
+// the result is that of std::sort, whatever the number of threads.
+template <typename T, typename C> static void parallel_sort(std::vector<T> &v, C comp) {
+  const size_t n = v.size();
+  int nt = host_threads();
+  while (nt > 1 && n / (size_t)nt < 16384)
+    nt /= 2;
+  if (nt <= 1) {
+    std::sort(v.begin(), v.end(), comp);
+    return;
+  }
+  std::vector<size_t> b(nt + 1);
+  for (int c = 0; c <= nt; c++)
+    b[c] = n * (size_t)c / (size_t)nt;
+  {
+    std::vector<std::thread> th;
+    for (int c = 0; c < nt; c++)
+      th.emplace_back([&, c] { std::sort(v.begin() + b[c], v.begin() + b[c + 1], comp); });
+    for (auto &x : th)
+      x.join();
+  }
+  std::vector<T> tmp(n);
+  std::vector<T> *src = &v, *dst = &tmp;
+  for (int w = 1; w < nt; w *= 2) {
+    std::vector<std::thread> th;
+    for (int c = 0; c < nt; c += 2 * w)
+      th.emplace_back([&, c] {
+        const size_t lo = b[c], mid = b[std::min(c + w, nt)], hi = b[std::min(c + 2 * w, nt)];
+        std::merge(src->begin() + lo, src->begin() + mid, src->begin() + mid,
+                   src->begin() + hi, dst->begin() + lo, comp);
+      });
+    for (auto &x : th)
+      x.join();
+    std::swap(src, dst);
+  }
+  if (src != &v)
+    v.swap(*src);
+}
+
 static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nkinds,
                         int nblocks, const int *block_offsets, const double *atom_positions,
                         const int *atom_kinds, const grid_basis_set **basis_sets,
@@ -868,6 +969,7 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
                         const double *rab_list, const int *npts_global, const int *npts_local,
                         const int *shift_local, const int *border_width, const double *dh,
                         const double *dh_inv, bool host_only = false) {
+  const HostPhases hp("create");
   TaskList *t = new TaskList();
   t->ortho = ortho;
   t->ntasks = ntasks;
@@ -926,6 +1028,7 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
     if (!(radius_list[i] >= 0.0) || !std::isfinite(radius_list[i]))
       fail("task %d: invalid radius %g", i, radius_list[i]);
   }
+  hp.mark("validated");
   // stable order by (block, iset, jset, level): sort packed keys with the
   // input index as the last key
   {
@@ -933,9 +1036,12 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
       int block, iset, jset, level, i;
     };
     std::vector<Key> keys(ntasks);
-    for (int i = 0; i < ntasks; i++)
+    bool by_block = true; // input already in block order (as the generators make it)
+    for (int i = 0; i < ntasks; i++) {
       keys[i] = Key{block_num_list[i], iset_list[i], jset_list[i], level_list[i], i};
-    std::sort(keys.begin(), keys.end(), [](const Key &a, const Key &b) {
+      by_block = by_block && (i == 0 || block_num_list[i] >= block_num_list[i - 1]);
+    }
+    const auto less = [](const Key &a, const Key &b) {
       if (a.block != b.block)
         return a.block < b.block;
       if (a.iset != b.iset)
@@ -945,10 +1051,23 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
       if (a.level != b.level)
         return a.level < b.level;
       return a.i < b.i;
-    });
+    };
+    if (by_block) { // each block's run on its own, in parallel
+      std::vector<int> run = {0};
+      for (int i = 1; i < ntasks; i++)
+        if (keys[i].block != keys[i - 1].block)
+          run.push_back(i);
+      run.push_back(ntasks);
+      parallel_for((int)run.size() - 1, [&](int r) {
+        std::sort(keys.begin() + run[r], keys.begin() + run[r + 1], less);
+      });
+    } else {
+      parallel_sort(keys, less);
+    }
     for (int i = 0; i < ntasks; i++)
       order[i] = keys[i].i;
   }
+  hp.mark("sorted");
   // ---- tasks, subblocks, sphere tables
   t->tasks.resize(ntasks);
   t->points.assign(ntasks, 0);
@@ -1089,6 +1208,7 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
     fe[4] = (float)L.dh_max;
     fe[5] = (float)skew;
   });
+  hp.mark("per-task geometry");
   // Phase 2, in task order: the sphere tables of the orthorhombic tasks
   // (shared, built on first use) and the subblocks.
   std::vector<std::vector<char>> sphi_identity(nkinds); // per kind and set
@@ -1097,36 +1217,62 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
       sphi_identity[kd].push_back(sphi_is_identity(basis_sets[kd], st) ? 1 : 0);
   std::vector<std::vector<int>> sphere_of(nlevels); // [level][nrad] -> sphere, or -1
   std::vector<long long> sphere_points;
-  long long maxbuf = 0;
-  for (int s = 0; s < ntasks; s++) {
-    const int i = order[s];
-    TaskDesc &d = t->tasks[s];
-    const int lev = d.level, ia = d.iatom, ja = d.jatom;
-    const int iset = iset_list[i] - 1, jset = jset_list[i] - 1;
-    const grid_basis_set *bi = basis_sets[atom_kinds[ia] - 1];
-    const grid_basis_set *bj = basis_sets[atom_kinds[ja] - 1];
-    const LevelDesc &L = t->levels.lv[lev];
-    if (nrad_of[s] >= 0) {
-      const double drmin = fmin(L.dh[0], fmin(L.dh[4], L.dh[8]));
+  {
+    // the spheres in order of first use, then built in parallel and joined
+    std::vector<std::pair<int, int>> uniq; // (level, nrad)
+    for (int s = 0; s < ntasks; s++) {
+      if (nrad_of[s] < 0)
+        continue;
+      const int lev = t->tasks[s].level;
       const long long nrad = nrad_of[s];
-      std::vector<int> &known = sphere_of[lev];
       // the sphere tables hold int16 offsets: radii past 32767 grid steps
       // cannot be tabulated (and must not size this lookup)
       if (nrad > 32767)
-        fail("task %d: radius %g spans more than 32767 grid steps of level %d", i,
-             radius_list[i], lev);
+        fail("task %d: radius %g spans more than 32767 grid steps of level %d", order[s],
+             radius_list[order[s]], lev);
+      std::vector<int> &known = sphere_of[lev];
       if ((long long)known.size() <= nrad)
         known.resize((size_t)nrad + 1, -1);
       if (known[nrad] < 0) {
-        SphereHdr h;
-        long long np = 0;
-        build_sphere(L, drmin * (double)nrad, h, t->sph_tab, np);
-        build_sphere_points(h, t->sph_tab, t->sph_pts, t->sph_ploff);
-        t->sph.push_back(h);
-        sphere_points.push_back(np);
-        known[nrad] = (int)t->sph.size() - 1;
+        known[nrad] = (int)uniq.size();
+        uniq.emplace_back(lev, (int)nrad);
       }
-      d.sphere = known[nrad];
+    }
+    const int U = (int)uniq.size();
+    std::vector<SphereHdr> hdr(U);
+    std::vector<std::vector<int16_t>> tabs(U);
+    std::vector<std::vector<int>> pts(U), plo(U);
+    sphere_points.assign(U, 0);
+    parallel_items(U, [&](int u) {
+      const LevelDesc &L = t->levels.lv[uniq[u].first];
+      const double drmin = fmin(L.dh[0], fmin(L.dh[4], L.dh[8]));
+      build_sphere(L, drmin * (double)uniq[u].second, hdr[u], tabs[u], sphere_points[u]);
+      build_sphere_points(hdr[u], tabs[u], pts[u], plo[u]);
+    });
+    for (int u = 0; u < U; u++) {
+      SphereHdr h = hdr[u];
+      h.off += (int)t->sph_tab.size();
+      h.plo += (int)t->sph_ploff.size();
+      const long long base = (long long)t->sph_pts.size();
+      if (base + (long long)pts[u].size() > (long long)INT32_MAX)
+        fail("sphere point lists exceed int offsets");
+      t->sph_tab.insert(t->sph_tab.end(), tabs[u].begin(), tabs[u].end());
+      for (int e : plo[u])
+        t->sph_ploff.push_back((int)(e + base));
+      t->sph_pts.insert(t->sph_pts.end(), pts[u].begin(), pts[u].end());
+      t->sph.push_back(h);
+    }
+  }
+  // per task, in parallel: its sphere, point count and whether it starts a
+  // subblock (a new (block, iset, jset) in the sorted order)
+  std::vector<char> new_sub(ntasks, 0);
+  parallel_for(ntasks, [&](int s) {
+    const int i = order[s];
+    TaskDesc &d = t->tasks[s];
+    const int lev = d.level;
+    const LevelDesc &L = t->levels.lv[lev];
+    if (nrad_of[s] >= 0) {
+      d.sphere = sphere_of[lev][nrad_of[s]];
       const SphereHdr &h = t->sph[d.sphere];
       for (int k = 0; k < 3; k++)
         if (L.npts_global[k] != L.npts_local[k]) { // grid_ref_collint.h:247-255
@@ -1137,44 +1283,60 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
       t->points[s] = sphere_points[d.sphere];
       t->features[(size_t)s * 6 + 3] = (float)h.cmax;
     }
-    // subblock bookkeeping
+    const int p = s > 0 ? order[s - 1] : -1;
+    new_sub[s] = s == 0 || block_num_list[p] != block_num_list[i] || iset_list[p] != iset_list[i] ||
+                 jset_list[p] != jset_list[i];
+  });
+  // the subblocks in order (their Cartesian scratch offsets add up)
+  long long maxbuf = 0;
+  std::vector<int> sub_first;
+  for (int s = 0; s < ntasks; s++) {
+    if (!new_sub[s])
+      continue;
+    const int i = order[s];
+    const TaskDesc &d = t->tasks[s];
+    const int ia = d.iatom, ja = d.jatom;
+    const int iset = iset_list[i] - 1, jset = jset_list[i] - 1;
+    const grid_basis_set *bi = basis_sets[atom_kinds[ia] - 1];
+    const grid_basis_set *bj = basis_sets[atom_kinds[ja] - 1];
     const int bn = block_num_list[i] - 1;
-    const bool new_sub = s == 0 || block_num_list[order[s - 1]] != block_num_list[i] ||
-                         iset_list[order[s - 1]] != iset_list[i] ||
-                         jset_list[order[s - 1]] != jset_list[i];
-    if (new_sub) {
-      SubblockDesc sb;
-      memset(&sb, 0, sizeof(sb));
-      sb.block_offset = block_offsets[bn];
-      sb.ncoa = bi->npgf[iset] * ncoset(bi->lmax[iset]);
-      sb.ncob = bj->npgf[jset] * ncoset(bj->lmax[jset]);
-      sb.nsgf_seta = bi->nsgf_set[iset];
-      sb.nsgf_setb = bj->nsgf_set[jset];
-      sb.sgfa = bi->first_sgf[iset] - 1;
-      sb.sgfb = bj->first_sgf[jset] - 1;
-      sb.nsgfa = bi->nsgf;
-      sb.nsgfb = bj->nsgf;
-      sb.maxcoa = bi->maxco;
-      sb.maxcob = bj->maxco;
-      sb.sphia = (int)(sphi_off[atom_kinds[ia] - 1] + (long long)sb.sgfa * bi->maxco);
-      sb.sphib = (int)(sphi_off[atom_kinds[ja] - 1] + (long long)sb.sgfb * bj->maxco);
-      sb.transpose = ia <= ja;
-      sb.identity = sphi_identity[atom_kinds[ia] - 1][iset] && sphi_identity[atom_kinds[ja] - 1][jset];
-      sb.iatom = ia;
-      sb.jatom = ja;
-      sb.first_task = s;
-      sb.cart_offset = (int)t->cart_total;
-      t->cart_total += (size_t)sb.ncoa * sb.ncob;
-      if (t->cart_total > (size_t)INT32_MAX)
-        fail("Cartesian scratch exceeds int offsets");
-      t->contract_words = std::max(t->contract_words, sb.nsgf_setb * sb.ncoa);
-      t->subs.push_back(sb);
-      maxbuf = std::max(maxbuf, (long long)block_offsets[bn] + (long long)bi->nsgf * bj->nsgf);
-    }
-    t->subs.back().ntasks++;
-    d.subblock = (int)t->subs.size() - 1;
+    SubblockDesc sb;
+    memset(&sb, 0, sizeof(sb));
+    sb.block_offset = block_offsets[bn];
+    sb.ncoa = bi->npgf[iset] * ncoset(bi->lmax[iset]);
+    sb.ncob = bj->npgf[jset] * ncoset(bj->lmax[jset]);
+    sb.nsgf_seta = bi->nsgf_set[iset];
+    sb.nsgf_setb = bj->nsgf_set[jset];
+    sb.sgfa = bi->first_sgf[iset] - 1;
+    sb.sgfb = bj->first_sgf[jset] - 1;
+    sb.nsgfa = bi->nsgf;
+    sb.nsgfb = bj->nsgf;
+    sb.maxcoa = bi->maxco;
+    sb.maxcob = bj->maxco;
+    sb.sphia = (int)(sphi_off[atom_kinds[ia] - 1] + (long long)sb.sgfa * bi->maxco);
+    sb.sphib = (int)(sphi_off[atom_kinds[ja] - 1] + (long long)sb.sgfb * bj->maxco);
+    sb.transpose = ia <= ja;
+    sb.identity = sphi_identity[atom_kinds[ia] - 1][iset] && sphi_identity[atom_kinds[ja] - 1][jset];
+    sb.iatom = ia;
+    sb.jatom = ja;
+    sb.first_task = s;
+    sb.cart_offset = (int)t->cart_total;
+    t->cart_total += (size_t)sb.ncoa * sb.ncob;
+    if (t->cart_total > (size_t)INT32_MAX)
+      fail("Cartesian scratch exceeds int offsets");
+    t->contract_words = std::max(t->contract_words, sb.nsgf_setb * sb.ncoa);
+    t->subs.push_back(sb);
+    sub_first.push_back(s);
+    maxbuf = std::max(maxbuf, (long long)block_offsets[bn] + (long long)bi->nsgf * bj->nsgf);
   }
+  sub_first.push_back(ntasks);
+  parallel_for((int)t->subs.size(), [&](int u) {
+    t->subs[u].ntasks = sub_first[u + 1] - sub_first[u];
+    for (int s = sub_first[u]; s < sub_first[u + 1]; s++)
+      t->tasks[s].subblock = u;
+  });
   t->buffer_len = maxbuf;
+  hp.mark("spheres and subblocks");
   if (host_only) // grid_gb300_host_digest: the host preparation alone
     return t;
   // ---- upload
@@ -1212,12 +1374,34 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
   CK(cudaMalloc((void **)&t->d_counters, sizeof(int) * kMaxQueues));
   CK(cudaMalloc((void **)&t->d_error, sizeof(int)));
   CK(cudaMemset(t->d_error, 0, sizeof(int)));
+  hp.mark("uploaded");
   return t;
 }
 
 } // namespace gb300
 
 namespace gb300 {
+
+// frees a mode's work queues and their device arrays
+static void release_queues(Mode &m) {
+  if (m.d_core_r2)
+    cudaFree(m.d_core_r2);
+  m.d_core_r2 = nullptr;
+  if (m.d_qidx)
+    cudaFree(m.d_qidx);
+  if (m.d_qitems)
+    cudaFree(m.d_qitems);
+  m.d_qidx = nullptr;
+  m.d_qitems = nullptr;
+  m.queues.clear();
+  for (int *p : m.d_chunk_idx)
+    if (p)
+      cudaFree(p);
+  m.d_chunk_idx.clear();
+  m.chunk_n.clear();
+  m.core_r2.clear();
+  m.row_split = false;
+}
 
 // phase 0 collocate, 1 integrate, 2 integrate with tau
 static Mode &get_mode(TaskList *t, const LDiffs &d, int phase, int nch = 1) {
@@ -1233,6 +1417,7 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase, int nch = 1) {
   auto it = t->modes.find(key);
   if (it != t->modes.end() && it->second.sched_version == t->sched_version)
     return it->second;
+  const HostPhases hp("work queues");
   Mode &m = t->modes[key];
   m.d = d;
   if (m.d_coef_off == nullptr) {
@@ -1253,12 +1438,17 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase, int nch = 1) {
   {
     // shared memory of the coefficient / post kernels (depends on the
     // transform variant, so it is redone whenever the mode is rebuilt)
+    // per (la, lb): the words depend on the task's l only
     int words = 4;
+    bool seen[GB300_LMAX + 8][GB300_LMAX + 8] = {};
     for (int s = 0; s < t->ntasks; s++) {
       const TaskDesc &k = t->tasks[s];
       if (k.flags & TF_SKIP)
         continue;
       const int la = k.la_max + d.la_max, lb = k.lb_max + d.lb_max;
+      if (seen[la][lb])
+        continue;
+      seen[la][lb] = true;
       // collocate: the coefficient kernel (forward); integrate: the post kernel
       words = std::max(words, (int)coef_words(la, lb, uses_staged(t->transform_variant, la, lb,
                                                                   phase == 0)));
@@ -1266,12 +1456,65 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase, int nch = 1) {
     m.coef_words = words;
     m.transform = t->transform_variant;
   }
+  m.qsig = std::make_tuple(mode_key(d), t->precision, dshift, nch);
+  // a mode of the other phase built under the same settings has the same
+  // queues: copy them on the device instead of building them again
+  for (auto &kv : t->modes) {
+    const Mode &o = kv.second;
+    if (&o == &m || o.sched_version != t->sched_version || o.qsig != m.qsig || !o.d_qidx)
+      continue;
+    release_queues(m);
+    m.core_r2 = o.core_r2;
+    m.row_split = o.row_split;
+    m.d_core_r2 = o.row_split ? dalloc_copy(m.core_r2) : nullptr;
+    size_t nidx = 0, nitems = 0;
+    for (const Queue &q : o.queues) {
+      nidx += (size_t)q.n;
+      nitems += q.d_items ? (size_t)q.nitems : 0;
+    }
+    CK(cudaMalloc((void **)&m.d_qidx, sizeof(int) * std::max<size_t>(nidx, 1)));
+    CK(cudaMemcpy(m.d_qidx, o.d_qidx, sizeof(int) * nidx, cudaMemcpyDeviceToDevice));
+    if (nitems) {
+      CK(cudaMalloc((void **)&m.d_qitems, sizeof(int2) * nitems));
+      CK(cudaMemcpy(m.d_qitems, o.d_qitems, sizeof(int2) * nitems, cudaMemcpyDeviceToDevice));
+    }
+    m.queues = o.queues;
+    for (Queue &q : m.queues) {
+      q.d_idx = m.d_qidx + (q.d_idx - o.d_qidx);
+      q.d_items = q.d_items ? m.d_qitems + (q.d_items - o.d_qitems) : nullptr;
+    }
+    m.chunk_n = o.chunk_n;
+    for (size_t c = 0; c < o.d_chunk_idx.size(); c++) {
+      int *p = nullptr;
+      if (o.d_chunk_idx[c]) {
+        CK(cudaMalloc((void **)&p, sizeof(int) * (size_t)o.chunk_n[c]));
+        CK(cudaMemcpy(p, o.d_chunk_idx[c], sizeof(int) * (size_t)o.chunk_n[c],
+                      cudaMemcpyDeviceToDevice));
+      }
+      m.d_chunk_idx.push_back(p);
+    }
+    m.sched_version = t->sched_version;
+    t->gen++;
+    hp.mark("queues copied from the other phase");
+    return m;
+  }
   // row split (mixed mode, orthorhombic double-float tasks): the radius of
   // the double-float core per task, with the class test's derivative factor
   const bool split_rows = t->precision == GRID_GB300_MIXED && t->row_split;
-  m.core_r2.assign(t->ntasks, kCoreAll);
-  std::vector<double> outside(t->ntasks, 0.0);
-  if (split_rows)
+  // the radii depend on the l shifts, the derivative factor and the
+  // threshold only: a collocation and an integration without forces share
+  // them, so they are kept per list
+  const auto core_key = std::make_tuple(d.la_max, d.lb_max, dshift, t->mixed_threshold);
+  auto cached = split_rows ? t->core_cache.find(core_key) : t->core_cache.end();
+  const bool have_core = cached != t->core_cache.end();
+  if (have_core) {
+    m.core_r2 = cached->second.first;
+  } else {
+    m.core_r2.assign(t->ntasks, kCoreAll);
+  }
+  std::vector<double> outside =
+      have_core ? cached->second.second : std::vector<double>(t->ntasks, 0.0);
+  if (split_rows && !have_core)
     parallel_for(t->ntasks, [&](int s) {
       const TaskDesc &k = t->tasks[s];
       // general-path tasks stay whole: their kernels' cost is dominated by
@@ -1288,16 +1531,25 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase, int nch = 1) {
       m.core_r2[s] = core_radius2(k, d.la_max, d.lb_max, t->mixed_threshold / (fac * kShellMargin),
                                   &outside[s]);
     });
+  if (split_rows && !have_core)
+    t->core_cache[core_key] = std::make_pair(m.core_r2, outside);
+  hp.mark("coefficient offsets, row split radii");
   m.row_split = false;
   // work queues: (general, lp bucket, FP32 class, size class), descending
   // cost; the outside rows of split tasks in shell queues keyed from
   // kQueueKeys on
   std::map<int, std::vector<std::pair<double, int>>> items;
   std::vector<char> task_cls(t->ntasks, -1); // FP32 class, -1: skipped
-  for (int s = 0; s < t->ntasks; s++) {
+  std::vector<int> task_key(t->ntasks, -1);
+  std::vector<double> task_cost(t->ntasks, 0.0);
+  // what the queue build reads per task, in compact arrays (the queues visit
+  // the tasks in cost order): lp, cube width or j range, i range, planes
+  std::vector<int> task_lp(t->ntasks, 0), task_ext(t->ntasks, 0), task_iw(t->ntasks, 0),
+      task_nk(t->ntasks, 0);
+  parallel_for(t->ntasks, [&](int s) {
     const TaskDesc &k = t->tasks[s];
     if (k.flags & TF_SKIP)
-      continue;
+      return;
     const int lp = k.la_max + d.la_max + k.lb_max + d.lb_max;
     const int b = bucket_of(lp);
     if (b < 0)
@@ -1322,7 +1574,18 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase, int nch = 1) {
     } else
       cost = (double)t->points[s] * (lp + 1) + 64.0 * (lp + 1) * (lp + 2);
     task_cls[s] = (char)cls;
-    const int key = ((g * kNumBuckets + b) * 2 + cls) * 2 + sz;
+    task_key[s] = ((g * kNumBuckets + b) * 2 + cls) * 2 + sz;
+    task_cost[s] = cost;
+    task_lp[s] = lp;
+    task_ext[s] = ext;
+    task_iw[s] = g ? k.imax[0] - k.center[0] + 1 : 0;
+    task_nk[s] = g ? k.imax[2] - k.center[2] + 1 : 2 - 2 * t->sph[k.sphere].lb[2];
+  });
+  for (int s = 0; s < t->ntasks; s++) {
+    const int key = task_key[s];
+    if (key < 0)
+      continue;
+    const double cost = task_cost[s];
     if (m.core_r2[s] < kCoreAll) {
       const double out = outside[s];
       items[key].push_back({cost * (1.0 - out), s});
@@ -1332,21 +1595,16 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase, int nch = 1) {
       items[key].push_back({cost, s});
     }
   }
-  if (m.d_core_r2)
-    cudaFree(m.d_core_r2);
-  m.d_core_r2 = m.row_split ? dalloc_copy(m.core_r2) : nullptr;
-  for (auto &q : m.queues) {
-    if (q.d_idx)
-      cudaFree(q.d_idx);
-    if (q.d_items)
-      cudaFree(q.d_items);
+  hp.mark("classes and costs");
+  {
+    const bool split_any = m.row_split;
+    std::vector<float> r2;
+    r2.swap(m.core_r2);
+    release_queues(m);
+    m.core_r2.swap(r2);
+    m.row_split = split_any;
   }
-  m.queues.clear();
-  for (int *p : m.d_chunk_idx)
-    if (p)
-      cudaFree(p);
-  m.d_chunk_idx.clear();
-  m.chunk_n.clear();
+  m.d_core_r2 = m.row_split ? dalloc_copy(m.core_r2) : nullptr;
   if (nch > 1) {
     // tasks are in subblock order: chunk c's tasks are those of its subblocks
     for (int c = 0; c < nch; c++) {
@@ -1388,97 +1646,135 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase, int nch = 1) {
       return sx > sy;
     return x < y;
   });
+  hp.mark("chunk lists");
+  // descending cost; ties in task order (the lists are filled in task order,
+  // so this is their stable sort by cost)
   for (auto &kv : items)
-    std::stable_sort(kv.second.begin(), kv.second.end(),
-                     [](const std::pair<double, int> &x, const std::pair<double, int> &y) {
-                       return x.first > y.first;
-                     });
-  for (int qc = 0; qc < (nch > 1 ? nch : 1); qc++)
-  for (int key : keys) {
-    std::vector<std::pair<double, int>> v;
-    if (nch > 1) {
-      for (const auto &e : items[key])
-        if (chunk_of[e.second] == qc)
-          v.push_back(e);
-      if (v.empty())
-        continue;
-    } else {
-      v.swap(items[key]);
-    }
+    parallel_sort(kv.second, [](const std::pair<double, int> &x,
+                                const std::pair<double, int> &y) {
+      return x.first > y.first || (x.first == y.first && x.second < y.second);
+    });
+  hp.mark("queue items sorted");
+  // the queues in launch order, each built on its own thread; their task
+  // indices and work items then go to the device in one piece each
+  struct QueueBuild {
     Queue q;
-    q.chunk = qc;
-    q.key = key;
+    std::vector<std::pair<double, int>> v;
+    std::vector<int> idx;
+    std::vector<int2> items;
+  };
+  std::vector<QueueBuild> qb;
+  for (int qc = 0; qc < (nch > 1 ? nch : 1); qc++)
+    for (int key : keys) {
+      QueueBuild b;
+      if (nch > 1) {
+        for (const auto &e : items[key])
+          if (chunk_of[e.second] == qc)
+            b.v.push_back(e);
+        if (b.v.empty())
+          continue;
+      } else {
+        b.v.swap(items[key]);
+      }
+      b.q.chunk = qc;
+      b.q.key = key;
+      qb.push_back(std::move(b));
+    }
+  parallel_items((int)qb.size(), [&](int n) {
+    QueueBuild &b = qb[n];
+    Queue &q = b.q;
+    const int key = q.key;
+    const std::vector<std::pair<double, int>> &v = b.v;
     q.base = key; // shell queues tune apart from the FP32 class's
     const int kb = key % kQueueKeys;
     q.general = kb / (2 * 2 * kNumBuckets);
     q.bucket = (kb / 4) % kNumBuckets;
     q.fp32 = (kb >> 1) & 1;
-    std::vector<int> idx(v.size());
+    std::vector<int> &idx = b.idx;
+    idx.resize(v.size());
     int ext = 1;
     for (size_t i = 0; i < v.size(); i++) {
-      idx[i] = v[i].second;
-      const TaskDesc &k = t->tasks[idx[i]];
-      const int lpk = k.la_max + d.la_max + k.lb_max + d.lb_max;
-      long long pts = t->points[idx[i]]; // of the task's points in this queue
-      if (m.core_r2[idx[i]] < kCoreAll) { // estimated split, the two parts adding up
+      const int ts = v[i].second;
+      idx[i] = ts;
+      long long pts = t->points[ts]; // of the task's points in this queue
+      if (m.core_r2[ts] < kCoreAll) { // estimated split, the two parts adding up
         q.side = key >= kQueueKeys ? 2 : 1;
-        const long long in = llround((1.0 - outside[idx[i]]) * (double)pts);
+        const long long in = llround((1.0 - outside[ts]) * (double)pts);
         pts = key >= kQueueKeys ? pts - in : in;
       }
       q.points += pts;
-      q.flops += 2.0 * (lpk + 1) * (double)pts;
-      if (q.general == 0)
-        ext = std::max(ext, 2 * t->sph[k.sphere].cmax + 2);
-      else {
-        ext = std::max(ext, k.imax[1] - k.center[1] + 1);
-        q.iwidth = std::max(q.iwidth, k.imax[0] - k.center[0] + 1);
-      }
+      q.flops += 2.0 * (task_lp[ts] + 1) * (double)pts;
+      ext = std::max(ext, task_ext[ts]);
+      if (q.general)
+        q.iwidth = std::max(q.iwidth, task_iw[ts]);
     }
     q.n = (int)idx.size();
     q.extent = ext;
-    q.d_idx = dalloc_copy(idx);
-    {
-      // Large tasks are split by planes into several work items, so that a
-      // few of them do not keep single warps busy while the GPU idles.
-      // General path: boxes of more than kSlicePoints points, in items of at
-      // least kSlicePlanes planes.  Orthorhombic path: tasks of more than
-      // twice the queue's balanced share per resident warp, in items of half
-      // that share (at least kOrthoSliceMin points and two planes).
-      const double share = (double)q.points / kNominalWarps;
-      const long long target =
-          std::max<long long>(kOrthoSliceMin, (long long)(0.5 * share));
-      std::vector<int2> items;
-      bool split = false;
-      for (int s : idx) {
-        const TaskDesc &k = t->tasks[s];
-        int nk, ns;
-        if (q.general) {
-          nk = k.imax[2] - k.center[2] + 1;
-          const long long by_pts = (t->points[s] + kSlicePoints - 1) / kSlicePoints;
-          ns = (int)std::max<long long>(
-              1, std::min<long long>(by_pts, (nk + kSlicePlanes - 1) / kSlicePlanes));
-        } else {
-          nk = 2 - 2 * t->sph[k.sphere].lb[2];
-          ns = 1;
-          if (t->points[s] > 2 * target)
-            ns = (int)std::min<long long>(nk / 2, (t->points[s] + target - 1) / target);
-          ns = std::max(ns, 1);
-        }
-        split |= ns > 1;
-        for (int c = 0; c < ns; c++) {
-          const int k0 = (int)((long long)nk * c / ns), k1 = (int)((long long)nk * (c + 1) / ns);
-          items.push_back(make_int2(s, k0 | ((k1 - k0) << 16)));
-        }
+    // Large tasks are split by planes into several work items, so that a
+    // few of them do not keep single warps busy while the GPU idles.
+    // General path: boxes of more than kSlicePoints points, in items of at
+    // least kSlicePlanes planes.  Orthorhombic path: tasks of more than
+    // twice the queue's balanced share per resident warp, in items of half
+    // that share (at least kOrthoSliceMin points and two planes).
+    const double share = (double)q.points / kNominalWarps;
+    const long long target = std::max<long long>(kOrthoSliceMin, (long long)(0.5 * share));
+    std::vector<int2> &wi = b.items;
+    bool split = false;
+    for (int s : idx) {
+      const int nk = task_nk[s];
+      int ns;
+      if (q.general) {
+        const long long by_pts = (t->points[s] + kSlicePoints - 1) / kSlicePoints;
+        ns = (int)std::max<long long>(
+            1, std::min<long long>(by_pts, (nk + kSlicePlanes - 1) / kSlicePlanes));
+      } else {
+        ns = 1;
+        if (t->points[s] > 2 * target)
+          ns = (int)std::min<long long>(nk / 2, (t->points[s] + target - 1) / target);
+        ns = std::max(ns, 1);
       }
-      if (split) {
-        q.nitems = (int)items.size();
-        q.d_items = dalloc_copy(items);
+      split |= ns > 1;
+      for (int c = 0; c < ns; c++) {
+        const int k0 = (int)((long long)nk * c / ns), k1 = (int)((long long)nk * (c + 1) / ns);
+        wi.push_back(make_int2(s, k0 | ((k1 - k0) << 16)));
       }
     }
-    m.queues.push_back(q);
+    if (split)
+      q.nitems = (int)wi.size();
+    else
+      wi.clear();
+  });
+  {
+    size_t nidx = 0, nitems = 0;
+    for (const QueueBuild &b : qb) {
+      nidx += b.idx.size();
+      nitems += b.items.size();
+    }
+    std::vector<int> all_idx;
+    std::vector<int2> all_items;
+    all_idx.reserve(nidx);
+    all_items.reserve(nitems);
+    for (const QueueBuild &b : qb) {
+      all_idx.insert(all_idx.end(), b.idx.begin(), b.idx.end());
+      all_items.insert(all_items.end(), b.items.begin(), b.items.end());
+    }
+    m.d_qidx = dalloc_copy(all_idx);
+    m.d_qitems = nitems ? dalloc_copy(all_items) : nullptr;
+    size_t oi = 0, ow = 0;
+    for (QueueBuild &b : qb) {
+      b.q.d_idx = m.d_qidx + oi;
+      oi += b.idx.size();
+      b.q.d_items = nullptr;
+      if (b.q.nitems > 0) {
+        b.q.d_items = m.d_qitems + ow;
+        ow += b.items.size();
+      }
+      m.queues.push_back(b.q);
+    }
   }
   m.sched_version = t->sched_version;
   t->gen++;
+  hp.mark("queues sorted, split and uploaded");
   return m;
 }
 

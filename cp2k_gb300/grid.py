@@ -296,9 +296,13 @@ class GridTaskList:
             self.api = "backend"
             self.h = C.c_void_p()
         old_basis = getattr(self, "basis", [])
+        old_inp = getattr(self, "inp", None)
+        if old_basis and old_inp is not None and old_inp.basis_sets is inp.basis_sets:
+            old_basis = []  # the same basis sets: keep their handles
+        else:
+            self.basis = [BasisSet(b) for b in inp.basis_sets]
+            self._bs = (C.c_void_p * max(1, len(self.basis)))(*[b.h.value for b in self.basis])
         self.inp = inp
-        self.basis = [BasisSet(b) for b in inp.basis_sets]
-        self._bs = (C.c_void_p * max(1, len(self.basis)))(*[b.h.value for b in self.basis])
         i32 = lambda a: np.ascontiguousarray(a, np.int32)
         f64 = lambda a: np.ascontiguousarray(a, np.float64)
         levels = [i32(inp.npts_global), i32(inp.npts_local), i32(inp.shift_local),
