@@ -409,7 +409,51 @@ def hartree_step(torch, G, tl, inp, pab, grids, hab, stream, flush, nsteps):
                      "potential_g2rs, integrate; all buffers on the device"}
 
 
-def task_generation(torch, G, inp, host_s, pab=None, flush=None, peaks=None, reps=5):
+def geometry_change(torch, G, inp, gen, V, grids, stream, nsteps=3):
+    """A change of geometry as an MD step makes it, mixed mode: the atoms
+    moved (0.05 bohr rms), the task list generated on the device, re-created
+    through its handle from the device arrays (grid_gb300_taskgen_create_
+    task_list), then the first collocate + integrate (which build the work
+    queues) and a second one.  Returns per-geometry means."""
+    dev = grids[0].device
+    cap = int(inp.buffer_size * 1.05) + 1024
+    pab = torch.zeros(cap, dtype=torch.float64, device=dev)
+    hab = torch.empty(cap, dtype=torch.float64, device=dev)
+    rng = np.random.default_rng(5)
+    pos = inp.atom_positions.copy()
+    tl, rows = None, []
+    for _ in range(nsteps + 1):
+        pos = pos + rng.normal(scale=0.05, size=pos.shape)
+        t0 = time.perf_counter()
+        gen.run(pos)
+        t1 = time.perf_counter()
+        if gen.buffer_size > cap:
+            continue
+        tl = G.GridTaskList.from_generator(gen, precision=G.MIXED, existing=tl)
+        steps = []
+        for _k in range(2):
+            torch.cuda.synchronize()
+            a = time.perf_counter()
+            with torch.cuda.stream(stream):
+                tl.collocate_device(100, pab, grids, stream=stream)
+                tl.integrate_device(V, hab, stream=stream)
+            torch.cuda.synchronize()
+            steps.append((time.perf_counter() - a) * 1e3)
+        rows.append(((t1 - t0) * 1e3, tl.create_s * 1e3, steps[0], steps[1]))
+    if tl is not None:
+        tl.close()
+    del pab, hab
+    rows = np.array(rows[1:] if len(rows) > 1 else rows)  # the first builds the list's streams
+    gen_ms, create_ms, first_ms, step_ms = (float(x) for x in rows.mean(axis=0))
+    return {"geometries": int(len(rows)), "generate_ms": gen_ms, "create_task_list_ms": create_ms,
+            "first_step_ms": first_ms, "step_ms": step_ms,
+            "overhead_ms": gen_ms + create_ms + first_ms - step_ms,
+            "timing": "wall clock; create is the C call alone; the first step builds the "
+                      "work queues on the host"}
+
+
+def task_generation(torch, G, inp, host_s, pab=None, flush=None, peaks=None, reps=5,
+                    geom=None):
     """The workload's task list generated on the device (grid_gb300_taskgen_run:
     the screening, radii, levels and block offsets of CP2K's
     generate_qs_task_list) against the host generator's arrays, the task list
@@ -430,12 +474,15 @@ def task_generation(torch, G, inp, host_s, pab=None, flush=None, peaks=None, rep
     tl2 = G.GridTaskList.from_generator(gen, precision=None, schedule=None)
     create_s = time.perf_counter() - t0
     tl2.close()
+    geo = geometry_change(torch, G, inp, gen, *geom) if geom is not None else None
     gen.free()
     res = {"ntasks": inp.ntasks, "device_ms": float(np.median(ts)),
            "host_generator_s": host_s, "arrays_equal_host_generator": bool(equal),
            "create_task_list_from_device_arrays_s": create_s,
            "timing": "wall clock of the whole call (positions upload, 5 kernels, 2 reads of "
                      "the totals), median of %d" % reps}
+    if geo is not None:
+        res["geometry_change"] = geo
     if pab is None:
         return res
     # a block store: the task list's blocks at shuffled places in one arena
@@ -666,7 +713,8 @@ def gpu_arm(args, world, rank, local):
     hab32 = hab.cpu().numpy()
     hartree = hartree_step(torch, G, tl, inp, pab, grids, hab, stream, flush,
                            max(1, min(args.steps, 5)))
-    taskgen = task_generation(torch, G, inp, host_gen_s, pab, flush, _peaks()[0])
+    taskgen = task_generation(torch, G, inp, host_gen_s, pab, flush, _peaks()[0],
+                              geom=(V, grids, stream))
 
     ms_mixed = max_over_ranks(float(np.mean(t_mixed)), world)
     ms_model = max_over_ranks(float(np.mean(t_model)), world) if t_model else None

@@ -309,9 +309,12 @@ class GridTaskList:
                   i32(inp.border_width), f64(inp.dh), f64(inp.dh_inv)]
         self._arrays = levels
         self.npts_local = levels[1]
+        import time
+        t0 = time.perf_counter()
         lib().grid_gb300_taskgen_create_task_list(gen.h, bool(inp.orthorhombic), inp.nlevels,
                                                   C.cast(self._bs, C.c_void_p),
                                                   *[_p(a) for a in levels], C.byref(self.h))
+        self.create_s = time.perf_counter() - t0  # the C call alone
         self.impl = self.h
         for b in old_basis:
             b.free()
