@@ -760,6 +760,56 @@ __device__ __forceinline__ dfloat df_acc(dfloat acc, dfloat b) {
   return dfloat{s, ((acc.h - (s - bb)) + (b.h - bb)) + (acc.l + b.l)};
 }
 
+// binomial coefficients up to the largest contraction order
+struct BinomD {
+  double v[GB300_LP_MAX + 1][GB300_LP_MAX + 1];
+};
+constexpr BinomD make_binom_d() {
+  BinomD t{};
+  for (int n = 0; n <= GB300_LP_MAX; n++) {
+    t.v[n][0] = 1.0;
+    for (int k = 1; k <= n; k++)
+      t.v[n][k] = t.v[n][k - 1] * (n - k + 1) / k;
+  }
+  return t;
+}
+__constant__ BinomD kBinomD = make_binom_d();
+
+// acc[cidx(kl, jl, il, lp)] holds sum w (i - r_i)^il (j - r_j)^jl (k - r_k)^kl
+// over the task's points; replaced in place by the same sums about the
+// centre c (c - r within half a grid step, so the binomial sums carry no
+// cancellation).  One warp, lanes over the lines of each axis.
+__device__ void shift_moments(double *acc, int lp, const double *c, const int *r, int lane) {
+  for (int ax = 0; ax < 3; ax++) { // 0: i, 1: j, 2: k
+    const double s = (double)r[ax] - c[ax]; // (x - c) = (x - r) + (r - c)
+    double sp[GB300_LP_MAX + 1];
+    sp[0] = 1.0;
+    for (int n = 1; n <= lp; n++)
+      sp[n] = sp[n - 1] * s;
+    const int nlines = ntri(lp);
+    for (int q = lane; q < nlines; q += 32) {
+      // the line's two fixed exponents (u, v), u + v <= lp
+      int u = 0, rem = q;
+      while (rem > lp - u) {
+        rem -= lp - u + 1;
+        u++;
+      }
+      const int v = rem, L = lp - u - v;
+      auto at = [&](int m) -> double & {
+        return ax == 0 ? acc[cidx(u, v, m, lp)]
+                       : (ax == 1 ? acc[cidx(u, m, v, lp)] : acc[cidx(m, u, v, lp)]);
+      };
+      for (int n = L; n >= 0; n--) {
+        double sum = 0.0;
+        for (int m = 0; m <= n; m++)
+          sum = fma(kBinomD.v[n][m] * sp[n - m], at(m), sum);
+        at(n) = sum;
+      }
+    }
+    __syncwarp();
+  }
+}
+
 template <int LPB>
 __global__ void __launch_bounds__(128) integrate_general_df(GridArgs a, int njmax) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -812,7 +862,14 @@ __global__ void __launch_bounds__(128) integrate_general_df(GridArgs a, int njma
     const int G = 32 / SW, sub = lane % SW, grp = lane / SW;
     const double zetp = d.zetp, inv_hh1 = 1.0 / g.hh[1];
     const double fj0 = (double)g.imin[1] - g.gp[1];
-    const dfloat A = df_make(zetp * g.hh[1]), dj0 = df_make(fj0);
+    const dfloat A = df_make(zetp * g.hh[1]);
+    // the moments are taken about the grid point nearest the Gaussian's
+    // centre, so that every power is of an exact small integer offset, and
+    // shifted to the centre at the end
+    int cref[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+      cref[c] = (int)rint(g.gp[c]);
 
     for (int xc = g.imin[0]; xc <= g.imax[0]; xc += SW) {
       const int i = xc + sub;
@@ -848,17 +905,17 @@ __global__ void __launch_bounds__(128) integrate_general_df(GridArgs a, int njma
           const float rf = (float)(j - g.imin[1]);
           const float2 gv = __ldg(gplane + (size_t)jg * nx + ig);
           dfloat pj = df_mul(dfloat{gv.x, gv.y}, df_gauss(line, A, rf, tab));
-          const dfloat dj = df_add1(dj0, rf);
+          const float dj = (float)(j - cref[1]);
 #pragma unroll
           for (int jl = 0; jl < P; jl++) {
             if (jl <= lp)
               wj[jl] = df_acc(wj[jl], pj);
             if (jl < P - 1)
-              pj = df_mul(pj, dj);
+              pj = df_mul1(pj, dj);
           }
         }
         __syncwarp();
-        const dfloat dkd = df_make(dk);
+        const float dkd = (float)(k - cref[2]);
         dfloat pk{1.f, 0.f};
 #pragma unroll
         for (int kl = 0; kl < P; kl++) {
@@ -870,7 +927,7 @@ __global__ void __launch_bounds__(128) integrate_general_df(GridArgs a, int njma
               dfloat &x = akj[kl * P - (kl * (kl - 1)) / 2 + jl];
               x = df_fma_acc(x, df_norm(wj[jl]), pk);
             }
-          pk = df_mul(pk, dkd);
+          pk = df_norm(df_mul1(pk, dkd));
         }
       }
       // fold i and reduce over the warp through shared memory, KC rows of
@@ -878,12 +935,12 @@ __global__ void __launch_bounds__(128) integrate_general_df(GridArgs a, int njma
       {
         constexpr int KC = S::KC, RS = S::red_stride();
         dfloat *rl = red + lane * RS;
-        const dfloat dd = df_make(di);
+        const float dd = (float)(i - cref[0]);
         dfloat pi = xin ? dfloat{1.f, 0.f} : dfloat{0.f, 0.f};
 #pragma unroll
         for (int l = 0; l < P; l++) {
           rl[KC + l] = pi;
-          pi = df_mul(pi, dd);
+          pi = df_norm(df_mul1(pi, dd));
         }
 #pragma unroll
         for (int c0 = 0; c0 < NKJ; c0 += KC) {
@@ -909,6 +966,9 @@ __global__ void __launch_bounds__(128) integrate_general_df(GridArgs a, int njma
       }
     }
     __syncwarp();
+    // moments about the reference point -> moments about the centre:
+    // (x - c)^n = sum_m C(n, m) (x - r)^m (r - c)^(n - m), axis by axis
+    shift_moments(acc, lp, g.gp, cref, lane);
     double *dst = out + a.coef_off[t];
     for (int e = lane; e < nco; e += 32) {
       if (a.items || a.accum) // parts of one task add up (the buffer is zeroed)

@@ -85,6 +85,16 @@ __device__ __forceinline__ dfloat df_mul(dfloat a, dfloat b) {
   return df_fma(dfloat{0.f, 0.f}, a, b);
 }
 
+// a*b with b a plain float that is exactly representable (a small integer):
+// the exact leading product and its error term, not renormalised (|l| stays
+// within a few ulps of h), for power chains
+__device__ __forceinline__ dfloat df_mul1(dfloat a, float b) {
+  const float p = a.h * b;
+  float e = fmaf(a.h, b, -p);
+  e = fmaf(a.l, b, e);
+  return dfloat{p, e};
+}
+
 __device__ __forceinline__ dfloat df_add(dfloat a, dfloat b) {
   const float s = a.h + b.h;
   const float bb = s - a.h;
