@@ -166,7 +166,7 @@ struct Grp {
 };
 
 // Group layout of a CTA: gsize 16 (two tasks per warp), 32 (one per warp) or
-// blockDim.x (one large task per CTA).
+// blockDim.x (one large task per CTA, 256 threads).
 struct GrpLayout {
   Grp g;
   int gid, ngroups, slot; // first task, stride, shared-memory slot in the CTA
@@ -714,7 +714,7 @@ __device__ void coef_task(const CoefArgs &a, int t, const TaskDesc &d, double *w
 // U: working type of the tasks (the mixed mode launches one kernel per work
 // queue, each in the type of its class)
 template <typename U, typename Tout>
-__global__ void __launch_bounds__(128) coefficients_kernel(CoefArgs a, int words_per_group,
+__global__ void __launch_bounds__(256) coefficients_kernel(CoefArgs a, int words_per_group,
                                                            int gsize) {
   extern __shared__ __align__(16) unsigned char smem[];
   const GrpLayout gl = grp_layout(gsize);
@@ -946,7 +946,7 @@ __device__ void post_task(const PostArgs &a, int t, const TaskDesc &d, double *w
 }
 
 template <typename U>
-__global__ void __launch_bounds__(128) post_kernel(PostArgs a, int words_per_group, int gsize) {
+__global__ void __launch_bounds__(256) post_kernel(PostArgs a, int words_per_group, int gsize) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ double vir_cta[9];
   const int lane = threadIdx.x & 31;
@@ -1337,7 +1337,7 @@ struct GroupLaunch {
 static GroupLaunch group_launch(int words_per_group, int ntasks) {
   GroupLaunch L{};
   if (words_per_group > kLargeTaskWords) {
-    L.gsize = L.threads = 128;
+    L.gsize = L.threads = 256;
     L.smem = (size_t)words_per_group * 8;
     L.grid = std::max(1, std::min(ntasks, 152 * 32));
     return L;
