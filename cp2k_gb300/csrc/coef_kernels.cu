@@ -166,7 +166,7 @@ struct Grp {
 };
 
 // Group layout of a CTA: gsize 16 (two tasks per warp), 32 (one per warp) or
-// blockDim.x (one large task per CTA, 256 threads).
+// blockDim.x (one large task per CTA, 128 or 256 threads).
 struct GrpLayout {
   Grp g;
   int gid, ngroups, slot; // first task, stride, shared-memory slot in the CTA
@@ -1334,10 +1334,13 @@ struct GroupLaunch {
   int gsize, threads, grid;
   size_t smem;
 };
-static GroupLaunch group_launch(int words_per_group, int ntasks) {
+// large_threads: the CTA of a large task; 256 where the kernel's registers
+// still let that many warps reside (more warps for an issue-bound kernel),
+// else 128
+static GroupLaunch group_launch(int words_per_group, int ntasks, int large_threads = 256) {
   GroupLaunch L{};
   if (words_per_group > kLargeTaskWords) {
-    L.gsize = L.threads = 256;
+    L.gsize = L.threads = large_threads;
     L.smem = (size_t)words_per_group * 8;
     L.grid = std::max(1, std::min(ntasks, 152 * 32));
     return L;
@@ -1388,7 +1391,11 @@ void launch_coefficients(const CoefArgs &a, int arith, int words_per_warp, cudaS
 
 template <typename U>
 static void launch_post_t(const PostArgs &a, int words_per_group, cudaStream_t s) {
-  const GroupLaunch L = group_launch(words_per_group, a.order ? a.norder : a.ntasks);
+  // the FP32 and FP64 post kernels take 120-128 registers: 256-thread CTAs
+  // would not add resident warps (measured slower); the double-float one
+  // takes 80
+  const GroupLaunch L = group_launch(words_per_group, a.order ? a.norder : a.ntasks,
+                                     std::is_same<U, dfloat>::value ? 256 : 128);
   if (L.grid < 1 || L.smem > kSmemBudget)
     return launch_error("post-processing: angular momenta too large for shared memory");
   auto k = post_kernel<U>;
