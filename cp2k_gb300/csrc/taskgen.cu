@@ -10,6 +10,10 @@
 //     pair);
 //   * every primitive pair (iset, ipgf, jset, jpgf), in that order, whose
 //     Gaussian-product prefactor exp(-zeta zetb / zetp |rab|^2) exceeds eps;
+//     or, after grid_gb300_taskgen_set_radius_screen, Quickstep's own
+//     screening by the basis radii (set radius + kind radius, set + set,
+//     primitive + set, primitive + primitive against |rab|,
+//     task_list_methods.F:673-696), in its order iset, jset, ipgf, jpgf;
 //   * the grid level of gaussian_gridlevel (src/pw_env/gaussian_gridlevels.F:
 //     147-167): the coarsest level whose cutoff covers zetp * rel_cutoff;
 //   * the radius of exp_radius_very_extended (src/aobasis/ao_util.F:207-290)
@@ -89,6 +93,11 @@ struct TgParams {
   float cellf[3][3], cellnorm[3], rmaxf, leps;
   float cinvf[3][3], hf[3];  // inverse cell; column norms (reciprocal lengths)
   const float *zetf;   // [nsets][maxpgf]
+  // basis-radius screening (Quickstep's task_list_inner_loop), when set
+  int screen;
+  const double *rpgf;        // [nsets][maxpgf]
+  const double *set_radius;  // [nsets]
+  const double *kind_radius; // [nkinds]
   const double *pos;   // [natoms][3]
   const int *kind;     // [natoms], 0-based
   const int *set_off;  // [nkinds]
@@ -172,9 +181,42 @@ __device__ __forceinline__ bool passes(const TgParams &P, double za, double zb, 
   return pref > P.eps;
 }
 
+// Quickstep's screening of one atom pair (task_list_methods.F:673-696):
+// sets and primitives whose radii reach |rab|, in the loop order iset, jset,
+// ipgf, jpgf; f(iset, jset, ipgf, jpgf) for each pair that is kept
+template <class F>
+__device__ __forceinline__ void radius_screen(const TgParams &P, int ki, int kj, double rab2,
+                                              F &&f) {
+  const double dab = __dsqrt_rn(rab2);
+  const double krb = P.kind_radius[kj];
+  const int si0 = P.set_off[ki], sj0 = P.set_off[kj];
+  for (int is = 0; is < P.nset[ki]; is++) {
+    const double sra = P.set_radius[si0 + is];
+    if (dadd(sra, krb) < dab)
+      continue;
+    for (int js = 0; js < P.nset[kj]; js++) {
+      const double srb = P.set_radius[sj0 + js];
+      if (dadd(sra, srb) < dab)
+        continue;
+      for (int ip = 0; ip < P.npgf[si0 + is]; ip++) {
+        const double rpa = P.rpgf[(size_t)(si0 + is) * P.maxpgf + ip];
+        if (dadd(rpa, srb) < dab)
+          continue;
+        for (int jp = 0; jp < P.npgf[sj0 + js]; jp++)
+          if (!(dadd(rpa, P.rpgf[(size_t)(sj0 + js) * P.maxpgf + jp]) < dab))
+            f(is, js, ip, jp);
+      }
+    }
+  }
+}
+
 // tasks of one image of the pair (ki, kj): primitive pairs that pass
 __device__ int image_tasks(const TgParams &P, int ki, int kj, double rab2) {
   int c = 0;
+  if (P.screen) {
+    radius_screen(P, ki, kj, rab2, [&](int, int, int, int) { c++; });
+    return c;
+  }
   const float rab2f = __double2float_rn(rab2);
   const int si0 = P.set_off[ki], sj0 = P.set_off[kj];
   for (int is = 0; is < P.nset[ki]; is++)
@@ -431,6 +473,28 @@ __global__ void __launch_bounds__(256)
     long long t = task0[b];
     const int si0 = P.set_off[ki], sj0 = P.set_off[kj];
     for_images(P, i, j, q, [&](const double *rab, double rab2) {
+      auto write = [&](int is, int js, int ip, int jp, double za, double zb) {
+        o.level[t] = grid_level(P, dadd(za, zb));
+        o.iatom[t] = i + 1;
+        o.jatom[t] = j + 1;
+        o.iset[t] = is + 1;
+        o.jset[t] = js + 1;
+        o.ipgf[t] = ip + 1;
+        o.jpgf[t] = jp + 1;
+        o.border_mask[t] = 0;
+        o.block_num[t] = (int)b + 1;
+        o.rab[3 * t] = rab[0];
+        o.rab[3 * t + 1] = rab[1];
+        o.rab[3 * t + 2] = rab[2];
+        t++;
+      };
+      if (P.screen) {
+        radius_screen(P, ki, kj, rab2, [&](int is, int js, int ip, int jp) {
+          write(is, js, ip, jp, P.zet[(size_t)(si0 + is) * P.maxpgf + ip],
+                P.zet[(size_t)(sj0 + js) * P.maxpgf + jp]);
+        });
+        return;
+      }
       const float rab2f = __double2float_rn(rab2);
       for (int is = 0; is < P.nset[ki]; is++)
         for (int ip = 0; ip < P.npgf[si0 + is]; ip++) {
@@ -443,19 +507,7 @@ __global__ void __launch_bounds__(256)
               const double zb = P.zet[ib];
               if (!passes(P, za, zb, zaf, P.zetf[ib], rab2, rab2f))
                 continue;
-              o.level[t] = grid_level(P, dadd(za, zb));
-              o.iatom[t] = i + 1;
-              o.jatom[t] = j + 1;
-              o.iset[t] = is + 1;
-              o.jset[t] = js + 1;
-              o.ipgf[t] = ip + 1;
-              o.jpgf[t] = jp + 1;
-              o.border_mask[t] = 0;
-              o.block_num[t] = (int)b + 1;
-              o.rab[3 * t] = rab[0];
-              o.rab[3 * t + 1] = rab[1];
-              o.rab[3 * t + 2] = rab[2];
-              t++;
+              write(is, js, ip, jp, za, zb);
             }
         }
     });
@@ -718,6 +770,8 @@ struct TaskGenerator {
   int *d_lmax = nullptr, *d_npgf = nullptr;
   double *d_zet = nullptr, *d_pos = nullptr;
   float *d_zetf = nullptr;
+  double *d_rpgf = nullptr, *d_set_radius = nullptr, *d_kind_radius = nullptr;
+  int nsets = 0;
   // work
   int *d_cnt = nullptr;
   size_t cap_cnt = 0;
@@ -815,6 +869,7 @@ GB300_API void grid_gb300_taskgen_create(
   }
   auto *g = new TaskGenerator();
   g->nkinds = nkinds;
+  g->nsets = nsets;
   g->h_kind1.assign(atom_kinds, atom_kinds + natoms);
   TgParams &P = g->P;
   P.natoms = natoms;
@@ -894,13 +949,41 @@ GB300_API void grid_gb300_taskgen_create(
   *generator = g;
 }
 
+GB300_API void grid_gb300_taskgen_set_radius_screen(grid_gb300_task_generator *generator,
+                                                   const double *pgf_radius,
+                                                   const double *set_radius,
+                                                   const double *kind_radius) {
+  using namespace gb300;
+  auto *g = (TaskGenerator *)generator;
+  if (!g || !pgf_radius || !set_radius || !kind_radius)
+    tg_fail("null generator or radii", 0);
+  const size_t npr = (size_t)g->nsets * g->P.maxpgf;
+  for (size_t q = 0; q < npr; q++)
+    if (!(pgf_radius[q] >= 0.0))
+      tg_fail("negative or invalid primitive radius", (int)q);
+  auto up = [](double *&dst, const double *src, size_t n) {
+    if (!dst)
+      CKT(cudaMalloc((void **)&dst, std::max<size_t>(n, 1) * sizeof(double)));
+    if (n)
+      CKT(cudaMemcpy(dst, src, n * sizeof(double), cudaMemcpyHostToDevice));
+  };
+  up(g->d_rpgf, pgf_radius, npr);
+  up(g->d_set_radius, set_radius, (size_t)g->nsets);
+  up(g->d_kind_radius, kind_radius, (size_t)g->nkinds);
+  g->P.rpgf = g->d_rpgf;
+  g->P.set_radius = g->d_set_radius;
+  g->P.kind_radius = g->d_kind_radius;
+  g->P.screen = 1;
+}
+
 GB300_API void grid_gb300_taskgen_free(grid_gb300_task_generator *generator) {
   using namespace gb300;
   auto *g = (TaskGenerator *)generator;
   if (!g)
     return;
   void *d[] = {g->d_kind, g->d_set_off, g->d_nset, g->d_nsgf, g->d_lmax, g->d_npgf,
-               g->d_zet, g->d_zetf, g->d_pos, g->d_cnt, g->d_partial, g->d_pair_i, g->d_pair_j,
+               g->d_zet, g->d_zetf, g->d_rpgf, g->d_set_radius, g->d_kind_radius, g->d_pos,
+               g->d_cnt, g->d_partial, g->d_pair_i, g->d_pair_j,
                g->d_size, g->d_task0, g->d_radius, g->d_rab, g->d_block_offsets};
   for (void *p : d)
     if (p)

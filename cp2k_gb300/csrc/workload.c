@@ -42,6 +42,13 @@ typedef struct {
   double zet_min, zet_max;
   int random_sphi; /* 0: identity contraction, 1: random orthonormal rows */
   int npgf[WL_MAX_ELEM]; /* primitives per set */
+  /* 0: primitive pairs screened by prefactor > eps (the benchmark
+   * workloads); 1: by the basis radii as Quickstep does
+   * (task_list_methods.F:673-696), in its loop order iset, jset, ipgf,
+   * jpgf, with the radii of qs_interactions.F:472-492 (every shell
+   * coefficient 1, threshold eps_pgf_orb) */
+  int screen;
+  double eps_pgf_orb;
 } wl_params;
 
 typedef struct {
@@ -64,6 +71,8 @@ typedef struct {
   double dh[WL_MAX_LEVELS][3][3], dh_inv[WL_MAX_LEVELS][3][3];
   int nimg[3];  /* periodic images searched per cell vector: -nimg..nimg */
   double rmax;  /* pair distance cut (bohr) */
+  /* basis radii (screen 1): [sum nset][maxpgf_all], [sum nset], [nkinds] */
+  double *rpgf, *set_radius, *kind_radius;
 } wl_out;
 
 /* --------------------------------------------------------------- random -- */
@@ -232,9 +241,16 @@ static void build_tasks(wl_out *o, const wl_params *p) {
                  o->ipgf, o->jpgf, o->border_mask, o->block_num, o->radius, o->rab};
   for (size_t q = 0; q < sizeof(old) / sizeof(old[0]); q++)
     free(old[q]);
-  /* image range from the most diffuse possible product */
+  /* image range from the most diffuse possible product (screen 0), or
+   * from the largest sum of two kind radii (screen 1) */
   const double ln_eps = log(1.0 / p->eps);
-  const double rmax = sqrt(ln_eps / (0.5 * p->zet_min));
+  double rmax = sqrt(ln_eps / (0.5 * p->zet_min));
+  if (p->screen == 1) {
+    double kr = 0.0;
+    for (int k = 0; k < o->nkinds; k++)
+      kr = fmax(kr, o->kind_radius[k]);
+    rmax = 2.0 * kr;
+  }
   double cinv[3][3];
   inv3(p->cell, cinv);
   int nimg[3];
@@ -274,6 +290,54 @@ static void build_tasks(wl_out *o, const wl_params *p) {
             const double rab2 = rab[0] * rab[0] + rab[1] * rab[1] + rab[2] * rab[2];
             if (rab2 > rmax * rmax)
               continue;
+            if (p->screen == 1) {
+              /* task_list_inner_loop (task_list_methods.F:673-696) */
+              const double dab = sqrt(rab2);
+              const double krb = o->kind_radius[j];
+              for (int is = 0; is < o->nset[i]; is++) {
+                const int gi = o->set_off[i] + is;
+                if (o->set_radius[gi] + krb < dab)
+                  continue;
+                for (int js = 0; js < o->nset[j]; js++) {
+                  const int gj = o->set_off[j] + js;
+                  if (o->set_radius[gi] + o->set_radius[gj] < dab)
+                    continue;
+                  for (int ip = 0; ip < o->npgf[gi]; ip++) {
+                    const double rpa = o->rpgf[(size_t)gi * maxpgf_all + ip];
+                    if (rpa + o->set_radius[gj] < dab)
+                      continue;
+                    const double za = o->zet[(size_t)gi * maxpgf_all + ip];
+                    for (int jp = 0; jp < o->npgf[gj]; jp++) {
+                      if (rpa + o->rpgf[(size_t)gj * maxpgf_all + jp] < dab)
+                        continue;
+                      const double zb = o->zet[(size_t)gj * maxpgf_all + jp];
+                      const double zetp = za + zb, f = zb / zetp;
+                      const double pref = exp(-za * f * rab2);
+                      double rp[3], rb[3];
+                      for (int d = 0; d < 3; d++) {
+                        rp[d] = ra[d] + f * rab[d];
+                        rb[d] = ra[d] + rab[d];
+                      }
+                      const double radius = exp_radius_very_extended(
+                          o->lmax[gi], o->lmax[gj], ra, rb, rp, zetp, p->eps, pref);
+                      if (!block) {
+                        block = ++nblocks;
+                        const int off = (int)offset;
+                        vpush(&vblk, &off);
+                        offset += (long long)o->nsgf[i] * o->nsgf[j];
+                      }
+                      const int v[9] = {grid_level(p, zetp), i + 1, j + 1, is + 1, js + 1,
+                                        ip + 1, jp + 1, 0, block};
+                      for (int q = 0; q < 9; q++)
+                        vpush(&vi[q], &v[q]);
+                      vpush(&vr, &radius);
+                      vpush(&vrab, rab);
+                    }
+                  }
+                }
+              }
+              continue;
+            }
             for (int is = 0; is < o->nset[i]; is++)
             for (int ip = 0; ip < o->npgf[o->set_off[i] + is]; ip++) {
               const int gi = o->set_off[i] + is;
@@ -425,6 +489,33 @@ wl_out *wl_generate(const wl_params *p) {
       }
     }
   }
+  /* basis radii (qs_interactions.F:472-492): per primitive the largest
+   * exp_radius over the set's shells l = 0..lmax, coefficient 1, threshold
+   * eps_pgf_orb, absolute accuracy 1e-12 (exp_radius without epsabs) */
+  o->rpgf = calloc((size_t)totsets * maxpgf_all, sizeof(double));
+  o->set_radius = calloc((size_t)totsets, sizeof(double));
+  o->kind_radius = calloc((size_t)na, sizeof(double));
+  {
+    const double epo = p->eps_pgf_orb > 0.0 ? p->eps_pgf_orb : 1.0e-5;
+    for (int i = 0; i < na; i++) {
+      double kr = 0.0;
+      for (int k = 0; k < o->nset[i]; k++) {
+        const int gs = o->set_off[i] + k;
+        double sr = 0.0;
+        for (int q = 0; q < o->npgf[gs]; q++) {
+          const double z = o->zet[(size_t)gs * maxpgf_all + q];
+          double r = 0.0;
+          for (int l = o->lmin[gs]; l <= o->lmax[gs]; l++)
+            r = fmax(r, exp_radius(l, z, epo, 1.0, 1.0e-12, r));
+          o->rpgf[(size_t)gs * maxpgf_all + q] = r;
+          sr = fmax(sr, r);
+        }
+        o->set_radius[gs] = sr;
+        kr = fmax(kr, sr);
+      }
+      o->kind_radius[i] = kr;
+    }
+  }
   /* grid levels */
   for (int l = 0; l < p->nlevels; l++) {
     for (int a = 0; a < 3; a++)
@@ -454,7 +545,8 @@ void wl_free(wl_out *o) {
                   o->maxpgf, o->set_off, o->lmin, o->lmax, o->npgf, o->nsgf_set,
                   o->first_sgf, o->sphi_off, o->sphi, o->zet, o->block_offsets,
                   o->level, o->iatom, o->jatom, o->iset, o->jset, o->ipgf, o->jpgf,
-                  o->border_mask, o->block_num, o->radius, o->rab};
+                  o->border_mask, o->block_num, o->radius, o->rab, o->rpgf, o->set_radius,
+                  o->kind_radius};
   for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++)
     free(ptrs[i]);
   free(o);

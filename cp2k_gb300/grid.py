@@ -621,6 +621,7 @@ def _bind_taskgen(L):
                                             + [C.c_double, C.c_double, C.c_int, vp, C.c_double,
                                                C.POINTER(vp)])
     L.grid_gb300_taskgen_free.argtypes = [vp]
+    L.grid_gb300_taskgen_set_radius_screen.argtypes = [vp, vp, vp, vp]
     L.grid_gb300_taskgen_run.argtypes = [vp, vp, C.c_int, vp, vp, vp, vp]
     L.grid_gb300_taskgen_arrays.argtypes = [vp] + [vp] * 12
     L.grid_gb300_taskgen_copy.argtypes = [vp] + [vp] * 12
@@ -671,6 +672,14 @@ class TaskGenerator:
                                     _p(nimg), float(m["rmax"]), float(m["eps"]),
                                     len(cut), _p(cut), float(m["rel_cutoff"]),
                                     C.byref(self.h))
+        if m.get("screen") == "radius":  # Quickstep's screening by basis radii
+            rp = np.zeros((int(nset.sum()), self.maxpgf))
+            src = np.asarray(m["rpgf"], np.float64)
+            rp[:, :src.shape[1]] = src
+            sr = np.ascontiguousarray(m["set_radius"], np.float64)
+            kr = np.ascontiguousarray(m["kind_radius"], np.float64)
+            self._keep += [rp, sr, kr]
+            L.grid_gb300_taskgen_set_radius_screen(self.h, _p(rp), _p(sr), _p(kr))
         self.ntasks = self.nblocks = self.buffer_size = 0
         self.positions = None
 

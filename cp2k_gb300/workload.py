@@ -29,6 +29,7 @@ class _Params(C.Structure):
         ("elem_fraction", C.c_double * _MAXE), ("nsets", C.c_int * _MAXE),
         ("set_lmax", C.c_int * (_MAXE * _MAXS)), ("zet_min", C.c_double),
         ("zet_max", C.c_double), ("random_sphi", C.c_int), ("npgf", C.c_int * _MAXE),
+        ("screen", C.c_int), ("eps_pgf_orb", C.c_double),
     ]
 
 
@@ -50,6 +51,7 @@ class _Out(C.Structure):
         ("radius", _dp), ("rab", _dp),
         ("dh", C.c_double * (_MAXL * 9)), ("dh_inv", C.c_double * (_MAXL * 9)),
         ("nimg", C.c_int * 3), ("rmax", C.c_double),
+        ("rpgf", _dp), ("set_radius", _dp), ("kind_radius", _dp),
     ]
 
 
@@ -128,11 +130,16 @@ def make_cell(spec) -> np.ndarray:
 
 def generate(natoms: int, cell: np.ndarray, npts, elements, zet, seed: int = 1,
              rel_cutoff: float = 40.0, eps: float = 1e-10, random_sphi: bool = False,
-             cutoffs=None, positions=None) -> TaskListInputs:
+             cutoffs=None, positions=None, screen: str = "prefactor",
+             eps_pgf_orb: float = 1e-5) -> TaskListInputs:
     """Build a task list.  ``npts`` is a list of per-level point counts (int or
     3-tuple), finest first; ``elements`` a list of (fraction, [set lmax...]).
     ``positions`` ([natoms][3], bohr) replaces the seeded atom positions
-    (same basis sets): the task list of a moved geometry."""
+    (same basis sets): the task list of a moved geometry.  ``screen``:
+    "prefactor" keeps primitive pairs whose Gaussian-product prefactor
+    exceeds eps (the benchmark workloads); "radius" screens by the basis
+    radii as Quickstep's task_list_inner_loop does (radii from exp_radius
+    at threshold ``eps_pgf_orb``)."""
     npts = [(n, n, n) if np.isscalar(n) else tuple(n) for n in npts]
     cell = np.asarray(cell, np.float64)
     p = _Params()
@@ -158,6 +165,10 @@ def generate(natoms: int, cell: np.ndarray, npts, elements, zet, seed: int = 1,
             p.set_lmax[e * _MAXS + k] = L
     p.zet_min, p.zet_max = zet
     p.random_sphi = int(random_sphi)
+    if screen not in ("prefactor", "radius"):
+        raise ValueError("screen must be 'prefactor' or 'radius'")
+    p.screen = 1 if screen == "radius" else 0
+    p.eps_pgf_orb = eps_pgf_orb
     L = _lib()
     op = L.wl_generate(C.byref(p))
     if not op:
@@ -168,9 +179,15 @@ def generate(natoms: int, cell: np.ndarray, npts, elements, zet, seed: int = 1,
             if L.wl_retask(op, C.byref(p), pos.ctypes.data_as(C.c_void_p)) != 0:
                 raise ValueError("positions do not match the workload")
         o = op.contents
+        nsets = int(np.ctypeslib.as_array(o.nset, shape=(o.natoms,)).sum())
+        radii = dict(rpgf=_arr(o.rpgf, nsets * o.maxpgf_all, np.float64).reshape(nsets, -1),
+                     set_radius=_arr(o.set_radius, nsets, np.float64),
+                     kind_radius=_arr(o.kind_radius, o.nkinds, np.float64))
         return _to_inputs(o, cell, npts, cut, dict(natoms=natoms, seed=seed, zet=zet,
                                                    elements=elements, rel_cutoff=rel_cutoff,
-                                                   eps=eps, nimg=list(o.nimg), rmax=o.rmax))
+                                                   eps=eps, nimg=list(o.nimg), rmax=o.rmax,
+                                                   screen=screen, eps_pgf_orb=eps_pgf_orb,
+                                                   **radii))
     finally:
         L.wl_free(op)
 
@@ -233,7 +250,7 @@ def _to_inputs(o, cell, npts, cutoffs, meta) -> TaskListInputs:
 
 
 def config(name: str, seed: int = 1, scale: float = 1.0, random_sphi: bool = False,
-           positions=None, **overrides) -> TaskListInputs:
+           positions=None, screen: str = "prefactor", **overrides) -> TaskListInputs:
     """A named benchmark configuration.  ``scale`` < 1 shrinks the atom count,
     the cell edge (at fixed density) and the grid point counts (at fixed
     spacing) for quick parity runs.  ``positions`` moves the atoms (see
@@ -246,7 +263,8 @@ def config(name: str, seed: int = 1, scale: float = 1.0, random_sphi: bool = Fal
     npts = [max(8, int(round(n * lin))) for n in c["npts"]]
     cutoffs = _cutoffs(cell, [(n, n, n) for n in c["npts"]])
     return generate(natoms, cell * lin, npts, c["elements"], c["zet"], seed=seed,
-                    random_sphi=random_sphi, cutoffs=cutoffs, positions=positions)
+                    random_sphi=random_sphi, cutoffs=cutoffs, positions=positions,
+                    screen=screen)
 
 
 def density_blocks(inp: TaskListInputs, seed: int = 2) -> np.ndarray:

@@ -620,6 +620,16 @@ void grid_gb300_taskgen_create(
     const double eps, const int nlevels, const double *cutoff, const double rel_cutoff,
     grid_gb300_task_generator **generator);
 void grid_gb300_taskgen_free(grid_gb300_task_generator *generator);
+/* Screen primitive pairs by the basis radii as Quickstep does
+ * (task_list_methods.F:673-696: set_radius(a) + kind_radius(b),
+ * set_radius(a) + set_radius(b), pgf_radius(a) + set_radius(b),
+ * pgf_radius(a) + pgf_radius(b) against |rab|, loop order iset, jset, ipgf,
+ * jpgf) instead of by the prefactor: pgf_radius [sum nset][maxpgf],
+ * set_radius [sum nset], kind_radius [nkinds], the basis set's radii
+ * (qs_interactions.F:472-492). */
+void grid_gb300_taskgen_set_radius_screen(grid_gb300_task_generator *generator,
+                                          const double *pgf_radius, const double *set_radius,
+                                          const double *kind_radius);
 /* Generates the task list for atom_positions ([natoms][3], bohr; a device
  * pointer when on_device != 0, else host); returns the task and block counts
  * and the pab buffer length (doubles).  Synchronises the stream. */

@@ -25,6 +25,24 @@ def _same_lists(host, arrays, nblocks, buffer_size):
         assert bad.size == 0, (k, bad[:5], a[bad[:5]], arrays[k][bad[:5]])
 
 
+def test_host_radius_screen_rules():
+    """CPU: the host generator's radius screening keeps exactly the
+    primitive pairs whose radii reach |rab| (Quickstep's four tests), and
+    its radii are exp_radius maxima over the set's shells."""
+    inp = W.config("c1_64atoms", scale=0.4, seed=3, screen="radius")
+    m = inp.meta
+    rp, sr, kr = m["rpgf"], m["set_radius"], m["kind_radius"]
+    off = np.concatenate([[0], np.cumsum([b.nset for b in inp.basis_sets])])
+    assert np.allclose(sr, rp.max(axis=1)) and np.all(sr > 0)
+    for k in range(len(kr)):
+        assert kr[k] == sr[off[k]:off[k + 1]].max()
+    dab = np.linalg.norm(inp.rab_list, axis=1)
+    gi = off[inp.atom_kinds[inp.iatom_list - 1] - 1] + inp.iset_list - 1
+    gj = off[inp.atom_kinds[inp.jatom_list - 1] - 1] + inp.jset_list - 1
+    assert np.all(rp[gi, inp.ipgf_list - 1] + rp[gj, inp.jpgf_list - 1] >= dab)
+    assert np.all(sr[gi] + sr[gj] >= dab)
+
+
 def test_host_retask_reproduces_and_moves():
     """CPU: re-tasking the host generator at its own positions gives the same
     arrays; moved atoms give another list of the same kind."""
@@ -47,6 +65,20 @@ def test_host_retask_reproduces_and_moves():
 def test_taskgen_matches_host(name, scale):
     from cp2k_gb300 import grid as G
     host = W.config(name, scale=scale)
+    gen = G.TaskGenerator(host)
+    nt, nb, bs = gen.run(host.atom_positions)
+    assert nt == host.ntasks
+    _same_lists(host, gen.host_arrays(), nb, bs)
+    gen.free()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["c1_64atoms", "c3_256atoms_triclinic", "c2_512atoms"])
+def test_taskgen_radius_screen_matches_host(name):
+    """Quickstep's screening by the basis radii (task_list_methods.F:
+    673-696) on the device against the host generator's."""
+    from cp2k_gb300 import grid as G
+    host = W.config(name, screen="radius")
     gen = G.TaskGenerator(host)
     nt, nb, bs = gen.run(host.atom_positions)
     assert nt == host.ntasks
