@@ -689,10 +689,11 @@ static double contribution_bound(const TaskDesc &d, const double *ra) {
 // FP32 rounding errors are correlated within a task (one set of rounded
 // coefficients and table values), unlike those of many small FP32-class
 // tasks.  Measured on the 512-atom workload (mixed step, Tr(V rho) error per
-// atom against FP64): margin 1 gives 7.0e-10 Ha, 3 gives 2.8e-10, 10 gives
-// 6.6e-11, and keeping every task whole 1.1e-10; the step takes 20.5, 20.9,
-// 21.4 and 22.3 ms.
-constexpr double kShellMargin = 3.0;
+// atom against the oracle; the errors do not fall monotonically): margin 1
+// gives 7.0e-10 Ha, 1.5 gives 7.2e-10, 2 gives 8.3e-11, 3 gives 2.8e-10,
+// against the 1e-8 target; the step takes 18.83, 18.85, 19.01 and 19.11 ms
+// (rho 5.7e-8 throughout).  Earlier, with every task whole, 1.1e-10.
+constexpr double kShellMargin = 1.5;
 
 static float core_radius2(const TaskDesc &d, int dla, int dlb, double tau, double *outside) {
   *outside = 0.0;
