@@ -351,7 +351,6 @@ struct TaskList {
   int coll_variant = -1; // orthorhombic collocate lanes: 0 row walk, 1 point list, -1 by arith
   int transform_variant = -1; // C_ab <-> C_xyz: 0 direct, 1 staged, -1 by l (uses_staged)
   std::vector<double> gbound;    // per task bound of |contribution| for |P| <= 1
-  std::vector<float2> seeds;     // per task [3][6] dfloat recurrence seeds (ortho)
   float2 *d_seeds = nullptr;
   double mixed_threshold = 0.3;  // mixed path: tasks with gbound <= this run FP32
   std::vector<int> npts_local;   // [nlevels][3]
@@ -960,6 +959,36 @@ template <typename T, typename C> static void parallel_sort(std::vector<T> &v, C
     v.swap(*src);
 }
 
+// The FP64 seeds of the double-float Gaussian recurrences of every
+// orthorhombic task (zeros for skipped and general-path tasks), per
+// direction exp(-z r^2), exp(-z h (h - 2r)), exp(-z h (h + 2r)),
+// exp(-2 z h^2), h, -r as (high, low) float pairs, from the task's
+// descriptor and its level's spacing (the recurrences of grid_kernels.cu)
+__global__ void seeds_kernel(const TaskDesc *__restrict__ tasks, int ntasks,
+                             const LevelSet *__restrict__ levels, float2 *__restrict__ seeds) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntasks; t += gridDim.x * blockDim.x) {
+    const TaskDesc &d = tasks[t];
+    float2 *o = seeds + (size_t)t * 18;
+    if (d.flags & (TF_SKIP | TF_GENERAL)) {
+      for (int q = 0; q < 18; q++)
+        o[q] = make_float2(0.f, 0.f);
+      continue;
+    }
+    const LevelDesc &L = levels->lv[d.level];
+    for (int dir = 0; dir < 3; dir++) {
+      const double h = L.dh[dir * 4], r = d.roff[dir], z = d.zetp;
+      const double v[6] = {exp(__dmul_rn(__dmul_rn(-z, r), r)),
+                           exp(__dmul_rn(__dmul_rn(-z, h), __dsub_rn(h, __dmul_rn(2.0, r)))),
+                           exp(__dmul_rn(__dmul_rn(-z, h), __dadd_rn(h, __dmul_rn(2.0, r)))),
+                           exp(__dmul_rn(__dmul_rn(__dmul_rn(-2.0, z), h), h)), h, -r};
+      for (int q = 0; q < 6; q++) {
+        const float hi = __double2float_rn(v[q]);
+        o[dir * 6 + q] = make_float2(hi, __double2float_rn(v[q] - (double)hi));
+      }
+    }
+  }
+}
+
 static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nkinds,
                         int nblocks, const int *block_offsets, const double *atom_positions,
                         const int *atom_kinds, const grid_basis_set **basis_sets,
@@ -1073,7 +1102,7 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
   t->tasks.resize(ntasks);
   t->points.assign(ntasks, 0);
   t->gbound.assign(ntasks, 0.0);
-  t->seeds.assign((size_t)ntasks * 18, make_float2(0.f, 0.f));
+
   t->features.assign((size_t)ntasks * 6, 0.f);
   // cell skew of the finest level's cell (0 for orthorhombic cells)
   double skew = 0.0;
@@ -1139,16 +1168,8 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
       const double drmin = fmin(L.dh[0], fmin(L.dh[4], L.dh[8]));
       // clamped before the cast; radii past the int16 tables fail later
       nrad_of[s] = (long long)fmin(fmax(1.0, ceil(d.radius / drmin)), 1e9);
-      // FP64 seeds of the dfloat Gaussian recurrences (grid_kernels.cu)
-      for (int dir = 0; dir < 3; dir++) {
-        const double h = L.dh[dir * 4], r = d.roff[dir], z = d.zetp;
-        const double v[6] = {exp(-z * r * r), exp(-z * h * (h - 2.0 * r)),
-                             exp(-z * h * (h + 2.0 * r)), exp(-2.0 * z * h * h), h, -r};
-        for (int q = 0; q < 6; q++) {
-          const float hi = (float)v[q];
-          t->seeds[(size_t)s * 18 + dir * 6 + q] = make_float2(hi, (float)(v[q] - (double)hi));
-        }
-      }
+      // the FP64 seeds of its double-float Gaussian recurrences are
+      // computed on the device after the upload (seeds_kernel)
     } else {
       // general_cijk_to_grid (grid_ref_collint.h:609-640)
       d.flags |= TF_GENERAL;
@@ -1345,7 +1366,7 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
   for (auto &e : t->ev)
     CK(cudaEventCreate(&e));
   t->d_tasks = dalloc_copy(t->tasks);
-  t->d_seeds = dalloc_copy(t->seeds);
+  CK(cudaMalloc((void **)&t->d_seeds, sizeof(float2) * 18 * (size_t)ntasks));
   t->d_subs = dalloc_copy(t->subs);
   t->d_sph = dalloc_copy(t->sph);
   t->d_sph_tab = dalloc_copy(t->sph_tab);
@@ -1368,6 +1389,11 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
   t->d_sphi = dalloc_copy(sphi_all);
   CK(cudaMalloc((void **)&t->d_levels, sizeof(LevelSet)));
   CK(cudaMemcpy(t->d_levels, &t->levels, sizeof(LevelSet), cudaMemcpyHostToDevice));
+  seeds_kernel<<<(unsigned)std::min<long long>((ntasks + 255) / 256, 152LL * 16), 256, 0,
+                 t->stream>>>(t->d_tasks, ntasks, t->d_levels, t->d_seeds);
+  count_launch();
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(t->stream));
   CK(cudaMalloc((void **)&t->d_pab_cart, sizeof(double) * std::max<size_t>(t->cart_total, 1)));
   CK(cudaMalloc((void **)&t->d_hab_cart, sizeof(double) * std::max<size_t>(t->cart_total, 1)));
   CK(cudaMalloc((void **)&t->d_forces, sizeof(double) * 3 * std::max(natoms, 1)));
@@ -1582,18 +1608,41 @@ static Mode &get_mode(TaskList *t, const LDiffs &d, int phase, int nch = 1) {
     task_iw[s] = g ? k.imax[0] - k.center[0] + 1 : 0;
     task_nk[s] = g ? k.imax[2] - k.center[2] + 1 : 2 - 2 * t->sph[k.sphere].lb[2];
   });
-  for (int s = 0; s < t->ntasks; s++) {
-    const int key = task_key[s];
-    if (key < 0)
-      continue;
-    const double cost = task_cost[s];
-    if (m.core_r2[s] < kCoreAll) {
-      const double out = outside[s];
-      items[key].push_back({cost * (1.0 - out), s});
-      items[kQueueKeys + key + 2].push_back({cost * out, s}); // FP32 class bit set
-      m.row_split = true;
-    } else {
-      items[key].push_back({cost, s});
+  {
+    // filled per thread over contiguous task ranges, then joined: the
+    // queue sort below orders its items totally, so the join order is free
+    const int nt = std::max(1, std::min(host_threads(), t->ntasks / 4096 + 1));
+    std::vector<std::map<int, std::vector<std::pair<double, int>>>> part(nt);
+    std::vector<char> split_any(nt, 0);
+    std::vector<std::thread> th;
+    for (int c = 0; c < nt; c++)
+      th.emplace_back([&, c] {
+        const int s0 = (int)((long long)t->ntasks * c / nt);
+        const int s1 = (int)((long long)t->ntasks * (c + 1) / nt);
+        auto &its = part[c];
+        for (int s = s0; s < s1; s++) {
+          const int key = task_key[s];
+          if (key < 0)
+            continue;
+          const double cost = task_cost[s];
+          if (m.core_r2[s] < kCoreAll) {
+            const double out = outside[s];
+            its[key].push_back({cost * (1.0 - out), s});
+            its[kQueueKeys + key + 2].push_back({cost * out, s}); // FP32 class bit set
+            split_any[c] = 1;
+          } else {
+            its[key].push_back({cost, s});
+          }
+        }
+      });
+    for (auto &x : th)
+      x.join();
+    for (int c = 0; c < nt; c++) {
+      for (auto &kv : part[c]) {
+        auto &dst = items[kv.first];
+        dst.insert(dst.end(), kv.second.begin(), kv.second.end());
+      }
+      m.row_split = m.row_split || split_any[c];
     }
   }
   hp.mark("classes and costs");
@@ -2361,7 +2410,7 @@ GB300_API void grid_gb300_host_digest(
                        border_mask_list, block_num_list, radius_list, rab_list, npts_global,
                        npts_local, shift_local, border_width, dh, dh_inv, true);
   digest[0] = fnv_bytes(t->tasks);
-  digest[1] = fnv_bytes(t->seeds);
+  digest[1] = 0; // the seeds are computed on the device
   digest[2] = fnv_bytes(t->gbound);
   digest[3] = fnv_bytes(t->features);
   digest[4] = fnv_bytes(t->points);

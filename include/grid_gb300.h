@@ -684,9 +684,10 @@ const char *grid_gb300_last_error(void);
 
 /* ---- testing ---------------------------------------------------------------
  * Runs the host-side preparation of grid_gb300_create_task_list (ordering,
- * per-task geometry, seeds, class bounds, features, sphere tables,
- * subblocks) without touching the GPU, and returns FNV-1a hashes of the
- * prepared arrays: digest[0..9] tasks, seeds, class bounds, features, point
+ * per-task geometry, class bounds, features, sphere tables, subblocks)
+ * without touching the GPU, and returns FNV-1a hashes of the prepared
+ * arrays: digest[0..9] tasks, 0 (the recurrence seeds are computed on the
+ * device), class bounds, features, point
  * counts, subblocks, sphere headers, sphere tables, sphere points, point
  * offsets; digest[10] the Cartesian scratch size; digest[11] the number of
  * tasks whose class bound is <= 0.3.  The preparation runs on the host's
