@@ -1265,6 +1265,7 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
     std::vector<std::vector<int16_t>> tabs(U);
     std::vector<std::vector<int>> pts(U), plo(U);
     sphere_points.assign(U, 0);
+    hp.mark("spheres listed");
     parallel_items(U, [&](int u) {
       const LevelDesc &L = t->levels.lv[uniq[u].first];
       const double drmin = fmin(L.dh[0], fmin(L.dh[4], L.dh[8]));
@@ -1285,6 +1286,7 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
       t->sph.push_back(h);
     }
   }
+  hp.mark("spheres built");
   // per task, in parallel: its sphere, point count and whether it starts a
   // subblock (a new (block, iset, jset) in the sorted order)
   std::vector<char> new_sub(ntasks, 0);
@@ -1309,12 +1311,18 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
     new_sub[s] = s == 0 || block_num_list[p] != block_num_list[i] || iset_list[p] != iset_list[i] ||
                  jset_list[p] != jset_list[i];
   });
-  // the subblocks in order (their Cartesian scratch offsets add up)
-  long long maxbuf = 0;
+  hp.mark("tasks placed");
+  // the subblocks: their descriptors in parallel, then the Cartesian scratch
+  // offsets (a running sum) and the buffer and scratch maxima in order
   std::vector<int> sub_first;
-  for (int s = 0; s < ntasks; s++) {
-    if (!new_sub[s])
-      continue;
+  for (int s = 0; s < ntasks; s++)
+    if (new_sub[s])
+      sub_first.push_back(s);
+  const int nsub = (int)sub_first.size();
+  t->subs.assign(nsub, SubblockDesc{});
+  std::vector<long long> block_end(nsub);
+  parallel_for(nsub, [&](int u) {
+    const int s = sub_first[u];
     const int i = order[s];
     const TaskDesc &d = t->tasks[s];
     const int ia = d.iatom, ja = d.jatom;
@@ -1322,7 +1330,7 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
     const grid_basis_set *bi = basis_sets[atom_kinds[ia] - 1];
     const grid_basis_set *bj = basis_sets[atom_kinds[ja] - 1];
     const int bn = block_num_list[i] - 1;
-    SubblockDesc sb;
+    SubblockDesc &sb = t->subs[u];
     memset(&sb, 0, sizeof(sb));
     sb.block_offset = block_offsets[bn];
     sb.ncoa = bi->npgf[iset] * ncoset(bi->lmax[iset]);
@@ -1342,14 +1350,17 @@ static TaskList *create(bool ortho, int ntasks, int nlevels, int natoms, int nki
     sb.iatom = ia;
     sb.jatom = ja;
     sb.first_task = s;
+    block_end[u] = (long long)block_offsets[bn] + (long long)bi->nsgf * bj->nsgf;
+  });
+  long long maxbuf = 0;
+  for (int u = 0; u < nsub; u++) {
+    SubblockDesc &sb = t->subs[u];
     sb.cart_offset = (int)t->cart_total;
     t->cart_total += (size_t)sb.ncoa * sb.ncob;
     if (t->cart_total > (size_t)INT32_MAX)
       fail("Cartesian scratch exceeds int offsets");
     t->contract_words = std::max(t->contract_words, sb.nsgf_setb * sb.ncoa);
-    t->subs.push_back(sb);
-    sub_first.push_back(s);
-    maxbuf = std::max(maxbuf, (long long)block_offsets[bn] + (long long)bi->nsgf * bj->nsgf);
+    maxbuf = std::max(maxbuf, block_end[u]);
   }
   sub_first.push_back(ntasks);
   parallel_for((int)t->subs.size(), [&](int u) {
