@@ -251,10 +251,10 @@ def measure_peak(torch, dtype, n):
 # launch split; the bench cannot run ncu itself, and divides by its own
 # launches per step.  Keys: kernel label as in "roofline.kernel".
 NCU_TRAFFIC_PER_STEP = {
-    "integrate_ortho_tc<4>": (2.641 + 0.024 + 25.110 + 0.087 + 176.468 + 47.204
-                              + 114.270 + 19.439) * 1e6,
-    "collocate_ortho<float,4>": (3.380 + 0.050 + 32.582 + 7.295 + 261.180 + 1072.604
-                                 + 143.043 + 393.604) * 1e6,
+    "integrate_ortho_tc<4>": (2.628 + 0.021 + 26.141 + 0.091 + 167.054 + 42.108
+                              + 112.559 + 15.697) * 1e6,
+    "collocate_ortho<float,4>": (3.369 + 0.040 + 33.993 + 8.245 + 263.428 + 1072.301
+                                 + 145.123 + 406.260) * 1e6,
     "integrate_ortho<double,4>": ((35.777 + 0.760) + (594.138 + 123.159)) * 1e6,
 }
 
