@@ -426,11 +426,15 @@ def test_transform_variants_agree(G, O, prec, case):
     tl.close()
 
 
-@pytest.mark.parametrize("api", ["cp2k", "backend"])
-def test_copy_chunks_agree(G, O, api):
+@pytest.mark.parametrize("api,precision", [("cp2k", "fp64"), ("backend", "fp64"),
+                                           ("cp2k", "mixed")])
+def test_copy_chunks_agree(G, O, api, precision):
     """Host-buffer calls copy pab in and hab out in pieces that overlap the
-    kernels (grid_gb300_set_copy_chunks); 1, 2 and 3 pieces give the oracle's
-    results, and hab entries past the task list's blocks come back zeroed."""
+    kernels (grid_gb300_set_copy_chunks), each piece with work queues of its
+    own tasks; 1, 2 and 3 pieces give the oracle's results (FP64: to 1e-12;
+    mixed, with its row split: rho and hab to 1e-6, forces and virial to 1e-5,
+    relative to max(1, |ref|)), and hab entries past the task list's blocks
+    come back zeroed."""
     from cp2k_gb300 import workload as W
     inp = W.config("c2_512atoms", scale=0.1, seed=37)
     pab = W.density_blocks(inp)
@@ -439,17 +443,19 @@ def test_copy_chunks_agree(G, O, api):
     g_ref = ot.collocate(100, pab)
     h_ref, f_ref, v_ref = ot.integrate(V, pab, forces=True, virial=True)
     ot.close()
-    tl = G.GridTaskList(inp, precision=G.FP64, api=api)
+    prec = G.FP64 if precision == "fp64" else G.MIXED
+    tol_g, tol_d = (TOL_GRID, TOL_DERIV) if precision == "fp64" else (1e-6, 1e-5)
+    tl = G.GridTaskList(inp, precision=prec, api=api)
     for chunks in (1, 2, 3):
         tl.set_copy_chunks(chunks)
         g = tl.collocate(100, pab)
-        assert max(rel_diff(a, b) for a, b in zip(g, g_ref)) < TOL_GRID, chunks
+        assert max(rel_diff(a, b) for a, b in zip(g, g_ref)) < tol_g, chunks
         _, hab_buf, _ = tl.host_buffers()
         hab_buf.host[:] = 7.0  # stale values must not survive
         h, f, v = tl.integrate(V, pab, forces=True, virial=True)
-        assert rel_diff(h, h_ref) < TOL_GRID, chunks
-        assert rel_diff(f, f_ref) < TOL_DERIV
-        assert rel_diff(v, v_ref) < TOL_DERIV
+        assert rel_diff(h, h_ref) < tol_g, chunks
+        assert rel_diff(f, f_ref) < tol_d
+        assert rel_diff(v, v_ref) < tol_d
     tl.close()
 
 
